@@ -1,0 +1,180 @@
+/* GB300 hot path of libbfm: additive C ABI.
+ *
+ * Nothing here replaces or changes a reference prototype.  The reference's
+ * hot entry bfm_sim_run (libbfm/src/sim.c:137-155, sim.h:33) keeps its
+ * signature and runs on top of these functions; this header adds what the old
+ * API cannot express (solver options, statistics, per-element material) and a
+ * device-resident problem handle for callers that keep meshes in GPU memory.
+ *
+ * Conventions: 0 = success, -1 = failure (as the reference, bfm.h:27-34); on
+ * failure bfm_gpu_last_error() returns a message.  Plain pointers and sizes
+ * only.  `where` arguments say whether a pointer is host (BFM_GPU_HOST) or
+ * device (BFM_GPU_DEVICE) memory.  `stream` is a cudaStream_t passed as void*
+ * (NULL: the problem creates and owns a stream).
+ *
+ * Data layout on the device: node coordinates as interleaved doubles,
+ * connectivity as int32, stiffness as 2x2-block CSR (one block per pair of
+ * nodes sharing an element, columns ascending, block entries row-major
+ * k_uu k_uv k_vu k_vv), right-hand side and solution as interleaved u,v.
+ */
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <bfm/instance.h>
+#include <bfm/sim.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { BFM_GPU_HOST = 0, BFM_GPU_DEVICE = 1 };
+
+/* arithmetic of the stiffness matrix and Krylov vectors */
+enum {
+	BFM_GPU_FP64 = 0,  /* FP64 element integration (reference operation order), FP64 CG          */
+	BFM_GPU_MIXED = 1, /* FP32 element integration and SpMV; FP64 inner products, FP64 solution,
+	                      FP64 residual replacement and outer refinement                          */
+};
+
+/* preconditioner */
+enum {
+	BFM_GPU_PC_JACOBI = 0,       /* diagonal                                   */
+	BFM_GPU_PC_BLOCK_JACOBI = 1, /* inverse of each node's 2x2 diagonal block  */
+	BFM_GPU_PC_LEARNED = 2,      /* message-passing network, flexible CG       */
+};
+
+/* solver status codes (bfm_gpu_stats_t.status) */
+enum {
+	BFM_GPU_OK = 0,
+	BFM_GPU_NOT_CONVERGED = 1, /* max_iters reached                         */
+	BFM_GPU_BREAKDOWN = 2,     /* p.Ap <= 0 or NaN: matrix not SPD / singular */
+	BFM_GPU_BAD_MESH = 3,      /* valence or row length above the kernel caps */
+	BFM_GPU_CUDA_ERROR = 4,
+};
+
+typedef struct {
+	int precision;     /* BFM_GPU_FP64 or BFM_GPU_MIXED                         */
+	int precond;       /* BFM_GPU_PC_*                                          */
+	double rtol;       /* stop when ||b - A x||_2 <= rtol ||b||_2               */
+	int max_iters;     /* hard cap on CG iterations                             */
+	double replace_drop; /* mixed: replace the recurrence residual by the FP64
+	                        true residual each time it has dropped by this factor */
+	int deterministic; /* 1: fixed reduction order (always on; kept for ABI)    */
+} bfm_gpu_opts_t;
+
+typedef struct {
+	int status;           /* BFM_GPU_* status code                        */
+	int iterations;       /* CG iterations performed                      */
+	int replacements;     /* mixed: FP64 residual replacements             */
+	int fallback;         /* learned: 1 if Jacobi took over                */
+	double rel_residual;  /* FP64 ||b - A x|| / ||b|| of the returned x    */
+	int64_t n_blocks;     /* 2x2 blocks in the stiffness matrix            */
+	int64_t n_dof;
+	double ms_assemble;   /* pattern + element loop + conditions (device)  */
+	double ms_solve;      /* CG (device)                                   */
+} bfm_gpu_stats_t;
+
+/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 1e-2. */
+void bfm_gpu_default_opts(bfm_gpu_opts_t* opts);
+
+/* Options used by bfm_sim_run and the bfm_system_* creators of this thread. */
+int bfm_gpu_set_opts(const bfm_gpu_opts_t* opts);
+int bfm_gpu_get_opts(bfm_gpu_opts_t* opts);
+
+/* Statistics of the last instance solved by bfm_sim_run on this thread. */
+int bfm_gpu_last_stats(bfm_gpu_stats_t* stats);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* bfm_gpu_last_error(void);
+
+/* Number of usable CUDA devices (0 without a GPU; never fails). */
+int bfm_gpu_device_count(void);
+
+/* Per-element Young's modulus and Poisson ratio for one instance (an
+ * extension: the reference holds one material per object, obj.h:8-14).
+ * Arrays of n_elems doubles, host memory, owned by the caller and read at
+ * bfm_sim_run time; NULL for either keeps the material's value.  Passing both
+ * NULL removes the override. */
+int bfm_gpu_instance_set_elem_material(bfm_instance_t* instance, const double* E, const double* nu);
+
+/* ---------------------------------------------------------------- device-resident problems */
+
+typedef struct bfm_gpu_problem bfm_gpu_problem_t;
+
+/* Allocate device storage for a mesh of n_nodes nodes and n_elems elements of
+ * `kind` nodes (3 or 4), with up to n_edges boundary edges and n_conds
+ * conditions.  Sizes every buffer for the worst case, so nothing is
+ * allocated after this call. */
+int bfm_gpu_problem_create(bfm_gpu_problem_t** problem, int kind, int n_nodes, int n_elems,
+                           int n_edges, int n_conds, void* stream);
+int bfm_gpu_problem_destroy(bfm_gpu_problem_t* problem);
+
+/* coords[2*n_nodes] (x,y interleaved), elems[kind*n_elems] (int32). */
+int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* problem, const double* coords, const int32_t* elems, int where);
+
+/* Uniform material (E, nu, rho) and plane stress (1) or plane strain (0);
+ * elem_E / elem_nu (n_elems each, may be NULL) override E / nu per element. */
+int bfm_gpu_problem_set_material(bfm_gpu_problem_t* problem, double E, double nu, double rho, int stress,
+                                 const double* elem_E, const double* elem_nu, int where);
+
+/* Integration rule sampled on the host: weights[n_points], and phi, dxi, deta
+ * [n_points*kind] (shape value and derivatives at each point). */
+int bfm_gpu_problem_set_rule(bfm_gpu_problem_t* problem, int n_points, const double* weights,
+                             const double* phi, const double* dxi, const double* deta);
+
+/* Body forces (accelerations, multiplied by rho as in the reference).
+ * force k is constant (values[2k..2k+1]) when node_values[k] is NULL, else a
+ * per-node field node_values[k][2*n_nodes] in `where` memory. */
+int bfm_gpu_problem_set_forces(bfm_gpu_problem_t* problem, int n_forces, const double* values,
+                               const double* const* node_values, int where);
+
+/* Conditions in application order: kinds[c] (BFM_CONDITION_KIND_DIRICHLET_X/Y,
+ * NEUMANN_X/Y), values[c], masks[c*n_nodes + i] != 0 when node i is flagged;
+ * edges[2*n_edges] node pairs used by the Neumann conditions. */
+int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* problem, int n_conds, const int* kinds, const double* values,
+                                   const uint8_t* masks, int n_edges, const int32_t* edges, int where);
+
+/* Enqueue: sparsity pattern, element loop, Dirichlet elimination, Neumann
+ * loads and preconditioner set-up, in `precision`.  Asynchronous. */
+int bfm_gpu_problem_assemble(bfm_gpu_problem_t* problem, int precision);
+
+/* Enqueue the CG solve (one CUDA graph launch).  Asynchronous; statistics via
+ * bfm_gpu_problem_stats. */
+int bfm_gpu_problem_solve(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t* opts);
+
+/* Wait for the problem's stream and report the last assemble/solve. */
+int bfm_gpu_problem_stats(bfm_gpu_problem_t* problem, bfm_gpu_stats_t* stats);
+
+/* Copy the solution (2*n_nodes doubles, interleaved u,v) out. */
+int bfm_gpu_problem_solution(bfm_gpu_problem_t* problem, double* out, int where);
+
+/* Inspection: number of 2x2 blocks of the last assembled matrix. */
+int bfm_gpu_problem_n_blocks(bfm_gpu_problem_t* problem, int64_t* n_blocks);
+
+/* Inspection: copy the assembled system to the host.  row_ptr[n_nodes+1] and
+ * cols[n_blocks] of the node-block pattern, vals[4*n_blocks] (FP64; FP32
+ * entries widened in mixed precision) and b[2*n_nodes].  Any may be NULL. */
+int bfm_gpu_problem_download(bfm_gpu_problem_t* problem, int32_t* row_ptr, int32_t* cols, double* vals, double* b);
+
+/* Measurement hook: launch the CG's SpMV+dots kernel and its vector-update
+ * kernel `reps` times each on the problem's stream and return their mean
+ * durations (ms, CUDA events).  Overwrites the Krylov vectors. */
+int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* problem, int reps, double* ms_spmv, double* ms_update);
+
+/* The CUDA stream the problem's work is enqueued on (cudaStream_t as void*). */
+void* bfm_gpu_problem_stream(bfm_gpu_problem_t* problem);
+
+/* ---------------------------------------------------------------- sparse RCM */
+
+/* Reverse Cuthill-McKee of a scalar CSR matrix (columns ascending per row),
+ * ignoring entries that are exactly zero: the permutation the reference's
+ * bfm_perm_rcm (perm.c:117-331) computes on the equivalent dense matrix,
+ * bit for bit, in O(nnz log) instead of O(n^2).  perm[old] = new. */
+int bfm_gpu_rcm_csr(int64_t n, const int64_t* row_ptr, const int64_t* cols, const double* vals,
+                    int64_t* perm, int64_t* inv_perm);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,179 @@
+"""Generate tests/golden/*.npz from the reference libbfm itself.
+
+Run in a tree where the reference sources exist (it compiles them into
+oracle/_ref/ with oracle/Makefile):
+
+    python tests/golden/make_golden.py [--reference /path/to/bfm]
+
+Every fixture holds the problem's input arrays and what the reference library
+returned for it through its own public API (bfm_sim_run for displacements;
+bfm_system_create_planar_* + bfm_system_renumber for the assembled matrix, the
+right-hand side and the RCM permutation).  The 8.lepl1110 case also holds the
+values of the reference's shipped golden files data/U.txt and data/V.txt.
+The GPU machine never needs the reference tree: tests read only these files.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+OUT = Path(__file__).resolve().parent
+
+
+def parse_lepl1110(path: Path):
+    """Nodes, edges, elements and domains of a LEPL1110 mesh file."""
+    lines = path.read_text().splitlines()
+    i = 0
+    coords, edges, elems, domains = [], [], [], {}
+    kind = None
+    while i < len(lines):
+        t = lines[i].strip()
+        if t.startswith("Number of nodes"):
+            n = int(t.split()[-1])
+            coords = [tuple(map(float, lines[i + 1 + k].split(":")[1].split())) for k in range(n)]
+            i += n
+        elif t.startswith("Number of edges"):
+            n = int(t.split()[-1])
+            edges = [tuple(map(int, lines[i + 1 + k].split(":")[1].split())) for k in range(n)]
+            i += n
+        elif t.startswith("Number of triangles") or t.startswith("Number of quads"):
+            kind = 3 if "triangles" in t else 4
+            n = int(t.split()[-1])
+            elems = [tuple(map(int, lines[i + 1 + k].split(":")[1].split())) for k in range(n)]
+            i += n
+        elif t.startswith("Domain"):
+            name = lines[i + 1].split(":", 1)[1].strip()
+            cnt = int(lines[i + 2].split(":")[1])
+            vals = []
+            j = i + 3
+            while len(vals) < cnt:
+                vals += [int(v) for v in lines[j].split()]
+                j += 1
+            domains[name] = vals
+            i = j - 1
+        i += 1
+    return (np.array(coords, np.float64), np.array(edges, np.int64), np.array(elems, np.int64), kind, domains)
+
+
+def read_golden_values(path: Path) -> np.ndarray:
+    txt = path.read_text().splitlines()[1:]
+    vals = []
+    for line in txt:
+        for k in range(0, len(line), 14):
+            chunk = line[k:k + 14].strip()
+            if chunk:
+                vals.append(float(chunk))
+    return np.array(vals)
+
+
+def save(name: str, p, h, extra: dict | None = None, system: bool = True):
+    from bfm_gb300 import meshgen as M
+    eff = h.effects()
+    d = dict(kind=p.kind, stress=int(p.stress), coords=p.coords, elems=p.elems, E=p.E, nu=p.nu, rho=p.rho,
+             forces=np.array(p.forces, np.float64).reshape(-1, 2),
+             cond_kind=np.array([c[0] for c in p.conds], np.int32),
+             cond_value=np.array([c[1] for c in p.conds], np.float64),
+             cond_nodes=np.packbits(np.stack([np.asarray(c[2], bool) for c in p.conds]), axis=1),
+             edges=p.edges if p.edges is not None else np.zeros((0, 2), np.int64),
+             effects=eff)
+    if system:
+        K, b, perm = h.system(renumber=True)
+        nz = np.nonzero(K)
+        d.update(K_rows=nz[0].astype(np.int32), K_cols=nz[1].astype(np.int32), K_vals=K[nz], b=b, perm=perm)
+    d.update(extra or {})
+    np.savez_compressed(OUT / f"{name}.npz", **d)
+    print(f"{name}: N={p.n_nodes} E={p.n_elems} |u|max={np.abs(eff).max():.3e}", file=sys.stderr)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("BFM_REFERENCE", "/root/reference"))
+    args = ap.parse_args()
+    os.environ["BFM_REFERENCE"] = args.reference
+    from oracle import oracle as O
+    O.REF_TREE = Path(args.reference)
+    from bfm_gb300 import api, meshgen as M
+    R = O.ref_lib()
+    assert R is not None, "reference sources not found"
+    ref = Path(args.reference)
+
+    # 1. the reference's own fixture: Q1 mesh, planar strain, gravity, two Dirichlet domains
+    coords, edges, elems, kind, domains = parse_lepl1110(ref / "meshes" / "8.lepl1110")
+    N = len(coords)
+
+    def dom_mask(name):
+        m = np.zeros(N, bool)
+        for e in domains[name]:
+            m[edges[e]] = True
+        return m
+
+    p = M.Problem("lepl8", kind, coords, elems, E=2.11e11, nu=0.3, rho=7850.0, stress=False,
+                  forces=[(0.0, -9.81)], conds=[(M.DIRICHLET_X, 0.0, dom_mask("Symmetry")),
+                                                (M.DIRICHLET_Y, 0.0, dom_mask("Bottom"))], edges=edges)
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    U = read_golden_values(ref / "data" / "U.txt")
+    V = read_golden_values(ref / "data" / "V.txt")
+    names = np.array(list(domains.keys()))
+    dom_edges = [np.array(domains[k], np.int64) for k in domains]
+    save("lepl8", p, h, dict(U_txt=U, V_txt=V, domain_names=names,
+                             domain_ptr=np.cumsum([0] + [len(v) for v in dom_edges]),
+                             domain_edges=np.concatenate(dom_edges)))
+
+    # 2. 64x16 P1 plate, plane stress, gravity, left edge clamped
+    p = M.cfg_small()
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    save("p1_64x16", p, h)
+
+    # 3. jittered Q1 plate with a right-edge traction
+    p = M.plate(24, 8, 4, name="q1_24x8_jitter", jitter_frac=0.2, seed=7, traction=1e6)
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    save("q1_24x8_jitter", p, h)
+
+    # 4. condition-order semantics: non-zero and repeated Dirichlet values,
+    #    Neumann before and after Dirichlet on shared nodes, plane strain
+    coords, el = M.grid(12, 6, 3)
+    left, right = M.side_mask(coords, "left"), M.side_mask(coords, "right")
+    bottom, top = M.side_mask(coords, "bottom"), M.side_mask(coords, "top")
+    conds = [(M.NEUMANN_X, 2e5, right), (M.DIRICHLET_X, 1e-4, left), (M.DIRICHLET_Y, 0.0, left),
+             (M.DIRICHLET_X, -2e-4, left & (coords[:, 1] > 0.5)), (M.NEUMANN_Y, -3e5, top),
+             (M.DIRICHLET_Y, 5e-5, bottom & (coords[:, 0] > 3.0)), (M.NEUMANN_Y, 1e5, bottom)]
+    p = M.Problem("p1_12x6_conds", 3, coords, el, stress=False, forces=[(0.0, -9.81), (1.5, 0.0)], conds=conds,
+                  edges=M.boundary_edges(12, 6))
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    save("p1_12x6_conds", p, h)
+
+    # 5. jittered P1 plate with shuffled node numbering (an unbanded matrix for RCM)
+    rng = np.random.default_rng(11)
+    base = M.plate(20, 10, 3, jitter_frac=0.25, seed=5)
+    order = rng.permutation(base.n_nodes)      # new id of old node
+    inv = np.argsort(order)
+    p = M.Problem("p1_20x10_shuffled", 3, base.coords[inv], order[base.elems], forces=base.forces,
+                  conds=[(k, v, m[inv]) for k, v, m in base.conds])
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    save("p1_20x10_shuffled", p, h)
+
+    # 6. an unstructured P1 mesh from the reference's meshes (no edge section:
+    #    the reference reader cannot load it, so it goes in through the C API)
+    coords, _, elems, kind, _ = parse_lepl1110(ref / "meshes" / "gear12.lepl1110")
+    hub = np.hypot(coords[:, 0], coords[:, 1]) < 10.0
+    p = M.Problem("gear12", 3, coords, elems, stress=True, forces=[(0.0, -9.81)],
+                  conds=[(M.DIRICHLET_X, 0.0, hub), (M.DIRICHLET_Y, 0.0, hub)])
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    save("gear12", p, h)
+
+
+if __name__ == "__main__":
+    main()
