@@ -197,7 +197,9 @@ __global__ void k_rows_count(int N, int kind, const int* __restrict__ elems, con
 	if (r >= N) return;
 	int const s = inc_ptr[r], deg = inc_ptr[r + 1] - s;
 	if (deg > MAXV) {
+		// flagged; keep the row well formed (diagonal only) so later kernels stay in bounds
 		atomicOr(err, ERR_VALENCE);
+		cand[(long) kind * s] = r;
 		row_len[r] = 1;
 		return;
 	}
@@ -649,7 +651,8 @@ struct CgArgs {
 	unsigned* ticket;
 	CgState* st;
 	cudaGraphConditionalHandle cond;
-	int use_cond;
+	int use_cond;  // launched inside the solve graph: drive its while-node
+	int timing;    // measurement launches: ignore the stop flag, never set it
 };
 
 template <typename V>
@@ -686,16 +689,18 @@ __global__ void __launch_bounds__(TPB) k_cg_init(CgArgs<V> a) {
 		st->gamma_old = 0; st->alpha_old = 0;
 		st->alpha = 0; st->beta = 0;
 		st->rho = out[0];
+		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
 }
 
 template <typename V>
 __global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
 	CgState* st = a.st;
-	if (st->done) {
-		if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
-		return;
-	}
+	// The while-node continues only if this launch's finisher says so: block 0
+	// clears the condition first, the last block sets it after the stopping
+	// test.  A launch whose finisher did not run therefore ends the loop.
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
+	if (st->done && !a.timing) return;
 	double v[3] = {0.0, 0.0, 0.0};  // gamma, delta, rho
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		int const ks = a.row_ptr[i], ke = a.row_ptr[i + 1];
@@ -737,7 +742,7 @@ __global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
 			}
 			if (!(den > 0.0) || !(gamma > 0.0)) {
 				stop = 1;
-				st->status = BFM_GPU_BREAKDOWN;
+				if (!a.timing) st->status = BFM_GPU_BREAKDOWN;
 			}
 			else {
 				double const alpha = gamma / den;
@@ -748,15 +753,16 @@ __global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
 				st->iter += 1;
 			}
 		}
+		if (a.timing) return;
 		st->done = stop;
-		if (a.use_cond) cudaGraphSetConditional(a.cond, stop ? 0u : 1u);
+		if (a.use_cond && !stop) cudaGraphSetConditional(a.cond, 1u);
 	}
 }
 
 template <typename V>
 __global__ void __launch_bounds__(TPB) k_cg_update(CgArgs<V> a) {
 	CgState const* st = a.st;
-	if (st->done) return;
+	if (st->done && !a.timing) return;
 	V const alpha = (V) st->alpha, beta = (V) st->beta;
 	double const alpha64 = st->alpha;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
@@ -959,6 +965,7 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, cudaGraphConditionalHandle h, int use_cond
 	a.st = P->st;
 	a.cond = h;
 	a.use_cond = use_cond;
+	a.timing = 0;
 	return a;
 }
 
@@ -1422,6 +1429,7 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 	if (P->precision == BFM_GPU_FP64) {
 		CgArgs<double> a = cg_args<double>(P, 0, 0);
 		a.st = scratch;
+		a.timing = 1;
 		k_cg_init<double><<<P->grid, TPB, 0, P->stream>>>(a);
 		cudaMemcpyAsync(scratch, &h, sizeof h, cudaMemcpyHostToDevice, P->stream);
 		cudaEventRecord(e[0], P->stream);
@@ -1433,6 +1441,7 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 	else {
 		CgArgs<float> a = cg_args<float>(P, 0, 0);
 		a.st = scratch;
+		a.timing = 1;
 		k_cg_init<float><<<P->grid, TPB, 0, P->stream>>>(a);
 		cudaMemcpyAsync(scratch, &h, sizeof h, cudaMemcpyHostToDevice, P->stream);
 		cudaEventRecord(e[0], P->stream);
