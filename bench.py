@@ -157,8 +157,10 @@ def run_gpu(args, rank: int, world: int):
     lib = bfm_gb300.lib()
     p = workload(args.workload)
     stream = torch.cuda.current_stream()
-    methods = {"fp64": (bfm_gb300.FP64, bfm_gb300.PC_JACOBI), "mixed": (bfm_gb300.MIXED, bfm_gb300.PC_JACOBI)}
-    chosen = ["fp64"] if args.method in ("fp64", "best") else [args.method]
+    methods = {"fp64": (bfm_gb300.FP64, bfm_gb300.PC_JACOBI),
+               "mixed": (bfm_gb300.MIXED, bfm_gb300.PC_JACOBI),
+               "mixed_exact": (bfm_gb300.MIXED_EXACT, bfm_gb300.PC_JACOBI)}
+    chosen = ["fp64", "mixed_exact", "mixed"] if args.method == "best" else [args.method]
     results = {}
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
     for m in chosen:
@@ -195,13 +197,18 @@ def run_gpu(args, rank: int, world: int):
         # per-kernel durations for the roofline (same stream, CUDA events)
         t_spmv, t_upd = C.c_double(), C.c_double()
         assert lib.bfm_gpu_problem_time_kernels(P, 50, C.byref(t_spmv), C.byref(t_upd)) == 0
-        results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual,
+        results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual, repl=s.replacements,
                           ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks,
                           ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, x=x)
     lib.bfm_gpu_problem_destroy(P)
+    # displacement error of every method against the FP64 solution
+    ref = results.get("fp64", {}).get("x")
+    for m, r in results.items():
+        r["err_vs_fp64"] = None if ref is None else float(np.linalg.norm(r["x"] - ref) / np.linalg.norm(ref))
+    ok = [m for m, r in results.items() if r["status"] == 0 and (r["err_vs_fp64"] is None or r["err_vs_fp64"] <= 1e-6)]
+    best = min(ok or results, key=lambda k: results[k]["ms"])
 
     # end-to-end through bfm_sim_run with host buffers
-    best = min(results, key=lambda k: results[k]["ms"])
     prec, pc = methods[best]
     lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc)))
     h = api.SimHandle.from_problem(lib, p)
@@ -216,6 +223,27 @@ def run_gpu(args, rank: int, world: int):
         (0 if p.elem_E is None else 8 * p.n_elems)
     d2h = p.n_dof * 8
     return p, results, best, dict(ms=e2e_ms, h2d=h2d, d2h=d2h)
+
+
+def profile(args):
+    """Assemble once, then the CG's SpMV+dots and update kernels as standalone
+    launches (the solve itself runs them inside a CUDA graph)."""
+    import bfm_gb300
+    lib = bfm_gb300.lib()
+    p = workload(args.workload)
+    prec = {"fp64": bfm_gb300.FP64, "mixed": bfm_gb300.MIXED, "mixed_exact": bfm_gb300.MIXED_EXACT,
+            "best": bfm_gb300.FP64}[args.method]
+    P, keep = device_problem(lib, p, None)
+    assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
+    s = bfm_gb300.bfm_gpu_stats_t()
+    assert lib.bfm_gpu_problem_stats(P, C.byref(s)) == 0
+    t_spmv, t_upd = C.c_double(), C.c_double()
+    assert lib.bfm_gpu_problem_time_kernels(P, args.reps, C.byref(t_spmv), C.byref(t_upd)) == 0
+    lib.bfm_gpu_problem_destroy(P)
+    nbytes = algorithmic_bytes_spmv(s.n_blocks, p.n_nodes, prec)
+    return {"workload": p.name, "method": args.method, "n_blocks": s.n_blocks, "ms_assemble": s.ms_assemble,
+            "spmv_ms": t_spmv.value, "update_ms": t_upd.value, "spmv_algorithmic_bytes": nbytes,
+            "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9}
 
 
 def run_reference(args, rank: int, world: int):
@@ -234,11 +262,18 @@ def main():
     ap.add_argument("--workload", default="perforated")
     ap.add_argument("--method", default="best", choices=["fp64", "mixed", "best"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="assemble once and launch the two CG kernels --reps times each, standalone "
+                         "(for ncu: one JSON line with their CUDA-event durations)")
+    ap.add_argument("--reps", type=int, default=5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.profile:
+        print(json.dumps(profile(args)))
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -277,7 +312,7 @@ def main():
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if r["prec"] == 0 else "f32+f64",
+        "dtype": "f64" if r["prec"] == 0 else "f32 (f64 dots/solution/residuals)",
         "data": "synthetic (seeded plate generator)",
         "config": {"workload": f"{p.name}: {p.n_dof} DOF, {p.n_elems} P{1 if p.kind == 3 else 2} elements",
                    "method": best, "rtol": RTOL, "l2": "inputs larger than L2 (matrix %.0f MB)" %
@@ -287,7 +322,11 @@ def main():
         "ms_assemble": round(r["ms_assemble"], 3),
         "ms_solve": round(r["ms_solve"], 3),
         "methods": {k: {"ms": round(v["ms"], 3), "iterations": v["iters"], "status": v["status"],
-                        "rel_residual": v["rel_res"]} for k, v in results.items()},
+                        "rel_residual": v["rel_res"], "err_vs_fp64": v["err_vs_fp64"],
+                        "replacements": v["repl"], "ms_assemble": round(v["ms_assemble"], 3),
+                        "spmv_ms": round(v["ms_spmv"], 5), "update_ms": round(v["ms_update"], 5)}
+                    for k, v in results.items()},
+        "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 3), "traffic": None, "kernel": "k_cg_spmv_dots",

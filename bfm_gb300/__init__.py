@@ -31,7 +31,7 @@ class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
                 ("ms_assemble", C.c_double), ("ms_solve", C.c_double)]
 
 
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_EXACT = 0, 1, 2
 PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED = 0, 1, 2
 HOST, DEVICE = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error"}

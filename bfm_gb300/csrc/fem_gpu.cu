@@ -626,11 +626,19 @@ struct CgState {
 	double bnorm2;
 	double gamma_old, alpha_old;
 	double alpha, beta;
-	double rho;         // (r,r) of the current iterate
-	double true_res2;   // ||b - A x||^2 after the solve
-	double rtol;
+	double rho;        // (r,r) of the current recurrence residual
+	double rho_ref;    // mixed: (r,r) right after the last residual replacement
+	double true_res2;  // ||b - A x||^2 after the solve
+	double rtol, drop2;
 	int iter, max_iters;
 	int done, status;
+	int replacements;
+};
+
+struct CgOpts {
+	double rtol;
+	double drop2;  // mixed: replace when (r,r) has dropped by this factor since the last replacement
+	int max_iters;
 };
 
 template <typename V>
@@ -638,7 +646,8 @@ struct CgArgs {
 	int N;
 	const int* row_ptr;
 	const int* cols;
-	const V* vals;
+	const V* vals;          // iteration operator
+	const double* vals64;   // FP64 operator for true residuals (nullptr: `vals` widened)
 	const V* dinv;
 	int block_pc;
 	const double* b;
@@ -650,21 +659,73 @@ struct CgArgs {
 	double* partials;
 	unsigned* ticket;
 	CgState* st;
-	cudaGraphConditionalHandle cond;
-	int use_cond;  // launched inside the solve graph: drive its while-node
+	CgOpts opts;
+	cudaGraphConditionalHandle cond;       // while-node: keep iterating
+	cudaGraphConditionalHandle cond_repl;  // if-node: replace the residual this iteration
+	int use_cond;  // launched inside the solve graph: drive its conditional nodes
 	int timing;    // measurement launches: ignore the stop flag, never set it
+	int mixed;     // FP32 recurrence with FP64 residual replacement
 };
+
+template <typename V> struct Vec2;
+template <> struct Vec2<double> { using T = double2; };
+template <> struct Vec2<float> { using T = float2; };
+
+template <typename V>
+__device__ __forceinline__ typename Vec2<V>::T ld2(const V* p, int i) {
+	return reinterpret_cast<const typename Vec2<V>::T*>(p)[i];
+}
+template <typename V>
+__device__ __forceinline__ void st2(V* p, int i, V a, V b) {
+	typename Vec2<V>::T t;
+	t.x = a;
+	t.y = b;
+	reinterpret_cast<typename Vec2<V>::T*>(p)[i] = t;
+}
+
+// 2x2 block k of the matrix: m0 m1 / m2 m3
+__device__ __forceinline__ void ld_block(const double* v, long k, double& m0, double& m1, double& m2, double& m3) {
+	double2 const a = reinterpret_cast<const double2*>(v)[2 * k];
+	double2 const b = reinterpret_cast<const double2*>(v)[2 * k + 1];
+	m0 = a.x; m1 = a.y; m2 = b.x; m3 = b.y;
+}
+__device__ __forceinline__ void ld_block(const float* v, long k, float& m0, float& m1, float& m2, float& m3) {
+	float4 const a = reinterpret_cast<const float4*>(v)[k];
+	m0 = a.x; m1 = a.y; m2 = a.z; m3 = a.w;
+}
 
 template <typename V>
 __device__ __forceinline__ void precond_apply(const CgArgs<V>& a, int c, V r0, V r1, V& u0, V& u1) {
 	if (a.block_pc) {
-		V const m0 = a.dinv[4 * c], m1 = a.dinv[4 * c + 1], m2 = a.dinv[4 * c + 2], m3 = a.dinv[4 * c + 3];
+		V m0, m1, m2, m3;
+		ld_block(a.dinv, c, m0, m1, m2, m3);
 		u0 = m0 * r0 + m1 * r1;
 		u1 = m2 * r0 + m3 * r1;
 	}
 	else {
-		u0 = a.dinv[2 * c] * r0;
-		u1 = a.dinv[2 * c + 1] * r1;
+		auto const d = ld2(a.dinv, c);
+		u0 = d.x * r0;
+		u1 = d.y * r1;
+	}
+}
+
+// y = A_res x in FP64 for row i (the residual operator)
+template <typename V>
+__device__ __forceinline__ void spmv64_row(const CgArgs<V>& a, int i, double& y0, double& y1) {
+	y0 = 0.0;
+	y1 = 0.0;
+	for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
+		int const c = a.cols[k];
+		double2 const xc = ld2(a.x, c);
+		double m0, m1, m2, m3;
+		if (a.vals64) ld_block(a.vals64, k, m0, m1, m2, m3);
+		else {
+			V n0, n1, n2, n3;
+			ld_block(a.vals, k, n0, n1, n2, n3);
+			m0 = n0; m1 = n1; m2 = n2; m3 = n3;
+		}
+		y0 += m0 * xc.x + m1 * xc.y;
+		y1 += m2 * xc.x + m3 * xc.y;
 	}
 }
 
@@ -672,67 +733,79 @@ template <typename V>
 __global__ void __launch_bounds__(TPB) k_cg_init(CgArgs<V> a) {
 	double v[1] = {0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		double const b0 = a.b[2 * i], b1 = a.b[2 * i + 1];
-		a.x[2 * i] = 0.0; a.x[2 * i + 1] = 0.0;
-		a.r[2 * i] = (V) b0; a.r[2 * i + 1] = (V) b1;
-		a.p[2 * i] = 0; a.p[2 * i + 1] = 0;
-		a.s[2 * i] = 0; a.s[2 * i + 1] = 0;
-		v[0] += b0 * b0 + b1 * b1;
+		double2 const bb = ld2(a.b, i);
+		st2(a.x, i, 0.0, 0.0);
+		st2(a.r, i, (V) bb.x, (V) bb.y);
+		st2(a.p, i, (V) 0, (V) 0);
+		st2(a.s, i, (V) 0, (V) 0);
+		v[0] += bb.x * bb.x + bb.y * bb.y;
 	}
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		CgState* st = a.st;
 		st->bnorm2 = out[0];
+		st->rtol = a.opts.rtol;
+		st->drop2 = a.opts.drop2;
+		st->max_iters = a.opts.max_iters;
 		st->iter = 0;
+		st->replacements = 0;
 		st->status = BFM_GPU_OK;
 		st->done = out[0] == 0.0;  // b = 0: x = 0 is exact
 		st->gamma_old = 0; st->alpha_old = 0;
 		st->alpha = 0; st->beta = 0;
 		st->rho = out[0];
+		st->rho_ref = out[0];
+		st->true_res2 = out[0];
 		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
 }
 
+// w = A u with u = M r formed on the fly; gamma = (r,u), delta = (w,u), rho = (r,r)
 template <typename V>
 __global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
 	CgState* st = a.st;
-	// The while-node continues only if this launch's finisher says so: block 0
-	// clears the condition first, the last block sets it after the stopping
-	// test.  A launch whose finisher did not run therefore ends the loop.
-	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
+	// The loop continues only if this launch's finisher says so: block 0
+	// clears the conditions first, the last block sets them after the
+	// stopping test.  A launch whose finisher did not run ends the loop.
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+		cudaGraphSetConditional(a.cond, 0u);
+		if (a.mixed) cudaGraphSetConditional(a.cond_repl, 0u);
+	}
 	if (st->done && !a.timing) return;
-	double v[3] = {0.0, 0.0, 0.0};  // gamma, delta, rho
+	double v[3] = {0.0, 0.0, 0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		int const ks = a.row_ptr[i], ke = a.row_ptr[i + 1];
 		V y0 = 0, y1 = 0;
 		for (int k = ks; k < ke; k++) {
 			int const c = a.cols[k];
+			auto const rc = ld2(a.r, c);
 			V u0, u1;
-			precond_apply(a, c, a.r[2 * c], a.r[2 * c + 1], u0, u1);
-			V const* m = a.vals + 4l * k;
-			y0 += m[0] * u0 + m[1] * u1;
-			y1 += m[2] * u0 + m[3] * u1;
+			precond_apply(a, c, rc.x, rc.y, u0, u1);
+			V m0, m1, m2, m3;
+			ld_block(a.vals, k, m0, m1, m2, m3);
+			y0 += m0 * u0 + m1 * u1;
+			y1 += m2 * u0 + m3 * u1;
 		}
-		a.w[2 * i] = y0;
-		a.w[2 * i + 1] = y1;
-		V const r0 = a.r[2 * i], r1 = a.r[2 * i + 1];
+		st2(a.w, i, y0, y1);
+		auto const ri = ld2(a.r, i);
 		V u0, u1;
-		precond_apply(a, i, r0, r1, u0, u1);
-		v[0] += (double) r0 * (double) u0 + (double) r1 * (double) u1;
+		precond_apply(a, i, ri.x, ri.y, u0, u1);
+		v[0] += (double) ri.x * (double) u0 + (double) ri.y * (double) u1;
 		v[1] += (double) y0 * (double) u0 + (double) y1 * (double) u1;
-		v[2] += (double) r0 * (double) r0 + (double) r1 * (double) r1;
+		v[2] += (double) ri.x * (double) ri.x + (double) ri.y * (double) ri.y;
 	}
 	double out[3];
 	if (grid_sum<3>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		double const gamma = out[0], delta = out[1], rho = out[2];
+		double const tol2 = st->rtol * st->rtol * st->bnorm2;
 		st->rho = rho;
-		int stop = 0;
-		if (rho <= st->rtol * st->rtol * st->bnorm2) {
+		int stop = 0, repl = 0;
+		if (!a.mixed && rho <= tol2) {
 			stop = 1;
 		}
 		else if (st->iter >= st->max_iters) {
 			stop = 1;
-			st->status = BFM_GPU_NOT_CONVERGED;
+			if (!a.timing) st->status = BFM_GPU_NOT_CONVERGED;
 		}
 		else {
 			double beta = 0.0, den = delta;
@@ -751,11 +824,17 @@ __global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
 				st->gamma_old = gamma;
 				st->alpha_old = alpha;
 				st->iter += 1;
+				// mixed: the FP32 recurrence has lost `drop` since the last
+				// FP64 residual, or claims convergence -> refresh from FP64
+				if (a.mixed) repl = rho <= st->drop2 * st->rho_ref || rho <= tol2;
 			}
 		}
 		if (a.timing) return;
 		st->done = stop;
-		if (a.use_cond && !stop) cudaGraphSetConditional(a.cond, 1u);
+		if (a.use_cond && !stop) {
+			cudaGraphSetConditional(a.cond, 1u);
+			if (repl) cudaGraphSetConditional(a.cond_repl, 1u);
+		}
 	}
 }
 
@@ -766,40 +845,69 @@ __global__ void __launch_bounds__(TPB) k_cg_update(CgArgs<V> a) {
 	V const alpha = (V) st->alpha, beta = (V) st->beta;
 	double const alpha64 = st->alpha;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		V const r0 = a.r[2 * i], r1 = a.r[2 * i + 1];
+		auto const r = ld2(a.r, i);
 		V u0, u1;
-		precond_apply(a, i, r0, r1, u0, u1);
-		V const p0 = u0 + beta * a.p[2 * i], p1 = u1 + beta * a.p[2 * i + 1];
-		V const s0 = a.w[2 * i] + beta * a.s[2 * i], s1 = a.w[2 * i + 1] + beta * a.s[2 * i + 1];
-		a.p[2 * i] = p0; a.p[2 * i + 1] = p1;
-		a.s[2 * i] = s0; a.s[2 * i + 1] = s1;
-		a.x[2 * i] += alpha64 * (double) p0;
-		a.x[2 * i + 1] += alpha64 * (double) p1;
-		a.r[2 * i] = r0 - alpha * s0;
-		a.r[2 * i + 1] = r1 - alpha * s1;
+		precond_apply(a, i, r.x, r.y, u0, u1);
+		auto const p = ld2(a.p, i);
+		auto const s = ld2(a.s, i);
+		auto const w = ld2(a.w, i);
+		V const p0 = u0 + beta * p.x, p1 = u1 + beta * p.y;
+		V const s0 = w.x + beta * s.x, s1 = w.y + beta * s.y;
+		st2(a.p, i, p0, p1);
+		st2(a.s, i, s0, s1);
+		double2 const x = ld2(a.x, i);
+		st2(a.x, i, x.x + alpha64 * (double) p0, x.y + alpha64 * (double) p1);
+		st2(a.r, i, r.x - alpha * s0, r.y - alpha * s1);
 	}
 }
 
-// ||b - A x||^2 in FP64 with the FP64 matrix (or the FP32 one widened)
+// Mixed precision, run only when requested (IF node): r = b - A_res x in
+// FP64 (rounded to the iteration precision), s = A p afresh, and the FP64
+// stopping test on the true residual.
 template <typename V>
-__global__ void __launch_bounds__(TPB) k_true_residual(CgArgs<V> a, const double* vals64) {
+__global__ void __launch_bounds__(TPB) k_cg_replace(CgArgs<V> a) {
+	CgState* st = a.st;
+	if (st->done) return;
 	double v[1] = {0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		double y0 = 0, y1 = 0;
+		double y0, y1;
+		spmv64_row(a, i, y0, y1);
+		double2 const bb = ld2(a.b, i);
+		double const e0 = bb.x - y0, e1 = bb.y - y1;
+		st2(a.r, i, (V) e0, (V) e1);
+		v[0] += e0 * e0 + e1 * e1;
+		V s0 = 0, s1 = 0;
 		for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
 			int const c = a.cols[k];
-			double const x0 = a.x[2 * c], x1 = a.x[2 * c + 1];
-			double m0, m1, m2, m3;
-			if (vals64) {
-				m0 = vals64[4l * k]; m1 = vals64[4l * k + 1]; m2 = vals64[4l * k + 2]; m3 = vals64[4l * k + 3];
-			}
-			else {
-				m0 = a.vals[4l * k]; m1 = a.vals[4l * k + 1]; m2 = a.vals[4l * k + 2]; m3 = a.vals[4l * k + 3];
-			}
-			y0 += m0 * x0 + m1 * x1;
-			y1 += m2 * x0 + m3 * x1;
+			auto const pc = ld2(a.p, c);
+			V m0, m1, m2, m3;
+			ld_block(a.vals, k, m0, m1, m2, m3);
+			s0 += m0 * pc.x + m1 * pc.y;
+			s1 += m2 * pc.x + m3 * pc.y;
 		}
-		double const e0 = a.b[2 * i] - y0, e1 = a.b[2 * i + 1] - y1;
+		st2(a.s, i, s0, s1);
+	}
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		st->replacements += 1;
+		st->rho_ref = out[0];
+		st->true_res2 = out[0];
+		if (out[0] <= st->rtol * st->rtol * st->bnorm2) {
+			st->done = 1;
+			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		}
+	}
+}
+
+// ||b - A_res x||^2 in FP64
+template <typename V>
+__global__ void __launch_bounds__(TPB) k_true_residual(CgArgs<V> a) {
+	double v[1] = {0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		double y0, y1;
+		spmv64_row(a, i, y0, y1);
+		double2 const bb = ld2(a.b, i);
+		double const e0 = bb.x - y0, e1 = bb.y - y1;
 		v[0] += e0 * e0 + e1 * e1;
 	}
 	double out[1];
@@ -875,6 +983,7 @@ struct bfm_gpu_problem {
 
 	cudaGraphExec_t graph;
 	int graph_precision, graph_precond;
+	bfm_gpu_opts_t graph_opts;
 
 	cudaEvent_t ev[4];
 	bool assembled, solved;
@@ -940,18 +1049,22 @@ int incidence(bfm_gpu_problem* P, const int* items, int n_items, int arity, int*
 }
 
 template <typename V>
-CgArgs<V> cg_args(bfm_gpu_problem* P, cudaGraphConditionalHandle h, int use_cond) {
+CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	CgArgs<V> a;
+	memset(&a, 0, sizeof a);
 	a.N = P->N;
 	a.row_ptr = P->row_ptr;
 	a.cols = P->cols;
 	if constexpr (sizeof(V) == 8) {
 		a.vals = P->vals64;
 		a.dinv = P->dinv64;
+		a.vals64 = P->vals64;
 	}
 	else {
 		a.vals = P->vals32;
 		a.dinv = P->dinv32;
+		a.vals64 = P->precision == BFM_GPU_MIXED_EXACT ? P->vals64 : nullptr;
+		a.mixed = 1;
 	}
 	a.block_pc = P->precond == BFM_GPU_PC_BLOCK_JACOBI;
 	a.b = P->b;
@@ -963,17 +1076,18 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, cudaGraphConditionalHandle h, int use_cond
 	a.partials = P->partials;
 	a.ticket = P->ticket;
 	a.st = P->st;
-	a.cond = h;
-	a.use_cond = use_cond;
-	a.timing = 0;
+	if (o) {
+		a.opts.rtol = o->rtol;
+		a.opts.drop2 = o->replace_drop * o->replace_drop;
+		a.opts.max_iters = o->max_iters;
+	}
 	return a;
 }
 
 template <typename V>
-int add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps, void* fn, int grid, CgArgs<V>* args,
-               const double** extra = nullptr) {
+int add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps, void* fn, int grid, CgArgs<V>* args) {
 	cudaKernelNodeParams kp = {};
-	void* params[2] = {args, (void*) extra};
+	void* params[1] = {args};
 	kp.func = fn;
 	kp.gridDim = dim3(grid);
 	kp.blockDim = dim3(TPB);
@@ -983,33 +1097,42 @@ int add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps
 	return 0;
 }
 
-// init -> while(not done){ spmv+dots ; update } -> true residual
+// init -> while(running){ spmv+dots ; update ; [mixed: if(replace){ FP64 residual }] } -> true residual
 template <typename V>
-int build_graph(bfm_gpu_problem* P) {
+int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	cudaGraph_t g;
 	CK(cudaGraphCreate(&g, 0));
-	cudaGraphConditionalHandle h;
-	CK(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
-	CgArgs<V> a = cg_args<V>(P, h, 1);
-	cudaGraphNode_t n_init, n_cond, n_a, n_b, n_res;
-	if (add_kernel<V>(g, &n_init, nullptr, 0, (void*) k_cg_init<V>, P->grid, &a)) return -1;
+	CgArgs<V> a = cg_args<V>(P, o);
+	a.use_cond = 1;
+	CK(cudaGraphConditionalHandleCreate(&a.cond, g, 1u, cudaGraphCondAssignDefault));
+	cudaGraphNode_t n_init, n_cond, n_a, n_b, n_if, n_r, n_res;
+	// the body's if-handle is created once the body graph exists; the
+	// kernels of every node must carry it, so add the nodes afterwards
 	cudaGraphNodeParams cp = {};
 	cp.type = cudaGraphNodeTypeConditional;
-	cp.conditional.handle = h;
+	cp.conditional.handle = a.cond;
 	cp.conditional.type = cudaGraphCondTypeWhile;
 	cp.conditional.size = 1;
+	// init first (no dependency), then the while node after it
+	CgArgs<V> a0 = a;
+	if (add_kernel<V>(g, &n_init, nullptr, 0, (void*) k_cg_init<V>, P->grid, &a0)) return -1;
 	CK(cudaGraphAddNode(&n_cond, g, &n_init, nullptr, 1, &cp));
 	cudaGraph_t body = cp.conditional.phGraph_out[0];
+	cudaGraphNodeParams ip = {};
+	if (a.mixed) {
+		CK(cudaGraphConditionalHandleCreate(&a.cond_repl, body, 0u, cudaGraphCondAssignDefault));
+		ip.type = cudaGraphNodeTypeConditional;
+		ip.conditional.handle = a.cond_repl;
+		ip.conditional.type = cudaGraphCondTypeIf;
+		ip.conditional.size = 1;
+	}
 	if (add_kernel<V>(body, &n_a, nullptr, 0, (void*) k_cg_spmv_dots<V>, P->grid, &a)) return -1;
 	if (add_kernel<V>(body, &n_b, &n_a, 1, (void*) k_cg_update<V>, P->grid, &a)) return -1;
-	const double* v64 = sizeof(V) == 8 ? nullptr : P->vals64;
-	cudaKernelNodeParams kp = {};
-	void* params[2] = {&a, &v64};
-	kp.func = (void*) k_true_residual<V>;
-	kp.gridDim = dim3(P->grid);
-	kp.blockDim = dim3(TPB);
-	kp.kernelParams = params;
-	CK(cudaGraphAddKernelNode(&n_res, g, &n_cond, 1, &kp));
+	if (a.mixed) {
+		CK(cudaGraphAddNode(&n_if, body, &n_b, nullptr, 1, &ip));
+		if (add_kernel<V>(ip.conditional.phGraph_out[0], &n_r, nullptr, 0, (void*) k_cg_replace<V>, P->grid, &a)) return -1;
+	}
+	if (add_kernel<V>(g, &n_res, &n_cond, 1, (void*) k_true_residual<V>, P->grid, &a)) return -1;
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	P->graph = nullptr;
 	CK(cudaGraphInstantiate(&P->graph, g, 0));
@@ -1213,16 +1336,19 @@ int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int*
 
 int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	g_err[0] = 0;
-	if (precision != BFM_GPU_FP64 && precision != BFM_GPU_MIXED) return fail("unknown precision");
+	if (precision != BFM_GPU_FP64 && precision != BFM_GPU_MIXED && precision != BFM_GPU_MIXED_EXACT)
+		return fail("unknown precision %d", precision);
+	bool const want64 = precision != BFM_GPU_MIXED;  // FP64 values: the operator, or the residual operator
+	bool const want32 = precision != BFM_GPU_FP64;   // FP32 values: the mixed iteration operator
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
 	// value storage for this precision (allocated once, on first use)
-	if (precision == BFM_GPU_FP64 && !P->vals64 && dalloc(&P->vals64, 4 * P->nb_cap)) return -1;
-	if (precision == BFM_GPU_MIXED && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
-	if (precision == BFM_GPU_FP64 && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
-	if (precision == BFM_GPU_MIXED && !P->dinv32 && dalloc(&P->dinv32, 4 * N)) return -1;
+	if (want64 && !P->vals64 && dalloc(&P->vals64, 4 * P->nb_cap)) return -1;
+	if (want32 && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
+	if (!want32 && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
+	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 4 * N)) return -1;
 	size_t const vsz = precision == BFM_GPU_FP64 ? sizeof(double) : sizeof(float);
-	if (P->precision != precision) {
+	if ((P->precision == BFM_GPU_FP64) != (precision == BFM_GPU_FP64) || !P->r) {
 		void** vecs[] = {&P->r, &P->p, &P->s, &P->w};
 		for (void** v : vecs) {
 			if (*v) cudaFree(*v);
@@ -1269,14 +1395,14 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.last_ci = P->last_ci;
 	a.first = P->first;
 	a.last = P->last;
-	a.vals64 = precision == BFM_GPU_FP64 ? P->vals64 : nullptr;
-	a.vals32 = precision == BFM_GPU_MIXED ? P->vals32 : nullptr;
+	a.vals64 = want64 ? P->vals64 : nullptr;
+	a.vals32 = want32 ? P->vals32 : nullptr;
 	a.b = P->b;
-	a.dinv64 = precision == BFM_GPU_FP64 ? P->dinv64 : nullptr;
-	a.dinv32 = precision == BFM_GPU_MIXED ? P->dinv32 : nullptr;
+	a.dinv64 = want32 ? nullptr : P->dinv64;
+	a.dinv32 = want32 ? P->dinv32 : nullptr;
 	a.precond = P->precond;
 	a.err = P->err;
-	if (precision == BFM_GPU_FP64) k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
+	if (precision != BFM_GPU_MIXED) k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
 	else k_assemble<false><<<blocks_for(N, 128), 128, 0, st>>>(a);
 	// 5. Neumann loads
 	bool has_neu = false;
@@ -1314,25 +1440,24 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	bfm_gpu_opts_t o;
 	if (opts) o = *opts;
 	else bfm_gpu_default_opts(&o);
+	if (!(o.rtol >= 0.0) || o.max_iters < 0) return fail("invalid solver options");
+	if (o.precond == BFM_GPU_PC_LEARNED) return fail("learned preconditioner not available in this build");
 	if (o.precond != P->precond) {
-		// the preconditioner diagonal is formed by the assembly epilogue
+		// the preconditioner is formed by the assembly epilogue
 		P->precond = o.precond;
 		if (bfm_gpu_problem_assemble(P, P->precision)) return -1;
 	}
-	if (o.precond == BFM_GPU_PC_LEARNED) return fail("learned preconditioner not available in this build");
-	if (!P->graph || P->graph_precision != P->precision || P->graph_precond != P->precond) {
-		int const rc = P->precision == BFM_GPU_FP64 ? build_graph<double>(P) : build_graph<float>(P);
+	// options are baked into the graph's kernel parameters: rebuild only when they change
+	bool const same = P->graph && P->graph_precision == P->precision && P->graph_precond == P->precond &&
+	                  P->graph_opts.rtol == o.rtol && P->graph_opts.max_iters == o.max_iters &&
+	                  P->graph_opts.replace_drop == o.replace_drop;
+	if (!same) {
+		int const rc = P->precision == BFM_GPU_FP64 ? build_graph<double>(P, &o) : build_graph<float>(P, &o);
 		if (rc) return -1;
 		P->graph_precision = P->precision;
 		P->graph_precond = P->precond;
+		P->graph_opts = o;
 	}
-	// options live in device memory so one graph serves every tolerance
-	CgState* h = P->st_host;
-	CK(cudaStreamSynchronize(P->stream));  // h may still be read by an earlier copy
-	memset(h, 0, sizeof *h);
-	h->rtol = o.rtol;
-	h->max_iters = o.max_iters;
-	CK(cudaMemcpyAsync(P->st, h, sizeof *h, cudaMemcpyHostToDevice, P->stream));
 	CK(cudaEventRecord(P->ev[2], P->stream));
 	CK(cudaGraphLaunch(P->graph, P->stream));
 	CK(cudaEventRecord(P->ev[3], P->stream));
@@ -1365,6 +1490,7 @@ int bfm_gpu_problem_stats(bfm_gpu_problem_t* P, bfm_gpu_stats_t* s) {
 		CgState const* h = P->st_host;
 		s->status = h->status;
 		s->iterations = h->iter;
+		s->replacements = h->replacements;
 		s->rel_residual = h->bnorm2 > 0 ? sqrt(h->true_res2 / h->bnorm2) : 0.0;
 	}
 	return 0;
@@ -1427,7 +1553,9 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 	for (auto& x : e) cudaEventCreate(&x);
 	float t1 = 0, t2 = 0;
 	if (P->precision == BFM_GPU_FP64) {
-		CgArgs<double> a = cg_args<double>(P, 0, 0);
+		CgArgs<double> a = cg_args<double>(P, nullptr);
+		a.opts.rtol = 0.0;
+		a.opts.max_iters = 1 << 30;
 		a.st = scratch;
 		a.timing = 1;
 		k_cg_init<double><<<P->grid, TPB, 0, P->stream>>>(a);
@@ -1439,7 +1567,9 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 		cudaEventRecord(e[2], P->stream);
 	}
 	else {
-		CgArgs<float> a = cg_args<float>(P, 0, 0);
+		CgArgs<float> a = cg_args<float>(P, nullptr);
+		a.opts.rtol = 0.0;
+		a.opts.max_iters = 1 << 30;
 		a.st = scratch;
 		a.timing = 1;
 		k_cg_init<float><<<P->grid, TPB, 0, P->stream>>>(a);

@@ -34,8 +34,12 @@ enum { BFM_GPU_HOST = 0, BFM_GPU_DEVICE = 1 };
 /* arithmetic of the stiffness matrix and Krylov vectors */
 enum {
 	BFM_GPU_FP64 = 0,  /* FP64 element integration (reference operation order), FP64 CG          */
-	BFM_GPU_MIXED = 1, /* FP32 element integration and SpMV; FP64 inner products, FP64 solution,
-	                      FP64 residual replacement and outer refinement                          */
+	BFM_GPU_MIXED = 1, /* FP32 element integration and SpMV, FP32 Krylov vectors; FP64 inner
+	                      products, FP64 solution and FP64 residual replacement (with the FP32
+	                      stiffness widened): converges to the FP32-integrated system             */
+	BFM_GPU_MIXED_EXACT = 2, /* as MIXED, but the element loop runs in FP64 once: the FP64 matrix is
+	                            the residual operator (solution of the FP64 system) and its FP32
+	                            rounding the iteration operator                                    */
 };
 
 /* preconditioner */
