@@ -156,7 +156,11 @@ def run_gpu(args, rank: int, world: int):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     lib = bfm_gb300.lib()
     p = workload(args.workload)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the problem's kernels and the timing events share it
+    # (torch's default stream is the legacy NULL stream, which the library
+    # would replace by a private one)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     methods = {"fp64": (bfm_gb300.FP64, bfm_gb300.PC_JACOBI),
                "mixed": (bfm_gb300.MIXED, bfm_gb300.PC_JACOBI),
                "mixed_exact": (bfm_gb300.MIXED_EXACT, bfm_gb300.PC_JACOBI)}
@@ -260,7 +264,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="perforated")
-    ap.add_argument("--method", default="best", choices=["fp64", "mixed", "best"])
+    ap.add_argument("--method", default="best", choices=["fp64", "mixed", "mixed_exact", "best"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="assemble once and launch the two CG kernels --reps times each, standalone "

@@ -22,7 +22,7 @@ _lib: C.CDLL | None = None
 
 class bfm_gpu_opts_t(C.Structure):  # include/bfm/gpu.h
     _fields_ = [("precision", C.c_int), ("precond", C.c_int), ("rtol", C.c_double), ("max_iters", C.c_int),
-                ("replace_drop", C.c_double), ("deterministic", C.c_int)]
+                ("replace_drop", C.c_double), ("deterministic", C.c_int), ("autotune", C.c_int)]
 
 
 class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
@@ -62,6 +62,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_download": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "bfm_gpu_problem_stream": (_vp, [_vp]),
     "bfm_gpu_problem_time_kernels": (_i, [_vp, _i, _P(_d), _P(_d)]),
+    "bfm_gpu_problem_autotune": (_i, [_vp, _P(_i)]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
 }
 

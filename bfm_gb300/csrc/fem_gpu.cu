@@ -624,6 +624,7 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double* __restrict__ p
 
 struct CgState {
 	double bnorm2;
+	double gamma;      // (r, M r) of the current residual
 	double gamma_old, alpha_old;
 	double alpha, beta;
 	double rho;        // (r,r) of the current recurrence residual
@@ -641,21 +642,24 @@ struct CgOpts {
 	int max_iters;
 };
 
+// Vectors are interleaved (u,v) per node and accessed as pairs.
 template <typename V>
 struct CgArgs {
 	int N;
 	const int* row_ptr;
 	const int* cols;
-	const V* vals;          // iteration operator
+	const V* vals;          // iteration operator (2x2 blocks)
 	const double* vals64;   // FP64 operator for true residuals (nullptr: `vals` widened)
-	const V* dinv;
+	const V* dinv;          // Jacobi: 2 per node; block Jacobi: 4 per node
 	int block_pc;
 	const double* b;
 	double* x;
 	V* r;
-	V* p;
-	V* s;
-	V* w;
+	V* u;   // FP64 path: u = M r (materialized); mixed path: unused
+	V* p;   // FP64 path: direction; mixed path: direction read this iteration
+	V* pn;  // mixed path: direction written this iteration (ping-pong with p)
+	V* s;   // FP64 path: s = A p by recurrence
+	V* w;   // FP64 path: w = A u; mixed path: q = A p
 	double* partials;
 	unsigned* ticket;
 	CgState* st;
@@ -664,7 +668,6 @@ struct CgArgs {
 	cudaGraphConditionalHandle cond_repl;  // if-node: replace the residual this iteration
 	int use_cond;  // launched inside the solve graph: drive its conditional nodes
 	int timing;    // measurement launches: ignore the stop flag, never set it
-	int mixed;     // FP32 recurrence with FP64 residual replacement
 };
 
 template <typename V> struct Vec2;
@@ -683,7 +686,7 @@ __device__ __forceinline__ void st2(V* p, int i, V a, V b) {
 	reinterpret_cast<typename Vec2<V>::T*>(p)[i] = t;
 }
 
-// 2x2 block k of the matrix: m0 m1 / m2 m3
+// 2x2 block k of the matrix: m0 m1 / m2 m3 (one 32-byte or 16-byte vector load)
 __device__ __forceinline__ void ld_block(const double* v, long k, double& m0, double& m1, double& m2, double& m3) {
 	double2 const a = reinterpret_cast<const double2*>(v)[2 * k];
 	double2 const b = reinterpret_cast<const double2*>(v)[2 * k + 1];
@@ -695,55 +698,78 @@ __device__ __forceinline__ void ld_block(const float* v, long k, float& m0, floa
 }
 
 template <typename V>
-__device__ __forceinline__ void precond_apply(const CgArgs<V>& a, int c, V r0, V r1, V& u0, V& u1) {
-	if (a.block_pc) {
+__device__ __forceinline__ void precond_apply(const V* dinv, int block_pc, int c, V r0, V r1, V& u0, V& u1) {
+	if (block_pc) {
 		V m0, m1, m2, m3;
-		ld_block(a.dinv, c, m0, m1, m2, m3);
+		ld_block(dinv, c, m0, m1, m2, m3);
 		u0 = m0 * r0 + m1 * r1;
 		u1 = m2 * r0 + m3 * r1;
 	}
 	else {
-		auto const d = ld2(a.dinv, c);
+		auto const d = ld2(dinv, c);
 		u0 = d.x * r0;
 		u1 = d.y * r1;
 	}
 }
 
-// y = A_res x in FP64 for row i (the residual operator)
-template <typename V>
-__device__ __forceinline__ void spmv64_row(const CgArgs<V>& a, int i, double& y0, double& y1) {
-	y0 = 0.0;
-	y1 = 0.0;
-	for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
-		int const c = a.cols[k];
-		double2 const xc = ld2(a.x, c);
-		double m0, m1, m2, m3;
-		if (a.vals64) ld_block(a.vals64, k, m0, m1, m2, m3);
-		else {
-			V n0, n1, n2, n3;
-			ld_block(a.vals, k, n0, n1, n2, n3);
-			m0 = n0; m1 = n1; m2 = n2; m3 = n3;
-		}
-		y0 += m0 * xc.x + m1 * xc.y;
-		y1 += m2 * xc.x + m3 * xc.y;
+// One block row of y = A g with LPR lanes per row: lane `sub` takes blocks
+// sub, sub+LPR, ... (adjacent lanes read adjacent blocks: coalesced vector
+// loads), then the group adds its partial sums with shuffles.  Every lane of
+// the warp must call this (rows past the end pass ks == ke).
+template <int LPR, typename A, typename V, typename G>
+__device__ __forceinline__ void row_product(const int* __restrict__ cols, const V* __restrict__ vals, int ks, int ke, int sub,
+                                            G gather, A& y0, A& y1) {
+	y0 = A(0);
+	y1 = A(0);
+#pragma unroll 2
+	for (int k = ks + sub; k < ke; k += LPR) {
+		int const c = cols[k];
+		A g0, g1;
+		gather(c, g0, g1);
+		V m0, m1, m2, m3;
+		ld_block(vals, k, m0, m1, m2, m3);
+		y0 += A(m0) * g0 + A(m1) * g1;
+		y1 += A(m2) * g0 + A(m3) * g1;
+	}
+#pragma unroll
+	for (int o = LPR / 2; o; o >>= 1) {
+		y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+		y1 += __shfl_xor_sync(0xffffffffu, y1, o);
 	}
 }
 
+// row loop shared by the SpMV kernels: every warp runs the same number of trips
+#define FOR_ROWS(LPR)                                                                          \
+	int const sub_ = threadIdx.x % (LPR);                                                       \
+	int const rows_per_block_ = blockDim.x / (LPR);                                             \
+	for (int base_ = blockIdx.x * rows_per_block_; base_ < a.N; base_ += gridDim.x * rows_per_block_) \
+		for (int row_ = base_ + threadIdx.x / (LPR), once_ = 1; once_; once_ = 0)
+
+// ---------------------------------------------------------------- init
+
 template <typename V>
-__global__ void __launch_bounds__(TPB) k_cg_init(CgArgs<V> a) {
-	double v[1] = {0.0};
+__global__ void __launch_bounds__(TPB) k_cg_init(CgArgs<V> a, int mixed) {
+	double v[2] = {0.0, 0.0};  // (b,b), (b, M b)
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		double2 const bb = ld2(a.b, i);
+		V const r0 = (V) bb.x, r1 = (V) bb.y;
+		V u0, u1;
+		precond_apply(a.dinv, a.block_pc, i, r0, r1, u0, u1);
 		st2(a.x, i, 0.0, 0.0);
-		st2(a.r, i, (V) bb.x, (V) bb.y);
+		st2(a.r, i, r0, r1);
 		st2(a.p, i, (V) 0, (V) 0);
-		st2(a.s, i, (V) 0, (V) 0);
+		if (!mixed) {
+			st2(a.u, i, u0, u1);
+			st2(a.s, i, (V) 0, (V) 0);
+		}
 		v[0] += bb.x * bb.x + bb.y * bb.y;
+		v[1] += (double) r0 * (double) u0 + (double) r1 * (double) u1;
 	}
-	double out[1];
-	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		CgState* st = a.st;
 		st->bnorm2 = out[0];
+		st->gamma = out[1];
 		st->rtol = a.opts.rtol;
 		st->drop2 = a.opts.drop2;
 		st->max_iters = a.opts.max_iters;
@@ -760,47 +786,48 @@ __global__ void __launch_bounds__(TPB) k_cg_init(CgArgs<V> a) {
 	}
 }
 
-// w = A u with u = M r formed on the fly; gamma = (r,u), delta = (w,u), rho = (r,r)
-template <typename V>
-__global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
+// ---------------------------------------------------------------- FP64 path
+// Chronopoulos-Gear PCG: one reduction per iteration and only the SpMV's
+// 4 FP64 FMAs per block in the gathered loop (FP64 issue rate bounds this
+// path on GB300, so u = M r is materialized once per node instead of being
+// formed per neighbour).
+//   A: w = A u; gamma = (r,u), delta = (w,u), rho = (r,r); alpha, beta
+//   B: p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = M r
+
+template <int LPR>
+__global__ void __launch_bounds__(TPB) k_cg64_spmv(CgArgs<double> a) {
 	CgState* st = a.st;
 	// The loop continues only if this launch's finisher says so: block 0
-	// clears the conditions first, the last block sets them after the
-	// stopping test.  A launch whose finisher did not run ends the loop.
-	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
-		cudaGraphSetConditional(a.cond, 0u);
-		if (a.mixed) cudaGraphSetConditional(a.cond_repl, 0u);
-	}
+	// clears the condition first, the last block sets it after the stopping
+	// test.  A launch whose finisher did not run therefore ends the loop.
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
 	if (st->done && !a.timing) return;
 	double v[3] = {0.0, 0.0, 0.0};
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		int const ks = a.row_ptr[i], ke = a.row_ptr[i + 1];
-		V y0 = 0, y1 = 0;
-		for (int k = ks; k < ke; k++) {
-			int const c = a.cols[k];
-			auto const rc = ld2(a.r, c);
-			V u0, u1;
-			precond_apply(a, c, rc.x, rc.y, u0, u1);
-			V m0, m1, m2, m3;
-			ld_block(a.vals, k, m0, m1, m2, m3);
-			y0 += m0 * u0 + m1 * u1;
-			y1 += m2 * u0 + m3 * u1;
+	const double* __restrict__ u = a.u;
+	auto gather = [u](int c, double& g0, double& g1) {
+		double2 const t = ld2(u, c);
+		g0 = t.x;
+		g1 = t.y;
+	};
+	FOR_ROWS(LPR) {
+		bool const ok = row_ < a.N;
+		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		double y0, y1;
+		row_product<LPR, double>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		if (ok && sub_ == 0) {
+			st2(a.w, row_, y0, y1);
+			double2 const ri = ld2(a.r, row_), ui = ld2(u, row_);
+			v[0] += ri.x * ui.x + ri.y * ui.y;
+			v[1] += y0 * ui.x + y1 * ui.y;
+			v[2] += ri.x * ri.x + ri.y * ri.y;
 		}
-		st2(a.w, i, y0, y1);
-		auto const ri = ld2(a.r, i);
-		V u0, u1;
-		precond_apply(a, i, ri.x, ri.y, u0, u1);
-		v[0] += (double) ri.x * (double) u0 + (double) ri.y * (double) u1;
-		v[1] += (double) y0 * (double) u0 + (double) y1 * (double) u1;
-		v[2] += (double) ri.x * (double) ri.x + (double) ri.y * (double) ri.y;
 	}
 	double out[3];
 	if (grid_sum<3>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		double const gamma = out[0], delta = out[1], rho = out[2];
-		double const tol2 = st->rtol * st->rtol * st->bnorm2;
 		st->rho = rho;
-		int stop = 0, repl = 0;
-		if (!a.mixed && rho <= tol2) {
+		int stop = 0;
+		if (rho <= st->rtol * st->rtol * st->bnorm2) {
 			stop = 1;
 		}
 		else if (st->iter >= st->max_iters) {
@@ -824,74 +851,194 @@ __global__ void __launch_bounds__(TPB) k_cg_spmv_dots(CgArgs<V> a) {
 				st->gamma_old = gamma;
 				st->alpha_old = alpha;
 				st->iter += 1;
-				// mixed: the FP32 recurrence has lost `drop` since the last
-				// FP64 residual, or claims convergence -> refresh from FP64
-				if (a.mixed) repl = rho <= st->drop2 * st->rho_ref || rho <= tol2;
 			}
 		}
 		if (a.timing) return;
 		st->done = stop;
-		if (a.use_cond && !stop) {
-			cudaGraphSetConditional(a.cond, 1u);
-			if (repl) cudaGraphSetConditional(a.cond_repl, 1u);
-		}
+		if (a.use_cond && !stop) cudaGraphSetConditional(a.cond, 1u);
 	}
 }
 
-template <typename V>
-__global__ void __launch_bounds__(TPB) k_cg_update(CgArgs<V> a) {
+__global__ void __launch_bounds__(TPB) k_cg64_update(CgArgs<double> a) {
 	CgState const* st = a.st;
 	if (st->done && !a.timing) return;
-	V const alpha = (V) st->alpha, beta = (V) st->beta;
-	double const alpha64 = st->alpha;
+	double const alpha = st->alpha, beta = st->beta;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		auto const r = ld2(a.r, i);
-		V u0, u1;
-		precond_apply(a, i, r.x, r.y, u0, u1);
-		auto const p = ld2(a.p, i);
-		auto const s = ld2(a.s, i);
-		auto const w = ld2(a.w, i);
-		V const p0 = u0 + beta * p.x, p1 = u1 + beta * p.y;
-		V const s0 = w.x + beta * s.x, s1 = w.y + beta * s.y;
+		double2 const u = ld2(a.u, i), p = ld2(a.p, i), s = ld2(a.s, i), w = ld2(a.w, i);
+		double2 const x = ld2(a.x, i), r = ld2(a.r, i);
+		double const p0 = u.x + beta * p.x, p1 = u.y + beta * p.y;
+		double const s0 = w.x + beta * s.x, s1 = w.y + beta * s.y;
+		double const r0 = r.x - alpha * s0, r1 = r.y - alpha * s1;
 		st2(a.p, i, p0, p1);
 		st2(a.s, i, s0, s1);
-		double2 const x = ld2(a.x, i);
-		st2(a.x, i, x.x + alpha64 * (double) p0, x.y + alpha64 * (double) p1);
-		st2(a.r, i, r.x - alpha * s0, r.y - alpha * s1);
+		st2(a.x, i, x.x + alpha * p0, x.y + alpha * p1);
+		st2(a.r, i, r0, r1);
+		double u0, u1;
+		precond_apply(a.dinv, a.block_pc, i, r0, r1, u0, u1);
+		st2(a.u, i, u0, u1);
 	}
 }
 
-// Mixed precision, run only when requested (IF node): r = b - A_res x in
-// FP64 (rounded to the iteration precision), s = A p afresh, and the FP64
-// stopping test on the true residual.
-template <typename V>
-__global__ void __launch_bounds__(TPB) k_cg_replace(CgArgs<V> a) {
+// ---------------------------------------------------------------- mixed path
+// Hestenes-Stiefel PCG in FP32 with FP64 inner products and FP64 solution.
+// The direction update is fused into the SpMV: a neighbour's new direction
+// M r + beta p_old is formed where it is gathered (FP32 arithmetic is cheap),
+// the row's own one is stored in the other buffer of a ping-pong pair.
+//   K1: p' = M r + beta p; q = A p'; alpha = gamma / (p', q)
+//   K2: x += alpha p' (FP64); r -= alpha q; gamma' = (r, M r), rho = (r,r); beta
+//   R (only when requested): r = b - A64 x in FP64; gamma = (r, M r)
+// Stable under residual replacement (unlike the single-reduction variant,
+// whose alpha assumes orthogonality that replacement breaks).
+
+template <int LPR>
+__global__ void __launch_bounds__(TPB) k_mx_spmv(CgArgs<float> a) {
 	CgState* st = a.st;
-	if (st->done) return;
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+		cudaGraphSetConditional(a.cond, 0u);
+		cudaGraphSetConditional(a.cond_repl, 0u);
+	}
+	if (st->done && !a.timing) return;
+	float const beta = (float) st->beta;
+	const float* __restrict__ r = a.r;
+	const float* __restrict__ p = a.p;
+	const float* __restrict__ dinv = a.dinv;
+	int const bpc = a.block_pc;
+	auto gather = [=](int c, float& g0, float& g1) {
+		float2 const rc = ld2(r, c), pc = ld2(p, c);
+		float z0, z1;
+		precond_apply(dinv, bpc, c, rc.x, rc.y, z0, z1);
+		g0 = z0 + beta * pc.x;
+		g1 = z1 + beta * pc.y;
+	};
 	double v[1] = {0.0};
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		double y0, y1;
-		spmv64_row(a, i, y0, y1);
-		double2 const bb = ld2(a.b, i);
-		double const e0 = bb.x - y0, e1 = bb.y - y1;
-		st2(a.r, i, (V) e0, (V) e1);
-		v[0] += e0 * e0 + e1 * e1;
-		V s0 = 0, s1 = 0;
-		for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
-			int const c = a.cols[k];
-			auto const pc = ld2(a.p, c);
-			V m0, m1, m2, m3;
-			ld_block(a.vals, k, m0, m1, m2, m3);
-			s0 += m0 * pc.x + m1 * pc.y;
-			s1 += m2 * pc.x + m3 * pc.y;
+	FOR_ROWS(LPR) {
+		bool const ok = row_ < a.N;
+		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		float y0, y1;
+		row_product<LPR, float>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		if (ok && sub_ == 0) {
+			float g0, g1;
+			gather(row_, g0, g1);
+			st2(a.pn, row_, g0, g1);
+			st2(a.w, row_, y0, y1);
+			v[0] += (double) g0 * (double) y0 + (double) g1 * (double) y1;
 		}
-		st2(a.s, i, s0, s1);
 	}
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		double const pq = out[0];
+		if (!(pq > 0.0)) {
+			if (!a.timing) {
+				st->done = 1;
+				st->status = BFM_GPU_BREAKDOWN;
+			}
+			return;  // the while condition stays cleared
+		}
+		st->alpha = st->gamma / pq;
+		if (a.use_cond) cudaGraphSetConditional(a.cond, 1u);
+	}
+}
+
+__global__ void __launch_bounds__(TPB) k_mx_update(CgArgs<float> a) {
+	CgState* st = a.st;
+	if (st->done && !a.timing) return;
+	double const alpha64 = st->alpha;
+	float const alpha = (float) alpha64;
+	double v[2] = {0.0, 0.0};  // gamma' = (r, M r), rho = (r, r)
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		float2 const pn = ld2(a.pn, i), q = ld2(a.w, i), r = ld2(a.r, i);
+		double2 const x = ld2(a.x, i);
+		st2(a.x, i, x.x + alpha64 * (double) pn.x, x.y + alpha64 * (double) pn.y);
+		float const r0 = r.x - alpha * q.x, r1 = r.y - alpha * q.y;
+		st2(a.r, i, r0, r1);
+		float z0, z1;
+		precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
+		v[0] += (double) r0 * (double) z0 + (double) r1 * (double) z1;
+		v[1] += (double) r0 * (double) r0 + (double) r1 * (double) r1;
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		if (a.timing) return;
+		double const gamma = out[0], rho = out[1];
+		double const tol2 = st->rtol * st->rtol * st->bnorm2;
+		st->rho = rho;
+		st->iter += 1;
+		st->beta = gamma / st->gamma;
+		st->gamma = gamma;
+		int stop = 0, repl = 0;
+		if (st->iter >= st->max_iters) {
+			stop = 1;
+			st->status = BFM_GPU_NOT_CONVERGED;
+		}
+		else if (!(gamma > 0.0)) {
+			// r = 0 exactly, or NaN: let the FP64 residual decide
+			repl = gamma == 0.0;
+			if (!repl) {
+				stop = 1;
+				st->status = BFM_GPU_BREAKDOWN;
+			}
+		}
+		else {
+			// the FP32 recurrence has lost `drop` since the last FP64
+			// residual, or claims convergence: refresh from FP64
+			repl = rho <= st->drop2 * st->rho_ref || rho <= tol2;
+		}
+		if (stop) {
+			st->done = 1;
+			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		}
+		else if (repl && a.use_cond) {
+			cudaGraphSetConditional(a.cond_repl, 1u);
+		}
+	}
+}
+
+// y = A_res x in FP64, LPR lanes per row; the residual operator is the FP64
+// matrix when present, else the iteration matrix widened
+template <int LPR, typename V>
+__device__ __forceinline__ void residual_row(const CgArgs<V>& a, int row, int sub, double& e0, double& e1) {
+	bool const ok = row < a.N;
+	int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+	const double* __restrict__ x = a.x;
+	auto gather = [x](int c, double& g0, double& g1) {
+		double2 const t = ld2(x, c);
+		g0 = t.x;
+		g1 = t.y;
+	};
+	double y0, y1;
+	if (a.vals64) row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gather, y0, y1);
+	else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, gather, y0, y1);
+	e0 = e1 = 0.0;
+	if (ok) {
+		double2 const bb = ld2(a.b, row);
+		e0 = bb.x - y0;
+		e1 = bb.y - y1;
+	}
+}
+
+template <int LPR>
+__global__ void __launch_bounds__(TPB) k_mx_replace(CgArgs<float> a) {
+	CgState* st = a.st;
+	if (st->done) return;
+	double v[2] = {0.0, 0.0};  // (r,r), (r, M r)
+	FOR_ROWS(LPR) {
+		double e0, e1;
+		residual_row<LPR>(a, row_, sub_, e0, e1);
+		if (row_ < a.N && sub_ == 0) {
+			float const r0 = (float) e0, r1 = (float) e1;
+			st2(a.r, row_, r0, r1);
+			float z0, z1;
+			precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
+			v[0] += e0 * e0 + e1 * e1;
+			v[1] += (double) r0 * (double) z0 + (double) r1 * (double) z1;
+		}
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		st->replacements += 1;
 		st->rho_ref = out[0];
 		st->true_res2 = out[0];
+		st->gamma = out[1];
 		if (out[0] <= st->rtol * st->rtol * st->bnorm2) {
 			st->done = 1;
 			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
@@ -900,18 +1047,41 @@ __global__ void __launch_bounds__(TPB) k_cg_replace(CgArgs<V> a) {
 }
 
 // ||b - A_res x||^2 in FP64
-template <typename V>
+template <int LPR, typename V>
 __global__ void __launch_bounds__(TPB) k_true_residual(CgArgs<V> a) {
 	double v[1] = {0.0};
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		double y0, y1;
-		spmv64_row(a, i, y0, y1);
-		double2 const bb = ld2(a.b, i);
-		double const e0 = bb.x - y0, e1 = bb.y - y1;
-		v[0] += e0 * e0 + e1 * e1;
+	FOR_ROWS(LPR) {
+		double e0, e1;
+		residual_row<LPR>(a, row_, sub_, e0, e1);
+		if (sub_ == 0) v[0] += e0 * e0 + e1 * e1;
 	}
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) a.st->true_res2 = out[0];
+}
+
+// kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner
+struct CgKernels {
+	void* spmv64;
+	void* spmvmx;
+	void* replace;
+	void* res64;
+	void* resmx;
+};
+
+template <int LPR>
+CgKernels kernels_for() {
+	return {(void*) k_cg64_spmv<LPR>, (void*) k_mx_spmv<LPR>, (void*) k_mx_replace<LPR>,
+	        (void*) k_true_residual<LPR, double>, (void*) k_true_residual<LPR, float>};
+}
+
+CgKernels kernels_lpr(int lpr) {
+	switch (lpr) {
+	case 1: return kernels_for<1>();
+	case 2: return kernels_for<2>();
+	case 4: return kernels_for<4>();
+	case 16: return kernels_for<16>();
+	default: return kernels_for<8>();
+	}
 }
 
 int g_num_sms = 0;
@@ -973,7 +1143,8 @@ struct bfm_gpu_problem {
 
 	// CG
 	double* x;
-	void *r, *p, *s, *w;  // double or float
+	void* vec[5];  // r, u, p, s, w (FP64 path) or r, -, p, pn, q (mixed path)
+	int lpr;       // lanes per block row of the SpMV kernels (autotuned)
 	double* partials;
 	unsigned* ticket;
 	CgState* st;
@@ -982,7 +1153,8 @@ struct bfm_gpu_problem {
 	int* err_host;     // pinned
 
 	cudaGraphExec_t graph;
-	int graph_precision, graph_precond;
+	int graph_precision, graph_precond, graph_lpr;
+	int tuned;
 	bfm_gpu_opts_t graph_opts;
 
 	cudaEvent_t ev[4];
@@ -1064,15 +1236,16 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		a.vals = P->vals32;
 		a.dinv = P->dinv32;
 		a.vals64 = P->precision == BFM_GPU_MIXED_EXACT ? P->vals64 : nullptr;
-		a.mixed = 1;
 	}
 	a.block_pc = P->precond == BFM_GPU_PC_BLOCK_JACOBI;
 	a.b = P->b;
 	a.x = P->x;
-	a.r = (V*) P->r;
-	a.p = (V*) P->p;
-	a.s = (V*) P->s;
-	a.w = (V*) P->w;
+	a.r = (V*) P->vec[0];
+	a.u = (V*) P->vec[1];
+	a.p = (V*) P->vec[2];
+	a.s = (V*) P->vec[3];
+	a.pn = (V*) P->vec[3];
+	a.w = (V*) P->vec[4];
 	a.partials = P->partials;
 	a.ticket = P->ticket;
 	a.st = P->st;
@@ -1084,59 +1257,152 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	return a;
 }
 
-template <typename V>
-int add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps, void* fn, int grid, CgArgs<V>* args) {
+int add_node(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, void* fn, int grid, void** params) {
 	cudaKernelNodeParams kp = {};
-	void* params[1] = {args};
 	kp.func = fn;
 	kp.gridDim = dim3(grid);
 	kp.blockDim = dim3(TPB);
 	kp.sharedMemBytes = 0;
 	kp.kernelParams = params;
-	CK(cudaGraphAddKernelNode(node, g, deps, ndeps, &kp));
+	CK(cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp));
 	return 0;
 }
 
-// init -> while(running){ spmv+dots ; update ; [mixed: if(replace){ FP64 residual }] } -> true residual
-template <typename V>
-int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
-	cudaGraph_t g;
-	CK(cudaGraphCreate(&g, 0));
-	CgArgs<V> a = cg_args<V>(P, o);
-	a.use_cond = 1;
-	CK(cudaGraphConditionalHandleCreate(&a.cond, g, 1u, cudaGraphCondAssignDefault));
-	cudaGraphNode_t n_init, n_cond, n_a, n_b, n_if, n_r, n_res;
-	// the body's if-handle is created once the body graph exists; the
-	// kernels of every node must carry it, so add the nodes afterwards
+int add_conditional(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, cudaGraphConditionalHandle h,
+                    cudaGraphConditionalNodeType type, cudaGraph_t* body) {
 	cudaGraphNodeParams cp = {};
 	cp.type = cudaGraphNodeTypeConditional;
-	cp.conditional.handle = a.cond;
-	cp.conditional.type = cudaGraphCondTypeWhile;
+	cp.conditional.handle = h;
+	cp.conditional.type = type;
 	cp.conditional.size = 1;
-	// init first (no dependency), then the while node after it
-	CgArgs<V> a0 = a;
-	if (add_kernel<V>(g, &n_init, nullptr, 0, (void*) k_cg_init<V>, P->grid, &a0)) return -1;
-	CK(cudaGraphAddNode(&n_cond, g, &n_init, nullptr, 1, &cp));
-	cudaGraph_t body = cp.conditional.phGraph_out[0];
-	cudaGraphNodeParams ip = {};
-	if (a.mixed) {
-		CK(cudaGraphConditionalHandleCreate(&a.cond_repl, body, 0u, cudaGraphCondAssignDefault));
-		ip.type = cudaGraphNodeTypeConditional;
-		ip.conditional.handle = a.cond_repl;
-		ip.conditional.type = cudaGraphCondTypeIf;
-		ip.conditional.size = 1;
+	CK(cudaGraphAddNode(node, g, dep, nullptr, dep ? 1 : 0, &cp));
+	*body = cp.conditional.phGraph_out[0];
+	return 0;
+}
+
+// FP64:  init -> while(running){ A ; B } -> true residual
+// mixed: init -> while(running){ K1 ; K2 ; if(replace){R} ; K1' ; K2' ; if(replace'){R'} } -> true residual
+//        (two iterations per body pass, so each node has fixed ping-pong direction buffers)
+int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
+	bool const mixed = P->precision != BFM_GPU_FP64;
+	CgKernels const K = kernels_lpr(P->lpr);
+	cudaGraph_t g, body;
+	CK(cudaGraphCreate(&g, 0));
+	cudaGraphConditionalHandle h;
+	CK(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
+	cudaGraphNode_t n_init, n_loop, n_res, prev = nullptr;
+	int imixed = mixed;
+	if (!mixed) {
+		CgArgs<double> a = cg_args<double>(P, o);
+		a.use_cond = 1;
+		a.cond = h;
+		void* pi[2] = {&a, &imixed};
+		void* pa[1] = {&a};
+		if (add_node(g, &n_init, nullptr, (void*) k_cg_init<double>, P->grid, pi)) return -1;
+		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
+		cudaGraphNode_t n_a, n_b;
+		if (add_node(body, &n_a, nullptr, K.spmv64, P->grid, pa)) return -1;
+		if (add_node(body, &n_b, &n_a, (void*) k_cg64_update, P->grid, pa)) return -1;
+		if (add_node(g, &n_res, &n_loop, K.res64, P->grid, pa)) return -1;
 	}
-	if (add_kernel<V>(body, &n_a, nullptr, 0, (void*) k_cg_spmv_dots<V>, P->grid, &a)) return -1;
-	if (add_kernel<V>(body, &n_b, &n_a, 1, (void*) k_cg_update<V>, P->grid, &a)) return -1;
-	if (a.mixed) {
-		CK(cudaGraphAddNode(&n_if, body, &n_b, nullptr, 1, &ip));
-		if (add_kernel<V>(ip.conditional.phGraph_out[0], &n_r, nullptr, 0, (void*) k_cg_replace<V>, P->grid, &a)) return -1;
+	else {
+		CgArgs<float> a[2];
+		a[0] = cg_args<float>(P, o);
+		a[0].use_cond = 1;
+		a[0].cond = h;
+		a[1] = a[0];
+		a[1].p = a[0].pn;
+		a[1].pn = a[0].p;
+		void* pi[2] = {&a[0], &imixed};
+		if (add_node(g, &n_init, nullptr, (void*) k_cg_init<float>, P->grid, pi)) return -1;
+		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
+		for (int half = 0; half < 2; half++) {
+			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
+			void* pa[1] = {&a[half]};
+			cudaGraphNode_t n1, n2, nif, nr;
+			cudaGraph_t ifbody;
+			if (add_node(body, &n1, prev ? &prev : nullptr, K.spmvmx, P->grid, pa)) return -1;
+			if (add_node(body, &n2, &n1, (void*) k_mx_update, P->grid, pa)) return -1;
+			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
+			if (add_node(ifbody, &nr, nullptr, K.replace, P->grid, pa)) return -1;
+			prev = nif;
+		}
+		void* pa[1] = {&a[0]};
+		if (add_node(g, &n_res, &n_loop, K.resmx, P->grid, pa)) return -1;
 	}
-	if (add_kernel<V>(g, &n_res, &n_cond, 1, (void*) k_true_residual<V>, P->grid, &a)) return -1;
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	P->graph = nullptr;
 	CK(cudaGraphInstantiate(&P->graph, g, 0));
 	cudaGraphDestroy(g);
+	return 0;
+}
+
+// Mean duration (ms) of the two per-iteration kernels with `lpr` lanes per
+// row, launched standalone on a scratch solver state.  Overwrites the Krylov
+// vectors.
+int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, double* ms_update) {
+	CgState* scratch = nullptr;
+	if (dalloc(&scratch, 1)) return -1;
+	CgKernels const K = kernels_lpr(lpr);
+	cudaEvent_t e[3];
+	for (auto& x : e) cudaEventCreate(&x);
+	int const grid = P->grid;
+	cudaStream_t const st = P->stream;
+	if (P->precision == BFM_GPU_FP64) {
+		CgArgs<double> a = cg_args<double>(P, nullptr);
+		a.opts.rtol = 0.0;
+		a.opts.max_iters = 1 << 30;
+		a.st = scratch;
+		a.timing = 1;
+		k_cg_init<double><<<grid, TPB, 0, st>>>(a, 0);
+		void* pa[1] = {&a};
+		cudaEventRecord(e[0], st);
+		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.spmv64, dim3(grid), dim3(TPB), pa, 0, st);
+		cudaEventRecord(e[1], st);
+		for (int i = 0; i < reps; i++) k_cg64_update<<<grid, TPB, 0, st>>>(a);
+		cudaEventRecord(e[2], st);
+	}
+	else {
+		CgArgs<float> a = cg_args<float>(P, nullptr);
+		a.opts.rtol = 0.0;
+		a.opts.max_iters = 1 << 30;
+		a.st = scratch;
+		a.timing = 1;
+		k_cg_init<float><<<grid, TPB, 0, st>>>(a, 1);
+		void* pa[1] = {&a};
+		cudaEventRecord(e[0], st);
+		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.spmvmx, dim3(grid), dim3(TPB), pa, 0, st);
+		cudaEventRecord(e[1], st);
+		for (int i = 0; i < reps; i++) k_mx_update<<<grid, TPB, 0, st>>>(a);
+		cudaEventRecord(e[2], st);
+	}
+	cudaError_t const err = cudaStreamSynchronize(st);
+	float t1 = 0, t2 = 0;
+	cudaEventElapsedTime(&t1, e[0], e[1]);
+	cudaEventElapsedTime(&t2, e[1], e[2]);
+	for (auto& x : e) cudaEventDestroy(x);
+	cudaFree(scratch);
+	CK(err);
+	*ms_spmv = t1 / reps;
+	*ms_update = t2 / reps;
+	return 0;
+}
+
+// Project autotuner: time the SpMV kernel with 2, 4, 8 and 16 lanes per
+// block row on this problem's matrix and keep the fastest.
+int autotune_lpr(bfm_gpu_problem* P) {
+	int const cands[] = {2, 4, 8, 16};
+	double best = 1e30;
+	int best_lpr = 8;
+	for (int lpr : cands) {
+		double t_spmv = 0, t_upd = 0;
+		if (time_iteration(P, lpr, 5, &t_spmv, &t_upd)) return -1;
+		if (t_spmv < best) {
+			best = t_spmv;
+			best_lpr = lpr;
+		}
+	}
+	P->lpr = best_lpr;
 	return 0;
 }
 
@@ -1162,6 +1428,7 @@ void bfm_gpu_default_opts(bfm_gpu_opts_t* o) {
 	o->max_iters = 200000;
 	o->replace_drop = 1e-2;
 	o->deterministic = 1;
+	o->autotune = 1;
 }
 
 int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n_elems, int n_edges, int n_conds, void* stream) {
@@ -1181,6 +1448,7 @@ int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n
 	P->max_conds = n_conds;
 	P->precision = -1;
 	P->graph_precision = -1;
+	P->lpr = 8;
 	if (stream) {
 		P->stream = (cudaStream_t) stream;
 		P->own_stream = false;
@@ -1230,7 +1498,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->r, P->p, P->s, P->w,
+	                P->vals32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1348,12 +1616,11 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (!want32 && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
 	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 4 * N)) return -1;
 	size_t const vsz = precision == BFM_GPU_FP64 ? sizeof(double) : sizeof(float);
-	if ((P->precision == BFM_GPU_FP64) != (precision == BFM_GPU_FP64) || !P->r) {
-		void** vecs[] = {&P->r, &P->p, &P->s, &P->w};
-		for (void** v : vecs) {
-			if (*v) cudaFree(*v);
-			*v = nullptr;
-			CK(cudaMalloc(v, 2 * (N ? N : 1) * vsz));
+	if ((P->precision == BFM_GPU_FP64) != (precision == BFM_GPU_FP64) || !P->vec[0]) {
+		for (void*& v : P->vec) {
+			if (v) cudaFree(v);
+			v = nullptr;
+			CK(cudaMalloc(&v, 2 * (N ? N : 1) * vsz));
 		}
 	}
 	P->precision = precision;
@@ -1447,15 +1714,20 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		P->precond = o.precond;
 		if (bfm_gpu_problem_assemble(P, P->precision)) return -1;
 	}
+	if (o.autotune && !P->tuned) {
+		if (autotune_lpr(P)) return -1;
+		P->tuned = 1;
+		P->graph_lpr = -1;
+	}
 	// options are baked into the graph's kernel parameters: rebuild only when they change
 	bool const same = P->graph && P->graph_precision == P->precision && P->graph_precond == P->precond &&
-	                  P->graph_opts.rtol == o.rtol && P->graph_opts.max_iters == o.max_iters &&
-	                  P->graph_opts.replace_drop == o.replace_drop;
+	                  P->graph_lpr == P->lpr && P->graph_opts.rtol == o.rtol &&
+	                  P->graph_opts.max_iters == o.max_iters && P->graph_opts.replace_drop == o.replace_drop;
 	if (!same) {
-		int const rc = P->precision == BFM_GPU_FP64 ? build_graph<double>(P, &o) : build_graph<float>(P, &o);
-		if (rc) return -1;
+		if (build_graph(P, &o)) return -1;
 		P->graph_precision = P->precision;
 		P->graph_precond = P->precond;
+		P->graph_lpr = P->lpr;
 		P->graph_opts = o;
 	}
 	CK(cudaEventRecord(P->ev[2], P->stream));
@@ -1541,53 +1813,15 @@ int bfm_gpu_problem_download(bfm_gpu_problem_t* P, int32_t* row_ptr, int32_t* co
 int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv, double* ms_update) {
 	g_err[0] = 0;
 	if (!P->assembled) return fail("assemble first");
-	CgState* scratch = nullptr;
-	if (dalloc(&scratch, 1)) return -1;
-	CgState h;
-	memset(&h, 0, sizeof h);
-	h.rtol = 0.0;
-	h.max_iters = 1 << 30;
-	h.bnorm2 = 1.0;
-	CK(cudaMemcpyAsync(scratch, &h, sizeof h, cudaMemcpyHostToDevice, P->stream));
-	cudaEvent_t e[3];
-	for (auto& x : e) cudaEventCreate(&x);
-	float t1 = 0, t2 = 0;
-	if (P->precision == BFM_GPU_FP64) {
-		CgArgs<double> a = cg_args<double>(P, nullptr);
-		a.opts.rtol = 0.0;
-		a.opts.max_iters = 1 << 30;
-		a.st = scratch;
-		a.timing = 1;
-		k_cg_init<double><<<P->grid, TPB, 0, P->stream>>>(a);
-		cudaMemcpyAsync(scratch, &h, sizeof h, cudaMemcpyHostToDevice, P->stream);
-		cudaEventRecord(e[0], P->stream);
-		for (int i = 0; i < reps; i++) k_cg_spmv_dots<double><<<P->grid, TPB, 0, P->stream>>>(a);
-		cudaEventRecord(e[1], P->stream);
-		for (int i = 0; i < reps; i++) k_cg_update<double><<<P->grid, TPB, 0, P->stream>>>(a);
-		cudaEventRecord(e[2], P->stream);
-	}
-	else {
-		CgArgs<float> a = cg_args<float>(P, nullptr);
-		a.opts.rtol = 0.0;
-		a.opts.max_iters = 1 << 30;
-		a.st = scratch;
-		a.timing = 1;
-		k_cg_init<float><<<P->grid, TPB, 0, P->stream>>>(a);
-		cudaMemcpyAsync(scratch, &h, sizeof h, cudaMemcpyHostToDevice, P->stream);
-		cudaEventRecord(e[0], P->stream);
-		for (int i = 0; i < reps; i++) k_cg_spmv_dots<float><<<P->grid, TPB, 0, P->stream>>>(a);
-		cudaEventRecord(e[1], P->stream);
-		for (int i = 0; i < reps; i++) k_cg_update<float><<<P->grid, TPB, 0, P->stream>>>(a);
-		cudaEventRecord(e[2], P->stream);
-	}
-	cudaError_t const err = cudaStreamSynchronize(P->stream);
-	cudaEventElapsedTime(&t1, e[0], e[1]);
-	cudaEventElapsedTime(&t2, e[1], e[2]);
-	for (auto& x : e) cudaEventDestroy(x);
-	cudaFree(scratch);
-	CK(err);
-	*ms_spmv = t1 / reps;
-	*ms_update = t2 / reps;
+	return time_iteration(P, P->lpr, reps > 0 ? reps : 1, ms_spmv, ms_update);
+}
+
+int bfm_gpu_problem_autotune(bfm_gpu_problem_t* P, int* lanes_per_row) {
+	g_err[0] = 0;
+	if (!P->assembled) return fail("assemble first");
+	if (autotune_lpr(P)) return -1;
+	P->tuned = 1;
+	if (lanes_per_row) *lanes_per_row = P->lpr;
 	return 0;
 }
 

@@ -66,6 +66,8 @@ typedef struct {
 	double replace_drop; /* mixed: replace the recurrence residual by the FP64
 	                        true residual each time it has dropped by this factor */
 	int deterministic; /* 1: fixed reduction order (always on; kept for ABI)    */
+	int autotune;      /* 1: pick the SpMV shape (lanes per block row) by timing
+	                      the candidates on the problem's own matrix, once    */
 } bfm_gpu_opts_t;
 
 typedef struct {
@@ -80,7 +82,7 @@ typedef struct {
 	double ms_solve;      /* CG (device)                                   */
 } bfm_gpu_stats_t;
 
-/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 1e-2. */
+/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 1e-2, autotune on. */
 void bfm_gpu_default_opts(bfm_gpu_opts_t* opts);
 
 /* Options used by bfm_sim_run and the bfm_system_* creators of this thread. */
@@ -166,6 +168,11 @@ int bfm_gpu_problem_download(bfm_gpu_problem_t* problem, int32_t* row_ptr, int32
  * kernel `reps` times each on the problem's stream and return their mean
  * durations (ms, CUDA events).  Overwrites the Krylov vectors. */
 int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* problem, int reps, double* ms_spmv, double* ms_update);
+
+/* Project autotuner: time the SpMV with 2, 4, 8 and 16 lanes per block row
+ * on the assembled matrix and keep the fastest for this problem's solves.
+ * Overwrites the Krylov vectors. */
+int bfm_gpu_problem_autotune(bfm_gpu_problem_t* problem, int* lanes_per_row);
 
 /* The CUDA stream the problem's work is enqueued on (cudaStream_t as void*). */
 void* bfm_gpu_problem_stream(bfm_gpu_problem_t* problem);
