@@ -282,6 +282,7 @@ struct AsmArgs {
 	const double* last;
 	double* vals64;
 	float* vals32;
+	float* corr32;   // per node: 2x2 block of the row sums of (FP64 value - FP32 value)
 	double* b;
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
@@ -459,10 +460,27 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 		}
 	}
 
+	// FP32 integration: rebuild the diagonal block from the off-diagonal ones
+	// (FP64 sum), so every block row sums to zero as it does exactly: FP32
+	// rounding must not break the translation modes, or the FP32 operator
+	// stops being positive definite on ill-conditioned meshes.
+	int sd = -1;
+	for (int s = 0; s < len; s++)
+		if (col[s] == r) sd = s;
+	double dfix[4] = {0, 0, 0, 0};
+	if constexpr (!EXACT) {
+		if (sd >= 0 && is < ie) {
+			for (int s = 0; s < len; s++)
+				if (s != sd)
+					for (int k = 0; k < 4; k++) dfix[k] -= (double) acc[s][k];
+			for (int k = 0; k < 4; k++) acc[sd][k] = (T) dfix[k];
+		}
+	}
 	// symmetric Dirichlet elimination of this row
 	int const r0 = 2 * r, r1 = 2 * r + 1;
 	bool const c0 = a.last_ci[r0] >= 0, c1 = a.last_ci[r1] >= 0;
 	double k00 = 0, k01 = 0, k10 = 0, k11 = 0;
+	double corr[4] = {0, 0, 0, 0};  // FP64 row sums of what the FP32 copy loses
 	for (int s = 0; s < len; s++) {
 		int const c = col[s];
 		int const d0 = 2 * c, d1 = 2 * c + 1;
@@ -478,24 +496,34 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				if (e1) b1 -= f1 * (double) acc[s][3];
 			}
 		}
-		T v[4] = {acc[s][0], acc[s][1], acc[s][2], acc[s][3]};
-		if (c0 || e0) v[0] = (r0 == d0) ? T(1) : T(0);
-		if (c0 || e1) v[1] = T(0);
-		if (c1 || e0) v[2] = T(0);
-		if (c1 || e1) v[3] = (r1 == d1) ? T(1) : T(0);
+		double v[4] = {(double) acc[s][0], (double) acc[s][1], (double) acc[s][2], (double) acc[s][3]};
+		if (s == sd && !EXACT) {
+			v[0] = dfix[0]; v[1] = dfix[1]; v[2] = dfix[2]; v[3] = dfix[3];
+		}
+		if (c0 || e0) v[0] = (r0 == d0) ? 1.0 : 0.0;
+		if (c0 || e1) v[1] = 0.0;
+		if (c1 || e0) v[2] = 0.0;
+		if (c1 || e1) v[3] = (r1 == d1) ? 1.0 : 0.0;
 		long const o = 4l * (rs + s);
 		if (a.vals64) {
-			a.vals64[o + 0] = (double) v[0]; a.vals64[o + 1] = (double) v[1];
-			a.vals64[o + 2] = (double) v[2]; a.vals64[o + 3] = (double) v[3];
+			a.vals64[o + 0] = v[0]; a.vals64[o + 1] = v[1];
+			a.vals64[o + 2] = v[2]; a.vals64[o + 3] = v[3];
 		}
 		if (a.vals32) {
-			a.vals32[o + 0] = (float) v[0]; a.vals32[o + 1] = (float) v[1];
-			a.vals32[o + 2] = (float) v[2]; a.vals32[o + 3] = (float) v[3];
+			for (int k = 0; k < 4; k++) {
+				float const f = (float) v[k];
+				a.vals32[o + k] = f;
+				corr[k] += v[k] - (double) f;
+			}
 		}
 		if (c == r) {
-			k00 = (double) v[0]; k01 = (double) v[1];
-			k10 = (double) v[2]; k11 = (double) v[3];
+			k00 = v[0]; k01 = v[1];
+			k10 = v[2]; k11 = v[3];
 		}
+	}
+	if (a.corr32) {
+		a.corr32[4 * r + 0] = (float) corr[0]; a.corr32[4 * r + 1] = (float) corr[1];
+		a.corr32[4 * r + 2] = (float) corr[2]; a.corr32[4 * r + 3] = (float) corr[3];
 	}
 	if (c0) b0 = a.last[r0];
 	if (c1) b1 = a.last[r1];
@@ -651,11 +679,12 @@ struct CgArgs {
 	const V* vals;          // iteration operator (2x2 blocks)
 	const double* vals64;   // FP64 operator for true residuals (nullptr: `vals` widened)
 	const V* dinv;          // Jacobi: 2 per node; block Jacobi: 4 per node
+	const float* corr;      // mixed: per-node 2x2 row-sum correction of the FP32 operator
 	int block_pc;
 	const double* b;
 	double* x;
 	V* r;
-	V* u;   // FP64 path: u = M r (materialized); mixed path: unused
+	V* u;   // FP64 path: u = M r (materialized); mixed path: dx, the grouped solution update
 	V* p;   // FP64 path: direction; mixed path: direction read this iteration
 	V* pn;  // mixed path: direction written this iteration (ping-pong with p)
 	V* s;   // FP64 path: s = A p by recurrence
@@ -761,6 +790,9 @@ __global__ void __launch_bounds__(TPB) k_cg_init(CgArgs<V> a, int mixed) {
 		if (!mixed) {
 			st2(a.u, i, u0, u1);
 			st2(a.s, i, (V) 0, (V) 0);
+		}
+		else {
+			st2(a.u, i, (V) 0, (V) 0);
 		}
 		v[0] += bb.x * bb.x + bb.y * bb.y;
 		v[1] += (double) r0 * (double) u0 + (double) r1 * (double) u1;
@@ -880,15 +912,39 @@ __global__ void __launch_bounds__(TPB) k_cg64_update(CgArgs<double> a) {
 }
 
 // ---------------------------------------------------------------- mixed path
-// Hestenes-Stiefel PCG in FP32 with FP64 inner products and FP64 solution.
-// The direction update is fused into the SpMV: a neighbour's new direction
-// M r + beta p_old is formed where it is gathered (FP32 arithmetic is cheap),
-// the row's own one is stored in the other buffer of a ping-pong pair.
-//   K1: p' = M r + beta p; q = A p'; alpha = gamma / (p', q)
-//   K2: x += alpha p' (FP64); r -= alpha q; gamma' = (r, M r), rho = (r,r); beta
-//   R (only when requested): r = b - A64 x in FP64; gamma = (r, M r)
-// Stable under residual replacement (unlike the single-reduction variant,
-// whose alpha assumes orthogonality that replacement breaks).
+// Hestenes-Stiefel PCG with an FP32 operator, FP32 Krylov vectors and FP64
+// only where accuracy needs it.  GB300 issues FP64 at a small fraction of its
+// FP32 rate, so the iteration does no per-entry FP64 arithmetic at all:
+//   - inner products accumulate in double-float pairs (error-free FP32
+//     transformations, about 48 significant bits) and become FP64 once per
+//     thread;
+//   - the solution update is grouped: dx += alpha p' in FP32, flushed into the
+//     FP64 x only before each FP64 residual replacement and at the end;
+//   - the FP32 operator keeps the FP64 matrix's block row sums through a
+//     per-node 2x2 correction block, so rounding does not break the rigid
+//     translation modes (without it the FP32 operator loses definiteness on
+//     ill-conditioned meshes and CG diverges).
+//   K1: p' = M r + beta p; q = (A32 + C) p'; alpha = gamma / (p', q)
+//   K2: dx += alpha p'; r -= alpha q; gamma' = (r, M r), rho = (r, r); beta
+//   on request (IF node): x += dx, dx = 0; r = b - A64 x in FP64; gamma = (r, M r)
+
+struct DF {
+	float hi, lo;
+};
+
+// s += a*b without rounding loss (TwoProduct via FMA, TwoSum); the _rn
+// intrinsics keep the compiler from contracting or reassociating
+__device__ __forceinline__ void df_add_prod(DF& s, float a, float b) {
+	float const p = __fmul_rn(a, b);
+	float const e = __fmaf_rn(a, b, -p);
+	float const t = __fadd_rn(s.hi, p);
+	float const z = __fsub_rn(t, s.hi);
+	float const err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, z)), __fsub_rn(p, z));
+	s.hi = t;
+	s.lo = __fadd_rn(s.lo, __fadd_rn(err, e));
+}
+
+__device__ __forceinline__ double df_value(DF const& s) { return (double) s.hi + (double) s.lo; }
 
 template <int LPR>
 __global__ void __launch_bounds__(TPB) k_mx_spmv(CgArgs<float> a) {
@@ -910,7 +966,7 @@ __global__ void __launch_bounds__(TPB) k_mx_spmv(CgArgs<float> a) {
 		g0 = z0 + beta * pc.x;
 		g1 = z1 + beta * pc.y;
 	};
-	double v[1] = {0.0};
+	DF pq = {0.f, 0.f};
 	FOR_ROWS(LPR) {
 		bool const ok = row_ < a.N;
 		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
@@ -919,22 +975,27 @@ __global__ void __launch_bounds__(TPB) k_mx_spmv(CgArgs<float> a) {
 		if (ok && sub_ == 0) {
 			float g0, g1;
 			gather(row_, g0, g1);
+			float4 const cc = reinterpret_cast<const float4*>(a.corr)[row_];
+			y0 += cc.x * g0 + cc.y * g1;
+			y1 += cc.z * g0 + cc.w * g1;
 			st2(a.pn, row_, g0, g1);
 			st2(a.w, row_, y0, y1);
-			v[0] += (double) g0 * (double) y0 + (double) g1 * (double) y1;
+			df_add_prod(pq, g0, y0);
+			df_add_prod(pq, g1, y1);
 		}
 	}
+	double v[1] = {df_value(pq)};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		double const pq = out[0];
-		if (!(pq > 0.0)) {
+		double const d = out[0];
+		if (!(d > 0.0)) {
 			if (!a.timing) {
 				st->done = 1;
 				st->status = BFM_GPU_BREAKDOWN;
 			}
 			return;  // the while condition stays cleared
 		}
-		st->alpha = st->gamma / pq;
+		st->alpha = st->gamma / d;
 		if (a.use_cond) cudaGraphSetConditional(a.cond, 1u);
 	}
 }
@@ -942,20 +1003,21 @@ __global__ void __launch_bounds__(TPB) k_mx_spmv(CgArgs<float> a) {
 __global__ void __launch_bounds__(TPB) k_mx_update(CgArgs<float> a) {
 	CgState* st = a.st;
 	if (st->done && !a.timing) return;
-	double const alpha64 = st->alpha;
-	float const alpha = (float) alpha64;
-	double v[2] = {0.0, 0.0};  // gamma' = (r, M r), rho = (r, r)
+	float const alpha = (float) st->alpha;
+	DF g = {0.f, 0.f}, rr = {0.f, 0.f};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		float2 const pn = ld2(a.pn, i), q = ld2(a.w, i), r = ld2(a.r, i);
-		double2 const x = ld2(a.x, i);
-		st2(a.x, i, x.x + alpha64 * (double) pn.x, x.y + alpha64 * (double) pn.y);
+		float2 const pn = ld2(a.pn, i), q = ld2(a.w, i), r = ld2(a.r, i), dx = ld2(a.u, i);
+		st2(a.u, i, dx.x + alpha * pn.x, dx.y + alpha * pn.y);
 		float const r0 = r.x - alpha * q.x, r1 = r.y - alpha * q.y;
 		st2(a.r, i, r0, r1);
 		float z0, z1;
 		precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
-		v[0] += (double) r0 * (double) z0 + (double) r1 * (double) z1;
-		v[1] += (double) r0 * (double) r0 + (double) r1 * (double) r1;
+		df_add_prod(g, r0, z0);
+		df_add_prod(g, r1, z1);
+		df_add_prod(rr, r0, r0);
+		df_add_prod(rr, r1, r1);
 	}
+	double v[2] = {df_value(g), df_value(rr)};
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		if (a.timing) return;
@@ -993,8 +1055,20 @@ __global__ void __launch_bounds__(TPB) k_mx_update(CgArgs<float> a) {
 	}
 }
 
-// y = A_res x in FP64, LPR lanes per row; the residual operator is the FP64
-// matrix when present, else the iteration matrix widened
+// x += dx (FP64), dx = 0
+__global__ void __launch_bounds__(TPB) k_mx_flush(CgArgs<float> a) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		float2 const dx = ld2(a.u, i);
+		if (dx.x == 0.f && dx.y == 0.f) continue;
+		double2 const x = ld2(a.x, i);
+		st2(a.x, i, x.x + (double) dx.x, x.y + (double) dx.y);
+		st2(a.u, i, 0.f, 0.f);
+	}
+}
+
+// y = A_res x in FP64, LPR lanes per row.  The residual operator is the FP64
+// matrix when present, else the iteration matrix widened plus its
+// correction blocks.
 template <int LPR, typename V>
 __device__ __forceinline__ void residual_row(const CgArgs<V>& a, int row, int sub, double& e0, double& e1) {
 	bool const ok = row < a.N;
@@ -1010,6 +1084,12 @@ __device__ __forceinline__ void residual_row(const CgArgs<V>& a, int row, int su
 	else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, gather, y0, y1);
 	e0 = e1 = 0.0;
 	if (ok) {
+		if (!a.vals64 && a.corr) {
+			float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
+			double2 const xi = ld2(x, row);
+			y0 += (double) cc.x * xi.x + (double) cc.y * xi.y;
+			y1 += (double) cc.z * xi.x + (double) cc.w * xi.y;
+		}
 		double2 const bb = ld2(a.b, row);
 		e0 = bb.x - y0;
 		e1 = bb.y - y1;
@@ -1134,6 +1214,7 @@ struct bfm_gpu_problem {
 	// system
 	double* vals64;
 	float* vals32;
+	float* corr32;  // mixed: per-node 2x2 row-sum correction of the FP32 operator
 	double* b;
 	int* last_ci;
 	double *first, *last;
@@ -1235,6 +1316,7 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	else {
 		a.vals = P->vals32;
 		a.dinv = P->dinv32;
+		a.corr = P->corr32;
 		a.vals64 = P->precision == BFM_GPU_MIXED_EXACT ? P->vals64 : nullptr;
 	}
 	a.block_pc = P->precond == BFM_GPU_PC_BLOCK_JACOBI;
@@ -1324,11 +1406,15 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			if (add_node(body, &n1, prev ? &prev : nullptr, K.spmvmx, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_mx_update, P->grid, pa)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
-			if (add_node(ifbody, &nr, nullptr, K.replace, P->grid, pa)) return -1;
+			cudaGraphNode_t nf;
+			if (add_node(ifbody, &nf, nullptr, (void*) k_mx_flush, P->grid, pa)) return -1;
+			if (add_node(ifbody, &nr, &nf, K.replace, P->grid, pa)) return -1;
 			prev = nif;
 		}
 		void* pa[1] = {&a[0]};
-		if (add_node(g, &n_res, &n_loop, K.resmx, P->grid, pa)) return -1;
+		cudaGraphNode_t n_flush;
+		if (add_node(g, &n_flush, &n_loop, (void*) k_mx_flush, P->grid, pa)) return -1;
+		if (add_node(g, &n_res, &n_flush, K.resmx, P->grid, pa)) return -1;
 	}
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	P->graph = nullptr;
@@ -1388,10 +1474,10 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 	return 0;
 }
 
-// Project autotuner: time the SpMV kernel with 2, 4, 8 and 16 lanes per
+// Project autotuner: time the SpMV kernel with 1, 2, 4, 8 and 16 lanes per
 // block row on this problem's matrix and keep the fastest.
 int autotune_lpr(bfm_gpu_problem* P) {
-	int const cands[] = {2, 4, 8, 16};
+	int const cands[] = {1, 2, 4, 8, 16};
 	double best = 1e30;
 	int best_lpr = 8;
 	for (int lpr : cands) {
@@ -1426,7 +1512,7 @@ void bfm_gpu_default_opts(bfm_gpu_opts_t* o) {
 	o->precond = BFM_GPU_PC_JACOBI;
 	o->rtol = 1e-10;
 	o->max_iters = 200000;
-	o->replace_drop = 1e-2;
+	o->replace_drop = 1e-1;
 	o->deterministic = 1;
 	o->autotune = 1;
 }
@@ -1498,7 +1584,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4],
+	                P->vals32, P->corr32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1615,6 +1701,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (want32 && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
 	if (!want32 && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
 	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 4 * N)) return -1;
+	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
 	size_t const vsz = precision == BFM_GPU_FP64 ? sizeof(double) : sizeof(float);
 	if ((P->precision == BFM_GPU_FP64) != (precision == BFM_GPU_FP64) || !P->vec[0]) {
 		for (void*& v : P->vec) {
@@ -1664,6 +1751,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.last = P->last;
 	a.vals64 = want64 ? P->vals64 : nullptr;
 	a.vals32 = want32 ? P->vals32 : nullptr;
+	a.corr32 = want32 ? P->corr32 : nullptr;
 	a.b = P->b;
 	a.dinv64 = want32 ? nullptr : P->dinv64;
 	a.dinv32 = want32 ? P->dinv32 : nullptr;

@@ -34,9 +34,9 @@ enum { BFM_GPU_HOST = 0, BFM_GPU_DEVICE = 1 };
 /* arithmetic of the stiffness matrix and Krylov vectors */
 enum {
 	BFM_GPU_FP64 = 0,  /* FP64 element integration (reference operation order), FP64 CG          */
-	BFM_GPU_MIXED = 1, /* FP32 element integration and SpMV, FP32 Krylov vectors; FP64 inner
-	                      products, FP64 solution and FP64 residual replacement (with the FP32
-	                      stiffness widened): converges to the FP32-integrated system             */
+	BFM_GPU_MIXED = 1, /* FP32 element integration and SpMV, FP32 Krylov vectors; FP64-accurate
+	                      inner products, FP64 solution and FP64 residual replacement with the
+	                      FP32 operator widened: converges to the FP32-integrated system         */
 	BFM_GPU_MIXED_EXACT = 2, /* as MIXED, but the element loop runs in FP64 once: the FP64 matrix is
 	                            the residual operator (solution of the FP64 system) and its FP32
 	                            rounding the iteration operator                                    */
@@ -82,7 +82,7 @@ typedef struct {
 	double ms_solve;      /* CG (device)                                   */
 } bfm_gpu_stats_t;
 
-/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 1e-2, autotune on. */
+/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 0.1, autotune on. */
 void bfm_gpu_default_opts(bfm_gpu_opts_t* opts);
 
 /* Options used by bfm_sim_run and the bfm_system_* creators of this thread. */
@@ -169,7 +169,7 @@ int bfm_gpu_problem_download(bfm_gpu_problem_t* problem, int32_t* row_ptr, int32
  * durations (ms, CUDA events).  Overwrites the Krylov vectors. */
 int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* problem, int reps, double* ms_spmv, double* ms_update);
 
-/* Project autotuner: time the SpMV with 2, 4, 8 and 16 lanes per block row
+/* Project autotuner: time the SpMV with 1, 2, 4, 8 and 16 lanes per block row
  * on the assembled matrix and keep the fastest for this problem's solves.
  * Overwrites the Krylov vectors. */
 int bfm_gpu_problem_autotune(bfm_gpu_problem_t* problem, int* lanes_per_row);
