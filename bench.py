@@ -241,11 +241,14 @@ def profile(args):
     assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
     s = bfm_gb300.bfm_gpu_stats_t()
     assert lib.bfm_gpu_problem_stats(P, C.byref(s)) == 0
+    lpr = C.c_int(0)
+    assert lib.bfm_gpu_problem_autotune(P, C.byref(lpr)) == 0, bfm_gb300.last_error()
     t_spmv, t_upd = C.c_double(), C.c_double()
     assert lib.bfm_gpu_problem_time_kernels(P, args.reps, C.byref(t_spmv), C.byref(t_upd)) == 0
     lib.bfm_gpu_problem_destroy(P)
     nbytes = algorithmic_bytes_spmv(s.n_blocks, p.n_nodes, prec)
-    return {"workload": p.name, "method": args.method, "n_blocks": s.n_blocks, "ms_assemble": s.ms_assemble,
+    return {"workload": p.name, "method": args.method, "lanes_per_row": lpr.value, "n_blocks": s.n_blocks,
+            "ms_assemble": s.ms_assemble,
             "spmv_ms": t_spmv.value, "update_ms": t_upd.value, "spmv_algorithmic_bytes": nbytes,
             "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9}
 
