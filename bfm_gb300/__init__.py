@@ -63,6 +63,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_stream": (_vp, [_vp]),
     "bfm_gpu_problem_time_kernels": (_i, [_vp, _i, _P(_d), _P(_d)]),
     "bfm_gpu_problem_autotune": (_i, [_vp, _P(_i)]),
+    "bfm_gpu_pcg_solve_noalloc": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _i, _P(_i), _P(_d), _vp]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
 }
 

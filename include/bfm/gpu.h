@@ -177,6 +177,27 @@ int bfm_gpu_problem_autotune(bfm_gpu_problem_t* problem, int* lanes_per_row);
 /* The CUDA stream the problem's work is enqueued on (cudaStream_t as void*). */
 void* bfm_gpu_problem_stream(bfm_gpu_problem_t* problem);
 
+/* ---------------------------------------------------------------- allocation-free solve */
+
+/* No counterpart in the reference: an additive entry point for callers that
+ * cannot allocate device memory (an application that owns every device byte
+ * through its own pool, or code that must not call cudaMalloc).  Solves
+ * A x = b by FP64 Jacobi-PCG, the method of bfm_gpu_problem_solve, with A a
+ * 2x2-block CSR matrix already in device memory: row_ptr[n_nodes+1],
+ * cols[row_ptr[n_nodes]], vals[4*row_ptr[n_nodes]] (the layout
+ * bfm_gpu_problem_download returns), b and x interleaved u,v, all device
+ * pointers; x is written.  Nothing is allocated: the Krylov vectors and
+ * solver state live in a fixed scratch array of about 6.4 MB that the library
+ * keeps on every GPU that loads it, which limits n_nodes to 65,536
+ * (131,072 DOF); larger sizes return -1 with a message.  The first call on a
+ * device looks up that array's device address; make this first call before
+ * any stream capture.  Calls share the array, so calls that overlap on the GPU
+ * (two streams, two threads) race: serialize them.  Reports the iteration
+ * count and the FP64 relative residual; returns -1 if CG does not converge. */
+int bfm_gpu_pcg_solve_noalloc(int n_nodes, const int32_t* row_ptr, const int32_t* cols, const double* vals,
+                              const double* b, double* x, double rtol, int max_iters, int* iterations,
+                              double* rel_residual, void* stream);
+
 /* ---------------------------------------------------------------- sparse RCM */
 
 /* Reverse Cuthill-McKee of a scalar CSR matrix (columns ascending per row),
