@@ -64,6 +64,10 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_time_kernels": (_i, [_vp, _i, _P(_d), _P(_d)]),
     "bfm_gpu_problem_autotune": (_i, [_vp, _P(_i)]),
     "bfm_gpu_pcg_solve_noalloc": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _i, _P(_i), _P(_d), _vp]),
+    "bfm_gpu_problem_set_edge_loads": (_i, [_vp, _i, _vp, _vp, _i]),
+    "bfm_gpu_problem_set_parts": (_i, [_vp, _i, _vp]),
+    "bfm_gpu_problem_solve_parts": (_i, [_vp, _P(bfm_gpu_opts_t)]),
+    "bfm_gpu_problem_part_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _P(_i), _P(_i), _P(_d)]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
 }
 

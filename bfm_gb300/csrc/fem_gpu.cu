@@ -290,6 +290,7 @@ struct AsmArgs {
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
 	int precond;
+	int skip_upto;  // rows of at most this many blocks are another kernel's
 	int* err;
 };
 
@@ -331,6 +332,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 	int const kind = a.kind;
 	int const rs = a.row_ptr[r], len = a.row_ptr[r + 1] - rs;
 	if (len > MAXR) return;  // already flagged by the pattern kernels
+	if (len <= a.skip_upto) return;
 
 	int col[MAXR];
 	T acc[MAXR][4];
@@ -535,6 +537,213 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 	store_precond(a, r, k00, k01, k10, k11);
 }
 
+// FP32 element integration, fast form (BFM_GPU_MIXED): one thread per node
+// row as above (owner computes, no atomics), but with the row's accumulators
+// in registers -- rows of up to RMAX blocks, with the block index resolved by
+// fully unrolled predicated adds -- each element's contribution summed over
+// the integration points before it is added, and the block's output rows
+// staged in shared memory so the contiguous span of values is written with
+// coalesced 16-byte stores.  Rows longer than RMAX are left to k_assemble<false>.
+template <int RMAX>
+__global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
+	__shared__ float4 stage[128 * RMAX];
+	__shared__ int first_rs, long_rows;
+	int const r = blockIdx.x * blockDim.x + threadIdx.x;
+	bool const valid = r < a.N;
+	int const rs = valid ? a.row_ptr[r] : 0;
+	int const len = valid ? a.row_ptr[r + 1] - rs : 0;
+	if (threadIdx.x == 0) {
+		first_rs = a.row_ptr[blockIdx.x * blockDim.x];
+		long_rows = 0;
+	}
+	__syncthreads();
+	if (len > RMAX) atomicOr(&long_rows, 1);
+	bool const mine = valid && len <= RMAX;
+
+	int col[RMAX];
+	float acc[RMAX][4];
+#pragma unroll
+	for (int t = 0; t < RMAX; t++) {
+		col[t] = (mine && t < len) ? a.cols[rs + t] : -1;
+		acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+	}
+	double b0 = 0.0, b1 = 0.0;
+	int const kind = a.kind;
+	double ca = 0, cb = 0, cc = 0;
+	if (!a.elemE && !a.elemNu) material_abc(a.E, a.nu, a.stress, ca, cb, cc);
+	int const is = mine ? a.inc_ptr[r] : 0, ie = mine ? a.inc_ptr[r + 1] : 0;
+	int prev_e = -1;
+	for (int t = is; t < ie; t++) {
+		int const e = a.inc[t];
+		if (e == prev_e) continue;
+		prev_e = e;
+		int map[4];
+		double x[4], y[4];
+		int jr = 0;
+#pragma unroll
+		for (int j = 0; j < 4; j++) {
+			if (j < kind) {
+				map[j] = a.elems[(long) e * kind + j];
+				double2 const c = reinterpret_cast<const double2*>(a.coords)[map[j]];
+				x[j] = c.x;
+				y[j] = c.y;
+			}
+			else {
+				map[j] = -2;
+				x[j] = y[j] = 0.0;
+			}
+		}
+#pragma unroll
+		for (int j = 3; j >= 0; j--)
+			if (j < kind && map[j] == r) jr = j;
+		double ea = ca, eb = cb, ec = cc;
+		if (a.elemE || a.elemNu) {
+			double const E = a.elemE ? a.elemE[e] : a.E;
+			double const nu = a.elemNu ? a.elemNu[e] : a.nu;
+			material_abc(E, nu, a.stress, ea, eb, ec);
+		}
+		float const fa = (float) ea, fb = (float) eb, fc = (float) ec;
+		float lx[4], ly[4];
+#pragma unroll
+		for (int j = 0; j < 4; j++) {
+			lx[j] = (float) (x[j] - x[0]);
+			ly[j] = (float) (y[j] - y[0]);
+		}
+		float ek[4][4];
+#pragma unroll
+		for (int k = 0; k < 4; k++) ek[k][0] = ek[k][1] = ek[k][2] = ek[k][3] = 0.f;
+		for (int q = 0; q < a.rule.nq; q++) {
+			float const w = (float) a.rule.w[q];
+			float dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
+			float gx[4], ge[4];
+#pragma unroll
+			for (int j = 0; j < 4; j++) {
+				gx[j] = j < kind ? (float) a.rule.dxi[q][j] : 0.f;
+				ge[j] = j < kind ? (float) a.rule.deta[q][j] : 0.f;
+				dx_dxsi += lx[j] * gx[j];
+				dx_deta += lx[j] * ge[j];
+				dy_dxsi += ly[j] * gx[j];
+				dy_deta += ly[j] * ge[j];
+			}
+			float const det = fabsf(dx_dxsi * dy_deta - dx_deta * dy_dxsi);
+			float const idet = 1.0f / det;
+			float dx[4], dy[4];
+#pragma unroll
+			for (int j = 0; j < 4; j++) {
+				dx[j] = (gx[j] * dy_deta - ge[j] * dy_dxsi) * idet;
+				dy[j] = (ge[j] * dx_dxsi - gx[j] * dx_deta) * idet;
+			}
+			float const dw = det * w;
+			double const ph = a.rule.phi[q][jr];
+			for (int f = 0; f < a.forces.nf; f++) {
+				double fx = a.forces.f[f][0], fy = a.forces.f[f][1];
+				if (a.forces.field[f]) {
+					fx = a.forces.field[f][2l * r];
+					fy = a.forces.field[f][2l * r + 1];
+				}
+				b0 += (double) dw * fx * a.rho * ph;
+				b1 += (double) dw * fy * a.rho * ph;
+			}
+			float xj = dx[0], yj = dy[0];
+#pragma unroll
+			for (int j = 1; j < 4; j++)
+				if (j == jr) {
+					xj = dx[j];
+					yj = dy[j];
+				}
+#pragma unroll
+			for (int k = 0; k < 4; k++) {
+				ek[k][0] += dw * (fa * xj * dx[k] + fc * yj * dy[k]);
+				ek[k][1] += dw * (fb * xj * dy[k] + fc * yj * dx[k]);
+				ek[k][2] += dw * (fb * yj * dx[k] + fc * xj * dy[k]);
+				ek[k][3] += dw * (fa * yj * dy[k] + fc * xj * dx[k]);
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			if (k >= kind) continue;
+			int const m = map[k];
+#pragma unroll
+			for (int t = 0; t < RMAX; t++)
+				if (col[t] == m) {
+					acc[t][0] += ek[k][0];
+					acc[t][1] += ek[k][1];
+					acc[t][2] += ek[k][2];
+					acc[t][3] += ek[k][3];
+				}
+		}
+	}
+	// translation-preserving diagonal (see k_assemble): FP64 sum of the off-diagonal blocks
+	double dfix[4] = {0, 0, 0, 0};
+	bool has_diag = false;
+#pragma unroll
+	for (int t = 0; t < RMAX; t++) {
+		if (col[t] == r) has_diag = true;
+		else if (col[t] >= 0)
+			for (int k = 0; k < 4; k++) dfix[k] -= (double) acc[t][k];
+	}
+	bool const fix = has_diag && is < ie;
+	int const r0 = 2 * r, r1 = 2 * r + 1;
+	bool const c0 = mine && a.last_ci[r0] >= 0, c1 = mine && a.last_ci[r1] >= 0;
+	double k00 = 0, k01 = 0, k10 = 0, k11 = 0;
+	double corr[4] = {0, 0, 0, 0};
+	__syncthreads();
+	bool const staged = long_rows == 0;
+#pragma unroll
+	for (int t = 0; t < RMAX; t++) {
+		int const c = col[t];
+		if (c < 0) continue;
+		int const d0 = 2 * c, d1 = 2 * c + 1;
+		bool const e0 = a.last_ci[d0] >= 0, e1 = a.last_ci[d1] >= 0;
+		double v[4] = {(double) acc[t][0], (double) acc[t][1], (double) acc[t][2], (double) acc[t][3]};
+		if (c == r && fix) {
+			v[0] = dfix[0]; v[1] = dfix[1]; v[2] = dfix[2]; v[3] = dfix[3];
+		}
+		if (e0 || e1) {
+			double const f0 = e0 ? a.first[d0] : 0.0, f1 = e1 ? a.first[d1] : 0.0;
+			if (!c0) {
+				if (e0) b0 -= f0 * v[0];
+				if (e1) b0 -= f1 * v[1];
+			}
+			if (!c1) {
+				if (e0) b1 -= f0 * v[2];
+				if (e1) b1 -= f1 * v[3];
+			}
+		}
+		if (c0 || e0) v[0] = (r0 == d0) ? 1.0 : 0.0;
+		if (c0 || e1) v[1] = 0.0;
+		if (c1 || e0) v[2] = 0.0;
+		if (c1 || e1) v[3] = (r1 == d1) ? 1.0 : 0.0;
+		float4 f4 = make_float4((float) v[0], (float) v[1], (float) v[2], (float) v[3]);
+		corr[0] += v[0] - (double) f4.x;
+		corr[1] += v[1] - (double) f4.y;
+		corr[2] += v[2] - (double) f4.z;
+		corr[3] += v[3] - (double) f4.w;
+		if (staged) stage[rs - first_rs + t] = f4;
+		else reinterpret_cast<float4*>(a.vals32)[rs + t] = f4;
+		if (c == r) {
+			k00 = v[0]; k01 = v[1];
+			k10 = v[2]; k11 = v[3];
+		}
+	}
+	if (mine) {
+		reinterpret_cast<float4*>(a.corr32)[r] =
+			make_float4((float) corr[0], (float) corr[1], (float) corr[2], (float) corr[3]);
+		if (c0) b0 = a.last[r0];
+		if (c1) b1 = a.last[r1];
+		a.b[r0] = b0;
+		a.b[r1] = b1;
+		store_precond(a, r, k00, k01, k10, k11);
+	}
+	__syncthreads();
+	if (staged) {
+		int const last_row = min(a.N, (int) (blockIdx.x + 1) * (int) blockDim.x);
+		int const end = a.row_ptr[last_row];
+		float4* const out = reinterpret_cast<float4*>(a.vals32);
+		for (int k = first_rs + threadIdx.x; k < end; k += blockDim.x) out[k] = stage[k - first_rs];
+	}
+}
+
 // Neumann X/Y loads (system.c:477-498), gathered per node in condition order
 // then edge order (deterministic, no atomics).  A load on a constrained DOF
 // survives only when applied after that DOF's last Dirichlet condition.
@@ -582,6 +791,33 @@ __global__ void k_neumann(NeuArgs a) {
 	}
 	a.b[2 * r] += add0;
 	a.b[2 * r + 1] += add1;
+}
+
+// Per-edge tractions (fx, fy per unit length): each end of an edge receives
+// (length/2) * load, as the reference's Neumann X/Y loop does for a flagged
+// edge (system.c:477-498).  Gathered per node over its edges in ascending
+// order (deterministic); constrained DOFs keep their Dirichlet value, as if
+// the loads were listed before the Dirichlet conditions.
+__global__ void k_edge_loads(int N, const int* __restrict__ ledges, const double* __restrict__ lloads,
+                             const int* __restrict__ lptr, const int* __restrict__ llist, const double* __restrict__ coords,
+                             const int* __restrict__ last_ci, double* __restrict__ b) {
+	int const r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= N) return;
+	double add0 = 0.0, add1 = 0.0;
+	for (int k = lptr[r]; k < lptr[r + 1]; k++) {
+		int const e = llist[k];
+		int const n1 = ledges[2 * e], n2 = ledges[2 * e + 1];
+		double const dx = coords[2l * n1] - coords[2l * n2];
+		double const dy = coords[2l * n1 + 1] - coords[2l * n2 + 1];
+		double const jac = sqrt(dx * dx + dy * dy) / 2;
+		int const mult = (n1 == r) + (n2 == r);
+		for (int u = 0; u < mult; u++) {
+			add0 += jac * lloads[2 * e];
+			add1 += jac * lloads[2 * e + 1];
+		}
+	}
+	if (last_ci[2 * r] < 0) b[2 * r] += add0;
+	if (last_ci[2 * r + 1] < 0) b[2 * r + 1] += add1;
 }
 
 }  // namespace
@@ -666,6 +902,15 @@ struct bfm_gpu_problem {
 
 	cudaEvent_t ev[4];
 	bool assembled, solved;
+
+	// per-edge tractions (extension of the Neumann conditions)
+	int n_loads, cap_loads;
+	int* ledges;
+	double* lloads;
+	int *lcnt, *lptr, *llist;
+
+	void* ext;               // batch solver state (batch.cu)
+	void (*ext_free)(void*);
 };
 
 namespace {
@@ -1028,6 +1273,10 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 		if (p) cudaFree(p);
 	for (int i = 0; i < MAXF; i++)
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
+	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist};
+	for (void* q : lb)
+		if (q) cudaFree(q);
+	if (P->ext && P->ext_free) P->ext_free(P->ext);
 	if (P->st_host) cudaFreeHost(P->st_host);
 	if (P->err_host) cudaFreeHost(P->err_host);
 	for (int i = 0; i < 4; i++)
@@ -1126,6 +1375,57 @@ int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int*
 	return 0;
 }
 
+int bfm_gpu_problem_set_edge_loads(bfm_gpu_problem_t* P, int n_loads, const int32_t* edges, const double* loads, int where) {
+	g_err[0] = 0;
+	if (n_loads < 0) return fail("negative load count");
+	if (n_loads > P->cap_loads) {
+		void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist};
+		for (void* q : lb)
+			if (q) cudaFree(q);
+		P->ledges = P->lcnt = P->lptr = P->llist = nullptr;
+		P->lloads = nullptr;
+		P->cap_loads = 0;
+		if (dalloc(&P->ledges, 2l * n_loads) || dalloc(&P->lloads, 2l * n_loads) || dalloc(&P->lcnt, P->N + 1l) ||
+		    dalloc(&P->lptr, P->N + 1l) || dalloc(&P->llist, 2l * n_loads))
+			return -1;
+		P->cap_loads = n_loads;
+	}
+	P->n_loads = n_loads;
+	if (n_loads) {
+		CK(cudaMemcpyAsync(P->ledges, edges, 2l * n_loads * sizeof(int), kind_of(where), P->stream));
+		CK(cudaMemcpyAsync(P->lloads, loads, 2l * n_loads * sizeof(double), kind_of(where), P->stream));
+	}
+	P->assembled = false;
+	return 0;
+}
+
+int bfmi_buffers(bfm_gpu_problem_t* P, bfmi_buffers_t* o) {
+	memset(o, 0, sizeof *o);
+	o->N = P->N;
+	o->n_elems = P->NE;
+	o->kind = P->kind;
+	o->precision = P->precision;
+	o->precond = P->precond;
+	o->assembled = P->assembled;
+	o->grid = P->grid;
+	o->row_ptr = P->row_ptr;
+	o->cols = P->cols;
+	o->vals32 = P->vals32;
+	o->corr32 = P->corr32;
+	o->dinv32 = P->dinv32;
+	o->vals64 = P->precision == BFM_GPU_MIXED_EXACT || P->precision == BFM_GPU_FP64 ? P->vals64 : nullptr;
+	o->b = P->b;
+	o->x = P->x;
+	for (int i = 0; i < 5; i++) o->vec[i] = P->vec[i];
+	o->stream = (void*) P->stream;
+	return 0;
+}
+
+void** bfmi_ext_slot(bfm_gpu_problem_t* P, void (**free_fn)(void*)) {
+	if (free_fn) P->ext_free = *free_fn;
+	return &P->ext;
+}
+
 int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	g_err[0] = 0;
 	if (precision != BFM_GPU_FP64 && precision != BFM_GPU_MIXED && precision != BFM_GPU_MIXED_EXACT)
@@ -1195,8 +1495,14 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.dinv32 = want32 ? P->dinv32 : nullptr;
 	a.precond = P->precond;
 	a.err = P->err;
-	if (precision != BFM_GPU_MIXED) k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
-	else k_assemble<false><<<blocks_for(N, 128), 128, 0, st>>>(a);
+	if (precision != BFM_GPU_MIXED) {
+		k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
+	}
+	else {
+		k_assemble32<12><<<blocks_for(N, 128), 128, 0, st>>>(a);
+		a.skip_upto = 12;
+		k_assemble<false><<<blocks_for(N, 128), 128, 0, st>>>(a);
+	}
 	// 5. Neumann loads
 	bool has_neu = false;
 	for (int c = 0; c < P->n_conds; c++)
@@ -1219,6 +1525,11 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		na.last_ci = P->last_ci;
 		na.b = P->b;
 		k_neumann<<<blocks_for(N), TPB, 0, st>>>(na);
+	}
+	if (P->n_loads) {
+		// the incidence helper counts into a buffer of N+1 ints and scans N entries
+		if (incidence(P, P->ledges, P->n_loads, 2, P->lcnt, P->lptr, P->llist, 1 << 30, 0)) return -1;
+		k_edge_loads<<<blocks_for(N), TPB, 0, st>>>(P->N, P->ledges, P->lloads, P->lptr, P->llist, P->coords, P->last_ci, P->b);
 	}
 	CK(cudaGetLastError());
 	CK(cudaEventRecord(P->ev[1], st));

@@ -170,7 +170,8 @@ def batch_uneven(n: int = 256, seed: int = 4) -> list[Problem]:
         eE = np.exp(rng.uniform(np.log(1e9), np.log(2e11), len(elems)))
         cm = side_mask(coords, clamp)
         lm = side_mask(coords, load)
-        conds = [(DIRICHLET_X, 0.0, cm), (DIRICHLET_Y, 0.0, cm), (NEUMANN_Y, -tr, lm)]
+        # the traction is listed first, so a corner shared with the clamped side stays clamped
+        conds = [(NEUMANN_Y, -tr, lm), (DIRICHLET_X, 0.0, cm), (DIRICHLET_Y, 0.0, cm)]
         out.append(Problem(name=f"batch{k}_{nx}x{ny}", kind=3, coords=coords, elems=elems, nu=nu, elem_E=eE,
                            forces=[], conds=conds, edges=boundary_edges(nx, ny)))
     return out

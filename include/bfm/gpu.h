@@ -177,6 +177,39 @@ int bfm_gpu_problem_autotune(bfm_gpu_problem_t* problem, int* lanes_per_row);
 /* The CUDA stream the problem's work is enqueued on (cudaStream_t as void*). */
 void* bfm_gpu_problem_stream(bfm_gpu_problem_t* problem);
 
+/* Per-edge tractions, an extension of the Neumann X/Y conditions for loads
+ * that differ from edge to edge: edge e (nodes edges[2e], edges[2e+1])
+ * carries the traction (loads[2e], loads[2e+1]) per unit length, and each of
+ * its ends receives length/2 times it, as the reference's Neumann loop does
+ * (system.c:477-498).  DOFs under a Dirichlet condition keep their value.
+ * Applied by the next bfm_gpu_problem_assemble. */
+int bfm_gpu_problem_set_edge_loads(bfm_gpu_problem_t* problem, int n_loads, const int32_t* edges, const double* loads,
+                                   int where);
+
+/* ---------------------------------------------------------------- batches of uneven meshes */
+
+/* Declare the problem a batch: node ranges [node_offsets[k], node_offsets[k+1])
+ * (host array of n_parts+1, from 0 to n_nodes, 1 <= n_parts <= 512) are
+ * independent meshes sharing no element.  Their elements are assembled
+ * together as one block-diagonal system (bfm_gpu_problem_assemble), and
+ * bfm_gpu_problem_solve_parts then solves every part with its own CG. */
+int bfm_gpu_problem_set_parts(bfm_gpu_problem_t* problem, int n_parts, const int32_t* node_offsets);
+
+/* Enqueue the batched solve: one persistent cooperative kernel in which each
+ * part runs mixed-precision Jacobi-PCG (FP32 operator and vectors, FP64
+ * inner products and residual replacement) with its own scalars and stopping
+ * test, captured in a CUDA graph.  Needs an assembly in BFM_GPU_MIXED or
+ * BFM_GPU_MIXED_EXACT.  With opts->autotune the first call times the tile
+ * shapes (rows per tile x lanes per row) on this batch and keeps the fastest.
+ * Grid barriers inside the kernel wait a bounded time, then report an error. */
+int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t* opts);
+
+/* Wait, then per part (arrays of n_parts, any may be NULL): iterations,
+ * status (BFM_GPU_*), FP64 residual replacements, FP64 relative residual;
+ * and the tile shape used and the device time of the last solve. */
+int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int* status, int* replacements,
+                               double* rel_residual, int* rows_per_tile, int* lanes_per_row, double* ms_solve);
+
 /* ---------------------------------------------------------------- allocation-free solve */
 
 /* No counterpart in the reference: an additive entry point for callers that
