@@ -141,9 +141,10 @@ def device_problem(lib, p, stream):
 
 def algorithmic_bytes_spmv(n_blocks: int, n_nodes: int, precision: int) -> int:
     """Bytes one SpMV+dots launch must move at least: block values + column
-    indices + row pointers, the residual and the diagonal read once, the
-    product written once."""
-    vb = 8 if precision == 0 else 4
+    indices + row pointers, and three node vectors touched once (FP64 and
+    double-float: the gathered u, the residual, the product written; mixed:
+    the residual, the previous direction, the product written)."""
+    vb = 8 if precision in (0, 3) else 4   # bytes per vector entry (double-float pairs: 8)
     n = 2 * n_nodes
     return n_blocks * (4 * vb + 4) + 4 * (n_nodes + 1) + n * (vb + vb + vb)
 
@@ -163,8 +164,9 @@ def run_gpu(args, rank: int, world: int):
     torch.cuda.set_stream(stream)
     methods = {"fp64": (bfm_gb300.FP64, bfm_gb300.PC_JACOBI),
                "mixed": (bfm_gb300.MIXED, bfm_gb300.PC_JACOBI),
-               "mixed_exact": (bfm_gb300.MIXED_EXACT, bfm_gb300.PC_JACOBI)}
-    chosen = ["fp64", "mixed_exact", "mixed"] if args.method == "best" else [args.method]
+               "mixed_exact": (bfm_gb300.MIXED_EXACT, bfm_gb300.PC_JACOBI),
+               "fp64_df": (bfm_gb300.FP64_DF, bfm_gb300.PC_JACOBI)}
+    chosen = ["fp64", "fp64_df", "mixed_exact", "mixed"] if args.method == "best" else [args.method]
     results = {}
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
     for m in chosen:
@@ -272,7 +274,7 @@ def profile(args):
     lib = bfm_gb300.lib()
     p = workload(args.workload)
     prec = {"fp64": bfm_gb300.FP64, "mixed": bfm_gb300.MIXED, "mixed_exact": bfm_gb300.MIXED_EXACT,
-            "best": bfm_gb300.FP64}[args.method]
+            "fp64_df": bfm_gb300.FP64_DF, "best": bfm_gb300.FP64}[args.method]
     P, keep = device_problem(lib, p, None)
     assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
     s = bfm_gb300.bfm_gpu_stats_t()
@@ -303,7 +305,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="perforated")
-    ap.add_argument("--method", default="best", choices=["fp64", "mixed", "mixed_exact", "best"])
+    ap.add_argument("--method", default="best", choices=["fp64", "fp64_df", "mixed", "mixed_exact", "best"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="assemble once and launch the two CG kernels --reps times each, standalone "

@@ -31,10 +31,10 @@ class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
                 ("ms_assemble", C.c_double), ("ms_solve", C.c_double)]
 
 
-FP64, MIXED, MIXED_EXACT = 0, 1, 2
+FP64, MIXED, MIXED_EXACT, FP64_DF = 0, 1, 2, 3
 PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED = 0, 1, 2
 HOST, DEVICE = 0, 1
-STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error"}
+STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error", 5: "stagnated"}
 
 _vp, _i, _d = C.c_void_p, C.c_int, C.c_double
 _P = C.POINTER

@@ -96,10 +96,32 @@ struct CgState {
 	double rho_ref;    // mixed: (r,r) right after the last residual replacement
 	double true_res2;  // ||b - A x||^2 after the solve
 	double rtol, drop2;
+	double best_true2;  // smallest true residual seen at a replacement
 	int iter, max_iters;
 	int done, status;
 	int replacements;
+	int stall;          // replacements in a row without halving best_true2's norm
 };
+
+// After an FP64 true residual: converged, or stagnating at the roundoff floor
+// of the arithmetic (three replacements without halving the best residual),
+// or keep going.  Returns 1 when the solve should stop.
+__device__ __forceinline__ int true_residual_verdict(CgState* st, double res2) {
+	st->replacements += 1;
+	st->rho_ref = res2;
+	st->true_res2 = res2;
+	if (res2 <= st->rtol * st->rtol * st->bnorm2) return 1;
+	if (st->replacements == 1 || res2 < 0.25 * st->best_true2) {
+		st->best_true2 = res2;
+		st->stall = 0;
+		return 0;
+	}
+	if (++st->stall >= 3) {
+		st->status = BFM_GPU_STAGNATED;
+		return 1;
+	}
+	return 0;
+}
 
 struct CgOpts {
 	double rtol;
@@ -244,6 +266,8 @@ __global__ void __launch_bounds__(TPB_K) k_cg_init(CgArgs<V> a, int mixed) {
 		st->max_iters = a.opts.max_iters;
 		st->iter = 0;
 		st->replacements = 0;
+		st->stall = 0;
+		st->best_true2 = out[0];
 		st->status = BFM_GPU_OK;
 		st->done = out[0] == 0.0;  // b = 0: x = 0 is exact
 		st->gamma_old = 0; st->alpha_old = 0;
@@ -255,8 +279,8 @@ __global__ void __launch_bounds__(TPB_K) k_cg_init(CgArgs<V> a, int mixed) {
 	}
 }
 
-// ---------------------------------------------------------------- FP64 path
-// Chronopoulos-Gear PCG: one reduction per iteration and only the SpMV's
+// ---------------------------------------------------------------- FP64, single reduction
+// (bfm_gpu_pcg_solve_noalloc) Chronopoulos-Gear PCG: one reduction per iteration and only the SpMV's
 // 4 FP64 FMAs per block in the gathered loop (FP64 issue rate bounds this
 // path on GB300, so u = M r is materialized once per node instead of being
 // formed per neighbour).
@@ -552,11 +576,8 @@ __global__ void __launch_bounds__(TPB_K) k_mx_replace(CgArgs<float> a) {
 	}
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		st->replacements += 1;
-		st->rho_ref = out[0];
-		st->true_res2 = out[0];
 		st->gamma = out[1];
-		if (out[0] <= st->rtol * st->rtol * st->bnorm2) {
+		if (true_residual_verdict(st, out[0])) {
 			st->done = 1;
 			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
 		}
@@ -576,6 +597,413 @@ __global__ void __launch_bounds__(TPB_K) k_true_residual(CgArgs<V> a) {
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) a.st->true_res2 = out[0];
 }
 
+// ---------------------------------------------------------------- double-float path
+// FP64-accurate PCG computed on the FP32 pipe (BFM_GPU_FP64_DF).  GB300 issues
+// FP64 at a small fraction of its FP32 rate, and the FP64 SpMV is bound by
+// that issue rate, not by memory.  Here every value is an unevaluated sum of
+// two floats (hi + lo, about 48 significant bits): the matrix (two FP32
+// copies, 32 bytes per block as in FP64), the Krylov vectors and the
+// solution; products and sums use error-free transformations (TwoProduct by
+// FMA, TwoSum), so the iteration behaves like FP64 CG at memory-bound speed.
+// Same single-reduction iteration as the FP64 path (u = M r materialized).
+
+struct dfl {
+	float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_make(double v) {
+	float const h = (float) v;
+	return {h, (float) (v - (double) h)};
+}
+__device__ __forceinline__ double df_dbl(dfl a) { return (double) a.hi + (double) a.lo; }
+
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+	float const s = __fadd_rn(a.hi, b.hi);
+	float const bb = __fsub_rn(s, a.hi);
+	float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+	e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+	float const h = __fadd_rn(s, e);
+	return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+	float const p = __fmul_rn(a.hi, b.hi);
+	float e = __fmaf_rn(a.hi, b.hi, -p);
+	e = __fmaf_rn(a.hi, b.lo, e);
+	e = __fmaf_rn(a.lo, b.hi, e);
+	float const h = __fadd_rn(p, e);
+	return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+// a*b + c
+__device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) { return df_add(df_mul(a, b), c); }
+
+// node vector element: (u_hi, v_hi, u_lo, v_lo) in one float4
+__device__ __forceinline__ void df_ld(const float* v, int i, dfl& a, dfl& b) {
+	float4 const t = reinterpret_cast<const float4*>(v)[i];
+	a = {t.x, t.z};
+	b = {t.y, t.w};
+}
+__device__ __forceinline__ void df_st(float* v, int i, dfl a, dfl b) {
+	reinterpret_cast<float4*>(v)[i] = make_float4(a.hi, b.hi, a.lo, b.lo);
+}
+
+struct DfArgs {
+	int N;
+	const int* row_ptr;
+	const int* cols;
+	const float* hi;    // 2x2 blocks, FP32 rounding of the FP64 value
+	const float* lo;    // FP32 rounding of the remainder
+	const double* vals64;  // the FP64 matrix, for the replacement residuals
+	const float* dinv;  // per node, df pair layout
+	const double* b;
+	float* x;           // df solution (converted to FP64 at the end)
+	double* x64;
+	float* r;
+	float* u;
+	float* p;
+	float* s;
+	float* w;
+	double* partials;
+	unsigned* ticket;
+	CgState* st;
+	CgOpts opts;
+	cudaGraphConditionalHandle cond;
+	cudaGraphConditionalHandle cond_repl;
+	int use_cond;
+	int timing;
+};
+
+__global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
+	DF bb2 = {0.f, 0.f};
+	double v[2] = {0.0, 0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		double2 const bb = ld2(a.b, i);
+		dfl const r0 = df_make(bb.x), r1 = df_make(bb.y);
+		dfl d0, d1;
+		df_ld(a.dinv, i, d0, d1);
+		dfl const u0 = df_mul(d0, r0), u1 = df_mul(d1, r1);
+		dfl const z = {0.f, 0.f};
+		df_st(a.x, i, z, z);
+		df_st(a.r, i, r0, r1);
+		df_st(a.u, i, u0, u1);
+		df_st(a.p, i, z, z);
+		df_st(a.s, i, z, z);
+		v[0] += bb.x * bb.x + bb.y * bb.y;
+		v[1] += df_dbl(df_add(df_mul(r0, u0), df_mul(r1, u1)));
+	}
+	(void) bb2;
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		CgState* st = a.st;
+		st->bnorm2 = out[0];
+		st->gamma = out[1];
+		st->rtol = a.opts.rtol;
+		st->drop2 = a.opts.drop2;
+		st->max_iters = a.opts.max_iters;
+		st->iter = 0;
+		st->replacements = 0;
+		st->stall = 0;
+		st->best_true2 = out[0];
+		st->status = BFM_GPU_OK;
+		st->done = out[0] == 0.0;
+		st->gamma_old = 0; st->alpha_old = 0;
+		st->alpha = 0; st->beta = 0;
+		st->rho = out[0];
+		st->rho_ref = out[0];
+		st->true_res2 = out[0];
+		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
+	}
+}
+
+__global__ void k_df_finish(DfArgs a) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		dfl x0, x1;
+		df_ld(a.x, i, x0, x1);
+		st2(a.x64, i, df_dbl(x0), df_dbl(x1));
+	}
+}
+
+// Jacobi in double-float layout from the FP64 diagonal (1/d, or 0 if d == 0)
+__global__ void k_df_dinv(int N, const double* __restrict__ dinv64, float* __restrict__ dinv) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	df_st(dinv, i, df_make(dinv64[2 * i]), df_make(dinv64[2 * i + 1]));
+}
+
+// ---------------------------------------------------------------- Hestenes-Stiefel, FP64 and double-float
+// The default iteration of the FP64 and double-float paths: two reductions
+// per iteration, A p formed afresh every iteration (no nested recurrences,
+// so the recurrence residual tracks the true one), reliable updates through
+// an IF node, convergence decided on the true residual only.
+//   K1: p' = z + beta p (neighbours formed on the fly, own row stored in the
+//       other ping-pong buffer); q = A p'; alpha = gamma / (p', q)
+//   K2: x += alpha p'; r -= alpha q; z = M r; gamma' = (r, z), rho = (r, r);
+//       beta; request a replacement when rho dropped by `drop` or claims rtol
+//   R:  r = b - A x; z = M r; gamma; verdict on the true residual
+// FP64: vectors double2 per node, z materialized so a neighbour costs 2 FMAs
+// on top of the SpMV's 4.  Double-float: pairs of floats, FP32 pipe only.
+
+// shared K1 finisher: alpha from (p', q); breakdown if not positive
+__device__ __forceinline__ void hs_alpha(CgState* st, double pq, int timing, int use_cond,
+                                         cudaGraphConditionalHandle cond) {
+	if (!(pq > 0.0)) {
+		if (!timing) {
+			st->done = 1;
+			st->status = BFM_GPU_BREAKDOWN;
+		}
+		return;
+	}
+	st->alpha = st->gamma / pq;
+	if (use_cond && !timing) cudaGraphSetConditional(cond, 1u);
+}
+
+// shared K2 finisher: beta, max_iters, breakdown, replacement request
+__device__ __forceinline__ void hs_beta(CgState* st, double gamma, double rho, int timing, int use_cond,
+                                        cudaGraphConditionalHandle cond, cudaGraphConditionalHandle cond_repl) {
+	if (timing) return;
+	double const tol2 = st->rtol * st->rtol * st->bnorm2;
+	st->rho = rho;
+	st->iter += 1;
+	st->beta = gamma / st->gamma;
+	st->gamma = gamma;
+	int stop = 0, repl = 0;
+	if (st->iter >= st->max_iters) {
+		stop = 1;
+		st->status = BFM_GPU_NOT_CONVERGED;
+	}
+	else if (!(gamma > 0.0)) {
+		repl = gamma == 0.0;
+		if (!repl) {
+			stop = 1;
+			st->status = BFM_GPU_BREAKDOWN;
+		}
+	}
+	else {
+		repl = rho <= st->drop2 * st->rho_ref || rho <= tol2;
+	}
+	if (stop) {
+		st->done = 1;
+		if (use_cond) cudaGraphSetConditional(cond, 0u);
+	}
+	else if (repl && use_cond) {
+		cudaGraphSetConditional(cond_repl, 1u);
+	}
+}
+
+template <int LPR>
+__global__ void __launch_bounds__(TPB_K) k_hs64_spmv(CgArgs<double> a) {
+	CgState* st = a.st;
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+		cudaGraphSetConditional(a.cond, 0u);
+		cudaGraphSetConditional(a.cond_repl, 0u);
+	}
+	if (st->done && !a.timing) return;
+	double const beta = st->beta;
+	const double* __restrict__ z = a.u;
+	const double* __restrict__ pp = a.p;
+	auto gather = [=](int c, double& g0, double& g1) {
+		double2 const zc = ld2(z, c), pc = ld2(pp, c);
+		g0 = zc.x + beta * pc.x;
+		g1 = zc.y + beta * pc.y;
+	};
+	double v[1] = {0.0};
+	FOR_ROWS(LPR) {
+		bool const ok = row_ < a.N;
+		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		double y0, y1;
+		row_product<LPR, double>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		if (ok && sub_ == 0) {
+			double g0, g1;
+			gather(row_, g0, g1);
+			st2(a.pn, row_, g0, g1);
+			st2(a.w, row_, y0, y1);
+			v[0] += g0 * y0 + g1 * y1;
+		}
+	}
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
+}
+
+__global__ void __launch_bounds__(TPB_K) k_hs64_update(CgArgs<double> a) {
+	CgState* st = a.st;
+	if (st->done && !a.timing) return;
+	double const alpha = st->alpha;
+	double v[2] = {0.0, 0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		double2 const pn = ld2(a.pn, i), q = ld2(a.w, i), r = ld2(a.r, i), x = ld2(a.x, i);
+		st2(a.x, i, x.x + alpha * pn.x, x.y + alpha * pn.y);
+		double const r0 = r.x - alpha * q.x, r1 = r.y - alpha * q.y;
+		st2(a.r, i, r0, r1);
+		double z0, z1;
+		precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
+		st2(a.u, i, z0, z1);
+		v[0] += r0 * z0 + r1 * z1;
+		v[1] += r0 * r0 + r1 * r1;
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0)
+		hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+}
+
+template <int LPR>
+__global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
+	CgState* st = a.st;
+	if (st->done) return;
+	double v[2] = {0.0, 0.0};
+	const double* __restrict__ x = a.x;
+	auto gx = [x](int c, double& g0, double& g1) {
+		double2 const t = ld2(x, c);
+		g0 = t.x;
+		g1 = t.y;
+	};
+	FOR_ROWS(LPR) {
+		bool const ok = row_ < a.N;
+		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		double y0, y1;
+		row_product<LPR, double>(a.cols, a.vals, ks, ke, sub_, gx, y0, y1);
+		if (ok && sub_ == 0) {
+			double2 const bb = ld2(a.b, row_);
+			double const r0 = bb.x - y0, r1 = bb.y - y1;
+			st2(a.r, row_, r0, r1);
+			double z0, z1;
+			precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
+			st2(a.u, row_, z0, z1);
+			v[0] += r0 * r0 + r1 * r1;
+			v[1] += r0 * z0 + r1 * z1;
+		}
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		st->gamma = out[1];
+		if (true_residual_verdict(st, out[0])) {
+			st->done = 1;
+			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		}
+	}
+}
+
+// ---- double-float HS kernels: x, r, z (in u), p, p' (in s), q (in w)
+template <int LPR>
+__global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
+	CgState* st = a.st;
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+		cudaGraphSetConditional(a.cond, 0u);
+		cudaGraphSetConditional(a.cond_repl, 0u);
+	}
+	if (st->done && !a.timing) return;
+	dfl const beta = df_make(st->beta);
+	double v[1] = {0.0};
+	int const sub = threadIdx.x % LPR;
+	int const rpb = blockDim.x / LPR;
+	for (int base = blockIdx.x * rpb; base < a.N; base += gridDim.x * rpb) {
+		int const row = base + threadIdx.x / LPR;
+		bool const ok = row < a.N;
+		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+		dfl y0 = {0.f, 0.f}, y1 = {0.f, 0.f};
+		for (int k = ks + sub; k < ke; k += LPR) {
+			int const c = a.cols[k];
+			dfl z0, z1, p0, p1;
+			df_ld(a.u, c, z0, z1);
+			df_ld(a.p, c, p0, p1);
+			dfl const g0 = df_fma(beta, p0, z0), g1 = df_fma(beta, p1, z1);
+			float4 const h = reinterpret_cast<const float4*>(a.hi)[k];
+			float4 const l = reinterpret_cast<const float4*>(a.lo)[k];
+			y0 = df_fma({h.x, l.x}, g0, y0);
+			y0 = df_fma({h.y, l.y}, g1, y0);
+			y1 = df_fma({h.z, l.z}, g0, y1);
+			y1 = df_fma({h.w, l.w}, g1, y1);
+		}
+#pragma unroll
+		for (int o = LPR / 2; o; o >>= 1) {
+			y0 = df_add(y0, {__shfl_xor_sync(0xffffffffu, y0.hi, o), __shfl_xor_sync(0xffffffffu, y0.lo, o)});
+			y1 = df_add(y1, {__shfl_xor_sync(0xffffffffu, y1.hi, o), __shfl_xor_sync(0xffffffffu, y1.lo, o)});
+		}
+		if (ok && sub == 0) {
+			dfl z0, z1, p0, p1;
+			df_ld(a.u, row, z0, z1);
+			df_ld(a.p, row, p0, p1);
+			dfl const g0 = df_fma(beta, p0, z0), g1 = df_fma(beta, p1, z1);
+			df_st(a.s, row, g0, g1);
+			df_st(a.w, row, y0, y1);
+			v[0] += df_dbl(df_add(df_mul(g0, y0), df_mul(g1, y1)));
+		}
+	}
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
+}
+
+__global__ void __launch_bounds__(TPB_K) k_hsdf_update(DfArgs a) {
+	CgState* st = a.st;
+	if (st->done && !a.timing) return;
+	dfl const alpha = df_make(st->alpha), nalpha = df_neg(alpha);
+	double v[2] = {0.0, 0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		dfl pn0, pn1, q0, q1, r0, r1, x0, x1, d0, d1;
+		df_ld(a.s, i, pn0, pn1);
+		df_ld(a.w, i, q0, q1);
+		df_ld(a.r, i, r0, r1);
+		df_ld(a.x, i, x0, x1);
+		df_ld(a.dinv, i, d0, d1);
+		df_st(a.x, i, df_fma(alpha, pn0, x0), df_fma(alpha, pn1, x1));
+		r0 = df_fma(nalpha, q0, r0);
+		r1 = df_fma(nalpha, q1, r1);
+		df_st(a.r, i, r0, r1);
+		dfl const z0 = df_mul(d0, r0), z1 = df_mul(d1, r1);
+		df_st(a.u, i, z0, z1);
+		v[0] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));
+		v[1] += df_dbl(df_add(df_mul(r0, r0), df_mul(r1, r1)));
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0)
+		hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+}
+
+// Replacement of the double-float path: the true residual in FP64 from the
+// FP64 matrix (the rare FP64 SpMV sets the attainable accuracy; the
+// iteration itself stays on the FP32 pipe), r and z = M r back in pairs.
+template <int LPR>
+__global__ void __launch_bounds__(TPB_K) k_hsdf_replace(DfArgs a) {
+	CgState* st = a.st;
+	if (st->done) return;
+	double v[2] = {0.0, 0.0};
+	int const sub = threadIdx.x % LPR;
+	int const rpb = blockDim.x / LPR;
+	const float* __restrict__ xdf = a.x;
+	auto gx = [xdf](int c, double& g0, double& g1) {
+		dfl x0, x1;
+		df_ld(xdf, c, x0, x1);
+		g0 = df_dbl(x0);
+		g1 = df_dbl(x1);
+	};
+	for (int base = blockIdx.x * rpb; base < a.N; base += gridDim.x * rpb) {
+		int const row = base + threadIdx.x / LPR;
+		bool const ok = row < a.N;
+		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+		double y0, y1;
+		row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gx, y0, y1);
+		if (ok && sub == 0) {
+			double2 const bb = ld2(a.b, row);
+			double const e0 = bb.x - y0, e1 = bb.y - y1;
+			dfl const r0 = df_make(e0), r1 = df_make(e1);
+			df_st(a.r, row, r0, r1);
+			dfl d0, d1;
+			df_ld(a.dinv, row, d0, d1);
+			dfl const z0 = df_mul(d0, r0), z1 = df_mul(d1, r1);
+			df_st(a.u, row, z0, z1);
+			v[0] += e0 * e0 + e1 * e1;
+			v[1] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));
+		}
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		st->gamma = out[1];
+		if (true_residual_verdict(st, out[0])) {
+			st->done = 1;
+			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		}
+	}
+}
+
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner
 struct CgKernels {
 	void* spmv64;
@@ -583,12 +1011,17 @@ struct CgKernels {
 	void* replace;
 	void* res64;
 	void* resmx;
+	void* hs64;
+	void* hs64repl;
+	void* hsdf;
+	void* hsdfrepl;
 };
 
 template <int LPR>
 CgKernels kernels_for() {
 	return {(void*) k_cg64_spmv<LPR>, (void*) k_mx_spmv<LPR>, (void*) k_mx_replace<LPR>,
-	        (void*) k_true_residual<LPR, double>, (void*) k_true_residual<LPR, float>};
+	        (void*) k_true_residual<LPR, double>, (void*) k_true_residual<LPR, float>, (void*) k_hs64_spmv<LPR>,
+	        (void*) k_hs64_replace<LPR>, (void*) k_hsdf_spmv<LPR>, (void*) k_hsdf_replace<LPR>};
 }
 
 CgKernels kernels_lpr(int lpr) {

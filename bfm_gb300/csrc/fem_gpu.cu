@@ -286,6 +286,7 @@ struct AsmArgs {
 	double* vals64;
 	float* vals32;
 	float* corr32;   // per node: 2x2 block of the row sums of (FP64 value - FP32 value)
+	float* vals32lo; // double-float path: FP32 rounding of (FP64 value - FP32 value)
 	double* b;
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
@@ -519,6 +520,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				float const f = (float) v[k];
 				a.vals32[o + k] = f;
 				corr[k] += v[k] - (double) f;
+				if (a.vals32lo) a.vals32lo[o + k] = (float) (v[k] - (double) f);
 			}
 		}
 		if (c == r) {
@@ -526,7 +528,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			k10 = v[2]; k11 = v[3];
 		}
 	}
-	if (a.corr32) {
+	if (a.corr32 && !a.vals32lo) {
 		a.corr32[4 * r + 0] = (float) corr[0]; a.corr32[4 * r + 1] = (float) corr[1];
 		a.corr32[4 * r + 2] = (float) corr[2]; a.corr32[4 * r + 3] = (float) corr[3];
 	}
@@ -877,6 +879,7 @@ struct bfm_gpu_problem {
 	double* vals64;
 	float* vals32;
 	float* corr32;  // mixed: per-node 2x2 row-sum correction of the FP32 operator
+	float* vals32lo;  // double-float path: low parts of the block values
 	double* b;
 	int* last_ci;
 	double *first, *last;
@@ -886,7 +889,7 @@ struct bfm_gpu_problem {
 
 	// CG
 	double* x;
-	void* vec[5];  // r, u, p, s, w (FP64 path) or r, -, p, pn, q (mixed path)
+	void* vec[6];  // r, u, p, s, w (FP64 path), + x (double-float path); r, dx, p, pn, q (mixed path)
 	int lpr;       // lanes per block row of the SpMV kernels (autotuned)
 	double* partials;
 	unsigned* ticket;
@@ -1010,6 +1013,35 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	return a;
 }
 
+DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
+	DfArgs a;
+	memset(&a, 0, sizeof a);
+	a.N = P->N;
+	a.row_ptr = P->row_ptr;
+	a.cols = P->cols;
+	a.hi = P->vals32;
+	a.lo = P->vals32lo;
+	a.vals64 = P->vals64;
+	a.dinv = P->dinv32;
+	a.b = P->b;
+	a.x = (float*) P->vec[5];
+	a.x64 = P->x;
+	a.r = (float*) P->vec[0];
+	a.u = (float*) P->vec[1];
+	a.p = (float*) P->vec[2];
+	a.s = (float*) P->vec[3];
+	a.w = (float*) P->vec[4];
+	a.partials = P->partials;
+	a.ticket = P->ticket;
+	a.st = P->st;
+	if (o) {
+		a.opts.rtol = o->rtol;
+		a.opts.drop2 = o->replace_drop * o->replace_drop;
+		a.opts.max_iters = o->max_iters;
+	}
+	return a;
+}
+
 int add_node(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, void* fn, int grid, void** params) {
 	cudaKernelNodeParams kp = {};
 	kp.func = fn;
@@ -1037,7 +1069,7 @@ int add_conditional(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t*
 // mixed: init -> while(running){ K1 ; K2 ; if(replace){R} ; K1' ; K2' ; if(replace'){R'} } -> true residual
 //        (two iterations per body pass, so each node has fixed ping-pong direction buffers)
 int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
-	bool const mixed = P->precision != BFM_GPU_FP64;
+	bool const mixed = P->precision == BFM_GPU_MIXED || P->precision == BFM_GPU_MIXED_EXACT;
 	CgKernels const K = kernels_lpr(P->lpr);
 	cudaGraph_t g, body;
 	CK(cudaGraphCreate(&g, 0));
@@ -1045,17 +1077,57 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	CK(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
 	cudaGraphNode_t n_init, n_loop, n_res, prev = nullptr;
 	int imixed = mixed;
-	if (!mixed) {
-		CgArgs<double> a = cg_args<double>(P, o);
-		a.use_cond = 1;
-		a.cond = h;
-		void* pi[2] = {&a, &imixed};
-		void* pa[1] = {&a};
+	if (P->precision == BFM_GPU_FP64_DF) {
+		DfArgs a[2];
+		a[0] = df_args(P, o);
+		a[0].use_cond = 1;
+		a[0].cond = h;
+		a[1] = a[0];
+		a[1].p = a[0].s;
+		a[1].s = a[0].p;
+		CgArgs<double> ar = cg_args<double>(P, o);  // final FP64 residual with the FP64 matrix
+		void* pi[1] = {&a[0]};
+		void* pr[1] = {&ar};
+		if (add_node(g, &n_init, nullptr, (void*) k_df_init, P->grid, pi)) return -1;
+		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
+		for (int half = 0; half < 2; half++) {
+			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
+			void* pa[1] = {&a[half]};
+			cudaGraphNode_t n1, n2, nif, nr;
+			cudaGraph_t ifbody;
+			if (add_node(body, &n1, prev ? &prev : nullptr, K.hsdf, P->grid, pa)) return -1;
+			if (add_node(body, &n2, &n1, (void*) k_hsdf_update, P->grid, pa)) return -1;
+			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
+			if (add_node(ifbody, &nr, nullptr, K.hsdfrepl, P->grid, pa)) return -1;
+			prev = nif;
+		}
+		cudaGraphNode_t n_fin;
+		if (add_node(g, &n_fin, &n_loop, (void*) k_df_finish, P->grid, pi)) return -1;
+		if (add_node(g, &n_res, &n_fin, K.res64, P->grid, pr)) return -1;
+	}
+	else if (!mixed) {
+		CgArgs<double> a[2];
+		a[0] = cg_args<double>(P, o);
+		a[0].use_cond = 1;
+		a[0].cond = h;
+		a[1] = a[0];
+		a[1].p = a[0].pn;
+		a[1].pn = a[0].p;
+		void* pi[2] = {&a[0], &imixed};
 		if (add_node(g, &n_init, nullptr, (void*) k_cg_init<double>, P->grid, pi)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
-		cudaGraphNode_t n_a, n_b;
-		if (add_node(body, &n_a, nullptr, K.spmv64, P->grid, pa)) return -1;
-		if (add_node(body, &n_b, &n_a, (void*) k_cg64_update, P->grid, pa)) return -1;
+		for (int half = 0; half < 2; half++) {
+			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
+			void* pa[1] = {&a[half]};
+			cudaGraphNode_t n1, n2, nif, nr;
+			cudaGraph_t ifbody;
+			if (add_node(body, &n1, prev ? &prev : nullptr, K.hs64, P->grid, pa)) return -1;
+			if (add_node(body, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
+			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
+			if (add_node(ifbody, &nr, nullptr, K.hs64repl, P->grid, pa)) return -1;
+			prev = nif;
+		}
+		void* pa[1] = {&a[0]};
 		if (add_node(g, &n_res, &n_loop, K.res64, P->grid, pa)) return -1;
 	}
 	else {
@@ -1105,7 +1177,21 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 	for (auto& x : e) cudaEventCreate(&x);
 	int const grid = P->grid;
 	cudaStream_t const st = P->stream;
-	if (P->precision == BFM_GPU_FP64) {
+	if (P->precision == BFM_GPU_FP64_DF) {
+		DfArgs a = df_args(P, nullptr);
+		a.opts.rtol = 0.0;
+		a.opts.max_iters = 1 << 30;
+		a.st = scratch;
+		a.timing = 1;
+		k_df_init<<<grid, TPB, 0, st>>>(a);
+		void* pa[1] = {&a};
+		cudaEventRecord(e[0], st);
+		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.hsdf, dim3(grid), dim3(TPB), pa, 0, st);
+		cudaEventRecord(e[1], st);
+		for (int i = 0; i < reps; i++) k_hsdf_update<<<grid, TPB, 0, st>>>(a);
+		cudaEventRecord(e[2], st);
+	}
+	else if (P->precision == BFM_GPU_FP64) {
 		CgArgs<double> a = cg_args<double>(P, nullptr);
 		a.opts.rtol = 0.0;
 		a.opts.max_iters = 1 << 30;
@@ -1114,9 +1200,9 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 		k_cg_init<double><<<grid, TPB, 0, st>>>(a, 0);
 		void* pa[1] = {&a};
 		cudaEventRecord(e[0], st);
-		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.spmv64, dim3(grid), dim3(TPB), pa, 0, st);
+		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.hs64, dim3(grid), dim3(TPB), pa, 0, st);
 		cudaEventRecord(e[1], st);
-		for (int i = 0; i < reps; i++) k_cg64_update<<<grid, TPB, 0, st>>>(a);
+		for (int i = 0; i < reps; i++) k_hs64_update<<<grid, TPB, 0, st>>>(a);
 		cudaEventRecord(e[2], st);
 	}
 	else {
@@ -1224,7 +1310,9 @@ int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n
 	int const sms = num_sms();
 	int occ = 8;
 	void* const ks[] = {(void*) k_cg64_spmv<1>, (void*) k_cg64_spmv<8>, (void*) k_mx_spmv<1>, (void*) k_mx_spmv<8>,
-	                    (void*) k_cg64_update, (void*) k_mx_update, (void*) k_mx_replace<8>};
+	                    (void*) k_cg64_update, (void*) k_mx_update, (void*) k_mx_replace<8>, (void*) k_hs64_spmv<1>,
+	                    (void*) k_hs64_spmv<8>,
+	                    (void*) k_hs64_update, (void*) k_hsdf_spmv<1>, (void*) k_hsdf_spmv<8>, (void*) k_hsdf_update};
 	for (void* k : ks) {
 		int nb = 0;
 		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, TPB, 0) == cudaSuccess && nb > 0 && nb < occ) occ = nb;
@@ -1267,7 +1355,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4],
+	                P->vals32, P->corr32, P->vals32lo, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1428,20 +1516,26 @@ void** bfmi_ext_slot(bfm_gpu_problem_t* P, void (**free_fn)(void*)) {
 
 int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	g_err[0] = 0;
-	if (precision != BFM_GPU_FP64 && precision != BFM_GPU_MIXED && precision != BFM_GPU_MIXED_EXACT)
+	if (precision != BFM_GPU_FP64 && precision != BFM_GPU_MIXED && precision != BFM_GPU_MIXED_EXACT &&
+	    precision != BFM_GPU_FP64_DF)
 		return fail("unknown precision %d", precision);
+	bool const dfp = precision == BFM_GPU_FP64_DF;
 	bool const want64 = precision != BFM_GPU_MIXED;  // FP64 values: the operator, or the residual operator
-	bool const want32 = precision != BFM_GPU_FP64;   // FP32 values: the mixed iteration operator
+	bool const want32 = precision != BFM_GPU_FP64;   // FP32 values: the mixed iteration operator / hi parts
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
 	// value storage for this precision (allocated once, on first use)
 	if (want64 && !P->vals64 && dalloc(&P->vals64, 4 * P->nb_cap)) return -1;
 	if (want32 && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
-	if (!want32 && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
+	if ((!want32 || dfp) && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
 	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 4 * N)) return -1;
 	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
-	size_t const vsz = precision == BFM_GPU_FP64 ? sizeof(double) : sizeof(float);
-	if ((P->precision == BFM_GPU_FP64) != (precision == BFM_GPU_FP64) || !P->vec[0]) {
+	if (dfp && !P->vals32lo && dalloc(&P->vals32lo, 4 * P->nb_cap)) return -1;
+	// 16 bytes per node per vector for FP64 and double-float, 8 for the mixed FP32 vectors
+	bool const wide = precision == BFM_GPU_FP64 || dfp;
+	size_t const vsz = wide ? sizeof(double) : sizeof(float);
+	bool const was_wide = P->precision == BFM_GPU_FP64 || P->precision == BFM_GPU_FP64_DF;
+	if (was_wide != wide || !P->vec[0]) {
 		for (void*& v : P->vec) {
 			if (v) cudaFree(v);
 			v = nullptr;
@@ -1490,13 +1584,15 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.vals64 = want64 ? P->vals64 : nullptr;
 	a.vals32 = want32 ? P->vals32 : nullptr;
 	a.corr32 = want32 ? P->corr32 : nullptr;
+	a.vals32lo = dfp ? P->vals32lo : nullptr;
 	a.b = P->b;
-	a.dinv64 = want32 ? nullptr : P->dinv64;
-	a.dinv32 = want32 ? P->dinv32 : nullptr;
+	a.dinv64 = want32 && !dfp ? nullptr : P->dinv64;
+	a.dinv32 = want32 && !dfp ? P->dinv32 : nullptr;
 	a.precond = P->precond;
 	a.err = P->err;
 	if (precision != BFM_GPU_MIXED) {
 		k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
+		if (dfp) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32);
 	}
 	else {
 		k_assemble32<12><<<blocks_for(N, 128), 128, 0, st>>>(a);
@@ -1629,7 +1725,7 @@ int bfm_gpu_problem_download(bfm_gpu_problem_t* P, int32_t* row_ptr, int32_t* co
 	if (row_ptr) CK(cudaMemcpy(row_ptr, P->row_ptr, (P->N + 1) * sizeof(int), cudaMemcpyDeviceToHost));
 	if (cols) CK(cudaMemcpy(cols, P->cols, nb * sizeof(int), cudaMemcpyDeviceToHost));
 	if (vals) {
-		if (P->precision == BFM_GPU_FP64) CK(cudaMemcpy(vals, P->vals64, 4 * nb * sizeof(double), cudaMemcpyDeviceToHost));
+		if (P->precision != BFM_GPU_MIXED) CK(cudaMemcpy(vals, P->vals64, 4 * nb * sizeof(double), cudaMemcpyDeviceToHost));
 		else {
 			float* tmp = (float*) malloc(4 * nb * sizeof(float) + 1);
 			if (!tmp) return fail("out of host memory");

@@ -47,6 +47,8 @@ static bfm_gpu_opts_t current_opts(void) {
 		bfm_gpu_default_opts(&t_opts);
 		char const* p = getenv("BFM_GPU_PRECISION");
 		if (p && (!strcmp(p, "mixed") || !strcmp(p, "1"))) t_opts.precision = BFM_GPU_MIXED;
+		if (p && (!strcmp(p, "mixed_exact") || !strcmp(p, "2"))) t_opts.precision = BFM_GPU_MIXED_EXACT;
+		if (p && (!strcmp(p, "df") || !strcmp(p, "3"))) t_opts.precision = BFM_GPU_FP64_DF;
 		char const* r = getenv("BFM_GPU_RTOL");
 		if (r) t_opts.rtol = strtod(r, NULL);
 		t_opts_set = 1;
@@ -300,6 +302,7 @@ static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	t_stats = s;
 	if (s.status == BFM_GPU_BAD_MESH) return REPORT(st, "%s", bfm_gpu_last_error());
 	if (bfm_gpu_problem_solution(P, inst->effects, BFM_GPU_HOST) < 0) return REPORT(st, "%s", bfm_gpu_last_error());
+	/* BFM_GPU_STAGNATED: the residual reached the roundoff floor above rtol; x is usable */
 	if (s.status == BFM_GPU_NOT_CONVERGED)
 		return REPORT(st, "CG did not reach rtol %g in %d iterations (relative residual %g)", o.rtol, s.iterations, s.rel_residual);
 	if (s.status == BFM_GPU_BREAKDOWN)

@@ -40,6 +40,9 @@ enum {
 	BFM_GPU_MIXED_EXACT = 2, /* as MIXED, but the element loop runs in FP64 once: the FP64 matrix is
 	                            the residual operator (solution of the FP64 system) and its FP32
 	                            rounding the iteration operator                                    */
+	BFM_GPU_FP64_DF = 3, /* FP64-accurate CG on the FP32 pipe: matrix, vectors and solution held as
+	                        pairs of floats (about 48 significant bits), error-free FP32
+	                        arithmetic; FP64 element loop and final FP64 residual              */
 };
 
 /* preconditioner */
@@ -56,15 +59,18 @@ enum {
 	BFM_GPU_BREAKDOWN = 2,     /* p.Ap <= 0 or NaN: matrix not SPD / singular */
 	BFM_GPU_BAD_MESH = 3,      /* valence or row length above the kernel caps */
 	BFM_GPU_CUDA_ERROR = 4,
+	BFM_GPU_STAGNATED = 5,     /* the FP64 true residual stopped decreasing above rtol: the
+	                              roundoff floor of this system; x is as accurate as it gets */
 };
 
 typedef struct {
 	int precision;     /* BFM_GPU_FP64 or BFM_GPU_MIXED                         */
 	int precond;       /* BFM_GPU_PC_*                                          */
-	double rtol;       /* stop when ||b - A x||_2 <= rtol ||b||_2               */
+	double rtol;       /* stop when the true ||b - A x||_2 <= rtol ||b||_2      */
 	int max_iters;     /* hard cap on CG iterations                             */
-	double replace_drop; /* mixed: replace the recurrence residual by the FP64
-	                        true residual each time it has dropped by this factor */
+	double replace_drop; /* replace the recurrence residual by the true residual
+	                        (computed from the matrix) each time it has dropped by
+	                        this factor, and whenever it claims convergence     */
 	int deterministic; /* 1: fixed reduction order (always on; kept for ABI)    */
 	int autotune;      /* 1: pick the SpMV shape (lanes per block row) by timing
 	                      the candidates on the problem's own matrix, once    */

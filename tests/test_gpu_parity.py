@@ -38,8 +38,9 @@ def test_sim_run_matches_reference(libbfm, name):
     h = api.SimHandle.from_problem(libbfm, p)
     assert h.run() == 0, h.error()
     s = stats(libbfm)
-    # the FP64 true residual floors near eps*||K||*||u||/||b|| (K ~ 1e11, cond ~ 1e12 unscaled)
-    assert s.status == 0 and s.rel_residual < 1e-8
+    # the FP64 true residual floors near eps*||K||*||u||/||b|| (K ~ 1e11, cond ~ 1e12 unscaled):
+    # at rtol 1e-12 the solver may stop there (BFM_GPU_STAGNATED, 5) instead of at rtol
+    assert s.status in (0, 5) and s.rel_residual < 1e-8
     assert rel(h.effects(), d["effects"]) < PARITY_RTOL
 
 
