@@ -139,14 +139,16 @@ def device_problem(lib, p, stream):
     return P, keep
 
 
-def algorithmic_bytes_spmv(n_blocks: int, n_nodes: int, precision: int) -> int:
-    """Bytes one SpMV+dots launch must move at least: block values + column
-    indices + row pointers, and three node vectors touched once (FP64 and
-    double-float: the gathered u, the residual, the product written; mixed:
-    the residual, the previous direction, the product written)."""
-    vb = 8 if precision in (0, 3) else 4   # bytes per vector entry (double-float pairs: 8)
-    n = 2 * n_nodes
-    return n_blocks * (4 * vb + 4) + 4 * (n_nodes + 1) + n * (vb + vb + vb)
+def algorithmic_bytes_spmv(n_blocks: int, n_nodes: int, precision: int, block_pc: bool = False) -> int:
+    """Bytes one launch of the fused SpMV kernel (K1: direction update, A p,
+    (p, A p)) must move at least: block values + column indices + row
+    pointers, plus its node vectors touched once.  FP64 and double-float
+    (16 B per node vector): z and p read, p' and q written.  Mixed (8 B per
+    node vector): r, p and the preconditioner read (Jacobi 8 B, block 16 B
+    per node), the 16 B correction block read, p' and q written."""
+    if precision in (0, 3):
+        return n_blocks * (32 + 4) + 4 * (n_nodes + 1) + n_nodes * 64
+    return n_blocks * (16 + 4) + 4 * (n_nodes + 1) + n_nodes * (8 + 8 + (16 if block_pc else 8) + 16 + 8 + 8)
 
 
 def run_gpu(args, rank: int, world: int):

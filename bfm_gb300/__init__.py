@@ -69,6 +69,18 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_solve_parts": (_i, [_vp, _P(bfm_gpu_opts_t)]),
     "bfm_gpu_problem_part_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _P(_i), _P(_i), _P(_d)]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
+    "bfm_gpu_problem_apply": (_i, [_vp, _vp, _vp, _i]),
+    "bfm_gpu_mpnn_param_count": (_i, []),
+    "bfm_gpu_mpnn_create": (_i, [_P(_vp), C.c_uint]),
+    "bfm_gpu_mpnn_destroy": (_i, [_vp]),
+    "bfm_gpu_mpnn_get_weights": (_i, [_vp, _vp]),
+    "bfm_gpu_mpnn_set_weights": (_i, [_vp, _vp]),
+    "bfm_gpu_mpnn_save": (_i, [_vp, C.c_char_p]),
+    "bfm_gpu_mpnn_load": (_i, [_vp, C.c_char_p]),
+    "bfm_gpu_mpnn_forward": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "bfm_gpu_mpnn_gradient": (_i, [_vp, _vp, _vp, _vp, _P(_d), _vp]),
+    "bfm_gpu_mpnn_train_step": (_i, [_vp, _vp, _vp, _vp, _d, _P(_d)]),
+    "bfm_gpu_mpnn_use": (_i, [_vp]),
 }
 
 

@@ -11,71 +11,9 @@
 
 #include <bfm/gpu.h>
 
+#include "reduce.cuh"
+
 namespace {
-
-#ifndef BFM_TPB
-#define BFM_TPB 256
-#endif
-constexpr int TPB_K = BFM_TPB;
-
-// ------------------------------------------------------------------ reductions
-
-// Sum NV values over the whole grid: every block writes its partial sums,
-// the last block to arrive (atomic ticket) adds them in block order and
-// returns true with the totals in `out`.  The result does not depend on which
-// block arrives last.
-template <int NV>
-__device__ __forceinline__ bool grid_sum(double (&v)[NV], double* __restrict__ partials, unsigned* ticket,
-                                         double (&out)[NV]) {
-	__shared__ double sm[TPB_K / 32][NV];
-	__shared__ bool is_last;
-	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-	for (int i = 0; i < NV; i++)
-		for (int o = 16; o; o >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
-	if (lane == 0)
-		for (int i = 0; i < NV; i++) sm[wid][i] = v[i];
-	__syncthreads();
-	if (wid == 0) {
-#pragma unroll
-		for (int i = 0; i < NV; i++) {
-			double t = lane < nw ? sm[lane][i] : 0.0;
-			for (int o = 16; o; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-			if (lane == 0) partials[blockIdx.x * NV + i] = t;
-		}
-	}
-	if (threadIdx.x == 0) {
-		__threadfence();
-		unsigned const tk = atomicAdd(ticket, 1u);
-		is_last = tk == gridDim.x - 1;
-	}
-	__syncthreads();
-	if (!is_last) return false;
-	__threadfence();
-	double w[NV];
-#pragma unroll
-	for (int i = 0; i < NV; i++) w[i] = 0.0;
-	for (int blk = threadIdx.x; blk < gridDim.x; blk += blockDim.x)
-#pragma unroll
-		for (int i = 0; i < NV; i++) w[i] += __ldcg(&partials[blk * NV + i]);
-#pragma unroll
-	for (int i = 0; i < NV; i++)
-		for (int o = 16; o; o >>= 1) w[i] += __shfl_down_sync(0xffffffffu, w[i], o);
-	__syncthreads();
-	if (lane == 0)
-		for (int i = 0; i < NV; i++) sm[wid][i] = w[i];
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		for (int i = 0; i < NV; i++) {
-			double t = 0.0;
-			for (int k = 0; k < nw; k++) t += sm[k][i];
-			out[i] = t;
-		}
-		*ticket = 0u;
-	}
-	__syncthreads();
-	return true;
-}
 
 // ------------------------------------------------------------------ CG (Chronopoulos-Gear PCG)
 //
@@ -157,22 +95,6 @@ struct CgArgs {
 	int use_cond;  // launched inside the solve graph: drive its conditional nodes
 	int timing;    // measurement launches: ignore the stop flag, never set it
 };
-
-template <typename V> struct Vec2;
-template <> struct Vec2<double> { using T = double2; };
-template <> struct Vec2<float> { using T = float2; };
-
-template <typename V>
-__device__ __forceinline__ typename Vec2<V>::T ld2(const V* p, int i) {
-	return reinterpret_cast<const typename Vec2<V>::T*>(p)[i];
-}
-template <typename V>
-__device__ __forceinline__ void st2(V* p, int i, V a, V b) {
-	typename Vec2<V>::T t;
-	t.x = a;
-	t.y = b;
-	reinterpret_cast<typename Vec2<V>::T*>(p)[i] = t;
-}
 
 // 2x2 block k of the matrix: m0 m1 / m2 m3 (one 32-byte or 16-byte vector load)
 __device__ __forceinline__ void ld_block(const double* v, long k, double& m0, double& m1, double& m2, double& m3) {
@@ -647,6 +569,22 @@ __device__ __forceinline__ void df_st(float* v, int i, dfl a, dfl b) {
 	reinterpret_cast<float4*>(v)[i] = make_float4(a.hi, b.hi, a.lo, b.lo);
 }
 
+// z = M r in double-float: Jacobi (one float4 per node) or a 2x2 block (two)
+__device__ __forceinline__ void df_precond(const float* dinv, int block, int i, dfl r0, dfl r1, dfl& z0, dfl& z1) {
+	if (block) {
+		float4 const h = reinterpret_cast<const float4*>(dinv)[2 * i];
+		float4 const l = reinterpret_cast<const float4*>(dinv)[2 * i + 1];
+		z0 = df_add(df_mul({h.x, l.x}, r0), df_mul({h.y, l.y}, r1));
+		z1 = df_add(df_mul({h.z, l.z}, r0), df_mul({h.w, l.w}, r1));
+	}
+	else {
+		dfl d0, d1;
+		df_ld(dinv, i, d0, d1);
+		z0 = df_mul(d0, r0);
+		z1 = df_mul(d1, r1);
+	}
+}
+
 struct DfArgs {
 	int N;
 	const int* row_ptr;
@@ -654,7 +592,8 @@ struct DfArgs {
 	const float* hi;    // 2x2 blocks, FP32 rounding of the FP64 value
 	const float* lo;    // FP32 rounding of the remainder
 	const double* vals64;  // the FP64 matrix, for the replacement residuals
-	const float* dinv;  // per node, df pair layout
+	const float* dinv;  // per node, df pair layout: Jacobi (u_hi, v_hi, u_lo, v_lo); block (4 hi, 4 lo)
+	int block_pc;
 	const double* b;
 	float* x;           // df solution (converted to FP64 at the end)
 	double* x64;
@@ -674,14 +613,12 @@ struct DfArgs {
 };
 
 __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
-	DF bb2 = {0.f, 0.f};
 	double v[2] = {0.0, 0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		double2 const bb = ld2(a.b, i);
 		dfl const r0 = df_make(bb.x), r1 = df_make(bb.y);
-		dfl d0, d1;
-		df_ld(a.dinv, i, d0, d1);
-		dfl const u0 = df_mul(d0, r0), u1 = df_mul(d1, r1);
+		dfl u0, u1;
+		df_precond(a.dinv, a.block_pc, i, r0, r1, u0, u1);
 		dfl const z = {0.f, 0.f};
 		df_st(a.x, i, z, z);
 		df_st(a.r, i, r0, r1);
@@ -691,7 +628,6 @@ __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
 		v[0] += bb.x * bb.x + bb.y * bb.y;
 		v[1] += df_dbl(df_add(df_mul(r0, u0), df_mul(r1, u1)));
 	}
-	(void) bb2;
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
 		CgState* st = a.st;
@@ -723,11 +659,18 @@ __global__ void k_df_finish(DfArgs a) {
 	}
 }
 
-// Jacobi in double-float layout from the FP64 diagonal (1/d, or 0 if d == 0)
-__global__ void k_df_dinv(int N, const double* __restrict__ dinv64, float* __restrict__ dinv) {
+// FP64 preconditioner (Jacobi: 2 per node; block: 4 per node) in double-float layout
+__global__ void k_df_dinv(int N, const double* __restrict__ dinv64, float* __restrict__ dinv, int block) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
-	df_st(dinv, i, df_make(dinv64[2 * i]), df_make(dinv64[2 * i + 1]));
+	if (!block) {
+		df_st(dinv, i, df_make(dinv64[2 * i]), df_make(dinv64[2 * i + 1]));
+		return;
+	}
+	dfl m[4];
+	for (int k = 0; k < 4; k++) m[k] = df_make(dinv64[4 * i + k]);
+	reinterpret_cast<float4*>(dinv)[2 * i] = make_float4(m[0].hi, m[1].hi, m[2].hi, m[3].hi);
+	reinterpret_cast<float4*>(dinv)[2 * i + 1] = make_float4(m[0].lo, m[1].lo, m[2].lo, m[3].lo);
 }
 
 // ---------------------------------------------------------------- Hestenes-Stiefel, FP64 and double-float
@@ -938,17 +881,17 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_update(DfArgs a) {
 	dfl const alpha = df_make(st->alpha), nalpha = df_neg(alpha);
 	double v[2] = {0.0, 0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		dfl pn0, pn1, q0, q1, r0, r1, x0, x1, d0, d1;
+		dfl pn0, pn1, q0, q1, r0, r1, x0, x1;
 		df_ld(a.s, i, pn0, pn1);
 		df_ld(a.w, i, q0, q1);
 		df_ld(a.r, i, r0, r1);
 		df_ld(a.x, i, x0, x1);
-		df_ld(a.dinv, i, d0, d1);
 		df_st(a.x, i, df_fma(alpha, pn0, x0), df_fma(alpha, pn1, x1));
 		r0 = df_fma(nalpha, q0, r0);
 		r1 = df_fma(nalpha, q1, r1);
 		df_st(a.r, i, r0, r1);
-		dfl const z0 = df_mul(d0, r0), z1 = df_mul(d1, r1);
+		dfl z0, z1;
+		df_precond(a.dinv, a.block_pc, i, r0, r1, z0, z1);
 		df_st(a.u, i, z0, z1);
 		v[0] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));
 		v[1] += df_dbl(df_add(df_mul(r0, r0), df_mul(r1, r1)));
@@ -986,9 +929,8 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_replace(DfArgs a) {
 			double const e0 = bb.x - y0, e1 = bb.y - y1;
 			dfl const r0 = df_make(e0), r1 = df_make(e1);
 			df_st(a.r, row, r0, r1);
-			dfl d0, d1;
-			df_ld(a.dinv, row, d0, d1);
-			dfl const z0 = df_mul(d0, r0), z1 = df_mul(d1, r1);
+			dfl z0, z1;
+			df_precond(a.dinv, a.block_pc, row, r0, r1, z0, z1);
 			df_st(a.u, row, z0, z1);
 			v[0] += e0 * e0 + e1 * e1;
 			v[1] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));

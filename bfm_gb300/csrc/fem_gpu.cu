@@ -296,7 +296,7 @@ struct AsmArgs {
 };
 
 __device__ __forceinline__ void store_precond(const AsmArgs& a, int r, double k00, double k01, double k10, double k11) {
-	if (a.precond == BFM_GPU_PC_BLOCK_JACOBI) {
+	if (a.precond != BFM_GPU_PC_JACOBI) {  // block Jacobi; also the starting blocks of the learned one
 		double const det = k00 * k11 - k01 * k10;
 		double const id = det != 0.0 ? 1.0 / det : 0.0;
 		double const m0 = k11 * id, m1 = -k01 * id, m2 = -k10 * id, m3 = k00 * id;
@@ -822,6 +822,62 @@ __global__ void k_edge_loads(int N, const int* __restrict__ ledges, const double
 	if (last_ci[2 * r + 1] < 0) b[2 * r + 1] += add1;
 }
 
+// Per-node 2x2 preconditioner blocks into the layout of the iteration:
+// 0 FP64 (4 doubles), 1 FP32 (4 floats), 2 double-float (4 hi, then 4 lo).
+// blocks == nullptr: Jacobi blocks from the diagonal of the operator.
+__global__ void k_store_blocks(int N, const double* __restrict__ blocks, const int* __restrict__ row_ptr,
+                               const int* __restrict__ cols, const double* __restrict__ v64, const float* __restrict__ v32,
+                               int layout, double* __restrict__ dinv64, float* __restrict__ dinv32) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double m[4];
+	if (blocks) {
+		for (int k = 0; k < 4; k++) m[k] = blocks[4l * i + k];
+	}
+	else {
+		double k00 = 0.0, k11 = 0.0;
+		for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++)
+			if (cols[k] == i) {
+				k00 = v64 ? v64[4l * k] : (double) v32[4l * k];
+				k11 = v64 ? v64[4l * k + 3] : (double) v32[4l * k + 3];
+			}
+		m[0] = k00 != 0.0 ? 1.0 / k00 : 0.0;
+		m[1] = m[2] = 0.0;
+		m[3] = k11 != 0.0 ? 1.0 / k11 : 0.0;
+	}
+	if (layout == 0) {
+		for (int k = 0; k < 4; k++) dinv64[4l * i + k] = m[k];
+	}
+	else if (layout == 1) {
+		for (int k = 0; k < 4; k++) dinv32[4l * i + k] = (float) m[k];
+	}
+	else {
+		float h[4], l[4];
+		for (int k = 0; k < 4; k++) {
+			h[k] = (float) m[k];
+			l[k] = (float) (m[k] - (double) h[k]);
+		}
+		reinterpret_cast<float4*>(dinv32)[2l * i] = make_float4(h[0], h[1], h[2], h[3]);
+		reinterpret_cast<float4*>(dinv32)[2l * i + 1] = make_float4(l[0], l[1], l[2], l[3]);
+	}
+}
+
+// y = K x with the FP64 operator (one thread per block row)
+__global__ void k_apply64(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, const double* __restrict__ vals,
+                          const double* __restrict__ x, double* __restrict__ y) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double y0 = 0.0, y1 = 0.0;
+	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+		int const c = cols[k];
+		double const x0 = x[2l * c], x1 = x[2l * c + 1];
+		y0 += vals[4l * k] * x0 + vals[4l * k + 1] * x1;
+		y1 += vals[4l * k + 2] * x0 + vals[4l * k + 3] * x1;
+	}
+	y[2l * i] = y0;
+	y[2l * i + 1] = y1;
+}
+
 }  // namespace
 
 #include "cg_kernels.cuh"
@@ -829,6 +885,9 @@ __global__ void k_edge_loads(int N, const int* __restrict__ ledges, const double
 namespace {
 
 int g_num_sms = 0;
+
+// A learned solve that stagnates above this relative residual is redone with Jacobi
+constexpr double LEARNED_FALLBACK_REL = 1e-6;
 
 int num_sms() {
 	if (!g_num_sms) {
@@ -905,6 +964,7 @@ struct bfm_gpu_problem {
 
 	cudaEvent_t ev[4];
 	bool assembled, solved;
+	int fallback;  // the last learned solve was taken over by Jacobi
 
 	// per-edge tractions (extension of the Neumann conditions)
 	int n_loads, cap_loads;
@@ -993,7 +1053,7 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		a.corr = P->corr32;
 		a.vals64 = P->precision == BFM_GPU_MIXED_EXACT ? P->vals64 : nullptr;
 	}
-	a.block_pc = P->precond == BFM_GPU_PC_BLOCK_JACOBI;
+	a.block_pc = P->precond != BFM_GPU_PC_JACOBI;
 	a.b = P->b;
 	a.x = P->x;
 	a.r = (V*) P->vec[0];
@@ -1023,6 +1083,7 @@ DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	a.lo = P->vals32lo;
 	a.vals64 = P->vals64;
 	a.dinv = P->dinv32;
+	a.block_pc = P->precond != BFM_GPU_PC_JACOBI;
 	a.b = P->b;
 	a.x = (float*) P->vec[5];
 	a.x64 = P->x;
@@ -1502,6 +1563,8 @@ int bfmi_buffers(bfm_gpu_problem_t* P, bfmi_buffers_t* o) {
 	o->corr32 = P->corr32;
 	o->dinv32 = P->dinv32;
 	o->vals64 = P->precision == BFM_GPU_MIXED_EXACT || P->precision == BFM_GPU_FP64 ? P->vals64 : nullptr;
+	o->vals64_any = P->precision != BFM_GPU_MIXED ? P->vals64 : nullptr;
+	o->dinv64 = P->dinv64;
 	o->b = P->b;
 	o->x = P->x;
 	for (int i = 0; i < 5; i++) o->vec[i] = P->vec[i];
@@ -1512,6 +1575,54 @@ int bfmi_buffers(bfm_gpu_problem_t* P, bfmi_buffers_t* o) {
 void** bfmi_ext_slot(bfm_gpu_problem_t* P, void (**free_fn)(void*)) {
 	if (free_fn) P->ext_free = *free_fn;
 	return &P->ext;
+}
+
+int bfmi_mesh(bfm_gpu_problem_t* P, bfmi_mesh_t* o) {
+	memset(o, 0, sizeof *o);
+	o->coords = P->coords;
+	o->inc_ptr = P->inc_ptr;
+	o->inc = P->inc;
+	o->elemE = P->has_elemE ? P->elemE : nullptr;
+	o->elemNu = P->has_elemNu ? P->elemNu : nullptr;
+	o->E = P->E;
+	o->nu = P->nu;
+	o->last_ci = P->last_ci;
+	return 0;
+}
+
+int bfmi_set_precond_blocks(bfm_gpu_problem_t* P, const double* blocks) {
+	if (!P->assembled) return fail("assemble before setting the preconditioner");
+	int const layout = P->precision == BFM_GPU_FP64 ? 0 : P->precision == BFM_GPU_FP64_DF ? 2 : 1;
+	k_store_blocks<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, blocks, P->row_ptr, P->cols,
+	                                                        P->precision != BFM_GPU_MIXED ? P->vals64 : nullptr, P->vals32,
+	                                                        layout, P->dinv64, P->dinv32);
+	CK(cudaGetLastError());
+	return 0;
+}
+
+int bfm_gpu_problem_apply(bfm_gpu_problem_t* P, const double* x, double* y, int where) {
+	g_err[0] = 0;
+	if (!P->assembled) return fail("assemble before applying the operator");
+	if (P->precision == BFM_GPU_MIXED) return fail("the FP64 operator is not assembled in the MIXED precision");
+	long const n = 2l * P->N;
+	const double* dx = x;
+	double* dy = y;
+	double* tmp = nullptr;
+	if (where != BFM_GPU_DEVICE) {
+		if (dalloc(&tmp, 2 * n)) return -1;
+		CK(cudaMemcpyAsync(tmp, x, n * sizeof(double), cudaMemcpyHostToDevice, P->stream));
+		dx = tmp;
+		dy = tmp + n;
+	}
+	k_apply64<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, P->row_ptr, P->cols, P->vals64, dx, dy);
+	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess && tmp) {
+		e = cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, P->stream);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+	}
+	if (tmp) cudaFree(tmp);
+	if (e != cudaSuccess) return fail("CUDA error %s in bfm_gpu_problem_apply", cudaGetErrorString(e));
+	return 0;
 }
 
 int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
@@ -1528,7 +1639,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (want64 && !P->vals64 && dalloc(&P->vals64, 4 * P->nb_cap)) return -1;
 	if (want32 && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
 	if ((!want32 || dfp) && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
-	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 4 * N)) return -1;
+	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 8 * N)) return -1;  // up to a double-float 2x2 block per node
 	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
 	if (dfp && !P->vals32lo && dalloc(&P->vals32lo, 4 * P->nb_cap)) return -1;
 	// 16 bytes per node per vector for FP64 and double-float, 8 for the mixed FP32 vectors
@@ -1592,7 +1703,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.err = P->err;
 	if (precision != BFM_GPU_MIXED) {
 		k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
-		if (dfp) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32);
+		if (dfp) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32, P->precond != BFM_GPU_PC_JACOBI);
 	}
 	else {
 		k_assemble32<12><<<blocks_for(N, 128), 128, 0, st>>>(a);
@@ -1641,7 +1752,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	if (opts) o = *opts;
 	else bfm_gpu_default_opts(&o);
 	if (!(o.rtol >= 0.0) || o.max_iters < 0) return fail("invalid solver options");
-	if (o.precond == BFM_GPU_PC_LEARNED) return fail("learned preconditioner not available in this build");
+	if (o.precond < BFM_GPU_PC_JACOBI || o.precond > BFM_GPU_PC_LEARNED) return fail("unknown preconditioner %d", o.precond);
 	if (o.precond != P->precond) {
 		// the preconditioner is formed by the assembly epilogue
 		P->precond = o.precond;
@@ -1663,8 +1774,26 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		P->graph_lpr = P->lpr;
 		P->graph_opts = o;
 	}
+	bool const learned = P->precond == BFM_GPU_PC_LEARNED;
+	P->fallback = 0;
 	CK(cudaEventRecord(P->ev[2], P->stream));
+	// the learned blocks depend on the load vector: formed for every solve, inside the timed region
+	if (learned && bfmi_learned_precond(P, 0)) return -1;
 	CK(cudaGraphLaunch(P->graph, P->stream));
+	if (learned) {
+		// Jacobi takes over when the learned preconditioner breaks down (a non-SPD
+		// or non-finite block) or stagnates well above the roundoff floor
+		CK(cudaMemcpyAsync(P->st_host, P->st, sizeof(CgState), cudaMemcpyDeviceToHost, P->stream));
+		CK(cudaStreamSynchronize(P->stream));
+		CgState const* h = P->st_host;
+		double const rel = h->bnorm2 > 0 ? sqrt(h->true_res2 / h->bnorm2) : 0.0;
+		if (h->status == BFM_GPU_BREAKDOWN || !(rel == rel) ||
+		    (h->status == BFM_GPU_STAGNATED && rel > LEARNED_FALLBACK_REL)) {
+			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
+			CK(cudaGraphLaunch(P->graph, P->stream));
+			P->fallback = 1;
+		}
+	}
 	CK(cudaEventRecord(P->ev[3], P->stream));
 	P->solved = true;
 	return 0;
@@ -1697,6 +1826,7 @@ int bfm_gpu_problem_stats(bfm_gpu_problem_t* P, bfm_gpu_stats_t* s) {
 		s->iterations = h->iter;
 		s->replacements = h->replacements;
 		s->rel_residual = h->bnorm2 > 0 ? sqrt(h->true_res2 / h->bnorm2) : 0.0;
+		s->fallback = P->fallback;
 	}
 	return 0;
 }

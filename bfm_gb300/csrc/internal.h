@@ -17,13 +17,38 @@ typedef struct {
 	const int* cols;
 	const float* vals32;
 	const float* corr32;
-	const float* dinv32;
-	const double* vals64;
+	const double* vals64;     /* FP64 operator of the FP64 and MIXED_EXACT iterations */
+	const double* vals64_any; /* FP64 values whenever this precision assembled them   */
+	double* dinv64;           /* preconditioner arrays (layout: bfmi_set_precond_blocks) */
+	float* dinv32;
 	const double* b;
 	double* x;
 	void* vec[5];
 	void* stream;
 } bfmi_buffers_t;
+
+/* Mesh-side device arrays of a problem (read only). */
+typedef struct {
+	const double* coords;
+	const int* inc_ptr;  /* node -> incident elements, ascending */
+	const int* inc;
+	const double* elemE; /* nullptr: uniform E */
+	const double* elemNu;
+	double E, nu;
+	const int* last_ci;  /* per DOF: index of its last Dirichlet condition, -1 if free */
+} bfmi_mesh_t;
+
+__attribute__((visibility("hidden"))) int bfmi_mesh(struct bfm_gpu_problem* P, bfmi_mesh_t* out);
+
+/* Preconditioner of the next solve from per-node 2x2 blocks (4 doubles per
+ * node, device, on the problem's stream), stored in the layout of the
+ * assembled precision.  Used by the learned preconditioner. */
+__attribute__((visibility("hidden"))) int bfmi_set_precond_blocks(struct bfm_gpu_problem* P, const double* blocks);
+
+/* Learned preconditioner blocks of the selected network for an assembled
+ * problem, written with bfmi_set_precond_blocks; jacobi != 0 writes the
+ * Jacobi blocks instead (the fallback), without a network. */
+__attribute__((visibility("hidden"))) int bfmi_learned_precond(struct bfm_gpu_problem* P, int jacobi);
 
 __attribute__((visibility("hidden"))) int bfmi_buffers(struct bfm_gpu_problem* P, bfmi_buffers_t* out);
 

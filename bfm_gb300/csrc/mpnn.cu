@@ -1,0 +1,856 @@
+// Learned block preconditioner of the GB300 libbfm: a message-passing network
+// over the mesh's node graph that predicts one SPD 2x2 block per node,
+//     B_i = S_i (I + C_i) S_i,  S_i = diag(K_ii)^(-1/2),  C_i = [[c0, c1], [c1, c2]],
+// used in place of the Jacobi diagonal inside PCG (c = 0 is exactly Jacobi,
+// which is where an untrained network starts).  No counterpart in the
+// reference; its CPU oracle is oracle/mpnn_ref.py.
+//
+// Network: h0 = relu(W0 f + b0) (16 -> 64); three layers
+// h = relu(W [h, mean_nbr(h)] + b) (128 -> 64); head c = 0.45 tanh(Wo h + bo)
+// (64 -> 3).  Weights are FP32 masters with BF16 copies; the dense layers of
+// the forward pass and both GEMMs of each layer's backward pass (dX and dW)
+// run on the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32
+// accumulation).  Everything per node is deterministic: split-K partials are
+// reduced in block order.
+//
+// Training loss of one (residual r, error e) pair, z = B r:
+//     L = 1 - (z.r)^2 / ((z.K z)(e.r)),
+// one minus the A-norm reduction of e by the optimal step along z.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <bfm/gpu.h>
+
+#include "internal.h"
+#include "reduce.cuh"
+
+namespace {
+
+constexpr int FIN = 16, HID = 64, HK = 128;
+constexpr int NPARAM = HID * FIN + HID + 3 * (HID * HK + HID) + 3 * HID + 3;
+// offsets of the parameter blocks, in the oracle's order
+constexpr int O_W0 = 0, O_B0 = O_W0 + HID * FIN, O_W1 = O_B0 + HID;
+constexpr int O_WO = O_W1 + 3 * (HID * HK + HID), O_BO = O_WO + 3 * HID;
+__host__ __device__ constexpr int o_w(int l) { return O_W1 + (l - 1) * (HID * HK + HID); }  // l = 1..3
+__host__ __device__ constexpr int o_b(int l) { return o_w(l) + HID * HK; }
+constexpr float C_SCALE = 0.45f;
+constexpr int MT = 128;        // threads per block of the tensor-core kernels
+constexpr int TILE = 64;       // nodes per tile
+constexpr int DW_CHUNK = 2048; // nodes per block in the weight-gradient reduction
+constexpr int FEAT_GRID = 256; // blocks of the reduction kernels
+
+thread_local char g_merr[512];
+
+int mfail(const char* fmt, ...) {
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(g_merr, sizeof g_merr, fmt, ap);
+	va_end(ap);
+	bfm_gpu_set_last_error(g_merr);
+	return -1;
+}
+
+#define MCK(call)                                                                                     \
+	do {                                                                                              \
+		cudaError_t const e_ = (call);                                                                \
+		if (e_ != cudaSuccess) return mfail("CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
+	} while (0)
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
+	return (uint32_t) __bfloat16_as_ushort(lo) | ((uint32_t) __bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], uint32_t const (&a)[4], uint32_t b0, uint32_t b1) {
+	asm volatile(
+		"mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+		: "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+		: "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// One warp: acc[j] (16 x 8 tile j) += A(16 x K) B(K x 8j..8j+7).  The
+// accessors return operand elements from shared memory, so transposed
+// operands cost nothing; fragments follow the m16n8k16 register layout
+// (group g = lane/4, thread t = lane%4).
+template <int NT, typename FA, typename FB>
+__device__ __forceinline__ void warp_gemm(float (&acc)[NT][4], int K, FA at_a, FB at_b) {
+	int const lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	for (int k0 = 0; k0 < K; k0 += 16) {
+		int const k1 = k0 + 2 * t;
+		uint32_t a[4];
+		a[0] = pack2(at_a(g, k1), at_a(g, k1 + 1));
+		a[1] = pack2(at_a(g + 8, k1), at_a(g + 8, k1 + 1));
+		a[2] = pack2(at_a(g, k1 + 8), at_a(g, k1 + 9));
+		a[3] = pack2(at_a(g + 8, k1 + 8), at_a(g + 8, k1 + 9));
+#pragma unroll
+		for (int j = 0; j < NT; j++) {
+			int const n = 8 * j + g;
+			mma16816(acc[j], a, pack2(at_b(k1, n), at_b(k1 + 1, n)), pack2(at_b(k1 + 8, n), at_b(k1 + 9, n)));
+		}
+	}
+}
+
+struct MpnnDev {
+	float* theta;   // FP32 masters
+	float* grad;
+	float* adam_m;
+	float* adam_v;
+	bf16* wb;       // BF16 copies, same offsets as theta (biases unused)
+	double* gpart;  // split-K partials of the weight gradients
+	long gpart_cap;
+};
+
+// ---------------------------------------------------------------- features
+
+struct FeatArgs {
+	int N, kind, n_elems;
+	const int* inc_ptr;
+	const int* inc;
+	const double* elemE;
+	const double* elemNu;
+	double E, nu;
+	const int* row_ptr;
+	const int* cols;
+	const double* vals64;
+	const float* vals32;
+	const int* last_ci;
+	const double* b;
+	double* scratch;   // N doubles: per-node log10 E, then reductions
+	double* partials;
+	unsigned* ticket;
+	double* rms;       // (Dinv b) root-mean-square
+	bf16* f;           // N x FIN
+};
+
+__device__ __forceinline__ void diag_block(const FeatArgs& a, int r, double& k00, double& k01, double& k11) {
+	k00 = k11 = 1.0;
+	k01 = 0.0;
+	for (int k = a.row_ptr[r]; k < a.row_ptr[r + 1]; k++)
+		if (a.cols[k] == r) {
+			k00 = a.vals64 ? a.vals64[4l * k] : (double) a.vals32[4l * k];
+			k01 = a.vals64 ? a.vals64[4l * k + 1] : (double) a.vals32[4l * k + 1];
+			k11 = a.vals64 ? a.vals64[4l * k + 3] : (double) a.vals32[4l * k + 3];
+		}
+}
+
+// per node: mean log10 E of the incident elements; RMS of Dinv b
+__global__ void k_feat1(FeatArgs a) {
+	double v[1] = {0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		double s = 0.0;
+		int const s0 = a.inc_ptr[i], s1 = a.inc_ptr[i + 1];
+		for (int t = s0; t < s1; t++) s += log10(a.elemE ? a.elemE[a.inc[t]] : a.E);
+		a.scratch[i] = s1 > s0 ? s / (s1 - s0) : log10(a.E);
+		double k00, k01, k11;
+		diag_block(a, i, k00, k01, k11);
+		double2 const bb = ld2(a.b, i);
+		double const z0 = k00 != 0.0 ? bb.x / k00 : 0.0, z1 = k11 != 0.0 ? bb.y / k11 : 0.0;
+		v[0] += z0 * z0 + z1 * z1;
+	}
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) a.rms[0] = sqrt(out[0] / (2.0 * (a.N > 0 ? a.N : 1)));
+}
+
+__global__ void k_feat2(FeatArgs a) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.N) return;
+	float f[FIN];
+	for (int k = 0; k < FIN; k++) f[k] = 0.f;
+	int const r0 = a.row_ptr[i], r1 = a.row_ptr[i + 1];
+	double nb = 0.0;
+	for (int k = r0; k < r1; k++) nb += a.scratch[a.cols[k]];
+	nb /= (r1 - r0);
+	double nu = 0.0, lmin = 0.0, lmax = 0.0;
+	int const s0 = a.inc_ptr[i], s1 = a.inc_ptr[i + 1];
+	for (int t = s0; t < s1; t++) {
+		nu += a.elemNu ? a.elemNu[a.inc[t]] : a.nu;
+		double const le = log10(a.elemE ? a.elemE[a.inc[t]] : a.E);
+		lmin = t == s0 ? le : fmin(lmin, le);
+		lmax = t == s0 ? le : fmax(lmax, le);
+	}
+	nu = s1 > s0 ? nu / (s1 - s0) : a.nu;
+	double k00, k01, k11;
+	diag_block(a, i, k00, k01, k11);
+	double2 const bb = ld2(a.b, i);
+	double const rms = a.rms[0] > 0.0 ? a.rms[0] : 1.0;
+	double const z0 = (k00 != 0.0 ? bb.x / k00 : 0.0) / rms, z1 = (k11 != 0.0 ? bb.y / k11 : 0.0) / rms;
+	f[0] = (float) (a.scratch[i] - nb);
+	f[1] = (float) ((nu - 0.3) * 10.0);
+	f[2] = a.last_ci[2 * i] >= 0 ? 1.f : 0.f;
+	f[3] = a.last_ci[2 * i + 1] >= 0 ? 1.f : 0.f;
+	f[4] = (float) (r1 - r0) / 9.f;
+	f[5] = (float) z0;
+	f[6] = (float) z1;
+	f[7] = (k00 > 0.0 && k11 > 0.0) ? (float) log10(k00 / k11) : 0.f;
+	f[8] = (k00 > 0.0 && k11 > 0.0) ? (float) (k01 / sqrt(k00 * k11)) : 0.f;
+	f[9] = (float) (fabs(z0) + fabs(z1));
+	f[10] = (float) (lmin - lmax);
+	for (int k = 0; k < FIN; k++) a.f[(long) i * FIN + k] = __float2bfloat16(f[k]);
+}
+
+// ---------------------------------------------------------------- forward
+
+// Y = relu(W [X0 | X1] + b): X0, X1 are N x 64 (or X0 alone N x 16), Y N x 64 BF16
+template <int K>
+__global__ void __launch_bounds__(MT) k_dense_fwd(int N, const bf16* __restrict__ x0, const bf16* __restrict__ x1,
+                                                  const bf16* __restrict__ w, const float* __restrict__ bias,
+                                                  bf16* __restrict__ y) {
+	__shared__ bf16 xs[TILE][K + 8];
+	__shared__ bf16 ws[HID][K + 8];
+	int const node0 = blockIdx.x * TILE;
+	for (int e = threadIdx.x; e < TILE * K; e += MT) {
+		int const n = e / K, k = e % K, node = node0 + n;
+		bf16 v = __float2bfloat16(0.f);
+		if (node < N) v = K == FIN ? x0[(long) node * FIN + k] : (k < HID ? x0[(long) node * HID + k] : x1[(long) node * HID + k - HID]);
+		xs[n][k] = v;
+	}
+	for (int e = threadIdx.x; e < HID * K; e += MT) ws[e / K][e % K] = w[e];
+	__syncthreads();
+	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	float acc[8][4] = {};
+	auto at_a = [&](int m, int k) { return xs[warp * 16 + m][k]; };
+	auto at_b = [&](int k, int n) { return ws[n][k]; };  // B(k, n) = W[n][k]
+	warp_gemm<8>(acc, K, at_a, at_b);
+#pragma unroll
+	for (int j = 0; j < 8; j++) {
+		int const n = 8 * j + 2 * t;
+#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			int const node = node0 + warp * 16 + g + 8 * h;
+			if (node >= N) continue;
+			float const v0 = fmaxf(acc[j][2 * h] + bias[n], 0.f), v1 = fmaxf(acc[j][2 * h + 1] + bias[n + 1], 0.f);
+			y[(long) node * HID + n] = __float2bfloat16(v0);
+			y[(long) node * HID + n + 1] = __float2bfloat16(v1);
+		}
+	}
+}
+
+// m_i = mean of h over the node's graph row (itself included)
+__global__ void k_agg(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, const bf16* __restrict__ h,
+                      bf16* __restrict__ m) {
+	int const i = blockIdx.x * (blockDim.x / HID) + threadIdx.x / HID, c = threadIdx.x % HID;
+	if (i >= N) return;
+	float s = 0.f;
+	int const r0 = row_ptr[i], r1 = row_ptr[i + 1];
+	for (int k = r0; k < r1; k++) s += __bfloat162float(h[(long) cols[k] * HID + c]);
+	m[(long) i * HID + c] = __float2bfloat16(s / (float) (r1 - r0));
+}
+
+// o = Wo h3 + bo, c = 0.45 tanh(o); the preconditioner blocks from c
+__global__ void k_head(int N, const bf16* __restrict__ h3, const float* __restrict__ theta, float* __restrict__ o,
+                       const int* __restrict__ row_ptr, const int* __restrict__ cols, const double* __restrict__ vals64,
+                       const float* __restrict__ vals32, double* __restrict__ blocks, double* __restrict__ scale2) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	float oo[3];
+	for (int q = 0; q < 3; q++) {
+		float s = theta[O_BO + q];
+		for (int k = 0; k < HID; k++) s += theta[O_WO + q * HID + k] * __bfloat162float(h3[(long) i * HID + k]);
+		oo[q] = s;
+		if (o) o[3 * i + q] = s;
+	}
+	double k00 = 0.0, k11 = 0.0;
+	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++)
+		if (cols[k] == i) {
+			k00 = vals64 ? vals64[4l * k] : (double) vals32[4l * k];
+			k11 = vals64 ? vals64[4l * k + 3] : (double) vals32[4l * k + 3];
+		}
+	double const s0 = k00 > 0.0 ? 1.0 / sqrt(k00) : 0.0, s1 = k11 > 0.0 ? 1.0 / sqrt(k11) : 0.0;
+	scale2[2 * i] = s0 * s0;
+	scale2[2 * i + 1] = s1 * s1;
+	double const c0 = C_SCALE * tanh((double) oo[0]), c1 = C_SCALE * tanh((double) oo[1]), c2 = C_SCALE * tanh((double) oo[2]);
+	blocks[4 * i + 0] = s0 * s0 * (1.0 + c0);
+	blocks[4 * i + 1] = s0 * s1 * c1;
+	blocks[4 * i + 2] = s0 * s1 * c1;
+	blocks[4 * i + 3] = s1 * s1 * (1.0 + c2);
+}
+
+// ---------------------------------------------------------------- loss
+
+struct LossArgs {
+	int N;
+	const int* row_ptr;
+	const int* cols;
+	const double* vals64;
+	const double* blocks;
+	const double* r;
+	const double* e;
+	double* z;
+	double* az;
+	double* partials;
+	unsigned* ticket;
+	double* sc;  // zr, zAz, er, loss
+};
+
+__global__ void k_loss_z(LossArgs a) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.N) return;
+	double2 const r = ld2(a.r, i);
+	const double* B = a.blocks + 4l * i;
+	st2(a.z, i, B[0] * r.x + B[1] * r.y, B[2] * r.x + B[3] * r.y);
+}
+
+__global__ void k_loss_dots(LossArgs a) {
+	double v[3] = {0.0, 0.0, 0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		double y0 = 0.0, y1 = 0.0;
+		for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
+			double2 const zc = ld2(a.z, a.cols[k]);
+			const double* m = a.vals64 + 4l * k;
+			y0 += m[0] * zc.x + m[1] * zc.y;
+			y1 += m[2] * zc.x + m[3] * zc.y;
+		}
+		st2(a.az, i, y0, y1);
+		double2 const z = ld2(a.z, i), r = ld2(a.r, i), e = ld2(a.e, i);
+		v[0] += z.x * r.x + z.y * r.y;
+		v[1] += z.x * y0 + z.y * y1;
+		v[2] += e.x * r.x + e.y * r.y;
+	}
+	double out[3];
+	if (grid_sum<3>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		a.sc[0] = out[0];
+		a.sc[1] = out[1];
+		a.sc[2] = out[2];
+		a.sc[3] = 1.0 - out[0] * out[0] / (out[1] * out[2]);
+	}
+}
+
+// dL/dz = (2 zr / (zAz er)) ((zr/zAz) Az - r) -> dL/dc -> dL/do (N x 3, FP32)
+__global__ void k_loss_back(LossArgs a, const float* __restrict__ o, const double* __restrict__ scale2, float* __restrict__ d_o) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.N) return;
+	double const zr = a.sc[0], zaz = a.sc[1], er = a.sc[2];
+	double const f = 2.0 * zr / (zaz * er), q = zr / zaz;
+	double2 const az = ld2(a.az, i), r = ld2(a.r, i);
+	double const g0 = f * (q * az.x - r.x), g1 = f * (q * az.y - r.y);
+	double const t0 = tanh((double) o[3 * i]), t1 = tanh((double) o[3 * i + 1]), t2 = tanh((double) o[3 * i + 2]);
+	double const s00 = scale2[2 * i], s11 = scale2[2 * i + 1], s01 = sqrt(s00 * s11);
+	double const dc0 = g0 * s00 * r.x;
+	double const dc1 = g0 * s01 * r.y + g1 * s01 * r.x;
+	double const dc2 = g1 * s11 * r.y;
+	d_o[3 * i + 0] = (float) (dc0 * C_SCALE * (1.0 - t0 * t0));
+	d_o[3 * i + 1] = (float) (dc1 * C_SCALE * (1.0 - t1 * t1));
+	d_o[3 * i + 2] = (float) (dc2 * C_SCALE * (1.0 - t2 * t2));
+}
+
+// ---------------------------------------------------------------- backward
+
+// head: dh3 = do Wo (FP32 N x 64); per-block partial sums of dWo = do^T h3
+// and dbo (thread t < 195 owns one output, nodes summed in ascending order)
+constexpr int HEAD_TPB = 256, HEAD_NODES = 256, HEAD_OUT = 3 * HID + 3;
+__global__ void __launch_bounds__(HEAD_TPB) k_head_back(int N, const float* __restrict__ d_o, const bf16* __restrict__ h3,
+                                                        const float* __restrict__ theta, float* __restrict__ dh,
+                                                        double* __restrict__ part) {
+	int const i0 = blockIdx.x * HEAD_NODES, i1 = min(N, i0 + HEAD_NODES);
+	for (int e = threadIdx.x; e < (i1 - i0) * HID; e += HEAD_TPB) {
+		int const i = i0 + e / HID, k = e % HID;
+		dh[(long) i * HID + k] = d_o[3 * i] * theta[O_WO + k] + d_o[3 * i + 1] * theta[O_WO + HID + k] +
+		                         d_o[3 * i + 2] * theta[O_WO + 2 * HID + k];
+	}
+	int const t = threadIdx.x;
+	if (t < HEAD_OUT) {
+		double acc = 0.0;
+		if (t < 3 * HID) {
+			int const q = t / HID, k = t % HID;
+			for (int i = i0; i < i1; i++) acc += (double) d_o[3 * i + q] * (double) __bfloat162float(h3[(long) i * HID + k]);
+		}
+		else {
+			for (int i = i0; i < i1; i++) acc += (double) d_o[3 * i + t - 3 * HID];
+		}
+		part[(long) blockIdx.x * HEAD_OUT + t] = acc;
+	}
+}
+
+// dpre = dh * (h > 0), as BF16 (the tensor-core operand)
+__global__ void k_relu_back(long n, const float* __restrict__ dh, const bf16* __restrict__ h, bf16* __restrict__ dpre) {
+	for (long e = blockIdx.x * (long) blockDim.x + threadIdx.x; e < n; e += (long) gridDim.x * blockDim.x)
+		dpre[e] = __float2bfloat16(__bfloat162float(h[e]) > 0.f ? dh[e] : 0.f);
+}
+
+// dX (N x 128, FP32) = dpre (N x 64) W (64 x 128)
+__global__ void __launch_bounds__(MT) k_dense_dx(int N, const bf16* __restrict__ dpre, const bf16* __restrict__ w,
+                                                 float* __restrict__ dx) {
+	__shared__ bf16 ps[TILE][HID + 8];
+	__shared__ bf16 ws[HID][HK + 8];
+	int const node0 = blockIdx.x * TILE;
+	for (int e = threadIdx.x; e < TILE * HID; e += MT) {
+		int const n = e / HID, k = e % HID, node = node0 + n;
+		ps[n][k] = node < N ? dpre[(long) node * HID + k] : __float2bfloat16(0.f);
+	}
+	for (int e = threadIdx.x; e < HID * HK; e += MT) ws[e / HK][e % HK] = w[e];
+	__syncthreads();
+	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	float acc[16][4] = {};
+	auto at_a = [&](int m, int k) { return ps[warp * 16 + m][k]; };
+	auto at_b = [&](int k, int n) { return ws[k][n]; };  // B(k=out, n=in) = W[out][in]
+	warp_gemm<16>(acc, HID, at_a, at_b);
+#pragma unroll
+	for (int j = 0; j < 16; j++) {
+		int const n = 8 * j + 2 * t;
+#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			int const node = node0 + warp * 16 + g + 8 * h;
+			if (node >= N) continue;
+			dx[(long) node * HK + n] = acc[j][2 * h];
+			dx[(long) node * HK + n + 1] = acc[j][2 * h + 1];
+		}
+	}
+}
+
+// Partial weight gradient of one block of nodes: dW (64 x K) = dpre^T [X0 | X1],
+// plus the bias gradient column sums, on the tensor cores.
+template <int K>
+__global__ void __launch_bounds__(MT) k_dense_dw(int N, const bf16* __restrict__ dpre, const bf16* __restrict__ x0,
+                                                 const bf16* __restrict__ x1, double* __restrict__ part) {
+	__shared__ bf16 ps[TILE][HID + 8];
+	__shared__ bf16 xs[TILE][K + 8];
+	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	constexpr int NT = K / 8;
+	float acc[NT][4] = {};
+	float bsum = 0.f;
+	int const c0 = blockIdx.x * DW_CHUNK, c1 = min(N, c0 + DW_CHUNK);
+	for (int node0 = c0; node0 < c1; node0 += TILE) {
+		__syncthreads();
+		for (int e = threadIdx.x; e < TILE * HID; e += MT) {
+			int const n = e / HID, k = e % HID, node = node0 + n;
+			ps[n][k] = node < c1 ? dpre[(long) node * HID + k] : __float2bfloat16(0.f);
+		}
+		for (int e = threadIdx.x; e < TILE * K; e += MT) {
+			int const n = e / K, k = e % K, node = node0 + n;
+			bf16 v = __float2bfloat16(0.f);
+			if (node < c1) v = K == FIN ? x0[(long) node * FIN + k] : (k < HID ? x0[(long) node * HID + k] : x1[(long) node * HID + k - HID]);
+			xs[n][k] = v;
+		}
+		__syncthreads();
+		auto at_a = [&](int m, int k) { return ps[k][warp * 16 + m]; };  // A(m=out, k=node)
+		auto at_b = [&](int k, int n) { return xs[k][n]; };              // B(k=node, n=in)
+		warp_gemm<NT>(acc, TILE, at_a, at_b);
+		if (threadIdx.x < HID)
+			for (int n = 0; n < TILE; n++) bsum += __bfloat162float(ps[n][threadIdx.x]);
+	}
+	double* out = part + (long) blockIdx.x * (HID * K + HID);
+#pragma unroll
+	for (int j = 0; j < NT; j++) {
+		int const n = 8 * j + 2 * t;
+#pragma unroll
+		for (int h = 0; h < 2; h++) {
+			int const m = warp * 16 + g + 8 * h;
+			out[m * K + n] = acc[j][2 * h];
+			out[m * K + n + 1] = acc[j][2 * h + 1];
+		}
+	}
+	if (threadIdx.x < HID) out[HID * K + threadIdx.x] = bsum;
+}
+
+// grad[off + k] = sum over blocks of part[blk][k], in block order
+__global__ void k_reduce_parts(const double* __restrict__ part, int nblk, int len, float* __restrict__ grad, int off_w,
+                               int n_w, int off_b) {
+	int const k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= len) return;
+	double s = 0.0;
+	for (int b = 0; b < nblk; b++) s += part[(long) b * len + k];
+	if (k < n_w) grad[off_w + k] = (float) s;
+	else grad[off_b + k - n_w] = (float) s;
+}
+
+// dh_prev = dX[:, :64] + sum over the node's row of dX[j, 64:] / deg_j  (adjoint of the mean)
+__global__ void k_agg_back(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, const float* __restrict__ dx,
+                           float* __restrict__ dh) {
+	int const i = blockIdx.x * (blockDim.x / HID) + threadIdx.x / HID, c = threadIdx.x % HID;
+	if (i >= N) return;
+	float s = dx[(long) i * HK + c];
+	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+		int const j = cols[k];
+		s += dx[(long) j * HK + HID + c] / (float) (row_ptr[j + 1] - row_ptr[j]);
+	}
+	dh[(long) i * HID + c] = s;
+}
+
+__global__ void k_adam(int n, float* theta, const float* g, float* m, float* v, bf16* wb, float lr, float b1t, float b2t) {
+	int const k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	float const gk = g[k];
+	float const mk = 0.9f * m[k] + 0.1f * gk;
+	float const vk = 0.999f * v[k] + 0.001f * gk * gk;
+	m[k] = mk;
+	v[k] = vk;
+	float const th = theta[k] - lr * (mk / (1.f - b1t)) / (sqrtf(vk / (1.f - b2t)) + 1e-8f);
+	theta[k] = th;
+	wb[k] = __float2bfloat16(th);
+}
+
+__global__ void k_to_bf16(int n, const float* theta, bf16* wb) {
+	int const k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k < n) wb[k] = __float2bfloat16(theta[k]);
+}
+
+inline int nb(long n, int t = 256) { return (int) ((n + t - 1) / t) > 0 ? (int) ((n + t - 1) / t) : 1; }
+
+}  // namespace
+
+// ====================================================================== host side
+
+struct bfm_gpu_mpnn {
+	MpnnDev d;
+	int step;
+	// activations of the problem last seen
+	long cap_n;
+	bf16 *f, *h[4], *m[3], *dpre;
+	float *o, *d_o, *dh, *dx;
+	double *blocks, *scale2, *z, *az, *sc, *partials, *rms, *scratch;
+	unsigned* ticket;
+};
+
+namespace {
+
+void free_acts(bfm_gpu_mpnn* net) {
+	void* p[] = {net->f, net->h[0], net->h[1], net->h[2], net->h[3], net->m[0], net->m[1], net->m[2], net->dpre, net->o,
+	             net->d_o, net->dh, net->dx, net->blocks, net->scale2, net->z, net->az, net->scratch};
+	for (void* q : p)
+		if (q) cudaFree(q);
+	net->f = net->dpre = nullptr;
+	for (auto& q : net->h) q = nullptr;
+	for (auto& q : net->m) q = nullptr;
+	net->o = net->d_o = net->dh = net->dx = nullptr;
+	net->blocks = net->scale2 = net->z = net->az = net->scratch = nullptr;
+	net->cap_n = 0;
+}
+
+template <typename T>
+int alloc(T** p, long n) {
+	*p = nullptr;
+	cudaError_t const e = cudaMalloc((void**) p, (n > 0 ? n : 1) * sizeof(T));
+	if (e != cudaSuccess) return mfail("cudaMalloc of %ld bytes failed: %s", n * (long) sizeof(T), cudaGetErrorString(e));
+	return 0;
+}
+
+int ensure_acts(bfm_gpu_mpnn* net, long N) {
+	if (N <= net->cap_n) return 0;
+	free_acts(net);
+	long const n = N > 0 ? N : 1;
+	if (alloc(&net->f, n * FIN)) return -1;
+	for (auto& q : net->h)
+		if (alloc(&q, n * HID)) return -1;
+	for (auto& q : net->m)
+		if (alloc(&q, n * HID)) return -1;
+	if (alloc(&net->dpre, n * HID) || alloc(&net->o, n * 3) || alloc(&net->d_o, n * 3) || alloc(&net->dh, n * HID) ||
+	    alloc(&net->dx, n * HK) || alloc(&net->blocks, n * 4) || alloc(&net->scale2, n * 2) || alloc(&net->z, n * 2) ||
+	    alloc(&net->az, n * 2) || alloc(&net->scratch, n))
+		return -1;
+	long const chunks = (n + DW_CHUNK - 1) / DW_CHUNK, heads = (n + HEAD_NODES - 1) / HEAD_NODES;
+	long const need = chunks * (HID * HK + HID) > heads * HEAD_OUT ? chunks * (HID * HK + HID) : heads * HEAD_OUT;
+	if (need > net->d.gpart_cap) {
+		if (net->d.gpart) cudaFree(net->d.gpart);
+		net->d.gpart = nullptr;
+		if (alloc(&net->d.gpart, need)) return -1;
+		net->d.gpart_cap = need;
+	}
+	net->cap_n = N;
+	return 0;
+}
+
+// features and forward pass on the problem's stream; blocks and scales of every node
+int forward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, cudaStream_t st) {
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	bfmi_mesh_t ms;
+	bfmi_mesh(P, &ms);
+	if (!bf.assembled) return mfail("assemble the problem before running the network");
+	int const N = bf.N;
+	if (ensure_acts(net, N)) return -1;
+	FeatArgs fa;
+	memset(&fa, 0, sizeof fa);
+	fa.N = N;
+	fa.kind = bf.kind;
+	fa.inc_ptr = ms.inc_ptr;
+	fa.inc = ms.inc;
+	fa.elemE = ms.elemE;
+	fa.elemNu = ms.elemNu;
+	fa.E = ms.E;
+	fa.nu = ms.nu;
+	fa.row_ptr = bf.row_ptr;
+	fa.cols = bf.cols;
+	fa.vals64 = bf.vals64_any;
+	fa.vals32 = bf.vals32;
+	fa.last_ci = ms.last_ci;
+	fa.b = bf.b;
+	fa.scratch = net->scratch;
+	fa.partials = net->partials;
+	fa.ticket = net->ticket;
+	fa.rms = net->rms;
+	fa.f = net->f;
+	k_feat1<<<FEAT_GRID, TPB_K, 0, st>>>(fa);
+	k_feat2<<<nb(N), 256, 0, st>>>(fa);
+	int const tiles = (N + TILE - 1) / TILE > 0 ? (N + TILE - 1) / TILE : 1;
+	k_dense_fwd<FIN><<<tiles, MT, 0, st>>>(N, net->f, nullptr, net->d.wb + O_W0, net->d.theta + O_B0, net->h[0]);
+	for (int l = 1; l <= 3; l++) {
+		k_agg<<<nb((long) N * HID), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->h[l - 1], net->m[l - 1]);
+		k_dense_fwd<HK><<<tiles, MT, 0, st>>>(N, net->h[l - 1], net->m[l - 1], net->d.wb + o_w(l), net->d.theta + o_b(l),
+		                                      net->h[l]);
+	}
+	k_head<<<nb(N), 256, 0, st>>>(N, net->h[3], net->d.theta, net->o, bf.row_ptr, bf.cols, bf.vals64_any, bf.vals32,
+	                               net->blocks, net->scale2);
+	MCK(cudaGetLastError());
+	return 0;
+}
+
+// loss of the pair (r, e) and the gradient of every parameter into d.grad
+int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const double* e, cudaStream_t st) {
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	if (!bf.vals64_any) return mfail("training needs the FP64 operator: assemble in FP64, MIXED_EXACT or FP64_DF");
+	int const N = bf.N;
+	LossArgs la;
+	memset(&la, 0, sizeof la);
+	la.N = N;
+	la.row_ptr = bf.row_ptr;
+	la.cols = bf.cols;
+	la.vals64 = bf.vals64_any;
+	la.blocks = net->blocks;
+	la.r = r;
+	la.e = e;
+	la.z = net->z;
+	la.az = net->az;
+	la.partials = net->partials;
+	la.ticket = net->ticket;
+	la.sc = net->sc;
+	k_loss_z<<<nb(N), 256, 0, st>>>(la);
+	k_loss_dots<<<FEAT_GRID, TPB_K, 0, st>>>(la);
+	k_loss_back<<<nb(N), 256, 0, st>>>(la, net->o, net->scale2, net->d_o);
+	int const heads = (N + HEAD_NODES - 1) / HEAD_NODES > 0 ? (N + HEAD_NODES - 1) / HEAD_NODES : 1;
+	k_head_back<<<heads, HEAD_TPB, 0, st>>>(N, net->d_o, net->h[3], net->d.theta, net->dh, net->d.gpart);
+	k_reduce_parts<<<nb(HEAD_OUT), 256, 0, st>>>(net->d.gpart, heads, HEAD_OUT, net->d.grad, O_WO, 3 * HID, O_BO);
+	int const tiles = (N + TILE - 1) / TILE > 0 ? (N + TILE - 1) / TILE : 1;
+	int const chunks = (N + DW_CHUNK - 1) / DW_CHUNK > 0 ? (N + DW_CHUNK - 1) / DW_CHUNK : 1;
+	long const nh = (long) N * HID;
+	for (int l = 3; l >= 1; l--) {
+		k_relu_back<<<nb(nh), 256, 0, st>>>(nh, net->dh, net->h[l], net->dpre);
+		k_dense_dw<HK><<<chunks, MT, 0, st>>>(N, net->dpre, net->h[l - 1], net->m[l - 1], net->d.gpart);
+		k_reduce_parts<<<nb(HID * HK + HID), 256, 0, st>>>(net->d.gpart, chunks, HID * HK + HID, net->d.grad, o_w(l), HID * HK,
+		                                                    o_b(l));
+		k_dense_dx<<<tiles, MT, 0, st>>>(N, net->dpre, net->d.wb + o_w(l), net->dx);
+		k_agg_back<<<nb(nh), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->dx, net->dh);
+	}
+	k_relu_back<<<nb(nh), 256, 0, st>>>(nh, net->dh, net->h[0], net->dpre);
+	k_dense_dw<FIN><<<chunks, MT, 0, st>>>(N, net->dpre, net->f, nullptr, net->d.gpart);
+	k_reduce_parts<<<nb(HID * FIN + HID), 256, 0, st>>>(net->d.gpart, chunks, HID * FIN + HID, net->d.grad, O_W0, HID * FIN,
+	                                                     O_B0);
+	MCK(cudaGetLastError());
+	return 0;
+}
+
+int read_loss(bfm_gpu_mpnn* net, double* loss, cudaStream_t st) {
+	if (!loss) return 0;
+	double sc[4];
+	MCK(cudaMemcpyAsync(sc, net->sc, sizeof sc, cudaMemcpyDeviceToHost, st));
+	MCK(cudaStreamSynchronize(st));
+	*loss = sc[3];
+	return 0;
+}
+
+// He-normal weights from a fixed-seed generator (xorshift64 + Box-Muller),
+// zero biases and a zero head: c = 0, so an untrained network is exactly Jacobi
+void init_theta(float* th, unsigned seed) {
+	uint64_t s = 0x9E3779B97F4A7C15ull ^ ((uint64_t) seed * 0xD1B54A32D192ED03ull);
+	auto uni = [&]() {
+		s ^= s << 13;
+		s ^= s >> 7;
+		s ^= s << 17;
+		return ((double) (s >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+	};
+	auto normal = [&]() { return sqrt(-2.0 * log(uni())) * cos(6.283185307179586 * uni()); };
+	memset(th, 0, sizeof(float) * NPARAM);
+	for (int k = 0; k < HID * FIN; k++) th[O_W0 + k] = (float) (normal() * sqrt(2.0 / FIN));
+	for (int l = 1; l <= 3; l++)
+		for (int k = 0; k < HID * HK; k++) th[o_w(l) + k] = (float) (normal() * sqrt(2.0 / HK));
+}
+
+bfm_gpu_mpnn* g_active_net = nullptr;
+
+// weights file: magic, version, layer sizes, parameter count, FP32 parameters (little endian)
+constexpr char MAGIC[8] = {'B', 'F', 'M', 'M', 'P', 'N', 'N', '\0'};
+constexpr uint32_t FILE_VERSION = 1;
+
+}  // namespace
+
+extern "C" {
+
+int bfm_gpu_mpnn_param_count(void) { return NPARAM; }
+
+int bfm_gpu_mpnn_create(bfm_gpu_mpnn_t** out, unsigned seed) {
+	*out = nullptr;
+	bfm_gpu_mpnn* net = (bfm_gpu_mpnn*) calloc(1, sizeof *net);
+	if (!net) return mfail("out of host memory");
+	if (alloc(&net->d.theta, NPARAM) || alloc(&net->d.grad, NPARAM) || alloc(&net->d.adam_m, NPARAM) ||
+	    alloc(&net->d.adam_v, NPARAM) || alloc(&net->d.wb, NPARAM) || alloc(&net->sc, 4) ||
+	    alloc(&net->partials, 4 * FEAT_GRID) || alloc(&net->rms, 1) || alloc(&net->ticket, 1)) {
+		bfm_gpu_mpnn_destroy(net);
+		return -1;
+	}
+	float* th = (float*) malloc(NPARAM * sizeof(float));
+	if (!th) {
+		bfm_gpu_mpnn_destroy(net);
+		return mfail("out of host memory");
+	}
+	init_theta(th, seed);
+	cudaError_t e = cudaMemcpy(net->d.theta, th, NPARAM * sizeof(float), cudaMemcpyHostToDevice);
+	free(th);
+	if (e == cudaSuccess) e = cudaMemset(net->ticket, 0, sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMemset(net->d.adam_m, 0, NPARAM * sizeof(float));
+	if (e == cudaSuccess) e = cudaMemset(net->d.adam_v, 0, NPARAM * sizeof(float));
+	if (e == cudaSuccess) {
+		k_to_bf16<<<nb(NPARAM), 256>>>(NPARAM, net->d.theta, net->d.wb);
+		e = cudaDeviceSynchronize();
+	}
+	if (e != cudaSuccess) {
+		bfm_gpu_mpnn_destroy(net);
+		return mfail("CUDA error %s creating the network", cudaGetErrorString(e));
+	}
+	*out = net;
+	return 0;
+}
+
+int bfm_gpu_mpnn_destroy(bfm_gpu_mpnn_t* net) {
+	if (!net) return 0;
+	if (g_active_net == net) g_active_net = nullptr;
+	cudaDeviceSynchronize();
+	free_acts(net);
+	void* p[] = {net->d.theta, net->d.grad, net->d.adam_m, net->d.adam_v, net->d.wb, net->d.gpart, net->sc, net->partials,
+	             net->rms, net->ticket};
+	for (void* q : p)
+		if (q) cudaFree(q);
+	free(net);
+	return 0;
+}
+
+int bfm_gpu_mpnn_get_weights(bfm_gpu_mpnn_t* net, float* out) {
+	MCK(cudaMemcpy(out, net->d.theta, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+	return 0;
+}
+
+int bfm_gpu_mpnn_set_weights(bfm_gpu_mpnn_t* net, const float* in) {
+	MCK(cudaMemcpy(net->d.theta, in, NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+	MCK(cudaMemset(net->d.adam_m, 0, NPARAM * sizeof(float)));
+	MCK(cudaMemset(net->d.adam_v, 0, NPARAM * sizeof(float)));
+	net->step = 0;
+	k_to_bf16<<<nb(NPARAM), 256>>>(NPARAM, net->d.theta, net->d.wb);
+	MCK(cudaDeviceSynchronize());
+	return 0;
+}
+
+int bfm_gpu_mpnn_save(bfm_gpu_mpnn_t* net, const char* path) {
+	float* th = (float*) malloc(NPARAM * sizeof(float));
+	if (!th) return mfail("out of host memory");
+	if (bfm_gpu_mpnn_get_weights(net, th)) {
+		free(th);
+		return -1;
+	}
+	FILE* f = fopen(path, "wb");
+	if (!f) {
+		free(th);
+		return mfail("cannot open %s for writing", path);
+	}
+	uint32_t const hdr[6] = {FILE_VERSION, FIN, HID, 3, 3, NPARAM};
+	bool ok = fwrite(MAGIC, 1, 8, f) == 8 && fwrite(hdr, sizeof hdr, 1, f) == 1 &&
+	          fwrite(th, sizeof(float), NPARAM, f) == (size_t) NPARAM;
+	ok = (fclose(f) == 0) && ok;
+	free(th);
+	return ok ? 0 : mfail("short write to %s", path);
+}
+
+int bfm_gpu_mpnn_load(bfm_gpu_mpnn_t* net, const char* path) {
+	FILE* f = fopen(path, "rb");
+	if (!f) return mfail("cannot open %s", path);
+	char magic[8];
+	uint32_t hdr[6];
+	float* th = (float*) malloc(NPARAM * sizeof(float));
+	bool ok = th && fread(magic, 1, 8, f) == 8 && memcmp(magic, MAGIC, 8) == 0 && fread(hdr, sizeof hdr, 1, f) == 1;
+	if (ok && (hdr[0] != FILE_VERSION || hdr[1] != FIN || hdr[2] != HID || hdr[3] != 3 || hdr[4] != 3 || hdr[5] != (uint32_t) NPARAM)) {
+		fclose(f);
+		free(th);
+		return mfail("%s: unsupported network file (version %u, %u parameters)", path, hdr[0], hdr[5]);
+	}
+	ok = ok && fread(th, sizeof(float), NPARAM, f) == (size_t) NPARAM;
+	fclose(f);
+	if (!ok) {
+		free(th);
+		return mfail("%s: not a network file or truncated", path);
+	}
+	int const rc = bfm_gpu_mpnn_set_weights(net, th);
+	free(th);
+	return rc;
+}
+
+int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, float* features, float* c_out, double* blocks) {
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	cudaStream_t const st = (cudaStream_t) bf.stream;
+	if (forward(net, P, st)) return -1;
+	MCK(cudaStreamSynchronize(st));
+	long const N = bf.N;
+	if (features) {
+		bf16* tmp = (bf16*) malloc(N * FIN * sizeof(bf16) + 1);
+		if (!tmp) return mfail("out of host memory");
+		cudaError_t const e = cudaMemcpy(tmp, net->f, N * FIN * sizeof(bf16), cudaMemcpyDeviceToHost);
+		for (long k = 0; k < N * FIN; k++) features[k] = __bfloat162float(tmp[k]);
+		free(tmp);
+		MCK(e);
+	}
+	if (c_out) {
+		MCK(cudaMemcpy(c_out, net->o, N * 3 * sizeof(float), cudaMemcpyDeviceToHost));
+		for (long k = 0; k < N * 3; k++) c_out[k] = C_SCALE * tanhf(c_out[k]);
+	}
+	if (blocks) MCK(cudaMemcpy(blocks, net->blocks, N * 4 * sizeof(double), cudaMemcpyDeviceToHost));
+	return 0;
+}
+
+int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double* loss,
+                          float* grad) {
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	cudaStream_t const st = (cudaStream_t) bf.stream;
+	if (forward(net, P, st) || backward(net, P, r, e, st) || read_loss(net, loss, st)) return -1;
+	if (grad) {
+		MCK(cudaStreamSynchronize(st));
+		MCK(cudaMemcpy(grad, net->d.grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+	}
+	return 0;
+}
+
+int bfm_gpu_mpnn_train_step(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double lr,
+                            double* loss) {
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	cudaStream_t const st = (cudaStream_t) bf.stream;
+	if (forward(net, P, st) || backward(net, P, r, e, st)) return -1;
+	net->step += 1;
+	float const b1t = powf(0.9f, (float) net->step), b2t = powf(0.999f, (float) net->step);
+	k_adam<<<nb(NPARAM), 256, 0, st>>>(NPARAM, net->d.theta, net->d.grad, net->d.adam_m, net->d.adam_v, net->d.wb, (float) lr,
+	                                    b1t, b2t);
+	MCK(cudaGetLastError());
+	return read_loss(net, loss, st);
+}
+
+int bfm_gpu_mpnn_use(bfm_gpu_mpnn_t* net) {
+	g_active_net = net;
+	return 0;
+}
+
+}  // extern "C"
+
+int bfmi_learned_precond(bfm_gpu_problem_t* P, int jacobi) {
+	if (jacobi) return bfmi_set_precond_blocks(P, nullptr);
+	if (!g_active_net) return mfail("BFM_GPU_PC_LEARNED needs a network: call bfm_gpu_mpnn_use first");
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	if (forward(g_active_net, P, (cudaStream_t) bf.stream)) return -1;
+	return bfmi_set_precond_blocks(P, g_active_net->blocks);
+}

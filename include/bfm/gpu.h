@@ -216,6 +216,57 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t
 int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int* status, int* replacements,
                                double* rel_residual, int* rows_per_tile, int* lanes_per_row, double* ms_solve);
 
+/* y = K x with the assembled FP64 operator (after Dirichlet elimination);
+ * x and y are 2*n_nodes doubles in host or device memory (`where`).  Needs an
+ * assembly in FP64, MIXED_EXACT or FP64_DF.  Forms r = K e from an error e
+ * when generating training pairs for the learned preconditioner. */
+int bfm_gpu_problem_apply(bfm_gpu_problem_t* problem, const double* x, double* y, int where);
+
+/* ---------------------------------------------------------------- learned preconditioner */
+
+/* No counterpart in the reference.  A message-passing network over the node
+ * graph predicts, per node i, an SPD 2x2 block
+ *     B_i = S_i (I + C_i) S_i,  S_i = diag(K_ii)^(-1/2),  C_i = 0.45 tanh(o_i)
+ * (o_i: the network's 3 outputs, C_i symmetric), used by PCG in place of the
+ * Jacobi diagonal when opts->precond is BFM_GPU_PC_LEARNED.  Inputs per node:
+ * log-stiffness contrasts of the incident elements, Poisson ratio, Dirichlet
+ * flags, graph degree, the Jacobi-scaled load (the initial residual), and the
+ * diagonal block's scale ratio and coupling.  Layers: 16 -> 64, three times
+ * [h, mean of h over the graph row] 128 -> 64 (ReLU), head 64 -> 3.  BF16
+ * weights and activations on the tensor cores, FP32 accumulation and FP32
+ * master weights; 26,051 parameters.  An untrained network (zero head) is
+ * exactly Jacobi.  The solve falls back to Jacobi (stats.fallback = 1) when
+ * the learned solve breaks down or stagnates above 1e-6. */
+typedef struct bfm_gpu_mpnn bfm_gpu_mpnn_t;
+
+int bfm_gpu_mpnn_param_count(void);
+/* He-normal hidden weights from `seed`, zero biases, zero head. */
+int bfm_gpu_mpnn_create(bfm_gpu_mpnn_t** net, unsigned seed);
+int bfm_gpu_mpnn_destroy(bfm_gpu_mpnn_t* net);
+/* FP32 parameters in the order W0[64x16], b0, W1[64x128], b1, W2, b2, W3, b3,
+ * Wo[3x64], bo (row-major, out x in); host memory. */
+int bfm_gpu_mpnn_get_weights(bfm_gpu_mpnn_t* net, float* theta);
+int bfm_gpu_mpnn_set_weights(bfm_gpu_mpnn_t* net, const float* theta);
+/* Versioned weights file: "BFMMPNN\0", u32 version, input width, hidden
+ * width, layers, outputs, parameter count, FP32 parameters. */
+int bfm_gpu_mpnn_save(bfm_gpu_mpnn_t* net, const char* path);
+int bfm_gpu_mpnn_load(bfm_gpu_mpnn_t* net, const char* path);
+/* Run the network on an assembled problem; any output may be NULL (host):
+ * features[16*n_nodes] as fed to the first layer (BF16 values), c[3*n_nodes]
+ * = (c0, c1, c2) per node, blocks[4*n_nodes] = B_i row-major. */
+int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, float* features, float* c, double* blocks);
+/* Loss of one (residual r, error e) pair, r = K e, z = B r:
+ *     L = 1 - (z.r)^2 / ((z.K z)(e.r)),
+ * and its gradient (FP32, parameter order above; NULL to skip).  r and e are
+ * device arrays of 2*n_nodes doubles; needs the FP64 operator. */
+int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, const double* r, const double* e,
+                          double* loss, float* grad);
+/* One Adam step (beta 0.9 / 0.999) on the pair's gradient; loss may be NULL. */
+int bfm_gpu_mpnn_train_step(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, const double* r, const double* e,
+                            double lr, double* loss);
+/* Network used by BFM_GPU_PC_LEARNED solves (NULL: none). */
+int bfm_gpu_mpnn_use(bfm_gpu_mpnn_t* net);
+
 /* ---------------------------------------------------------------- allocation-free solve */
 
 /* No counterpart in the reference: an additive entry point for callers that

@@ -1,0 +1,188 @@
+"""CPU restatement of the learned block preconditioner (TEST INFRASTRUCTURE ONLY).
+
+The network of bfm_gb300/csrc/mpnn.cu in float64 numpy, forward and analytic
+backward, used by tests/test_gpu_learned.py to check the GPU kernels'
+features, activations, blocks, loss and gradients.  It has no counterpart in the
+reference (libbfm has no learned part); it is the oracle of this build's own
+additive feature.
+
+Network (parameters in this order, FP32 masters, BF16 copies on the GPU):
+    h0 = relu(W0 f + b0)                       W0: 64 x 16
+    h_l = relu(W_l [h_{l-1}, m_{l-1}] + b_l)   W_l: 64 x 128, l = 1..3
+          m = mean of h over the node's row of the node graph (itself included)
+    o = Wo h3 + bo                             Wo: 3 x 64
+    c = 0.45 tanh(o)
+    B_i = S_i (I + [[c0, c1], [c1, c2]]) S_i,  S_i = diag(K_ii)^(-1/2)
+Loss of one (residual r, error e) pair, z = B r:
+    L = 1 - (z.r)^2 / ((z.K z)(e.r))
+the A-norm reduction of e by the optimal step along z, subtracted from 1.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+F_IN, H = 16, 64
+SHAPES = [(H, F_IN), (H,), (H, 2 * H), (H,), (H, 2 * H), (H,), (H, 2 * H), (H,), (3, H), (3,)]
+N_PARAMS = sum(int(np.prod(s)) for s in SHAPES)
+C_SCALE = 0.45
+
+
+def unpack(theta: np.ndarray):
+    out, k = [], 0
+    for s in SHAPES:
+        n = int(np.prod(s))
+        out.append(theta[k:k + n].reshape(s))
+        k += n
+    return out
+
+
+def bf16(x):
+    """Round to the nearest bfloat16 (ties to even), through float32, as
+    __float2bfloat16 does on the GPU."""
+    x = np.asarray(x, np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _id(x):
+    return x
+
+
+def mean_agg(rp, cols, h):
+    deg = np.diff(rp).astype(np.float64)
+    m = np.zeros_like(h)
+    rows = np.repeat(np.arange(len(deg)), np.diff(rp))
+    np.add.at(m, rows, h[cols])
+    return m / deg[:, None]
+
+
+def mean_agg_T(rp, cols, dm):
+    """adjoint of mean_agg: dh[j] = sum over rows i containing j of dm[i]/deg[i]"""
+    deg = np.diff(rp).astype(np.float64)
+    rows = np.repeat(np.arange(len(deg)), np.diff(rp))
+    dh = np.zeros_like(dm)
+    np.add.at(dh, cols, dm[rows] / deg[rows, None])
+    return dh
+
+
+def forward(theta, f, rp, cols, emulate=False):
+    """c (n, 3) and the activations.  emulate=True rounds to BF16 where the
+    GPU stores BF16 (weights of the dense layers, activations, aggregates);
+    the head and every accumulation stay in full precision."""
+    r = bf16 if emulate else _id
+    W0, b0, W1, b1, W2, b2, W3, b3, Wo, bo = unpack(theta)
+    hs = [r(np.maximum(f @ r(W0).T + b0, 0.0))]
+    xs = []
+    for W, b in ((W1, b1), (W2, b2), (W3, b3)):
+        x = np.concatenate([hs[-1], r(mean_agg(rp, cols, hs[-1]))], 1)
+        xs.append(x)
+        hs.append(r(np.maximum(x @ r(W).T + b, 0.0)))
+    o = hs[-1] @ Wo.T + bo
+    c = C_SCALE * np.tanh(o)
+    return c, dict(hs=hs, xs=xs, o=o)
+
+
+def blocks(c, diag2):
+    """B_i as (n, 2, 2) from c (n, 3) and the 2x2 diagonal entries (n, 2)"""
+    s = 1.0 / np.sqrt(diag2)
+    B = np.zeros((len(c), 2, 2))
+    B[:, 0, 0] = s[:, 0] * s[:, 0] * (1 + c[:, 0])
+    B[:, 0, 1] = B[:, 1, 0] = s[:, 0] * s[:, 1] * c[:, 1]
+    B[:, 1, 1] = s[:, 1] * s[:, 1] * (1 + c[:, 2])
+    return B
+
+
+def loss_and_grad(theta, f, rp, cols, K, diag2, r, e, emulate=False):
+    """loss and d loss / d theta (float64); emulate as in forward (the
+    back-propagated signal entering each dense layer's GEMMs is BF16 too)"""
+    q = bf16 if emulate else _id
+    c, cache = forward(theta, f, rp, cols, emulate)
+    n = len(c)
+    B = blocks(c, diag2)
+    r2 = r.reshape(n, 2)
+    z = np.einsum("nij,nj->ni", B, r2).reshape(-1)
+    Az = K @ z
+    zr, zAz, er = z @ r, z @ Az, e @ r
+    loss = 1.0 - zr * zr / (zAz * er)
+    gz = (2.0 * zr / (zAz * er)) * ((zr / zAz) * Az - r)
+    g2 = gz.reshape(n, 2)
+    s = 1.0 / np.sqrt(diag2)
+    dc = np.stack([g2[:, 0] * s[:, 0] ** 2 * r2[:, 0],
+                   g2[:, 0] * s[:, 0] * s[:, 1] * r2[:, 1] + g2[:, 1] * s[:, 1] * s[:, 0] * r2[:, 0],
+                   g2[:, 1] * s[:, 1] ** 2 * r2[:, 1]], 1)
+    do = dc * C_SCALE * (1.0 - np.tanh(cache["o"]) ** 2)
+    W0, b0, W1, b1, W2, b2, W3, b3, Wo, bo = unpack(theta)
+    grads = [None] * 10
+    grads[8] = do.T @ cache["hs"][3]
+    grads[9] = do.sum(0)
+    dh = do @ Wo
+    for li, (W, gi) in zip((2, 1, 0), ((W3, 6), (W2, 4), (W1, 2))):
+        dpre = q(dh * (cache["hs"][li + 1] > 0))
+        grads[gi] = dpre.T @ cache["xs"][li]
+        grads[gi + 1] = dpre.sum(0)
+        dx = dpre @ q(W)
+        dh = dx[:, :H] + mean_agg_T(rp, cols, dx[:, H:])
+    dpre = q(dh * (cache["hs"][0] > 0))
+    grads[0] = dpre.T @ f
+    grads[1] = dpre.sum(0)
+    return loss, np.concatenate([g.reshape(-1) for g in grads]), c
+
+
+def features(p, rp, cols, vals, b):
+    """Input features (n, 16) of the network for a meshgen.Problem with its
+    assembled 2x2-block CSR operator (rp, cols, vals (nb, 2, 2)) and load
+    vector b (2n): the restatement of k_feat1/k_feat2 in
+    bfm_gb300/csrc/mpnn.cu, in float64."""
+    n = p.n_nodes
+    eE = p.elem_E if p.elem_E is not None else np.full(p.n_elems, p.E)
+    enu = p.elem_nu if p.elem_nu is not None else np.full(p.n_elems, p.nu)
+    le = np.log10(eE)
+    cnt = np.bincount(p.elems.reshape(-1), minlength=n).astype(np.float64)
+    ids = p.elems.reshape(-1)
+    le_rep = np.repeat(le, p.kind)
+    nu_rep = np.repeat(enu, p.kind)
+    node_le = np.bincount(ids, le_rep, minlength=n)
+    node_nu = np.bincount(ids, nu_rep, minlength=n)
+    has = cnt > 0
+    node_le = np.where(has, node_le / np.maximum(cnt, 1), np.log10(p.E))
+    node_nu = np.where(has, node_nu / np.maximum(cnt, 1), p.nu)
+    lmin = np.full(n, np.inf)
+    lmax = np.full(n, -np.inf)
+    np.minimum.at(lmin, ids, le_rep)
+    np.maximum.at(lmax, ids, le_rep)
+    contrast = np.where(has, lmin - lmax, 0.0)
+    deg = np.diff(rp)
+    rows = np.repeat(np.arange(n), deg)
+    nb_mean = np.bincount(rows, node_le[cols], minlength=n) / deg
+    dk = np.zeros((n, 2, 2))
+    diag = rows == cols
+    dk[rows[diag]] = vals[diag]
+    k00, k01, k11 = dk[:, 0, 0], dk[:, 0, 1], dk[:, 1, 1]
+    b2 = b.reshape(n, 2)
+    z0 = np.where(k00 != 0, b2[:, 0] / np.where(k00 != 0, k00, 1), 0.0)
+    z1 = np.where(k11 != 0, b2[:, 1] / np.where(k11 != 0, k11, 1), 0.0)
+    rms = np.sqrt((z0 @ z0 + z1 @ z1) / (2.0 * max(n, 1)))
+    rms = rms if rms > 0 else 1.0
+    z0, z1 = z0 / rms, z1 / rms
+    dirx = np.zeros(n, bool)
+    diry = np.zeros(n, bool)
+    for kind, _, mask in p.conds:
+        if kind == 0:
+            dirx |= mask
+        elif kind == 1:
+            diry |= mask
+    pos = (k00 > 0) & (k11 > 0)
+    f = np.zeros((n, F_IN))
+    f[:, 0] = node_le - nb_mean
+    f[:, 1] = (node_nu - 0.3) * 10.0
+    f[:, 2] = dirx
+    f[:, 3] = diry
+    f[:, 4] = deg / 9.0
+    f[:, 5] = z0
+    f[:, 6] = z1
+    f[:, 7] = np.where(pos, np.log10(np.where(pos, k00 / np.where(pos, k11, 1), 1)), 0.0)
+    f[:, 8] = np.where(pos, k01 / np.sqrt(np.where(pos, k00 * k11, 1)), 0.0)
+    f[:, 9] = np.abs(z0) + np.abs(z1)
+    f[:, 10] = contrast
+    return f

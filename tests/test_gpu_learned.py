@@ -1,0 +1,248 @@
+"""Learned block preconditioner on the GPU: features, forward pass, loss and
+gradients of the tensor-core kernels against the float64 oracle
+(oracle/mpnn_ref.py, with the GPU's BF16 rounding points emulated), Adam
+training, the solve with the learned blocks, the Jacobi fallback, and what a
+trained network gains over Jacobi-PCG."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import bfm_gb300
+from bfm_gb300 import learned as LN, meshgen as M
+from oracle import mpnn_ref as R
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def soft_plate(nx=48, ny=12, seed=11):
+    """P1 plate, left edge clamped, traction on the right edge, gravity,
+    per-element E log-uniform in [1e9, 2e11] (seeded)."""
+    p = M.plate(nx, ny, 3, name=f"soft_{nx}x{ny}", traction=1e6)
+    p.elem_E = np.exp(np.random.default_rng(seed).uniform(np.log(1e9), np.log(2e11), p.n_elems))
+    return p
+
+
+def scalar_K(rp, cols, vals, n):
+    nb = len(cols)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    R_ = np.repeat(2 * rows, 4) + np.tile([0, 0, 1, 1], nb)
+    C_ = np.repeat(2 * cols, 4) + np.tile([0, 1, 0, 1], nb)
+    return sp.csr_matrix((vals.reshape(-1), (R_, C_)), shape=(2 * n, 2 * n))
+
+
+def diag2(rp, cols, vals, n):
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    d = rows == cols
+    out = np.zeros((n, 2))
+    out[rows[d], 0] = vals[d, 0, 0]
+    out[rows[d], 1] = vals[d, 1, 1]
+    return out
+
+
+def random_theta(net, seed, head=0.3):
+    """The network's initial weights with a random non-zero head (so c varies)."""
+    th = net.weights().astype(np.float64)
+    rng = np.random.default_rng(seed)
+    o = R.N_PARAMS - (3 * R.H + 3)
+    th[o:] = rng.normal(0.0, head, 3 * R.H + 3) / np.sqrt(R.H)
+    th[o + 3 * R.H:] = rng.normal(0.0, 0.2, 3)
+    th[:o] += rng.normal(0.0, 0.01, o)   # non-zero biases too
+    return th.astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def setup(libbfm):
+    p = soft_plate()
+    prob = LN.DeviceProblem(p)
+    rp, cols, vals, b = prob.download()
+    net = LN.Network(seed=3)
+    yield p, prob, net, (rp, cols, vals, b)
+    net.close()
+    prob.close()
+
+
+def test_features_match_oracle(setup):
+    p, prob, net, (rp, cols, vals, b) = setup
+    f_gpu, _, _ = net.forward(prob)
+    f_ref = R.features(p, rp, cols, vals, b)
+    # BF16 inputs: half a BF16 ulp of the reference value (plus double-rounding ties)
+    tol = 2.0 ** -8 * np.abs(f_ref) + 1e-6
+    bad = np.abs(f_gpu - f_ref) > tol
+    assert not bad.any(), (np.argwhere(bad)[:5], f_gpu[bad][:5], f_ref[bad][:5])
+    assert np.count_nonzero(f_gpu[:, 11:]) == 0
+
+
+def test_untrained_network_is_jacobi(setup):
+    p, prob, net, (rp, cols, vals, b) = setup
+    _, c, B = net.forward(prob)
+    assert np.all(c == 0.0)
+    d = diag2(rp, cols, vals, p.n_nodes)
+    np.testing.assert_array_equal(B[:, 0, 1], 0.0)
+    np.testing.assert_allclose(B[:, 0, 0], 1.0 / d[:, 0], rtol=1e-15)
+    np.testing.assert_allclose(B[:, 1, 1], 1.0 / d[:, 1], rtol=1e-15)
+
+
+def test_forward_matches_oracle(setup):
+    p, prob, net, (rp, cols, vals, b) = setup
+    th = random_theta(net, 1)
+    init = net.weights()
+    net.set_weights(th)
+    try:
+        f_gpu, c_gpu, B_gpu = net.forward(prob)
+        c_ref, _ = R.forward(th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, emulate=True)
+        assert np.abs(c_ref).max() > 0.05
+        # FP32 accumulation order differs from float64: 1e-3 of the output scale
+        assert np.abs(c_gpu - c_ref).max() <= 1e-3 * R.C_SCALE
+        B_ref = R.blocks(c_ref, diag2(rp, cols, vals, p.n_nodes))
+        assert np.linalg.norm(B_gpu - B_ref) <= 5e-3 * np.linalg.norm(B_ref)
+        # every block SPD: 1 + c0 > 0 and det(I + C) > 0 for |c| < 0.45
+        det = B_gpu[:, 0, 0] * B_gpu[:, 1, 1] - B_gpu[:, 0, 1] ** 2
+        assert (B_gpu[:, 0, 0] > 0).all() and (det > 0).all()
+    finally:
+        net.set_weights(init)
+
+
+@pytest.fixture(scope="module")
+def pair(setup):
+    p, prob, net, _ = setup
+    prs = LN.pairs(prob, stops=(32,))
+    assert prs
+    return prs[0]
+
+
+def test_gradient_matches_oracle(setup, pair):
+    p, prob, net, (rp, cols, vals, b) = setup
+    r, e = pair
+    th = random_theta(net, 2)
+    init = net.weights()
+    net.set_weights(th)
+    try:
+        f_gpu, _, _ = net.forward(prob)
+        loss_gpu, g_gpu = net.gradient(prob, r.data_ptr(), e.data_ptr())
+        K = scalar_K(rp, cols, vals, p.n_nodes)
+        args = (th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, K, diag2(rp, cols, vals, p.n_nodes),
+                r.cpu().numpy(), e.cpu().numpy())
+        loss_ref, g_ref, _ = R.loss_and_grad(*args, emulate=True)
+        assert 0.0 <= loss_gpu <= 1.0
+        assert abs(loss_gpu - loss_ref) <= 1e-4 * abs(loss_ref)
+        # every parameter block, relative to its own norm: BF16 storage emulated, FP32 sums
+        k = 0
+        for shape in R.SHAPES:
+            n = int(np.prod(shape))
+            gg, gr = g_gpu[k:k + n], g_ref[k:k + n]
+            assert np.linalg.norm(gg - gr) <= 2e-2 * np.linalg.norm(gr) + 1e-12, (shape, k)
+            k += n
+        # and the float64 network without any BF16 rounding: same direction
+        _, g64, _ = R.loss_and_grad(*args, emulate=False)
+        cos = g_gpu @ g64 / (np.linalg.norm(g_gpu) * np.linalg.norm(g64))
+        assert cos > 0.98
+    finally:
+        net.set_weights(init)
+
+
+def test_training_lowers_the_loss(setup, pair):
+    p, prob, _, _ = setup
+    r, e = pair
+    net = LN.Network(seed=4)
+    try:
+        losses = [net.train_step(prob, r.data_ptr(), e.data_ptr(), 1e-3) for _ in range(60)]
+        assert np.isfinite(losses).all()
+        assert np.mean(losses[-10:]) < 0.9 * np.mean(losses[:10])
+    finally:
+        net.close()
+
+
+def test_save_load_roundtrip(setup, tmp_path):
+    _, _, net, _ = setup
+    th = random_theta(net, 5)
+    other = LN.Network(seed=9)
+    try:
+        other.set_weights(th)
+        other.save(tmp_path / "w.bin")
+        third = LN.Network(seed=10, path=tmp_path / "w.bin")
+        np.testing.assert_array_equal(third.weights(), th)
+        third.close()
+        (tmp_path / "bad.bin").write_bytes(b"not a network")
+        lib = bfm_gb300.lib()
+        assert lib.bfm_gpu_mpnn_load(other.h, str(tmp_path / "bad.bin").encode()) == -1
+        assert "network file" in bfm_gb300.last_error()
+    finally:
+        other.close()
+
+
+@pytest.mark.parametrize("precision", [bfm_gb300.FP64, bfm_gb300.MIXED_EXACT, bfm_gb300.FP64_DF])
+def test_untrained_learned_solve_equals_jacobi(libbfm, precision):
+    p = soft_plate(64, 16, seed=12)
+    prob = LN.DeviceProblem(p, precision=precision)
+    net = LN.Network(seed=0)
+    try:
+        net.use()
+        sj = prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-8)
+        xj = prob.solution()
+        sl = prob.solve(precond=bfm_gb300.PC_LEARNED, rtol=1e-8)
+        xl = prob.solution()
+        assert sj.status == 0 and sl.status == 0 and sl.fallback == 0
+        assert sl.iterations == sj.iterations
+        assert np.linalg.norm(xl - xj) <= 1e-12 * np.linalg.norm(xj)
+    finally:
+        net.close()
+        prob.close()
+
+
+def test_learned_without_network_is_an_error(libbfm):
+    prob = LN.DeviceProblem(soft_plate(16, 4))
+    try:
+        libbfm.bfm_gpu_mpnn_use(None)
+        o = bfm_gb300.default_opts(precond=bfm_gb300.PC_LEARNED)
+        import ctypes as C
+        assert libbfm.bfm_gpu_problem_solve(prob.P, C.byref(o)) == -1
+        assert "network" in bfm_gb300.last_error()
+    finally:
+        prob.close()
+
+
+def test_nan_network_falls_back_to_jacobi(libbfm):
+    """Fault injection on the host: non-finite network output -> breakdown of
+    the learned solve -> Jacobi takes over and converges."""
+    p = soft_plate(64, 16, seed=13)
+    prob = LN.DeviceProblem(p)
+    net = LN.Network(seed=0)
+    try:
+        th = net.weights()
+        th[-1] = np.nan
+        net.set_weights(th)
+        net.use()
+        sj = prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-8)
+        xj = prob.solution()
+        s = prob.solve(precond=bfm_gb300.PC_LEARNED, rtol=1e-8)
+        assert s.fallback == 1 and s.status == 0
+        assert s.iterations == sj.iterations
+        np.testing.assert_allclose(prob.solution(), xj, rtol=0, atol=1e-12 * np.abs(xj).max())
+    finally:
+        net.close()
+        prob.close()
+
+
+def test_trained_network_beats_jacobi(libbfm):
+    """The gain test: a network trained here on solver-generated pairs from
+    small uneven plates and perforated plates cuts the PCG iterations of a
+    held-out perforated plate below Jacobi's, at the same accuracy."""
+    train_meshes = LN.training_meshes(21, n_plates=1, n_batch=1, batch_parts=6)
+    train_meshes[0] = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=22)
+    probs = [LN.DeviceProblem(q) for q in train_meshes]
+    held = LN.DeviceProblem(M.cfg_perforated(nx=384, ny=96, n_holes=200, seed=3))
+    net = LN.Network(seed=5)
+    try:
+        hist, n = LN.train(net, probs, 1500, lr=1e-3, epochs=1, seed=1)
+        ev = LN.evaluate(net, held, rtol=1e-8)
+        print("gain test:", hist, ev)
+        assert ev["learned"]["status"] == 0 and ev["learned"]["fallback"] == 0
+        assert ev["learned"]["rel_residual"] <= 1e-8
+        assert ev["learned"]["iterations"] < ev["jacobi"]["iterations"]
+    finally:
+        net.close()
+        for q in probs:
+            q.close()
+        held.close()

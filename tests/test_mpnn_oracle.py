@@ -1,0 +1,61 @@
+"""The learned preconditioner's CPU oracle (oracle/mpnn_ref.py) on its own:
+analytic gradients against central finite differences, the BF16 rounding
+helper against known values, and the blocks' SPD property."""
+import numpy as np
+
+from oracle import mpnn_ref as R
+
+
+def tiny_graph(n=24, seed=0):
+    rng = np.random.default_rng(seed)
+    rows = [sorted({i, (i + 1) % n, (i - 1) % n, int(rng.integers(n))}) for i in range(n)]
+    rp = np.cumsum([0] + [len(r) for r in rows])
+    cols = np.concatenate(rows)
+    return rp, cols
+
+
+def spd(n, seed):
+    rng = np.random.default_rng(seed)
+    A = rng.normal(size=(2 * n, 2 * n))
+    return A @ A.T + 2 * n * np.eye(2 * n)
+
+
+def test_param_count():
+    assert R.N_PARAMS == 26051
+
+
+def test_gradient_matches_finite_differences():
+    n = 24
+    rp, cols = tiny_graph(n)
+    rng = np.random.default_rng(1)
+    f = rng.normal(size=(n, R.F_IN))
+    K = spd(n, 2)
+    d2 = np.stack([np.diag(K)[0::2], np.diag(K)[1::2]], 1)
+    e = rng.normal(size=2 * n)
+    r = K @ e
+    th = rng.normal(0, 0.3, R.N_PARAMS)
+    loss, g, _ = R.loss_and_grad(th, f, rp, cols, K, d2, r, e)
+    assert 0.0 <= loss <= 1.0
+    idx = rng.choice(R.N_PARAMS, 60, replace=False)
+    h = 1e-6
+    for k in idx:
+        tp, tm = th.copy(), th.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd = (R.loss_and_grad(tp, f, rp, cols, K, d2, r, e)[0] - R.loss_and_grad(tm, f, rp, cols, K, d2, r, e)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(g).max()), (k, fd, g[k])
+
+
+def test_bf16_rounding():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, -3.0 + 2 ** -7 + 2 ** -8, 65504.0, 1e-3])
+    want = np.array([1.0, 1.0, 1.0 + 2 ** -7, -3.0 + 2 ** -6, 65536.0, 0.00099945068359375])
+    np.testing.assert_array_equal(R.bf16(x), want)
+
+
+def test_blocks_are_spd_for_any_output():
+    rng = np.random.default_rng(3)
+    c = R.C_SCALE * np.tanh(rng.normal(0, 10, (1000, 3)))
+    d2 = np.exp(rng.normal(0, 3, (1000, 2)))
+    B = R.blocks(c, d2)
+    ev = np.linalg.eigvalsh(B)
+    assert (ev > 0).all()
