@@ -34,19 +34,9 @@ class Batch:
         enu = np.concatenate([p.elem_nu if p.elem_nu is not None else np.full(p.n_elems, p.nu) for p in problems])
         dx = np.concatenate([self._mask(p, M.DIRICHLET_X) for p in problems]).astype(np.uint8)
         dy = np.concatenate([self._mask(p, M.DIRICHLET_Y) for p in problems]).astype(np.uint8)
-        ledges, lloads = [], []
-        for k, p in enumerate(problems):
-            for kind, value, mask in p.conds:
-                if kind not in (M.NEUMANN_X, M.NEUMANN_Y) or p.edges is None:
-                    continue
-                sel = mask[p.edges[:, 0]] & mask[p.edges[:, 1]]
-                e = p.edges[sel] + node_off[k]
-                ld = np.zeros((len(e), 2))
-                ld[:, 0 if kind == M.NEUMANN_X else 1] = value
-                ledges.append(e)
-                lloads.append(ld)
-        ledges = np.concatenate(ledges).astype(np.int32) if ledges else np.zeros((0, 2), np.int32)
-        lloads = np.concatenate(lloads) if lloads else np.zeros((0, 2))
+        loads = [M.neumann_edge_loads(p, node_off[k]) for k, p in enumerate(problems)]
+        ledges = np.concatenate([e for e, _ in loads]).astype(np.int32)
+        lloads = np.concatenate([l for _, l in loads])
         self.n_nodes = int(node_off[-1])
         self.n_elems = len(elems)
         self.keep = [coords, elems, eE, enu, dx, dy, ledges, lloads, node_off]

@@ -288,6 +288,7 @@ struct AsmArgs {
 	float* corr32;   // per node: 2x2 block of the row sums of (FP64 value - FP32 value)
 	float* vals32lo; // double-float path: FP32 rounding of (FP64 value - FP32 value)
 	double* b;
+	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
 	int precond;
@@ -540,15 +541,58 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 }
 
 // FP32 element integration, fast form (BFM_GPU_MIXED): one thread per node
-// row as above (owner computes, no atomics), but with the row's accumulators
-// in registers -- rows of up to RMAX blocks, with the block index resolved by
-// fully unrolled predicated adds -- each element's contribution summed over
-// the integration points before it is added, and the block's output rows
-// staged in shared memory so the contiguous span of values is written with
-// coalesced 16-byte stores.  Rows longer than RMAX are left to k_assemble<false>.
+// row as above (owner computes, no atomics), with every per-element and
+// per-row operation on the FP32 pipe (GB300 issues FP64 at a small fraction
+// of its FP32 rate):
+//  - node offsets within an element from a hi/lo float split of the FP64
+//    coordinates (the hi difference of nearby nodes is exact, the lo
+//    difference restores what the split dropped);
+//  - material constants per element in FP32; the Gauss rule from shared memory;
+//  - the row's accumulators in registers, rows of up to RMAX blocks, the block
+//    index resolved by fully unrolled predicated adds, each element's
+//    contribution summed over the integration points before it is added;
+//  - the diagonal block rebuilt as a double-float sum of the off-diagonal
+//    blocks: its FP32 value is the high part and the low part goes to the
+//    correction block, so K32 + C keeps the exact zero row sums of the
+//    translation modes;
+//  - the block's output rows staged in shared memory and written with
+//    coalesced 16-byte stores.
+// Rows longer than RMAX are left to k_assemble<false>.
+__device__ __forceinline__ void material_abc32(float E, float nu, int stress, float& a, float& b, float& c) {
+	if (!stress) {
+		float const den = (1.f + nu) * (1.f - 2.f * nu);
+		a = E * (1.f - nu) / den;
+		b = E * nu / den;
+	}
+	else {
+		float const den = 1.f - nu * nu;
+		a = E / den;
+		b = E * nu / den;
+	}
+	c = E / (2.f * (1.f + nu));
+}
+
+// s + x as an unevaluated float pair (TwoSum, no ordering assumption)
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+	float const t = __fadd_rn(hi, x);
+	float const z = __fsub_rn(t, hi);
+	float const err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(x, z));
+	hi = t;
+	lo = __fadd_rn(lo, err);
+}
+
+__global__ void k_split_coords(int N, const double* __restrict__ coords, float4* __restrict__ out) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double2 const c = reinterpret_cast<const double2*>(coords)[i];
+	float const xh = (float) c.x, yh = (float) c.y;
+	out[i] = make_float4(xh, yh, (float) (c.x - (double) xh), (float) (c.y - (double) yh));
+}
+
 template <int RMAX>
 __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 	__shared__ float4 stage[128 * RMAX];
+	__shared__ float sw[MAXQ], sphi[MAXQ][4], sdxi[MAXQ][4], sdeta[MAXQ][4];
 	__shared__ int first_rs, long_rows;
 	int const r = blockIdx.x * blockDim.x + threadIdx.x;
 	bool const valid = r < a.N;
@@ -558,6 +602,13 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		first_rs = a.row_ptr[blockIdx.x * blockDim.x];
 		long_rows = 0;
 	}
+	for (int k = threadIdx.x; k < MAXQ * 4; k += blockDim.x) {
+		int const q = k >> 2, j = k & 3;
+		sphi[q][j] = (float) a.rule.phi[q][j];
+		sdxi[q][j] = (float) a.rule.dxi[q][j];
+		sdeta[q][j] = (float) a.rule.deta[q][j];
+	}
+	if (threadIdx.x < MAXQ) sw[threadIdx.x] = (float) a.rule.w[threadIdx.x];
 	__syncthreads();
 	if (len > RMAX) atomicOr(&long_rows, 1);
 	bool const mine = valid && len <= RMAX;
@@ -569,10 +620,23 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		col[t] = (mine && t < len) ? a.cols[rs + t] : -1;
 		acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
 	}
-	double b0 = 0.0, b1 = 0.0;
-	int const kind = a.kind;
-	double ca = 0, cb = 0, cc = 0;
-	if (!a.elemE && !a.elemNu) material_abc(a.E, a.nu, a.stress, ca, cb, cc);
+	int const kind = a.kind, nq = a.rule.nq;
+	bool const per_elem = a.elemE || a.elemNu;
+	float ca = 0.f, cb = 0.f, cc = 0.f;
+	if (!per_elem) material_abc32((float) a.E, (float) a.nu, a.stress, ca, cb, cc);
+	// body forces at this node (the reference evaluates them at the node), times rho
+	float gfx = 0.f, gfy = 0.f;
+	if (mine)
+		for (int f = 0; f < a.forces.nf; f++) {
+			double fx = a.forces.f[f][0], fy = a.forces.f[f][1];
+			if (a.forces.field[f]) {
+				fx = a.forces.field[f][2l * r];
+				fy = a.forces.field[f][2l * r + 1];
+			}
+			gfx += (float) fx * (float) a.rho;
+			gfy += (float) fy * (float) a.rho;
+		}
+	float bf0 = 0.f, bf1 = 0.f;
 	int const is = mine ? a.inc_ptr[r] : 0, ie = mine ? a.inc_ptr[r + 1] : 0;
 	int prev_e = -1;
 	for (int t = is; t < ie; t++) {
@@ -580,48 +644,41 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		if (e == prev_e) continue;
 		prev_e = e;
 		int map[4];
-		double x[4], y[4];
+		float lx[4], ly[4];
 		int jr = 0;
+		float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
 		for (int j = 0; j < 4; j++) {
+			lx[j] = ly[j] = 0.f;
+			map[j] = -2;
 			if (j < kind) {
 				map[j] = a.elems[(long) e * kind + j];
-				double2 const c = reinterpret_cast<const double2*>(a.coords)[map[j]];
-				x[j] = c.x;
-				y[j] = c.y;
-			}
-			else {
-				map[j] = -2;
-				x[j] = y[j] = 0.0;
+				float4 const cj = a.coords32[map[j]];
+				if (j == 0) c0 = cj;
+				lx[j] = __fadd_rn(__fsub_rn(cj.x, c0.x), __fsub_rn(cj.z, c0.z));
+				ly[j] = __fadd_rn(__fsub_rn(cj.y, c0.y), __fsub_rn(cj.w, c0.w));
 			}
 		}
 #pragma unroll
 		for (int j = 3; j >= 0; j--)
 			if (j < kind && map[j] == r) jr = j;
-		double ea = ca, eb = cb, ec = cc;
-		if (a.elemE || a.elemNu) {
-			double const E = a.elemE ? a.elemE[e] : a.E;
-			double const nu = a.elemNu ? a.elemNu[e] : a.nu;
-			material_abc(E, nu, a.stress, ea, eb, ec);
-		}
-		float const fa = (float) ea, fb = (float) eb, fc = (float) ec;
-		float lx[4], ly[4];
-#pragma unroll
-		for (int j = 0; j < 4; j++) {
-			lx[j] = (float) (x[j] - x[0]);
-			ly[j] = (float) (y[j] - y[0]);
+		float fa = ca, fb = cb, fc = cc;
+		if (per_elem) {
+			float const E = a.elemE ? (float) a.elemE[e] : (float) a.E;
+			float const nu = a.elemNu ? (float) a.elemNu[e] : (float) a.nu;
+			material_abc32(E, nu, a.stress, fa, fb, fc);
 		}
 		float ek[4][4];
 #pragma unroll
 		for (int k = 0; k < 4; k++) ek[k][0] = ek[k][1] = ek[k][2] = ek[k][3] = 0.f;
-		for (int q = 0; q < a.rule.nq; q++) {
-			float const w = (float) a.rule.w[q];
+		for (int q = 0; q < nq; q++) {
+			float const w = sw[q];
 			float dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
 			float gx[4], ge[4];
 #pragma unroll
 			for (int j = 0; j < 4; j++) {
-				gx[j] = j < kind ? (float) a.rule.dxi[q][j] : 0.f;
-				ge[j] = j < kind ? (float) a.rule.deta[q][j] : 0.f;
+				gx[j] = sdxi[q][j];
+				ge[j] = sdeta[q][j];
 				dx_dxsi += lx[j] * gx[j];
 				dx_deta += lx[j] * ge[j];
 				dy_dxsi += ly[j] * gx[j];
@@ -636,16 +693,9 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 				dy[j] = (ge[j] * dx_dxsi - gx[j] * dx_deta) * idet;
 			}
 			float const dw = det * w;
-			double const ph = a.rule.phi[q][jr];
-			for (int f = 0; f < a.forces.nf; f++) {
-				double fx = a.forces.f[f][0], fy = a.forces.f[f][1];
-				if (a.forces.field[f]) {
-					fx = a.forces.field[f][2l * r];
-					fy = a.forces.field[f][2l * r + 1];
-				}
-				b0 += (double) dw * fx * a.rho * ph;
-				b1 += (double) dw * fy * a.rho * ph;
-			}
+			float const dwp = dw * sphi[q][jr];
+			bf0 += dwp * gfx;
+			bf1 += dwp * gfy;
 			float xj = dx[0], yj = dy[0];
 #pragma unroll
 			for (int j = 1; j < 4; j++)
@@ -675,20 +725,28 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 				}
 		}
 	}
-	// translation-preserving diagonal (see k_assemble): FP64 sum of the off-diagonal blocks
-	double dfix[4] = {0, 0, 0, 0};
+	// translation-preserving diagonal: minus the double-float sum of the off-diagonal blocks
+	float dh[4] = {0.f, 0.f, 0.f, 0.f}, dl[4] = {0.f, 0.f, 0.f, 0.f};
 	bool has_diag = false;
 #pragma unroll
 	for (int t = 0; t < RMAX; t++) {
 		if (col[t] == r) has_diag = true;
 		else if (col[t] >= 0)
-			for (int k = 0; k < 4; k++) dfix[k] -= (double) acc[t][k];
+#pragma unroll
+			for (int k = 0; k < 4; k++) two_sum_acc(dh[k], dl[k], -acc[t][k]);
+	}
+#pragma unroll
+	for (int k = 0; k < 4; k++) {
+		float const h = __fadd_rn(dh[k], dl[k]);
+		dl[k] = __fsub_rn(dl[k], __fsub_rn(h, dh[k]));
+		dh[k] = h;
 	}
 	bool const fix = has_diag && is < ie;
 	int const r0 = 2 * r, r1 = 2 * r + 1;
 	bool const c0 = mine && a.last_ci[r0] >= 0, c1 = mine && a.last_ci[r1] >= 0;
-	double k00 = 0, k01 = 0, k10 = 0, k11 = 0;
-	double corr[4] = {0, 0, 0, 0};
+	float k00 = 0.f, k01 = 0.f, k10 = 0.f, k11 = 0.f;
+	float4 corr = make_float4(0.f, 0.f, 0.f, 0.f);
+	double b0 = bf0, b1 = bf1;
 	__syncthreads();
 	bool const staged = long_rows == 0;
 #pragma unroll
@@ -697,30 +755,34 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		if (c < 0) continue;
 		int const d0 = 2 * c, d1 = 2 * c + 1;
 		bool const e0 = a.last_ci[d0] >= 0, e1 = a.last_ci[d1] >= 0;
-		double v[4] = {(double) acc[t][0], (double) acc[t][1], (double) acc[t][2], (double) acc[t][3]};
-		if (c == r && fix) {
-			v[0] = dfix[0]; v[1] = dfix[1]; v[2] = dfix[2]; v[3] = dfix[3];
+		bool const dg = c == r && fix;
+		float v[4] = {acc[t][0], acc[t][1], acc[t][2], acc[t][3]};
+		float lo[4] = {0.f, 0.f, 0.f, 0.f};
+		if (dg) {
+#pragma unroll
+			for (int k = 0; k < 4; k++) {
+				v[k] = dh[k];
+				lo[k] = dl[k];
+			}
 		}
 		if (e0 || e1) {
+			// non-homogeneous Dirichlet values leave the row through b (rare rows)
 			double const f0 = e0 ? a.first[d0] : 0.0, f1 = e1 ? a.first[d1] : 0.0;
 			if (!c0) {
-				if (e0) b0 -= f0 * v[0];
-				if (e1) b0 -= f1 * v[1];
+				if (e0) b0 -= f0 * ((double) v[0] + lo[0]);
+				if (e1) b0 -= f1 * ((double) v[1] + lo[1]);
 			}
 			if (!c1) {
-				if (e0) b1 -= f0 * v[2];
-				if (e1) b1 -= f1 * v[3];
+				if (e0) b1 -= f0 * ((double) v[2] + lo[2]);
+				if (e1) b1 -= f1 * ((double) v[3] + lo[3]);
 			}
 		}
-		if (c0 || e0) v[0] = (r0 == d0) ? 1.0 : 0.0;
-		if (c0 || e1) v[1] = 0.0;
-		if (c1 || e0) v[2] = 0.0;
-		if (c1 || e1) v[3] = (r1 == d1) ? 1.0 : 0.0;
-		float4 f4 = make_float4((float) v[0], (float) v[1], (float) v[2], (float) v[3]);
-		corr[0] += v[0] - (double) f4.x;
-		corr[1] += v[1] - (double) f4.y;
-		corr[2] += v[2] - (double) f4.z;
-		corr[3] += v[3] - (double) f4.w;
+		if (c0 || e0) { v[0] = (r0 == d0) ? 1.f : 0.f; lo[0] = 0.f; }
+		if (c0 || e1) { v[1] = 0.f; lo[1] = 0.f; }
+		if (c1 || e0) { v[2] = 0.f; lo[2] = 0.f; }
+		if (c1 || e1) { v[3] = (r1 == d1) ? 1.f : 0.f; lo[3] = 0.f; }
+		if (dg) corr = make_float4(lo[0], lo[1], lo[2], lo[3]);
+		float4 const f4 = make_float4(v[0], v[1], v[2], v[3]);
 		if (staged) stage[rs - first_rs + t] = f4;
 		else reinterpret_cast<float4*>(a.vals32)[rs + t] = f4;
 		if (c == r) {
@@ -729,13 +791,18 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		}
 	}
 	if (mine) {
-		reinterpret_cast<float4*>(a.corr32)[r] =
-			make_float4((float) corr[0], (float) corr[1], (float) corr[2], (float) corr[3]);
+		reinterpret_cast<float4*>(a.corr32)[r] = corr;
 		if (c0) b0 = a.last[r0];
 		if (c1) b1 = a.last[r1];
-		a.b[r0] = b0;
-		a.b[r1] = b1;
-		store_precond(a, r, k00, k01, k10, k11);
+		reinterpret_cast<double2*>(a.b)[r] = make_double2(b0, b1);
+		if (a.precond != BFM_GPU_PC_JACOBI) {
+			float const det = k00 * k11 - k01 * k10;
+			float const id = det != 0.f ? 1.f / det : 0.f;
+			reinterpret_cast<float4*>(a.dinv32)[r] = make_float4(k11 * id, -k01 * id, -k10 * id, k00 * id);
+		}
+		else {
+			reinterpret_cast<float2*>(a.dinv32)[r] = make_float2(k00 != 0.f ? 1.f / k00 : 0.f, k11 != 0.f ? 1.f / k11 : 0.f);
+		}
 	}
 	__syncthreads();
 	if (staged) {
@@ -939,6 +1006,7 @@ struct bfm_gpu_problem {
 	float* vals32;
 	float* corr32;  // mixed: per-node 2x2 row-sum correction of the FP32 operator
 	float* vals32lo;  // double-float path: low parts of the block values
+	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
 	double* b;
 	int* last_ci;
 	double *first, *last;
@@ -1416,7 +1484,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->vals32lo, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
+	                P->vals32, P->corr32, P->vals32lo, P->coords32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1706,8 +1774,14 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		if (dfp) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32, P->precond != BFM_GPU_PC_JACOBI);
 	}
 	else {
-		k_assemble32<12><<<blocks_for(N, 128), 128, 0, st>>>(a);
-		a.skip_upto = 12;
+		if (!P->coords32 && dalloc(&P->coords32, N)) return -1;
+		k_split_coords<<<blocks_for(N), TPB, 0, st>>>(P->N, P->coords, P->coords32);
+		a.coords32 = P->coords32;
+		// register rows: 8 blocks cover structured P1 meshes (7 per row), 10 cover Q1 (9)
+		int const rmax = P->kind == 3 ? 8 : 10;
+		if (rmax == 8) k_assemble32<8><<<blocks_for(N, 128), 128, 0, st>>>(a);
+		else k_assemble32<10><<<blocks_for(N, 128), 128, 0, st>>>(a);
+		a.skip_upto = rmax;
 		k_assemble<false><<<blocks_for(N, 128), 128, 0, st>>>(a);
 	}
 	// 5. Neumann loads

@@ -14,8 +14,9 @@
 // reduced in block order.
 //
 // Training loss of one (residual r, error e) pair, z = B r:
-//     L = 1 - (z.r)^2 / ((z.K z)(e.r)),
-// one minus the A-norm reduction of e by the optimal step along z.
+//     L = -log( (z.r)^2 / ((z.K z)(e.r)) ) >= 0,
+// the log of the fraction of e's energy norm that the optimal step along z
+// removes (0 when z is parallel to e).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -263,14 +264,16 @@ __global__ void k_head(int N, const bf16* __restrict__ h3, const float* __restri
 			k00 = vals64 ? vals64[4l * k] : (double) vals32[4l * k];
 			k11 = vals64 ? vals64[4l * k + 3] : (double) vals32[4l * k + 3];
 		}
-	double const s0 = k00 > 0.0 ? 1.0 / sqrt(k00) : 0.0, s1 = k11 > 0.0 ? 1.0 / sqrt(k11) : 0.0;
-	scale2[2 * i] = s0 * s0;
-	scale2[2 * i + 1] = s1 * s1;
+	// diagonal entries as (1 + c) / k: exactly the Jacobi values at c = 0
+	double const i0 = k00 > 0.0 ? 1.0 / k00 : 0.0, i1 = k11 > 0.0 ? 1.0 / k11 : 0.0;
+	double const s01 = sqrt(i0 * i1);
+	scale2[2 * i] = i0;
+	scale2[2 * i + 1] = i1;
 	double const c0 = C_SCALE * tanh((double) oo[0]), c1 = C_SCALE * tanh((double) oo[1]), c2 = C_SCALE * tanh((double) oo[2]);
-	blocks[4 * i + 0] = s0 * s0 * (1.0 + c0);
-	blocks[4 * i + 1] = s0 * s1 * c1;
-	blocks[4 * i + 2] = s0 * s1 * c1;
-	blocks[4 * i + 3] = s1 * s1 * (1.0 + c2);
+	blocks[4 * i + 0] = (1.0 + c0) * i0;
+	blocks[4 * i + 1] = s01 * c1;
+	blocks[4 * i + 2] = s01 * c1;
+	blocks[4 * i + 3] = (1.0 + c2) * i1;
 }
 
 // ---------------------------------------------------------------- loss
@@ -319,18 +322,17 @@ __global__ void k_loss_dots(LossArgs a) {
 		a.sc[0] = out[0];
 		a.sc[1] = out[1];
 		a.sc[2] = out[2];
-		a.sc[3] = 1.0 - out[0] * out[0] / (out[1] * out[2]);
+		a.sc[3] = log(out[1]) + log(out[2]) - 2.0 * log(fabs(out[0]));
 	}
 }
 
-// dL/dz = (2 zr / (zAz er)) ((zr/zAz) Az - r) -> dL/dc -> dL/do (N x 3, FP32)
+// dL/dz = 2 Az / (z.Az) - 2 r / (z.r) -> dL/dc -> dL/do (N x 3, FP32)
 __global__ void k_loss_back(LossArgs a, const float* __restrict__ o, const double* __restrict__ scale2, float* __restrict__ d_o) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.N) return;
-	double const zr = a.sc[0], zaz = a.sc[1], er = a.sc[2];
-	double const f = 2.0 * zr / (zaz * er), q = zr / zaz;
+	double const zr = a.sc[0], zaz = a.sc[1];
 	double2 const az = ld2(a.az, i), r = ld2(a.r, i);
-	double const g0 = f * (q * az.x - r.x), g1 = f * (q * az.y - r.y);
+	double const g0 = 2.0 * az.x / zaz - 2.0 * r.x / zr, g1 = 2.0 * az.y / zaz - 2.0 * r.y / zr;
 	double const t0 = tanh((double) o[3 * i]), t1 = tanh((double) o[3 * i + 1]), t2 = tanh((double) o[3 * i + 2]);
 	double const s00 = scale2[2 * i], s11 = scale2[2 * i + 1], s01 = sqrt(s00 * s11);
 	double const dc0 = g0 * s00 * r.x;

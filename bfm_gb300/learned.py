@@ -66,6 +66,9 @@ class DeviceProblem:
         masks = a(np.stack([c[2] for c in p.conds]).astype(np.uint8), np.uint8)
         edges = a(p.edges, np.int32) if p.edges is not None else None
         ok = ok and L.bfm_gpu_problem_set_conditions(P, len(p.conds), kinds, vals, masks, n_edges, edges, 0) == 0
+        if p.edge_loads is not None:
+            le, ll = p.edge_loads
+            ok = ok and L.bfm_gpu_problem_set_edge_loads(P, len(le), a(le, np.int32), a(ll, np.float64), 0) == 0
         assert ok, last_error()
         self.keep = keep
         self.precision = None
@@ -206,30 +209,31 @@ def training_meshes(seed: int, n_plates: int = 2, n_batch: int = 1, batch_parts:
 
 
 def concat(problems) -> M.Problem:
-    """Block-diagonal union of P1 problems as one Problem (per-element E and
-    nu; every Dirichlet and Neumann condition kept, node masks padded)."""
+    """Block-diagonal union of P1 problems as one Problem: per-element E and
+    nu, the Dirichlet masks of each kind merged (homogeneous values only),
+    every Neumann condition carried as per-edge loads (each mesh keeps its
+    own magnitude; loads skip constrained DOFs)."""
     off = np.cumsum([0] + [p.n_nodes for p in problems])
     n = int(off[-1])
     coords = np.concatenate([p.coords for p in problems])
     elems = np.concatenate([p.elems + off[k] for k, p in enumerate(problems)])
     eE = np.concatenate([p.elem_E if p.elem_E is not None else np.full(p.n_elems, p.E) for p in problems])
     enu = np.concatenate([p.elem_nu if p.elem_nu is not None else np.full(p.n_elems, p.nu) for p in problems])
-    conds, edges = [], []
+    masks = {M.DIRICHLET_X: np.zeros(n, bool), M.DIRICHLET_Y: np.zeros(n, bool)}
     for k, p in enumerate(problems):
         for kind, v, mask in p.conds:
-            m = np.zeros(n, bool)
-            m[off[k]:off[k + 1]] = mask
-            conds.append((kind, v, m))
-        if p.edges is not None:
-            edges.append(p.edges + off[k])
-    # Neumann conditions first so a node shared with a clamped side stays clamped
-    conds.sort(key=lambda c: c[0] < 2)
+            if kind in masks:
+                if v != 0.0:
+                    raise ValueError("concatenated Dirichlet conditions must be homogeneous")
+                masks[kind][off[k]:off[k + 1]] |= mask
+    loads = [M.neumann_edge_loads(p, off[k]) for k, p in enumerate(problems)]
     return M.Problem(name=f"concat{len(problems)}", kind=problems[0].kind, coords=coords, elems=elems,
-                     elem_E=eE, elem_nu=enu, forces=list(problems[0].forces), conds=conds,
-                     edges=np.concatenate(edges) if edges else None)
+                     elem_E=eE, elem_nu=enu, forces=list(problems[0].forces),
+                     conds=[(kind, 0.0, m) for kind, m in masks.items()],
+                     edge_loads=(np.concatenate([e for e, _ in loads]), np.concatenate([l for _, l in loads])))
 
 
-def pairs(prob: DeviceProblem, stops=(4, 16, 64, 256, 1024), rtol: float = 1e-10):
+def pairs(prob: DeviceProblem, stops=(2, 4, 8, 16, 32, 64, 128, 256, 512, 1024), rtol: float = 1e-10):
     """(r, e) device pairs (torch float64 tensors) from partial Jacobi-PCG solves."""
     import torch
     n = 2 * prob.n_nodes

@@ -34,6 +34,7 @@ class Problem:
     forces: list = field(default_factory=list)      # [(fx, fy)] body accelerations
     conds: list = field(default_factory=list)       # [(kind, value, mask[N] bool)]
     edges: np.ndarray | None = None                 # (M, 2) int64 boundary edges
+    edge_loads: tuple | None = None                 # (edges (M, 2), tractions (M, 2)): per-edge Neumann loads
 
     @property
     def n_nodes(self) -> int:
@@ -175,6 +176,26 @@ def batch_uneven(n: int = 256, seed: int = 4) -> list[Problem]:
         out.append(Problem(name=f"batch{k}_{nx}x{ny}", kind=3, coords=coords, elems=elems, nu=nu, elem_E=eE,
                            forces=[], conds=conds, edges=boundary_edges(nx, ny)))
     return out
+
+
+def neumann_edge_loads(p: Problem, node_offset: int = 0):
+    """The Neumann X/Y conditions of p as per-edge tractions: every boundary
+    edge with both end nodes flagged gets the condition's value in its
+    component (edges shifted by node_offset).  Returns (edges (M, 2) int32,
+    loads (M, 2) float64)."""
+    ed, ld = [], []
+    for kind, value, mask in p.conds:
+        if kind not in (NEUMANN_X, NEUMANN_Y) or p.edges is None:
+            continue
+        sel = mask[p.edges[:, 0]] & mask[p.edges[:, 1]]
+        e = p.edges[sel] + node_offset
+        l = np.zeros((len(e), 2))
+        l[:, 0 if kind == NEUMANN_X else 1] = value
+        ed.append(e)
+        ld.append(l)
+    if not ed:
+        return np.zeros((0, 2), np.int32), np.zeros((0, 2))
+    return np.concatenate(ed).astype(np.int32), np.concatenate(ld)
 
 
 def gauss_tables(kind: int):

@@ -256,7 +256,7 @@ int bfm_gpu_mpnn_load(bfm_gpu_mpnn_t* net, const char* path);
  * = (c0, c1, c2) per node, blocks[4*n_nodes] = B_i row-major. */
 int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, float* features, float* c, double* blocks);
 /* Loss of one (residual r, error e) pair, r = K e, z = B r:
- *     L = 1 - (z.r)^2 / ((z.K z)(e.r)),
+ *     L = -log( (z.r)^2 / ((z.K z)(e.r)) )  (>= 0; 0 when z is parallel to e),
  * and its gradient (FP32, parameter order above; NULL to skip).  r and e are
  * device arrays of 2*n_nodes doubles; needs the FP64 operator. */
 int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, const double* r, const double* e,

@@ -14,8 +14,9 @@ Network (parameters in this order, FP32 masters, BF16 copies on the GPU):
     c = 0.45 tanh(o)
     B_i = S_i (I + [[c0, c1], [c1, c2]]) S_i,  S_i = diag(K_ii)^(-1/2)
 Loss of one (residual r, error e) pair, z = B r:
-    L = 1 - (z.r)^2 / ((z.K z)(e.r))
-the A-norm reduction of e by the optimal step along z, subtracted from 1.
+    L = -log( (z.r)^2 / ((z.K z)(e.r)) )
+minus the log of the fraction of e's energy norm that the optimal step along
+z removes.
 """
 from __future__ import annotations
 
@@ -104,8 +105,8 @@ def loss_and_grad(theta, f, rp, cols, K, diag2, r, e, emulate=False):
     z = np.einsum("nij,nj->ni", B, r2).reshape(-1)
     Az = K @ z
     zr, zAz, er = z @ r, z @ Az, e @ r
-    loss = 1.0 - zr * zr / (zAz * er)
-    gz = (2.0 * zr / (zAz * er)) * ((zr / zAz) * Az - r)
+    loss = np.log(zAz) + np.log(er) - 2.0 * np.log(abs(zr))
+    gz = 2.0 * Az / zAz - 2.0 * r / zr
     g2 = gz.reshape(n, 2)
     s = 1.0 / np.sqrt(diag2)
     dc = np.stack([g2[:, 0] * s[:, 0] ** 2 * r2[:, 0],

@@ -125,8 +125,8 @@ def test_gradient_matches_oracle(setup, pair):
         args = (th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, K, diag2(rp, cols, vals, p.n_nodes),
                 r.cpu().numpy(), e.cpu().numpy())
         loss_ref, g_ref, _ = R.loss_and_grad(*args, emulate=True)
-        assert 0.0 <= loss_gpu <= 1.0
-        assert abs(loss_gpu - loss_ref) <= 1e-4 * abs(loss_ref)
+        assert loss_gpu >= 0.0
+        assert abs(loss_gpu - loss_ref) <= 1e-6 * max(1.0, abs(loss_ref))
         # every parameter block, relative to its own norm: BF16 storage emulated, FP32 sums
         k = 0
         for shape in R.SHAPES:
@@ -149,7 +149,8 @@ def test_training_lowers_the_loss(setup, pair):
     try:
         losses = [net.train_step(prob, r.data_ptr(), e.data_ptr(), 1e-3) for _ in range(60)]
         assert np.isfinite(losses).all()
-        assert np.mean(losses[-10:]) < 0.9 * np.mean(losses[:10])
+        # the energy removed by one preconditioned step grows by at least 10%
+        assert np.mean(losses[-10:]) < np.mean(losses[:10]) - np.log(1.1)
     finally:
         net.close()
 
@@ -185,7 +186,7 @@ def test_untrained_learned_solve_equals_jacobi(libbfm, precision):
         xl = prob.solution()
         assert sj.status == 0 and sl.status == 0 and sl.fallback == 0
         assert sl.iterations == sj.iterations
-        assert np.linalg.norm(xl - xj) <= 1e-12 * np.linalg.norm(xj)
+        np.testing.assert_array_equal(xl, xj)
     finally:
         net.close()
         prob.close()

@@ -35,7 +35,7 @@ def test_gradient_matches_finite_differences():
     r = K @ e
     th = rng.normal(0, 0.3, R.N_PARAMS)
     loss, g, _ = R.loss_and_grad(th, f, rp, cols, K, d2, r, e)
-    assert 0.0 <= loss <= 1.0
+    assert loss >= 0.0
     idx = rng.choice(R.N_PARAMS, 60, replace=False)
     h = 1e-6
     for k in idx:
