@@ -40,6 +40,32 @@ sys.path.insert(0, str(ROOT))
 METRIC = "solve ms to 1e-8 residual: learned+mixed PCG vs plain FP64 PCG; SpMV HBM GB/s"
 RTOL = 1e-8
 
+# solve methods: precision and preconditioner of bfm_gpu_problem_solve
+METHODS = {"fp64": ("FP64", "PC_JACOBI"), "fp64_df": ("FP64_DF", "PC_JACOBI"),
+           "mixed_exact": ("MIXED_EXACT", "PC_JACOBI"), "mixed": ("MIXED", "PC_JACOBI"),
+           "learned_fp64": ("FP64", "PC_LEARNED"), "learned_df": ("FP64_DF", "PC_LEARNED"),
+           "learned_mixed": ("MIXED", "PC_LEARNED")}
+# fused SpMV kernel (K1) of each precision: the roofline kernel
+SPMV_KERNEL = {0: "k_hs64_spmv", 1: "k_mx_spmv", 2: "k_mx_spmv", 3: "k_hsdf_spmv"}
+# DRAM bytes (read + write) of one K1 launch on the 2048x512 perforated plate,
+# from one ncu capture each (the profiles/ summaries named here)
+SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md"),
+                3: (329_563_136, "profiles/spmv_df_hs_perforated_2048x512.md"),
+                1: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md"),
+                2: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md")}
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    """Max of a per-rank number over all ranks (NCCL on GPUs, gloo on CPUs)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
 
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
@@ -164,11 +190,18 @@ def run_gpu(args, rank: int, world: int):
     # would replace by a private one)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    methods = {"fp64": (bfm_gb300.FP64, bfm_gb300.PC_JACOBI),
-               "mixed": (bfm_gb300.MIXED, bfm_gb300.PC_JACOBI),
-               "mixed_exact": (bfm_gb300.MIXED_EXACT, bfm_gb300.PC_JACOBI),
-               "fp64_df": (bfm_gb300.FP64_DF, bfm_gb300.PC_JACOBI)}
-    chosen = ["fp64", "fp64_df", "mixed_exact", "mixed"] if args.method == "best" else [args.method]
+    methods = {k: (getattr(bfm_gb300, a), getattr(bfm_gb300, b)) for k, (a, b) in METHODS.items()}
+    net = None
+    from bfm_gb300 import learned
+    if learned.WEIGHTS.exists():
+        net = learned.Network(path=learned.WEIGHTS)
+        net.use()
+    if args.method == "best":
+        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed"] + (["learned_df", "learned_mixed"] if net else [])
+    else:
+        chosen = [args.method]
+        if methods[args.method][1] == bfm_gb300.PC_LEARNED and net is None:
+            raise SystemExit(f"{learned.WEIGHTS} is missing: train it with python -m bfm_gb300.learned")
     results = {}
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
     for m in chosen:
@@ -193,11 +226,7 @@ def run_gpu(args, rank: int, world: int):
                 step()
             ev1.record(stream)
             torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1) / args.steps
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world)
         s = bfm_gb300.bfm_gpu_stats_t()
         assert lib.bfm_gpu_problem_stats(P, C.byref(s)) == 0
         x = np.zeros(p.n_dof)
@@ -206,17 +235,20 @@ def run_gpu(args, rank: int, world: int):
         t_spmv, t_upd = C.c_double(), C.c_double()
         assert lib.bfm_gpu_problem_time_kernels(P, 50, C.byref(t_spmv), C.byref(t_upd)) == 0
         results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual, repl=s.replacements,
-                          ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks,
-                          ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, x=x)
+                          ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks, fallback=s.fallback,
+                          ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, pc=pc, x=x)
     lib.bfm_gpu_problem_destroy(P)
-    # displacement error of every method against the FP64 solution
+    # displacement error of every method against the FP64 solution (the FP64
+    # direct oracle does not fit the host at this size; the FP64 PCG solution
+    # to 1e-8 stands in for it and is itself checked against the oracle in tests/)
     ref = results.get("fp64", {}).get("x")
     for m, r in results.items():
         r["err_vs_fp64"] = None if ref is None else float(np.linalg.norm(r["x"] - ref) / np.linalg.norm(ref))
     ok = [m for m, r in results.items() if r["status"] == 0 and (r["err_vs_fp64"] is None or r["err_vs_fp64"] <= 1e-6)]
     best = min(ok or results, key=lambda k: results[k]["ms"])
 
-    # end-to-end through bfm_sim_run with host buffers
+    # end-to-end through bfm_sim_run with host buffers (the learned methods use
+    # the network selected above through the same global options)
     prec, pc = methods[best]
     lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc)))
     h = api.SimHandle.from_problem(lib, p)
@@ -230,6 +262,9 @@ def run_gpu(args, rank: int, world: int):
     h2d = p.n_nodes * 16 + p.n_elems * p.kind * 4 + n_masks + (0 if p.edges is None else 8 * len(p.edges)) + \
         (0 if p.elem_E is None else 8 * p.n_elems)
     d2h = p.n_dof * 8
+    lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
+    if net is not None:
+        net.close()
     return p, results, best, dict(ms=e2e_ms, h2d=h2d, d2h=d2h)
 
 
@@ -275,8 +310,7 @@ def profile(args):
     import bfm_gb300
     lib = bfm_gb300.lib()
     p = workload(args.workload)
-    prec = {"fp64": bfm_gb300.FP64, "mixed": bfm_gb300.MIXED, "mixed_exact": bfm_gb300.MIXED_EXACT,
-            "fp64_df": bfm_gb300.FP64_DF, "best": bfm_gb300.FP64}[args.method]
+    prec = getattr(bfm_gb300, METHODS.get(args.method, ("FP64", ""))[0])
     P, keep = device_problem(lib, p, None)
     assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
     s = bfm_gb300.bfm_gpu_stats_t()
@@ -307,7 +341,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="perforated")
-    ap.add_argument("--method", default="best", choices=["fp64", "fp64_df", "mixed", "mixed_exact", "best"])
+    ap.add_argument("--method", default="best", choices=list(METHODS) + ["best"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="assemble once and launch the two CG kernels --reps times each, standalone "
@@ -347,9 +381,14 @@ def main():
     hbm, peak_kind = peaks()
     r = results[best]
     nb = r["n_blocks"]
-    bytes_spmv = algorithmic_bytes_spmv(nb, p.n_nodes, r["prec"])
+    bytes_spmv = algorithmic_bytes_spmv(nb, p.n_nodes, r["prec"], r["pc"] != 0)
     achieved = bytes_spmv / (r["ms_spmv"] * 1e-3) / 1e9
-    launches_per_step = 24 + 2 * r["iters"] + 1
+    traffic, traffic_src = (SPMV_TRAFFIC.get(r["prec"], (None, None))
+                            if args.workload == "perforated" and r["pc"] == 0 else (None, None))
+    # assembly (pattern, Dirichlet marks, element loop, loads: about 24 kernels),
+    # solve init + 2 kernels per iteration + replacement kernels, finish;
+    # the learned preconditioner adds its 12 inference kernels per solve
+    launches_per_step = 24 + 1 + 2 * r["iters"] + 2 * r["repl"] + 2 + (12 if r["pc"] == 2 else 0)
     value = r["ms"] / world
     line = {
         "metric": METRIC,
@@ -373,15 +412,15 @@ def main():
         "ms_solve": round(r["ms_solve"], 3),
         "methods": {k: {"ms": round(v["ms"], 3), "iterations": v["iters"], "status": v["status"],
                         "rel_residual": v["rel_res"], "err_vs_fp64": v["err_vs_fp64"],
-                        "replacements": v["repl"], "ms_assemble": round(v["ms_assemble"], 3),
+                        "replacements": v["repl"], "fallback": v["fallback"], "ms_assemble": round(v["ms_assemble"], 3),
                         "spmv_ms": round(v["ms_spmv"], 5), "update_ms": round(v["ms_update"], 5)}
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 3), "traffic": None, "kernel": "k_cg_spmv_dots",
-                     "algorithmic_bytes": bytes_spmv, "kernel_ms": round(r["ms_spmv"], 5),
-                     "peak_source": peak_kind},
+                     "frac": round(achieved / hbm, 3), "traffic": traffic, "traffic_source": traffic_src,
+                     "kernel": SPMV_KERNEL[r["prec"]], "algorithmic_bytes": bytes_spmv,
+                     "kernel_ms": round(r["ms_spmv"], 5), "peak_source": peak_kind},
         "e2e": {"value": round(e2e["ms"], 3), "unit": "ms", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},
         "gpu_launches": launches_per_step * args.steps,

@@ -1,7 +1,8 @@
 // Learned block preconditioner of the GB300 libbfm: a message-passing network
-// over the mesh's node graph that predicts one SPD 2x2 block per node,
-//     B_i = S_i (I + C_i) S_i,  S_i = diag(K_ii)^(-1/2),  C_i = [[c0, c1], [c1, c2]],
-// used in place of the Jacobi diagonal inside PCG (c = 0 is exactly Jacobi,
+// over the mesh's node graph that predicts, per node, a correction of the
+// block-Jacobi block,
+//     B_i = K_ii^-1 + L_i C_i L_i^T,  L_i L_i^T = K_ii^-1,  C_i = [[c0, c1], [c1, c2]],
+// used in place of the Jacobi diagonal inside PCG (c = 0 is block Jacobi,
 // which is where an untrained network starts).  No counterpart in the
 // reference; its CPU oracle is oracle/mpnn_ref.py.
 //
@@ -245,10 +246,16 @@ __global__ void k_agg(int N, const int* __restrict__ row_ptr, const int* __restr
 	m[(long) i * HID + c] = __float2bfloat16(s / (float) (r1 - r0));
 }
 
-// o = Wo h3 + bo, c = 0.45 tanh(o); the preconditioner blocks from c
+// o = Wo h3 + bo, c = 0.45 tanh(o); the preconditioner blocks from c:
+//     B = Kd^-1 + L C L^T,  L L^T = Kd^-1 (Cholesky),  C = [[c0, c1], [c1, c2]],
+// Kd the node's 2x2 diagonal block.  L = [[sqrt(k11/det), 0],
+// [-k01/sqrt(det k11), 1/sqrt(k11)]].  B = L (I + C) L^T is SPD for
+// |c| <= 0.45, and at c = 0 it is block Jacobi (the inverse computed as the
+// assembly epilogue does).  A non-SPD diagonal block gives B = 0 (the solve
+// then breaks down and falls back to Jacobi).
 __global__ void k_head(int N, const bf16* __restrict__ h3, const float* __restrict__ theta, float* __restrict__ o,
                        const int* __restrict__ row_ptr, const int* __restrict__ cols, const double* __restrict__ vals64,
-                       const float* __restrict__ vals32, double* __restrict__ blocks, double* __restrict__ scale2) {
+                       const float* __restrict__ vals32, double* __restrict__ blocks, double* __restrict__ lfac) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
 	float oo[3];
@@ -258,22 +265,30 @@ __global__ void k_head(int N, const bf16* __restrict__ h3, const float* __restri
 		oo[q] = s;
 		if (o) o[3 * i + q] = s;
 	}
-	double k00 = 0.0, k11 = 0.0;
+	double k00 = 0.0, k01 = 0.0, k10 = 0.0, k11 = 0.0;
 	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++)
 		if (cols[k] == i) {
 			k00 = vals64 ? vals64[4l * k] : (double) vals32[4l * k];
+			k01 = vals64 ? vals64[4l * k + 1] : (double) vals32[4l * k + 1];
+			k10 = vals64 ? vals64[4l * k + 2] : (double) vals32[4l * k + 2];
 			k11 = vals64 ? vals64[4l * k + 3] : (double) vals32[4l * k + 3];
 		}
-	// diagonal entries as (1 + c) / k: exactly the Jacobi values at c = 0
-	double const i0 = k00 > 0.0 ? 1.0 / k00 : 0.0, i1 = k11 > 0.0 ? 1.0 / k11 : 0.0;
-	double const s01 = sqrt(i0 * i1);
-	scale2[2 * i] = i0;
-	scale2[2 * i + 1] = i1;
+	double const det = k00 * k11 - k01 * k10;
+	bool const spd = det > 0.0 && k11 > 0.0;
+	double const id = spd ? 1.0 / det : 0.0;
+	double const m0 = k11 * id, m1 = -k01 * id, m3 = k00 * id;
+	double const l00 = spd ? sqrt(k11 * id) : 0.0;
+	double const l10 = spd ? -k01 / sqrt(det * k11) : 0.0;
+	double const l11 = spd ? 1.0 / sqrt(k11) : 0.0;
+	lfac[3 * i] = l00;
+	lfac[3 * i + 1] = l10;
+	lfac[3 * i + 2] = l11;
 	double const c0 = C_SCALE * tanh((double) oo[0]), c1 = C_SCALE * tanh((double) oo[1]), c2 = C_SCALE * tanh((double) oo[2]);
-	blocks[4 * i + 0] = (1.0 + c0) * i0;
-	blocks[4 * i + 1] = s01 * c1;
-	blocks[4 * i + 2] = s01 * c1;
-	blocks[4 * i + 3] = (1.0 + c2) * i1;
+	double const b01 = l00 * l10 * c0 + l00 * l11 * c1;
+	blocks[4 * i + 0] = m0 + l00 * l00 * c0;
+	blocks[4 * i + 1] = m1 + b01;
+	blocks[4 * i + 2] = m1 + b01;
+	blocks[4 * i + 3] = m3 + (l10 * l10 * c0 + 2.0 * l10 * l11 * c1 + l11 * l11 * c2);
 }
 
 // ---------------------------------------------------------------- loss
@@ -327,17 +342,20 @@ __global__ void k_loss_dots(LossArgs a) {
 }
 
 // dL/dz = 2 Az / (z.Az) - 2 r / (z.r) -> dL/dc -> dL/do (N x 3, FP32)
-__global__ void k_loss_back(LossArgs a, const float* __restrict__ o, const double* __restrict__ scale2, float* __restrict__ d_o) {
+__global__ void k_loss_back(LossArgs a, const float* __restrict__ o, const double* __restrict__ lfac, float* __restrict__ d_o) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.N) return;
 	double const zr = a.sc[0], zaz = a.sc[1];
 	double2 const az = ld2(a.az, i), r = ld2(a.r, i);
 	double const g0 = 2.0 * az.x / zaz - 2.0 * r.x / zr, g1 = 2.0 * az.y / zaz - 2.0 * r.y / zr;
 	double const t0 = tanh((double) o[3 * i]), t1 = tanh((double) o[3 * i + 1]), t2 = tanh((double) o[3 * i + 2]);
-	double const s00 = scale2[2 * i], s11 = scale2[2 * i + 1], s01 = sqrt(s00 * s11);
-	double const dc0 = g0 * s00 * r.x;
-	double const dc1 = g0 * s01 * r.y + g1 * s01 * r.x;
-	double const dc2 = g1 * s11 * r.y;
+	// z = L (I + C) y with y = L^T r: dL/dc from w = L^T dL/dz
+	double const l00 = lfac[3 * i], l10 = lfac[3 * i + 1], l11 = lfac[3 * i + 2];
+	double const y0 = l00 * r.x + l10 * r.y, y1 = l11 * r.y;
+	double const w0 = l00 * g0 + l10 * g1, w1 = l11 * g1;
+	double const dc0 = w0 * y0;
+	double const dc1 = w0 * y1 + w1 * y0;
+	double const dc2 = w1 * y1;
 	d_o[3 * i + 0] = (float) (dc0 * C_SCALE * (1.0 - t0 * t0));
 	d_o[3 * i + 1] = (float) (dc1 * C_SCALE * (1.0 - t1 * t1));
 	d_o[3 * i + 2] = (float) (dc2 * C_SCALE * (1.0 - t2 * t2));
@@ -507,7 +525,7 @@ struct bfm_gpu_mpnn {
 	long cap_n;
 	bf16 *f, *h[4], *m[3], *dpre;
 	float *o, *d_o, *dh, *dx;
-	double *blocks, *scale2, *z, *az, *sc, *partials, *rms, *scratch;
+	double *blocks, *lfac, *z, *az, *sc, *partials, *rms, *scratch;
 	unsigned* ticket;
 };
 
@@ -515,14 +533,14 @@ namespace {
 
 void free_acts(bfm_gpu_mpnn* net) {
 	void* p[] = {net->f, net->h[0], net->h[1], net->h[2], net->h[3], net->m[0], net->m[1], net->m[2], net->dpre, net->o,
-	             net->d_o, net->dh, net->dx, net->blocks, net->scale2, net->z, net->az, net->scratch};
+	             net->d_o, net->dh, net->dx, net->blocks, net->lfac, net->z, net->az, net->scratch};
 	for (void* q : p)
 		if (q) cudaFree(q);
 	net->f = net->dpre = nullptr;
 	for (auto& q : net->h) q = nullptr;
 	for (auto& q : net->m) q = nullptr;
 	net->o = net->d_o = net->dh = net->dx = nullptr;
-	net->blocks = net->scale2 = net->z = net->az = net->scratch = nullptr;
+	net->blocks = net->lfac = net->z = net->az = net->scratch = nullptr;
 	net->cap_n = 0;
 }
 
@@ -544,7 +562,7 @@ int ensure_acts(bfm_gpu_mpnn* net, long N) {
 	for (auto& q : net->m)
 		if (alloc(&q, n * HID)) return -1;
 	if (alloc(&net->dpre, n * HID) || alloc(&net->o, n * 3) || alloc(&net->d_o, n * 3) || alloc(&net->dh, n * HID) ||
-	    alloc(&net->dx, n * HK) || alloc(&net->blocks, n * 4) || alloc(&net->scale2, n * 2) || alloc(&net->z, n * 2) ||
+	    alloc(&net->dx, n * HK) || alloc(&net->blocks, n * 4) || alloc(&net->lfac, n * 3) || alloc(&net->z, n * 2) ||
 	    alloc(&net->az, n * 2) || alloc(&net->scratch, n))
 		return -1;
 	long const chunks = (n + DW_CHUNK - 1) / DW_CHUNK, heads = (n + HEAD_NODES - 1) / HEAD_NODES;
@@ -599,7 +617,7 @@ int forward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, cudaStream_t st) {
 		                                      net->h[l]);
 	}
 	k_head<<<nb(N), 256, 0, st>>>(N, net->h[3], net->d.theta, net->o, bf.row_ptr, bf.cols, bf.vals64_any, bf.vals32,
-	                               net->blocks, net->scale2);
+	                               net->blocks, net->lfac);
 	MCK(cudaGetLastError());
 	return 0;
 }
@@ -626,7 +644,7 @@ int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const dou
 	la.sc = net->sc;
 	k_loss_z<<<nb(N), 256, 0, st>>>(la);
 	k_loss_dots<<<FEAT_GRID, TPB_K, 0, st>>>(la);
-	k_loss_back<<<nb(N), 256, 0, st>>>(la, net->o, net->scale2, net->d_o);
+	k_loss_back<<<nb(N), 256, 0, st>>>(la, net->o, net->lfac, net->d_o);
 	int const heads = (N + HEAD_NODES - 1) / HEAD_NODES > 0 ? (N + HEAD_NODES - 1) / HEAD_NODES : 1;
 	k_head_back<<<heads, HEAD_TPB, 0, st>>>(N, net->d_o, net->h[3], net->d.theta, net->dh, net->d.gpart);
 	k_reduce_parts<<<nb(HEAD_OUT), 256, 0, st>>>(net->d.gpart, heads, HEAD_OUT, net->d.grad, O_WO, 3 * HID, O_BO);
@@ -659,7 +677,7 @@ int read_loss(bfm_gpu_mpnn* net, double* loss, cudaStream_t st) {
 }
 
 // He-normal weights from a fixed-seed generator (xorshift64 + Box-Muller),
-// zero biases and a zero head: c = 0, so an untrained network is exactly Jacobi
+// zero biases and a zero head: c = 0, so an untrained network is block Jacobi
 void init_theta(float* th, unsigned seed) {
 	uint64_t s = 0x9E3779B97F4A7C15ull ^ ((uint64_t) seed * 0xD1B54A32D192ED03ull);
 	auto uni = [&]() {

@@ -27,7 +27,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import (DEVICE, FP64, PC_JACOBI, PC_LEARNED, bfm_gpu_stats_t, default_opts, last_error, lib)
+from . import (DEVICE, FP64, PC_BLOCK_JACOBI, PC_JACOBI, PC_LEARNED, bfm_gpu_stats_t, default_opts, last_error, lib)
 from . import meshgen as M
 
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "mpnn_plate.bin"
@@ -285,12 +285,13 @@ def train(net: Network, probs, n_pairs: int, lr: float = 3e-4, epochs: int = 1, 
 
 
 def evaluate(net: Network, prob: DeviceProblem, rtol: float = 1e-8, precision: int | None = None):
-    """Iterations and ms of Jacobi vs learned PCG on one problem."""
+    """Iterations and ms of Jacobi, block-Jacobi (the untrained network) and
+    learned PCG on one problem."""
     if precision is not None and precision != prob.precision:
         prob.assemble(precision)
     net.use()
     res = {}
-    for name, pc in (("jacobi", PC_JACOBI), ("learned", PC_LEARNED)):
+    for name, pc in (("jacobi", PC_JACOBI), ("block_jacobi", PC_BLOCK_JACOBI), ("learned", PC_LEARNED)):
         s = prob.solve(precond=pc, rtol=rtol)
         res[name] = dict(iterations=s.iterations, status=s.status, fallback=s.fallback, ms=s.ms_solve,
                          rel_residual=s.rel_residual)

@@ -225,18 +225,20 @@ int bfm_gpu_problem_apply(bfm_gpu_problem_t* problem, const double* x, double* y
 /* ---------------------------------------------------------------- learned preconditioner */
 
 /* No counterpart in the reference.  A message-passing network over the node
- * graph predicts, per node i, an SPD 2x2 block
- *     B_i = S_i (I + C_i) S_i,  S_i = diag(K_ii)^(-1/2),  C_i = 0.45 tanh(o_i)
- * (o_i: the network's 3 outputs, C_i symmetric), used by PCG in place of the
+ * graph predicts, per node i, a correction C_i of the block-Jacobi block:
+ *     B_i = K_ii^-1 + L_i C_i L_i^T,  L_i L_i^T = K_ii^-1 (Cholesky),
+ *     C_i = 0.45 tanh(o_i) as [[c0, c1], [c1, c2]]
+ * (K_ii: node i's 2x2 diagonal block; o_i: the network's 3 outputs).  B_i =
+ * L_i (I + C_i) L_i^T is SPD for any output, and PCG uses it in place of the
  * Jacobi diagonal when opts->precond is BFM_GPU_PC_LEARNED.  Inputs per node:
  * log-stiffness contrasts of the incident elements, Poisson ratio, Dirichlet
  * flags, graph degree, the Jacobi-scaled load (the initial residual), and the
  * diagonal block's scale ratio and coupling.  Layers: 16 -> 64, three times
  * [h, mean of h over the graph row] 128 -> 64 (ReLU), head 64 -> 3.  BF16
  * weights and activations on the tensor cores, FP32 accumulation and FP32
- * master weights; 26,051 parameters.  An untrained network (zero head) is
- * exactly Jacobi.  The solve falls back to Jacobi (stats.fallback = 1) when
- * the learned solve breaks down or stagnates above 1e-6. */
+ * master weights; 26,051 parameters.  An untrained network (zero head) gives
+ * block Jacobi.  The solve falls back to plain Jacobi (stats.fallback = 1)
+ * when the learned solve breaks down or stagnates above 1e-6. */
 typedef struct bfm_gpu_mpnn bfm_gpu_mpnn_t;
 
 int bfm_gpu_mpnn_param_count(void);

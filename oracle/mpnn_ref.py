@@ -12,7 +12,8 @@ Network (parameters in this order, FP32 masters, BF16 copies on the GPU):
           m = mean of h over the node's row of the node graph (itself included)
     o = Wo h3 + bo                             Wo: 3 x 64
     c = 0.45 tanh(o)
-    B_i = S_i (I + [[c0, c1], [c1, c2]]) S_i,  S_i = diag(K_ii)^(-1/2)
+    B_i = K_ii^-1 + L_i C_i L_i^T,  L_i L_i^T = K_ii^-1 (Cholesky),  C_i = [[c0, c1], [c1, c2]]
+          (K_ii: the node's 2x2 diagonal block; c = 0 is block Jacobi)
 Loss of one (residual r, error e) pair, z = B r:
     L = -log( (z.r)^2 / ((z.K z)(e.r)) )
 minus the log of the fraction of e's energy norm that the optimal step along
@@ -84,23 +85,32 @@ def forward(theta, f, rp, cols, emulate=False):
     return c, dict(hs=hs, xs=xs, o=o)
 
 
-def blocks(c, diag2):
-    """B_i as (n, 2, 2) from c (n, 3) and the 2x2 diagonal entries (n, 2)"""
-    s = 1.0 / np.sqrt(diag2)
-    B = np.zeros((len(c), 2, 2))
-    B[:, 0, 0] = s[:, 0] * s[:, 0] * (1 + c[:, 0])
-    B[:, 0, 1] = B[:, 1, 0] = s[:, 0] * s[:, 1] * c[:, 1]
-    B[:, 1, 1] = s[:, 1] * s[:, 1] * (1 + c[:, 2])
-    return B
+def chol_inv(Kd):
+    """L (n, 2, 2) lower triangular with L L^T = Kd^-1 for SPD 2x2 blocks Kd."""
+    k00, k01, k11 = Kd[:, 0, 0], Kd[:, 0, 1], Kd[:, 1, 1]
+    det = k00 * k11 - k01 * Kd[:, 1, 0]
+    L = np.zeros_like(Kd)
+    L[:, 0, 0] = np.sqrt(k11 / det)
+    L[:, 1, 0] = -k01 / np.sqrt(det * k11)
+    L[:, 1, 1] = 1.0 / np.sqrt(k11)
+    return L
 
 
-def loss_and_grad(theta, f, rp, cols, K, diag2, r, e, emulate=False):
+def blocks(c, Kd):
+    """B_i as (n, 2, 2) from c (n, 3) and the diagonal blocks Kd (n, 2, 2)"""
+    L = chol_inv(Kd)
+    C = np.zeros_like(Kd)
+    C[:, 0, 0], C[:, 0, 1], C[:, 1, 0], C[:, 1, 1] = c[:, 0], c[:, 1], c[:, 1], c[:, 2]
+    return np.linalg.inv(Kd) + L @ C @ np.transpose(L, (0, 2, 1))
+
+
+def loss_and_grad(theta, f, rp, cols, K, Kd, r, e, emulate=False):
     """loss and d loss / d theta (float64); emulate as in forward (the
     back-propagated signal entering each dense layer's GEMMs is BF16 too)"""
     q = bf16 if emulate else _id
     c, cache = forward(theta, f, rp, cols, emulate)
     n = len(c)
-    B = blocks(c, diag2)
+    B = blocks(c, Kd)
     r2 = r.reshape(n, 2)
     z = np.einsum("nij,nj->ni", B, r2).reshape(-1)
     Az = K @ z
@@ -108,10 +118,12 @@ def loss_and_grad(theta, f, rp, cols, K, diag2, r, e, emulate=False):
     loss = np.log(zAz) + np.log(er) - 2.0 * np.log(abs(zr))
     gz = 2.0 * Az / zAz - 2.0 * r / zr
     g2 = gz.reshape(n, 2)
-    s = 1.0 / np.sqrt(diag2)
-    dc = np.stack([g2[:, 0] * s[:, 0] ** 2 * r2[:, 0],
-                   g2[:, 0] * s[:, 0] * s[:, 1] * r2[:, 1] + g2[:, 1] * s[:, 1] * s[:, 0] * r2[:, 0],
-                   g2[:, 1] * s[:, 1] ** 2 * r2[:, 1]], 1)
+    # z = L (I + C) y, y = L^T r: d loss / dc from w = L^T d loss / dz
+    L = chol_inv(Kd)
+    Lt = np.transpose(L, (0, 2, 1))
+    y = np.einsum("nij,nj->ni", Lt, r2)
+    w = np.einsum("nij,nj->ni", Lt, g2)
+    dc = np.stack([w[:, 0] * y[:, 0], w[:, 0] * y[:, 1] + w[:, 1] * y[:, 0], w[:, 1] * y[:, 1]], 1)
     do = dc * C_SCALE * (1.0 - np.tanh(cache["o"]) ** 2)
     W0, b0, W1, b1, W2, b2, W3, b3, Wo, bo = unpack(theta)
     grads = [None] * 10

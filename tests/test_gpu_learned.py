@@ -32,12 +32,11 @@ def scalar_K(rp, cols, vals, n):
     return sp.csr_matrix((vals.reshape(-1), (R_, C_)), shape=(2 * n, 2 * n))
 
 
-def diag2(rp, cols, vals, n):
+def diag_blocks(rp, cols, vals, n):
     rows = np.repeat(np.arange(n), np.diff(rp))
     d = rows == cols
-    out = np.zeros((n, 2))
-    out[rows[d], 0] = vals[d, 0, 0]
-    out[rows[d], 1] = vals[d, 1, 1]
+    out = np.zeros((n, 2, 2))
+    out[rows[d]] = vals[d]
     return out
 
 
@@ -74,14 +73,12 @@ def test_features_match_oracle(setup):
     assert np.count_nonzero(f_gpu[:, 11:]) == 0
 
 
-def test_untrained_network_is_jacobi(setup):
+def test_untrained_network_is_block_jacobi(setup):
     p, prob, net, (rp, cols, vals, b) = setup
     _, c, B = net.forward(prob)
     assert np.all(c == 0.0)
-    d = diag2(rp, cols, vals, p.n_nodes)
-    np.testing.assert_array_equal(B[:, 0, 1], 0.0)
-    np.testing.assert_allclose(B[:, 0, 0], 1.0 / d[:, 0], rtol=1e-15)
-    np.testing.assert_allclose(B[:, 1, 1], 1.0 / d[:, 1], rtol=1e-15)
+    Kd = diag_blocks(rp, cols, vals, p.n_nodes)
+    np.testing.assert_allclose(B, np.linalg.inv(Kd), rtol=1e-13, atol=0)
 
 
 def test_forward_matches_oracle(setup):
@@ -95,7 +92,7 @@ def test_forward_matches_oracle(setup):
         assert np.abs(c_ref).max() > 0.05
         # FP32 accumulation order differs from float64: 1e-3 of the output scale
         assert np.abs(c_gpu - c_ref).max() <= 1e-3 * R.C_SCALE
-        B_ref = R.blocks(c_ref, diag2(rp, cols, vals, p.n_nodes))
+        B_ref = R.blocks(c_ref, diag_blocks(rp, cols, vals, p.n_nodes))
         assert np.linalg.norm(B_gpu - B_ref) <= 5e-3 * np.linalg.norm(B_ref)
         # every block SPD: 1 + c0 > 0 and det(I + C) > 0 for |c| < 0.45
         det = B_gpu[:, 0, 0] * B_gpu[:, 1, 1] - B_gpu[:, 0, 1] ** 2
@@ -122,7 +119,7 @@ def test_gradient_matches_oracle(setup, pair):
         f_gpu, _, _ = net.forward(prob)
         loss_gpu, g_gpu = net.gradient(prob, r.data_ptr(), e.data_ptr())
         K = scalar_K(rp, cols, vals, p.n_nodes)
-        args = (th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, K, diag2(rp, cols, vals, p.n_nodes),
+        args = (th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, K, diag_blocks(rp, cols, vals, p.n_nodes),
                 r.cpu().numpy(), e.cpu().numpy())
         loss_ref, g_ref, _ = R.loss_and_grad(*args, emulate=True)
         assert loss_gpu >= 0.0
@@ -174,13 +171,13 @@ def test_save_load_roundtrip(setup, tmp_path):
 
 
 @pytest.mark.parametrize("precision", [bfm_gb300.FP64, bfm_gb300.MIXED_EXACT, bfm_gb300.FP64_DF])
-def test_untrained_learned_solve_equals_jacobi(libbfm, precision):
+def test_untrained_learned_solve_equals_block_jacobi(libbfm, precision):
     p = soft_plate(64, 16, seed=12)
     prob = LN.DeviceProblem(p, precision=precision)
     net = LN.Network(seed=0)
     try:
         net.use()
-        sj = prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-8)
+        sj = prob.solve(precond=bfm_gb300.PC_BLOCK_JACOBI, rtol=1e-8)
         xj = prob.solution()
         sl = prob.solve(precond=bfm_gb300.PC_LEARNED, rtol=1e-8)
         xl = prob.solution()
@@ -242,6 +239,8 @@ def test_trained_network_beats_jacobi(libbfm):
         assert ev["learned"]["status"] == 0 and ev["learned"]["fallback"] == 0
         assert ev["learned"]["rel_residual"] <= 1e-8
         assert ev["learned"]["iterations"] < ev["jacobi"]["iterations"]
+        # training moves it from its block-Jacobi start without losing ground
+        assert ev["learned"]["iterations"] <= ev["block_jacobi"]["iterations"]
     finally:
         net.close()
         for q in probs:

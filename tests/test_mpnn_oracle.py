@@ -30,7 +30,7 @@ def test_gradient_matches_finite_differences():
     rng = np.random.default_rng(1)
     f = rng.normal(size=(n, R.F_IN))
     K = spd(n, 2)
-    d2 = np.stack([np.diag(K)[0::2], np.diag(K)[1::2]], 1)
+    d2 = np.stack([K[2 * i:2 * i + 2, 2 * i:2 * i + 2] for i in range(n)])
     e = rng.normal(size=2 * n)
     r = K @ e
     th = rng.normal(0, 0.3, R.N_PARAMS)
@@ -55,7 +55,10 @@ def test_bf16_rounding():
 def test_blocks_are_spd_for_any_output():
     rng = np.random.default_rng(3)
     c = R.C_SCALE * np.tanh(rng.normal(0, 10, (1000, 3)))
-    d2 = np.exp(rng.normal(0, 3, (1000, 2)))
-    B = R.blocks(c, d2)
+    A = rng.normal(size=(1000, 2, 2))
+    Kd = A @ np.transpose(A, (0, 2, 1)) + 0.1 * np.eye(2) * np.exp(rng.normal(0, 3, (1000, 1, 1)))
+    B = R.blocks(c, Kd)
     ev = np.linalg.eigvalsh(B)
     assert (ev > 0).all()
+    # c = 0: block Jacobi
+    np.testing.assert_allclose(R.blocks(0 * c, Kd), np.linalg.inv(Kd), rtol=1e-12)
