@@ -63,6 +63,8 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_stream": (_vp, [_vp]),
     "bfm_gpu_problem_time_kernels": (_i, [_vp, _i, _P(_d), _P(_d)]),
     "bfm_gpu_problem_autotune": (_i, [_vp, _P(_i)]),
+    "bfm_gpu_problem_shape": (_i, [_vp, _P(_i)]),
+    "bfm_gpu_problem_set_shape": (_i, [_vp, _i]),
     "bfm_gpu_pcg_solve_noalloc": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _i, _P(_i), _P(_d), _vp]),
     "bfm_gpu_problem_set_edge_loads": (_i, [_vp, _i, _vp, _vp, _i]),
     "bfm_gpu_problem_set_parts": (_i, [_vp, _i, _vp]),
@@ -78,8 +80,8 @@ GPU_PROTOTYPES = {
     "bfm_gpu_mpnn_save": (_i, [_vp, C.c_char_p]),
     "bfm_gpu_mpnn_load": (_i, [_vp, C.c_char_p]),
     "bfm_gpu_mpnn_forward": (_i, [_vp, _vp, _vp, _vp, _vp]),
-    "bfm_gpu_mpnn_gradient": (_i, [_vp, _vp, _vp, _vp, _P(_d), _vp]),
-    "bfm_gpu_mpnn_train_step": (_i, [_vp, _vp, _vp, _vp, _d, _P(_d)]),
+    "bfm_gpu_mpnn_gradient": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _P(_d), _vp]),
+    "bfm_gpu_mpnn_train_step": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _d, _P(_d)]),
     "bfm_gpu_mpnn_use": (_i, [_vp]),
 }
 

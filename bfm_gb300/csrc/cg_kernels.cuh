@@ -148,6 +148,52 @@ __device__ __forceinline__ void row_product(const int* __restrict__ cols, const 
 	}
 }
 
+// Same product with the loads batched: each lane first reads NB column
+// indices, then issues the NB neighbour gathers and the NB block loads, then
+// does the arithmetic, so NB independent memory chains are in flight per lane
+// instead of one (the kernels are bound by gather latency, not bandwidth).
+// Entries are summed in the order k = ks+sub, ks+sub+LPR, ... as above.
+template <int LPR, int NB, typename A, typename V, typename G>
+__device__ __forceinline__ void row_product_pf(const int* __restrict__ cols, const V* __restrict__ vals, int ks, int ke,
+                                               int sub, G gather, A& y0, A& y1) {
+	y0 = A(0);
+	y1 = A(0);
+	for (int k0 = ks + sub; k0 < ke; k0 += LPR * NB) {
+		int c[NB];
+#pragma unroll
+		for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? cols[k0 + j * LPR] : -1;
+		A g0[NB], g1[NB];
+#pragma unroll
+		for (int j = 0; j < NB; j++) {
+			g0[j] = g1[j] = A(0);
+			if (c[j] >= 0) gather(c[j], g0[j], g1[j]);
+		}
+		V m[NB][4];
+#pragma unroll
+		for (int j = 0; j < NB; j++) {
+			m[j][0] = m[j][1] = m[j][2] = m[j][3] = V(0);
+			if (c[j] >= 0) ld_block(vals, k0 + j * LPR, m[j][0], m[j][1], m[j][2], m[j][3]);
+		}
+#pragma unroll
+		for (int j = 0; j < NB; j++) {
+			y0 += A(m[j][0]) * g0[j] + A(m[j][1]) * g1[j];
+			y1 += A(m[j][2]) * g0[j] + A(m[j][3]) * g1[j];
+		}
+	}
+#pragma unroll
+	for (int o = LPR / 2; o; o >>= 1) {
+		y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+		y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+	}
+}
+
+template <int LPR, int NB, typename A, typename V, typename G>
+__device__ __forceinline__ void row_product_nb(const int* __restrict__ cols, const V* __restrict__ vals, int ks, int ke,
+                                               int sub, G gather, A& y0, A& y1) {
+	if constexpr (NB == 1) row_product<LPR, A>(cols, vals, ks, ke, sub, gather, y0, y1);
+	else row_product_pf<LPR, NB, A>(cols, vals, ks, ke, sub, gather, y0, y1);
+}
+
 // row loop shared by the SpMV kernels: every warp runs the same number of trips
 #define FOR_ROWS(LPR)                                                                          \
 	int const sub_ = threadIdx.x % (LPR);                                                       \
@@ -329,7 +375,7 @@ __device__ __forceinline__ void df_add_prod(DF& s, float a, float b) {
 
 __device__ __forceinline__ double df_value(DF const& s) { return (double) s.hi + (double) s.lo; }
 
-template <int LPR>
+template <int LPR, int NB = 1>
 __global__ void __launch_bounds__(TPB_K) k_mx_spmv(CgArgs<float> a) {
 	CgState* st = a.st;
 	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -354,7 +400,7 @@ __global__ void __launch_bounds__(TPB_K) k_mx_spmv(CgArgs<float> a) {
 		bool const ok = row_ < a.N;
 		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
 		float y0, y1;
-		row_product<LPR, float>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		row_product_nb<LPR, NB, float>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
 		if (ok && sub_ == 0) {
 			float g0, g1;
 			gather(row_, g0, g1);
@@ -733,7 +779,7 @@ __device__ __forceinline__ void hs_beta(CgState* st, double gamma, double rho, i
 	}
 }
 
-template <int LPR>
+template <int LPR, int NB = 1>
 __global__ void __launch_bounds__(TPB_K) k_hs64_spmv(CgArgs<double> a) {
 	CgState* st = a.st;
 	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -754,7 +800,7 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_spmv(CgArgs<double> a) {
 		bool const ok = row_ < a.N;
 		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
 		double y0, y1;
-		row_product<LPR, double>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		row_product_nb<LPR, NB, double>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
 		if (ok && sub_ == 0) {
 			double g0, g1;
 			gather(row_, g0, g1);
@@ -826,7 +872,7 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
 }
 
 // ---- double-float HS kernels: x, r, z (in u), p, p' (in s), q (in w)
-template <int LPR>
+template <int LPR, int NB = 1>
 __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 	CgState* st = a.st;
 	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -843,18 +889,32 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 		bool const ok = row < a.N;
 		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
 		dfl y0 = {0.f, 0.f}, y1 = {0.f, 0.f};
-		for (int k = ks + sub; k < ke; k += LPR) {
-			int const c = a.cols[k];
-			dfl z0, z1, p0, p1;
-			df_ld(a.u, c, z0, z1);
-			df_ld(a.p, c, p0, p1);
-			dfl const g0 = df_fma(beta, p0, z0), g1 = df_fma(beta, p1, z1);
-			float4 const h = reinterpret_cast<const float4*>(a.hi)[k];
-			float4 const l = reinterpret_cast<const float4*>(a.lo)[k];
-			y0 = df_fma({h.x, l.x}, g0, y0);
-			y0 = df_fma({h.y, l.y}, g1, y0);
-			y1 = df_fma({h.z, l.z}, g0, y1);
-			y1 = df_fma({h.w, l.w}, g1, y1);
+		for (int k0 = ks + sub; k0 < ke; k0 += LPR * NB) {
+			// NB entries per trip: indices, then gathers and block loads, then arithmetic
+			int c[NB];
+#pragma unroll
+			for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? a.cols[k0 + j * LPR] : -1;
+			float4 zv[NB], pv[NB], h[NB], l[NB];
+#pragma unroll
+			for (int j = 0; j < NB; j++) {
+				zv[j] = pv[j] = h[j] = l[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+				if (c[j] >= 0) {
+					zv[j] = reinterpret_cast<const float4*>(a.u)[c[j]];
+					pv[j] = reinterpret_cast<const float4*>(a.p)[c[j]];
+					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
+					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
+				}
+			}
+#pragma unroll
+			for (int j = 0; j < NB; j++) {
+				if (c[j] < 0) continue;
+				dfl const g0 = df_fma(beta, {pv[j].x, pv[j].z}, {zv[j].x, zv[j].z});
+				dfl const g1 = df_fma(beta, {pv[j].y, pv[j].w}, {zv[j].y, zv[j].w});
+				y0 = df_fma({h[j].x, l[j].x}, g0, y0);
+				y0 = df_fma({h[j].y, l[j].y}, g1, y0);
+				y1 = df_fma({h[j].z, l[j].z}, g0, y1);
+				y1 = df_fma({h[j].w, l[j].w}, g1, y1);
+			}
 		}
 #pragma unroll
 		for (int o = LPR / 2; o; o >>= 1) {
@@ -959,22 +1019,29 @@ struct CgKernels {
 	void* hsdfrepl;
 };
 
-template <int LPR>
+template <int LPR, int NB = 1>
 CgKernels kernels_for() {
-	return {(void*) k_cg64_spmv<LPR>, (void*) k_mx_spmv<LPR>, (void*) k_mx_replace<LPR>,
-	        (void*) k_true_residual<LPR, double>, (void*) k_true_residual<LPR, float>, (void*) k_hs64_spmv<LPR>,
-	        (void*) k_hs64_replace<LPR>, (void*) k_hsdf_spmv<LPR>, (void*) k_hsdf_replace<LPR>};
+	return {(void*) k_cg64_spmv<LPR>, (void*) k_mx_spmv<LPR, NB>, (void*) k_mx_replace<LPR>,
+	        (void*) k_true_residual<LPR, double>, (void*) k_true_residual<LPR, float>, (void*) k_hs64_spmv<LPR, NB>,
+	        (void*) k_hs64_replace<LPR>, (void*) k_hsdf_spmv<LPR, NB>, (void*) k_hsdf_replace<LPR>};
 }
 
-CgKernels kernels_lpr(int lpr) {
-	switch (lpr) {
+// SpMV shape code: lanes per row + 100 x entries batched per lane (1: unbatched)
+constexpr int SHAPES[] = {1, 2, 4, 8, 16, 401, 801, 402, 204};
+constexpr int shape_lanes(int code) { return code % 100; }
+
+CgKernels kernels_lpr(int code) {
+	switch (code) {
 	case 1: return kernels_for<1>();
 	case 2: return kernels_for<2>();
 	case 4: return kernels_for<4>();
 	case 16: return kernels_for<16>();
+	case 401: return kernels_for<1, 4>();
+	case 801: return kernels_for<1, 8>();
+	case 402: return kernels_for<2, 4>();
+	case 204: return kernels_for<4, 2>();
 	default: return kernels_for<8>();
 	}
 }
-
 
 }  // namespace

@@ -1363,10 +1363,9 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 // Project autotuner: time the SpMV kernel with 1, 2, 4, 8 and 16 lanes per
 // block row on this problem's matrix and keep the fastest.
 int autotune_lpr(bfm_gpu_problem* P) {
-	int const cands[] = {1, 2, 4, 8, 16};
 	double best = 1e30;
 	int best_lpr = 8;
-	for (int lpr : cands) {
+	for (int lpr : SHAPES) {
 		double t_spmv = 0, t_upd = 0;
 		if (time_iteration(P, lpr, 5, &t_spmv, &t_upd)) return -1;
 		if (t_spmv < best) {
@@ -1958,7 +1957,27 @@ int bfm_gpu_problem_autotune(bfm_gpu_problem_t* P, int* lanes_per_row) {
 	if (!P->assembled) return fail("assemble first");
 	if (autotune_lpr(P)) return -1;
 	P->tuned = 1;
-	if (lanes_per_row) *lanes_per_row = P->lpr;
+	if (lanes_per_row) *lanes_per_row = shape_lanes(P->lpr);
+	return 0;
+}
+
+int bfm_gpu_problem_shape(bfm_gpu_problem_t* P, int* shape) {
+	g_err[0] = 0;
+	*shape = P->lpr;
+	return 0;
+}
+
+int bfm_gpu_problem_set_shape(bfm_gpu_problem_t* P, int shape) {
+	g_err[0] = 0;
+	if (shape == 0) {
+		P->tuned = 0;
+		return 0;
+	}
+	bool known = false;
+	for (int c : SHAPES) known |= c == shape;
+	if (!known) return fail("unknown SpMV shape %d", shape);
+	P->lpr = shape;
+	P->tuned = 1;
 	return 0;
 }
 

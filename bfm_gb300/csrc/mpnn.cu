@@ -14,10 +14,11 @@
 // accumulation).  Everything per node is deterministic: split-K partials are
 // reduced in block order.
 //
-// Training loss of one (residual r, error e) pair, z = B r:
-//     L = -log( (z.r)^2 / ((z.K z)(e.r)) ) >= 0,
-// the log of the fraction of e's energy norm that the optimal step along z
-// removes (0 when z is parallel to e).
+// Training loss of one (residual r = K e, error e) pair: the log of a
+// condition-number estimate of the preconditioned operator,
+//     L = log R(v) - log R(e),  R(x) = (x.K x) / (x.B^-1 x),
+// v a power-iteration vector of B K (top of the spectrum), e the solver's
+// error (bottom of the spectrum).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -292,6 +293,14 @@ __global__ void k_head(int N, const bf16* __restrict__ h3, const float* __restri
 }
 
 // ---------------------------------------------------------------- loss
+// Condition-number loss of the preconditioned operator B K.  With the
+// generalized Rayleigh quotient R(x) = (x.Kx) / (x.B^-1 x), which lies in
+// [lambda_min, lambda_max] of B K:
+//     L = log R(v) - log R(e),
+// v from power iterations on B K (approaching the top eigenvector; the
+// caller keeps it between steps), e a solver error (smooth: dominated by the
+// bottom of the spectrum).  Per node, with u = L_i^-1 x_i and
+// w = (I + C_i)^-1 u: x_i.B_i^-1 x_i = u.w, and d(u.w)/dC = -w w^T.
 
 struct LossArgs {
 	int N;
@@ -299,63 +308,92 @@ struct LossArgs {
 	const int* cols;
 	const double* vals64;
 	const double* blocks;
-	const double* r;
+	const double* lfac;
+	const float* o;
+	const double* r;   // K e
 	const double* e;
-	double* z;
-	double* az;
+	const double* v;   // power vector
 	double* partials;
 	unsigned* ticket;
-	double* sc;  // zr, zAz, er, loss
+	double* sc;  // v.Kv, sum v.B^-1 v, e.Ke, sum e.B^-1 e, loss
 };
 
-__global__ void k_loss_z(LossArgs a) {
-	int const i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= a.N) return;
-	double2 const r = ld2(a.r, i);
-	const double* B = a.blocks + 4l * i;
-	st2(a.z, i, B[0] * r.x + B[1] * r.y, B[2] * r.x + B[3] * r.y);
+// x_i.B_i^-1 x_i and w = (I + C_i)^-1 L_i^-1 x_i
+__device__ __forceinline__ double binv_quad(const double* lf, double c0, double c1, double c2, double x0, double x1,
+                                            double& w0, double& w1) {
+	double const l00 = lf[0], l10 = lf[1], l11 = lf[2];
+	if (!(l00 > 0.0 && l11 > 0.0)) {
+		w0 = w1 = 0.0;
+		return 0.0;
+	}
+	double const u0 = x0 / l00, u1 = (x1 - l10 * u0) / l11;
+	double const det = (1.0 + c0) * (1.0 + c2) - c1 * c1;
+	w0 = ((1.0 + c2) * u0 - c1 * u1) / det;
+	w1 = (-c1 * u0 + (1.0 + c0) * u1) / det;
+	return u0 * w0 + u1 * w1;
 }
 
-__global__ void k_loss_dots(LossArgs a) {
-	double v[3] = {0.0, 0.0, 0.0};
+__device__ __forceinline__ void node_c(const float* o, int i, double& c0, double& c1, double& c2) {
+	c0 = C_SCALE * tanh((double) o[3 * i]);
+	c1 = C_SCALE * tanh((double) o[3 * i + 1]);
+	c2 = C_SCALE * tanh((double) o[3 * i + 2]);
+}
+
+// one power step: out = B (K in)
+__global__ void k_power(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, const double* __restrict__ vals,
+                        const double* __restrict__ blocks, const double* __restrict__ vin, double* __restrict__ vout) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double y0 = 0.0, y1 = 0.0;
+	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+		double2 const x = ld2(vin, cols[k]);
+		const double* m = vals + 4l * k;
+		y0 += m[0] * x.x + m[1] * x.y;
+		y1 += m[2] * x.x + m[3] * x.y;
+	}
+	const double* B = blocks + 4l * i;
+	st2(vout, i, B[0] * y0 + B[1] * y1, B[2] * y0 + B[3] * y1);
+}
+
+__global__ void k_loss_terms(LossArgs a) {
+	double v[4] = {0.0, 0.0, 0.0, 0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		double y0 = 0.0, y1 = 0.0;
 		for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
-			double2 const zc = ld2(a.z, a.cols[k]);
+			double2 const x = ld2(a.v, a.cols[k]);
 			const double* m = a.vals64 + 4l * k;
-			y0 += m[0] * zc.x + m[1] * zc.y;
-			y1 += m[2] * zc.x + m[3] * zc.y;
+			y0 += m[0] * x.x + m[1] * x.y;
+			y1 += m[2] * x.x + m[3] * x.y;
 		}
-		st2(a.az, i, y0, y1);
-		double2 const z = ld2(a.z, i), r = ld2(a.r, i), e = ld2(a.e, i);
-		v[0] += z.x * r.x + z.y * r.y;
-		v[1] += z.x * y0 + z.y * y1;
-		v[2] += e.x * r.x + e.y * r.y;
+		double c0, c1, c2, w0, w1;
+		node_c(a.o, i, c0, c1, c2);
+		double2 const vv = ld2(a.v, i), ee = ld2(a.e, i), rr = ld2(a.r, i);
+		v[0] += vv.x * y0 + vv.y * y1;
+		v[1] += binv_quad(a.lfac + 3l * i, c0, c1, c2, vv.x, vv.y, w0, w1);
+		v[2] += ee.x * rr.x + ee.y * rr.y;
+		v[3] += binv_quad(a.lfac + 3l * i, c0, c1, c2, ee.x, ee.y, w0, w1);
 	}
-	double out[3];
-	if (grid_sum<3>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		a.sc[0] = out[0];
-		a.sc[1] = out[1];
-		a.sc[2] = out[2];
-		a.sc[3] = log(out[1]) + log(out[2]) - 2.0 * log(fabs(out[0]));
+	double out[4];
+	if (grid_sum<4>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		for (int k = 0; k < 4; k++) a.sc[k] = out[k];
+		a.sc[4] = log(out[0]) - log(out[1]) - log(out[2]) + log(out[3]);
 	}
 }
 
-// dL/dz = 2 Az / (z.Az) - 2 r / (z.r) -> dL/dc -> dL/do (N x 3, FP32)
-__global__ void k_loss_back(LossArgs a, const float* __restrict__ o, const double* __restrict__ lfac, float* __restrict__ d_o) {
+// dL/dc = (w_v w_v^T) / Q_v - (w_e w_e^T) / Q_e as (c0, c1, c2) -> dL/do (N x 3, FP32)
+__global__ void k_loss_back(LossArgs a, float* __restrict__ d_o) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= a.N) return;
-	double const zr = a.sc[0], zaz = a.sc[1];
-	double2 const az = ld2(a.az, i), r = ld2(a.r, i);
-	double const g0 = 2.0 * az.x / zaz - 2.0 * r.x / zr, g1 = 2.0 * az.y / zaz - 2.0 * r.y / zr;
-	double const t0 = tanh((double) o[3 * i]), t1 = tanh((double) o[3 * i + 1]), t2 = tanh((double) o[3 * i + 2]);
-	// z = L (I + C) y with y = L^T r: dL/dc from w = L^T dL/dz
-	double const l00 = lfac[3 * i], l10 = lfac[3 * i + 1], l11 = lfac[3 * i + 2];
-	double const y0 = l00 * r.x + l10 * r.y, y1 = l11 * r.y;
-	double const w0 = l00 * g0 + l10 * g1, w1 = l11 * g1;
-	double const dc0 = w0 * y0;
-	double const dc1 = w0 * y1 + w1 * y0;
-	double const dc2 = w1 * y1;
+	double const qv = a.sc[1], qe = a.sc[3];
+	double c0, c1, c2, a0, a1, b0, b1;
+	node_c(a.o, i, c0, c1, c2);
+	double2 const vv = ld2(a.v, i), ee = ld2(a.e, i);
+	binv_quad(a.lfac + 3l * i, c0, c1, c2, vv.x, vv.y, a0, a1);
+	binv_quad(a.lfac + 3l * i, c0, c1, c2, ee.x, ee.y, b0, b1);
+	double const dc0 = a0 * a0 / qv - b0 * b0 / qe;
+	double const dc1 = 2.0 * (a0 * a1 / qv - b0 * b1 / qe);
+	double const dc2 = a1 * a1 / qv - b1 * b1 / qe;
+	double const t0 = c0 / C_SCALE, t1 = c1 / C_SCALE, t2 = c2 / C_SCALE;
 	d_o[3 * i + 0] = (float) (dc0 * C_SCALE * (1.0 - t0 * t0));
 	d_o[3 * i + 1] = (float) (dc1 * C_SCALE * (1.0 - t1 * t1));
 	d_o[3 * i + 2] = (float) (dc2 * C_SCALE * (1.0 - t2 * t2));
@@ -623,11 +661,17 @@ int forward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, cudaStream_t st) {
 }
 
 // loss of the pair (r, e) and the gradient of every parameter into d.grad
-int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const double* e, cudaStream_t st) {
+int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const double* e, double* v, int power_iters,
+             cudaStream_t st) {
 	bfmi_buffers_t bf;
 	bfmi_buffers(P, &bf);
 	if (!bf.vals64_any) return mfail("training needs the FP64 operator: assemble in FP64, MIXED_EXACT or FP64_DF");
 	int const N = bf.N;
+	// the power vector: v <- B K v, power_iters times (ping-pong through z)
+	for (int k = 0; k < power_iters; k++) {
+		k_power<<<nb(N), 256, 0, st>>>(N, bf.row_ptr, bf.cols, bf.vals64_any, net->blocks, v, net->z);
+		MCK(cudaMemcpyAsync(v, net->z, 2l * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+	}
 	LossArgs la;
 	memset(&la, 0, sizeof la);
 	la.N = N;
@@ -635,16 +679,16 @@ int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const dou
 	la.cols = bf.cols;
 	la.vals64 = bf.vals64_any;
 	la.blocks = net->blocks;
+	la.lfac = net->lfac;
+	la.o = net->o;
 	la.r = r;
 	la.e = e;
-	la.z = net->z;
-	la.az = net->az;
+	la.v = v;
 	la.partials = net->partials;
 	la.ticket = net->ticket;
 	la.sc = net->sc;
-	k_loss_z<<<nb(N), 256, 0, st>>>(la);
-	k_loss_dots<<<FEAT_GRID, TPB_K, 0, st>>>(la);
-	k_loss_back<<<nb(N), 256, 0, st>>>(la, net->o, net->lfac, net->d_o);
+	k_loss_terms<<<FEAT_GRID, TPB_K, 0, st>>>(la);
+	k_loss_back<<<nb(N), 256, 0, st>>>(la, net->d_o);
 	int const heads = (N + HEAD_NODES - 1) / HEAD_NODES > 0 ? (N + HEAD_NODES - 1) / HEAD_NODES : 1;
 	k_head_back<<<heads, HEAD_TPB, 0, st>>>(N, net->d_o, net->h[3], net->d.theta, net->dh, net->d.gpart);
 	k_reduce_parts<<<nb(HEAD_OUT), 256, 0, st>>>(net->d.gpart, heads, HEAD_OUT, net->d.grad, O_WO, 3 * HID, O_BO);
@@ -669,10 +713,10 @@ int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const dou
 
 int read_loss(bfm_gpu_mpnn* net, double* loss, cudaStream_t st) {
 	if (!loss) return 0;
-	double sc[4];
+	double sc[5];
 	MCK(cudaMemcpyAsync(sc, net->sc, sizeof sc, cudaMemcpyDeviceToHost, st));
 	MCK(cudaStreamSynchronize(st));
-	*loss = sc[3];
+	*loss = sc[4];
 	return 0;
 }
 
@@ -710,7 +754,7 @@ int bfm_gpu_mpnn_create(bfm_gpu_mpnn_t** out, unsigned seed) {
 	bfm_gpu_mpnn* net = (bfm_gpu_mpnn*) calloc(1, sizeof *net);
 	if (!net) return mfail("out of host memory");
 	if (alloc(&net->d.theta, NPARAM) || alloc(&net->d.grad, NPARAM) || alloc(&net->d.adam_m, NPARAM) ||
-	    alloc(&net->d.adam_v, NPARAM) || alloc(&net->d.wb, NPARAM) || alloc(&net->sc, 4) ||
+	    alloc(&net->d.adam_v, NPARAM) || alloc(&net->d.wb, NPARAM) || alloc(&net->sc, 5) ||
 	    alloc(&net->partials, 4 * FEAT_GRID) || alloc(&net->rms, 1) || alloc(&net->ticket, 1)) {
 		bfm_gpu_mpnn_destroy(net);
 		return -1;
@@ -832,12 +876,12 @@ int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, float* featu
 	return 0;
 }
 
-int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double* loss,
-                          float* grad) {
+int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double* v,
+                          int power_iters, double* loss, float* grad) {
 	bfmi_buffers_t bf;
 	bfmi_buffers(P, &bf);
 	cudaStream_t const st = (cudaStream_t) bf.stream;
-	if (forward(net, P, st) || backward(net, P, r, e, st) || read_loss(net, loss, st)) return -1;
+	if (forward(net, P, st) || backward(net, P, r, e, v, power_iters, st) || read_loss(net, loss, st)) return -1;
 	if (grad) {
 		MCK(cudaStreamSynchronize(st));
 		MCK(cudaMemcpy(grad, net->d.grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
@@ -845,12 +889,12 @@ int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const doubl
 	return 0;
 }
 
-int bfm_gpu_mpnn_train_step(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double lr,
-                            double* loss) {
+int bfm_gpu_mpnn_train_step(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double* v,
+                            int power_iters, double lr, double* loss) {
 	bfmi_buffers_t bf;
 	bfmi_buffers(P, &bf);
 	cudaStream_t const st = (cudaStream_t) bf.stream;
-	if (forward(net, P, st) || backward(net, P, r, e, st)) return -1;
+	if (forward(net, P, st) || backward(net, P, r, e, v, power_iters, st)) return -1;
 	net->step += 1;
 	float const b1t = powf(0.9f, (float) net->step), b2t = powf(0.999f, (float) net->step);
 	k_adam<<<nb(NPARAM), 256, 0, st>>>(NPARAM, net->d.theta, net->d.grad, net->d.adam_m, net->d.adam_v, net->d.wb, (float) lr,

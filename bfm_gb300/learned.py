@@ -8,9 +8,10 @@ iterations gives x_k, a converged solve gives x*, and the pair is
 (r, e) = (K e, x* - x_k), formed on the device (bfm_gpu_problem_apply).
 Small batches of uneven plates (the batched workload's generator, solved as
 one block-diagonal system) and scaled-down perforated plates provide the
-meshes.  The loss of a pair is 1 - (z.r)^2 / ((z.Kz)(e.r)) with z = B r: the
-part of e's energy norm that one optimal step along the preconditioned
-residual leaves.
+meshes.  The loss is the log of a condition-number estimate of the
+preconditioned operator B K: log R(v) - log R(e) with the Rayleigh quotient
+R(x) = (x.Kx) / (x.B^-1 x), v a power-iteration vector of B K kept per mesh,
+e the solver's error (smooth, so R(e) approaches the bottom of the spectrum).
 
 Device memory for pairs is held in torch tensors (plumbing only): every
 computation is a library kernel.
@@ -168,17 +169,18 @@ class Network:
             last_error()
         return f, c, B
 
-    def gradient(self, prob: DeviceProblem, r_ptr: int, e_ptr: int):
+    def gradient(self, prob: DeviceProblem, r_ptr: int, e_ptr: int, v_ptr: int, power_iters: int = 0):
         loss = C.c_double()
         g = np.zeros(self.n_params, np.float32)
-        assert self.lib.bfm_gpu_mpnn_gradient(self.h, prob.P, C.c_void_p(r_ptr), C.c_void_p(e_ptr), C.byref(loss),
-                                              g.ctypes.data) == 0, last_error()
+        assert self.lib.bfm_gpu_mpnn_gradient(self.h, prob.P, C.c_void_p(r_ptr), C.c_void_p(e_ptr), C.c_void_p(v_ptr),
+                                              power_iters, C.byref(loss), g.ctypes.data) == 0, last_error()
         return loss.value, g
 
-    def train_step(self, prob: DeviceProblem, r_ptr: int, e_ptr: int, lr: float) -> float:
+    def train_step(self, prob: DeviceProblem, r_ptr: int, e_ptr: int, v_ptr: int, lr: float,
+                   power_iters: int = 4) -> float:
         loss = C.c_double()
-        assert self.lib.bfm_gpu_mpnn_train_step(self.h, prob.P, C.c_void_p(r_ptr), C.c_void_p(e_ptr), lr,
-                                                C.byref(loss)) == 0, last_error()
+        assert self.lib.bfm_gpu_mpnn_train_step(self.h, prob.P, C.c_void_p(r_ptr), C.c_void_p(e_ptr),
+                                                C.c_void_p(v_ptr), power_iters, lr, C.byref(loss)) == 0, last_error()
         return loss.value
 
     def use(self):
@@ -233,7 +235,7 @@ def concat(problems) -> M.Problem:
                      edge_loads=(np.concatenate([e for e, _ in loads]), np.concatenate([l for _, l in loads])))
 
 
-def pairs(prob: DeviceProblem, stops=(2, 4, 8, 16, 32, 64, 128, 256, 512, 1024), rtol: float = 1e-10):
+def pairs(prob: DeviceProblem, stops=(32, 64, 128, 256, 512, 1024, 2048), rtol: float = 1e-10):
     """(r, e) device pairs (torch float64 tensors) from partial Jacobi-PCG solves."""
     import torch
     n = 2 * prob.n_nodes
@@ -258,23 +260,34 @@ def pairs(prob: DeviceProblem, stops=(2, 4, 8, 16, 32, 64, 128, 256, 512, 1024),
     return out
 
 
-def train(net: Network, probs, n_pairs: int, lr: float = 3e-4, epochs: int = 1, seed: int = 0, log=None):
+def train(net: Network, probs, n_pairs: int, lr: float = 3e-4, epochs: int = 1, seed: int = 0, log=None,
+          power_iters: int = 4, warm_power: int = 60):
     """Adam over the pairs of `probs` (a list of DeviceProblem); returns the
-    mean loss of each epoch."""
+    mean loss of each epoch and the number of distinct pairs.  Each problem
+    keeps its power-iteration vector: `warm_power` steps before training,
+    `power_iters` more at every training step on it."""
+    import torch
     rng = np.random.default_rng(seed)
-    data = []
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    data, vecs = [], []
     for i, pr in enumerate(probs):
         for r, e in pairs(pr):
             data.append((i, r, e))
+        v = torch.rand(2 * pr.n_nodes, dtype=torch.float64, device="cuda", generator=gen) - 0.5
+        torch.cuda.synchronize()
+        vecs.append(v)
     if not data:
         raise RuntimeError("no training pairs")
+    for i, pr in enumerate(probs):
+        r, e = next((r, e) for j, r, e in data if j == i)
+        net.gradient(pr, r.data_ptr(), e.data_ptr(), vecs[i].data_ptr(), warm_power)
     hist = []
     steps = max(n_pairs, len(data)) * epochs
     order = rng.integers(0, len(data), steps)
     losses = []
     for t, j in enumerate(order):
         i, r, e = data[j]
-        losses.append(net.train_step(probs[i], r.data_ptr(), e.data_ptr(), lr))
+        losses.append(net.train_step(probs[i], r.data_ptr(), e.data_ptr(), vecs[i].data_ptr(), lr, power_iters))
         if log and (t + 1) % 500 == 0:
             log(f"step {t + 1}/{steps} loss {np.mean(losses[-500:]):.5f}")
     n_ep = max(1, epochs)

@@ -175,10 +175,16 @@ int bfm_gpu_problem_download(bfm_gpu_problem_t* problem, int32_t* row_ptr, int32
  * durations (ms, CUDA events).  Overwrites the Krylov vectors. */
 int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* problem, int reps, double* ms_spmv, double* ms_update);
 
-/* Project autotuner: time the SpMV with 1, 2, 4, 8 and 16 lanes per block row
- * on the assembled matrix and keep the fastest for this problem's solves.
+/* Project autotuner: time the SpMV shapes -- 1, 2, 4, 8 or 16 lanes per block
+ * row, and 1, 2, 4 or 8 entries batched per lane (column indices, then
+ * gathers and block loads, then arithmetic) -- on the assembled matrix and
+ * keep the fastest for this problem's solves.  Returns the lanes per row of
+ * the winner (and its shape code, lanes + 100 x batch, if shape != NULL).
  * Overwrites the Krylov vectors. */
 int bfm_gpu_problem_autotune(bfm_gpu_problem_t* problem, int* lanes_per_row);
+int bfm_gpu_problem_shape(bfm_gpu_problem_t* problem, int* shape);
+/* Force an SpMV shape code (as returned above; 0 restores autotuning). */
+int bfm_gpu_problem_set_shape(bfm_gpu_problem_t* problem, int shape);
 
 /* The CUDA stream the problem's work is enqueued on (cudaStream_t as void*). */
 void* bfm_gpu_problem_stream(bfm_gpu_problem_t* problem);
@@ -257,15 +263,20 @@ int bfm_gpu_mpnn_load(bfm_gpu_mpnn_t* net, const char* path);
  * features[16*n_nodes] as fed to the first layer (BF16 values), c[3*n_nodes]
  * = (c0, c1, c2) per node, blocks[4*n_nodes] = B_i row-major. */
 int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, float* features, float* c, double* blocks);
-/* Loss of one (residual r, error e) pair, r = K e, z = B r:
- *     L = -log( (z.r)^2 / ((z.K z)(e.r)) )  (>= 0; 0 when z is parallel to e),
- * and its gradient (FP32, parameter order above; NULL to skip).  r and e are
- * device arrays of 2*n_nodes doubles; needs the FP64 operator. */
+/* Training loss of one (residual r = K e, error e) pair: the log of a
+ * condition-number estimate of the preconditioned operator B K,
+ *     L = log R(v) - log R(e),  R(x) = (x.K x) / (x.B^-1 x),
+ * with v the power-iteration vector of B K (top of its spectrum) and e a
+ * solver error (smooth: the bottom).  v (device, 2*n_nodes doubles, kept by
+ * the caller between calls) first takes power_iters steps v <- B K v with the
+ * current network.  Returns the loss and its gradient (FP32, parameter order
+ * above; NULL to skip).  r and e are device arrays of 2*n_nodes doubles;
+ * needs the FP64 operator. */
 int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, const double* r, const double* e,
-                          double* loss, float* grad);
-/* One Adam step (beta 0.9 / 0.999) on the pair's gradient; loss may be NULL. */
+                          double* v, int power_iters, double* loss, float* grad);
+/* One Adam step (beta 0.9 / 0.999) on that gradient; loss may be NULL. */
 int bfm_gpu_mpnn_train_step(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* problem, const double* r, const double* e,
-                            double lr, double* loss);
+                            double* v, int power_iters, double lr, double* loss);
 /* Network used by BFM_GPU_PC_LEARNED solves (NULL: none). */
 int bfm_gpu_mpnn_use(bfm_gpu_mpnn_t* net);
 

@@ -14,10 +14,9 @@ Network (parameters in this order, FP32 masters, BF16 copies on the GPU):
     c = 0.45 tanh(o)
     B_i = K_ii^-1 + L_i C_i L_i^T,  L_i L_i^T = K_ii^-1 (Cholesky),  C_i = [[c0, c1], [c1, c2]]
           (K_ii: the node's 2x2 diagonal block; c = 0 is block Jacobi)
-Loss of one (residual r, error e) pair, z = B r:
-    L = -log( (z.r)^2 / ((z.K z)(e.r)) )
-minus the log of the fraction of e's energy norm that the optimal step along
-z removes.
+Loss of one (residual r = K e, error e) pair with a power vector v of B K:
+    L = log R(v) - log R(e),  R(x) = (x.K x) / (x.B^-1 x)
+the log of a condition-number estimate of the preconditioned operator.
 """
 from __future__ import annotations
 
@@ -104,26 +103,30 @@ def blocks(c, Kd):
     return np.linalg.inv(Kd) + L @ C @ np.transpose(L, (0, 2, 1))
 
 
-def loss_and_grad(theta, f, rp, cols, K, Kd, r, e, emulate=False):
-    """loss and d loss / d theta (float64); emulate as in forward (the
-    back-propagated signal entering each dense layer's GEMMs is BF16 too)"""
+def binv_quad(L, c, x2):
+    """Per node u = L^-1 x, w = (I + C)^-1 u; returns (sum of u.w, w)."""
+    u0 = x2[:, 0] / L[:, 0, 0]
+    u1 = (x2[:, 1] - L[:, 1, 0] * u0) / L[:, 1, 1]
+    det = (1 + c[:, 0]) * (1 + c[:, 2]) - c[:, 1] ** 2
+    w0 = ((1 + c[:, 2]) * u0 - c[:, 1] * u1) / det
+    w1 = (-c[:, 1] * u0 + (1 + c[:, 0]) * u1) / det
+    return float(u0 @ w0 + u1 @ w1), np.stack([w0, w1], 1)
+
+
+def loss_and_grad(theta, f, rp, cols, K, Kd, r, e, v, emulate=False):
+    """Loss log R(v) - log R(e), R(x) = (x.Kx) / (x.B^-1 x), and d loss /
+    d theta (float64); r = K e; emulate as in forward (the back-propagated
+    signal entering each dense layer's GEMMs is BF16 too)."""
     q = bf16 if emulate else _id
     c, cache = forward(theta, f, rp, cols, emulate)
     n = len(c)
-    B = blocks(c, Kd)
-    r2 = r.reshape(n, 2)
-    z = np.einsum("nij,nj->ni", B, r2).reshape(-1)
-    Az = K @ z
-    zr, zAz, er = z @ r, z @ Az, e @ r
-    loss = np.log(zAz) + np.log(er) - 2.0 * np.log(abs(zr))
-    gz = 2.0 * Az / zAz - 2.0 * r / zr
-    g2 = gz.reshape(n, 2)
-    # z = L (I + C) y, y = L^T r: d loss / dc from w = L^T d loss / dz
     L = chol_inv(Kd)
-    Lt = np.transpose(L, (0, 2, 1))
-    y = np.einsum("nij,nj->ni", Lt, r2)
-    w = np.einsum("nij,nj->ni", Lt, g2)
-    dc = np.stack([w[:, 0] * y[:, 0], w[:, 0] * y[:, 1] + w[:, 1] * y[:, 0], w[:, 1] * y[:, 1]], 1)
+    Qv, wv = binv_quad(L, c, v.reshape(n, 2))
+    Qe, we = binv_quad(L, c, e.reshape(n, 2))
+    loss = np.log(v @ (K @ v)) - np.log(Qv) - np.log(e @ r) + np.log(Qe)
+    dc = np.stack([wv[:, 0] ** 2 / Qv - we[:, 0] ** 2 / Qe,
+                   2 * (wv[:, 0] * wv[:, 1] / Qv - we[:, 0] * we[:, 1] / Qe),
+                   wv[:, 1] ** 2 / Qv - we[:, 1] ** 2 / Qe], 1)
     do = dc * C_SCALE * (1.0 - np.tanh(cache["o"]) ** 2)
     W0, b0, W1, b1, W2, b2, W3, b3, Wo, bo = unpack(theta)
     grads = [None] * 10

@@ -103,27 +103,33 @@ def test_forward_matches_oracle(setup):
 
 @pytest.fixture(scope="module")
 def pair(setup):
+    """(r, e, v): a solver pair and a power vector of B K (60 steps, untrained network)."""
     p, prob, net, _ = setup
-    prs = LN.pairs(prob, stops=(32,))
+    prs = LN.pairs(prob, stops=(256,))
     assert prs
-    return prs[0]
+    r, e = prs[0]
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    v = torch.rand(2 * p.n_nodes, dtype=torch.float64, device="cuda", generator=gen) - 0.5
+    torch.cuda.synchronize()
+    net.gradient(prob, r.data_ptr(), e.data_ptr(), v.data_ptr(), 60)
+    return r, e, v
 
 
 def test_gradient_matches_oracle(setup, pair):
     p, prob, net, (rp, cols, vals, b) = setup
-    r, e = pair
+    r, e, v = pair
     th = random_theta(net, 2)
     init = net.weights()
     net.set_weights(th)
     try:
         f_gpu, _, _ = net.forward(prob)
-        loss_gpu, g_gpu = net.gradient(prob, r.data_ptr(), e.data_ptr())
+        loss_gpu, g_gpu = net.gradient(prob, r.data_ptr(), e.data_ptr(), v.data_ptr(), 0)
         K = scalar_K(rp, cols, vals, p.n_nodes)
         args = (th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, K, diag_blocks(rp, cols, vals, p.n_nodes),
-                r.cpu().numpy(), e.cpu().numpy())
+                r.cpu().numpy(), e.cpu().numpy(), v.cpu().numpy())
         loss_ref, g_ref, _ = R.loss_and_grad(*args, emulate=True)
-        assert loss_gpu >= 0.0
-        assert abs(loss_gpu - loss_ref) <= 1e-6 * max(1.0, abs(loss_ref))
+        assert loss_gpu > 0.0          # log of a condition-number estimate
+        assert abs(loss_gpu - loss_ref) <= 1e-4 * max(1.0, abs(loss_ref))
         # every parameter block, relative to its own norm: BF16 storage emulated, FP32 sums
         k = 0
         for shape in R.SHAPES:
@@ -141,13 +147,13 @@ def test_gradient_matches_oracle(setup, pair):
 
 def test_training_lowers_the_loss(setup, pair):
     p, prob, _, _ = setup
-    r, e = pair
+    r, e, v = pair
     net = LN.Network(seed=4)
     try:
-        losses = [net.train_step(prob, r.data_ptr(), e.data_ptr(), 1e-3) for _ in range(60)]
+        # fixed power vector: the condition-number estimate falls by at least 5%
+        losses = [net.train_step(prob, r.data_ptr(), e.data_ptr(), v.data_ptr(), 1e-3, 0) for _ in range(60)]
         assert np.isfinite(losses).all()
-        # the energy removed by one preconditioned step grows by at least 10%
-        assert np.mean(losses[-10:]) < np.mean(losses[:10]) - np.log(1.1)
+        assert np.mean(losses[-10:]) < np.mean(losses[:10]) - np.log(1.05)
     finally:
         net.close()
 

@@ -30,20 +30,39 @@ def test_gradient_matches_finite_differences():
     rng = np.random.default_rng(1)
     f = rng.normal(size=(n, R.F_IN))
     K = spd(n, 2)
-    d2 = np.stack([K[2 * i:2 * i + 2, 2 * i:2 * i + 2] for i in range(n)])
+    Kd = np.stack([K[2 * i:2 * i + 2, 2 * i:2 * i + 2] for i in range(n)])
     e = rng.normal(size=2 * n)
+    v = rng.normal(size=2 * n)
     r = K @ e
     th = rng.normal(0, 0.3, R.N_PARAMS)
-    loss, g, _ = R.loss_and_grad(th, f, rp, cols, K, d2, r, e)
-    assert loss >= 0.0
+    args = (f, rp, cols, K, Kd, r, e, v)
+    loss, g, _ = R.loss_and_grad(th, *args)
+    assert np.isfinite(loss)
     idx = rng.choice(R.N_PARAMS, 60, replace=False)
     h = 1e-6
     for k in idx:
         tp, tm = th.copy(), th.copy()
         tp[k] += h
         tm[k] -= h
-        fd = (R.loss_and_grad(tp, f, rp, cols, K, d2, r, e)[0] - R.loss_and_grad(tm, f, rp, cols, K, d2, r, e)[0]) / (2 * h)
+        fd = (R.loss_and_grad(tp, *args)[0] - R.loss_and_grad(tm, *args)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(g).max()), (k, fd, g[k])
+
+
+def test_loss_is_log_rayleigh_ratio():
+    """With c = 0 (block Jacobi) the loss is log R(v) - log R(e) computed directly."""
+    n = 10
+    rp, cols = tiny_graph(n)
+    rng = np.random.default_rng(4)
+    K = spd(n, 5)
+    Kd = np.stack([K[2 * i:2 * i + 2, 2 * i:2 * i + 2] for i in range(n)])
+    th = np.zeros(R.N_PARAMS)
+    e, v = rng.normal(size=2 * n), rng.normal(size=2 * n)
+    loss, _, c = R.loss_and_grad(th, rng.normal(size=(n, R.F_IN)), rp, cols, K, Kd, K @ e, e, v)
+    Binv = np.zeros((2 * n, 2 * n))
+    for i in range(n):
+        Binv[2 * i:2 * i + 2, 2 * i:2 * i + 2] = Kd[i]
+    Rq = lambda x: (x @ K @ x) / (x @ Binv @ x)
+    assert abs(loss - (np.log(Rq(v)) - np.log(Rq(e)))) < 1e-12
 
 
 def test_bf16_rounding():
