@@ -1006,8 +1006,122 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_replace(DfArgs a) {
 	}
 }
 
+// ---- split form of K1: a direction kernel forms p' = z + beta p for every
+// node (and clears the graph's conditions), then the SpMV gathers p' alone:
+// one gathered vector instead of two and no direction arithmetic per
+// neighbour (FP64: 4 DFMA per block instead of 6).
+__global__ void __launch_bounds__(TPB_K) k_hs64_dir(CgArgs<double> a) {
+	CgState* st = a.st;
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+		cudaGraphSetConditional(a.cond, 0u);
+		cudaGraphSetConditional(a.cond_repl, 0u);
+	}
+	if (st->done && !a.timing) return;
+	double const beta = st->beta;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		double2 const z = ld2(a.u, i), p = ld2(a.p, i);
+		st2(a.pn, i, z.x + beta * p.x, z.y + beta * p.y);
+	}
+}
+
+template <int LPR, int NB = 1>
+__global__ void __launch_bounds__(TPB_K) k_hs64_spmv_s(CgArgs<double> a) {
+	CgState* st = a.st;
+	if (st->done && !a.timing) return;
+	const double* __restrict__ pn = a.pn;
+	auto gather = [=](int c, double& g0, double& g1) {
+		double2 const t = ld2(pn, c);
+		g0 = t.x;
+		g1 = t.y;
+	};
+	double v[1] = {0.0};
+	FOR_ROWS(LPR) {
+		bool const ok = row_ < a.N;
+		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		double y0, y1;
+		row_product_nb<LPR, NB, double>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		if (ok && sub_ == 0) {
+			double2 const g = ld2(pn, row_);
+			st2(a.w, row_, y0, y1);
+			v[0] += g.x * y0 + g.y * y1;
+		}
+	}
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
+}
+
+__global__ void __launch_bounds__(TPB_K) k_hsdf_dir(DfArgs a) {
+	CgState* st = a.st;
+	if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+		cudaGraphSetConditional(a.cond, 0u);
+		cudaGraphSetConditional(a.cond_repl, 0u);
+	}
+	if (st->done && !a.timing) return;
+	dfl const beta = df_make(st->beta);
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+		dfl z0, z1, p0, p1;
+		df_ld(a.u, i, z0, z1);
+		df_ld(a.p, i, p0, p1);
+		df_st(a.s, i, df_fma(beta, p0, z0), df_fma(beta, p1, z1));
+	}
+}
+
+template <int LPR, int NB = 1>
+__global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
+	CgState* st = a.st;
+	if (st->done && !a.timing) return;
+	double v[1] = {0.0};
+	int const sub = threadIdx.x % LPR;
+	int const rpb = blockDim.x / LPR;
+	for (int base = blockIdx.x * rpb; base < a.N; base += gridDim.x * rpb) {
+		int const row = base + threadIdx.x / LPR;
+		bool const ok = row < a.N;
+		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+		dfl y0 = {0.f, 0.f}, y1 = {0.f, 0.f};
+		for (int k0 = ks + sub; k0 < ke; k0 += LPR * NB) {
+			int c[NB];
+#pragma unroll
+			for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? a.cols[k0 + j * LPR] : -1;
+			float4 gv[NB], h[NB], l[NB];
+#pragma unroll
+			for (int j = 0; j < NB; j++) {
+				gv[j] = h[j] = l[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+				if (c[j] >= 0) {
+					gv[j] = reinterpret_cast<const float4*>(a.s)[c[j]];
+					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
+					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
+				}
+			}
+#pragma unroll
+			for (int j = 0; j < NB; j++) {
+				if (c[j] < 0) continue;
+				dfl const g0 = {gv[j].x, gv[j].z}, g1 = {gv[j].y, gv[j].w};
+				y0 = df_fma({h[j].x, l[j].x}, g0, y0);
+				y0 = df_fma({h[j].y, l[j].y}, g1, y0);
+				y1 = df_fma({h[j].z, l[j].z}, g0, y1);
+				y1 = df_fma({h[j].w, l[j].w}, g1, y1);
+			}
+		}
+#pragma unroll
+		for (int o = LPR / 2; o; o >>= 1) {
+			y0 = df_add(y0, {__shfl_xor_sync(0xffffffffu, y0.hi, o), __shfl_xor_sync(0xffffffffu, y0.lo, o)});
+			y1 = df_add(y1, {__shfl_xor_sync(0xffffffffu, y1.hi, o), __shfl_xor_sync(0xffffffffu, y1.lo, o)});
+		}
+		if (ok && sub == 0) {
+			dfl g0, g1;
+			df_ld(a.s, row, g0, g1);
+			df_st(a.w, row, y0, y1);
+			v[0] += df_dbl(df_add(df_mul(g0, y0), df_mul(g1, y1)));
+		}
+	}
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
+}
+
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner
 struct CgKernels {
+	void* hs64s;   // split-form K1 (with k_hs64_dir before it)
+	void* hsdfs;   // split-form K1 (with k_hsdf_dir before it)
 	void* spmv64;
 	void* spmvmx;
 	void* replace;
@@ -1021,17 +1135,21 @@ struct CgKernels {
 
 template <int LPR, int NB = 1>
 CgKernels kernels_for() {
-	return {(void*) k_cg64_spmv<LPR>, (void*) k_mx_spmv<LPR, NB>, (void*) k_mx_replace<LPR>,
+	return {(void*) k_hs64_spmv_s<LPR, NB>, (void*) k_hsdf_spmv_s<LPR, NB>,
+	        (void*) k_cg64_spmv<LPR>, (void*) k_mx_spmv<LPR, NB>, (void*) k_mx_replace<LPR>,
 	        (void*) k_true_residual<LPR, double>, (void*) k_true_residual<LPR, float>, (void*) k_hs64_spmv<LPR, NB>,
 	        (void*) k_hs64_replace<LPR>, (void*) k_hsdf_spmv<LPR, NB>, (void*) k_hsdf_replace<LPR>};
 }
 
-// SpMV shape code: lanes per row + 100 x entries batched per lane (1: unbatched)
-constexpr int SHAPES[] = {1, 2, 4, 8, 16, 401, 801, 402, 204};
+// SpMV shape code: lanes per row + 100 x entries batched per lane (1:
+// unbatched), + 1000 for the split form (direction kernel + p'-only SpMV;
+// FP64 and double-float paths)
+constexpr int SHAPES[] = {1, 2, 4, 8, 16, 401, 801, 402, 204, 1001, 1002, 1004, 1401, 1402, 1801};
 constexpr int shape_lanes(int code) { return code % 100; }
+constexpr bool shape_split(int code) { return code >= 1000; }
 
 CgKernels kernels_lpr(int code) {
-	switch (code) {
+	switch (code % 1000) {
 	case 1: return kernels_for<1>();
 	case 2: return kernels_for<2>();
 	case 4: return kernels_for<4>();

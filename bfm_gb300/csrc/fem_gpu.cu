@@ -318,6 +318,37 @@ __device__ __forceinline__ void store_precond(const AsmArgs& a, int r, double k0
 	}
 }
 
+__device__ __forceinline__ void material_abc32(float E, float nu, int stress, float& a, float& b, float& c) {
+	if (!stress) {
+		float const den = (1.f + nu) * (1.f - 2.f * nu);
+		a = E * (1.f - nu) / den;
+		b = E * nu / den;
+	}
+	else {
+		float const den = 1.f - nu * nu;
+		a = E / den;
+		b = E * nu / den;
+	}
+	c = E / (2.f * (1.f + nu));
+}
+
+// s + x as an unevaluated float pair (TwoSum, no ordering assumption)
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+	float const t = __fadd_rn(hi, x);
+	float const z = __fsub_rn(t, hi);
+	float const err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(x, z));
+	hi = t;
+	lo = __fadd_rn(lo, err);
+}
+
+__global__ void k_split_coords(int N, const double* __restrict__ coords, float4* __restrict__ out) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double2 const c = reinterpret_cast<const double2*>(coords)[i];
+	float const xh = (float) c.x, yh = (float) c.y;
+	out[i] = make_float4(xh, yh, (float) (c.x - (double) xh), (float) (c.y - (double) yh));
+}
+
 // One thread per node row (owner computes, no atomics): walk the node's
 // incident elements in ascending order, evaluate each element at every
 // integration point exactly as system.c:136-224 does and accumulate the terms
@@ -420,12 +451,18 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			// FP32 integration on coordinates relative to the element's first
 			// node (taken in FP64), which keeps the Jacobian accurate for
 			// small elements far from the origin.
+			// (the same offsets and FP32 materials as k_assemble32, so rows
+			// shared with it stay exactly symmetric)
 			float lx[4], ly[4];
+			float4 const c0 = a.coords32[map[0]];
 			for (int j = 0; j < kind; j++) {
-				lx[j] = (float) (x[j] - x[0]);
-				ly[j] = (float) (y[j] - y[0]);
+				float4 const cj = a.coords32[map[j]];
+				lx[j] = __fadd_rn(__fsub_rn(cj.x, c0.x), __fsub_rn(cj.z, c0.z));
+				ly[j] = __fadd_rn(__fsub_rn(cj.y, c0.y), __fsub_rn(cj.w, c0.w));
 			}
-			float const fa = (float) ea, fb = (float) eb, fc = (float) ec;
+			float fa, fb, fc;
+			material_abc32(a.elemE ? (float) a.elemE[e] : (float) a.E, a.elemNu ? (float) a.elemNu[e] : (float) a.nu,
+			               a.stress, fa, fb, fc);
 			for (int q = 0; q < a.rule.nq; q++) {
 				float const w = (float) a.rule.w[q];
 				float dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
@@ -458,10 +495,11 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				float const xj = dx[jr], yj = dy[jr];
 				for (int k = 0; k < kind; k++) {
 					int const s = slot[k];
-					acc[s][0] += dw * (fa * xj * dx[k] + fc * yj * dy[k]);
-					acc[s][1] += dw * (fb * xj * dy[k] + fc * yj * dx[k]);
-					acc[s][2] += dw * (fb * yj * dx[k] + fc * xj * dy[k]);
-					acc[s][3] += dw * (fa * yj * dy[k] + fc * xj * dx[k]);
+					float const pxx = xj * dx[k], pyy = yj * dy[k], pxy = xj * dy[k], pyx = yj * dx[k];
+					acc[s][0] += dw * (fa * pxx + fc * pyy);
+					acc[s][1] += dw * (fb * pxy + fc * pyx);
+					acc[s][2] += dw * (fb * pyx + fc * pxy);
+					acc[s][3] += dw * (fa * pyy + fc * pxx);
 				}
 			}
 		}
@@ -517,8 +555,10 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			a.vals64[o + 2] = v[2]; a.vals64[o + 3] = v[3];
 		}
 		if (a.vals32) {
+			// FP32 path: one value for both off-diagonal entries of the diagonal block (symmetric)
+			float const sym = (float) (0.5 * (v[1] + v[2]));
 			for (int k = 0; k < 4; k++) {
-				float const f = (float) v[k];
+				float const f = (!EXACT && s == sd && (k == 1 || k == 2)) ? sym : (float) v[k];
 				a.vals32[o + k] = f;
 				corr[k] += v[k] - (double) f;
 				if (a.vals32lo) a.vals32lo[o + k] = (float) (v[k] - (double) f);
@@ -558,37 +598,6 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 //  - the block's output rows staged in shared memory and written with
 //    coalesced 16-byte stores.
 // Rows longer than RMAX are left to k_assemble<false>.
-__device__ __forceinline__ void material_abc32(float E, float nu, int stress, float& a, float& b, float& c) {
-	if (!stress) {
-		float const den = (1.f + nu) * (1.f - 2.f * nu);
-		a = E * (1.f - nu) / den;
-		b = E * nu / den;
-	}
-	else {
-		float const den = 1.f - nu * nu;
-		a = E / den;
-		b = E * nu / den;
-	}
-	c = E / (2.f * (1.f + nu));
-}
-
-// s + x as an unevaluated float pair (TwoSum, no ordering assumption)
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
-	float const t = __fadd_rn(hi, x);
-	float const z = __fsub_rn(t, hi);
-	float const err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(x, z));
-	hi = t;
-	lo = __fadd_rn(lo, err);
-}
-
-__global__ void k_split_coords(int N, const double* __restrict__ coords, float4* __restrict__ out) {
-	int const i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= N) return;
-	double2 const c = reinterpret_cast<const double2*>(coords)[i];
-	float const xh = (float) c.x, yh = (float) c.y;
-	out[i] = make_float4(xh, yh, (float) (c.x - (double) xh), (float) (c.y - (double) yh));
-}
-
 template <int RMAX>
 __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 	__shared__ float4 stage[128 * RMAX];
@@ -703,12 +712,16 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 					xj = dx[j];
 					yj = dy[j];
 				}
+			// gradient products first: the owner of the transposed block forms
+			// the same products (multiplication commutes exactly), so the FP32
+			// operator is exactly symmetric
 #pragma unroll
 			for (int k = 0; k < 4; k++) {
-				ek[k][0] += dw * (fa * xj * dx[k] + fc * yj * dy[k]);
-				ek[k][1] += dw * (fb * xj * dy[k] + fc * yj * dx[k]);
-				ek[k][2] += dw * (fb * yj * dx[k] + fc * xj * dy[k]);
-				ek[k][3] += dw * (fa * yj * dy[k] + fc * xj * dx[k]);
+				float const pxx = xj * dx[k], pyy = yj * dy[k], pxy = xj * dy[k], pyx = yj * dx[k];
+				ek[k][0] += dw * (fa * pxx + fc * pyy);
+				ek[k][1] += dw * (fb * pxy + fc * pyx);
+				ek[k][2] += dw * (fb * pyx + fc * pxy);
+				ek[k][3] += dw * (fa * pyy + fc * pxx);
 			}
 		}
 #pragma unroll
@@ -740,6 +753,14 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		float const h = __fadd_rn(dh[k], dl[k]);
 		dl[k] = __fsub_rn(dl[k], __fsub_rn(h, dh[k]));
 		dh[k] = h;
+	}
+	{
+		// one FP32 value for both off-diagonal entries of the diagonal block
+		// (symmetric operator); each entry's remainder goes to the correction
+		float const m = __fmul_rn(0.5f, __fadd_rn(dh[1], dh[2]));
+		dl[1] = __fadd_rn(__fsub_rn(dh[1], m), dl[1]);
+		dl[2] = __fadd_rn(__fsub_rn(dh[2], m), dl[2]);
+		dh[1] = dh[2] = m;
 	}
 	bool const fix = has_diag && is < ie;
 	int const r0 = 2 * r, r1 = 2 * r + 1;
@@ -1224,7 +1245,12 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			void* pa[1] = {&a[half]};
 			cudaGraphNode_t n1, n2, nif, nr;
 			cudaGraph_t ifbody;
-			if (add_node(body, &n1, prev ? &prev : nullptr, K.hsdf, P->grid, pa)) return -1;
+			if (shape_split(P->lpr)) {
+				cudaGraphNode_t n0;
+				if (add_node(body, &n0, prev ? &prev : nullptr, (void*) k_hsdf_dir, P->grid, pa)) return -1;
+				if (add_node(body, &n1, &n0, K.hsdfs, P->grid, pa)) return -1;
+			}
+			else if (add_node(body, &n1, prev ? &prev : nullptr, K.hsdf, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_hsdf_update, P->grid, pa)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			if (add_node(ifbody, &nr, nullptr, K.hsdfrepl, P->grid, pa)) return -1;
@@ -1250,7 +1276,12 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			void* pa[1] = {&a[half]};
 			cudaGraphNode_t n1, n2, nif, nr;
 			cudaGraph_t ifbody;
-			if (add_node(body, &n1, prev ? &prev : nullptr, K.hs64, P->grid, pa)) return -1;
+			if (shape_split(P->lpr)) {
+				cudaGraphNode_t n0;
+				if (add_node(body, &n0, prev ? &prev : nullptr, (void*) k_hs64_dir, P->grid, pa)) return -1;
+				if (add_node(body, &n1, &n0, K.hs64s, P->grid, pa)) return -1;
+			}
+			else if (add_node(body, &n1, prev ? &prev : nullptr, K.hs64, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			if (add_node(ifbody, &nr, nullptr, K.hs64repl, P->grid, pa)) return -1;
@@ -1295,9 +1326,9 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	return 0;
 }
 
-// Mean duration (ms) of the two per-iteration kernels with `lpr` lanes per
-// row, launched standalone on a scratch solver state.  Overwrites the Krylov
-// vectors.
+// Mean duration (ms) of the two per-iteration steps with SpMV shape `lpr`
+// (the SpMV step includes the direction kernel of the split form), launched
+// standalone on a scratch solver state.  Overwrites the Krylov vectors.
 int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, double* ms_update) {
 	CgState* scratch = nullptr;
 	if (dalloc(&scratch, 1)) return -1;
@@ -1315,7 +1346,13 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 		k_df_init<<<grid, TPB, 0, st>>>(a);
 		void* pa[1] = {&a};
 		cudaEventRecord(e[0], st);
-		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.hsdf, dim3(grid), dim3(TPB), pa, 0, st);
+		for (int i = 0; i < reps; i++) {
+			if (shape_split(lpr)) {
+				k_hsdf_dir<<<grid, TPB, 0, st>>>(a);
+				cudaLaunchKernel(K.hsdfs, dim3(grid), dim3(TPB), pa, 0, st);
+			}
+			else cudaLaunchKernel(K.hsdf, dim3(grid), dim3(TPB), pa, 0, st);
+		}
 		cudaEventRecord(e[1], st);
 		for (int i = 0; i < reps; i++) k_hsdf_update<<<grid, TPB, 0, st>>>(a);
 		cudaEventRecord(e[2], st);
@@ -1329,7 +1366,13 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 		k_cg_init<double><<<grid, TPB, 0, st>>>(a, 0);
 		void* pa[1] = {&a};
 		cudaEventRecord(e[0], st);
-		for (int i = 0; i < reps; i++) cudaLaunchKernel(K.hs64, dim3(grid), dim3(TPB), pa, 0, st);
+		for (int i = 0; i < reps; i++) {
+			if (shape_split(lpr)) {
+				k_hs64_dir<<<grid, TPB, 0, st>>>(a);
+				cudaLaunchKernel(K.hs64s, dim3(grid), dim3(TPB), pa, 0, st);
+			}
+			else cudaLaunchKernel(K.hs64, dim3(grid), dim3(TPB), pa, 0, st);
+		}
 		cudaEventRecord(e[1], st);
 		for (int i = 0; i < reps; i++) k_hs64_update<<<grid, TPB, 0, st>>>(a);
 		cudaEventRecord(e[2], st);
@@ -1365,7 +1408,9 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 int autotune_lpr(bfm_gpu_problem* P) {
 	double best = 1e30;
 	int best_lpr = 8;
+	bool const mixed = P->precision == BFM_GPU_MIXED || P->precision == BFM_GPU_MIXED_EXACT;
 	for (int lpr : SHAPES) {
+		if (mixed && shape_split(lpr)) continue;  // the mixed path has no split form
 		double t_spmv = 0, t_upd = 0;
 		if (time_iteration(P, lpr, 5, &t_spmv, &t_upd)) return -1;
 		if (t_spmv < best) {
@@ -1976,6 +2021,8 @@ int bfm_gpu_problem_set_shape(bfm_gpu_problem_t* P, int shape) {
 	bool known = false;
 	for (int c : SHAPES) known |= c == shape;
 	if (!known) return fail("unknown SpMV shape %d", shape);
+	if (shape_split(shape) && (P->precision == BFM_GPU_MIXED || P->precision == BFM_GPU_MIXED_EXACT))
+		return fail("the split SpMV form exists for the FP64 and FP64_DF paths only");
 	P->lpr = shape;
 	P->tuned = 1;
 	return 0;

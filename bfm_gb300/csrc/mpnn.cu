@@ -315,7 +315,7 @@ struct LossArgs {
 	const double* v;   // power vector
 	double* partials;
 	unsigned* ticket;
-	double* sc;  // v.Kv, sum v.B^-1 v, e.Ke, sum e.B^-1 e, loss
+	double* sc;  // v.Kv, sum v.B^-1 v, e.Ke, sum e.B^-1 e, loss, v.v
 };
 
 // x_i.B_i^-1 x_i and w = (I + C_i)^-1 L_i^-1 x_i
@@ -353,6 +353,25 @@ __global__ void k_power(int N, const int* __restrict__ row_ptr, const int* __res
 	}
 	const double* B = blocks + 4l * i;
 	st2(vout, i, B[0] * y0 + B[1] * y1, B[2] * y0 + B[3] * y1);
+}
+
+// v.v into sc[5]; then v /= |v| (the loss and its gradient do not depend on v's scale)
+__global__ void k_vnorm(int N, const double* __restrict__ v, double* partials, unsigned* ticket, double* sc) {
+	double t[1] = {0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+		double2 const x = ld2(v, i);
+		t[0] += x.x * x.x + x.y * x.y;
+	}
+	double out[1];
+	if (grid_sum<1>(t, partials, ticket, out) && threadIdx.x == 0) sc[5] = out[0];
+}
+
+__global__ void k_vscale(int N, double* __restrict__ v, const double* __restrict__ sc) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N || !(sc[5] > 0.0)) return;
+	double const f = 1.0 / sqrt(sc[5]);
+	double2 const x = ld2(v, i);
+	st2(v, i, x.x * f, x.y * f);
 }
 
 __global__ void k_loss_terms(LossArgs a) {
@@ -667,10 +686,15 @@ int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const dou
 	bfmi_buffers(P, &bf);
 	if (!bf.vals64_any) return mfail("training needs the FP64 operator: assemble in FP64, MIXED_EXACT or FP64_DF");
 	int const N = bf.N;
-	// the power vector: v <- B K v, power_iters times (ping-pong through z)
+	// the power vector: v <- B K v, power_iters times (ping-pong through z),
+	// rescaled to unit length every 16 steps and at the end
 	for (int k = 0; k < power_iters; k++) {
 		k_power<<<nb(N), 256, 0, st>>>(N, bf.row_ptr, bf.cols, bf.vals64_any, net->blocks, v, net->z);
 		MCK(cudaMemcpyAsync(v, net->z, 2l * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+		if (k % 16 == 15 || k == power_iters - 1) {
+			k_vnorm<<<FEAT_GRID, TPB_K, 0, st>>>(N, v, net->partials, net->ticket, net->sc);
+			k_vscale<<<nb(N), 256, 0, st>>>(N, v, net->sc);
+		}
 	}
 	LossArgs la;
 	memset(&la, 0, sizeof la);
@@ -754,7 +778,7 @@ int bfm_gpu_mpnn_create(bfm_gpu_mpnn_t** out, unsigned seed) {
 	bfm_gpu_mpnn* net = (bfm_gpu_mpnn*) calloc(1, sizeof *net);
 	if (!net) return mfail("out of host memory");
 	if (alloc(&net->d.theta, NPARAM) || alloc(&net->d.grad, NPARAM) || alloc(&net->d.adam_m, NPARAM) ||
-	    alloc(&net->d.adam_v, NPARAM) || alloc(&net->d.wb, NPARAM) || alloc(&net->sc, 5) ||
+	    alloc(&net->d.adam_v, NPARAM) || alloc(&net->d.wb, NPARAM) || alloc(&net->sc, 6) ||
 	    alloc(&net->partials, 4 * FEAT_GRID) || alloc(&net->rms, 1) || alloc(&net->ticket, 1)) {
 		bfm_gpu_mpnn_destroy(net);
 		return -1;
