@@ -45,6 +45,11 @@ METHODS = {"fp64": ("FP64", "PC_JACOBI"), "fp64_df": ("FP64_DF", "PC_JACOBI"),
            "mixed_exact": ("MIXED_EXACT", "PC_JACOBI"), "mixed": ("MIXED", "PC_JACOBI"),
            "learned_fp64": ("FP64", "PC_LEARNED"), "learned_df": ("FP64_DF", "PC_LEARNED"),
            "learned_mixed": ("MIXED", "PC_LEARNED")}
+# FP64 residual-replacement threshold per precision (the recurrence residual
+# must drop by this factor between replacements), from a sweep on the
+# 2048x512 perforated plate: FP64 is insensitive, the FP32-pipe paths converge
+# in fewer iterations with rarer replacements
+REPLACE_DROP = {"FP64": 0.1, "FP64_DF": 0.01, "MIXED_EXACT": 0.001, "MIXED": 0.001}
 # fused SpMV kernel (K1) of each precision: the roofline kernel
 SPMV_KERNEL = {0: "k_hs64_spmv", 1: "k_mx_spmv", 2: "k_mx_spmv", 3: "k_hsdf_spmv"}
 # DRAM bytes (read + write) of one K1 launch on the 2048x512 perforated plate,
@@ -197,7 +202,8 @@ def run_gpu(args, rank: int, world: int):
         net = learned.Network(path=learned.WEIGHTS)
         net.use()
     if args.method == "best":
-        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed"] + (["learned_df", "learned_mixed"] if net else [])
+        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed"] + (["learned_fp64", "learned_df", "learned_mixed"]
+                                                                 if net else [])
     else:
         chosen = [args.method]
         if methods[args.method][1] == bfm_gb300.PC_LEARNED and net is None:
@@ -206,7 +212,7 @@ def run_gpu(args, rank: int, world: int):
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
     for m in chosen:
         prec, pc = methods[m]
-        o = bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc)
+        o = bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc, replace_drop=REPLACE_DROP[METHODS[m][0]])
 
         def step():
             assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
@@ -234,9 +240,12 @@ def run_gpu(args, rank: int, world: int):
         # per-kernel durations for the roofline (same stream, CUDA events)
         t_spmv, t_upd = C.c_double(), C.c_double()
         assert lib.bfm_gpu_problem_time_kernels(P, 50, C.byref(t_spmv), C.byref(t_upd)) == 0
+        shape = C.c_int()
+        lib.bfm_gpu_problem_shape(P, C.byref(shape))
         results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual, repl=s.replacements,
                           ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks, fallback=s.fallback,
-                          ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, pc=pc, x=x)
+                          ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, pc=pc, x=x,
+                          shape=shape.value)
     lib.bfm_gpu_problem_destroy(P)
     # displacement error of every method against the FP64 solution (the FP64
     # direct oracle does not fit the host at this size; the FP64 PCG solution
@@ -250,7 +259,8 @@ def run_gpu(args, rank: int, world: int):
     # end-to-end through bfm_sim_run with host buffers (the learned methods use
     # the network selected above through the same global options)
     prec, pc = methods[best]
-    lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc)))
+    lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc,
+                                                        replace_drop=REPLACE_DROP[METHODS[best][0]])))
     h = api.SimHandle.from_problem(lib, p)
     assert h.run() == 0, h.error()  # warm: allocates the device problem once
     torch.cuda.synchronize()
@@ -383,8 +393,12 @@ def main():
     nb = r["n_blocks"]
     bytes_spmv = algorithmic_bytes_spmv(nb, p.n_nodes, r["prec"], r["pc"] != 0)
     achieved = bytes_spmv / (r["ms_spmv"] * 1e-3) / 1e9
+    split = r["shape"] >= 1000
     traffic, traffic_src = (SPMV_TRAFFIC.get(r["prec"], (None, None))
-                            if args.workload == "perforated" and r["pc"] == 0 else (None, None))
+                            if args.workload == "perforated" and r["pc"] == 0 and r["shape"] in (1, 2) else (None, None))
+    kernel = SPMV_KERNEL[r["prec"]]
+    if split:
+        kernel = kernel.replace("_spmv", "_dir") + " + " + kernel + "_s"
     # assembly (pattern, Dirichlet marks, element loop, loads: about 24 kernels),
     # solve init + 2 kernels per iteration + replacement kernels, finish;
     # the learned preconditioner adds its 12 inference kernels per solve
@@ -413,13 +427,14 @@ def main():
         "methods": {k: {"ms": round(v["ms"], 3), "iterations": v["iters"], "status": v["status"],
                         "rel_residual": v["rel_res"], "err_vs_fp64": v["err_vs_fp64"],
                         "replacements": v["repl"], "fallback": v["fallback"], "ms_assemble": round(v["ms_assemble"], 3),
-                        "spmv_ms": round(v["ms_spmv"], 5), "update_ms": round(v["ms_update"], 5)}
+                        "spmv_ms": round(v["ms_spmv"], 5), "update_ms": round(v["ms_update"], 5),
+                        "spmv_shape": v["shape"]}
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 3), "traffic": traffic, "traffic_source": traffic_src,
-                     "kernel": SPMV_KERNEL[r["prec"]], "algorithmic_bytes": bytes_spmv,
+                     "kernel": kernel, "spmv_shape": r["shape"], "algorithmic_bytes": bytes_spmv,
                      "kernel_ms": round(r["ms_spmv"], 5), "peak_source": peak_kind},
         "e2e": {"value": round(e2e["ms"], 3), "unit": "ms", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},
