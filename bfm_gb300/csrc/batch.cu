@@ -9,7 +9,7 @@
 // Work layout: the rows of every part are cut into tiles (part, first row,
 // end row); block b owns tiles b, b+G, b+2G, ... for the whole solve.  Per
 // iteration:
-//   phase 1  tiles: p' = M r + beta_k p, q = (A32 + C) p', partial (p', q)
+//   phase 1  tiles: p' = M r + beta_k p, q = A32 p' in difference form, partial (p', q)
 //   barrier; every block sums each part's tile partials in tile order
 //            (deterministic, identical in all blocks): alpha_k
 //   phase 2  tiles: dx += alpha_k p', r -= alpha_k q, partials (r, M r), (r, r)
@@ -56,9 +56,9 @@ struct BatchArgs {
 	const int* row_ptr;
 	const int* cols;
 	const float* vals;
-	const float* corr;
+	const float* corr;       // row-sum block S of the FP32 operator (difference form)
 	const float* dinv;
-	const double* vals64;    // FP64 residual operator (nullptr: vals widened + corr)
+	const double* vals64;    // FP64 residual operator (nullptr: the FP32 one in difference form)
 	const double* b;
 	double* x;
 	float* r;
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 		__syncthreads();
 		if (sh.active == 0 || (a.timing_iters > 0 && it >= a.timing_iters)) break;
 
-		// ---- phase 1: q = (A32 + C) p', p' = M r + beta p
+		// ---- phase 1: q = A32 p' (difference form), p' = M r + beta p
 		for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
 			int const k = a.tile_part[t];
 			if (sh.done[k]) continue;
@@ -224,11 +224,17 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 				int const row = base + threadIdx.x / LPR;
 				bool const ok = row < t1;
 				int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+				// difference form: q_r = S_r g_r + sum_c A_rc (g_c - g_r)
+				float g0 = 0.f, g1 = 0.f;
+				if (ok) gather(row, g0, g1);
+				auto dgather = [=](int c, float& d0, float& d1) {
+					gather(c, d0, d1);
+					d0 -= g0;
+					d1 -= g1;
+				};
 				float y0, y1;
-				row_product<LPR, float>(a.cols, a.vals, ks, ke, sub, gather, y0, y1);
+				row_product<LPR, float>(a.cols, a.vals, ks, ke, sub, dgather, y0, y1);
 				if (ok && sub == 0) {
-					float g0, g1;
-					gather(row, g0, g1);
 					float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
 					y0 += cc.x * g0 + cc.y * g1;
 					y1 += cc.z * g0 + cc.w * g1;
@@ -331,20 +337,22 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 			double v0 = 0.0, v1 = 0.0;
 			int const t0 = a.tile_begin[t], t1 = a.tile_end[t];
 			const double* __restrict__ xx = a.x;
-			auto gx = [xx](int c, double& g0, double& g1) {
-				double2 const v = ld2(xx, c);
-				g0 = v.x;
-				g1 = v.y;
-			};
 			for (int base = t0; base < t1; base += rows_per_pass) {
 				int const row = base + threadIdx.x / LPR;
 				bool const ok = row < t1;
 				int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+				double2 const xi = ok ? ld2(xx, row) : make_double2(0.0, 0.0);
+				// FP64 operator as stored; the FP32 one in difference form
+				double2 const x0 = a.vals64 ? make_double2(0.0, 0.0) : xi;
+				auto gx = [xx, x0](int c, double& g0, double& g1) {
+					double2 const v = ld2(xx, c);
+					g0 = v.x - x0.x;
+					g1 = v.y - x0.y;
+				};
 				double y0, y1;
 				if (a.vals64) row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gx, y0, y1);
 				else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, gx, y0, y1);
 				if (ok && sub == 0) {
-					double2 const xi = ld2(a.x, row);
 					if (!a.vals64) {
 						float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
 						y0 += (double) cc.x * xi.x + (double) cc.y * xi.y;
@@ -404,9 +412,13 @@ __global__ void __launch_bounds__(BT) k_batch_residual(BatchArgs a) {
 		double v0 = 0.0, v1 = 0.0;
 		for (int row = a.tile_begin[t] + threadIdx.x; row < a.tile_end[t]; row += BT) {
 			double y0 = 0, y1 = 0;
+			double2 const xi = ld2(a.x, row);
+			double2 const x0 = a.vals64 ? make_double2(0.0, 0.0) : xi;  // difference form of the FP32 operator
 			for (int k = a.row_ptr[row]; k < a.row_ptr[row + 1]; k++) {
 				int const c = a.cols[k];
-				double2 const xc = ld2(a.x, c);
+				double2 xc = ld2(a.x, c);
+				xc.x -= x0.x;
+				xc.y -= x0.y;
 				double m0, m1, m2, m3;
 				if (a.vals64) ld_block(a.vals64, k, m0, m1, m2, m3);
 				else {
@@ -419,7 +431,6 @@ __global__ void __launch_bounds__(BT) k_batch_residual(BatchArgs a) {
 			}
 			if (!a.vals64) {
 				float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
-				double2 const xi = ld2(a.x, row);
 				y0 += (double) cc.x * xi.x + (double) cc.y * xi.y;
 				y1 += (double) cc.z * xi.x + (double) cc.w * xi.y;
 			}

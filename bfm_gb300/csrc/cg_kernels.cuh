@@ -76,7 +76,7 @@ struct CgArgs {
 	const V* vals;          // iteration operator (2x2 blocks)
 	const double* vals64;   // FP64 operator for true residuals (nullptr: `vals` widened)
 	const V* dinv;          // Jacobi: 2 per node; block Jacobi: 4 per node
-	const float* corr;      // mixed: per-node 2x2 row-sum correction of the FP32 operator
+	const float* corr;      // mixed: per-node 2x2 row-sum block S of the operator (difference form)
 	int block_pc;
 	const double* b;
 	double* x;
@@ -349,11 +349,15 @@ __global__ void __launch_bounds__(TPB_K) k_cg64_update(CgArgs<double> a) {
 //     thread;
 //   - the solution update is grouped: dx += alpha p' in FP32, flushed into the
 //     FP64 x only before each FP64 residual replacement and at the end;
-//   - the FP32 operator keeps the FP64 matrix's block row sums through a
-//     per-node 2x2 correction block, so rounding does not break the rigid
-//     translation modes (without it the FP32 operator loses definiteness on
-//     ill-conditioned meshes and CG diverges).
-//   K1: p' = M r + beta p; q = (A32 + C) p'; alpha = gamma / (p', q)
+//   - the FP32 operator is applied in difference form,
+//         (A g)_r = S_r g_r + sum_c A32_rc (g_c - g_r),
+//     with S_r the node's 2x2 block row sum of the operator (zero for an
+//     interior node, kept from the FP64 sums or as a double-float sum).  It
+//     keeps the rigid translation modes exact (without them the FP32 operator
+//     loses definiteness on ill-conditioned meshes and CG diverges), and for a
+//     smooth g the differences are small and exact, so the cancellation of a
+//     stiffness row (its terms sum to about zero) costs no FP32 accuracy.
+//   K1: p' = M r + beta p; q = A p' (difference form); alpha = gamma / (p', q)
 //   K2: dx += alpha p'; r -= alpha q; gamma' = (r, M r), rho = (r, r); beta
 //   on request (IF node): x += dx, dx = 0; r = b - A64 x in FP64; gamma = (r, M r)
 
@@ -399,11 +403,18 @@ __global__ void __launch_bounds__(TPB_K) k_mx_spmv(CgArgs<float> a) {
 	FOR_ROWS(LPR) {
 		bool const ok = row_ < a.N;
 		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		// difference form: y = S g_r + sum_c K_rc (g_c - g_r); for a smooth g
+		// the differences are small and exact, so nothing cancels in FP32
+		float g0 = 0.f, g1 = 0.f;
+		if (ok) gather(row_, g0, g1);
+		auto dgather = [=](int c, float& d0, float& d1) {
+			gather(c, d0, d1);
+			d0 -= g0;
+			d1 -= g1;
+		};
 		float y0, y1;
-		row_product_nb<LPR, NB, float>(a.cols, a.vals, ks, ke, sub_, gather, y0, y1);
+		row_product_nb<LPR, NB, float>(a.cols, a.vals, ks, ke, sub_, dgather, y0, y1);
 		if (ok && sub_ == 0) {
-			float g0, g1;
-			gather(row_, g0, g1);
 			float4 const cc = reinterpret_cast<const float4*>(a.corr)[row_];
 			y0 += cc.x * g0 + cc.y * g1;
 			y1 += cc.z * g0 + cc.w * g1;
@@ -508,14 +519,19 @@ __device__ __forceinline__ void residual_row(const CgArgs<V>& a, int row, int su
 		g0 = t.x;
 		g1 = t.y;
 	};
+	double2 const xi = ok ? ld2(x, row) : make_double2(0.0, 0.0);
+	auto dgather = [x, xi](int c, double& g0, double& g1) {  // difference form of the FP32 operator
+		double2 const t = ld2(x, c);
+		g0 = t.x - xi.x;
+		g1 = t.y - xi.y;
+	};
 	double y0, y1;
 	if (a.vals64) row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gather, y0, y1);
-	else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, gather, y0, y1);
+	else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, dgather, y0, y1);
 	e0 = e1 = 0.0;
 	if (ok) {
 		if (!a.vals64 && a.corr) {
 			float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
-			double2 const xi = ld2(x, row);
 			y0 += (double) cc.x * xi.x + (double) cc.y * xi.y;
 			y1 += (double) cc.z * xi.x + (double) cc.w * xi.y;
 		}

@@ -285,7 +285,7 @@ struct AsmArgs {
 	const double* last;
 	double* vals64;
 	float* vals32;
-	float* corr32;   // per node: 2x2 block of the row sums of (FP64 value - FP32 value)
+	float* corr32;   // per node: the FP32 operator's 2x2 block row sum S (difference form)
 	float* vals32lo; // double-float path: FP32 rounding of (FP64 value - FP32 value)
 	double* b;
 	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 	int const r0 = 2 * r, r1 = 2 * r + 1;
 	bool const c0 = a.last_ci[r0] >= 0, c1 = a.last_ci[r1] >= 0;
 	double k00 = 0, k01 = 0, k10 = 0, k11 = 0;
-	double corr[4] = {0, 0, 0, 0};  // FP64 row sums of what the FP32 copy loses
+	double rsum[4] = {0, 0, 0, 0};  // FP64 block row sum: the FP32 operator's S block (difference form)
 	for (int s = 0; s < len; s++) {
 		int const c = col[s];
 		int const d0 = 2 * c, d1 = 2 * c + 1;
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			for (int k = 0; k < 4; k++) {
 				float const f = (!EXACT && s == sd && (k == 1 || k == 2)) ? sym : (float) v[k];
 				a.vals32[o + k] = f;
-				corr[k] += v[k] - (double) f;
+				rsum[k] += v[k];
 				if (a.vals32lo) a.vals32lo[o + k] = (float) (v[k] - (double) f);
 			}
 		}
@@ -570,8 +570,8 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 		}
 	}
 	if (a.corr32 && !a.vals32lo) {
-		a.corr32[4 * r + 0] = (float) corr[0]; a.corr32[4 * r + 1] = (float) corr[1];
-		a.corr32[4 * r + 2] = (float) corr[2]; a.corr32[4 * r + 3] = (float) corr[3];
+		a.corr32[4 * r + 0] = (float) rsum[0]; a.corr32[4 * r + 1] = (float) rsum[1];
+		a.corr32[4 * r + 2] = (float) rsum[2]; a.corr32[4 * r + 3] = (float) rsum[3];
 	}
 	if (c0) b0 = a.last[r0];
 	if (c1) b1 = a.last[r1];
@@ -592,9 +592,10 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 //    index resolved by fully unrolled predicated adds, each element's
 //    contribution summed over the integration points before it is added;
 //  - the diagonal block rebuilt as a double-float sum of the off-diagonal
-//    blocks: its FP32 value is the high part and the low part goes to the
-//    correction block, so K32 + C keeps the exact zero row sums of the
-//    translation modes;
+//    blocks (exact zero row sums: the translation modes), and the row-sum
+//    block S of the difference form that the solver applies,
+//    (K g)_r = S_r g_r + sum_c K_rc (g_c - g_r), as a double-float sum of
+//    the stored row (zero for an interior node);
 //  - the block's output rows staged in shared memory and written with
 //    coalesced 16-byte stores.
 // Rows longer than RMAX are left to k_assemble<false>.
@@ -756,7 +757,8 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 	}
 	{
 		// one FP32 value for both off-diagonal entries of the diagonal block
-		// (symmetric operator); each entry's remainder goes to the correction
+		// (a symmetric stored matrix); each entry keeps its remainder in the
+		// row-sum block
 		float const m = __fmul_rn(0.5f, __fadd_rn(dh[1], dh[2]));
 		dl[1] = __fadd_rn(__fsub_rn(dh[1], m), dl[1]);
 		dl[2] = __fadd_rn(__fsub_rn(dh[2], m), dl[2]);
@@ -766,7 +768,9 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 	int const r0 = 2 * r, r1 = 2 * r + 1;
 	bool const c0 = mine && a.last_ci[r0] >= 0, c1 = mine && a.last_ci[r1] >= 0;
 	float k00 = 0.f, k01 = 0.f, k10 = 0.f, k11 = 0.f;
-	float4 corr = make_float4(0.f, 0.f, 0.f, 0.f);
+	// S block of the difference form: double-float row sum of what is stored
+	// plus the diagonal's low parts (zero for an interior node)
+	float sh[4] = {0.f, 0.f, 0.f, 0.f}, sl[4] = {0.f, 0.f, 0.f, 0.f};
 	double b0 = bf0, b1 = bf1;
 	__syncthreads();
 	bool const staged = long_rows == 0;
@@ -802,7 +806,11 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		if (c0 || e1) { v[1] = 0.f; lo[1] = 0.f; }
 		if (c1 || e0) { v[2] = 0.f; lo[2] = 0.f; }
 		if (c1 || e1) { v[3] = (r1 == d1) ? 1.f : 0.f; lo[3] = 0.f; }
-		if (dg) corr = make_float4(lo[0], lo[1], lo[2], lo[3]);
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			two_sum_acc(sh[k], sl[k], v[k]);
+			sl[k] = __fadd_rn(sl[k], lo[k]);
+		}
 		float4 const f4 = make_float4(v[0], v[1], v[2], v[3]);
 		if (staged) stage[rs - first_rs + t] = f4;
 		else reinterpret_cast<float4*>(a.vals32)[rs + t] = f4;
@@ -812,7 +820,8 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		}
 	}
 	if (mine) {
-		reinterpret_cast<float4*>(a.corr32)[r] = corr;
+		reinterpret_cast<float4*>(a.corr32)[r] =
+			make_float4(__fadd_rn(sh[0], sl[0]), __fadd_rn(sh[1], sl[1]), __fadd_rn(sh[2], sl[2]), __fadd_rn(sh[3], sl[3]));
 		if (c0) b0 = a.last[r0];
 		if (c1) b1 = a.last[r1];
 		reinterpret_cast<double2*>(a.b)[r] = make_double2(b0, b1);
@@ -1025,7 +1034,7 @@ struct bfm_gpu_problem {
 	// system
 	double* vals64;
 	float* vals32;
-	float* corr32;  // mixed: per-node 2x2 row-sum correction of the FP32 operator
+	float* corr32;  // mixed: per-node 2x2 block row sum S of the FP32 operator (difference form)
 	float* vals32lo;  // double-float path: low parts of the block values
 	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
 	double* b;
@@ -1765,6 +1774,8 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 			CK(cudaMalloc(&v, 2 * (N ? N : 1) * vsz));
 		}
 	}
+	// the SpMV shape is tuned per precision (each has its own kernels)
+	if (P->precision != precision) P->tuned = 0;
 	P->precision = precision;
 	CK(cudaEventRecord(P->ev[0], st));
 	CK(cudaMemsetAsync(P->err, 0, sizeof(int), st));
