@@ -42,8 +42,8 @@ struct CgState {
 };
 
 // After an FP64 true residual: converged, or stagnating at the roundoff floor
-// of the arithmetic (three replacements without halving the best residual),
-// or keep going.  Returns 1 when the solve should stop.
+// of the arithmetic (five replacements in a row without halving the best
+// residual), or keep going.  Returns 1 when the solve should stop.
 __device__ __forceinline__ int true_residual_verdict(CgState* st, double res2) {
 	st->replacements += 1;
 	st->rho_ref = res2;
@@ -54,7 +54,7 @@ __device__ __forceinline__ int true_residual_verdict(CgState* st, double res2) {
 		st->stall = 0;
 		return 0;
 	}
-	if (++st->stall >= 3) {
+	if (++st->stall >= 5) {
 		st->status = BFM_GPU_STAGNATED;
 		return 1;
 	}
