@@ -621,6 +621,23 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
 // a*b + c
 __device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) { return df_add(df_mul(a, b), c); }
 
+// (h + l + l2) * b + c for a matrix value held in three parts (the FP64 value
+// exactly): the third part's product joins the low-order sum, so the operator
+// the iteration applies is the FP64 matrix, not its 48-bit rounding (a fixed
+// 48-bit perturbation of the operator costs about 40% more iterations on the
+// ill-conditioned plates; rounding noise of that size does not)
+__device__ __forceinline__ dfl df_fma3(float h, float l, float l2, dfl b, dfl c) {
+	float const p = __fmul_rn(h, b.hi);
+	float e = __fmaf_rn(h, b.hi, -p);
+	e = __fmaf_rn(h, b.lo, e);
+	e = __fmaf_rn(l, b.hi, e);
+	e = __fmaf_rn(l2, b.hi, e);
+	float const hh = __fadd_rn(p, e);
+	return df_add({hh, __fsub_rn(e, __fsub_rn(hh, p))}, c);
+}
+
+__device__ __forceinline__ float bf16_bits(unsigned short u) { return __uint_as_float((unsigned) u << 16); }
+
 // node vector element: (u_hi, v_hi, u_lo, v_lo) in one float4
 __device__ __forceinline__ void df_ld(const float* v, int i, dfl& a, dfl& b) {
 	float4 const t = reinterpret_cast<const float4*>(v)[i];
@@ -653,6 +670,7 @@ struct DfArgs {
 	const int* cols;
 	const float* hi;    // 2x2 blocks, FP32 rounding of the FP64 value
 	const float* lo;    // FP32 rounding of the remainder
+	const ushort4* lo2; // BF16 bits of the second remainder: hi + lo + lo2 is the FP64 value
 	const double* vals64;  // the FP64 matrix, for the replacement residuals
 	const float* dinv;  // per node, df pair layout: Jacobi (u_hi, v_hi, u_lo, v_lo); block (4 hi, 4 lo)
 	int block_pc;
@@ -911,14 +929,17 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 #pragma unroll
 			for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? a.cols[k0 + j * LPR] : -1;
 			float4 zv[NB], pv[NB], h[NB], l[NB];
+			ushort4 l2[NB];
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				zv[j] = pv[j] = h[j] = l[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+				l2[j] = make_ushort4(0, 0, 0, 0);
 				if (c[j] >= 0) {
 					zv[j] = reinterpret_cast<const float4*>(a.u)[c[j]];
 					pv[j] = reinterpret_cast<const float4*>(a.p)[c[j]];
 					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
 					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
+					l2[j] = a.lo2[k0 + j * LPR];
 				}
 			}
 #pragma unroll
@@ -926,10 +947,10 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 				if (c[j] < 0) continue;
 				dfl const g0 = df_fma(beta, {pv[j].x, pv[j].z}, {zv[j].x, zv[j].z});
 				dfl const g1 = df_fma(beta, {pv[j].y, pv[j].w}, {zv[j].y, zv[j].w});
-				y0 = df_fma({h[j].x, l[j].x}, g0, y0);
-				y0 = df_fma({h[j].y, l[j].y}, g1, y0);
-				y1 = df_fma({h[j].z, l[j].z}, g0, y1);
-				y1 = df_fma({h[j].w, l[j].w}, g1, y1);
+				y0 = df_fma3(h[j].x, l[j].x, bf16_bits(l2[j].x), g0, y0);
+				y0 = df_fma3(h[j].y, l[j].y, bf16_bits(l2[j].y), g1, y0);
+				y1 = df_fma3(h[j].z, l[j].z, bf16_bits(l2[j].z), g0, y1);
+				y1 = df_fma3(h[j].w, l[j].w, bf16_bits(l2[j].w), g1, y1);
 			}
 		}
 #pragma unroll
@@ -1099,23 +1120,26 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 #pragma unroll
 			for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? a.cols[k0 + j * LPR] : -1;
 			float4 gv[NB], h[NB], l[NB];
+			ushort4 l2[NB];
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				gv[j] = h[j] = l[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+				l2[j] = make_ushort4(0, 0, 0, 0);
 				if (c[j] >= 0) {
 					gv[j] = reinterpret_cast<const float4*>(a.s)[c[j]];
 					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
 					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
+					l2[j] = a.lo2[k0 + j * LPR];
 				}
 			}
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				if (c[j] < 0) continue;
 				dfl const g0 = {gv[j].x, gv[j].z}, g1 = {gv[j].y, gv[j].w};
-				y0 = df_fma({h[j].x, l[j].x}, g0, y0);
-				y0 = df_fma({h[j].y, l[j].y}, g1, y0);
-				y1 = df_fma({h[j].z, l[j].z}, g0, y1);
-				y1 = df_fma({h[j].w, l[j].w}, g1, y1);
+				y0 = df_fma3(h[j].x, l[j].x, bf16_bits(l2[j].x), g0, y0);
+				y0 = df_fma3(h[j].y, l[j].y, bf16_bits(l2[j].y), g1, y0);
+				y1 = df_fma3(h[j].z, l[j].z, bf16_bits(l2[j].z), g0, y1);
+				y1 = df_fma3(h[j].w, l[j].w, bf16_bits(l2[j].w), g1, y1);
 			}
 		}
 #pragma unroll

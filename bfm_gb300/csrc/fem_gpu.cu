@@ -19,6 +19,7 @@
 // with the reference's operation order and no fused multiply-add (the __d*_rn
 // intrinsics are never contracted), so K is bit-identical to libbfm's dense
 // K and the integer work derived from its exact zeros (RCM) matches exactly.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -287,6 +288,7 @@ struct AsmArgs {
 	float* vals32;
 	float* corr32;   // per node: the FP32 operator's 2x2 block row sum S (difference form)
 	float* vals32lo; // double-float path: FP32 rounding of (FP64 value - FP32 value)
+	unsigned short* vals16lo2;  // double-float path: BF16 bits of what hi + lo still miss
 	double* b;
 	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
@@ -561,7 +563,13 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				float const f = (!EXACT && s == sd && (k == 1 || k == 2)) ? sym : (float) v[k];
 				a.vals32[o + k] = f;
 				rsum[k] += v[k];
-				if (a.vals32lo) a.vals32lo[o + k] = (float) (v[k] - (double) f);
+				if (a.vals32lo) {
+					float const lo = (float) (v[k] - (double) f);
+					a.vals32lo[o + k] = lo;
+					// third part: hi + lo carry 48 bits, the BF16 remainder 8 more (the
+					// subtractions are exact), so hi + lo + lo2 holds the FP64 value
+					a.vals16lo2[o + k] = __bfloat16_as_ushort(__float2bfloat16_rn((float) (v[k] - (double) f - (double) lo)));
+				}
 			}
 		}
 		if (c == r) {
@@ -1036,6 +1044,7 @@ struct bfm_gpu_problem {
 	float* vals32;
 	float* corr32;  // mixed: per-node 2x2 block row sum S of the FP32 operator (difference form)
 	float* vals32lo;  // double-float path: low parts of the block values
+	unsigned short* vals16lo2;  // double-float path: BF16 third parts of the block values
 	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
 	double* b;
 	int* last_ci;
@@ -1179,6 +1188,7 @@ DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	a.cols = P->cols;
 	a.hi = P->vals32;
 	a.lo = P->vals32lo;
+	a.lo2 = reinterpret_cast<const ushort4*>(P->vals16lo2);
 	a.vals64 = P->vals64;
 	a.dinv = P->dinv32;
 	a.block_pc = P->precond != BFM_GPU_PC_JACOBI;
@@ -1537,7 +1547,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->vals32lo, P->coords32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
+	                P->vals32, P->corr32, P->vals32lo, P->vals16lo2, P->coords32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1763,6 +1773,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 8 * N)) return -1;  // up to a double-float 2x2 block per node
 	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
 	if (dfp && !P->vals32lo && dalloc(&P->vals32lo, 4 * P->nb_cap)) return -1;
+	if (dfp && !P->vals16lo2 && dalloc(&P->vals16lo2, 4 * P->nb_cap)) return -1;
 	// 16 bytes per node per vector for FP64 and double-float, 8 for the mixed FP32 vectors
 	bool const wide = precision == BFM_GPU_FP64 || dfp;
 	size_t const vsz = wide ? sizeof(double) : sizeof(float);
@@ -1819,6 +1830,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.vals32 = want32 ? P->vals32 : nullptr;
 	a.corr32 = want32 ? P->corr32 : nullptr;
 	a.vals32lo = dfp ? P->vals32lo : nullptr;
+	a.vals16lo2 = dfp ? P->vals16lo2 : nullptr;
 	a.b = P->b;
 	a.dinv64 = want32 && !dfp ? nullptr : P->dinv64;
 	a.dinv32 = want32 && !dfp ? P->dinv32 : nullptr;
