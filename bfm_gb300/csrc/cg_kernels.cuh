@@ -621,22 +621,7 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
 // a*b + c
 __device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) { return df_add(df_mul(a, b), c); }
 
-// (h + l + l2) * b + c for a matrix value held in three parts (the FP64 value
-// exactly): the third part's product joins the low-order sum, so the operator
-// the iteration applies is the FP64 matrix, not its 48-bit rounding (a fixed
-// 48-bit perturbation of the operator costs about 40% more iterations on the
-// ill-conditioned plates; rounding noise of that size does not)
-__device__ __forceinline__ dfl df_fma3(float h, float l, float l2, dfl b, dfl c) {
-	float const p = __fmul_rn(h, b.hi);
-	float e = __fmaf_rn(h, b.hi, -p);
-	e = __fmaf_rn(h, b.lo, e);
-	e = __fmaf_rn(l, b.hi, e);
-	e = __fmaf_rn(l2, b.hi, e);
-	float const hh = __fadd_rn(p, e);
-	return df_add({hh, __fsub_rn(e, __fsub_rn(hh, p))}, c);
-}
 
-__device__ __forceinline__ float bf16_bits(unsigned short u) { return __uint_as_float((unsigned) u << 16); }
 
 // node vector element: (u_hi, v_hi, u_lo, v_lo) in one float4
 __device__ __forceinline__ void df_ld(const float* v, int i, dfl& a, dfl& b) {
@@ -670,7 +655,7 @@ struct DfArgs {
 	const int* cols;
 	const float* hi;    // 2x2 blocks, FP32 rounding of the FP64 value
 	const float* lo;    // FP32 rounding of the remainder
-	const ushort4* lo2; // BF16 bits of the second remainder: hi + lo + lo2 is the FP64 value
+	const float* srow;  // per node: FP64 block row sum of the matrix as a df pair (4 hi, then 4 lo)
 	const double* vals64;  // the FP64 matrix, for the replacement residuals
 	const float* dinv;  // per node, df pair layout: Jacobi (u_hi, v_hi, u_lo, v_lo); block (4 hi, 4 lo)
 	int block_pc;
@@ -906,6 +891,22 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
 }
 
 // ---- double-float HS kernels: x, r, z (in u), p, p' (in s), q (in w)
+// Difference form of the double-float SpMV:
+//     (A g)_r = S_r g_r + sum_c A_rc (g_c - g_r),
+// S_r the node's block row sum taken from the FP64 matrix.  The stored values
+// hold 48 of the FP64 values' 53 bits; applied directly that 48-bit operator
+// costs about 13-40% more CG iterations on the perforated plates, applied in
+// this form (exact row sums, and small exact differences for smooth g) it
+// converges like FP64.
+__device__ __forceinline__ void df_srow(const float* srow, int r, dfl g0, dfl g1, dfl& y0, dfl& y1) {
+	float4 const h = reinterpret_cast<const float4*>(srow)[2 * r];
+	float4 const l = reinterpret_cast<const float4*>(srow)[2 * r + 1];
+	y0 = df_fma({h.x, l.x}, g0, y0);
+	y0 = df_fma({h.y, l.y}, g1, y0);
+	y1 = df_fma({h.z, l.z}, g0, y1);
+	y1 = df_fma({h.w, l.w}, g1, y1);
+}
+
 template <int LPR, int NB = 1>
 __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 	CgState* st = a.st;
@@ -922,6 +923,15 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 		int const row = base + threadIdx.x / LPR;
 		bool const ok = row < a.N;
 		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+		dfl gr0 = {0.f, 0.f}, gr1 = {0.f, 0.f};
+		if (ok) {
+			dfl z0, z1, p0, p1;
+			df_ld(a.u, row, z0, z1);
+			df_ld(a.p, row, p0, p1);
+			gr0 = df_fma(beta, p0, z0);
+			gr1 = df_fma(beta, p1, z1);
+		}
+		dfl const ng0 = df_neg(gr0), ng1 = df_neg(gr1);
 		dfl y0 = {0.f, 0.f}, y1 = {0.f, 0.f};
 		for (int k0 = ks + sub; k0 < ke; k0 += LPR * NB) {
 			// NB entries per trip: indices, then gathers and block loads, then arithmetic
@@ -929,28 +939,25 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 #pragma unroll
 			for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? a.cols[k0 + j * LPR] : -1;
 			float4 zv[NB], pv[NB], h[NB], l[NB];
-			ushort4 l2[NB];
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				zv[j] = pv[j] = h[j] = l[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-				l2[j] = make_ushort4(0, 0, 0, 0);
 				if (c[j] >= 0) {
 					zv[j] = reinterpret_cast<const float4*>(a.u)[c[j]];
 					pv[j] = reinterpret_cast<const float4*>(a.p)[c[j]];
 					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
 					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
-					l2[j] = a.lo2[k0 + j * LPR];
 				}
 			}
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				if (c[j] < 0) continue;
-				dfl const g0 = df_fma(beta, {pv[j].x, pv[j].z}, {zv[j].x, zv[j].z});
-				dfl const g1 = df_fma(beta, {pv[j].y, pv[j].w}, {zv[j].y, zv[j].w});
-				y0 = df_fma3(h[j].x, l[j].x, bf16_bits(l2[j].x), g0, y0);
-				y0 = df_fma3(h[j].y, l[j].y, bf16_bits(l2[j].y), g1, y0);
-				y1 = df_fma3(h[j].z, l[j].z, bf16_bits(l2[j].z), g0, y1);
-				y1 = df_fma3(h[j].w, l[j].w, bf16_bits(l2[j].w), g1, y1);
+				dfl const g0 = df_add(df_fma(beta, {pv[j].x, pv[j].z}, {zv[j].x, zv[j].z}), ng0);
+				dfl const g1 = df_add(df_fma(beta, {pv[j].y, pv[j].w}, {zv[j].y, zv[j].w}), ng1);
+				y0 = df_fma({h[j].x, l[j].x}, g0, y0);
+				y0 = df_fma({h[j].y, l[j].y}, g1, y0);
+				y1 = df_fma({h[j].z, l[j].z}, g0, y1);
+				y1 = df_fma({h[j].w, l[j].w}, g1, y1);
 			}
 		}
 #pragma unroll
@@ -959,13 +966,10 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 			y1 = df_add(y1, {__shfl_xor_sync(0xffffffffu, y1.hi, o), __shfl_xor_sync(0xffffffffu, y1.lo, o)});
 		}
 		if (ok && sub == 0) {
-			dfl z0, z1, p0, p1;
-			df_ld(a.u, row, z0, z1);
-			df_ld(a.p, row, p0, p1);
-			dfl const g0 = df_fma(beta, p0, z0), g1 = df_fma(beta, p1, z1);
-			df_st(a.s, row, g0, g1);
+			df_srow(a.srow, row, gr0, gr1, y0, y1);
+			df_st(a.s, row, gr0, gr1);
 			df_st(a.w, row, y0, y1);
-			v[0] += df_dbl(df_add(df_mul(g0, y0), df_mul(g1, y1)));
+			v[0] += df_dbl(df_add(df_mul(gr0, y0), df_mul(gr1, y1)));
 		}
 	}
 	double out[1];
@@ -1114,32 +1118,32 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 		int const row = base + threadIdx.x / LPR;
 		bool const ok = row < a.N;
 		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+		dfl gr0 = {0.f, 0.f}, gr1 = {0.f, 0.f};
+		if (ok) df_ld(a.s, row, gr0, gr1);
+		dfl const ng0 = df_neg(gr0), ng1 = df_neg(gr1);
 		dfl y0 = {0.f, 0.f}, y1 = {0.f, 0.f};
 		for (int k0 = ks + sub; k0 < ke; k0 += LPR * NB) {
 			int c[NB];
 #pragma unroll
 			for (int j = 0; j < NB; j++) c[j] = k0 + j * LPR < ke ? a.cols[k0 + j * LPR] : -1;
 			float4 gv[NB], h[NB], l[NB];
-			ushort4 l2[NB];
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				gv[j] = h[j] = l[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-				l2[j] = make_ushort4(0, 0, 0, 0);
 				if (c[j] >= 0) {
 					gv[j] = reinterpret_cast<const float4*>(a.s)[c[j]];
 					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
 					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
-					l2[j] = a.lo2[k0 + j * LPR];
 				}
 			}
 #pragma unroll
 			for (int j = 0; j < NB; j++) {
 				if (c[j] < 0) continue;
-				dfl const g0 = {gv[j].x, gv[j].z}, g1 = {gv[j].y, gv[j].w};
-				y0 = df_fma3(h[j].x, l[j].x, bf16_bits(l2[j].x), g0, y0);
-				y0 = df_fma3(h[j].y, l[j].y, bf16_bits(l2[j].y), g1, y0);
-				y1 = df_fma3(h[j].z, l[j].z, bf16_bits(l2[j].z), g0, y1);
-				y1 = df_fma3(h[j].w, l[j].w, bf16_bits(l2[j].w), g1, y1);
+				dfl const g0 = df_add({gv[j].x, gv[j].z}, ng0), g1 = df_add({gv[j].y, gv[j].w}, ng1);
+				y0 = df_fma({h[j].x, l[j].x}, g0, y0);
+				y0 = df_fma({h[j].y, l[j].y}, g1, y0);
+				y1 = df_fma({h[j].z, l[j].z}, g0, y1);
+				y1 = df_fma({h[j].w, l[j].w}, g1, y1);
 			}
 		}
 #pragma unroll
@@ -1148,10 +1152,9 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 			y1 = df_add(y1, {__shfl_xor_sync(0xffffffffu, y1.hi, o), __shfl_xor_sync(0xffffffffu, y1.lo, o)});
 		}
 		if (ok && sub == 0) {
-			dfl g0, g1;
-			df_ld(a.s, row, g0, g1);
+			df_srow(a.srow, row, gr0, gr1, y0, y1);
 			df_st(a.w, row, y0, y1);
-			v[0] += df_dbl(df_add(df_mul(g0, y0), df_mul(g1, y1)));
+			v[0] += df_dbl(df_add(df_mul(gr0, y0), df_mul(gr1, y1)));
 		}
 	}
 	double out[1];

@@ -19,7 +19,6 @@
 // with the reference's operation order and no fused multiply-add (the __d*_rn
 // intrinsics are never contracted), so K is bit-identical to libbfm's dense
 // K and the integer work derived from its exact zeros (RCM) matches exactly.
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -288,9 +287,10 @@ struct AsmArgs {
 	float* vals32;
 	float* corr32;   // per node: the FP32 operator's 2x2 block row sum S (difference form)
 	float* vals32lo; // double-float path: FP32 rounding of (FP64 value - FP32 value)
-	unsigned short* vals16lo2;  // double-float path: BF16 bits of what hi + lo still miss
+	float* srow_df;  // double-float path: per node the FP64 block row sum as a df pair (4 hi, 4 lo)
 	double* b;
 	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
+	int const_grad;          // FP32 integration: shape gradients equal at every Gauss point (P1)
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
 	int precond;
@@ -563,13 +563,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				float const f = (!EXACT && s == sd && (k == 1 || k == 2)) ? sym : (float) v[k];
 				a.vals32[o + k] = f;
 				rsum[k] += v[k];
-				if (a.vals32lo) {
-					float const lo = (float) (v[k] - (double) f);
-					a.vals32lo[o + k] = lo;
-					// third part: hi + lo carry 48 bits, the BF16 remainder 8 more (the
-					// subtractions are exact), so hi + lo + lo2 holds the FP64 value
-					a.vals16lo2[o + k] = __bfloat16_as_ushort(__float2bfloat16_rn((float) (v[k] - (double) f - (double) lo)));
-				}
+				if (a.vals32lo) a.vals32lo[o + k] = (float) (v[k] - (double) f);
 			}
 		}
 		if (c == r) {
@@ -580,6 +574,16 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 	if (a.corr32 && !a.vals32lo) {
 		a.corr32[4 * r + 0] = (float) rsum[0]; a.corr32[4 * r + 1] = (float) rsum[1];
 		a.corr32[4 * r + 2] = (float) rsum[2]; a.corr32[4 * r + 3] = (float) rsum[3];
+	}
+	if (a.srow_df) {
+		// the double-float SpMV's row-sum block, from the FP64 values
+		float h[4], l[4];
+		for (int k = 0; k < 4; k++) {
+			h[k] = (float) rsum[k];
+			l[k] = (float) (rsum[k] - (double) h[k]);
+		}
+		reinterpret_cast<float4*>(a.srow_df)[2 * r] = make_float4(h[0], h[1], h[2], h[3]);
+		reinterpret_cast<float4*>(a.srow_df)[2 * r + 1] = make_float4(l[0], l[1], l[2], l[3]);
 	}
 	if (c0) b0 = a.last[r0];
 	if (c1) b1 = a.last[r1];
@@ -609,36 +613,49 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 // Rows longer than RMAX are left to k_assemble<false>.
 template <int RMAX>
 __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
-	__shared__ float4 stage[128 * RMAX];
-	__shared__ float sw[MAXQ], sphi[MAXQ][4], sdxi[MAXQ][4], sdeta[MAXQ][4];
+	constexpr int BT = 128;
+	__shared__ float4 stage[BT * RMAX];
+	__shared__ float sacc[RMAX * 4][BT];  // the row's blocks: [slot * 4 + entry][thread]
+	__shared__ float sw[MAXQ], sphi[MAXQ][4], sdxi[MAXQ][4], sdeta[MAXQ][4], swphi[4], swsum;
 	__shared__ int first_rs, long_rows;
-	int const r = blockIdx.x * blockDim.x + threadIdx.x;
+	int const tid = threadIdx.x;
+	int const r = blockIdx.x * BT + tid;
 	bool const valid = r < a.N;
 	int const rs = valid ? a.row_ptr[r] : 0;
 	int const len = valid ? a.row_ptr[r + 1] - rs : 0;
-	if (threadIdx.x == 0) {
-		first_rs = a.row_ptr[blockIdx.x * blockDim.x];
+	if (tid == 0) {
+		first_rs = a.row_ptr[blockIdx.x * BT];
 		long_rows = 0;
 	}
-	for (int k = threadIdx.x; k < MAXQ * 4; k += blockDim.x) {
+	for (int k = tid; k < MAXQ * 4; k += BT) {
 		int const q = k >> 2, j = k & 3;
 		sphi[q][j] = (float) a.rule.phi[q][j];
 		sdxi[q][j] = (float) a.rule.dxi[q][j];
 		sdeta[q][j] = (float) a.rule.deta[q][j];
 	}
-	if (threadIdx.x < MAXQ) sw[threadIdx.x] = (float) a.rule.w[threadIdx.x];
+	if (tid < MAXQ) sw[tid] = (float) a.rule.w[tid];
+	if (tid < 4) {
+		// constant-gradient rules (P1): one evaluation with the summed weights
+		double wp = 0.0;
+		for (int q = 0; q < a.rule.nq; q++) wp += a.rule.w[q] * a.rule.phi[q][tid];
+		swphi[tid] = (float) wp;
+	}
+	if (tid == 0) {
+		double ws = 0.0;
+		for (int q = 0; q < a.rule.nq; q++) ws += a.rule.w[q];
+		swsum = (float) ws;
+	}
+#pragma unroll
+	for (int t = 0; t < RMAX * 4; t++) sacc[t][tid] = 0.f;
 	__syncthreads();
 	if (len > RMAX) atomicOr(&long_rows, 1);
 	bool const mine = valid && len <= RMAX;
 
 	int col[RMAX];
-	float acc[RMAX][4];
 #pragma unroll
-	for (int t = 0; t < RMAX; t++) {
-		col[t] = (mine && t < len) ? a.cols[rs + t] : -1;
-		acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-	}
-	int const kind = a.kind, nq = a.rule.nq;
+	for (int t = 0; t < RMAX; t++) col[t] = (mine && t < len) ? a.cols[rs + t] : -1;
+	int const kind = a.kind;
+	int const nq = a.const_grad ? 1 : a.rule.nq;
 	bool const per_elem = a.elemE || a.elemNu;
 	float ca = 0.f, cb = 0.f, cc = 0.f;
 	if (!per_elem) material_abc32((float) a.E, (float) a.nu, a.stress, ca, cb, cc);
@@ -661,25 +678,27 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		int const e = a.inc[t];
 		if (e == prev_e) continue;
 		prev_e = e;
-		int map[4];
+		int slot[4];
 		float lx[4], ly[4];
 		int jr = 0;
 		float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
 		for (int j = 0; j < 4; j++) {
 			lx[j] = ly[j] = 0.f;
-			map[j] = -2;
+			slot[j] = -1;
 			if (j < kind) {
-				map[j] = a.elems[(long) e * kind + j];
-				float4 const cj = a.coords32[map[j]];
+				int const m = a.elems[(long) e * kind + j];
+				float4 const cj = a.coords32[m];
 				if (j == 0) c0 = cj;
 				lx[j] = __fadd_rn(__fsub_rn(cj.x, c0.x), __fsub_rn(cj.z, c0.z));
 				ly[j] = __fadd_rn(__fsub_rn(cj.y, c0.y), __fsub_rn(cj.w, c0.w));
+				if (m == r) jr = j;
+				int s = 0;
+#pragma unroll
+				for (int u = 1; u < RMAX; u++) s = col[u] == m ? u : s;
+				slot[j] = s;
 			}
 		}
-#pragma unroll
-		for (int j = 3; j >= 0; j--)
-			if (j < kind && map[j] == r) jr = j;
 		float fa = ca, fb = cb, fc = cc;
 		if (per_elem) {
 			float const E = a.elemE ? (float) a.elemE[e] : (float) a.E;
@@ -690,7 +709,6 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 #pragma unroll
 		for (int k = 0; k < 4; k++) ek[k][0] = ek[k][1] = ek[k][2] = ek[k][3] = 0.f;
 		for (int q = 0; q < nq; q++) {
-			float const w = sw[q];
 			float dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
 			float gx[4], ge[4];
 #pragma unroll
@@ -710,8 +728,8 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 				dx[j] = (gx[j] * dy_deta - ge[j] * dy_dxsi) * idet;
 				dy[j] = (ge[j] * dx_dxsi - gx[j] * dx_deta) * idet;
 			}
-			float const dw = det * w;
-			float const dwp = dw * sphi[q][jr];
+			float const dw = det * (a.const_grad ? swsum : sw[q]);
+			float const dwp = det * (a.const_grad ? swphi[jr] : sw[q] * sphi[q][jr]);
 			bf0 += dwp * gfx;
 			bf1 += dwp * gfy;
 			float xj = dx[0], yj = dy[0];
@@ -735,18 +753,19 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		}
 #pragma unroll
 		for (int k = 0; k < 4; k++) {
-			if (k >= kind) continue;
-			int const m = map[k];
-#pragma unroll
-			for (int t = 0; t < RMAX; t++)
-				if (col[t] == m) {
-					acc[t][0] += ek[k][0];
-					acc[t][1] += ek[k][1];
-					acc[t][2] += ek[k][2];
-					acc[t][3] += ek[k][3];
-				}
+			if (k >= kind || slot[k] < 0) continue;
+			int const s4 = 4 * slot[k];
+			sacc[s4 + 0][tid] += ek[k][0];
+			sacc[s4 + 1][tid] += ek[k][1];
+			sacc[s4 + 2][tid] += ek[k][2];
+			sacc[s4 + 3][tid] += ek[k][3];
 		}
 	}
+	float acc[RMAX][4];
+#pragma unroll
+	for (int t = 0; t < RMAX; t++)
+#pragma unroll
+		for (int k = 0; k < 4; k++) acc[t][k] = sacc[4 * t + k][tid];
 	// translation-preserving diagonal: minus the double-float sum of the off-diagonal blocks
 	float dh[4] = {0.f, 0.f, 0.f, 0.f}, dl[4] = {0.f, 0.f, 0.f, 0.f};
 	bool has_diag = false;
@@ -1044,7 +1063,7 @@ struct bfm_gpu_problem {
 	float* vals32;
 	float* corr32;  // mixed: per-node 2x2 block row sum S of the FP32 operator (difference form)
 	float* vals32lo;  // double-float path: low parts of the block values
-	unsigned short* vals16lo2;  // double-float path: BF16 third parts of the block values
+	float* srow_df;   // double-float path: block row sums (difference-form SpMV)
 	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
 	double* b;
 	int* last_ci;
@@ -1188,7 +1207,7 @@ DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	a.cols = P->cols;
 	a.hi = P->vals32;
 	a.lo = P->vals32lo;
-	a.lo2 = reinterpret_cast<const ushort4*>(P->vals16lo2);
+	a.srow = P->srow_df;
 	a.vals64 = P->vals64;
 	a.dinv = P->dinv32;
 	a.block_pc = P->precond != BFM_GPU_PC_JACOBI;
@@ -1547,7 +1566,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->vals32lo, P->vals16lo2, P->coords32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
+	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1773,7 +1792,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 8 * N)) return -1;  // up to a double-float 2x2 block per node
 	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
 	if (dfp && !P->vals32lo && dalloc(&P->vals32lo, 4 * P->nb_cap)) return -1;
-	if (dfp && !P->vals16lo2 && dalloc(&P->vals16lo2, 4 * P->nb_cap)) return -1;
+	if (dfp && !P->srow_df && dalloc(&P->srow_df, 8 * N)) return -1;
 	// 16 bytes per node per vector for FP64 and double-float, 8 for the mixed FP32 vectors
 	bool const wide = precision == BFM_GPU_FP64 || dfp;
 	size_t const vsz = wide ? sizeof(double) : sizeof(float);
@@ -1830,7 +1849,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.vals32 = want32 ? P->vals32 : nullptr;
 	a.corr32 = want32 ? P->corr32 : nullptr;
 	a.vals32lo = dfp ? P->vals32lo : nullptr;
-	a.vals16lo2 = dfp ? P->vals16lo2 : nullptr;
+	a.srow_df = dfp ? P->srow_df : nullptr;
 	a.b = P->b;
 	a.dinv64 = want32 && !dfp ? nullptr : P->dinv64;
 	a.dinv32 = want32 && !dfp ? P->dinv32 : nullptr;
@@ -1844,6 +1863,12 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		if (!P->coords32 && dalloc(&P->coords32, N)) return -1;
 		k_split_coords<<<blocks_for(N), TPB, 0, st>>>(P->N, P->coords, P->coords32);
 		a.coords32 = P->coords32;
+		// P1-type rules: every Gauss point has the same shape gradients, so the
+		// FP32 kernel integrates once with the summed weights
+		a.const_grad = 1;
+		for (int q = 1; q < P->rule.nq; q++)
+			for (int j = 0; j < P->kind; j++)
+				a.const_grad &= P->rule.dxi[q][j] == P->rule.dxi[0][j] && P->rule.deta[q][j] == P->rule.deta[0][j];
 		// register rows: 8 blocks cover structured P1 meshes (7 per row), 10 cover Q1 (9)
 		int const rmax = P->kind == 3 ? 8 : 10;
 		if (rmax == 8) k_assemble32<8><<<blocks_for(N, 128), 128, 0, st>>>(a);
