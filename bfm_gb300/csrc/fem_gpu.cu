@@ -291,6 +291,7 @@ struct AsmArgs {
 	double* b;
 	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
 	int const_grad;          // FP32 integration: shape gradients equal at every Gauss point (P1)
+	const float4* mat32;     // FP32 integration: per-element (a, b, c) material constants, or nullptr
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
 	int precond;
@@ -463,8 +464,13 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				ly[j] = __fadd_rn(__fsub_rn(cj.y, c0.y), __fsub_rn(cj.w, c0.w));
 			}
 			float fa, fb, fc;
-			material_abc32(a.elemE ? (float) a.elemE[e] : (float) a.E, a.elemNu ? (float) a.elemNu[e] : (float) a.nu,
-			               a.stress, fa, fb, fc);
+			if (a.mat32) {
+				float4 const m = a.mat32[e];
+				fa = m.x;
+				fb = m.y;
+				fc = m.z;
+			}
+			else material_abc32((float) a.E, (float) a.nu, a.stress, fa, fb, fc);
 			for (int q = 0; q < a.rule.nq; q++) {
 				float const w = (float) a.rule.w[q];
 				float dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
@@ -611,6 +617,17 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 //  - the block's output rows staged in shared memory and written with
 //    coalesced 16-byte stores.
 // Rows longer than RMAX are left to k_assemble<false>.
+// FP32 material constants (a, b, c) of every element, once per element
+// rather than once per owner row (three or four times)
+__global__ void k_elem_mat32(int NE, const double* __restrict__ elemE, const double* __restrict__ elemNu, double E,
+                             double nu, int stress, float4* __restrict__ mat) {
+	int const e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= NE) return;
+	float fa, fb, fc;
+	material_abc32(elemE ? (float) elemE[e] : (float) E, elemNu ? (float) elemNu[e] : (float) nu, stress, fa, fb, fc);
+	mat[e] = make_float4(fa, fb, fc, 0.f);
+}
+
 template <int RMAX>
 __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 	constexpr int BT = 128;
@@ -701,9 +718,10 @@ __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 		}
 		float fa = ca, fb = cb, fc = cc;
 		if (per_elem) {
-			float const E = a.elemE ? (float) a.elemE[e] : (float) a.E;
-			float const nu = a.elemNu ? (float) a.elemNu[e] : (float) a.nu;
-			material_abc32(E, nu, a.stress, fa, fb, fc);
+			float4 const m = a.mat32[e];
+			fa = m.x;
+			fb = m.y;
+			fc = m.z;
 		}
 		float ek[4][4];
 #pragma unroll
@@ -1065,6 +1083,7 @@ struct bfm_gpu_problem {
 	float* vals32lo;  // double-float path: low parts of the block values
 	float* srow_df;   // double-float path: block row sums (difference-form SpMV)
 	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
+	float4* mat32;    // FP32 integration: per-element material constants
 	double* b;
 	int* last_ci;
 	double *first, *last;
@@ -1566,7 +1585,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
+	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->mat32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1863,6 +1882,11 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		if (!P->coords32 && dalloc(&P->coords32, N)) return -1;
 		k_split_coords<<<blocks_for(N), TPB, 0, st>>>(P->N, P->coords, P->coords32);
 		a.coords32 = P->coords32;
+		if (a.elemE || a.elemNu) {
+			if (!P->mat32 && dalloc(&P->mat32, P->NE)) return -1;
+			k_elem_mat32<<<blocks_for(P->NE), TPB, 0, st>>>(P->NE, a.elemE, a.elemNu, P->E, P->nu, P->stress, P->mat32);
+			a.mat32 = P->mat32;
+		}
 		// P1-type rules: every Gauss point has the same shape gradients, so the
 		// FP32 kernel integrates once with the summed weights
 		a.const_grad = 1;
