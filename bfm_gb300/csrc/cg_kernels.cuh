@@ -660,8 +660,8 @@ struct DfArgs {
 	const float* dinv;  // per node, df pair layout: Jacobi (u_hi, v_hi, u_lo, v_lo); block (4 hi, 4 lo)
 	int block_pc;
 	const double* b;
-	float* x;           // df solution (converted to FP64 at the end)
-	double* x64;
+	float* x;           // df solution update since the last flush (grouped, like the mixed path's dx)
+	double* x64;        // the FP64 solution: every flush adds the update in FP64
 	float* r;
 	float* u;
 	float* p;
@@ -686,6 +686,7 @@ __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
 		df_precond(a.dinv, a.block_pc, i, r0, r1, u0, u1);
 		dfl const z = {0.f, 0.f};
 		df_st(a.x, i, z, z);
+		st2(a.x64, i, 0.0, 0.0);
 		df_st(a.r, i, r0, r1);
 		df_st(a.u, i, u0, u1);
 		df_st(a.p, i, z, z);
@@ -716,11 +717,18 @@ __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
 	}
 }
 
-__global__ void k_df_finish(DfArgs a) {
+// x64 += dx in FP64, dx = 0: before every FP64 residual and at the end.  The
+// update since the last flush is small next to x, so its 48 bits are plenty,
+// while x itself keeps FP64's 53 (a 48-bit x would put its rounding, times
+// the stiffness, into every true residual).
+__global__ void k_df_flush(DfArgs a) {
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		dfl x0, x1;
 		df_ld(a.x, i, x0, x1);
-		st2(a.x64, i, df_dbl(x0), df_dbl(x1));
+		double2 const x = ld2(a.x64, i);
+		st2(a.x64, i, x.x + df_dbl(x0), x.y + df_dbl(x1));
+		dfl const z = {0.f, 0.f};
+		df_st(a.x, i, z, z);
 	}
 }
 
@@ -1012,12 +1020,11 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_replace(DfArgs a) {
 	double v[2] = {0.0, 0.0};
 	int const sub = threadIdx.x % LPR;
 	int const rpb = blockDim.x / LPR;
-	const float* __restrict__ xdf = a.x;
-	auto gx = [xdf](int c, double& g0, double& g1) {
-		dfl x0, x1;
-		df_ld(xdf, c, x0, x1);
-		g0 = df_dbl(x0);
-		g1 = df_dbl(x1);
+	const double* __restrict__ x64 = a.x64;  // flushed just before
+	auto gx = [x64](int c, double& g0, double& g1) {
+		double2 const t = ld2(x64, c);
+		g0 = t.x;
+		g1 = t.y;
 	};
 	for (int base = blockIdx.x * rpb; base < a.N; base += gridDim.x * rpb) {
 		int const row = base + threadIdx.x / LPR;

@@ -1310,11 +1310,13 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			else if (add_node(body, &n1, prev ? &prev : nullptr, K.hsdf, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_hsdf_update, P->grid, pa)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
-			if (add_node(ifbody, &nr, nullptr, K.hsdfrepl, P->grid, pa)) return -1;
+			cudaGraphNode_t nf;
+			if (add_node(ifbody, &nf, nullptr, (void*) k_df_flush, P->grid, pa)) return -1;
+			if (add_node(ifbody, &nr, &nf, K.hsdfrepl, P->grid, pa)) return -1;
 			prev = nif;
 		}
 		cudaGraphNode_t n_fin;
-		if (add_node(g, &n_fin, &n_loop, (void*) k_df_finish, P->grid, pi)) return -1;
+		if (add_node(g, &n_fin, &n_loop, (void*) k_df_flush, P->grid, pi)) return -1;
 		if (add_node(g, &n_res, &n_fin, K.res64, P->grid, pr)) return -1;
 	}
 	else if (!mixed) {
