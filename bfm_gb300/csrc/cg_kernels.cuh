@@ -1168,6 +1168,65 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
 }
 
+// ---- precision switch: double-float iterations, then an FP64 tail
+// The double-float recurrence tracks FP64 PCG's residual history to about
+// 1e-7 on the perforated plates, then its attainable accuracy levels off near
+// 1e-8.  So the double-float loop stops at a looser tolerance, and this
+// kernel hands its state to FP64 HS-PCG without a restart: the latest
+// direction converted to FP64 (into the FP64 loop's first direction buffer),
+// r = b - A x in FP64 from the flushed solution, z = M r, gamma, and the
+// final tolerance.  beta stays from the last double-float step, exactly as
+// after a residual replacement.  A stagnated double-float loop continues in
+// FP64; a breakdown or the iteration cap ends the solve.
+__global__ void __launch_bounds__(TPB_K) k_df_switch(CgArgs<double> a, const float* __restrict__ dir_a,
+                                                      const float* __restrict__ dir_b, double rtol_final) {
+	CgState* st = a.st;
+	bool const go = st->iter > 0 && (st->status == BFM_GPU_OK || st->status == BFM_GPU_STAGNATED);
+	if (!go) {
+		if (blockIdx.x == 0 && threadIdx.x == 0 && a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		return;
+	}
+	// K1 of half (iter - 1) % 2 wrote the latest direction: half 0 into dir_a, half 1 into dir_b
+	const float* __restrict__ src = ((st->iter - 1) & 1) ? dir_b : dir_a;
+	double v[2] = {0.0, 0.0};
+	const double* __restrict__ x = a.x;
+	auto gx = [x](int c, double& g0, double& g1) {
+		double2 const t = ld2(x, c);
+		g0 = t.x;
+		g1 = t.y;
+	};
+	FOR_ROWS(1) {
+		bool const ok = row_ < a.N;
+		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
+		double y0, y1;
+		row_product<1, double>(a.cols, a.vals, ks, ke, sub_, gx, y0, y1);
+		if (ok) {
+			dfl p0, p1;
+			df_ld(src, row_, p0, p1);
+			st2(a.p, row_, df_dbl(p0), df_dbl(p1));  // same 16 bytes per node when src is a.p
+			double2 const bb = ld2(a.b, row_);
+			double const r0 = bb.x - y0, r1 = bb.y - y1;
+			st2(a.r, row_, r0, r1);
+			double z0, z1;
+			precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
+			st2(a.u, row_, z0, z1);
+			v[0] += r0 * r0 + r1 * r1;
+			v[1] += r0 * z0 + r1 * z1;
+		}
+	}
+	double out[2];
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		st->gamma = out[1];
+		st->rtol = rtol_final;
+		st->status = BFM_GPU_OK;
+		st->done = 0;
+		st->stall = 0;
+		st->best_true2 = 1e300;  // a fresh start for the stagnation test
+		st->done = true_residual_verdict(st, out[0]);
+		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
+	}
+}
+
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner
 struct CgKernels {
 	void* hs64s;   // split-form K1 (with k_hs64_dir before it)

@@ -998,6 +998,7 @@ __global__ void k_store_blocks(int N, const double* __restrict__ blocks, const i
 		for (int k = 0; k < 4; k++) {
 			h[k] = (float) m[k];
 			l[k] = (float) (m[k] - (double) h[k]);
+			dinv64[4l * i + k] = m[k];  // the FP64 tail of the double-float solve
 		}
 		reinterpret_cast<float4*>(dinv32)[2l * i] = make_float4(h[0], h[1], h[2], h[3]);
 		reinterpret_cast<float4*>(dinv32)[2l * i + 1] = make_float4(l[0], l[1], l[2], l[3]);
@@ -1030,6 +1031,9 @@ int g_num_sms = 0;
 
 // A learned solve that stagnates above this relative residual is redone with Jacobi
 constexpr double LEARNED_FALLBACK_REL = 1e-6;
+
+// The double-float path iterates to DF_SWITCH x rtol, then finishes in FP64
+constexpr double DF_SWITCH = 10.0;
 
 int num_sms() {
 	if (!g_num_sms) {
@@ -1285,16 +1289,25 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	cudaGraphNode_t n_init, n_loop, n_res, prev = nullptr;
 	int imixed = mixed;
 	if (P->precision == BFM_GPU_FP64_DF) {
+		// double-float iterations to DF_SWITCH x rtol, then FP64 iterations from the same state
+		bfm_gpu_opts_t od = *o;
+		od.rtol = o->rtol * DF_SWITCH < 1.0 ? o->rtol * DF_SWITCH : 1.0;
 		DfArgs a[2];
-		a[0] = df_args(P, o);
+		a[0] = df_args(P, &od);
 		a[0].use_cond = 1;
 		a[0].cond = h;
 		a[1] = a[0];
 		a[1].p = a[0].s;
 		a[1].s = a[0].p;
-		CgArgs<double> ar = cg_args<double>(P, o);  // final FP64 residual with the FP64 matrix
+		CgArgs<double> b[2];
+		b[0] = cg_args<double>(P, o);
+		CK(cudaGraphConditionalHandleCreate(&b[0].cond, g, 0u, cudaGraphCondAssignDefault));
+		b[0].use_cond = 1;
+		b[1] = b[0];
+		b[1].p = b[0].pn;
+		b[1].pn = b[0].p;
+		CgKernels const K64 = kernels_lpr(1001);
 		void* pi[1] = {&a[0]};
-		void* pr[1] = {&ar};
 		if (add_node(g, &n_init, nullptr, (void*) k_df_init, P->grid, pi)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
 		for (int half = 0; half < 2; half++) {
@@ -1315,9 +1328,31 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			if (add_node(ifbody, &nr, &nf, K.hsdfrepl, P->grid, pa)) return -1;
 			prev = nif;
 		}
-		cudaGraphNode_t n_fin;
+		cudaGraphNode_t n_fin, n_sw, n_loop2;
 		if (add_node(g, &n_fin, &n_loop, (void*) k_df_flush, P->grid, pi)) return -1;
-		if (add_node(g, &n_res, &n_fin, K.res64, P->grid, pr)) return -1;
+		// half 0 of the double-float loop writes its direction into a[0].s, half 1 into a[1].s
+		const float* dir_a = a[0].s;
+		const float* dir_b = a[1].s;
+		double rtol_final = o->rtol;
+		void* ps[4] = {&b[0], &dir_a, &dir_b, &rtol_final};
+		if (add_node(g, &n_sw, &n_fin, (void*) k_df_switch, P->grid, ps)) return -1;
+		cudaGraph_t body2;
+		if (add_conditional(g, &n_loop2, &n_sw, b[0].cond, cudaGraphCondTypeWhile, &body2)) return -1;
+		cudaGraphNode_t prev2 = nullptr;
+		for (int half = 0; half < 2; half++) {
+			CK(cudaGraphConditionalHandleCreate(&b[half].cond_repl, body2, 0u, cudaGraphCondAssignDefault));
+			void* pa[1] = {&b[half]};
+			cudaGraphNode_t n0, n1, n2, nif, nr;
+			cudaGraph_t ifbody;
+			if (add_node(body2, &n0, prev2 ? &prev2 : nullptr, (void*) k_hs64_dir, P->grid, pa)) return -1;
+			if (add_node(body2, &n1, &n0, K64.hs64s, P->grid, pa)) return -1;
+			if (add_node(body2, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
+			if (add_conditional(body2, &nif, &n2, b[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
+			if (add_node(ifbody, &nr, nullptr, K64.hs64repl, P->grid, pa)) return -1;
+			prev2 = nif;
+		}
+		void* pr[1] = {&b[0]};
+		if (add_node(g, &n_res, &n_loop2, K.res64, P->grid, pr)) return -1;
 	}
 	else if (!mixed) {
 		CgArgs<double> a[2];

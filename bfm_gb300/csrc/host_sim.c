@@ -51,6 +51,9 @@ static bfm_gpu_opts_t current_opts(void) {
 		if (p && (!strcmp(p, "df") || !strcmp(p, "3"))) t_opts.precision = BFM_GPU_FP64_DF;
 		char const* r = getenv("BFM_GPU_RTOL");
 		if (r) t_opts.rtol = strtod(r, NULL);
+		char const* pc = getenv("BFM_GPU_PRECOND");
+		if (pc && (!strcmp(pc, "block") || !strcmp(pc, "1"))) t_opts.precond = BFM_GPU_PC_BLOCK_JACOBI;
+		if (pc && (!strcmp(pc, "learned") || !strcmp(pc, "2"))) t_opts.precond = BFM_GPU_PC_LEARNED;
 		t_opts_set = 1;
 	}
 	return t_opts;
@@ -291,9 +294,28 @@ static bfm_gpu_problem_t* upload_and_assemble(bfm_state_t* st, bfm_sim_t* sim, b
 	return P;
 }
 
+/* The network the environment names (BFM_GPU_MPNN = weights file), loaded
+ * once and selected when a run asks for the learned preconditioner, so that
+ * unchanged callers can use it through environment variables alone. */
+static bfm_gpu_mpnn_t* g_env_net;
+
+static int env_network(bfm_state_t* st) {
+	char const* path = getenv("BFM_GPU_MPNN");
+	if (!path || g_env_net) return 0;
+	if (bfm_gpu_mpnn_create(&g_env_net, 0) < 0) return REPORT(st, "%s", bfm_gpu_last_error());
+	if (bfm_gpu_mpnn_load(g_env_net, path) < 0) {
+		REPORT(st, "%s", bfm_gpu_last_error());
+		bfm_gpu_mpnn_destroy(g_env_net);
+		g_env_net = NULL;
+		return -1;
+	}
+	return bfm_gpu_mpnn_use(g_env_net);
+}
+
 static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	bfm_state_t* const st = sim->state;
 	bfm_gpu_opts_t const o = current_opts();
+	if (o.precond == BFM_GPU_PC_LEARNED && env_network(st) < 0) return -1;
 	bfm_gpu_problem_t* P = upload_and_assemble(st, sim, inst, stress, o.precision, o.precond);
 	if (!P) return -1;
 	if (bfm_gpu_problem_solve(P, &o) < 0) return REPORT(st, "%s", bfm_gpu_last_error());
