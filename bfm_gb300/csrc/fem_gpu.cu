@@ -321,19 +321,6 @@ __device__ __forceinline__ void store_precond(const AsmArgs& a, int r, double k0
 	}
 }
 
-__device__ __forceinline__ void material_abc32(float E, float nu, int stress, float& a, float& b, float& c) {
-	if (!stress) {
-		float const den = (1.f + nu) * (1.f - 2.f * nu);
-		a = E * (1.f - nu) / den;
-		b = E * nu / den;
-	}
-	else {
-		float const den = 1.f - nu * nu;
-		a = E / den;
-		b = E * nu / den;
-	}
-	c = E / (2.f * (1.f + nu));
-}
 
 // s + x as an unevaluated float pair (TwoSum, no ordering assumption)
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
@@ -602,25 +589,6 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 	store_precond(a, r, k00, k01, k10, k11);
 }
 
-// FP32 element integration, fast form (BFM_GPU_MIXED): one thread per node
-// row as above (owner computes, no atomics), with every per-element and
-// per-row operation on the FP32 pipe (GB300 issues FP64 at a small fraction
-// of its FP32 rate):
-//  - node offsets within an element from a hi/lo float split of the FP64
-//    coordinates (the hi difference of nearby nodes is exact, the lo
-//    difference restores what the split dropped);
-//  - material constants per element in FP32; the Gauss rule from shared memory;
-//  - the row's accumulators in registers, rows of up to RMAX blocks, the block
-//    index resolved by fully unrolled predicated adds, each element's
-//    contribution summed over the integration points before it is added;
-//  - the diagonal block rebuilt as a double-float sum of the off-diagonal
-//    blocks (exact zero row sums: the translation modes), and the row-sum
-//    block S of the difference form that the solver applies,
-//    (K g)_r = S_r g_r + sum_c K_rc (g_c - g_r), as a double-float sum of
-//    the stored row (zero for an interior node);
-//  - the block's output rows staged in shared memory and written with
-//    coalesced 16-byte stores.
-// Rows longer than RMAX are left to k_assemble<false>.
 // Material constants (a, b, c) of every element for the FP32 integration,
 // once per element rather than once per owner row (three or four times):
 // computed in FP64 and rounded once, so they are the FP64 constants to FP32
@@ -634,6 +602,30 @@ __global__ void k_elem_mat32(int NE, const double* __restrict__ elemE, const dou
 	mat[e] = make_float4((float) da, (float) db, (float) dc, 0.f);
 }
 
+
+// FP32 element integration, fast form (BFM_GPU_MIXED): one thread per node
+// row as above (owner computes, no atomics), with the per-element and per-row
+// work on the FP32 pipe (GB300 issues FP64 at a small fraction of its FP32
+// rate):
+//  - node offsets within an element from a hi/lo float split of the FP64
+//    coordinates (the hi difference of nearby nodes is exact, the lo
+//    difference restores what the split dropped);
+//  - material constants from the per-element table above; the Gauss rule
+//    from shared memory; for rules whose shape gradients are the same at
+//    every point (P1) one evaluation with the summed weights;
+//  - the row's blocks accumulated in shared memory (slot found once per
+//    element node), each element's contribution summed over the integration
+//    points before it is added;
+//  - gradient products formed first, so the owner of the transposed block
+//    forms the same products and the FP32 operator is exactly symmetric;
+//  - the diagonal block rebuilt as a double-float sum of the off-diagonal
+//    blocks (exact zero row sums: the translation modes), and the row-sum
+//    block S of the difference form that the solver applies,
+//    (K g)_r = S_r g_r + sum_c K_rc (g_c - g_r), as a double-float sum of
+//    the stored row (zero for an interior node);
+//  - the block's output rows staged in shared memory and written with
+//    coalesced 16-byte stores.
+// Rows longer than RMAX are left to k_assemble<false>.
 template <int RMAX>
 __global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
 	constexpr int BT = 128;
