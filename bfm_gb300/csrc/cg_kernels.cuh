@@ -924,7 +924,7 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 	}
 	if (st->done && !a.timing) return;
 	dfl const beta = df_make(st->beta);
-	double v[1] = {0.0};
+	dfl dot = {0.f, 0.f};  // per-thread double-float sum of (p', q)
 	int const sub = threadIdx.x % LPR;
 	int const rpb = blockDim.x / LPR;
 	for (int base = blockIdx.x * rpb; base < a.N; base += gridDim.x * rpb) {
@@ -977,9 +977,10 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 			df_srow(a.srow, row, gr0, gr1, y0, y1);
 			df_st(a.s, row, gr0, gr1);
 			df_st(a.w, row, y0, y1);
-			v[0] += df_dbl(df_add(df_mul(gr0, y0), df_mul(gr1, y1)));
+			dot = df_add(dot, df_add(df_mul(gr0, y0), df_mul(gr1, y1)));
 		}
 	}
+	double v[1] = {df_dbl(dot)};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
 }
@@ -988,7 +989,8 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_update(DfArgs a) {
 	CgState* st = a.st;
 	if (st->done && !a.timing) return;
 	dfl const alpha = df_make(st->alpha), nalpha = df_neg(alpha);
-	double v[2] = {0.0, 0.0};
+	// per-thread double-float sums, one FP64 conversion per thread (FP64 is scarce on GB300)
+	dfl d0 = {0.f, 0.f}, d1 = {0.f, 0.f};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		dfl pn0, pn1, q0, q1, r0, r1, x0, x1;
 		df_ld(a.s, i, pn0, pn1);
@@ -1002,9 +1004,10 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_update(DfArgs a) {
 		dfl z0, z1;
 		df_precond(a.dinv, a.block_pc, i, r0, r1, z0, z1);
 		df_st(a.u, i, z0, z1);
-		v[0] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));
-		v[1] += df_dbl(df_add(df_mul(r0, r0), df_mul(r1, r1)));
+		d0 = df_add(d0, df_add(df_mul(r0, z0), df_mul(r1, z1)));
+		d1 = df_add(d1, df_add(df_mul(r0, r0), df_mul(r1, r1)));
 	}
+	double v[2] = {df_dbl(d0), df_dbl(d1)};
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0)
 		hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
@@ -1118,7 +1121,7 @@ template <int LPR, int NB = 1>
 __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 	CgState* st = a.st;
 	if (st->done && !a.timing) return;
-	double v[1] = {0.0};
+	dfl dot = {0.f, 0.f};  // per-thread double-float sum of (p', q)
 	int const sub = threadIdx.x % LPR;
 	int const rpb = blockDim.x / LPR;
 	for (int base = blockIdx.x * rpb; base < a.N; base += gridDim.x * rpb) {
@@ -1161,9 +1164,10 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 		if (ok && sub == 0) {
 			df_srow(a.srow, row, gr0, gr1, y0, y1);
 			df_st(a.w, row, y0, y1);
-			v[0] += df_dbl(df_add(df_mul(gr0, y0), df_mul(gr1, y1)));
+			dot = df_add(dot, df_add(df_mul(gr0, y0), df_mul(gr1, y1)));
 		}
 	}
+	double v[1] = {df_dbl(dot)};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) hs_alpha(st, out[0], a.timing, a.use_cond, a.cond);
 }
