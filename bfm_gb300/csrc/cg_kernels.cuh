@@ -610,11 +610,6 @@ __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
 	return {h, __fsub_rn(e, __fsub_rn(h, s))};
 }
 __device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
-// four BF16 bit patterns as floats
-__device__ __forceinline__ float4 bf16x4(ushort4 u) {
-	return make_float4(__uint_as_float((unsigned) u.x << 16), __uint_as_float((unsigned) u.y << 16),
-	                   __uint_as_float((unsigned) u.z << 16), __uint_as_float((unsigned) u.w << 16));
-}
 __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
 	float const p = __fmul_rn(a.hi, b.hi);
 	float e = __fmaf_rn(a.hi, b.hi, -p);
@@ -659,7 +654,7 @@ struct DfArgs {
 	const int* row_ptr;
 	const int* cols;
 	const float* hi;    // 2x2 blocks, FP32 rounding of the FP64 value
-	const ushort4* lo;  // BF16 rounding of the remainder: about 32 significant bits together
+	const float* lo;    // FP32 rounding of the remainder
 	const float* srow;  // per node: FP64 block row sum of the matrix as a df pair (4 hi, then 4 lo)
 	const double* vals64;  // the FP64 matrix, for the replacement residuals
 	const float* dinv;  // per node, df pair layout: Jacobi (u_hi, v_hi, u_lo, v_lo); block (4 hi, 4 lo)
@@ -959,7 +954,7 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv(DfArgs a) {
 					zv[j] = reinterpret_cast<const float4*>(a.u)[c[j]];
 					pv[j] = reinterpret_cast<const float4*>(a.p)[c[j]];
 					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
-					l[j] = bf16x4(a.lo[k0 + j * LPR]);
+					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
 				}
 			}
 #pragma unroll
@@ -1148,7 +1143,7 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_spmv_s(DfArgs a) {
 				if (c[j] >= 0) {
 					gv[j] = reinterpret_cast<const float4*>(a.s)[c[j]];
 					h[j] = reinterpret_cast<const float4*>(a.hi)[k0 + j * LPR];
-					l[j] = bf16x4(a.lo[k0 + j * LPR]);
+					l[j] = reinterpret_cast<const float4*>(a.lo)[k0 + j * LPR];
 				}
 			}
 #pragma unroll

@@ -286,7 +286,7 @@ struct AsmArgs {
 	double* vals64;
 	float* vals32;
 	float* corr32;   // per node: the FP32 operator's 2x2 block row sum S (difference form)
-	unsigned short* vals16lo; // double-float path: BF16 bits of (FP64 value - FP32 value)
+	float* vals32lo; // double-float path: FP32 rounding of (FP64 value - FP32 value)
 	float* srow_df;  // double-float path: per node the FP64 block row sum as a df pair (4 hi, 4 lo)
 	double* b;
 	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
@@ -321,12 +321,6 @@ __device__ __forceinline__ void store_precond(const AsmArgs& a, int r, double k0
 	}
 }
 
-
-// BF16 bits of x, rounded to nearest even (finite x)
-__device__ __forceinline__ unsigned short bf16_bits_rn(float x) {
-	unsigned const u = __float_as_uint(x);
-	return (unsigned short) ((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
-}
 
 // s + x as an unevaluated float pair (TwoSum, no ordering assumption)
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
@@ -566,7 +560,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 				float const f = (!EXACT && s == sd && (k == 1 || k == 2)) ? sym : (float) v[k];
 				a.vals32[o + k] = f;
 				rsum[k] += v[k];
-				if (a.vals16lo) a.vals16lo[o + k] = bf16_bits_rn((float) (v[k] - (double) f));
+				if (a.vals32lo) a.vals32lo[o + k] = (float) (v[k] - (double) f);
 			}
 		}
 		if (c == r) {
@@ -574,7 +568,7 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			k10 = v[2]; k11 = v[3];
 		}
 	}
-	if (a.corr32 && !a.vals16lo) {
+	if (a.corr32 && !a.vals32lo) {
 		a.corr32[4 * r + 0] = (float) rsum[0]; a.corr32[4 * r + 1] = (float) rsum[1];
 		a.corr32[4 * r + 2] = (float) rsum[2]; a.corr32[4 * r + 3] = (float) rsum[3];
 	}
@@ -1094,7 +1088,7 @@ struct bfm_gpu_problem {
 	double* vals64;
 	float* vals32;
 	float* corr32;  // mixed: per-node 2x2 block row sum S of the FP32 operator (difference form)
-	unsigned short* vals16lo;  // double-float path: BF16 low parts of the block values
+	float* vals32lo;  // double-float path: low parts of the block values
 	float* srow_df;   // double-float path: block row sums (difference-form SpMV)
 	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
 	float4* mat32;    // FP32 integration: per-element material constants
@@ -1239,7 +1233,7 @@ DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	a.row_ptr = P->row_ptr;
 	a.cols = P->cols;
 	a.hi = P->vals32;
-	a.lo = reinterpret_cast<const ushort4*>(P->vals16lo);
+	a.lo = P->vals32lo;
 	a.srow = P->srow_df;
 	a.vals64 = P->vals64;
 	a.dinv = P->dinv32;
@@ -1632,7 +1626,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->vals16lo, P->srow_df, P->coords32, P->mat32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
+	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->mat32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -1857,7 +1851,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if ((!want32 || dfp) && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
 	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 8 * N)) return -1;  // up to a double-float 2x2 block per node
 	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
-	if (dfp && !P->vals16lo && dalloc(&P->vals16lo, 4 * P->nb_cap)) return -1;
+	if (dfp && !P->vals32lo && dalloc(&P->vals32lo, 4 * P->nb_cap)) return -1;
 	if (dfp && !P->srow_df && dalloc(&P->srow_df, 8 * N)) return -1;
 	// 16 bytes per node per vector for FP64 and double-float, 8 for the mixed FP32 vectors
 	bool const wide = precision == BFM_GPU_FP64 || dfp;
@@ -1914,7 +1908,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.vals64 = want64 ? P->vals64 : nullptr;
 	a.vals32 = want32 ? P->vals32 : nullptr;
 	a.corr32 = want32 ? P->corr32 : nullptr;
-	a.vals16lo = dfp ? P->vals16lo : nullptr;
+	a.vals32lo = dfp ? P->vals32lo : nullptr;
 	a.srow_df = dfp ? P->srow_df : nullptr;
 	a.b = P->b;
 	a.dinv64 = want32 && !dfp ? nullptr : P->dinv64;
