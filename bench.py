@@ -329,12 +329,31 @@ def profile(args):
     assert lib.bfm_gpu_problem_autotune(P, C.byref(lpr)) == 0, bfm_gb300.last_error()
     t_spmv, t_upd = C.c_double(), C.c_double()
     assert lib.bfm_gpu_problem_time_kernels(P, args.reps, C.byref(t_spmv), C.byref(t_upd)) == 0
+    ms_net = None
+    if METHODS.get(args.method, ("", ""))[1] == "PC_LEARNED":
+        # the network's inference (features, 4 dense layers on the tensor cores, 3
+        # aggregations, head), timed on the problem's stream with CUDA events
+        from bfm_gb300 import learned
+        net = learned.Network(path=learned.WEIGHTS)
+        stream = lib.bfm_gpu_problem_stream(P)
+        import torch
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ext = torch.cuda.ExternalStream(stream)
+        for _ in range(2):
+            assert lib.bfm_gpu_mpnn_forward(net.h, P, None, None, None) == 0, bfm_gb300.last_error()
+        e0.record(ext)
+        for _ in range(args.reps):
+            assert lib.bfm_gpu_mpnn_forward(net.h, P, None, None, None) == 0, bfm_gb300.last_error()
+        e1.record(ext)
+        torch.cuda.synchronize()
+        ms_net = e0.elapsed_time(e1) / args.reps
+        net.close()
     lib.bfm_gpu_problem_destroy(P)
     nbytes = algorithmic_bytes_spmv(s.n_blocks, p.n_nodes, prec)
     return {"workload": p.name, "method": args.method, "lanes_per_row": lpr.value, "n_blocks": s.n_blocks,
             "ms_assemble": s.ms_assemble,
             "spmv_ms": t_spmv.value, "update_ms": t_upd.value, "spmv_algorithmic_bytes": nbytes,
-            "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9}
+            "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9, "network_forward_ms": ms_net}
 
 
 def run_reference(args, rank: int, world: int):
