@@ -627,10 +627,14 @@ __global__ void k_elem_mat32(int NE, const double* __restrict__ elemE, const dou
 //    coalesced 16-byte stores.
 // Rows longer than RMAX are left to k_assemble<false>.
 template <int RMAX>
-__global__ void __launch_bounds__(128) k_assemble32(AsmArgs a) {
+__global__ void __launch_bounds__(128, 6) k_assemble32(AsmArgs a) {
 	constexpr int BT = 128;
-	__shared__ float4 stage[BT * RMAX];
-	__shared__ float sacc[RMAX * 4][BT];  // the row's blocks: [slot * 4 + entry][thread]
+	// the rows' block accumulators, [slot * 4 + entry][thread]; once every thread
+	// has read its column back (before the epilogue's barrier) the same memory
+	// stages the block's output rows
+	__shared__ __align__(16) float smem_rows[RMAX * 4 * BT];
+	float (*const sacc)[BT] = reinterpret_cast<float (*)[BT]>(smem_rows);
+	float4* const stage = reinterpret_cast<float4*>(smem_rows);
 	__shared__ float sw[MAXQ], sphi[MAXQ][4], sdxi[MAXQ][4], sdeta[MAXQ][4], swphi[4], swsum;
 	__shared__ int first_rs, long_rows;
 	int const tid = threadIdx.x;
