@@ -144,19 +144,22 @@ __device__ __forceinline__ void diag_block(const FeatArgs& a, int r, double& k00
 		}
 }
 
-// per node: mean log10 E of the incident elements; RMS of Dinv b
+// per node: mean log10 E of the incident elements; RMS of Dinv b.  The
+// features end up in BF16, so they are computed in FP32 (FP64 is scarce on
+// GB300); the per-node means are stored exactly so that equal materials give
+// exactly zero contrasts.
 __global__ void k_feat1(FeatArgs a) {
 	double v[1] = {0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-		double s = 0.0;
+		float s = 0.f;
 		int const s0 = a.inc_ptr[i], s1 = a.inc_ptr[i + 1];
-		for (int t = s0; t < s1; t++) s += log10(a.elemE ? a.elemE[a.inc[t]] : a.E);
-		a.scratch[i] = s1 > s0 ? s / (s1 - s0) : log10(a.E);
+		for (int t = s0; t < s1; t++) s += log10f((float) (a.elemE ? a.elemE[a.inc[t]] : a.E));
+		a.scratch[i] = s1 > s0 ? (double) (s / (float) (s1 - s0)) : (double) log10f((float) a.E);
 		double k00, k01, k11;
 		diag_block(a, i, k00, k01, k11);
 		double2 const bb = ld2(a.b, i);
-		double const z0 = k00 != 0.0 ? bb.x / k00 : 0.0, z1 = k11 != 0.0 ? bb.y / k11 : 0.0;
-		v[0] += z0 * z0 + z1 * z1;
+		float const z0 = k00 != 0.0 ? (float) bb.x / (float) k00 : 0.f, z1 = k11 != 0.0 ? (float) bb.y / (float) k11 : 0.f;
+		v[0] += (double) (z0 * z0 + z1 * z1);
 	}
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) a.rms[0] = sqrt(out[0] / (2.0 * (a.N > 0 ? a.N : 1)));
@@ -168,83 +171,114 @@ __global__ void k_feat2(FeatArgs a) {
 	float f[FIN];
 	for (int k = 0; k < FIN; k++) f[k] = 0.f;
 	int const r0 = a.row_ptr[i], r1 = a.row_ptr[i + 1];
-	double nb = 0.0;
-	for (int k = r0; k < r1; k++) nb += a.scratch[a.cols[k]];
-	nb /= (r1 - r0);
-	double nu = 0.0, lmin = 0.0, lmax = 0.0;
+	float nb = 0.f;
+	for (int k = r0; k < r1; k++) nb += (float) a.scratch[a.cols[k]];
+	nb /= (float) (r1 - r0);
+	float nu = 0.f, lmin = 0.f, lmax = 0.f;
 	int const s0 = a.inc_ptr[i], s1 = a.inc_ptr[i + 1];
 	for (int t = s0; t < s1; t++) {
-		nu += a.elemNu ? a.elemNu[a.inc[t]] : a.nu;
-		double const le = log10(a.elemE ? a.elemE[a.inc[t]] : a.E);
-		lmin = t == s0 ? le : fmin(lmin, le);
-		lmax = t == s0 ? le : fmax(lmax, le);
+		nu += (float) (a.elemNu ? a.elemNu[a.inc[t]] : a.nu);
+		float const le = log10f((float) (a.elemE ? a.elemE[a.inc[t]] : a.E));
+		lmin = t == s0 ? le : fminf(lmin, le);
+		lmax = t == s0 ? le : fmaxf(lmax, le);
 	}
-	nu = s1 > s0 ? nu / (s1 - s0) : a.nu;
-	double k00, k01, k11;
-	diag_block(a, i, k00, k01, k11);
+	nu = s1 > s0 ? nu / (float) (s1 - s0) : (float) a.nu;
+	double k00d, k01d, k11d;
+	diag_block(a, i, k00d, k01d, k11d);
+	float const k00 = (float) k00d, k01 = (float) k01d, k11 = (float) k11d;
 	double2 const bb = ld2(a.b, i);
-	double const rms = a.rms[0] > 0.0 ? a.rms[0] : 1.0;
-	double const z0 = (k00 != 0.0 ? bb.x / k00 : 0.0) / rms, z1 = (k11 != 0.0 ? bb.y / k11 : 0.0) / rms;
-	f[0] = (float) (a.scratch[i] - nb);
-	f[1] = (float) ((nu - 0.3) * 10.0);
+	float const rms = a.rms[0] > 0.0 ? (float) a.rms[0] : 1.f;
+	float const z0 = (k00 != 0.f ? (float) bb.x / k00 : 0.f) / rms, z1 = (k11 != 0.f ? (float) bb.y / k11 : 0.f) / rms;
+	f[0] = (float) a.scratch[i] - nb;
+	f[1] = (nu - 0.3f) * 10.f;
 	f[2] = a.last_ci[2 * i] >= 0 ? 1.f : 0.f;
 	f[3] = a.last_ci[2 * i + 1] >= 0 ? 1.f : 0.f;
 	f[4] = (float) (r1 - r0) / 9.f;
-	f[5] = (float) z0;
-	f[6] = (float) z1;
-	f[7] = (k00 > 0.0 && k11 > 0.0) ? (float) log10(k00 / k11) : 0.f;
-	f[8] = (k00 > 0.0 && k11 > 0.0) ? (float) (k01 / sqrt(k00 * k11)) : 0.f;
-	f[9] = (float) (fabs(z0) + fabs(z1));
-	f[10] = (float) (lmin - lmax);
+	f[5] = z0;
+	f[6] = z1;
+	f[7] = (k00 > 0.f && k11 > 0.f) ? log10f(k00 / k11) : 0.f;
+	f[8] = (k00 > 0.f && k11 > 0.f) ? k01 / sqrtf(k00 * k11) : 0.f;
+	f[9] = fabsf(z0) + fabsf(z1);
+	f[10] = lmin - lmax;
 	for (int k = 0; k < FIN; k++) a.f[(long) i * FIN + k] = __float2bfloat16(f[k]);
 }
 
 // ---------------------------------------------------------------- forward
 
-// Y = relu(W [X0 | X1] + b): X0, X1 are N x 64 (or X0 alone N x 16), Y N x 64 BF16
+// Y = relu(W [X0 | X1] + b): X0, X1 are N x 64 (or X0 alone N x 16), Y N x 64
+// BF16.  Persistent blocks: the weight tile is staged in shared memory once,
+// then the block walks 64-node tiles; activations move in 16-byte vectors.
 template <int K>
 __global__ void __launch_bounds__(MT) k_dense_fwd(int N, const bf16* __restrict__ x0, const bf16* __restrict__ x1,
                                                   const bf16* __restrict__ w, const float* __restrict__ bias,
                                                   bf16* __restrict__ y) {
-	__shared__ bf16 xs[TILE][K + 8];
-	__shared__ bf16 ws[HID][K + 8];
-	int const node0 = blockIdx.x * TILE;
-	for (int e = threadIdx.x; e < TILE * K; e += MT) {
-		int const n = e / K, k = e % K, node = node0 + n;
-		bf16 v = __float2bfloat16(0.f);
-		if (node < N) v = K == FIN ? x0[(long) node * FIN + k] : (k < HID ? x0[(long) node * HID + k] : x1[(long) node * HID + k - HID]);
-		xs[n][k] = v;
+	__shared__ __align__(16) bf16 xs[TILE][K + 8];
+	__shared__ __align__(16) bf16 ws[HID][K + 8];
+	constexpr int CH = K / 8;  // 16-byte chunks per row
+	for (int e = threadIdx.x; e < HID * CH; e += MT) {
+		int const n = e / CH, c = e % CH;
+		*reinterpret_cast<uint4*>(&ws[n][8 * c]) = reinterpret_cast<const uint4*>(w)[e];
 	}
-	for (int e = threadIdx.x; e < HID * K; e += MT) ws[e / K][e % K] = w[e];
-	__syncthreads();
 	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	float acc[8][4] = {};
-	auto at_a = [&](int m, int k) { return xs[warp * 16 + m][k]; };
-	auto at_b = [&](int k, int n) { return ws[n][k]; };  // B(k, n) = W[n][k]
-	warp_gemm<8>(acc, K, at_a, at_b);
+	int const tiles = (N + TILE - 1) / TILE;
+	for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+		int const node0 = tile * TILE;
+		__syncthreads();  // the previous tile's reads of xs are done (and ws is staged)
+		for (int e = threadIdx.x; e < TILE * CH; e += MT) {
+			int const n = e / CH, c = e % CH, node = node0 + n;
+			uint4 v = make_uint4(0u, 0u, 0u, 0u);
+			if (node < N) {
+				if (K == FIN) v = reinterpret_cast<const uint4*>(x0 + (long) node * FIN)[c];
+				else v = c < HID / 8 ? reinterpret_cast<const uint4*>(x0 + (long) node * HID)[c]
+				                     : reinterpret_cast<const uint4*>(x1 + (long) node * HID)[c - HID / 8];
+			}
+			*reinterpret_cast<uint4*>(&xs[n][8 * c]) = v;
+		}
+		__syncthreads();
+		float acc[8][4] = {};
+		auto at_a = [&](int m, int k) { return xs[warp * 16 + m][k]; };
+		auto at_b = [&](int k, int n) { return ws[n][k]; };  // B(k, n) = W[n][k]
+		warp_gemm<8>(acc, K, at_a, at_b);
 #pragma unroll
-	for (int j = 0; j < 8; j++) {
-		int const n = 8 * j + 2 * t;
+		for (int j = 0; j < 8; j++) {
+			int const n = 8 * j + 2 * t;
 #pragma unroll
-		for (int h = 0; h < 2; h++) {
-			int const node = node0 + warp * 16 + g + 8 * h;
-			if (node >= N) continue;
-			float const v0 = fmaxf(acc[j][2 * h] + bias[n], 0.f), v1 = fmaxf(acc[j][2 * h + 1] + bias[n + 1], 0.f);
-			y[(long) node * HID + n] = __float2bfloat16(v0);
-			y[(long) node * HID + n + 1] = __float2bfloat16(v1);
+			for (int h = 0; h < 2; h++) {
+				int const node = node0 + warp * 16 + g + 8 * h;
+				if (node >= N) continue;
+				float const v0 = fmaxf(acc[j][2 * h] + bias[n], 0.f), v1 = fmaxf(acc[j][2 * h + 1] + bias[n + 1], 0.f);
+				*reinterpret_cast<uint32_t*>(y + (long) node * HID + n) = pack2(__float2bfloat16(v0), __float2bfloat16(v1));
+			}
 		}
 	}
 }
 
-// m_i = mean of h over the node's graph row (itself included)
+// m_i = mean of h over the node's graph row (itself included); one thread
+// per node and 8-channel chunk, 16-byte loads
 __global__ void k_agg(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, const bf16* __restrict__ h,
                       bf16* __restrict__ m) {
-	int const i = blockIdx.x * (blockDim.x / HID) + threadIdx.x / HID, c = threadIdx.x % HID;
+	constexpr int CH = HID / 8;
+	long const e = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	int const i = (int) (e / CH), c = (int) (e % CH);
 	if (i >= N) return;
-	float s = 0.f;
+	float s[8] = {};
 	int const r0 = row_ptr[i], r1 = row_ptr[i + 1];
-	for (int k = r0; k < r1; k++) s += __bfloat162float(h[(long) cols[k] * HID + c]);
-	m[(long) i * HID + c] = __float2bfloat16(s / (float) (r1 - r0));
+	for (int k = r0; k < r1; k++) {
+		uint4 const v = reinterpret_cast<const uint4*>(h + (long) cols[k] * HID)[c];
+		uint32_t const u[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			s[2 * q] += __uint_as_float(u[q] << 16);
+			s[2 * q + 1] += __uint_as_float(u[q] & 0xFFFF0000u);
+		}
+	}
+	float const inv = 1.f / (float) (r1 - r0);
+	uint4 o;
+	o.x = pack2(__float2bfloat16(s[0] * inv), __float2bfloat16(s[1] * inv));
+	o.y = pack2(__float2bfloat16(s[2] * inv), __float2bfloat16(s[3] * inv));
+	o.z = pack2(__float2bfloat16(s[4] * inv), __float2bfloat16(s[5] * inv));
+	o.w = pack2(__float2bfloat16(s[6] * inv), __float2bfloat16(s[7] * inv));
+	reinterpret_cast<uint4*>(m + (long) i * HID)[c] = o;
 }
 
 // o = Wo h3 + bo, c = 0.45 tanh(o); the preconditioner blocks from c:
@@ -588,6 +622,18 @@ struct bfm_gpu_mpnn {
 
 namespace {
 
+// blocks of the persistent dense kernels: six per SM
+int persistent_grid() {
+	static int g = 0;
+	if (!g) {
+		int dev = 0, sms = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		g = 6 * (sms > 0 ? sms : 1);
+	}
+	return g;
+}
+
 void free_acts(bfm_gpu_mpnn* net) {
 	void* p[] = {net->f, net->h[0], net->h[1], net->h[2], net->h[3], net->m[0], net->m[1], net->m[2], net->dpre, net->o,
 	             net->d_o, net->dh, net->dx, net->blocks, net->lfac, net->z, net->az, net->scratch};
@@ -667,10 +713,11 @@ int forward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, cudaStream_t st) {
 	k_feat1<<<FEAT_GRID, TPB_K, 0, st>>>(fa);
 	k_feat2<<<nb(N), 256, 0, st>>>(fa);
 	int const tiles = (N + TILE - 1) / TILE > 0 ? (N + TILE - 1) / TILE : 1;
-	k_dense_fwd<FIN><<<tiles, MT, 0, st>>>(N, net->f, nullptr, net->d.wb + O_W0, net->d.theta + O_B0, net->h[0]);
+	int const pgrid = tiles < persistent_grid() ? tiles : persistent_grid();
+	k_dense_fwd<FIN><<<pgrid, MT, 0, st>>>(N, net->f, nullptr, net->d.wb + O_W0, net->d.theta + O_B0, net->h[0]);
 	for (int l = 1; l <= 3; l++) {
-		k_agg<<<nb((long) N * HID), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->h[l - 1], net->m[l - 1]);
-		k_dense_fwd<HK><<<tiles, MT, 0, st>>>(N, net->h[l - 1], net->m[l - 1], net->d.wb + o_w(l), net->d.theta + o_b(l),
+		k_agg<<<nb((long) N * (HID / 8)), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->h[l - 1], net->m[l - 1]);
+		k_dense_fwd<HK><<<pgrid, MT, 0, st>>>(N, net->h[l - 1], net->m[l - 1], net->d.wb + o_w(l), net->d.theta + o_b(l),
 		                                      net->h[l]);
 	}
 	k_head<<<nb(N), 256, 0, st>>>(N, net->h[3], net->d.theta, net->o, bf.row_ptr, bf.cols, bf.vals64_any, bf.vals32,
@@ -762,6 +809,7 @@ void init_theta(float* th, unsigned seed) {
 }
 
 bfm_gpu_mpnn* g_active_net = nullptr;
+
 
 // weights file: magic, version, layer sizes, parameter count, FP32 parameters (little endian)
 constexpr char MAGIC[8] = {'B', 'F', 'M', 'M', 'P', 'N', 'N', '\0'};
