@@ -67,6 +67,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_set_shape": (_i, [_vp, _i]),
     "bfm_gpu_pcg_solve_noalloc": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _d, _i, _P(_i), _P(_d), _vp]),
     "bfm_gpu_problem_set_edge_loads": (_i, [_vp, _i, _vp, _vp, _i]),
+    "bfm_gpu_problem_set_edge_boundary": (_i, [_vp, _vp, _i]),
     "bfm_gpu_problem_set_parts": (_i, [_vp, _i, _vp]),
     "bfm_gpu_problem_solve_parts": (_i, [_vp, _P(bfm_gpu_opts_t)]),
     "bfm_gpu_problem_part_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _P(_i), _P(_i), _P(_d)]),

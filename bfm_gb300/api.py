@@ -58,11 +58,14 @@ class SimHandle:
         self.keep += [coords, elems]
         if p.edges is not None:
             edges = (abi.bfm_edge_t * len(p.edges))()
+            eb = getattr(p, "edge_boundary", None)
             for i, (a, b) in enumerate(p.edges):
                 edges[i].nodes[0] = int(a)
                 edges[i].nodes[1] = int(b)
                 edges[i].elems[0] = -1
-                edges[i].elems[1] = -1
+                # elems[1] == -1 marks a boundary edge (one adjacent element); interior
+                # edges get a placeholder id, which only that test reads
+                edges[i].elems[1] = -1 if eb is None or eb[i] else 0
             mesh.n_edges = len(p.edges)
             mesh.edges = C.cast(edges, C.POINTER(abi.bfm_edge_t))
             self.keep.append(edges)

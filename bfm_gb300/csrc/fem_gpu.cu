@@ -265,6 +265,44 @@ __global__ void k_dirichlet_mark(int N, int ci, int shift, double value, const u
 	last_ci[d] = ci;
 }
 
+// Dirichlet normal/tangent condition (system.c:388-425): for a flagged node,
+// the half-sums over its boundary edges (one adjacent element) of the unit
+// vector from the other end to the node, (tx, ty), in edge order; then both
+// DOFs are constrained, to value * (tx, ty) (tangent) or value * (-ty, tx)
+// (normal), with the same first/last bookkeeping as the X/Y conditions.
+// The arithmetic is the reference's, correctly rounded.
+__global__ void k_dirichlet_nt_mark(int N, int ci, int tangent, double value, const uint8_t* __restrict__ mask,
+                                    const int* __restrict__ eptr, const int* __restrict__ elist, const int* __restrict__ edges,
+                                    const uint8_t* __restrict__ eboundary, const double* __restrict__ coords,
+                                    int* __restrict__ last_ci, double* __restrict__ first, double* __restrict__ last) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N || !mask[i]) return;
+	double tx = 0.0, ty = 0.0;
+	int prev = -1;
+	int const k0 = eptr ? eptr[i] : 0, k1 = eptr ? eptr[i + 1] : 0;  // no edges: (tx, ty) = 0
+	for (int k = k0; k < k1; k++) {
+		int const e = elist[k];
+		if (e == prev) continue;  // an edge from the node to itself is listed twice, counted once
+		prev = e;
+		if (!eboundary[e]) continue;
+		int const n1 = edges[2 * e], n2 = edges[2 * e + 1];
+		int const other = n1 == i ? n2 : n1;
+		double const dx = xs(coords[2l * i], coords[2l * other]);
+		double const dy = xs(coords[2l * i + 1], coords[2l * other + 1]);
+		double const length = __dsqrt_rn(xa(xm(dx, dx), xm(dy, dy)));
+		tx = xa(tx, xd(xd(dx, length), 2.0));
+		ty = xa(ty, xd(xd(dy, length), 2.0));
+	}
+	double const v0 = xm(value, tangent ? tx : -ty), v1 = xm(value, tangent ? ty : tx);
+	for (int c = 0; c < 2; c++) {
+		int const d = 2 * i + c;
+		double const v = c ? v1 : v0;
+		if (last_ci[d] < 0) first[d] = v;
+		last[d] = v;
+		last_ci[d] = ci;
+	}
+}
+
 // ------------------------------------------------------------------ assembly
 
 struct AsmArgs {
@@ -920,8 +958,27 @@ __global__ void k_neumann(NeuArgs a) {
 	double add0 = 0, add1 = 0;
 	for (int ci = 0; ci < a.n_conds; ci++) {
 		int const kd = a.kinds[ci];
-		if (kd != BFM_CONDITION_KIND_NEUMANN_X && kd != BFM_CONDITION_KIND_NEUMANN_Y) continue;
 		const uint8_t* m = a.masks + (long) ci * a.N;
+		if (kd == BFM_CONDITION_KIND_NEUMANN_NORMAL || kd == BFM_CONDITION_KIND_NEUMANN_TANGENT) {
+			// system.c:500-522: each end of a flagged edge gets
+			// 0.5 value (dx, dy) (tangent) or 0.5 value (-dy, dx) (normal),
+			// (dx, dy) = first end - second end (the length cancels)
+			if (!m[r]) continue;
+			bool const tangent = kd == BFM_CONDITION_KIND_NEUMANN_TANGENT;
+			bool const on0 = a.last_ci[2 * r] <= ci, on1 = a.last_ci[2 * r + 1] <= ci;
+			for (int k = s; k < t; k++) {
+				int const ed = a.elist[k];
+				int const n1 = a.edges[2 * ed], n2 = a.edges[2 * ed + 1];
+				if (!m[n1] || !m[n2]) continue;
+				double const dx = xs(a.coords[2l * n1], a.coords[2l * n2]);
+				double const dy = xs(a.coords[2l * n1 + 1], a.coords[2l * n2 + 1]);
+				double const hv = xm(0.5, a.values[ci]);
+				if (on0) add0 = xa(add0, xm(hv, tangent ? dx : -dy));
+				if (on1) add1 = xa(add1, xm(hv, tangent ? dy : dx));
+			}
+			continue;
+		}
+		if (kd != BFM_CONDITION_KIND_NEUMANN_X && kd != BFM_CONDITION_KIND_NEUMANN_Y) continue;
 		if (!m[r]) continue;
 		int const shift = kd == BFM_CONDITION_KIND_NEUMANN_X ? 0 : 1;
 		int const lc = a.last_ci[2 * r + shift];
@@ -1080,6 +1137,7 @@ struct bfm_gpu_problem {
 	uint8_t* masks;
 	int n_edges;
 	int* edges;
+	uint8_t* eboundary;  // per edge: 1 if it has one adjacent element (normal/tangent Dirichlet)
 
 	// pattern
 	int *cnt, *inc_ptr, *inc, *cand, *row_len, *row_ptr, *cols;
@@ -1600,7 +1658,7 @@ int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n
 	long const tiles = (N + SCAN_TILE) / SCAN_TILE + 1;
 	*out = P;
 	if (dalloc(&P->coords, 2 * N) || dalloc(&P->elems, inc_total) || dalloc(&P->masks, (long) (n_conds ? n_conds : 1) * N) ||
-	    dalloc(&P->edges, 2l * n_edges) || dalloc(&P->cnt, N + 1) || dalloc(&P->inc_ptr, N + 1) || dalloc(&P->inc, inc_total) ||
+	    dalloc(&P->edges, 2l * n_edges) || dalloc(&P->eboundary, n_edges) || dalloc(&P->cnt, N + 1) || dalloc(&P->inc_ptr, N + 1) || dalloc(&P->inc, inc_total) ||
 	    dalloc(&P->cand, inc_total * kind) || dalloc(&P->row_len, N + 1) || dalloc(&P->row_ptr, N + 1) ||
 	    dalloc(&P->cols, P->nb_cap) || dalloc(&P->ecnt, N + 1) || dalloc(&P->eptr, N + 1) || dalloc(&P->elist, 2l * n_edges) ||
 	    dalloc(&P->scan_sums, tiles) || dalloc(&P->scan_total, 1) || dalloc(&P->b, 2 * N) || dalloc(&P->last_ci, 2 * N) ||
@@ -1628,7 +1686,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (!P) return 0;
 	if (P->stream) cudaStreamSynchronize(P->stream);
 	if (P->graph) cudaGraphExecDestroy(P->graph);
-	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->cnt, P->inc_ptr, P->inc, P->cand,
+	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->eboundary, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
 	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->mat32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
@@ -1724,9 +1782,8 @@ int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int*
 	if (n_edges > P->max_edges || n_edges < 0) return fail("more edges than the problem was created for");
 	for (int c = 0; c < n_conds; c++) {
 		int const k = kinds[c];
-		if (k != BFM_CONDITION_KIND_DIRICHLET_X && k != BFM_CONDITION_KIND_DIRICHLET_Y && k != BFM_CONDITION_KIND_NEUMANN_X &&
-		    k != BFM_CONDITION_KIND_NEUMANN_Y)
-			return fail("condition kind %d is not supported on the GPU path (X/Y Dirichlet and Neumann only)", k);
+		if (k < BFM_CONDITION_KIND_DIRICHLET_X || k > BFM_CONDITION_KIND_DIRICHLET_TANGENT)
+			return fail("unknown condition kind %d", k);
 		P->kinds[c] = k;
 		P->values[c] = values[c];
 	}
@@ -1734,6 +1791,15 @@ int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int*
 	P->n_edges = n_edges;
 	if (n_conds) CK(cudaMemcpyAsync(P->masks, masks, (long) n_conds * P->N, kind_of(where), P->stream));
 	if (n_edges) CK(cudaMemcpyAsync(P->edges, edges, 2l * n_edges * sizeof(int), kind_of(where), P->stream));
+	// every edge counts as a boundary edge until bfm_gpu_problem_set_edge_boundary says otherwise
+	if (n_edges) CK(cudaMemsetAsync(P->eboundary, 1, n_edges, P->stream));
+	P->assembled = false;
+	return 0;
+}
+
+int bfm_gpu_problem_set_edge_boundary(bfm_gpu_problem_t* P, const uint8_t* boundary, int where) {
+	g_err[0] = 0;
+	if (P->n_edges) CK(cudaMemcpyAsync(P->eboundary, boundary, P->n_edges, kind_of(where), P->stream));
 	P->assembled = false;
 	return 0;
 }
@@ -1879,13 +1945,23 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	k_rows_count<<<blocks_for(N), TPB, 0, st>>>(P->N, P->kind, P->elems, P->inc_ptr, P->inc, P->cand, P->row_len, P->err);
 	if (scan(P, P->row_len, P->row_ptr, P->N)) return -1;
 	k_rows_fill<<<blocks_for(N), TPB, 0, st>>>(P->N, P->kind, P->inc_ptr, P->cand, P->row_ptr, P->cols);
-	// 3. Dirichlet bookkeeping, conditions in order
+	// 3. Dirichlet bookkeeping, conditions in order (node -> edge incidence
+	// first when edges are needed: normal/tangent conditions, Neumann loads)
+	bool need_edges = false;
+	for (int c = 0; c < P->n_conds; c++) need_edges |= P->kinds[c] >= BFM_CONDITION_KIND_NEUMANN_X;
+	need_edges = need_edges && P->n_edges > 0;
+	if (need_edges && incidence(P, P->edges, P->n_edges, 2, P->ecnt, P->eptr, P->elist, 2 * MAXV, ERR_EDGE_VALENCE)) return -1;
 	CK(cudaMemsetAsync(P->last_ci, 0xff, 2 * N * sizeof(int), st));
 	for (int c = 0; c < P->n_conds; c++) {
 		int const k = P->kinds[c];
 		if (k == BFM_CONDITION_KIND_DIRICHLET_X || k == BFM_CONDITION_KIND_DIRICHLET_Y)
 			k_dirichlet_mark<<<blocks_for(N), TPB, 0, st>>>(P->N, c, k == BFM_CONDITION_KIND_DIRICHLET_X ? 0 : 1, P->values[c],
 			                                                 P->masks + (long) c * N, P->last_ci, P->first, P->last);
+		if (k == BFM_CONDITION_KIND_DIRICHLET_NORMAL || k == BFM_CONDITION_KIND_DIRICHLET_TANGENT)
+			k_dirichlet_nt_mark<<<blocks_for(N), TPB, 0, st>>>(P->N, c, k == BFM_CONDITION_KIND_DIRICHLET_TANGENT, P->values[c],
+			                                                    P->masks + (long) c * N, need_edges ? P->eptr : nullptr,
+			                                                    P->elist, P->edges, P->eboundary, P->coords, P->last_ci,
+			                                                    P->first, P->last);
 	}
 	// 4. element loop + elimination + preconditioner diagonal
 	AsmArgs a;
@@ -1945,12 +2021,11 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		a.skip_upto = rmax;
 		k_assemble<false><<<blocks_for(N, 128), 128, 0, st>>>(a);
 	}
-	// 5. Neumann loads
+	// 5. Neumann loads (X/Y, normal/tangent)
 	bool has_neu = false;
 	for (int c = 0; c < P->n_conds; c++)
-		has_neu |= P->kinds[c] == BFM_CONDITION_KIND_NEUMANN_X || P->kinds[c] == BFM_CONDITION_KIND_NEUMANN_Y;
+		has_neu |= P->kinds[c] >= BFM_CONDITION_KIND_NEUMANN_X && P->kinds[c] <= BFM_CONDITION_KIND_NEUMANN_TANGENT;
 	if (has_neu && P->n_edges) {
-		if (incidence(P, P->edges, P->n_edges, 2, P->ecnt, P->eptr, P->elist, 2 * MAXV, ERR_EDGE_VALENCE)) return -1;
 		NeuArgs na;
 		memset(&na, 0, sizeof na);
 		na.N = P->N;

@@ -164,12 +164,14 @@ typedef struct {
 	uint8_t* masks;
 	int n_edges;
 	int32_t* edges;
+	uint8_t* eboundary;
 } gathered_t;
 
 static void release(gathered_t* g) {
 	free(g->elems);
 	free(g->masks);
 	free(g->edges);
+	free(g->eboundary);
 	for (int i = 0; i < 8; i++) free(g->fields[i]);
 }
 
@@ -240,10 +242,9 @@ static int gather(bfm_state_t* st, bfm_sim_t* sim, bfm_instance_t* inst, gathere
 	for (int c = 0; c < g->nc; c++) {
 		bfm_condition_t* const C = inst->conditions[c];
 		int const k = C->kind;
-		if (k != BFM_CONDITION_KIND_DIRICHLET_X && k != BFM_CONDITION_KIND_DIRICHLET_Y && k != BFM_CONDITION_KIND_NEUMANN_X &&
-		    k != BFM_CONDITION_KIND_NEUMANN_Y)
-			return REPORT(st, "condition kind %d (normal/tangent) is not implemented on the GPU path", k);
-		need_edges |= k == BFM_CONDITION_KIND_NEUMANN_X || k == BFM_CONDITION_KIND_NEUMANN_Y;
+		if (k < BFM_CONDITION_KIND_DIRICHLET_X || k > BFM_CONDITION_KIND_DIRICHLET_TANGENT)
+			return REPORT(st, "unknown condition kind %d", k);
+		need_edges |= k != BFM_CONDITION_KIND_DIRICHLET_X && k != BFM_CONDITION_KIND_DIRICHLET_Y;
 		g->kinds[c] = k;
 		g->values[c] = C->value;
 		for (size_t i = 0; i < N; i++) g->masks[(size_t) c * N + i] = C->nodes[i] ? 1 : 0;
@@ -252,13 +253,16 @@ static int gather(bfm_state_t* st, bfm_sim_t* sim, bfm_instance_t* inst, gathere
 		if (mesh->n_edges > INT_MAX / 2) return REPORT(st, "too many edges");
 		g->n_edges = (int) mesh->n_edges;
 		g->edges = malloc(2 * mesh->n_edges * sizeof *g->edges + 1);
-		if (!g->edges) return REPORT(st, "out of host memory");
+		g->eboundary = malloc(mesh->n_edges + 1);
+		if (!g->edges || !g->eboundary) return REPORT(st, "out of host memory");
 		for (size_t e = 0; e < mesh->n_edges; e++) {
 			for (int k = 0; k < 2; k++) {
 				size_t const nd = mesh->edges[e].nodes[k];
 				if (nd >= N) return REPORT(st, "edge %zu refers to node %zu of %zu", e, nd, N);
 				g->edges[2 * e + k] = (int32_t) nd;
 			}
+			/* the normal/tangent Dirichlet condition sums over edges with one element (system.c:396) */
+			g->eboundary[e] = mesh->edges[e].elems[1] == -1;
 		}
 	}
 	return 0;
@@ -284,6 +288,7 @@ static bfm_gpu_problem_t* upload_and_assemble(bfm_state_t* st, bfm_sim_t* sim, b
 	ok = ok && bfm_gpu_problem_set_rule(P, g.nq, g.weights, g.phi, g.dxi, g.deta) == 0;
 	ok = ok && bfm_gpu_problem_set_forces(P, g.nf, g.fval, fields, BFM_GPU_HOST) == 0;
 	ok = ok && bfm_gpu_problem_set_conditions(P, g.nc, g.kinds, g.values, g.masks, g.n_edges, g.edges, BFM_GPU_HOST) == 0;
+	if (g.n_edges) ok = ok && bfm_gpu_problem_set_edge_boundary(P, g.eboundary, BFM_GPU_HOST) == 0;
 	(void) precond;
 	ok = ok && bfm_gpu_problem_assemble(P, precision) == 0;
 	release(&g);

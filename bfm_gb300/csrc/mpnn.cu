@@ -272,12 +272,12 @@ __global__ void k_agg(int N, const int* __restrict__ row_ptr, const int* __restr
 			s[2 * q + 1] += __uint_as_float(u[q] & 0xFFFF0000u);
 		}
 	}
-	float const inv = 1.f / (float) (r1 - r0);
+	float const d = (float) (r1 - r0);  // a correctly rounded quotient, as the mean is defined
 	uint4 o;
-	o.x = pack2(__float2bfloat16(s[0] * inv), __float2bfloat16(s[1] * inv));
-	o.y = pack2(__float2bfloat16(s[2] * inv), __float2bfloat16(s[3] * inv));
-	o.z = pack2(__float2bfloat16(s[4] * inv), __float2bfloat16(s[5] * inv));
-	o.w = pack2(__float2bfloat16(s[6] * inv), __float2bfloat16(s[7] * inv));
+	o.x = pack2(__float2bfloat16(s[0] / d), __float2bfloat16(s[1] / d));
+	o.y = pack2(__float2bfloat16(s[2] / d), __float2bfloat16(s[3] / d));
+	o.z = pack2(__float2bfloat16(s[4] / d), __float2bfloat16(s[5] / d));
+	o.w = pack2(__float2bfloat16(s[6] / d), __float2bfloat16(s[7] / d));
 	reinterpret_cast<uint4*>(m + (long) i * HID)[c] = o;
 }
 

@@ -67,6 +67,8 @@ class DeviceProblem:
         masks = a(np.stack([c[2] for c in p.conds]).astype(np.uint8), np.uint8)
         edges = a(p.edges, np.int32) if p.edges is not None else None
         ok = ok and L.bfm_gpu_problem_set_conditions(P, len(p.conds), kinds, vals, masks, n_edges, edges, 0) == 0
+        if n_edges and p.edge_boundary is not None:
+            ok = ok and L.bfm_gpu_problem_set_edge_boundary(P, a(p.edge_boundary, np.uint8), 0) == 0
         if p.edge_loads is not None:
             le, ll = p.edge_loads
             ok = ok and L.bfm_gpu_problem_set_edge_loads(P, len(le), a(le, np.int32), a(ll, np.float64), 0) == 0

@@ -33,7 +33,8 @@ class Problem:
     elem_nu: np.ndarray | None = None
     forces: list = field(default_factory=list)      # [(fx, fy)] body accelerations
     conds: list = field(default_factory=list)       # [(kind, value, mask[N] bool)]
-    edges: np.ndarray | None = None                 # (M, 2) int64 boundary edges
+    edges: np.ndarray | None = None                 # (M, 2) int64 edges (boundary edges unless edge_boundary says)
+    edge_boundary: np.ndarray | None = None         # (M,) bool: the edge has one adjacent element (None: all)
     edge_loads: tuple | None = None                 # (edges (M, 2), tractions (M, 2)): per-edge Neumann loads
 
     @property

@@ -207,6 +207,12 @@ int bfm_gpu_problem_set_edge_loads(bfm_gpu_problem_t* problem, int n_loads, cons
  * bfm_gpu_problem_solve_parts then solves every part with its own CG. */
 int bfm_gpu_problem_set_parts(bfm_gpu_problem_t* problem, int n_parts, const int32_t* node_offsets);
 
+/* Per edge of the last bfm_gpu_problem_set_conditions call: 1 if the edge has
+ * one adjacent element (a boundary edge), 0 otherwise.  The normal/tangent
+ * Dirichlet conditions sum over boundary edges only (reference system.c:396);
+ * without this call every edge counts as one. */
+int bfm_gpu_problem_set_edge_boundary(bfm_gpu_problem_t* problem, const uint8_t* boundary, int where);
+
 /* Enqueue the batched solve: one persistent cooperative kernel in which each
  * part runs mixed-precision Jacobi-PCG (FP32 operator and vectors, FP64
  * inner products and residual replacement) with its own scalars and stopping

@@ -26,7 +26,7 @@
 typedef int64_t i64;
 
 /* condition kinds, numbered as libbfm/src/bfm/condition.h:5-14 */
-enum { ORC_DIR_X = 0, ORC_DIR_Y = 1, ORC_NEU_X = 2, ORC_NEU_Y = 3 };
+enum { ORC_DIR_X = 0, ORC_DIR_Y = 1, ORC_NEU_X = 2, ORC_NEU_Y = 3, ORC_NEU_N = 4, ORC_NEU_T = 5, ORC_DIR_N = 6, ORC_DIR_T = 7 };
 
 typedef struct {
 	int kind;              /* nodes per element: 3 (P1 triangle) or 4 (Q1 quad) */
@@ -50,6 +50,7 @@ typedef struct {
 	const unsigned char* cond_nodes; /* [n_conds*n_nodes] node masks              */
 	i64 n_edges;
 	const i64* edges;      /* [n_edges*2] node pairs (libbfm/src/bfm/mesh.h:17-23) */
+	const unsigned char* edge_boundary; /* [n_edges] 1: one adjacent element (elems[1] == -1); NULL: all */
 } orc_problem_t;
 
 /* Gauss rule and shape tables, libbfm/src/rule.c:90-111 and shape.c:3-85. */
@@ -174,6 +175,44 @@ static void neumann(const orc_problem_t* P, int ci, double* bvec) {
 	}
 }
 
+/* Neumann normal/tangent edge loads, libbfm/src/system.c:500-522. */
+static void neumann_nt(const orc_problem_t* P, int ci, double* bvec) {
+	int const tangent = P->cond_kind[ci] == ORC_NEU_T;
+	double const value = P->cond_value[ci];
+	const unsigned char* mask = P->cond_nodes + (i64) ci * P->n_nodes;
+	for (i64 j = 0; j < P->n_edges; j++) {
+		i64 const n1 = P->edges[2 * j], n2 = P->edges[2 * j + 1];
+		if (!mask[n1] || !mask[n2]) continue;
+		double const dx = P->coords[n1 * 2 + 0] - P->coords[n2 * 2 + 0];
+		double const dy = P->coords[n1 * 2 + 1] - P->coords[n2 * 2 + 1];
+		bvec[n1 * 2 + 0] += 0.5 * value * (tangent ? dx : -dy);
+		bvec[n1 * 2 + 1] += 0.5 * value * (tangent ? dy : dx);
+		bvec[n2 * 2 + 0] += 0.5 * value * (tangent ? dx : -dy);
+		bvec[n2 * 2 + 1] += 0.5 * value * (tangent ? dy : dx);
+	}
+}
+
+/* The two values a Dirichlet normal/tangent condition prescribes at node i,
+ * libbfm/src/system.c:388-425: half-sums over the node's boundary edges of
+ * the unit vector from the other end, then value * (tx, ty) or (-ty, tx). */
+static void dirichlet_nt_values(const orc_problem_t* P, int ci, i64 i, double* v0, double* v1) {
+	double tx = 0, ty = 0;
+	for (i64 j = 0; j < P->n_edges; j++) {
+		int const boundary = P->edge_boundary ? P->edge_boundary[j] : 1;
+		i64 n2 = -1;
+		if (P->edges[2 * j] == i && boundary) n2 = P->edges[2 * j + 1];
+		else if (P->edges[2 * j + 1] == i && boundary) n2 = P->edges[2 * j];
+		if (n2 < 0) continue;
+		double const length = sqrt(pow(P->coords[i * 2 + 0] - P->coords[n2 * 2 + 0], 2) +
+		                           pow(P->coords[i * 2 + 1] - P->coords[n2 * 2 + 1], 2));
+		tx += (P->coords[i * 2 + 0] - P->coords[n2 * 2 + 0]) / length / 2;
+		ty += (P->coords[i * 2 + 1] - P->coords[n2 * 2 + 1]) / length / 2;
+	}
+	int const tangent = P->cond_kind[ci] == ORC_DIR_T;
+	*v0 = P->cond_value[ci] * (tangent ? tx : -ty);
+	*v1 = P->cond_value[ci] * (tangent ? ty : tx);
+}
+
 /* ---------------------------------------------------------------- dense */
 
 typedef struct { double* K; i64 n; } dense_ctx_t;
@@ -212,8 +251,21 @@ int orc_assemble_dense(const orc_problem_t* P, double* K, double* bvec) {
 		else if (k == ORC_NEU_X || k == ORC_NEU_Y) {
 			neumann(P, ci, bvec);
 		}
+		else if (k == ORC_NEU_N || k == ORC_NEU_T) {
+			neumann_nt(P, ci, bvec);
+		}
+		else if (k == ORC_DIR_N || k == ORC_DIR_T) {
+			const unsigned char* mask = P->cond_nodes + (i64) ci * P->n_nodes;
+			for (i64 j = 0; j < P->n_nodes; j++) {
+				if (!mask[j]) continue;
+				double v0, v1;
+				dirichlet_nt_values(P, ci, j, &v0, &v1);
+				dense_constraint(K, bvec, n, 2 * j + 0, v0);
+				dense_constraint(K, bvec, n, 2 * j + 1, v1);
+			}
+		}
 		else {
-			return -1; /* normal/tangent conditions are not restated */
+			return -1;
 		}
 	}
 	return 0;
@@ -525,7 +577,20 @@ i64 orc_assemble_csr(const orc_problem_t* P, i64* row_ptr, i64* cols, double* va
 				last_ci[d] = ci;
 			}
 		}
-		else if (k != ORC_NEU_X && k != ORC_NEU_Y) {
+		else if (k == ORC_DIR_N || k == ORC_DIR_T) {
+			for (i64 j = 0; j < N; j++) {
+				if (!mask[j]) continue;
+				double v[2];
+				dirichlet_nt_values(P, ci, j, &v[0], &v[1]);
+				for (int c = 0; c < 2; c++) {
+					i64 const d = 2 * j + c;
+					if (last_ci[d] < 0) first[d] = v[c];
+					last[d] = v[c];
+					last_ci[d] = ci;
+				}
+			}
+		}
+		else if (k < ORC_NEU_X || k > ORC_NEU_T) {
 			free(first); free(last); free(last_ci); free(nptr); free(ncols);
 			return -1;
 		}
@@ -548,9 +613,10 @@ i64 orc_assemble_csr(const orc_problem_t* P, i64* row_ptr, i64* cols, double* va
 	double* tmp = calloc(n, sizeof *tmp);
 	for (int ci = 0; ci < P->n_conds; ci++) {
 		int const k = P->cond_kind[ci];
-		if (k != ORC_NEU_X && k != ORC_NEU_Y) continue;
+		if (k < ORC_NEU_X || k > ORC_NEU_T) continue;
 		memset(tmp, 0, n * sizeof *tmp);
-		neumann(P, ci, tmp);
+		if (k == ORC_NEU_X || k == ORC_NEU_Y) neumann(P, ci, tmp);
+		else neumann_nt(P, ci, tmp);
 		for (i64 i = 0; i < n; i++)
 			if (tmp[i] != 0 && (last_ci[i] < 0 || last_ci[i] < ci)) bvec[i] += tmp[i];
 	}

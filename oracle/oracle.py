@@ -37,7 +37,7 @@ class orc_problem_t(C.Structure):
                 ("elem_E", _dp), ("elem_nu", _dp), ("n_points", C.c_int), ("weights", _dp), ("phi", _dp),
                 ("dxi", _dp), ("deta", _dp), ("n_forces", C.c_int), ("forces", _dp), ("n_conds", C.c_int),
                 ("cond_kind", C.POINTER(C.c_int)), ("cond_value", _dp), ("cond_nodes", C.POINTER(C.c_uint8)),
-                ("n_edges", C.c_int64), ("edges", _lp)]
+                ("n_edges", C.c_int64), ("edges", _lp), ("edge_boundary", C.POINTER(C.c_uint8))]
 
 
 def build(ref: bool = False) -> None:
@@ -111,6 +111,8 @@ class _Prob:
         if p.edges is not None:
             s.n_edges = len(p.edges)
             s.edges = self._a(p.edges, np.int64)
+            if getattr(p, "edge_boundary", None) is not None:
+                s.edge_boundary = self._a(np.asarray(p.edge_boundary, np.uint8), np.uint8, C.c_uint8)
         self.s = s
 
     def _a(self, arr, dtype=np.float64, ctype=None):

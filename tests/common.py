@@ -9,7 +9,7 @@ import numpy as np
 from bfm_gb300 import meshgen as M
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES = ["lepl8", "p1_64x16", "q1_24x8_jitter", "p1_12x6_conds", "p1_20x10_shuffled", "gear12"]
+CASES = ["lepl8", "p1_64x16", "q1_24x8_jitter", "p1_12x6_conds", "p1_20x10_shuffled", "gear12", "p1_16x8_nt"]
 
 
 def load(name: str):
@@ -20,7 +20,8 @@ def load(name: str):
     edges = d["edges"] if d["edges"].shape[0] else None
     p = M.Problem(name, int(d["kind"]), d["coords"], d["elems"], E=float(d["E"]), nu=float(d["nu"]),
                   rho=float(d["rho"]), stress=bool(d["stress"]), forces=[tuple(f) for f in d["forces"]],
-                  conds=conds, edges=edges)
+                  conds=conds, edges=edges,
+                  edge_boundary=d["edge_boundary"].astype(bool) if "edge_boundary" in d else None)
     return p, d
 
 

@@ -83,6 +83,8 @@ def save(name: str, p, h, extra: dict | None = None, system: bool = True):
              cond_nodes=np.packbits(np.stack([np.asarray(c[2], bool) for c in p.conds]), axis=1),
              edges=p.edges if p.edges is not None else np.zeros((0, 2), np.int64),
              effects=eff)
+    if p.edge_boundary is not None:
+        d["edge_boundary"] = np.asarray(p.edge_boundary, np.uint8)
     if system:
         K, b, perm = h.system(renumber=True)
         nz = np.nonzero(K)
@@ -95,6 +97,7 @@ def save(name: str, p, h, extra: dict | None = None, system: bool = True):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("BFM_REFERENCE", "/root/reference"))
+    ap.add_argument("--only", default=None, help="regenerate one fixture")
     args = ap.parse_args()
     os.environ["BFM_REFERENCE"] = args.reference
     from oracle import oracle as O
@@ -103,6 +106,11 @@ def main():
     R = O.ref_lib()
     assert R is not None, "reference sources not found"
     ref = Path(args.reference)
+
+    if args.only in (None, "p1_16x8_nt"):
+        normal_tangent_case(R, api, M)
+    if args.only is not None:
+        return
 
     # 1. the reference's own fixture: Q1 mesh, planar strain, gravity, two Dirichlet domains
     coords, edges, elems, kind, domains = parse_lepl1110(ref / "meshes" / "8.lepl1110")
@@ -173,6 +181,32 @@ def main():
     h = api.SimHandle.from_problem(R, p, elem_material=False)
     assert h.run() == 0
     save("gear12", p, h)
+
+
+def normal_tangent_case(R, api, M):
+    """Normal and tangent conditions (system.c:388-425, 500-522) mixed with
+    X/Y ones, in an order that exercises the first/last-value and
+    load-survival rules; the edge list holds interior edges too, which the
+    normal/tangent Dirichlet sums must skip (one adjacent element only)."""
+    nx, ny = 16, 8
+    coords, el = M.grid(nx, ny, 3)
+    w = nx + 1
+    bnd = M.boundary_edges(nx, ny)
+    inner = np.array([(4 * w + i, 4 * w + i + 1) for i in range(nx)], np.int64)
+    edges = np.concatenate([bnd, inner])
+    eb = np.concatenate([np.ones(len(bnd), bool), np.zeros(len(inner), bool)])
+    x, y = coords[:, 0], coords[:, 1]
+    left, right = M.side_mask(coords, "left"), M.side_mask(coords, "right")
+    bottom, top = M.side_mask(coords, "bottom"), M.side_mask(coords, "top")
+    DN, DT, NN, NT = 6, 7, 4, 5
+    conds = [(DN, 3e-5, x < 0.6), (M.DIRICHLET_X, 0.0, left), (M.DIRICHLET_Y, 0.0, left),
+             (NT, 2e5, top), (NN, -3e5, right), (DT, 5e-5, bottom & (x > 3.0)), (NN, 1e5, bottom),
+             (DN, 2e-5, right & (y > 0.8))]
+    p = M.Problem("p1_16x8_nt", 3, coords, el, stress=True, forces=[(0.0, -9.81)], conds=conds, edges=edges,
+                  edge_boundary=eb)
+    h = api.SimHandle.from_problem(R, p, elem_material=False)
+    assert h.run() == 0
+    save("p1_16x8_nt", p, h)
 
 
 if __name__ == "__main__":
