@@ -41,7 +41,8 @@ class SimHandle:
 
     @classmethod
     def from_problem(cls, lib: C.CDLL, problem, elem_material: bool = True) -> "SimHandle":
-        h = cls(lib, abi.SIM_PLANAR_STRESS if problem.stress else abi.SIM_PLANAR_STRAIN)
+        st = int(problem.stress)
+        h = cls(lib, abi.SIM_AXISYMMETRIC_STRAIN if st >= 2 else abi.SIM_PLANAR_STRESS if st else abi.SIM_PLANAR_STRAIN)
         h.add_problem(problem, elem_material=elem_material)
         return h
 
@@ -119,11 +120,13 @@ class SimHandle:
         return (e.msg or b"").decode() if e.has else ""
 
     def system(self, i: int = 0, renumber: bool = False):
-        """Dense K, b from bfm_system_create_planar_* (and the RCM permutation)."""
+        """Dense K, b from bfm_system_create_{planar_*,axisymmetric_strain} (and
+        the RCM permutation)."""
         lib = self.lib
         s = abi.bfm_system_t()
-        create = lib.bfm_system_create_planar_stress if self.sim.kind == abi.SIM_PLANAR_STRESS \
-            else lib.bfm_system_create_planar_strain
+        create = {abi.SIM_PLANAR_STRESS: lib.bfm_system_create_planar_stress,
+                  abi.SIM_AXISYMMETRIC_STRAIN: lib.bfm_system_create_axisymmetric_strain}.get(
+                      self.sim.kind, lib.bfm_system_create_planar_strain)
         rc = create(C.byref(s), C.byref(self.instances[i]), self.sim.n_forces, self.sim.forces)
         assert rc == 0, self.error()
         n = s.n

@@ -70,11 +70,15 @@ __device__ __forceinline__ double xa(double a, double b) { return __dadd_rn(a, b
 __device__ __forceinline__ double xs(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double xd(double a, double b) { return __ddiv_rn(a, b); }
 
-// material constants, reference system.c:454-458 (same operation order)
+// material constants, reference system.c:454-458 (same operation order).
+// stress 0 plane strain, 1 plane stress, 2 axisymmetric (the plane-strain
+// constants), 3 axisymmetric with the constant a of system.c:241, which
+// multiplies by (1 - 2 nu) where it should divide
 __device__ __forceinline__ void material_abc(double E, double nu, int stress, double& a, double& b, double& c) {
-	if (!stress) {
+	if (stress != 1) {
 		double const den = xs(1.0, xm(2.0, nu));
 		a = xd(xd(xm(E, xs(1.0, nu)), xa(1.0, nu)), den);
+		if (stress == 3) a = xm(xd(xm(E, xs(1.0, nu)), xa(1.0, nu)), den);
 		b = xd(xd(xm(E, nu), xa(1.0, nu)), den);
 	}
 	else {
@@ -435,14 +439,16 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			material_abc(E, nu, a.stress, ea, eb, ec);
 		}
 		if constexpr (EXACT) {
+			bool const axi = a.stress >= 2;
 			for (int q = 0; q < a.rule.nq; q++) {
 				double const w = a.rule.w[q];
-				double dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
+				double dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0, rad = 0;
 				for (int j = 0; j < kind; j++) {
 					dx_dxsi = xa(dx_dxsi, xm(x[j], a.rule.dxi[q][j]));
 					dx_deta = xa(dx_deta, xm(x[j], a.rule.deta[q][j]));
 					dy_dxsi = xa(dy_dxsi, xm(y[j], a.rule.dxi[q][j]));
 					dy_deta = xa(dy_deta, xm(y[j], a.rule.deta[q][j]));
+					rad = xa(rad, xm(x[j], a.rule.phi[q][j]));
 				}
 				double const det = fabs(xs(xm(dx_dxsi, dy_deta), xm(dx_deta, dy_dxsi)));
 				double dx[4], dy[4];
@@ -458,10 +464,40 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 						fx = a.forces.field[f][2l * r];
 						fy = a.forces.field[f][2l * r + 1];
 					}
-					b0 = xa(b0, xm(xm(xm(dw, fx), a.rho), ph));
-					b1 = xa(b1, xm(xm(xm(dw, fy), a.rho), ph));
+					double bx = xm(xm(xm(dw, fx), a.rho), ph), by = xm(xm(xm(dw, fy), a.rho), ph);
+					if (axi) {  // system.c:321-322: weighted by the radius of the Gauss point
+						bx = xm(bx, rad);
+						by = xm(by, rad);
+					}
+					b0 = xa(b0, bx);
+					b1 = xa(b1, by);
 				}
 				double const xj = dx[jr], yj = dy[jr];
+				if (axi) {
+					// axisymmetric terms, system.c:334-337, the reference's
+					// operation order; (r, z) = (x, y) and the hoop strain u/r.
+					// The reference leaves the radius off the c dphi_dx dphi_dx
+					// term of f_22; stress 2 puts it back, stress 3 keeps it off.
+					double const pj = ph;
+					for (int k = 0; k < kind; k++) {
+						double const pk = a.rule.phi[q][k];
+						double const f11 = xa(xa(xa(xm(xm(xm(ea, xj), dx[k]), rad), xm(xm(xm(ec, yj), dy[k]), rad)),
+						                         xm(pj, xa(xm(eb, dx[k]), xd(xm(ea, pk), rad)))),
+						                      xm(xm(xj, eb), pk));
+						double const f12 = xa(xa(xm(xm(xm(eb, xj), dy[k]), rad), xm(xm(xm(ec, yj), dx[k]), rad)),
+						                      xm(xm(pj, eb), dy[k]));
+						double const f21 = xa(xa(xm(xm(xm(eb, yj), dx[k]), rad), xm(xm(xm(ec, xj), dy[k]), rad)),
+						                      xm(xm(yj, eb), pk));
+						double const cxx = xm(xm(ec, xj), dx[k]);
+						double const f22 = xa(xm(xm(xm(ea, yj), dy[k]), rad), a.stress == 2 ? xm(cxx, rad) : cxx);
+						int const s = slot[k];
+						acc[s][0] = xa(acc[s][0], xm(dw, f11));
+						acc[s][1] = xa(acc[s][1], xm(dw, f12));
+						acc[s][2] = xa(acc[s][2], xm(dw, f21));
+						acc[s][3] = xa(acc[s][3], xm(dw, f22));
+					}
+					continue;
+				}
 				for (int k = 0; k < kind; k++) {
 					double const f11 = xa(xm(xm(ea, xj), dx[k]), xm(xm(ec, yj), dy[k]));
 					double const f12 = xa(xm(xm(eb, xj), dy[k]), xm(xm(ec, yj), dx[k]));
@@ -938,7 +974,7 @@ __global__ void __launch_bounds__(128, 6) k_assemble32(AsmArgs a) {
 // then edge order (deterministic, no atomics).  A load on a constrained DOF
 // survives only when applied after that DOF's last Dirichlet condition.
 struct NeuArgs {
-	int N, n_conds;
+	int N, n_conds, stress;
 	int kinds[MAXC];
 	double values[MAXC];
 	const uint8_t* masks;
@@ -960,6 +996,7 @@ __global__ void k_neumann(NeuArgs a) {
 		int const kd = a.kinds[ci];
 		const uint8_t* m = a.masks + (long) ci * a.N;
 		if (kd == BFM_CONDITION_KIND_NEUMANN_NORMAL || kd == BFM_CONDITION_KIND_NEUMANN_TANGENT) {
+			if (a.stress >= 2) continue;  // the axisymmetric system (system.c:573-616) has no such loads
 			// system.c:500-522: each end of a flagged edge gets
 			// 0.5 value (dx, dy) (tangent) or 0.5 value (-dy, dx) (normal),
 			// (dx, dy) = first end - second end (the length cancels)
@@ -990,11 +1027,26 @@ __global__ void k_neumann(NeuArgs a) {
 			double const dx = a.coords[2l * n1] - a.coords[2l * n2];
 			double const dy = a.coords[2l * n1 + 1] - a.coords[2l * n2 + 1];
 			double const jac = sqrt(dx * dx + dy * dy) / 2;
+			double load = jac * a.values[ci];
+			if (a.stress == 3) {
+				// system.c:591-601: both ends get (r1 + r2) jac value, r1 and
+				// r2 as written there (from the x and y of one node each)
+				double const g0 = (1.0 - 1.0 / sqrt(3.0)) / 2, g1 = (1.0 + 1.0 / sqrt(3.0)) / 2;
+				double const r1 = a.coords[2l * n1] * g0 + a.coords[2l * n1 + 1] * g1;
+				double const r2 = a.coords[2l * n2] * g0 + a.coords[2l * n2 + 1] * g1;
+				load = (r1 + r2) * jac * a.values[ci];
+			}
+			else if (a.stress == 2) {
+				// consistent load: value jac times the integral over [-1, 1] of
+				// (this end's shape function) x (radius) = (2 r_this + r_other) / 3
+				double const rt = a.coords[2l * (n1 == r ? n1 : n2)], ro = a.coords[2l * (n1 == r ? n2 : n1)];
+				load = (2.0 * rt + ro) / 3.0 * jac * a.values[ci];
+			}
 			// an edge whose two ends are the same node adds twice, as in the reference
 			int const mult = (n1 == r) + (n2 == r);
 			for (int u = 0; u < mult; u++) {
-				if (shift == 0) add0 += jac * a.values[ci];
-				else add1 += jac * a.values[ci];
+				if (shift == 0) add0 += load;
+				else add1 += load;
 			}
 		}
 	}
@@ -1722,6 +1774,7 @@ int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* P, const double* coords, con
 int bfm_gpu_problem_set_material(bfm_gpu_problem_t* P, double E, double nu, double rho, int stress, const double* elem_E,
                                  const double* elem_nu, int where) {
 	g_err[0] = 0;
+	if (stress < 0 || stress > 3) return fail("element formulation %d is not one of 0..3", stress);
 	P->E = E;
 	P->nu = nu;
 	P->rho = rho;
@@ -1995,7 +2048,9 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.dinv32 = want32 && !dfp ? P->dinv32 : nullptr;
 	a.precond = P->precond;
 	a.err = P->err;
-	if (precision != BFM_GPU_MIXED) {
+	if (precision != BFM_GPU_MIXED || P->stress >= 2) {
+		// (the FP32 element integration is planar only: axisymmetric
+		// mixed-precision solves round the exact FP64 values)
 		k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
 		if (dfp) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32, P->precond != BFM_GPU_PC_JACOBI);
 	}
@@ -2030,6 +2085,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		memset(&na, 0, sizeof na);
 		na.N = P->N;
 		na.n_conds = P->n_conds;
+		na.stress = P->stress;
 		for (int c = 0; c < P->n_conds; c++) {
 			na.kinds[c] = P->kinds[c];
 			na.values[c] = P->values[c];
@@ -2044,6 +2100,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		k_neumann<<<blocks_for(N), TPB, 0, st>>>(na);
 	}
 	if (P->n_loads) {
+		if (P->stress >= 2) return fail("per-edge loads are planar only");
 		// the incidence helper counts into a buffer of N+1 ints and scans N entries
 		if (incidence(P, P->ledges, P->n_loads, 2, P->lcnt, P->lptr, P->llist, 1 << 30, 0)) return -1;
 		k_edge_loads<<<blocks_for(N), TPB, 0, st>>>(P->N, P->ledges, P->lloads, P->lptr, P->llist, P->coords, P->last_ci, P->b);

@@ -338,12 +338,22 @@ static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	return 0;
 }
 
+/* Element mode of the axisymmetric system: 2 (the plane-strain constant a,
+ * the radius on every stiffness term, consistent edge loads) unless
+ * BFM_GPU_AXISYM_REFERENCE=1 asks for 3, the reference's own formulas
+ * (system.c:241, 337, 591-601), which make K indefinite for usual nu. */
+static int axisym_mode(void) {
+	char const* e = getenv("BFM_GPU_AXISYM_REFERENCE");
+	return e && e[0] == '1' ? 3 : 2;
+}
+
 int bfm_sim_run(bfm_sim_t* sim) {
 	if (sim->kind == BFM_SIM_KIND_NONE) return 0;
-	if (sim->kind == BFM_SIM_KIND_AXISYMMETRIC_STRAIN)
-		return REPORT(sim->state, "axisymmetric simulations are not implemented on the GPU path");
-	if (sim->kind != BFM_SIM_KIND_PLANAR_STRAIN && sim->kind != BFM_SIM_KIND_PLANAR_STRESS) return -1;
-	int const stress = sim->kind == BFM_SIM_KIND_PLANAR_STRESS;
+	if (sim->kind != BFM_SIM_KIND_PLANAR_STRAIN && sim->kind != BFM_SIM_KIND_PLANAR_STRESS &&
+	    sim->kind != BFM_SIM_KIND_AXISYMMETRIC_STRAIN)
+		return -1;
+	int const stress = sim->kind == BFM_SIM_KIND_AXISYMMETRIC_STRAIN ? axisym_mode()
+	                                                                 : sim->kind == BFM_SIM_KIND_PLANAR_STRESS;
 	for (size_t i = 0; i < sim->n_instances; i++)
 		if (run_instance(sim, sim->instances[i], stress) < 0) return -1;
 	return 0;
@@ -438,8 +448,5 @@ int bfm_system_create_planar_stress(bfm_system_t* s, bfm_instance_t* inst, size_
 }
 
 int bfm_system_create_axisymmetric_strain(bfm_system_t* s, bfm_instance_t* inst, size_t n_forces, bfm_force_t** forces) {
-	(void) s;
-	(void) n_forces;
-	(void) forces;
-	return REPORT(inst->state, "axisymmetric systems are not implemented on the GPU path");
+	return create_planar(s, inst, n_forces, forces, axisym_mode());
 }

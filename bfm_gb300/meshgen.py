@@ -28,7 +28,7 @@ class Problem:
     E: float = STEEL["E"]
     nu: float = STEEL["nu"]
     rho: float = STEEL["rho"]
-    stress: bool = True            # plane stress (True) or plane strain
+    stress: int = 1  # 0 plane strain, 1 plane stress, 2 axisymmetric (x = radius), 3 axisymmetric with the reference's formulas
     elem_E: np.ndarray | None = None
     elem_nu: np.ndarray | None = None
     forces: list = field(default_factory=list)      # [(fx, fy)] body accelerations

@@ -126,8 +126,13 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* problem);
 /* coords[2*n_nodes] (x,y interleaved), elems[kind*n_elems] (int32). */
 int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* problem, const double* coords, const int32_t* elems, int where);
 
-/* Uniform material (E, nu, rho) and plane stress (1) or plane strain (0);
- * elem_E / elem_nu (n_elems each, may be NULL) override E / nu per element. */
+/* Uniform material (E, nu, rho) and the element formulation `stress`:
+ * plane strain (0), plane stress (1), axisymmetric with x the radius (2), or
+ * axisymmetric with the reference's formulas (3: libbfm/src/system.c:241,
+ * 337 and 591-601 as written, for bit-exact parity; K is then indefinite for
+ * usual nu and CG is not expected to converge).
+ * elem_E / elem_nu (n_elems each, may be NULL) override E / nu per element.
+ * Per-edge loads (bfm_gpu_problem_set_edge_loads) are planar only. */
 int bfm_gpu_problem_set_material(bfm_gpu_problem_t* problem, double E, double nu, double rho, int stress,
                                  const double* elem_E, const double* elem_nu, int where);
 

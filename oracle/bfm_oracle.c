@@ -30,7 +30,8 @@ enum { ORC_DIR_X = 0, ORC_DIR_Y = 1, ORC_NEU_X = 2, ORC_NEU_Y = 3, ORC_NEU_N = 4
 
 typedef struct {
 	int kind;              /* nodes per element: 3 (P1 triangle) or 4 (Q1 quad) */
-	int stress;            /* 1: plane stress, 0: plane strain                   */
+	int stress;            /* 1: plane stress, 0: plane strain, 2: axisymmetric,
+	                          3: axisymmetric with the reference's constant a     */
 	i64 n_nodes, n_elems;
 	const double* coords;  /* [n_nodes*2] interleaved x,y                        */
 	const i64* elems;      /* [n_elems*kind]                                     */
@@ -89,10 +90,14 @@ int orc_gauss_tables(int kind, double* weights, double* phi, double* dxi, double
 	return -1;
 }
 
-/* Material constants, libbfm/src/system.c:454-458. */
+/* Material constants, libbfm/src/system.c:454-458; axisymmetric ones,
+ * system.c:241-243 (mode 3 keeps the reference's a = E(1-nu)/(1+nu)*(1-2nu),
+ * mode 2 the divided form of plane strain). */
 static void material_abc(double E, double nu, int stress, double* a, double* b, double* c) {
-	*a = !stress ? E * (1 - nu) / (1 + nu) / (1 - 2 * nu) : E / (1 - nu * nu);
-	*b = !stress ? E * nu / (1 + nu) / (1 - 2 * nu) : E * nu / (1 - nu * nu);
+	int const strain = stress != 1;
+	*a = strain ? E * (1 - nu) / (1 + nu) / (1 - 2 * nu) : E / (1 - nu * nu);
+	if (stress == 3) *a = E * (1 - nu) / (1 + nu) * (1 - 2 * nu);
+	*b = strain ? E * nu / (1 + nu) / (1 - 2 * nu) : E * nu / (1 - nu * nu);
 	*c = E / (2 * (1 + nu));
 }
 
@@ -136,6 +141,34 @@ static void element_terms(const orc_problem_t* P, i64 e, double* bvec, orc_add_f
 			dx[j] = (dxi[j] * dy_deta - deta[j] * dy_dxsi) / det;
 			dy[j] = (deta[j] * dx_dxsi - dxi[j] * dx_deta) / det;
 		}
+		if (P->stress >= 2) {
+			/* axisymmetric element, libbfm/src/system.c:229-356 */
+			double rr = 0;
+			for (int j = 0; j < kind; j++) rr += x[j] * phi[j];
+			for (int j = 0; j < kind; j++) {
+				i64 const r = 2 * map[j];
+				for (int f = 0; f < P->n_forces; f++) {
+					bvec[r + 0] += det * w * P->forces[2 * f + 0] * P->rho * phi[j] * rr;
+					bvec[r + 1] += det * w * P->forces[2 * f + 1] * P->rho * phi[j] * rr;
+				}
+			}
+			for (int j = 0; j < kind; j++) {
+				i64 const r = 2 * map[j];
+				for (int k = 0; k < kind; k++) {
+					i64 const s = 2 * map[k];
+					double const f11 = a * dx[j] * dx[k] * rr + c * dy[j] * dy[k] * rr + phi[j] * (b * dx[k] + a * phi[k] / rr) + dx[j] * b * phi[k];
+					double const f12 = b * dx[j] * dy[k] * rr + c * dy[j] * dx[k] * rr + phi[j] * b * dy[k];
+					double const f21 = b * dy[j] * dx[k] * rr + c * dx[j] * dy[k] * rr + dy[j] * b * phi[k];
+					/* the reference leaves the radius off this c term; mode 2 puts it back */
+					double const f22 = a * dy[j] * dy[k] * rr + (P->stress == 2 ? c * dx[j] * dx[k] * rr : c * dx[j] * dx[k]);
+					add(ctx, r + 0, s + 0, det * w * f11);
+					add(ctx, r + 0, s + 1, det * w * f12);
+					add(ctx, r + 1, s + 0, det * w * f21);
+					add(ctx, r + 1, s + 1, det * w * f22);
+				}
+			}
+			continue;
+		}
 		for (int j = 0; j < kind; j++) {
 			i64 const r = 2 * map[j];
 			for (int f = 0; f < P->n_forces; f++) {
@@ -170,6 +203,23 @@ static void neumann(const orc_problem_t* P, int ci, double* bvec) {
 		double const c2 = pow(P->coords[n1 * 2 + 0] - P->coords[n2 * 2 + 0], 2) +
 		                  pow(P->coords[n1 * 2 + 1] - P->coords[n2 * 2 + 1], 2);
 		double const jac = sqrt(c2) / 2;
+		if (P->stress == 2) {
+			/* consistent axisymmetric load: value jac times the integral over
+			 * [-1, 1] of (shape function) x (radius) = (2 r_this + r_other) / 3 */
+			double const x1 = P->coords[n1 * 2 + 0], x2 = P->coords[n2 * 2 + 0];
+			bvec[n1 * 2 + shift] += (2.0 * x1 + x2) / 3.0 * jac * P->cond_value[ci];
+			bvec[n2 * 2 + shift] += (2.0 * x2 + x1) / 3.0 * jac * P->cond_value[ci];
+			continue;
+		}
+		if (P->stress == 3) {
+			/* axisymmetric loads, libbfm/src/system.c:583-612 (radius factor as written there) */
+			double const r1 = P->coords[n1 * 2 + 0] * (1 - 1 / sqrt(3)) / 2 + P->coords[n1 * 2 + 1] * (1 + 1 / sqrt(3)) / 2;
+			double const r2 = P->coords[n2 * 2 + 0] * (1 - 1 / sqrt(3)) / 2 + P->coords[n2 * 2 + 1] * (1 + 1 / sqrt(3)) / 2;
+			double const fac = r1 + r2;
+			bvec[n1 * 2 + shift] += fac * jac * P->cond_value[ci];
+			bvec[n2 * 2 + shift] += fac * jac * P->cond_value[ci];
+			continue;
+		}
 		bvec[n1 * 2 + shift] += jac * P->cond_value[ci];
 		bvec[n2 * 2 + shift] += jac * P->cond_value[ci];
 	}
@@ -252,7 +302,7 @@ int orc_assemble_dense(const orc_problem_t* P, double* K, double* bvec) {
 			neumann(P, ci, bvec);
 		}
 		else if (k == ORC_NEU_N || k == ORC_NEU_T) {
-			neumann_nt(P, ci, bvec);
+			if (P->stress < 2) neumann_nt(P, ci, bvec);  /* the axisymmetric system skips them */
 		}
 		else if (k == ORC_DIR_N || k == ORC_DIR_T) {
 			const unsigned char* mask = P->cond_nodes + (i64) ci * P->n_nodes;
@@ -616,7 +666,7 @@ i64 orc_assemble_csr(const orc_problem_t* P, i64* row_ptr, i64* cols, double* va
 		if (k < ORC_NEU_X || k > ORC_NEU_T) continue;
 		memset(tmp, 0, n * sizeof *tmp);
 		if (k == ORC_NEU_X || k == ORC_NEU_Y) neumann(P, ci, tmp);
-		else neumann_nt(P, ci, tmp);
+		else if (P->stress < 2) neumann_nt(P, ci, tmp);
 		for (i64 i = 0; i < n; i++)
 			if (tmp[i] != 0 && (last_ci[i] < 0 || last_ci[i] < ci)) bvec[i] += tmp[i];
 	}

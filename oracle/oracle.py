@@ -88,7 +88,7 @@ class _Prob:
     def __init__(self, p):
         self.keep = []
         s = orc_problem_t()
-        s.kind, s.stress = p.kind, int(bool(p.stress))
+        s.kind, s.stress = p.kind, int(p.stress)
         s.n_nodes, s.n_elems = p.n_nodes, p.n_elems
         s.coords = self._a(p.coords, np.float64)
         s.elems = self._a(p.elems, np.int64)

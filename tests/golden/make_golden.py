@@ -109,6 +109,8 @@ def main():
 
     if args.only in (None, "p1_16x8_nt"):
         normal_tangent_case(R, api, M)
+    if args.only in (None, "axi"):
+        axisymmetric_cases(R, api, M)
     if args.only is not None:
         return
 
@@ -207,6 +209,28 @@ def normal_tangent_case(R, api, M):
     h = api.SimHandle.from_problem(R, p, elem_material=False)
     assert h.run() == 0
     save("p1_16x8_nt", p, h)
+
+
+def axisymmetric_cases(R, api, M):
+    """Axisymmetric systems (system.c:229-356, 539-622) with x the radius:
+    an annular section r in [1, 4], z in [0, 2], P1 and Q1, body force,
+    Neumann X/Y loads, a normal load (which that system skips) and Dirichlet
+    conditions in interleaved order.  stress=3 marks the reference's own
+    formulas; its band solve of the resulting (indefinite) K is kept too."""
+    for name, kind, nx, ny in (("axi_p1_12x8", 3, 12, 8), ("axi_q1_10x6", 4, 10, 6)):
+        grid, el = M.grid(nx, ny, kind)   # [0, 4] x [0, 1]
+        left, right = M.side_mask(grid, "left"), M.side_mask(grid, "right")
+        bottom, top = M.side_mask(grid, "bottom"), M.side_mask(grid, "top")
+        coords = np.stack([1.0 + grid[:, 0] * 0.75, grid[:, 1] * 2.0], axis=1)
+        y = coords[:, 1]
+        NN = 4  # Neumann normal
+        conds = [(M.NEUMANN_X, 2e5, left), (M.DIRICHLET_Y, 0.0, bottom), (M.NEUMANN_Y, -1e5, top),
+                 (NN, 1e5, right), (M.DIRICHLET_X, 1e-5, right & (y < 0.5)), (M.NEUMANN_X, -5e4, right)]
+        p = M.Problem(name, kind, coords, el, stress=3, forces=[(0.0, -9.81)], conds=conds,
+                      edges=M.boundary_edges(nx, ny))
+        h = api.SimHandle.from_problem(R, p, elem_material=False)
+        assert h.run() == 0
+        save(name, p, h)
 
 
 if __name__ == "__main__":
