@@ -44,7 +44,8 @@ RTOL = 1e-8
 METHODS = {"fp64": ("FP64", "PC_JACOBI"), "fp64_df": ("FP64_DF", "PC_JACOBI"),
            "mixed_exact": ("MIXED_EXACT", "PC_JACOBI"), "mixed": ("MIXED", "PC_JACOBI"),
            "learned_fp64": ("FP64", "PC_LEARNED"), "learned_df": ("FP64_DF", "PC_LEARNED"),
-           "learned_mixed": ("MIXED", "PC_LEARNED")}
+           "learned_mixed": ("MIXED", "PC_LEARNED"), "ssor_fp64": ("FP64", "PC_SSOR"),
+           "ssor_df": ("FP64_DF", "PC_SSOR"), "learned_ssor_df": ("FP64_DF", "PC_LEARNED_SSOR")}
 # FP64 residual-replacement threshold per precision (the recurrence residual
 # must drop by this factor between replacements), from a sweep on the
 # 2048x512 perforated plate: FP64 is insensitive, the FP32-pipe paths converge
@@ -202,11 +203,11 @@ def run_gpu(args, rank: int, world: int):
         net = learned.Network(path=learned.WEIGHTS)
         net.use()
     if args.method == "best":
-        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed"] + (["learned_fp64", "learned_df", "learned_mixed"]
-                                                                 if net else [])
+        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed", "ssor_fp64", "ssor_df"] + (
+            ["learned_fp64", "learned_df", "learned_mixed", "learned_ssor_df"] if net else [])
     else:
-        chosen = [args.method]
-        if methods[args.method][1] == bfm_gb300.PC_LEARNED and net is None:
+        chosen = args.method.split(",")
+        if any(methods[m][1] in (bfm_gb300.PC_LEARNED, bfm_gb300.PC_LEARNED_SSOR) for m in chosen) and net is None:
             raise SystemExit(f"{learned.WEIGHTS} is missing: train it with python -m bfm_gb300.learned")
     results = {}
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
@@ -242,10 +243,15 @@ def run_gpu(args, rank: int, world: int):
         assert lib.bfm_gpu_problem_time_kernels(P, 50, C.byref(t_spmv), C.byref(t_upd)) == 0
         shape = C.c_int()
         lib.bfm_gpu_problem_shape(P, C.byref(shape))
+        ncol = C.c_int(0)
+        lib.bfm_gpu_problem_ordering(P, None, None, C.byref(ncol))
+        t_pc, persist = C.c_double(0.0), C.c_int(0)
+        if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR):
+            assert lib.bfm_gpu_problem_time_precond(P, 20, C.byref(t_pc), C.byref(persist)) == 0, bfm_gb300.last_error()
         results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual, repl=s.replacements,
                           ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks, fallback=s.fallback,
                           ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, pc=pc, x=x,
-                          shape=shape.value)
+                          shape=shape.value, ncol=ncol.value, ms_precond=t_pc.value, persistent=persist.value)
     lib.bfm_gpu_problem_destroy(P)
     # displacement error of every method against the FP64 solution (the FP64
     # direct oracle does not fit the host at this size; the FP64 PCG solution
@@ -330,6 +336,17 @@ def profile(args):
     t_spmv, t_upd = C.c_double(), C.c_double()
     assert lib.bfm_gpu_problem_time_kernels(P, args.reps, C.byref(t_spmv), C.byref(t_upd)) == 0
     ms_net = None
+    ms_pc, ncol, persist = None, C.c_int(0), C.c_int(0)
+    pc = getattr(bfm_gb300, METHODS.get(args.method, ("", "PC_JACOBI"))[1])
+    if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR):
+        # two iterations form the colour order and the sweep graph; then the
+        # sweeps alone, `reps` standalone applications
+        o = bfm_gb300.default_opts(precision=prec, precond=bfm_gb300.PC_SSOR, max_iters=2)
+        assert lib.bfm_gpu_problem_solve(P, C.byref(o)) == 0, bfm_gb300.last_error()
+        t = C.c_double()
+        assert lib.bfm_gpu_problem_time_precond(P, args.reps, C.byref(t), C.byref(persist)) == 0, bfm_gb300.last_error()
+        lib.bfm_gpu_problem_ordering(P, None, None, C.byref(ncol))
+        ms_pc = t.value
     if METHODS.get(args.method, ("", ""))[1] == "PC_LEARNED":
         # the network's inference (features, 4 dense layers on the tensor cores, 3
         # aggregations, head), timed on the problem's stream with CUDA events
@@ -353,7 +370,8 @@ def profile(args):
     return {"workload": p.name, "method": args.method, "lanes_per_row": lpr.value, "n_blocks": s.n_blocks,
             "ms_assemble": s.ms_assemble,
             "spmv_ms": t_spmv.value, "update_ms": t_upd.value, "spmv_algorithmic_bytes": nbytes,
-            "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9, "network_forward_ms": ms_net}
+            "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9, "network_forward_ms": ms_net,
+            "precond_ms": ms_pc, "colours": ncol.value, "persistent_sweeps": persist.value}
 
 
 def run_reference(args, rank: int, world: int):
@@ -370,7 +388,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="perforated")
-    ap.add_argument("--method", default="best", choices=list(METHODS) + ["best"])
+    ap.add_argument("--method", default="best",
+                    help="best (all methods, fastest reported), or a comma-separated list of: " + ", ".join(METHODS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="assemble once and launch the two CG kernels --reps times each, standalone "
@@ -421,7 +440,10 @@ def main():
     # assembly (pattern, Dirichlet marks, element loop, loads: about 24 kernels),
     # solve init + 2 kernels per iteration + replacement kernels, finish;
     # the learned preconditioner adds its 12 inference kernels per solve
-    launches_per_step = 24 + 1 + 2 * r["iters"] + 2 * r["repl"] + 2 + (12 if r["pc"] == 2 else 0)
+    launches_per_step = 24 + 1 + 2 * r["iters"] + 2 * r["repl"] + 2 + (12 if r["pc"] in (2, 4) else 0)
+    if r["pc"] in (3, 4):
+        # the SSOR sweeps: 2 nc - 1 phases after the init, every update and every replacement
+        launches_per_step += (2 * r["ncol"] - 1) * (r["iters"] + r["repl"] + 1) + 3
     value = r["ms"] / world
     line = {
         "metric": METRIC,
@@ -447,7 +469,10 @@ def main():
                         "rel_residual": v["rel_res"], "err_vs_fp64": v["err_vs_fp64"],
                         "replacements": v["repl"], "fallback": v["fallback"], "ms_assemble": round(v["ms_assemble"], 3),
                         "spmv_ms": round(v["ms_spmv"], 5), "update_ms": round(v["ms_update"], 5),
-                        "spmv_shape": v["shape"]}
+                        "spmv_shape": v["shape"],
+                        **({"precond_ms": round(v["ms_precond"], 5), "colours": v["ncol"],
+                            "sweeps": "persistent" if v["persistent"] else "per colour"}
+                           if v["pc"] in (3, 4) else {})}
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),

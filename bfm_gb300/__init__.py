@@ -32,7 +32,7 @@ class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
 
 
 FP64, MIXED, MIXED_EXACT, FP64_DF = 0, 1, 2, 3
-PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED = 0, 1, 2
+PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_SSOR, PC_LEARNED_SSOR = 0, 1, 2, 3, 4
 HOST, DEVICE = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error", 5: "stagnated"}
 
@@ -73,6 +73,8 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_part_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _P(_i), _P(_i), _P(_d)]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
     "bfm_gpu_problem_apply": (_i, [_vp, _vp, _vp, _i]),
+    "bfm_gpu_problem_ordering": (_i, [_vp, _vp, _vp, _vp]),
+    "bfm_gpu_problem_time_precond": (_i, [_vp, _i, _vp, _vp]),
     "bfm_gpu_mpnn_param_count": (_i, []),
     "bfm_gpu_mpnn_create": (_i, [_P(_vp), C.c_uint]),
     "bfm_gpu_mpnn_destroy": (_i, [_vp]),

@@ -39,6 +39,8 @@ struct CgState {
 	int done, status;
 	int replacements;
 	int stall;          // replacements in a row without halving best_true2's norm
+	double ssor_acc;    // SSOR: (r, z) summed over the sweep phases
+	int ssor_err;       // SSOR: a grid barrier of the persistent sweep kernel timed out
 };
 
 // After an FP64 true residual: converged, or stagnating at the roundoff floor
@@ -94,6 +96,7 @@ struct CgArgs {
 	cudaGraphConditionalHandle cond_repl;  // if-node: replace the residual this iteration
 	int use_cond;  // launched inside the solve graph: drive its conditional nodes
 	int timing;    // measurement launches: ignore the stop flag, never set it
+	int no_pc;     // the SSOR sweeps form z = M r and gamma after this kernel
 };
 
 // 2x2 block k of the matrix: m0 m1 / m2 m3 (one 32-byte or 16-byte vector load)
@@ -209,8 +212,8 @@ __global__ void __launch_bounds__(TPB_K) k_cg_init(CgArgs<V> a, int mixed) {
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		double2 const bb = ld2(a.b, i);
 		V const r0 = (V) bb.x, r1 = (V) bb.y;
-		V u0, u1;
-		precond_apply(a.dinv, a.block_pc, i, r0, r1, u0, u1);
+		V u0 = (V) 0, u1 = (V) 0;
+		if (!a.no_pc) precond_apply(a.dinv, a.block_pc, i, r0, r1, u0, u1);
 		st2(a.x, i, 0.0, 0.0);
 		st2(a.r, i, r0, r1);
 		st2(a.p, i, (V) 0, (V) 0);
@@ -243,6 +246,7 @@ __global__ void __launch_bounds__(TPB_K) k_cg_init(CgArgs<V> a, int mixed) {
 		st->rho = out[0];
 		st->rho_ref = out[0];
 		st->true_res2 = out[0];
+		st->ssor_err = 0;
 		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
 }
@@ -675,6 +679,7 @@ struct DfArgs {
 	cudaGraphConditionalHandle cond_repl;
 	int use_cond;
 	int timing;
+	int no_pc;  // the SSOR sweeps form z = M r and gamma after this kernel
 };
 
 __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
@@ -682,8 +687,8 @@ __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
 		double2 const bb = ld2(a.b, i);
 		dfl const r0 = df_make(bb.x), r1 = df_make(bb.y);
-		dfl u0, u1;
-		df_precond(a.dinv, a.block_pc, i, r0, r1, u0, u1);
+		dfl u0 = {0.f, 0.f}, u1 = {0.f, 0.f};
+		if (!a.no_pc) df_precond(a.dinv, a.block_pc, i, r0, r1, u0, u1);
 		dfl const z = {0.f, 0.f};
 		df_st(a.x, i, z, z);
 		st2(a.x64, i, 0.0, 0.0);
@@ -713,6 +718,7 @@ __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
 		st->rho = out[0];
 		st->rho_ref = out[0];
 		st->true_res2 = out[0];
+		st->ssor_err = 0;
 		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
 }
@@ -806,6 +812,25 @@ __device__ __forceinline__ void hs_beta(CgState* st, double gamma, double rho, i
 	}
 }
 
+// K2 finisher when the SSOR sweeps come next: the iteration count, the cap
+// and the replacement request (from rho alone); beta and gamma follow from
+// the sweeps' (r, z)
+__device__ __forceinline__ void hs_rho(CgState* st, double rho, int timing, int use_cond, cudaGraphConditionalHandle cond,
+                                       cudaGraphConditionalHandle cond_repl) {
+	if (timing) return;
+	double const tol2 = st->rtol * st->rtol * st->bnorm2;
+	st->rho = rho;
+	st->iter += 1;
+	if (st->iter >= st->max_iters) {
+		st->status = BFM_GPU_NOT_CONVERGED;
+		st->done = 1;
+		if (use_cond) cudaGraphSetConditional(cond, 0u);
+	}
+	else if (use_cond && (rho <= st->drop2 * st->rho_ref || rho <= tol2)) {
+		cudaGraphSetConditional(cond_repl, 1u);
+	}
+}
+
 template <int LPR, int NB = 1>
 __global__ void __launch_bounds__(TPB_K) k_hs64_spmv(CgArgs<double> a) {
 	CgState* st = a.st;
@@ -850,15 +875,19 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_update(CgArgs<double> a) {
 		st2(a.x, i, x.x + alpha * pn.x, x.y + alpha * pn.y);
 		double const r0 = r.x - alpha * q.x, r1 = r.y - alpha * q.y;
 		st2(a.r, i, r0, r1);
-		double z0, z1;
-		precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
-		st2(a.u, i, z0, z1);
-		v[0] += r0 * z0 + r1 * z1;
+		if (!a.no_pc) {
+			double z0, z1;
+			precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
+			st2(a.u, i, z0, z1);
+			v[0] += r0 * z0 + r1 * z1;
+		}
 		v[1] += r0 * r0 + r1 * r1;
 	}
 	double out[2];
-	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0)
-		hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		if (a.no_pc) hs_rho(st, out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+		else hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+	}
 }
 
 template <int LPR>
@@ -881,16 +910,18 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
 			double2 const bb = ld2(a.b, row_);
 			double const r0 = bb.x - y0, r1 = bb.y - y1;
 			st2(a.r, row_, r0, r1);
-			double z0, z1;
-			precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
-			st2(a.u, row_, z0, z1);
 			v[0] += r0 * r0 + r1 * r1;
-			v[1] += r0 * z0 + r1 * z1;
+			if (!a.no_pc) {
+				double z0, z1;
+				precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
+				st2(a.u, row_, z0, z1);
+				v[1] += r0 * z0 + r1 * z1;
+			}
 		}
 	}
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		st->gamma = out[1];
+		if (!a.no_pc) st->gamma = out[1];
 		if (true_residual_verdict(st, out[0])) {
 			st->done = 1;
 			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
@@ -1001,16 +1032,20 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_update(DfArgs a) {
 		r0 = df_fma(nalpha, q0, r0);
 		r1 = df_fma(nalpha, q1, r1);
 		df_st(a.r, i, r0, r1);
-		dfl z0, z1;
-		df_precond(a.dinv, a.block_pc, i, r0, r1, z0, z1);
-		df_st(a.u, i, z0, z1);
-		d0 = df_add(d0, df_add(df_mul(r0, z0), df_mul(r1, z1)));
+		if (!a.no_pc) {
+			dfl z0, z1;
+			df_precond(a.dinv, a.block_pc, i, r0, r1, z0, z1);
+			df_st(a.u, i, z0, z1);
+			d0 = df_add(d0, df_add(df_mul(r0, z0), df_mul(r1, z1)));
+		}
 		d1 = df_add(d1, df_add(df_mul(r0, r0), df_mul(r1, r1)));
 	}
 	double v[2] = {df_dbl(d0), df_dbl(d1)};
 	double out[2];
-	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0)
-		hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		if (a.no_pc) hs_rho(st, out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+		else hs_beta(st, out[0], out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+	}
 }
 
 // Replacement of the double-float path: the true residual in FP64 from the
@@ -1040,16 +1075,18 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_replace(DfArgs a) {
 			double const e0 = bb.x - y0, e1 = bb.y - y1;
 			dfl const r0 = df_make(e0), r1 = df_make(e1);
 			df_st(a.r, row, r0, r1);
-			dfl z0, z1;
-			df_precond(a.dinv, a.block_pc, row, r0, r1, z0, z1);
-			df_st(a.u, row, z0, z1);
 			v[0] += e0 * e0 + e1 * e1;
-			v[1] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));
+			if (!a.no_pc) {
+				dfl z0, z1;
+				df_precond(a.dinv, a.block_pc, row, r0, r1, z0, z1);
+				df_st(a.u, row, z0, z1);
+				v[1] += df_dbl(df_add(df_mul(r0, z0), df_mul(r1, z1)));
+			}
 		}
 	}
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		st->gamma = out[1];
+		if (!a.no_pc) st->gamma = out[1];
 		if (true_residual_verdict(st, out[0])) {
 			st->done = 1;
 			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
@@ -1211,16 +1248,18 @@ __global__ void __launch_bounds__(TPB_K) k_df_switch(CgArgs<double> a, const flo
 			double2 const bb = ld2(a.b, row_);
 			double const r0 = bb.x - y0, r1 = bb.y - y1;
 			st2(a.r, row_, r0, r1);
-			double z0, z1;
-			precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
-			st2(a.u, row_, z0, z1);
 			v[0] += r0 * r0 + r1 * r1;
-			v[1] += r0 * z0 + r1 * z1;
+			if (!a.no_pc) {
+				double z0, z1;
+				precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
+				st2(a.u, row_, z0, z1);
+				v[1] += r0 * z0 + r1 * z1;
+			}
 		}
 	}
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		st->gamma = out[1];
+		if (!a.no_pc) st->gamma = out[1];
 		st->rtol = rtol_final;
 		st->status = BFM_GPU_OK;
 		st->done = 0;
@@ -1229,6 +1268,282 @@ __global__ void __launch_bounds__(TPB_K) k_df_switch(CgArgs<double> a, const flo
 		st->done = true_residual_verdict(st, out[0]);
 		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
+}
+
+// ---------------------------------------------------------------- multicolour block SSOR
+// z = M^-1 r with M = (D~ + L) D~^-1 (D~ + U): A = L + D + U in the
+// colour-major node order (L: blocks of lower-colour neighbours, U: higher),
+// D~ the 2x2 relaxation blocks (the diagonal blocks, or the network's).
+//   forward, colours 0 .. nc-1:   y_i = D~_i^-1 (r_i - sum_L A_ij y_j)
+//   backward, colours nc-2 .. 0:  z_i = y_i - D~_i^-1 sum_U A_ij z_j
+// (the backward solve of (D~ + U) z = D~ y, written without D~ itself; the
+// last colour has no U neighbours, so its z is its y).  Nodes of one colour
+// share no element, so each colour is one parallel phase.  The blocks and
+// D~^-1 are read in FP32 (rounding them only moves M a little, and M stays
+// fixed), but the vectors and sums are double-float: FP32 rounding there
+// makes M^-1 r vary from one application to the next at the 1e-7 level, which
+// cost the perforated plates half again as many CG iterations at 1e-10.  y is
+// overwritten by z colour by colour.  Every phase that finishes rows adds
+// their (r, z) to the state; the last phase turns the sum into beta and
+// gamma (after an update) or gamma (after a replacement).
+
+struct SsorArgs {
+	const int* row_ptr;
+	const int* cols;
+	const int* dpos;    // per row: first block at or after the diagonal
+	const float* hi;    // FP32 2x2 blocks
+	const float* dinv;  // relaxation block inverses, double-float layout: node i's FP32 block at [2 i]
+	const void* r;      // residual: double-float float4 (u_hi, v_hi, u_lo, v_lo) or FP64 double2 per node
+	void* z;            // z = M^-1 r, same layout
+	float* y;           // double-float float4 per node
+	double* partials;
+	unsigned* ticket;
+	CgState* st;
+	int lo, hi_row;     // the rows of this phase's colour
+	int fwd_last;       // forward phase of the last colour: its z is its y
+	int first_acc;      // first phase that finishes rows: (r, z) starts from zero
+	int final_phase;    // last phase: beta and gamma
+	int mode;           // 0 after an update (beta = gamma' / gamma), 1 after a residual replacement
+	cudaGraphConditionalHandle cond, cond_repl;
+	int use_cond;
+	int timing;
+	// persistent form: every phase in one cooperative launch
+	unsigned* bar;      // grid barrier: arrivals, generation
+	int ncol;
+	int off[65];        // colour c: rows [off[c], off[c + 1])
+};
+
+// a * b for a float and a double-float (TwoProduct of the high part)
+__device__ __forceinline__ dfl df_mul_f(float a, dfl b) {
+	float const p = __fmul_rn(a, b.hi);
+	float e = __fmaf_rn(a, b.hi, -p);
+	e = __fmaf_rn(a, b.lo, e);
+	float const h = __fadd_rn(p, e);
+	return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+
+// D~^-1 (s0, s1) with the FP32 block d
+__device__ __forceinline__ void ssor_blk(float4 d, dfl s0, dfl s1, dfl& o0, dfl& o1) {
+	o0 = df_add(df_mul_f(d.x, s0), df_mul_f(d.y, s1));
+	o1 = df_add(df_mul_f(d.z, s0), df_mul_f(d.w, s1));
+}
+
+// sum of A_ij v_j over blocks [k0, k1) of the row whose column lies in
+// [cmin, cmax), v double-float float4 per node (written by other blocks of
+// the persistent kernel: read past L1).  Four blocks at a time: their column
+// indices and values are loaded together, then their four gathers, so a row
+// costs two dependent memory trips instead of two per block.
+__device__ __forceinline__ void ssor_row(const SsorArgs& a, int k0, int k1, int cmin, int cmax, dfl& t0, dfl& t1) {
+	for (int kb = k0; kb < k1; kb += 4) {
+		int c[4];
+		float4 m[4];
+#pragma unroll
+		for (int j = 0; j < 4; j++) {
+			bool const in = kb + j < k1;
+			c[j] = in ? a.cols[kb + j] : -1;
+			m[j] = in ? reinterpret_cast<const float4*>(a.hi)[kb + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+		float4 g[4];
+#pragma unroll
+		for (int j = 0; j < 4; j++) {
+			bool const use = c[j] >= cmin && c[j] < cmax;
+			g[j] = use ? __ldcg(reinterpret_cast<const float4*>(a.y) + c[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+#pragma unroll
+		for (int j = 0; j < 4; j++) {
+			dfl const g0 = {g[j].x, g[j].z}, g1 = {g[j].y, g[j].w};
+			t0 = df_add(t0, df_add(df_mul_f(m[j].x, g0), df_mul_f(m[j].y, g1)));
+			t1 = df_add(t1, df_add(df_mul_f(m[j].z, g0), df_mul_f(m[j].w, g1)));
+		}
+	}
+}
+
+template <bool DF>
+__device__ __forceinline__ void ssor_ld_r(const void* r, int i, dfl& r0, dfl& r1, double& q0, double& q1) {
+	if constexpr (DF) {
+		df_ld((const float*) r, i, r0, r1);
+	}
+	else {
+		double2 const t = ld2((const double*) r, i);
+		q0 = t.x;
+		q1 = t.y;
+		r0 = df_make(q0);
+		r1 = df_make(q1);
+	}
+}
+
+template <bool DF>
+__device__ __forceinline__ void ssor_st_z(const SsorArgs& a, int i, dfl z0, dfl z1, dfl r0, dfl r1, double q0, double q1,
+                                          dfl& acc, double& acc64) {
+	if constexpr (DF) {
+		df_st((float*) a.z, i, z0, z1);
+		acc = df_add(acc, df_add(df_mul(r0, z0), df_mul(r1, z1)));
+	}
+	else {
+		double const w0 = df_dbl(z0), w1 = df_dbl(z1);
+		st2((double*) a.z, i, w0, w1);
+		acc64 += q0 * w0 + q1 * w1;
+	}
+}
+
+__device__ __forceinline__ void ssor_finish(const SsorArgs& a, double part) {
+	CgState* st = a.st;
+	st->ssor_acc = a.first_acc ? part : st->ssor_acc + part;
+	if (!a.final_phase || a.timing) return;
+	double const g = st->ssor_acc;
+	if (st->ssor_err) {
+		st->done = 1;
+		st->status = BFM_GPU_BREAKDOWN;
+		if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		return;
+	}
+	if (a.mode == 1) {
+		st->gamma = g;
+		return;
+	}
+	// as hs_beta: a zero (r, z) asks for a replacement, a negative one is a breakdown
+	st->beta = g / st->gamma;
+	st->gamma = g;
+	if (!(g > 0.0)) {
+		if (g == 0.0) {
+			if (a.use_cond) cudaGraphSetConditional(a.cond_repl, 1u);
+		}
+		else {
+			st->done = 1;
+			st->status = BFM_GPU_BREAKDOWN;
+			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+		}
+	}
+}
+
+template <bool DF>
+__global__ void __launch_bounds__(TPB_K) k_ssor_fwd(SsorArgs a) {
+	if (a.st->done && !a.timing) return;
+	dfl acc = {0.f, 0.f};
+	double acc64 = 0.0;
+	for (int i = a.lo + blockIdx.x * blockDim.x + threadIdx.x; i < a.hi_row; i += gridDim.x * blockDim.x) {
+		dfl r0, r1;
+		double q0 = 0.0, q1 = 0.0;
+		ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
+		dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
+		ssor_row(a, a.row_ptr[i], a.dpos[i], 0, a.lo, t0, t1);
+		dfl y0, y1;
+		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[2 * i], df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), y0, y1);
+		df_st(a.y, i, y0, y1);
+		if (a.fwd_last) ssor_st_z<DF>(a, i, y0, y1, r0, r1, q0, q1, acc, acc64);
+	}
+	if (!a.fwd_last) return;
+	double v[1] = {DF ? df_dbl(acc) : acc64};
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
+}
+
+template <bool DF>
+__global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
+	if (a.st->done && !a.timing) return;
+	dfl acc = {0.f, 0.f};
+	double acc64 = 0.0;
+	for (int i = a.lo + blockIdx.x * blockDim.x + threadIdx.x; i < a.hi_row; i += gridDim.x * blockDim.x) {
+		dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
+		ssor_row(a, a.dpos[i] + 1, a.row_ptr[i + 1], a.hi_row, 0x7fffffff, t0, t1);
+		dfl w0, w1, y0, y1;
+		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[2 * i], t0, t1, w0, w1);
+		df_ld(a.y, i, y0, y1);
+		dfl const z0 = df_add(y0, df_neg(w0)), z1 = df_add(y1, df_neg(w1));
+		df_st(a.y, i, z0, z1);
+		dfl r0, r1;
+		double q0 = 0.0, q1 = 0.0;
+		ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
+		ssor_st_z<DF>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
+	}
+	double v[1] = {DF ? df_dbl(acc) : acc64};
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
+}
+
+// Grid barrier of the persistent sweep kernel (cooperative launch: every
+// block is resident).  Arrivals count up; the last one resets the count and
+// advances the generation the others wait for.  The wait is bounded: past
+// the limit the kernel records the timeout, and the blocks stop sweeping.
+constexpr long SSOR_SPIN_LIMIT = 1l << 24;
+
+__device__ bool ssor_barrier(const SsorArgs& a) {
+	__shared__ int ok;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		unsigned* count = a.bar;
+		unsigned* gen = a.bar + 1;
+		unsigned const g = atomicAdd(gen, 0u);
+		__threadfence();
+		int good = 1;
+		if (atomicAdd(count, 1u) == gridDim.x - 1) {
+			atomicExch(count, 0u);
+			__threadfence();
+			atomicAdd(gen, 1u);
+		}
+		else {
+			long spins = 0;
+			unsigned cur;
+			while (true) {
+				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gen) : "memory");
+				if (cur != g) break;
+				__nanosleep(20);
+				if (++spins > SSOR_SPIN_LIMIT || atomicAdd(&a.st->ssor_err, 0) != 0) {
+					atomicExch(&a.st->ssor_err, 1);
+					good = 0;
+					break;
+				}
+			}
+		}
+		__threadfence();
+		ok = good;
+	}
+	__syncthreads();
+	return ok;
+}
+
+template <bool DF>
+__global__ void __launch_bounds__(TPB_K) k_ssor_all(SsorArgs a) {
+	if (a.st->done && !a.timing) return;
+	int const nc = a.ncol > 0 ? a.ncol : 1;
+	dfl acc = {0.f, 0.f};
+	double acc64 = 0.0;
+	bool alive = true;
+	int const stride = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+	for (int ph = 0; ph < 2 * nc - 1 && alive; ph++) {
+		bool const forward = ph < nc;
+		int const c = forward ? ph : 2 * nc - 2 - ph;
+		bool const final_rows = !forward || c == nc - 1;
+		int const lo = a.off[c], hi = a.off[c + 1];
+		for (int i = lo + tid; i < hi; i += stride) {
+			dfl r0, r1;
+			double q0 = 0.0, q1 = 0.0;
+			dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
+			float4 const d = reinterpret_cast<const float4*>(a.dinv)[2 * i];
+			dfl z0, z1;
+			if (forward) {
+				ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
+				ssor_row(a, a.row_ptr[i], a.dpos[i], 0, lo, t0, t1);
+				ssor_blk(d, df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), z0, z1);
+			}
+			else {
+				ssor_row(a, a.dpos[i] + 1, a.row_ptr[i + 1], hi, 0x7fffffff, t0, t1);
+				dfl w0, w1;
+				ssor_blk(d, t0, t1, w0, w1);
+				float4 const yv = __ldcg(reinterpret_cast<const float4*>(a.y) + i);
+				z0 = df_add({yv.x, yv.z}, df_neg(w0));
+				z1 = df_add({yv.y, yv.w}, df_neg(w1));
+				ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
+			}
+			__stcg(reinterpret_cast<float4*>(a.y) + i, make_float4(z0.hi, z1.hi, z0.lo, z1.lo));
+			if (final_rows) ssor_st_z<DF>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
+		}
+		if (ph < 2 * nc - 2) alive = ssor_barrier(a);
+	}
+	// every block reaches the reduction, finished or not
+	double v[1] = {DF ? df_dbl(acc) : acc64};
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
 }
 
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner

@@ -254,6 +254,43 @@ __global__ void k_rows_fill(int N, int kind, const int* __restrict__ inc_ptr, co
 	for (int i = 0; i < len; i++) cols[rs + i] = in[i];
 }
 
+// ------------------------------------------------------------------ multicolour node order
+// The SSOR preconditioners sweep the nodes colour by colour (no two nodes of
+// one colour share an element), so the problem is renumbered colour-major:
+// then every block row lists its lower-colour neighbours, its diagonal block
+// and its higher-colour neighbours in that order, and a colour is a
+// contiguous range of rows.
+
+// dst[i] = src[map[i]] for `width` consecutive elements per node
+template <typename T>
+__global__ void k_gather_nodes(long N, int width, const T* __restrict__ src, const int* __restrict__ map, T* __restrict__ dst) {
+	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (t >= N * width) return;
+	long const i = t / width;
+	int const k = (int) (t - i * width);
+	dst[t] = src[(long) map[i] * width + k];
+}
+
+// node ids through a map (ids outside [0, N) stay: the pattern kernels report them)
+__global__ void k_map_ids(long n, int N, int* __restrict__ ids, const int* __restrict__ map) {
+	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (t >= n) return;
+	int const v = ids[t];
+	if (v >= 0 && v < N) ids[t] = map[v];
+}
+
+// first block of each row at or after the diagonal: the lower-colour
+// neighbours are [row_ptr[i], dpos[i]), the higher-colour ones follow the
+// diagonal block
+__global__ void k_diag_pos(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, int* __restrict__ dpos) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	int k = row_ptr[i];
+	int const e = row_ptr[i + 1];
+	while (k < e && cols[k] < i) k++;
+	dpos[i] = k;
+}
+
 // ------------------------------------------------------------------ Dirichlet bookkeeping
 
 // Conditions are applied in order; per DOF we keep the first value (used to
@@ -1086,7 +1123,7 @@ __global__ void k_edge_loads(int N, const int* __restrict__ ledges, const double
 // blocks == nullptr: Jacobi blocks from the diagonal of the operator.
 __global__ void k_store_blocks(int N, const double* __restrict__ blocks, const int* __restrict__ row_ptr,
                                const int* __restrict__ cols, const double* __restrict__ v64, const float* __restrict__ v32,
-                               int layout, double* __restrict__ dinv64, float* __restrict__ dinv32) {
+                               int layout, int block, double* __restrict__ dinv64, float* __restrict__ dinv32) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
 	double m[4];
@@ -1094,15 +1131,27 @@ __global__ void k_store_blocks(int N, const double* __restrict__ blocks, const i
 		for (int k = 0; k < 4; k++) m[k] = blocks[4l * i + k];
 	}
 	else {
-		double k00 = 0.0, k11 = 0.0;
+		double k00 = 0.0, k01 = 0.0, k10 = 0.0, k11 = 0.0;
 		for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++)
 			if (cols[k] == i) {
 				k00 = v64 ? v64[4l * k] : (double) v32[4l * k];
+				k01 = v64 ? v64[4l * k + 1] : (double) v32[4l * k + 1];
+				k10 = v64 ? v64[4l * k + 2] : (double) v32[4l * k + 2];
 				k11 = v64 ? v64[4l * k + 3] : (double) v32[4l * k + 3];
 			}
-		m[0] = k00 != 0.0 ? 1.0 / k00 : 0.0;
-		m[1] = m[2] = 0.0;
-		m[3] = k11 != 0.0 ? 1.0 / k11 : 0.0;
+		if (block) {
+			double const det = k00 * k11 - k01 * k10;
+			double const id = det != 0.0 ? 1.0 / det : 0.0;
+			m[0] = k11 * id;
+			m[1] = -k01 * id;
+			m[2] = -k10 * id;
+			m[3] = k00 * id;
+		}
+		else {
+			m[0] = k00 != 0.0 ? 1.0 / k00 : 0.0;
+			m[1] = m[2] = 0.0;
+			m[3] = k11 != 0.0 ? 1.0 / k11 : 0.0;
+		}
 	}
 	if (layout == 0) {
 		for (int k = 0; k < 4; k++) dinv64[4l * i + k] = m[k];
@@ -1241,7 +1290,23 @@ struct bfm_gpu_problem {
 
 	void* ext;               // batch solver state (batch.cu)
 	void (*ext_free)(void*);
+
+	// multicolour node order of the SSOR preconditioners: the problem is
+	// assembled and solved with its nodes renumbered colour by colour.
+	// iperm: caller's node -> working node, perm: its inverse.  `ordered`
+	// holds an ORD_* bit for every input array kept in the working order.
+	unsigned ordered;
+	bool colored;  // perm is the colouring of the current geometry
+	int ncol;
+	int col_off[65];
+	int *perm, *iperm, *dpos;
+	void* otmp;    // scratch of the in-place permutations
+	float* ssor_y; // sweep vector (double-float, 4 floats per node)
+	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
+	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
 };
+
+enum : unsigned { ORD_COORDS = 1, ORD_ELEMS = 2, ORD_MASKS = 4, ORD_EDGES = 8, ORD_FIELDS = 16, ORD_LEDGES = 32, ORD_ALL = 63 };
 
 namespace {
 
@@ -1300,6 +1365,136 @@ int incidence(bfm_gpu_problem* P, const int* items, int n_items, int arity, int*
 	k_sort_lists<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, ptr, list, maxlen, P->err, code);
 	CK(cudaGetLastError());
 	return 0;
+}
+
+bool ssor_pc(int pc) { return pc == BFM_GPU_PC_SSOR || pc == BFM_GPU_PC_LEARNED_SSOR; }
+
+// Node-block pattern of the current element array (steps 1-2 of the assembly).
+int build_pattern(bfm_gpu_problem* P) {
+	cudaStream_t const st = P->stream;
+	if (incidence(P, P->elems, P->NE, P->kind, P->cnt, P->inc_ptr, P->inc, MAXV, ERR_VALENCE)) return -1;
+	k_rows_count<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->kind, P->elems, P->inc_ptr, P->inc, P->cand, P->row_len, P->err);
+	if (scan(P, P->row_len, P->row_ptr, P->N)) return -1;
+	k_rows_fill<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->kind, P->inc_ptr, P->cand, P->row_ptr, P->cols);
+	CK(cudaGetLastError());
+	return 0;
+}
+
+// Colour the node graph of the current (caller-order) pattern and derive the
+// colour-major numbering: colour by colour, ascending caller index within a
+// colour.  Greedy colouring in node order, on the host: meshes come numbered
+// with spatial locality (rows of a grid, sweeps of a mesher), and greedy in
+// that order finds 3-4 colours on triangle meshes where the parallel
+// random-priority colourings need 6-7 (each colour is one grid-wide phase
+// of every sweep).  One pass over the pattern, after a copy of it to the
+// host; it runs again only when the geometry changes.
+int color_nodes(bfm_gpu_problem* P) {
+	cudaStream_t const st = P->stream;
+	long const N = P->N;
+	if (!P->perm && (dalloc(&P->perm, N) || dalloc(&P->iperm, N) || dalloc(&P->dpos, N))) return -1;
+	int* rp = (int*) malloc((N + 1) * sizeof(int));
+	int* col = (int*) malloc((N + 1) * sizeof(int));
+	int* perm = (int*) malloc((N + 1) * sizeof(int));
+	int* iperm = (int*) malloc((N + 1) * sizeof(int));
+	int* cols = nullptr;
+	int rc = 0;
+	if (!rp || !col || !perm || !iperm) rc = fail("out of host memory");
+	if (!rc && cudaMemcpyAsync(rp, P->row_ptr, (N + 1) * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+		rc = fail("pattern copy failed");
+	if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = fail("pattern copy failed");
+	if (!rc && !(cols = (int*) malloc((size_t) rp[N] * sizeof(int) + 4))) rc = fail("out of host memory");
+	if (!rc && (cudaMemcpyAsync(cols, P->cols, (size_t) rp[N] * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+	            cudaStreamSynchronize(st) != cudaSuccess))
+		rc = fail("pattern copy failed");
+	if (!rc) {
+		// mark[c] == i: colour c is taken by a neighbour of node i
+		long mark[64];
+		for (int c = 0; c < 64; c++) mark[c] = -1;
+		int counts[64] = {0};
+		for (long i = 0; i < N; i++) {
+			for (int k = rp[i]; k < rp[i + 1]; k++) {
+				int const j = cols[k];
+				if (j < i && j >= 0) mark[col[j]] = i;
+			}
+			int c = 0;
+			while (c < 63 && mark[c] == i) c++;
+			col[i] = c;
+			counts[c]++;
+		}
+		P->ncol = 0;
+		P->col_off[0] = 0;
+		for (int c = 0; c < 64; c++) {
+			if (counts[c]) P->ncol = c + 1;
+			P->col_off[c + 1] = P->col_off[c] + counts[c];
+		}
+		int next[64];
+		for (int c = 0; c < 64; c++) next[c] = P->col_off[c];
+		for (long i = 0; i < N; i++) {
+			int const w = next[col[i]]++;
+			iperm[i] = w;
+			perm[w] = (int) i;
+		}
+		if (cudaMemcpyAsync(P->perm, perm, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+		    cudaMemcpyAsync(P->iperm, iperm, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+		    cudaStreamSynchronize(st) != cudaSuccess)
+			rc = fail("ordering upload failed");
+	}
+	free(rp);
+	free(col);
+	free(perm);
+	free(iperm);
+	free(cols);
+	if (rc) return rc;
+	P->colored = true;
+	P->graph_precision = -1;  // the solve graph's sweep phases follow the colour ranges
+	return 0;
+}
+
+// Bring the node-indexed inputs into the working order (to_work) or back to
+// the caller's, each array once: `ordered` tracks which are permuted.
+int reorder_inputs(bfm_gpu_problem* P, bool to_work) {
+	cudaStream_t const st = P->stream;
+	long const N = P->N;
+	if (!P->otmp) {
+		size_t const bytes = (size_t) (16 * N > (long) P->max_conds * N ? 16 * N : (long) P->max_conds * N) + 16;
+		CK(cudaMalloc(&P->otmp, bytes));
+	}
+	const int* data_map = to_work ? P->perm : P->iperm;  // dst[i] = src[map[i]]
+	const int* id_map = to_work ? P->iperm : P->perm;
+	auto todo = [&](unsigned bit) { return to_work ? !(P->ordered & bit) : (P->ordered & bit) != 0; };
+	auto gather_d2 = [&](double* a) -> int {
+		k_gather_nodes<double><<<blocks_for(2 * N), TPB, 0, st>>>(N, 2, a, data_map, (double*) P->otmp);
+		CK(cudaMemcpyAsync(a, P->otmp, 2 * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+		return 0;
+	};
+	if (todo(ORD_COORDS) && gather_d2(P->coords)) return -1;
+	for (int f = 0; f < P->forces.nf; f++)
+		if (todo(ORD_FIELDS) && P->forces.field[f] && gather_d2(P->force_fields[f])) return -1;
+	if (todo(ORD_MASKS)) {
+		for (int c = 0; c < P->n_conds; c++)
+			k_gather_nodes<uint8_t><<<blocks_for(N), TPB, 0, st>>>(N, 1, P->masks + c * N, data_map,
+			                                                     (uint8_t*) P->otmp + c * N);
+		if (P->n_conds) CK(cudaMemcpyAsync(P->masks, P->otmp, (long) P->n_conds * N, cudaMemcpyDeviceToDevice, st));
+	}
+	if (todo(ORD_ELEMS)) k_map_ids<<<blocks_for((long) P->NE * P->kind), TPB, 0, st>>>((long) P->NE * P->kind, P->N, P->elems, id_map);
+	if (todo(ORD_EDGES) && P->n_edges) k_map_ids<<<blocks_for(2l * P->n_edges), TPB, 0, st>>>(2l * P->n_edges, P->N, P->edges, id_map);
+	if (todo(ORD_LEDGES) && P->n_loads) k_map_ids<<<blocks_for(2l * P->n_loads), TPB, 0, st>>>(2l * P->n_loads, P->N, P->ledges, id_map);
+	CK(cudaGetLastError());
+	P->ordered = to_work ? ORD_ALL : 0u;
+	return 0;
+}
+
+// Node order for this assembly: colour-major for the SSOR preconditioners
+// (colouring the caller's graph when the geometry changed), else the caller's.
+int prepare_order(bfm_gpu_problem* P) {
+	bool const want = ssor_pc(P->precond);
+	if (P->ordered && (!want || !P->colored))
+		if (reorder_inputs(P, false)) return -1;
+	if (!want) return 0;
+	if (!P->colored) {
+		if (build_pattern(P) || color_nodes(P)) return -1;
+	}
+	return reorder_inputs(P, true);
 }
 
 template <typename V>
@@ -1394,6 +1589,74 @@ int add_conditional(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t*
 	return 0;
 }
 
+SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
+	SsorArgs a;
+	memset(&a, 0, sizeof a);
+	a.row_ptr = P->row_ptr;
+	a.cols = P->cols;
+	a.dpos = P->dpos;
+	a.hi = P->vals32;
+	a.dinv = P->dinv32;
+	a.r = r;
+	a.z = z;
+	a.y = P->ssor_y;
+	a.partials = P->partials;
+	a.ticket = P->ticket;
+	a.st = P->st;
+	return a;
+}
+
+// The 2 nc - 1 sweep phases of one z = M^-1 r after node `dep` (nullptr: first
+// in the graph), in graph g; *last gets the final node.  mode as SsorArgs.
+int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cudaGraphNode_t* dep, SsorArgs base, bool df,
+             int mode) {
+	int const nc = P->ncol > 0 ? P->ncol : 1;
+	if (P->ssor_grid > 0) {
+		// one cooperative launch for every phase
+		SsorArgs a = base;
+		a.ncol = nc;
+		for (int c = 0; c <= nc && c < 65; c++) a.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
+		a.bar = P->ssor_bar;
+		a.first_acc = 1;
+		a.final_phase = 1;
+		a.mode = mode;
+		void* pa[1] = {&a};
+		cudaGraphNode_t n;
+		if (add_node(g, &n, dep, df ? (void*) k_ssor_all<true> : (void*) k_ssor_all<false>, P->ssor_grid, pa)) return -1;
+		cudaLaunchAttributeValue v;
+		memset(&v, 0, sizeof v);
+		v.cooperative = 1;
+		if (cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v) == cudaSuccess) {
+			*last = n;
+			return 0;
+		}
+		// no cooperative kernel nodes here: the per-phase kernels instead
+		cudaGetLastError();
+		cudaGraphDestroyNode(n);
+		P->ssor_grid = 0;
+	}
+	void* fwd = df ? (void*) k_ssor_fwd<true> : (void*) k_ssor_fwd<false>;
+	void* bwd = df ? (void*) k_ssor_bwd<true> : (void*) k_ssor_bwd<false>;
+	const cudaGraphNode_t* d = dep;
+	cudaGraphNode_t n;
+	for (int ph = 0; ph < 2 * nc - 1; ph++) {
+		SsorArgs a = base;
+		bool const forward = ph < nc;
+		int const c = forward ? ph : 2 * nc - 2 - ph;
+		a.lo = P->col_off[c];
+		a.hi_row = P->col_off[c + 1];
+		a.fwd_last = forward && c == nc - 1;
+		a.first_acc = a.fwd_last;
+		a.final_phase = ph == 2 * nc - 2;
+		a.mode = mode;
+		void* pa[1] = {&a};
+		if (add_node(g, &n, d, forward ? fwd : bwd, P->grid, pa)) return -1;
+		*last = n;
+		d = last;
+	}
+	return 0;
+}
+
 // FP64:  init -> while(running){ A ; B } -> true residual
 // mixed: init -> while(running){ K1 ; K2 ; if(replace){R} ; K1' ; K2' ; if(replace'){R'} } -> true residual
 //        (two iterations per body pass, so each node has fixed ping-pong direction buffers)
@@ -1410,10 +1673,12 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		// double-float iterations to DF_SWITCH x rtol, then FP64 iterations from the same state
 		bfm_gpu_opts_t od = *o;
 		od.rtol = o->rtol * DF_SWITCH < 1.0 ? o->rtol * DF_SWITCH : 1.0;
+		bool const ssor = ssor_pc(P->precond);
 		DfArgs a[2];
 		a[0] = df_args(P, &od);
 		a[0].use_cond = 1;
 		a[0].cond = h;
+		a[0].no_pc = ssor;
 		a[1] = a[0];
 		a[1].p = a[0].s;
 		a[1].s = a[0].p;
@@ -1421,12 +1686,17 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		b[0] = cg_args<double>(P, o);
 		CK(cudaGraphConditionalHandleCreate(&b[0].cond, g, 0u, cudaGraphCondAssignDefault));
 		b[0].use_cond = 1;
+		b[0].no_pc = ssor;
 		b[1] = b[0];
 		b[1].p = b[0].pn;
 		b[1].pn = b[0].p;
 		CgKernels const K64 = kernels_lpr(1001);
+		SsorArgs sa = ssor_args(P, a[0].r, a[0].u);
+		sa.use_cond = 1;
+		sa.cond = h;
 		void* pi[1] = {&a[0]};
 		if (add_node(g, &n_init, nullptr, (void*) k_df_init, P->grid, pi)) return -1;
+		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, true, 1)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
 		for (int half = 0; half < 2; half++) {
 			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
@@ -1440,10 +1710,14 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			}
 			else if (add_node(body, &n1, prev ? &prev : nullptr, K.hsdf, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_hsdf_update, P->grid, pa)) return -1;
+			SsorArgs sh = sa;
+			sh.cond_repl = a[half].cond_repl;
+			if (ssor && add_ssor(P, body, &n2, &n2, sh, true, 0)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			cudaGraphNode_t nf;
 			if (add_node(ifbody, &nf, nullptr, (void*) k_df_flush, P->grid, pa)) return -1;
 			if (add_node(ifbody, &nr, &nf, K.hsdfrepl, P->grid, pa)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, true, 1)) return -1;
 			prev = nif;
 		}
 		cudaGraphNode_t n_fin, n_sw, n_loop2;
@@ -1454,6 +1728,10 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		double rtol_final = o->rtol;
 		void* ps[4] = {&b[0], &dir_a, &dir_b, &rtol_final};
 		if (add_node(g, &n_sw, &n_fin, (void*) k_df_switch, P->grid, ps)) return -1;
+		SsorArgs sb = ssor_args(P, b[0].r, b[0].u);
+		sb.use_cond = 1;
+		sb.cond = b[0].cond;
+		if (ssor && add_ssor(P, g, &n_sw, &n_sw, sb, false, 1)) return -1;
 		cudaGraph_t body2;
 		if (add_conditional(g, &n_loop2, &n_sw, b[0].cond, cudaGraphCondTypeWhile, &body2)) return -1;
 		cudaGraphNode_t prev2 = nullptr;
@@ -1465,23 +1743,33 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			if (add_node(body2, &n0, prev2 ? &prev2 : nullptr, (void*) k_hs64_dir, P->grid, pa)) return -1;
 			if (add_node(body2, &n1, &n0, K64.hs64s, P->grid, pa)) return -1;
 			if (add_node(body2, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
+			SsorArgs sh = sb;
+			sh.cond_repl = b[half].cond_repl;
+			if (ssor && add_ssor(P, body2, &n2, &n2, sh, false, 0)) return -1;
 			if (add_conditional(body2, &nif, &n2, b[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			if (add_node(ifbody, &nr, nullptr, K64.hs64repl, P->grid, pa)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, false, 1)) return -1;
 			prev2 = nif;
 		}
 		void* pr[1] = {&b[0]};
 		if (add_node(g, &n_res, &n_loop2, K.res64, P->grid, pr)) return -1;
 	}
 	else if (!mixed) {
+		bool const ssor = ssor_pc(P->precond);
 		CgArgs<double> a[2];
 		a[0] = cg_args<double>(P, o);
 		a[0].use_cond = 1;
 		a[0].cond = h;
+		a[0].no_pc = ssor;
 		a[1] = a[0];
 		a[1].p = a[0].pn;
 		a[1].pn = a[0].p;
+		SsorArgs sa = ssor_args(P, a[0].r, a[0].u);
+		sa.use_cond = 1;
+		sa.cond = h;
 		void* pi[2] = {&a[0], &imixed};
 		if (add_node(g, &n_init, nullptr, (void*) k_cg_init<double>, P->grid, pi)) return -1;
+		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, false, 1)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
 		for (int half = 0; half < 2; half++) {
 			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
@@ -1495,8 +1783,12 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			}
 			else if (add_node(body, &n1, prev ? &prev : nullptr, K.hs64, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
+			SsorArgs sh = sa;
+			sh.cond_repl = a[half].cond_repl;
+			if (ssor && add_ssor(P, body, &n2, &n2, sh, false, 0)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			if (add_node(ifbody, &nr, nullptr, K.hs64repl, P->grid, pa)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, false, 1)) return -1;
 			prev = nif;
 		}
 		void* pa[1] = {&a[0]};
@@ -1612,6 +1904,63 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 	CK(err);
 	*ms_spmv = t1 / reps;
 	*ms_update = t2 / reps;
+	return 0;
+}
+
+// Mean duration (ms) of one SSOR application z = M^-1 r (every sweep phase),
+// launched standalone on a scratch solver state.  Overwrites the Krylov vectors.
+int time_ssor(bfm_gpu_problem* P, int reps, double* ms) {
+	if (!ssor_pc(P->precond)) return fail("time the SSOR sweeps of a problem solved with an SSOR preconditioner");
+	CgState* scratch = nullptr;
+	if (dalloc(&scratch, 1)) return -1;
+	cudaStream_t const st = P->stream;
+	CK(cudaMemsetAsync(scratch, 0, sizeof(CgState), st));
+	bool const df = P->precision == BFM_GPU_FP64_DF;
+	SsorArgs base = ssor_args(P, P->vec[0], P->vec[1]);
+	base.st = scratch;
+	base.timing = 1;
+	int const nc = P->ncol > 0 ? P->ncol : 1;
+	cudaEvent_t e[2];
+	for (auto& x : e) cudaEventCreate(&x);
+	auto once = [&]() {
+		if (P->ssor_grid > 0) {
+			SsorArgs a = base;
+			a.ncol = nc;
+			for (int c = 0; c <= nc && c < 65; c++) a.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
+			a.bar = P->ssor_bar;
+			a.first_acc = a.final_phase = 1;
+			void* pa[1] = {&a};
+			cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), st);
+			cudaLaunchCooperativeKernel(df ? (void*) k_ssor_all<true> : (void*) k_ssor_all<false>, dim3(P->ssor_grid),
+			                            dim3(TPB), pa, 0, st);
+			return;
+		}
+		for (int ph = 0; ph < 2 * nc - 1; ph++) {
+			SsorArgs a = base;
+			bool const forward = ph < nc;
+			int const c = forward ? ph : 2 * nc - 2 - ph;
+			a.lo = P->col_off[c];
+			a.hi_row = P->col_off[c + 1];
+			a.fwd_last = forward && c == nc - 1;
+			a.first_acc = a.fwd_last;
+			a.final_phase = ph == 2 * nc - 2;
+			void* pa[1] = {&a};
+			cudaLaunchKernel(forward ? (df ? (void*) k_ssor_fwd<true> : (void*) k_ssor_fwd<false>)
+			                         : (df ? (void*) k_ssor_bwd<true> : (void*) k_ssor_bwd<false>),
+			                 dim3(P->grid), dim3(TPB), pa, 0, st);
+		}
+	};
+	once();
+	cudaEventRecord(e[0], st);
+	for (int i = 0; i < reps; i++) once();
+	cudaEventRecord(e[1], st);
+	cudaError_t const err = cudaStreamSynchronize(st);
+	float t = 0;
+	cudaEventElapsedTime(&t, e[0], e[1]);
+	for (auto& x : e) cudaEventDestroy(x);
+	cudaFree(scratch);
+	CK(err);
+	*ms = t / reps;
 	return 0;
 }
 
@@ -1746,7 +2095,8 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 		if (p) cudaFree(p);
 	for (int i = 0; i < MAXF; i++)
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
-	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist};
+	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y,
+	              P->ssor_bar};
 	for (void* q : lb)
 		if (q) cudaFree(q);
 	if (P->ext && P->ext_free) P->ext_free(P->ext);
@@ -1767,6 +2117,8 @@ int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* P, const double* coords, con
 	g_err[0] = 0;
 	CK(cudaMemcpyAsync(P->coords, coords, 2l * P->N * sizeof(double), kind_of(where), P->stream));
 	CK(cudaMemcpyAsync(P->elems, elems, (long) P->NE * P->kind * sizeof(int), kind_of(where), P->stream));
+	P->ordered &= ~(ORD_COORDS | ORD_ELEMS);
+	P->colored = false;
 	P->assembled = false;
 	return 0;
 }
@@ -1824,6 +2176,8 @@ int bfm_gpu_problem_set_forces(bfm_gpu_problem_t* P, int n_forces, const double*
 			P->forces.field[f] = P->force_fields[f];
 		}
 	}
+	// every field in use now holds the caller's order
+	P->ordered &= ~ORD_FIELDS;
 	P->assembled = false;
 	return 0;
 }
@@ -1846,6 +2200,7 @@ int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int*
 	if (n_edges) CK(cudaMemcpyAsync(P->edges, edges, 2l * n_edges * sizeof(int), kind_of(where), P->stream));
 	// every edge counts as a boundary edge until bfm_gpu_problem_set_edge_boundary says otherwise
 	if (n_edges) CK(cudaMemsetAsync(P->eboundary, 1, n_edges, P->stream));
+	P->ordered &= ~(ORD_MASKS | ORD_EDGES);
 	P->assembled = false;
 	return 0;
 }
@@ -1877,6 +2232,7 @@ int bfm_gpu_problem_set_edge_loads(bfm_gpu_problem_t* P, int n_loads, const int3
 		CK(cudaMemcpyAsync(P->ledges, edges, 2l * n_loads * sizeof(int), kind_of(where), P->stream));
 		CK(cudaMemcpyAsync(P->lloads, loads, 2l * n_loads * sizeof(double), kind_of(where), P->stream));
 	}
+	P->ordered &= ~ORD_LEDGES;
 	P->assembled = false;
 	return 0;
 }
@@ -1925,10 +2281,12 @@ int bfmi_mesh(bfm_gpu_problem_t* P, bfmi_mesh_t* o) {
 
 int bfmi_set_precond_blocks(bfm_gpu_problem_t* P, const double* blocks) {
 	if (!P->assembled) return fail("assemble before setting the preconditioner");
-	int const layout = P->precision == BFM_GPU_FP64 ? 0 : P->precision == BFM_GPU_FP64_DF ? 2 : 1;
+	// FP64 SSOR sweeps read FP32 relaxation blocks: the double-float layout
+	int const layout = P->precision == BFM_GPU_FP64_DF || ssor_pc(P->precond) ? 2 : P->precision == BFM_GPU_FP64 ? 0 : 1;
+	// without blocks: Jacobi, or block Jacobi as the SSOR relaxation blocks
 	k_store_blocks<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, blocks, P->row_ptr, P->cols,
 	                                                        P->precision != BFM_GPU_MIXED ? P->vals64 : nullptr, P->vals32,
-	                                                        layout, P->dinv64, P->dinv32);
+	                                                        layout, ssor_pc(P->precond), P->dinv64, P->dinv32);
 	CK(cudaGetLastError());
 	return 0;
 }
@@ -1966,13 +2324,17 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	bool const dfp = precision == BFM_GPU_FP64_DF;
 	bool const want64 = precision != BFM_GPU_MIXED;  // FP64 values: the operator, or the residual operator
 	bool const want32 = precision != BFM_GPU_FP64;   // FP32 values: the mixed iteration operator / hi parts
+	bool const ssor = ssor_pc(P->precond);
+	if (ssor && precision != BFM_GPU_FP64 && !dfp)
+		return fail("the SSOR preconditioners run on the FP64 and FP64_DF paths");
+	bool const fp64_ssor = ssor && precision == BFM_GPU_FP64;  // FP32 blocks and relaxation blocks for the sweeps
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
 	// value storage for this precision (allocated once, on first use)
 	if (want64 && !P->vals64 && dalloc(&P->vals64, 4 * P->nb_cap)) return -1;
-	if (want32 && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
+	if ((want32 || fp64_ssor) && !P->vals32 && dalloc(&P->vals32, 4 * P->nb_cap)) return -1;
 	if ((!want32 || dfp) && !P->dinv64 && dalloc(&P->dinv64, 4 * N)) return -1;
-	if (want32 && !P->dinv32 && dalloc(&P->dinv32, 8 * N)) return -1;  // up to a double-float 2x2 block per node
+	if ((want32 || fp64_ssor) && !P->dinv32 && dalloc(&P->dinv32, 8 * N)) return -1;  // up to a double-float 2x2 block per node
 	if (want32 && !P->corr32 && dalloc(&P->corr32, 4 * N)) return -1;
 	if (dfp && !P->vals32lo && dalloc(&P->vals32lo, 4 * P->nb_cap)) return -1;
 	if (dfp && !P->srow_df && dalloc(&P->srow_df, 8 * N)) return -1;
@@ -1992,12 +2354,31 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	P->precision = precision;
 	CK(cudaEventRecord(P->ev[0], st));
 	CK(cudaMemsetAsync(P->err, 0, sizeof(int), st));
-	// 1. node -> element incidence, ascending
-	if (incidence(P, P->elems, P->NE, P->kind, P->cnt, P->inc_ptr, P->inc, MAXV, ERR_VALENCE)) return -1;
-	// 2. node-block pattern
-	k_rows_count<<<blocks_for(N), TPB, 0, st>>>(P->N, P->kind, P->elems, P->inc_ptr, P->inc, P->cand, P->row_len, P->err);
-	if (scan(P, P->row_len, P->row_ptr, P->N)) return -1;
-	k_rows_fill<<<blocks_for(N), TPB, 0, st>>>(P->N, P->kind, P->inc_ptr, P->cand, P->row_ptr, P->cols);
+	// 0. node order (colour-major for the SSOR preconditioners)
+	if (prepare_order(P)) return -1;
+	// 1. node -> element incidence, ascending; 2. node-block pattern
+	if (build_pattern(P)) return -1;
+	if (ssor_pc(P->precond)) {
+		k_diag_pos<<<blocks_for(N), TPB, 0, st>>>(P->N, P->row_ptr, P->cols, P->dpos);
+		if (!P->ssor_y && dalloc(&P->ssor_y, 4 * N)) return -1;
+		if (!P->ssor_bar) {
+			if (dalloc(&P->ssor_bar, 2)) return -1;
+			CK(cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), st));
+			// every block of the persistent sweep kernel resident at once
+			int nb = 0, dev = 0, coop = 0;
+			CK(cudaGetDevice(&dev));
+			CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+			if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_ssor_all<true>, TPB, 0) == cudaSuccess &&
+			    nb > 0) {
+				int nb64 = 0;
+				if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb64, (const void*) k_ssor_all<false>, TPB, 0) == cudaSuccess &&
+				    nb64 > 0 && nb64 < nb)
+					nb = nb64;
+				P->ssor_grid = num_sms() * nb;
+			}
+			cudaGetLastError();
+		}
+	}
 	// 3. Dirichlet bookkeeping, conditions in order (node -> edge incidence
 	// first when edges are needed: normal/tangent conditions, Neumann loads)
 	bool need_edges = false;
@@ -2039,7 +2420,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	a.first = P->first;
 	a.last = P->last;
 	a.vals64 = want64 ? P->vals64 : nullptr;
-	a.vals32 = want32 ? P->vals32 : nullptr;
+	a.vals32 = want32 || fp64_ssor ? P->vals32 : nullptr;
 	a.corr32 = want32 ? P->corr32 : nullptr;
 	a.vals32lo = dfp ? P->vals32lo : nullptr;
 	a.srow_df = dfp ? P->srow_df : nullptr;
@@ -2052,7 +2433,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		// (the FP32 element integration is planar only: axisymmetric
 		// mixed-precision solves round the exact FP64 values)
 		k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
-		if (dfp) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32, P->precond != BFM_GPU_PC_JACOBI);
+		if (dfp || fp64_ssor) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32, P->precond != BFM_GPU_PC_JACOBI);
 	}
 	else {
 		if (!P->coords32 && dalloc(&P->coords32, N)) return -1;
@@ -2119,7 +2500,9 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	if (opts) o = *opts;
 	else bfm_gpu_default_opts(&o);
 	if (!(o.rtol >= 0.0) || o.max_iters < 0) return fail("invalid solver options");
-	if (o.precond < BFM_GPU_PC_JACOBI || o.precond > BFM_GPU_PC_LEARNED) return fail("unknown preconditioner %d", o.precond);
+	if (o.precond < BFM_GPU_PC_JACOBI || o.precond > BFM_GPU_PC_LEARNED_SSOR) return fail("unknown preconditioner %d", o.precond);
+	if (ssor_pc(o.precond) && P->precision != BFM_GPU_FP64 && P->precision != BFM_GPU_FP64_DF)
+		return fail("the SSOR preconditioners run on the FP64 and FP64_DF paths");
 	if (o.precond != P->precond) {
 		// the preconditioner is formed by the assembly epilogue
 		P->precond = o.precond;
@@ -2141,11 +2524,12 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		P->graph_lpr = P->lpr;
 		P->graph_opts = o;
 	}
-	bool const learned = P->precond == BFM_GPU_PC_LEARNED;
+	bool const learned = P->precond == BFM_GPU_PC_LEARNED || P->precond == BFM_GPU_PC_LEARNED_SSOR;
 	P->fallback = 0;
 	CK(cudaEventRecord(P->ev[2], P->stream));
 	// the learned blocks depend on the load vector: formed for every solve, inside the timed region
 	if (learned && bfmi_learned_precond(P, 0)) return -1;
+	if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), P->stream));
 	CK(cudaGraphLaunch(P->graph, P->stream));
 	if (learned) {
 		// Jacobi takes over when the learned preconditioner breaks down (a non-SPD
@@ -2157,6 +2541,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		if (h->status == BFM_GPU_BREAKDOWN || !(rel == rel) ||
 		    (h->status == BFM_GPU_STAGNATED && rel > LEARNED_FALLBACK_REL)) {
 			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
+			if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), P->stream));
 			CK(cudaGraphLaunch(P->graph, P->stream));
 			P->fallback = 1;
 		}
@@ -2200,9 +2585,35 @@ int bfm_gpu_problem_stats(bfm_gpu_problem_t* P, bfm_gpu_stats_t* s) {
 
 int bfm_gpu_problem_solution(bfm_gpu_problem_t* P, double* out, int where) {
 	g_err[0] = 0;
-	CK(cudaMemcpyAsync(out, P->x, 2l * P->N * sizeof(double),
+	const double* x = P->x;
+	if (P->ordered) {
+		// back to the caller's node order
+		double* dst = where == BFM_GPU_DEVICE ? out : (double*) P->otmp;
+		k_gather_nodes<double><<<blocks_for(2l * P->N), TPB, 0, P->stream>>>(P->N, 2, P->x, P->iperm, dst);
+		CK(cudaGetLastError());
+		if (where == BFM_GPU_DEVICE) return 0;
+		x = dst;
+	}
+	CK(cudaMemcpyAsync(out, x, 2l * P->N * sizeof(double),
 	                   where == BFM_GPU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, P->stream));
 	if (where != BFM_GPU_DEVICE) CK(cudaStreamSynchronize(P->stream));
+	return 0;
+}
+
+int bfm_gpu_problem_ordering(bfm_gpu_problem_t* P, int32_t* perm, int32_t* color_offsets, int* n_colors) {
+	g_err[0] = 0;
+	bool const on = P->ordered != 0;
+	if (perm) {
+		if (on) {
+			CK(cudaMemcpyAsync(perm, P->perm, P->N * sizeof(int), cudaMemcpyDeviceToHost, P->stream));
+			CK(cudaStreamSynchronize(P->stream));
+		}
+		else
+			for (int i = 0; i < P->N; i++) perm[i] = i;
+	}
+	if (color_offsets && on)
+		for (int c = 0; c <= P->ncol; c++) color_offsets[c] = P->col_off[c];
+	if (n_colors) *n_colors = on ? P->ncol : 0;
 	return 0;
 }
 
@@ -2244,6 +2655,13 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 	g_err[0] = 0;
 	if (!P->assembled) return fail("assemble first");
 	return time_iteration(P, P->lpr, reps > 0 ? reps : 1, ms_spmv, ms_update);
+}
+
+int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* P, int reps, double* ms, int* persistent) {
+	g_err[0] = 0;
+	if (!P->assembled) return fail("assemble first");
+	if (persistent) *persistent = P->ssor_grid > 0;
+	return time_ssor(P, reps > 0 ? reps : 1, ms);
 }
 
 int bfm_gpu_problem_autotune(bfm_gpu_problem_t* P, int* lanes_per_row) {

@@ -54,6 +54,8 @@ static bfm_gpu_opts_t current_opts(void) {
 		char const* pc = getenv("BFM_GPU_PRECOND");
 		if (pc && (!strcmp(pc, "block") || !strcmp(pc, "1"))) t_opts.precond = BFM_GPU_PC_BLOCK_JACOBI;
 		if (pc && (!strcmp(pc, "learned") || !strcmp(pc, "2"))) t_opts.precond = BFM_GPU_PC_LEARNED;
+		if (pc && (!strcmp(pc, "ssor") || !strcmp(pc, "3"))) t_opts.precond = BFM_GPU_PC_SSOR;
+		if (pc && (!strcmp(pc, "learned_ssor") || !strcmp(pc, "4"))) t_opts.precond = BFM_GPU_PC_LEARNED_SSOR;
 		t_opts_set = 1;
 	}
 	return t_opts;
@@ -320,7 +322,7 @@ static int env_network(bfm_state_t* st) {
 static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	bfm_state_t* const st = sim->state;
 	bfm_gpu_opts_t const o = current_opts();
-	if (o.precond == BFM_GPU_PC_LEARNED && env_network(st) < 0) return -1;
+	if ((o.precond == BFM_GPU_PC_LEARNED || o.precond == BFM_GPU_PC_LEARNED_SSOR) && env_network(st) < 0) return -1;
 	bfm_gpu_problem_t* P = upload_and_assemble(st, sim, inst, stress, o.precision, o.precond);
 	if (!P) return -1;
 	if (bfm_gpu_problem_solve(P, &o) < 0) return REPORT(st, "%s", bfm_gpu_last_error());

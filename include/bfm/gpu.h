@@ -50,6 +50,15 @@ enum {
 	BFM_GPU_PC_JACOBI = 0,       /* diagonal                                   */
 	BFM_GPU_PC_BLOCK_JACOBI = 1, /* inverse of each node's 2x2 diagonal block  */
 	BFM_GPU_PC_LEARNED = 2,      /* message-passing network, flexible CG       */
+	/* Multicolour block symmetric Gauss-Seidel (SSOR with the 2x2 diagonal
+	 * blocks as relaxation blocks), swept colour by colour in FP32.  The
+	 * problem is then assembled and solved with its nodes renumbered colour
+	 * by colour (bfm_gpu_problem_ordering); bfm_gpu_problem_solution returns
+	 * the caller's order.  FP64 and FP64_DF precisions. */
+	BFM_GPU_PC_SSOR = 3,
+	/* The same sweeps with relaxation blocks from the message-passing
+	 * network (bfm_gpu_mpnn_use); block SSOR is its fallback. */
+	BFM_GPU_PC_LEARNED_SSOR = 4,
 };
 
 /* solver status codes (bfm_gpu_stats_t.status) */
@@ -172,7 +181,9 @@ int bfm_gpu_problem_n_blocks(bfm_gpu_problem_t* problem, int64_t* n_blocks);
 
 /* Inspection: copy the assembled system to the host.  row_ptr[n_nodes+1] and
  * cols[n_blocks] of the node-block pattern, vals[4*n_blocks] (FP64; FP32
- * entries widened in mixed precision) and b[2*n_nodes].  Any may be NULL. */
+ * entries widened in mixed precision) and b[2*n_nodes].  Any may be NULL.
+ * Like bfm_gpu_problem_apply, it works in the problem's working node order
+ * (bfm_gpu_problem_ordering). */
 int bfm_gpu_problem_download(bfm_gpu_problem_t* problem, int32_t* row_ptr, int32_t* cols, double* vals, double* b);
 
 /* Measurement hook: launch the CG's SpMV+dots kernel and its vector-update
@@ -232,6 +243,20 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t
  * and the tile shape used and the device time of the last solve. */
 int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int* status, int* replacements,
                                double* rel_residual, int* rows_per_tile, int* lanes_per_row, double* ms_solve);
+
+/* Mean duration (ms) of one application of an SSOR preconditioner (every
+ * sweep phase) over `reps` standalone launches on a scratch solver state;
+ * *persistent = 1 when the phases run as one cooperative kernel.  Needs a
+ * solve with BFM_GPU_PC_SSOR or BFM_GPU_PC_LEARNED_SSOR first (which forms
+ * the colour order); overwrites the Krylov vectors. */
+int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* problem, int reps, double* ms, int* persistent);
+
+/* Working node order of the last assembly: perm[w] = the caller's index of
+ * working node w (n_nodes ints, host memory; the identity unless an SSOR
+ * preconditioner renumbered the nodes colour by colour), and the colour
+ * ranges: the nodes of colour c are [color_offsets[c], color_offsets[c+1])
+ * (at most 65 ints; *n_colors = 0 for the caller's order).  Any may be NULL. */
+int bfm_gpu_problem_ordering(bfm_gpu_problem_t* problem, int32_t* perm, int32_t* color_offsets, int* n_colors);
 
 /* y = K x with the assembled FP64 operator (after Dirichlet elimination);
  * x and y are 2*n_nodes doubles in host or device memory (`where`).  Needs an

@@ -1,0 +1,176 @@
+"""Multicolour block SSOR on the GPU: the colour-major renumbering (a valid
+colouring, K and b permuted bit for bit, the solution back in the caller's
+order), the solve against the FP64 direct oracle in FP64 and double-float,
+the iteration count against the float64 restatement (oracle/ssor_ref.py), the
+learned relaxation blocks, and switching preconditioners on one problem."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import bfm_gb300
+from bfm_gb300 import api, learned as LN, meshgen as M
+from common import load, rel
+from oracle import oracle as O, ssor_ref as S
+
+pytestmark = pytest.mark.gpu
+
+
+def plate(nx=96, ny=24, seed=3):
+    return M.cfg_perforated(nx=nx, ny=ny, n_holes=40, seed=seed)
+
+
+def ordering(prob):
+    L = prob.lib
+    n = prob.n_nodes
+    perm = np.zeros(n, np.int32)
+    off = np.zeros(65, np.int32)
+    nc = C.c_int()
+    assert L.bfm_gpu_problem_ordering(prob.P, perm.ctypes.data, off.ctypes.data, C.byref(nc)) == 0
+    return perm, off[:nc.value + 1], nc.value
+
+
+def scalar(rp, cols, vals, n):
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    R_ = np.repeat(2 * rows, 4) + np.tile([0, 0, 1, 1], len(cols))
+    C_ = np.repeat(2 * cols, 4) + np.tile([0, 1, 0, 1], len(cols))
+    return sp.csr_matrix((vals.reshape(-1), (R_, C_)), shape=(2 * n, 2 * n))
+
+
+@pytest.fixture(scope="module")
+def problem(libbfm):
+    p = plate()
+    prob = LN.DeviceProblem(p)
+    yield p, prob
+    prob.close()
+
+
+def test_colour_order_and_permuted_system(problem):
+    p, prob = problem
+    prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-8)
+    rp0, c0, v0, b0 = prob.download()
+    perm0, _, nc0 = ordering(prob)
+    assert nc0 == 0 and np.array_equal(perm0, np.arange(p.n_nodes))
+    s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+    assert s.status == 0
+    perm, off, nc = ordering(prob)
+    assert 2 <= nc <= 8 and off[0] == 0 and off[-1] == p.n_nodes
+    assert np.array_equal(np.sort(perm), np.arange(p.n_nodes))
+    K0 = scalar(rp0, c0, v0, p.n_nodes)
+    # a colouring, up to the nodes of small classes folded into large ones (at most 1%)
+    assert S.conflicts(S.node_graph(K0, p.n_nodes), perm, off) <= p.n_nodes // 100
+    # ascending caller index inside every colour
+    for c in range(nc):
+        assert np.all(np.diff(perm[off[c]:off[c + 1]]) > 0)
+    # the working system is P K P^T and P b, bit for bit
+    rp, cols, vals, b = prob.download()
+    dperm = np.stack([2 * perm, 2 * perm + 1], 1).ravel()
+    K = scalar(rp, cols, vals, p.n_nodes)
+    assert (K != K0[dperm][:, dperm]).nnz == 0
+    assert np.array_equal(b, b0[dperm])
+    # every row: lower-colour blocks, the diagonal, higher-colour blocks
+    rows = np.repeat(np.arange(p.n_nodes), np.diff(rp))
+    assert np.all(np.diff(cols)[np.diff(rows) == 0] > 0)
+
+
+@pytest.mark.parametrize("precision,tol", [(bfm_gb300.FP64, 1e-10), (bfm_gb300.FP64_DF, 1e-8)])
+def test_ssor_solve_matches_direct_oracle(libbfm, precision, tol):
+    p = plate(seed=5)
+    prob = LN.DeviceProblem(p, precision=precision)
+    try:
+        sj = prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-10)
+        s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-10)
+        assert s.status == 0 and s.rel_residual <= 1e-10
+        x, _, _ = O.solve_direct(p)
+        assert rel(prob.solution(), x) < tol
+        # the point of it: well under half of Jacobi's iterations
+        assert s.iterations < 0.5 * sj.iterations, (s.iterations, sj.iterations)
+    finally:
+        prob.close()
+
+
+def test_iterations_match_the_restatement(problem):
+    """FP64 CG with the FP32 sweeps vs float64 CG with the float64
+    restatement of the same preconditioner (same colouring): the counts agree
+    within the FP32 sweeps' few per cent."""
+    p, prob = problem
+    s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+    perm, off, _ = ordering(prob)
+    K, b = O.assemble_csr(p)
+    pc = S.BlockSSOR(K, perm, off)
+    x, it = S.pcg(sp.csr_matrix(K), b, pc.apply, rtol=1e-8)
+    assert abs(s.iterations - it) <= max(3, 0.1 * it), (s.iterations, it)
+    assert rel(prob.solution(), x) < 1e-6
+
+
+def test_untrained_learned_ssor_is_block_ssor(libbfm):
+    p = plate(seed=7)
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    net = LN.Network(seed=0)
+    try:
+        net.use()
+        s0 = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+        x0 = prob.solution()
+        s1 = prob.solve(precond=bfm_gb300.PC_LEARNED_SSOR, rtol=1e-8)
+        assert s1.status == 0 and s1.fallback == 0 and s1.iterations == s0.iterations
+        np.testing.assert_array_equal(prob.solution(), x0)
+    finally:
+        net.close()
+        prob.close()
+
+
+def test_nan_network_falls_back_to_block_ssor(libbfm):
+    p = plate(seed=8)
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    net = LN.Network(seed=0)
+    try:
+        th = net.weights()
+        th[-1] = np.nan
+        net.set_weights(th)
+        net.use()
+        s0 = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+        s1 = prob.solve(precond=bfm_gb300.PC_LEARNED_SSOR, rtol=1e-8)
+        assert s1.fallback == 1 and s1.status == 0 and s1.iterations == s0.iterations
+    finally:
+        net.close()
+        prob.close()
+
+
+def test_switching_back_restores_the_caller_order(problem):
+    p, prob = problem
+    s1 = prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-8)
+    x1 = prob.solution()
+    prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+    s2 = prob.solve(precond=bfm_gb300.PC_JACOBI, rtol=1e-8)
+    assert ordering(prob)[2] == 0
+    assert s2.iterations == s1.iterations
+    np.testing.assert_array_equal(prob.solution(), x1)
+
+
+def test_mixed_precision_is_refused(libbfm):
+    prob = LN.DeviceProblem(plate(32, 8), precision=bfm_gb300.MIXED)
+    try:
+        o = bfm_gb300.default_opts(precond=bfm_gb300.PC_SSOR)
+        assert libbfm.bfm_gpu_problem_solve(prob.P, C.byref(o)) == -1
+        assert "SSOR" in bfm_gb300.last_error()
+    finally:
+        prob.close()
+
+
+@pytest.mark.parametrize("name", ["p1_16x8_nt", "q1_24x8_jitter", "axi_p1_12x8"])
+def test_sim_run_with_ssor(libbfm, name, monkeypatch):
+    """Through bfm_sim_run (BFM_GPU_PRECOND=ssor): all condition kinds, Q1,
+    and the axisymmetric element, against the FP64 direct oracle."""
+    monkeypatch.setenv("BFM_GPU_AXISYM_REFERENCE", "0")
+    p, _ = load(name)
+    if p.stress == 3:
+        p.stress = 2
+    libbfm.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=1e-12, precond=bfm_gb300.PC_SSOR)))
+    try:
+        h = api.SimHandle.from_problem(libbfm, p)
+        assert h.run() == 0, h.error()
+        x, _, _ = O.solve_direct(p)
+        assert rel(h.effects(), x) < 1e-9
+    finally:
+        libbfm.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
