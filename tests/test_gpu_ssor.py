@@ -90,18 +90,24 @@ def test_ssor_solve_matches_direct_oracle(libbfm, precision, tol):
         prob.close()
 
 
-def test_iterations_match_the_restatement(problem):
-    """FP64 CG with the FP32 sweeps vs float64 CG with the float64
-    restatement of the same preconditioner (same colouring): the counts agree
-    within the FP32 sweeps' few per cent."""
-    p, prob = problem
-    s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
-    perm, off, _ = ordering(prob)
-    K, b = O.assemble_csr(p)
-    pc = S.BlockSSOR(K, perm, off)
-    x, it = S.pcg(sp.csr_matrix(K), b, pc.apply, rtol=1e-8)
-    assert abs(s.iterations - it) <= max(3, 0.1 * it), (s.iterations, it)
-    assert rel(prob.solution(), x) < 1e-6
+@pytest.mark.parametrize("precision", [bfm_gb300.FP64, bfm_gb300.FP64_DF])
+def test_iterations_match_the_restatement(libbfm, precision):
+    """CG with the GPU's sweeps (FP64: standard form; double-float:
+    Eisenstat's form) vs float64 CG with the float64 restatement of the same
+    preconditioner (same colouring): the counts agree within a few per cent."""
+    p = plate(seed=4)
+    prob = LN.DeviceProblem(p, precision=precision)
+    try:
+        s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+        assert s.status == 0
+        perm, off, _ = ordering(prob)
+        K, b = O.assemble_csr(p)
+        pc = S.BlockSSOR(K, perm, off)
+        x, it = S.pcg(sp.csr_matrix(K), b, pc.apply, rtol=1e-8)
+        assert abs(s.iterations - it) <= max(3, 0.1 * it), (s.iterations, it)
+        assert rel(prob.solution(), x) < 1e-6
+    finally:
+        prob.close()
 
 
 def test_untrained_learned_ssor_is_block_ssor(libbfm):
