@@ -1330,27 +1330,28 @@ __device__ __forceinline__ void ssor_blk(float4 d, dfl s0, dfl s1, dfl& o0, dfl&
 
 // sum of A_ij v_j over blocks [k0, k1) of the row whose column lies in
 // [cmin, cmax), v double-float float4 per node (written by other blocks of
-// the persistent kernel: read past L1).  Four blocks at a time: their column
-// indices and values are loaded together, then their four gathers, so a row
-// costs two dependent memory trips instead of two per block.
+// the persistent kernel: read past L1).  SSOR_CHUNK blocks at a time: their
+// column indices and values are loaded together, then their gathers.
+constexpr int SSOR_CHUNK = 2;  // with 8 resident blocks per SM (32 registers)
+
 __device__ __forceinline__ void ssor_row(const SsorArgs& a, int k0, int k1, int cmin, int cmax, dfl& t0, dfl& t1) {
-	for (int kb = k0; kb < k1; kb += 4) {
-		int c[4];
-		float4 m[4];
+	for (int kb = k0; kb < k1; kb += SSOR_CHUNK) {
+		int c[SSOR_CHUNK];
+		float4 m[SSOR_CHUNK];
 #pragma unroll
-		for (int j = 0; j < 4; j++) {
+		for (int j = 0; j < SSOR_CHUNK; j++) {
 			bool const in = kb + j < k1;
 			c[j] = in ? a.cols[kb + j] : -1;
 			m[j] = in ? reinterpret_cast<const float4*>(a.hi)[kb + j] : make_float4(0.f, 0.f, 0.f, 0.f);
 		}
-		float4 g[4];
+		float4 g[SSOR_CHUNK];
 #pragma unroll
-		for (int j = 0; j < 4; j++) {
+		for (int j = 0; j < SSOR_CHUNK; j++) {
 			bool const use = c[j] >= cmin && c[j] < cmax;
 			g[j] = use ? __ldcg(reinterpret_cast<const float4*>(a.y) + c[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
 		}
 #pragma unroll
-		for (int j = 0; j < 4; j++) {
+		for (int j = 0; j < SSOR_CHUNK; j++) {
 			dfl const g0 = {g[j].x, g[j].z}, g1 = {g[j].y, g[j].w};
 			t0 = df_add(t0, df_add(df_mul_f(m[j].x, g0), df_mul_f(m[j].y, g1)));
 			t1 = df_add(t1, df_add(df_mul_f(m[j].z, g0), df_mul_f(m[j].w, g1)));
@@ -1503,7 +1504,7 @@ __device__ bool ssor_barrier(const SsorArgs& a) {
 }
 
 template <bool DF>
-__global__ void __launch_bounds__(TPB_K) k_ssor_all(SsorArgs a) {
+__global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 	if (a.st->done && !a.timing) return;
 	int const nc = a.ncol > 0 ? a.ncol : 1;
 	dfl acc = {0.f, 0.f};

@@ -9,9 +9,9 @@ definition so the GPU sweeps can be checked against it:
     M = (D~ + L) D~^-1 (D~ + U),   A = L + D + U
 
 in a colour-major node order (L: the 2x2 blocks of lower-colour neighbours,
-U: higher-colour ones; couplings inside a colour range, which small classes
-folded into larger ones leave behind, belong to neither), D~ the relaxation
-blocks.  Only tests import it.
+U: higher-colour ones; a coupling inside a colour range, which a valid
+colouring does not have, would belong to neither), D~ the relaxation blocks.
+Only tests import it.
 """
 from __future__ import annotations
 
