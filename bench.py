@@ -197,22 +197,26 @@ def run_gpu(args, rank: int, world: int):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     methods = {k: (getattr(bfm_gb300, a), getattr(bfm_gb300, b)) for k, (a, b) in METHODS.items()}
-    net = None
+    # the networks: block-Jacobi blocks, and SSOR relaxation blocks (each
+    # trained in its own context)
     from bfm_gb300 import learned
-    if learned.WEIGHTS.exists():
-        net = learned.Network(path=learned.WEIGHTS)
-        net.use()
+    nets = {pc: learned.Network(path=w) for pc, w in ((bfm_gb300.PC_LEARNED, learned.WEIGHTS),
+                                                    (bfm_gb300.PC_LEARNED_SSOR, learned.WEIGHTS_SSOR)) if w.exists()}
     if args.method == "best":
-        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed", "ssor_fp64", "ssor_df"] + (
-            ["learned_fp64", "learned_df", "learned_mixed", "learned_ssor_df"] if net else [])
+        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed", "ssor_fp64", "ssor_df"] + \
+            (["learned_fp64", "learned_df", "learned_mixed"] if bfm_gb300.PC_LEARNED in nets else []) + \
+            (["learned_ssor_df"] if bfm_gb300.PC_LEARNED_SSOR in nets else [])
     else:
         chosen = args.method.split(",")
-        if any(methods[m][1] in (bfm_gb300.PC_LEARNED, bfm_gb300.PC_LEARNED_SSOR) for m in chosen) and net is None:
-            raise SystemExit(f"{learned.WEIGHTS} is missing: train it with python -m bfm_gb300.learned")
+        for m in chosen:
+            if methods[m][1] in (bfm_gb300.PC_LEARNED, bfm_gb300.PC_LEARNED_SSOR) and methods[m][1] not in nets:
+                raise SystemExit(f"the weights of {m} are missing: train them with python -m bfm_gb300.learned")
     results = {}
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
     for m in chosen:
         prec, pc = methods[m]
+        if pc in nets:
+            nets[pc].use()
         o = bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc, replace_drop=REPLACE_DROP[METHODS[m][0]])
 
         def step():
@@ -265,6 +269,8 @@ def run_gpu(args, rank: int, world: int):
     # end-to-end through bfm_sim_run with host buffers (the learned methods use
     # the network selected above through the same global options)
     prec, pc = methods[best]
+    if pc in nets:
+        nets[pc].use()
     lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc,
                                                         replace_drop=REPLACE_DROP[METHODS[best][0]])))
     h = api.SimHandle.from_problem(lib, p)
@@ -279,8 +285,8 @@ def run_gpu(args, rank: int, world: int):
         (0 if p.elem_E is None else 8 * p.n_elems)
     d2h = p.n_dof * 8
     lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
-    if net is not None:
-        net.close()
+    for n_ in nets.values():
+        n_.close()
     return p, results, best, dict(ms=e2e_ms, h2d=h2d, d2h=d2h)
 
 

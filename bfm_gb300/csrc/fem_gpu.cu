@@ -2258,6 +2258,11 @@ int bfmi_buffers(bfm_gpu_problem_t* P, bfmi_buffers_t* o) {
 	o->x = P->x;
 	for (int i = 0; i < 5; i++) o->vec[i] = P->vec[i];
 	o->stream = (void*) P->stream;
+	if (P->ordered) {
+		o->ncol = P->ncol;
+		for (int c = 0; c <= P->ncol && c < 65; c++) o->col_off[c] = P->col_off[c];
+		o->dpos = P->dpos;
+	}
 	return 0;
 }
 

@@ -25,6 +25,13 @@ typedef struct {
 	double* x;
 	void* vec[5];
 	void* stream;
+	/* colour-major order of the SSOR preconditioners (ncol = 0: caller's order):
+	 * colour c holds the working rows [col_off[c], col_off[c + 1]), and every
+	 * row's blocks before dpos[i] are lower-colour neighbours, after it the
+	 * diagonal block and then higher-colour ones */
+	int ncol;
+	int col_off[65];
+	const int* dpos;
 } bfmi_buffers_t;
 
 /* Mesh-side device arrays of a problem (read only). */

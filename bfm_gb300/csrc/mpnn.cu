@@ -349,8 +349,44 @@ struct LossArgs {
 	const double* v;   // power vector
 	double* partials;
 	unsigned* ticket;
-	double* sc;  // v.Kv, sum v.B^-1 v, e.Ke, sum e.B^-1 e, loss, v.v
+	double* sc;  // v.Kv, Q(v), e.Ke, Q(e), loss, v.v
+	// SSOR context (the problem in colour-major order, B the relaxation
+	// block inverses): M = (B^-1 + L) B (B^-1 + U) and
+	//     Q(x) = x.M x = sum_i (x_i.B_i^-1 x_i + u_i.B_i u_i) + 2 x.L x,
+	// u_i = sum over higher-colour neighbours A_ij x_j; with s = L_i^T u_i,
+	// u_i.B_i u_i = s.(I + C_i) s and d/dC = s s^T.  Otherwise Q(x) = x.B^-1 x.
+	int ssor;
 };
+
+// lower- and higher-colour parts of row i of A x (colour-major order: a
+// column below i is a lower colour)
+__device__ __forceinline__ void lu_parts(const LossArgs& a, const double* x, int i, double& l0, double& l1, double& u0,
+                                         double& u1) {
+	l0 = l1 = u0 = u1 = 0.0;
+	for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; k++) {
+		int const c = a.cols[k];
+		if (c == i) continue;
+		double2 const xv = ld2(x, c);
+		const double* m = a.vals64 + 4l * k;
+		double const y0 = m[0] * xv.x + m[1] * xv.y, y1 = m[2] * xv.x + m[3] * xv.y;
+		if (c < i) {
+			l0 += y0;
+			l1 += y1;
+		}
+		else {
+			u0 += y0;
+			u1 += y1;
+		}
+	}
+}
+
+// s = L_i^T u and s.(I + C) s
+__device__ __forceinline__ double b_quad(const double* lf, double c0, double c1, double c2, double u0, double u1, double& s0,
+                                         double& s1) {
+	s0 = lf[0] * u0 + lf[1] * u1;
+	s1 = lf[2] * u1;
+	return s0 * s0 + s1 * s1 + c0 * s0 * s0 + 2.0 * c1 * s0 * s1 + c2 * s1 * s1;
+}
 
 // x_i.B_i^-1 x_i and w = (I + C_i)^-1 L_i^-1 x_i
 __device__ __forceinline__ double binv_quad(const double* lf, double c0, double c1, double c2, double x0, double x1,
@@ -373,7 +409,7 @@ __device__ __forceinline__ void node_c(const float* o, int i, double& c0, double
 	c2 = C_SCALE * tanh((double) o[3 * i + 2]);
 }
 
-// one power step: out = B (K in)
+// one power step: out = B (K in) (blocks == nullptr: out = K in)
 __global__ void k_power(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, const double* __restrict__ vals,
                         const double* __restrict__ blocks, const double* __restrict__ vin, double* __restrict__ vout) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -385,8 +421,50 @@ __global__ void k_power(int N, const int* __restrict__ row_ptr, const int* __res
 		y0 += m[0] * x.x + m[1] * x.y;
 		y1 += m[2] * x.x + m[3] * x.y;
 	}
+	if (!blocks) {
+		st2(vout, i, y0, y1);
+		return;
+	}
 	const double* B = blocks + 4l * i;
 	st2(vout, i, B[0] * y0 + B[1] * y1, B[2] * y0 + B[3] * y1);
+}
+
+// SSOR power step, after t = K v: forward sweep of colour range [lo, hi),
+// v_i = B_i (t_i - sum_L A_ij v_j) (rows of one colour are independent)
+__global__ void k_pssor_fwd(int lo, int hi, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+                            const double* __restrict__ vals, const double* __restrict__ blocks, const double* __restrict__ t,
+                            double* __restrict__ v) {
+	int const i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= hi) return;
+	double s0 = t[2l * i], s1 = t[2l * i + 1];
+	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+		int const c = cols[k];
+		if (c >= lo) break;
+		const double* m = vals + 4l * k;
+		s0 -= m[0] * v[2l * c] + m[1] * v[2l * c + 1];
+		s1 -= m[2] * v[2l * c] + m[3] * v[2l * c + 1];
+	}
+	const double* B = blocks + 4l * i;
+	v[2l * i] = B[0] * s0 + B[1] * s1;
+	v[2l * i + 1] = B[2] * s0 + B[3] * s1;
+}
+
+// backward sweep of [lo, hi): v_i -= B_i sum_U A_ij v_j
+__global__ void k_pssor_bwd(int lo, int hi, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+                            const double* __restrict__ vals, const double* __restrict__ blocks, double* __restrict__ v) {
+	int const i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= hi) return;
+	double s0 = 0.0, s1 = 0.0;
+	for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+		int const c = cols[k];
+		if (c < hi) continue;
+		const double* m = vals + 4l * k;
+		s0 += m[0] * v[2l * c] + m[1] * v[2l * c + 1];
+		s1 += m[2] * v[2l * c] + m[3] * v[2l * c + 1];
+	}
+	const double* B = blocks + 4l * i;
+	v[2l * i] -= B[0] * s0 + B[1] * s1;
+	v[2l * i + 1] -= B[2] * s0 + B[3] * s1;
 }
 
 // v.v into sc[5]; then v /= |v| (the loss and its gradient do not depend on v's scale)
@@ -425,6 +503,13 @@ __global__ void k_loss_terms(LossArgs a) {
 		v[1] += binv_quad(a.lfac + 3l * i, c0, c1, c2, vv.x, vv.y, w0, w1);
 		v[2] += ee.x * rr.x + ee.y * rr.y;
 		v[3] += binv_quad(a.lfac + 3l * i, c0, c1, c2, ee.x, ee.y, w0, w1);
+		if (a.ssor) {
+			double l0, l1, u0, u1, s0, s1;
+			lu_parts(a, a.v, i, l0, l1, u0, u1);
+			v[1] += b_quad(a.lfac + 3l * i, c0, c1, c2, u0, u1, s0, s1) + 2.0 * (vv.x * l0 + vv.y * l1);
+			lu_parts(a, a.e, i, l0, l1, u0, u1);
+			v[3] += b_quad(a.lfac + 3l * i, c0, c1, c2, u0, u1, s0, s1) + 2.0 * (ee.x * l0 + ee.y * l1);
+		}
 	}
 	double out[4];
 	if (grid_sum<4>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
@@ -443,9 +528,20 @@ __global__ void k_loss_back(LossArgs a, float* __restrict__ d_o) {
 	double2 const vv = ld2(a.v, i), ee = ld2(a.e, i);
 	binv_quad(a.lfac + 3l * i, c0, c1, c2, vv.x, vv.y, a0, a1);
 	binv_quad(a.lfac + 3l * i, c0, c1, c2, ee.x, ee.y, b0, b1);
-	double const dc0 = a0 * a0 / qv - b0 * b0 / qe;
-	double const dc1 = 2.0 * (a0 * a1 / qv - b0 * b1 / qe);
-	double const dc2 = a1 * a1 / qv - b1 * b1 / qe;
+	double dc0 = a0 * a0 / qv - b0 * b0 / qe;
+	double dc1 = 2.0 * (a0 * a1 / qv - b0 * b1 / qe);
+	double dc2 = a1 * a1 / qv - b1 * b1 / qe;
+	if (a.ssor) {
+		// dQ/dC of the u.B u terms is + s s^T, so they enter with the opposite sign
+		double l0, l1, u0, u1, p0, p1, q0, q1;
+		lu_parts(a, a.v, i, l0, l1, u0, u1);
+		b_quad(a.lfac + 3l * i, c0, c1, c2, u0, u1, p0, p1);
+		lu_parts(a, a.e, i, l0, l1, u0, u1);
+		b_quad(a.lfac + 3l * i, c0, c1, c2, u0, u1, q0, q1);
+		dc0 += -p0 * p0 / qv + q0 * q0 / qe;
+		dc1 += 2.0 * (-p0 * p1 / qv + q0 * q1 / qe);
+		dc2 += -p1 * p1 / qv + q1 * q1 / qe;
+	}
 	double const t0 = c0 / C_SCALE, t1 = c1 / C_SCALE, t2 = c2 / C_SCALE;
 	d_o[3 * i + 0] = (float) (dc0 * C_SCALE * (1.0 - t0 * t0));
 	d_o[3 * i + 1] = (float) (dc1 * C_SCALE * (1.0 - t1 * t1));
@@ -733,11 +829,27 @@ int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const dou
 	bfmi_buffers(P, &bf);
 	if (!bf.vals64_any) return mfail("training needs the FP64 operator: assemble in FP64, MIXED_EXACT or FP64_DF");
 	int const N = bf.N;
-	// the power vector: v <- B K v, power_iters times (ping-pong through z),
-	// rescaled to unit length every 16 steps and at the end
+	// the power vector: v <- B K v (SSOR context: v <- M^-1 K v, the sweeps
+	// colour by colour in FP64), power_iters times, rescaled to unit length
+	// every 16 steps and at the end
+	bool const ssor = bf.ncol > 0 && (bf.precond == BFM_GPU_PC_SSOR || bf.precond == BFM_GPU_PC_LEARNED_SSOR);
 	for (int k = 0; k < power_iters; k++) {
-		k_power<<<nb(N), 256, 0, st>>>(N, bf.row_ptr, bf.cols, bf.vals64_any, net->blocks, v, net->z);
-		MCK(cudaMemcpyAsync(v, net->z, 2l * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+		if (ssor) {
+			k_power<<<nb(N), 256, 0, st>>>(N, bf.row_ptr, bf.cols, bf.vals64_any, nullptr, v, net->z);
+			for (int c = 0; c < bf.ncol; c++) {
+				int const lo = bf.col_off[c], hi = bf.col_off[c + 1];
+				if (hi > lo)
+					k_pssor_fwd<<<nb(hi - lo), 256, 0, st>>>(lo, hi, bf.row_ptr, bf.cols, bf.vals64_any, net->blocks, net->z, v);
+			}
+			for (int c = bf.ncol - 2; c >= 0; c--) {
+				int const lo = bf.col_off[c], hi = bf.col_off[c + 1];
+				if (hi > lo) k_pssor_bwd<<<nb(hi - lo), 256, 0, st>>>(lo, hi, bf.row_ptr, bf.cols, bf.vals64_any, net->blocks, v);
+			}
+		}
+		else {
+			k_power<<<nb(N), 256, 0, st>>>(N, bf.row_ptr, bf.cols, bf.vals64_any, net->blocks, v, net->z);
+			MCK(cudaMemcpyAsync(v, net->z, 2l * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+		}
 		if (k % 16 == 15 || k == power_iters - 1) {
 			k_vnorm<<<FEAT_GRID, TPB_K, 0, st>>>(N, v, net->partials, net->ticket, net->sc);
 			k_vscale<<<nb(N), 256, 0, st>>>(N, v, net->sc);
@@ -758,6 +870,7 @@ int backward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, const double* r, const dou
 	la.partials = net->partials;
 	la.ticket = net->ticket;
 	la.sc = net->sc;
+	la.ssor = ssor;
 	k_loss_terms<<<FEAT_GRID, TPB_K, 0, st>>>(la);
 	k_loss_back<<<nb(N), 256, 0, st>>>(la, net->d_o);
 	int const heads = (N + HEAD_NODES - 1) / HEAD_NODES > 0 ? (N + HEAD_NODES - 1) / HEAD_NODES : 1;

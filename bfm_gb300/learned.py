@@ -12,6 +12,9 @@ meshes.  The loss is the log of a condition-number estimate of the
 preconditioned operator B K: log R(v) - log R(e) with the Rayleigh quotient
 R(x) = (x.Kx) / (x.B^-1 x), v a power-iteration vector of B K kept per mesh,
 e the solver's error (smooth, so R(e) approaches the bottom of the spectrum).
+In the SSOR context (BFM_GPU_PC_LEARNED_SSOR) the blocks are the relaxation
+block inverses of the multicolour SSOR preconditioner M, the pairs come from
+SSOR-PCG solves, and x.B^-1 x becomes x.M x (mpnn.cu, k_loss_terms).
 
 Device memory for pairs is held in torch tensors (plumbing only): every
 computation is a library kernel.
@@ -28,10 +31,12 @@ from pathlib import Path
 
 import numpy as np
 
-from . import (DEVICE, FP64, PC_BLOCK_JACOBI, PC_JACOBI, PC_LEARNED, bfm_gpu_stats_t, default_opts, last_error, lib)
+from . import (DEVICE, FP64, PC_BLOCK_JACOBI, PC_JACOBI, PC_LEARNED, PC_LEARNED_SSOR, PC_SSOR, bfm_gpu_stats_t, default_opts,
+               last_error, lib)
 from . import meshgen as M
 
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "mpnn_plate.bin"
+WEIGHTS_SSOR = Path(__file__).resolve().parent / "weights" / "mpnn_ssor.bin"
 
 
 class DeviceProblem:
@@ -237,21 +242,40 @@ def concat(problems) -> M.Problem:
                      edge_loads=(np.concatenate([e for e, _ in loads]), np.concatenate([l for _, l in loads])))
 
 
-def pairs(prob: DeviceProblem, stops=(32, 64, 128, 256, 512, 1024, 2048), rtol: float = 1e-10):
-    """(r, e) device pairs (torch float64 tensors) from partial Jacobi-PCG solves."""
+def working_index(prob: DeviceProblem):
+    """Device index of the problem's working order per DOF (None for the
+    caller's order): x_working = x_caller[index]."""
+    import torch
+    perm = np.zeros(prob.n_nodes, np.int32)
+    nc = C.c_int(0)
+    assert prob.lib.bfm_gpu_problem_ordering(prob.P, perm.ctypes.data, None, C.byref(nc)) == 0, last_error()
+    if nc.value == 0:
+        return None
+    d = np.stack([2 * perm, 2 * perm + 1], 1).reshape(-1).astype(np.int64)
+    return torch.from_numpy(d).cuda()
+
+
+def pairs(prob: DeviceProblem, stops=(32, 64, 128, 256, 512, 1024, 2048), rtol: float = 1e-10, ssor: bool = False):
+    """(r, e) device pairs (torch float64 tensors) from partial PCG solves:
+    Jacobi, or with ssor the multicolour SSOR (vectors in the problem's
+    colour-major working order, as the loss kernels read them)."""
     import torch
     n = 2 * prob.n_nodes
-    st = prob.solve(precond=PC_JACOBI, rtol=rtol)
+    pc = PC_SSOR if ssor else PC_JACOBI
+    st = prob.solve(precond=pc, rtol=rtol)
     assert st.status in (0, 5), (st.status, last_error())
     xs = torch.empty(n, dtype=torch.float64, device="cuda")
     prob.solution(xs.data_ptr())
+    idx = working_index(prob) if ssor else None
     out = []
     for k in stops:
-        prob.solve(precond=PC_JACOBI, rtol=rtol, max_iters=k)
+        prob.solve(precond=pc, rtol=rtol, max_iters=k)
         xk = torch.empty(n, dtype=torch.float64, device="cuda")
         prob.solution(xk.data_ptr())
         torch.cuda.synchronize()
         e = xs - xk
+        if idx is not None:
+            e = e[idx].contiguous()
         if float(torch.linalg.vector_norm(e)) == 0.0:
             continue
         r = torch.empty_like(e)
@@ -263,17 +287,19 @@ def pairs(prob: DeviceProblem, stops=(32, 64, 128, 256, 512, 1024, 2048), rtol: 
 
 
 def train(net: Network, probs, n_pairs: int, lr: float = 3e-4, epochs: int = 1, seed: int = 0, log=None,
-          power_iters: int = 4, warm_power: int = 60):
+          power_iters: int = 4, warm_power: int = 60, ssor: bool = False):
     """Adam over the pairs of `probs` (a list of DeviceProblem); returns the
     mean loss of each epoch and the number of distinct pairs.  Each problem
     keeps its power-iteration vector: `warm_power` steps before training,
-    `power_iters` more at every training step on it."""
+    `power_iters` more at every training step on it.  ssor: train the
+    relaxation blocks of the SSOR preconditioner (the problems are left in
+    its colour order)."""
     import torch
     rng = np.random.default_rng(seed)
     gen = torch.Generator(device="cuda").manual_seed(seed)
     data, vecs = [], []
     for i, pr in enumerate(probs):
-        for r, e in pairs(pr):
+        for r, e in pairs(pr, ssor=ssor):
             data.append((i, r, e))
         v = torch.rand(2 * pr.n_nodes, dtype=torch.float64, device="cuda", generator=gen) - 0.5
         torch.cuda.synchronize()
@@ -299,14 +325,17 @@ def train(net: Network, probs, n_pairs: int, lr: float = 3e-4, epochs: int = 1, 
     return hist, len(data)
 
 
-def evaluate(net: Network, prob: DeviceProblem, rtol: float = 1e-8, precision: int | None = None):
+def evaluate(net: Network, prob: DeviceProblem, rtol: float = 1e-8, precision: int | None = None, ssor: bool = False):
     """Iterations and ms of Jacobi, block-Jacobi (the untrained network) and
-    learned PCG on one problem."""
+    learned PCG on one problem; ssor: Jacobi, block SSOR (the untrained
+    network) and learned SSOR."""
     if precision is not None and precision != prob.precision:
         prob.assemble(precision)
     net.use()
     res = {}
-    for name, pc in (("jacobi", PC_JACOBI), ("block_jacobi", PC_BLOCK_JACOBI), ("learned", PC_LEARNED)):
+    methods = ((("jacobi", PC_JACOBI), ("block_ssor", PC_SSOR), ("learned", PC_LEARNED_SSOR)) if ssor else
+               (("jacobi", PC_JACOBI), ("block_jacobi", PC_BLOCK_JACOBI), ("learned", PC_LEARNED)))
+    for name, pc in methods:
         s = prob.solve(precond=pc, rtol=rtol)
         res[name] = dict(iterations=s.iterations, status=s.status, fallback=s.fallback, ms=s.ms_solve,
                          rel_residual=s.rel_residual)
@@ -315,24 +344,28 @@ def evaluate(net: Network, prob: DeviceProblem, rtol: float = 1e-8, precision: i
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--out", default=str(WEIGHTS))
+    ap.add_argument("--context", choices=["jacobi", "ssor"], default="jacobi",
+                    help="blocks of the block-Jacobi preconditioner, or relaxation blocks of the multicolour SSOR")
+    ap.add_argument("--out", default=None, help="weights file (default: the package's file for the context)")
     ap.add_argument("--pairs", type=int, default=20000, help="training steps (one pair each)")
     ap.add_argument("--meshes", type=int, default=6, help="training meshes (each gives several pairs)")
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--seed", type=int, default=5)
     args = ap.parse_args(argv)
+    ssor = args.context == "ssor"
+    out = args.out or str(WEIGHTS_SSOR if ssor else WEIGHTS)
     import torch
     torch.cuda.init()
     t0 = time.time()
     meshes = training_meshes(args.seed, n_plates=args.meshes - args.meshes // 3, n_batch=args.meshes // 3)
     probs = [DeviceProblem(p) for p in meshes]
     net = Network(seed=args.seed)
-    hist, n_data = train(net, probs, args.pairs, lr=args.lr, seed=args.seed, log=print)
-    net.save(args.out)
+    hist, n_data = train(net, probs, args.pairs, lr=args.lr, seed=args.seed, log=print, ssor=ssor)
+    net.save(out)
     held = DeviceProblem(M.cfg_perforated(nx=512, ny=128, n_holes=200, seed=3))
-    ev = evaluate(net, held)
-    print(json.dumps({"pairs_distinct": n_data, "steps": args.pairs, "loss": hist, "held_out": ev,
-                      "seconds": round(time.time() - t0, 1), "out": args.out}))
+    ev = evaluate(net, held, ssor=ssor)
+    print(json.dumps({"context": args.context, "pairs_distinct": n_data, "steps": args.pairs, "loss": hist,
+                      "held_out": ev, "seconds": round(time.time() - t0, 1), "out": out}))
 
 
 if __name__ == "__main__":

@@ -21,6 +21,7 @@ the log of a condition-number estimate of the preconditioned operator.
 from __future__ import annotations
 
 import numpy as np
+import scipy.sparse as sp
 
 F_IN, H = 16, 64
 SHAPES = [(H, F_IN), (H,), (H, 2 * H), (H,), (H, 2 * H), (H,), (H, 2 * H), (H,), (3, H), (3,)]
@@ -113,20 +114,51 @@ def binv_quad(L, c, x2):
     return float(u0 @ w0 + u1 @ w1), np.stack([w0, w1], 1)
 
 
-def loss_and_grad(theta, f, rp, cols, K, Kd, r, e, v, emulate=False):
-    """Loss log R(v) - log R(e), R(x) = (x.Kx) / (x.B^-1 x), and d loss /
-    d theta (float64); r = K e; emulate as in forward (the back-propagated
-    signal entering each dense layer's GEMMs is BF16 too)."""
+def b_quad(L, c, u2):
+    """Per node s = L^T u, s.(I + C) s; returns (sum, s)."""
+    s0 = L[:, 0, 0] * u2[:, 0] + L[:, 1, 0] * u2[:, 1]
+    s1 = L[:, 1, 1] * u2[:, 1]
+    q = s0 * s0 + s1 * s1 + c[:, 0] * s0 * s0 + 2 * c[:, 1] * s0 * s1 + c[:, 2] * s1 * s1
+    return float(q.sum()), np.stack([s0, s1], 1)
+
+
+def lu_split(K, n):
+    """Strictly lower- and upper-node-block parts of K (scalar CSR, 2 DOFs per
+    node): in a colour-major order, the lower- and higher-colour couplings."""
+    Kc = sp.coo_matrix(K)
+    rn, cn = Kc.row // 2, Kc.col // 2
+    mk = lambda m: sp.csr_matrix((Kc.data[m], (Kc.row[m], Kc.col[m])), shape=K.shape)
+    return mk(cn < rn), mk(cn > rn)
+
+
+def loss_and_grad(theta, f, rp, cols, K, Kd, r, e, v, emulate=False, ssor=False):
+    """Loss log R(v) - log R(e), R(x) = (x.Kx) / Q(x), and d loss / d theta
+    (float64); r = K e; emulate as in forward (the back-propagated signal
+    entering each dense layer's GEMMs is BF16 too).  Q(x) = x.B^-1 x for the
+    block preconditioner B; with ssor (K in colour-major order, B the SSOR
+    relaxation block inverses) Q(x) = x.M x with
+    M = (B^-1 + L) B (B^-1 + U): per node x_i.B_i^-1 x_i + u_i.B_i u_i,
+    u = U x, plus 2 x.L x (bfm_gb300/csrc/mpnn.cu, k_loss_terms)."""
     q = bf16 if emulate else _id
     c, cache = forward(theta, f, rp, cols, emulate)
     n = len(c)
     L = chol_inv(Kd)
     Qv, wv = binv_quad(L, c, v.reshape(n, 2))
     Qe, we = binv_quad(L, c, e.reshape(n, 2))
-    loss = np.log(v @ (K @ v)) - np.log(Qv) - np.log(e @ r) + np.log(Qe)
     dc = np.stack([wv[:, 0] ** 2 / Qv - we[:, 0] ** 2 / Qe,
                    2 * (wv[:, 0] * wv[:, 1] / Qv - we[:, 0] * we[:, 1] / Qe),
                    wv[:, 1] ** 2 / Qv - we[:, 1] ** 2 / Qe], 1)
+    if ssor:
+        Lo, Up = lu_split(K, n)
+        qv2, sv = b_quad(L, c, (Up @ v).reshape(n, 2))
+        qe2, se = b_quad(L, c, (Up @ e).reshape(n, 2))
+        Qv = Qv + qv2 + 2 * v @ (Lo @ v)
+        Qe = Qe + qe2 + 2 * e @ (Lo @ e)
+        dc = np.stack([wv[:, 0] ** 2 - sv[:, 0] ** 2, 2 * (wv[:, 0] * wv[:, 1] - sv[:, 0] * sv[:, 1]),
+                       wv[:, 1] ** 2 - sv[:, 1] ** 2], 1) / Qv - \
+            np.stack([we[:, 0] ** 2 - se[:, 0] ** 2, 2 * (we[:, 0] * we[:, 1] - se[:, 0] * se[:, 1]),
+                      we[:, 1] ** 2 - se[:, 1] ** 2], 1) / Qe
+    loss = np.log(v @ (K @ v)) - np.log(Qv) - np.log(e @ r) + np.log(Qe)
     do = dc * C_SCALE * (1.0 - np.tanh(cache["o"]) ** 2)
     W0, b0, W1, b1, W2, b2, W3, b3, Wo, bo = unpack(theta)
     grads = [None] * 10

@@ -1,11 +1,13 @@
 """Learned block preconditioner on the GPU: features, forward pass, loss and
 gradients of the tensor-core kernels against the float64 oracle
-(oracle/mpnn_ref.py, with the GPU's BF16 rounding points emulated), Adam
-training, the solve with the learned blocks, the Jacobi fallback, and what a
-trained network gains over Jacobi-PCG."""
+(oracle/mpnn_ref.py, with the GPU's BF16 rounding points emulated) in the
+block-Jacobi and the SSOR contexts, Adam training, the solve with the learned
+blocks, the Jacobi fallback, and what a trained network gains over
+Jacobi-PCG."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
+import scipy.sparse.linalg  # noqa: F401 (sp.linalg)
 
 import bfm_gb300
 from bfm_gb300 import learned as LN, meshgen as M
@@ -252,3 +254,63 @@ def test_trained_network_beats_jacobi(libbfm):
         for q in probs:
             q.close()
         held.close()
+
+
+@pytest.fixture(scope="module")
+def ssor_setup(libbfm):
+    """A soft plate in the SSOR preconditioner's colour order, with one SSOR
+    training pair and a power vector of M^-1 K (40 steps, untrained network)."""
+    p = soft_plate(seed=14)
+    prob = LN.DeviceProblem(p)
+    net = LN.Network(seed=3)
+    r, e = LN.pairs(prob, stops=(64,), ssor=True)[0]
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    v = torch.rand(2 * p.n_nodes, dtype=torch.float64, device="cuda", generator=gen) - 0.5
+    torch.cuda.synchronize()
+    net.gradient(prob, r.data_ptr(), e.data_ptr(), v.data_ptr(), 40)
+    yield p, prob, net, (r, e, v)
+    net.close()
+    prob.close()
+
+
+def test_ssor_gradient_matches_oracle(ssor_setup):
+    """SSOR context (relaxation blocks): the loss x.M x terms and their
+    gradients on the GPU against oracle/mpnn_ref.py with ssor=True, the
+    matrix in the problem's colour-major working order."""
+    p, prob, net, (r, e, v) = ssor_setup
+    th = random_theta(net, 6)
+    init = net.weights()
+    net.set_weights(th)
+    try:
+        f_gpu, _, _ = net.forward(prob)
+        loss_gpu, g_gpu = net.gradient(prob, r.data_ptr(), e.data_ptr(), v.data_ptr(), 0)
+        rp, cols, vals, b = prob.download()
+        K = scalar_K(rp, cols, vals, p.n_nodes)
+        args = (th.astype(np.float64), f_gpu.astype(np.float64), rp, cols, K, diag_blocks(rp, cols, vals, p.n_nodes),
+                r.cpu().numpy(), e.cpu().numpy(), v.cpu().numpy())
+        loss_ref, g_ref, _ = R.loss_and_grad(*args, emulate=True, ssor=True)
+        assert abs(loss_gpu - loss_ref) <= 1e-4 * max(1.0, abs(loss_ref))
+        assert np.linalg.norm(g_gpu - g_ref) <= 2e-2 * np.linalg.norm(g_ref)
+        # a different objective from the block-Jacobi one
+        loss_j, _, _ = R.loss_and_grad(*args, emulate=True)
+        assert abs(loss_j - loss_ref) > 1e-3
+    finally:
+        net.set_weights(init)
+
+
+def test_ssor_power_vector_is_bounded_by_one(ssor_setup):
+    """With the untrained network (block SSOR, symmetric Gauss-Seidel) the
+    spectrum of M^-1 K lies in (0, 1] (M - K = L D^-1 U is semidefinite): the
+    power vector's Rayleigh quotient x.Kx / x.Mx is at most 1, and near the
+    top of the spectrum."""
+    p, prob, net, (r, e, v) = ssor_setup
+    loss, _ = net.gradient(prob, r.data_ptr(), e.data_ptr(), v.data_ptr(), 20)
+    rp, cols, vals, b = prob.download()
+    K = scalar_K(rp, cols, vals, p.n_nodes)
+    vv = v.cpu().numpy()
+    Lo, Up = R.lu_split(K, p.n_nodes)
+    Kd = diag_blocks(rp, cols, vals, p.n_nodes)
+    D = sp.block_diag(list(Kd), format="csr")
+    Mv = (D + Lo) @ sp.linalg.spsolve(D.tocsc(), (D + Up) @ vv)
+    ratio = (vv @ (K @ vv)) / (vv @ Mv)
+    assert 0.3 < ratio <= 1.0 + 1e-9

@@ -1,5 +1,6 @@
 """The learned preconditioner's CPU oracle (oracle/mpnn_ref.py) on its own:
-analytic gradients against central finite differences, the BF16 rounding
+analytic gradients against central finite differences (block-Jacobi and
+SSOR contexts), the losses against their definitions, the BF16 rounding
 helper against known values, and the blocks' SPD property."""
 import numpy as np
 
@@ -24,7 +25,11 @@ def test_param_count():
     assert R.N_PARAMS == 26051
 
 
-def test_gradient_matches_finite_differences():
+import pytest
+
+
+@pytest.mark.parametrize("ssor", [False, True])
+def test_gradient_matches_finite_differences(ssor):
     n = 24
     rp, cols = tiny_graph(n)
     rng = np.random.default_rng(1)
@@ -36,7 +41,7 @@ def test_gradient_matches_finite_differences():
     r = K @ e
     th = rng.normal(0, 0.3, R.N_PARAMS)
     args = (f, rp, cols, K, Kd, r, e, v)
-    loss, g, _ = R.loss_and_grad(th, *args)
+    loss, g, _ = R.loss_and_grad(th, *args, ssor=ssor)
     assert np.isfinite(loss)
     idx = rng.choice(R.N_PARAMS, 60, replace=False)
     h = 1e-6
@@ -44,7 +49,7 @@ def test_gradient_matches_finite_differences():
         tp, tm = th.copy(), th.copy()
         tp[k] += h
         tm[k] -= h
-        fd = (R.loss_and_grad(tp, *args)[0] - R.loss_and_grad(tm, *args)[0]) / (2 * h)
+        fd = (R.loss_and_grad(tp, *args, ssor=ssor)[0] - R.loss_and_grad(tm, *args, ssor=ssor)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(g).max()), (k, fd, g[k])
 
 
@@ -63,6 +68,26 @@ def test_loss_is_log_rayleigh_ratio():
         Binv[2 * i:2 * i + 2, 2 * i:2 * i + 2] = Kd[i]
     Rq = lambda x: (x @ K @ x) / (x @ Binv @ x)
     assert abs(loss - (np.log(Rq(v)) - np.log(Rq(e)))) < 1e-12
+
+
+def test_ssor_loss_is_log_rayleigh_ratio():
+    """SSOR context with c = 0: Q(x) = x.M x, M = (D + L) D^-1 (D + U) with
+    D the diagonal blocks, L / U the lower / upper node-block parts."""
+    n = 10
+    rp, cols = tiny_graph(n)
+    rng = np.random.default_rng(6)
+    K = spd(n, 7)
+    Kd = np.stack([K[2 * i:2 * i + 2, 2 * i:2 * i + 2] for i in range(n)])
+    th = np.zeros(R.N_PARAMS)
+    e, v = rng.normal(size=2 * n), rng.normal(size=2 * n)
+    loss, _, _ = R.loss_and_grad(th, rng.normal(size=(n, R.F_IN)), rp, cols, K, Kd, K @ e, e, v, ssor=True)
+    blk = np.kron(np.eye(n), np.ones((2, 2))) > 0
+    D = np.where(blk, K, 0.0)
+    Lo = np.where(blk, 0.0, np.tril(K))
+    Up = np.where(blk, 0.0, np.triu(K))
+    Mm = (D + Lo) @ np.linalg.inv(D) @ (D + Up)
+    Rq = lambda x: (x @ K @ x) / (x @ Mm @ x)
+    assert abs(loss - (np.log(Rq(v)) - np.log(Rq(e)))) < 1e-10
 
 
 def test_bf16_rounding():
