@@ -151,6 +151,57 @@ __device__ __forceinline__ void row_product(const int* __restrict__ cols, const 
 	}
 }
 
+// True residual of one block row, r = b - A x with the FP64 matrix, in
+// compensated arithmetic: every product split exactly by an FMA
+// (TwoProduct), the sums carried as (sum, error) pairs (TwoSum), the lanes'
+// pairs combined the same way, and b - (s + c) formed with a TwoSum.  An
+// FP64 residual carries an error near eps |A| |x|, which on the perforated
+// plates is a third of 1e-8 relative; computed this way it is accurate to
+// about eps |r|, so replacements and the convergence test see the residual
+// of the stored x rather than rounding noise.  Every lane must call it.
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+	s = __dadd_rn(a, b);
+	double const z = __dsub_rn(s, a);
+	e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, z)), __dsub_rn(b, z));
+}
+__device__ __forceinline__ void dd_acc(double& s, double& c, double a, double b) {
+	double const p = __dmul_rn(a, b);
+	double const pe = __fma_rn(a, b, -p);
+	double t, te;
+	two_sum(s, p, t, te);
+	s = t;
+	c = __dadd_rn(c, __dadd_rn(te, pe));
+}
+template <int LPR>
+__device__ __forceinline__ void residual_dd(const int* __restrict__ cols, const double* __restrict__ vals, int ks, int ke, int sub,
+                                            const double* __restrict__ x, double2 bb, double& r0, double& r1) {
+	double s0 = 0.0, c0 = 0.0, s1 = 0.0, c1 = 0.0;
+	for (int k = ks + sub; k < ke; k += LPR) {
+		double2 const g = ld2(x, cols[k]);
+		double m0, m1, m2, m3;
+		ld_block(vals, k, m0, m1, m2, m3);
+		dd_acc(s0, c0, m0, g.x);
+		dd_acc(s0, c0, m1, g.y);
+		dd_acc(s1, c1, m2, g.x);
+		dd_acc(s1, c1, m3, g.y);
+	}
+#pragma unroll
+	for (int o = LPR / 2; o; o >>= 1) {
+		double t, e;
+		two_sum(s0, __shfl_xor_sync(0xffffffffu, s0, o), t, e);
+		c0 = __dadd_rn(__dadd_rn(c0, __shfl_xor_sync(0xffffffffu, c0, o)), e);
+		s0 = t;
+		two_sum(s1, __shfl_xor_sync(0xffffffffu, s1, o), t, e);
+		c1 = __dadd_rn(__dadd_rn(c1, __shfl_xor_sync(0xffffffffu, c1, o)), e);
+		s1 = t;
+	}
+	double h, e;
+	two_sum(bb.x, -s0, h, e);
+	r0 = __dadd_rn(h, __dsub_rn(e, c0));
+	two_sum(bb.y, -s1, h, e);
+	r1 = __dadd_rn(h, __dsub_rn(e, c1));
+}
+
 // Same product with the loads batched: each lane first reads NB column
 // indices, then issues the NB neighbour gathers and the NB block loads, then
 // does the arithmetic, so NB independent memory chains are in flight per lane
@@ -529,9 +580,14 @@ __device__ __forceinline__ void residual_row(const CgArgs<V>& a, int row, int su
 		g0 = t.x - xi.x;
 		g1 = t.y - xi.y;
 	};
+	if (a.vals64) {
+		double2 const bb = ok ? ld2(a.b, row) : make_double2(0.0, 0.0);
+		residual_dd<LPR>(a.cols, a.vals64, ks, ke, sub, x, bb, e0, e1);
+		if (!ok) e0 = e1 = 0.0;
+		return;
+	}
 	double y0, y1;
-	if (a.vals64) row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gather, y0, y1);
-	else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, dgather, y0, y1);
+	row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, dgather, y0, y1);
 	e0 = e1 = 0.0;
 	if (ok) {
 		if (!a.vals64 && a.corr) {
@@ -904,11 +960,9 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
 	FOR_ROWS(LPR) {
 		bool const ok = row_ < a.N;
 		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
-		double y0, y1;
-		row_product<LPR, double>(a.cols, a.vals, ks, ke, sub_, gx, y0, y1);
+		double r0, r1;
+		residual_dd<LPR>(a.cols, a.vals, ks, ke, sub_, x, ok ? ld2(a.b, row_) : make_double2(0.0, 0.0), r0, r1);
 		if (ok && sub_ == 0) {
-			double2 const bb = ld2(a.b, row_);
-			double const r0 = bb.x - y0, r1 = bb.y - y1;
 			st2(a.r, row_, r0, r1);
 			v[0] += r0 * r0 + r1 * r1;
 			if (!a.no_pc) {
@@ -1068,11 +1122,9 @@ __global__ void __launch_bounds__(TPB_K) k_hsdf_replace(DfArgs a) {
 		int const row = base + threadIdx.x / LPR;
 		bool const ok = row < a.N;
 		int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
-		double y0, y1;
-		row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gx, y0, y1);
+		double e0, e1;
+		residual_dd<LPR>(a.cols, a.vals64, ks, ke, sub, x64, ok ? ld2(a.b, row) : make_double2(0.0, 0.0), e0, e1);
 		if (ok && sub == 0) {
-			double2 const bb = ld2(a.b, row);
-			double const e0 = bb.x - y0, e1 = bb.y - y1;
 			dfl const r0 = df_make(e0), r1 = df_make(e1);
 			df_st(a.r, row, r0, r1);
 			v[0] += e0 * e0 + e1 * e1;
@@ -1239,14 +1291,12 @@ __global__ void __launch_bounds__(TPB_K) k_df_switch(CgArgs<double> a, const flo
 	FOR_ROWS(1) {
 		bool const ok = row_ < a.N;
 		int const ks = ok ? a.row_ptr[row_] : 0, ke = ok ? a.row_ptr[row_ + 1] : 0;
-		double y0, y1;
-		row_product<1, double>(a.cols, a.vals, ks, ke, sub_, gx, y0, y1);
+		double r0, r1;
+		residual_dd<1>(a.cols, a.vals, ks, ke, sub_, x, ok ? ld2(a.b, row_) : make_double2(0.0, 0.0), r0, r1);
 		if (ok) {
 			dfl p0, p1;
 			df_ld(src, row_, p0, p1);
 			st2(a.p, row_, df_dbl(p0), df_dbl(p1));  // same 16 bytes per node when src is a.p
-			double2 const bb = ld2(a.b, row_);
-			double const r0 = bb.x - y0, r1 = bb.y - y1;
 			st2(a.r, row_, r0, r1);
 			v[0] += r0 * r0 + r1 * r1;
 			if (!a.no_pc) {

@@ -1964,8 +1964,9 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms) {
 	return 0;
 }
 
-// Project autotuner: time the SpMV kernel with 1, 2, 4, 8 and 16 lanes per
-// block row on this problem's matrix and keep the fastest.
+// Project autotuner: time every SpMV shape (lanes per block row, blocks in
+// flight per lane, split or fused direction) on this problem's matrix, 20
+// launches each, and keep the fastest.
 int autotune_lpr(bfm_gpu_problem* P) {
 	double best = 1e30;
 	int best_lpr = 8;
@@ -1973,7 +1974,7 @@ int autotune_lpr(bfm_gpu_problem* P) {
 	for (int lpr : SHAPES) {
 		if (mixed && shape_split(lpr)) continue;  // the mixed path has no split form
 		double t_spmv = 0, t_upd = 0;
-		if (time_iteration(P, lpr, 5, &t_spmv, &t_upd)) return -1;
+		if (time_iteration(P, lpr, 20, &t_spmv, &t_upd)) return -1;
 		if (t_spmv < best) {
 			best = t_spmv;
 			best_lpr = lpr;
@@ -2329,9 +2330,10 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	bool const dfp = precision == BFM_GPU_FP64_DF;
 	bool const want64 = precision != BFM_GPU_MIXED;  // FP64 values: the operator, or the residual operator
 	bool const want32 = precision != BFM_GPU_FP64;   // FP32 values: the mixed iteration operator / hi parts
+	// the preconditioner here is the last solve's: an SSOR one does not carry
+	// over to a precision without it (the next solve refuses SSOR there)
+	if (ssor_pc(P->precond) && precision != BFM_GPU_FP64 && !dfp) P->precond = BFM_GPU_PC_JACOBI;
 	bool const ssor = ssor_pc(P->precond);
-	if (ssor && precision != BFM_GPU_FP64 && !dfp)
-		return fail("the SSOR preconditioners run on the FP64 and FP64_DF paths");
 	bool const fp64_ssor = ssor && precision == BFM_GPU_FP64;  // FP32 blocks and relaxation blocks for the sweeps
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
