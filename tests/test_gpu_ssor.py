@@ -179,3 +179,35 @@ def test_sim_run_with_ssor(libbfm, name, monkeypatch):
         assert rel(h.effects(), x) < 1e-9
     finally:
         libbfm.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
+
+
+def test_colouring_is_reused_for_the_same_mesh(libbfm):
+    """Three colours on a triangle plate (DSATUR); uploading the same element
+    array again keeps the colouring, a different one makes a new one."""
+    p = plate(seed=9)
+    prob = LN.DeviceProblem(p)
+    try:
+        prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+        perm1, off1, nc1 = ordering(prob)
+        assert nc1 == 3
+        el = np.ascontiguousarray(p.elems, dtype=np.int32)
+        xy = np.ascontiguousarray(p.coords, dtype=np.float64)
+        assert libbfm.bfm_gpu_problem_set_geometry(prob.P, xy.ctypes.data, el.ctypes.data, 0) == 0
+        prob.assemble(bfm_gb300.FP64)
+        s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+        perm2, off2, _ = ordering(prob)
+        assert s.status == 0 and np.array_equal(perm1, perm2) and np.array_equal(off1, off2)
+        # flip the diagonal of one grid square: another graph, another colouring
+        el2 = el.copy()
+        el2[0], el2[1] = [el[0][0], el[0][1], el[1][2]], [el[0][1], el[0][2], el[1][2]]
+        assert libbfm.bfm_gpu_problem_set_geometry(prob.P, xy.ctypes.data, el2.ctypes.data, 0) == 0
+        prob.assemble(bfm_gb300.FP64)
+        s = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-8)
+        perm3, off3, _ = ordering(prob)
+        assert s.status == 0
+        p2 = M.Problem(p.name, 3, p.coords, el2, E=p.E, nu=p.nu, rho=p.rho, stress=p.stress, forces=p.forces,
+                       conds=p.conds, edges=p.edges, elem_E=p.elem_E)
+        K2, _ = O.assemble_csr(p2)
+        assert S.is_colouring(S.node_graph(sp.csr_matrix(K2), p.n_nodes), perm3, off3)
+    finally:
+        prob.close()
