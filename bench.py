@@ -1,7 +1,7 @@
 """Benchmark of the libbfm FEM hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                    [--workload perforated|q1] [--method fp64|mixed|best]
+                    [--workload perforated|q1|batch] [--method best|m1,m2,...] [--profile]
 
 Workload (default): the perforated plate -- 2048x512 P1 triangles, 1,051,137
 nodes, 2,102,274 DOF, 200 soft inclusions (E x 1e-3, seed 3), left edge
@@ -11,6 +11,12 @@ clamped, gravity, 1e6 Pa traction on the right edge, plane stress.  One step
 `e2e` is the same step through the reference-facing C API, bfm_sim_run, with
 host buffers: host->device upload of the mesh and conditions and
 device->host copy of the displacements are inside its timed region.
+
+Every method (precision x preconditioner, METHODS) is timed; the line reports
+the fastest one whose displacements agree with the FP64 solution to 1e-6, and
+`methods` lists them all.  `roofline` describes the dominant kernel of that
+method's iteration (the SSOR sweep kernel for the SSOR methods, with the SpMV in
+`roofline_spmv`; the SpMV otherwise).
 
 --impl reference times the reference's own algorithm (dense assembly, RCM,
 band LU), restated in oracle/ and run on the host cores, on bounded samples
@@ -59,6 +65,16 @@ SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md")
                 3: (329_563_136, "profiles/spmv_df_hs_perforated_2048x512.md"),
                 1: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md"),
                 2: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md")}
+# the same for one launch of the SSOR sweep kernel (double-float vectors)
+SSOR_TRAFFIC = (374_381_568, "profiles/ssor_sweeps_perforated_2048x512.md")
+
+
+def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int) -> int:
+    """One SSOR application: every off-diagonal block once (FP32 block + column
+    index, 20 B), and per node the row bounds and diagonal position (12 B), the
+    FP32 relaxation block (16 B), the residual in (16 B), z out (16 B) and the
+    sweep vector written once (12 B of its 16 B counted: 72 B in all)."""
+    return (n_blocks - n_nodes) * 20 + n_nodes * 72
 
 
 def max_over_ranks(x: float, world: int) -> float:
@@ -446,10 +462,31 @@ def main():
     # assembly (pattern, Dirichlet marks, element loop, loads: about 24 kernels),
     # solve init + 2 kernels per iteration + replacement kernels, finish;
     # the learned preconditioner adds its 12 inference kernels per solve
-    launches_per_step = 24 + 1 + 2 * r["iters"] + 2 * r["repl"] + 2 + (12 if r["pc"] in (2, 4) else 0)
-    if r["pc"] in (3, 4):
-        # the SSOR sweeps: 2 nc - 1 phases after the init, every update and every replacement
-        launches_per_step += (2 * r["ncol"] - 1) * (r["iters"] + r["repl"] + 1) + 3
+    per_iter = 3 if split else 2
+    ssor = r["pc"] in (3, 4)
+    if ssor:
+        # the SSOR sweeps after the init, every update and every replacement:
+        # one cooperative launch, or 2 nc - 1 colour phases
+        per_pc = 1 if r["persistent"] else 2 * r["ncol"] - 1
+    else:
+        per_pc = 0
+    launches_per_step = 24 + 1 + (per_iter + per_pc) * r["iters"] + (2 + per_pc) * r["repl"] + per_pc + 2 + \
+        (12 if r["pc"] in (2, 4) else 0)
+    spmv_roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                 "frac": round(achieved / hbm, 3), "traffic": traffic, "traffic_source": traffic_src,
+                 "kernel": kernel, "spmv_shape": r["shape"], "algorithmic_bytes": bytes_spmv,
+                 "kernel_ms": round(r["ms_spmv"], 5), "peak_source": peak_kind}
+    if ssor:
+        # the dominant kernel of an SSOR iteration is the sweep kernel
+        b_pc = algorithmic_bytes_ssor(nb, p.n_nodes)
+        a_pc = b_pc / (r["ms_precond"] * 1e-3) / 1e9
+        ok_tr = args.workload == "perforated" and r["persistent"] and r["prec"] == 3
+        roof = {"bound": "hbm", "achieved": round(a_pc, 1), "peak": hbm, "unit": "GB/s", "frac": round(a_pc / hbm, 3),
+                "traffic": SSOR_TRAFFIC[0] if ok_tr else None, "traffic_source": SSOR_TRAFFIC[1] if ok_tr else None,
+                "kernel": "k_ssor_all" if r["persistent"] else "k_ssor_fwd + k_ssor_bwd",
+                "algorithmic_bytes": b_pc, "kernel_ms": round(r["ms_precond"], 5), "peak_source": peak_kind}
+    else:
+        roof = spmv_roof
     value = r["ms"] / world
     line = {
         "metric": METRIC,
@@ -482,10 +519,8 @@ def main():
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 3), "traffic": traffic, "traffic_source": traffic_src,
-                     "kernel": kernel, "spmv_shape": r["shape"], "algorithmic_bytes": bytes_spmv,
-                     "kernel_ms": round(r["ms_spmv"], 5), "peak_source": peak_kind},
+        "roofline": roof,
+        **({"roofline_spmv": spmv_roof} if ssor else {}),
         "e2e": {"value": round(e2e["ms"], 3), "unit": "ms", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},
         "gpu_launches": launches_per_step * args.steps,
