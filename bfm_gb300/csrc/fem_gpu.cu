@@ -2466,6 +2466,10 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 			int nb = 0, dev = 0, coop = 0;
 			CK(cudaGetDevice(&dev));
 			CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+			// BFM_GPU_SSOR_PER_COLOUR=1: one launch per colour phase, as where the
+			// graph cannot hold a cooperative kernel node
+			char const* pcol = getenv("BFM_GPU_SSOR_PER_COLOUR");
+			if (pcol && pcol[0] == '1') coop = 0;
 			if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_ssor_all<true>, TPB, 0) == cudaSuccess &&
 			    nb > 0) {
 				int nb64 = 0;

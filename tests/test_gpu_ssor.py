@@ -163,10 +163,11 @@ def test_mixed_precision_is_refused(libbfm):
         prob.close()
 
 
-@pytest.mark.parametrize("name", ["p1_16x8_nt", "q1_24x8_jitter", "axi_p1_12x8"])
+@pytest.mark.parametrize("name", ["p1_16x8_nt", "q1_24x8_jitter", "axi_p1_12x8", "lepl8", "gear12"])
 def test_sim_run_with_ssor(libbfm, name, monkeypatch):
-    """Through bfm_sim_run (BFM_GPU_PRECOND=ssor): all condition kinds, Q1,
-    and the axisymmetric element, against the FP64 direct oracle."""
+    """Through bfm_sim_run with the SSOR preconditioner: all condition kinds,
+    Q1, the axisymmetric element and the reference's own unstructured meshes,
+    against the FP64 direct oracle."""
     monkeypatch.setenv("BFM_GPU_AXISYM_REFERENCE", "0")
     p, _ = load(name)
     if p.stress == 3:
@@ -211,3 +212,32 @@ def test_colouring_is_reused_for_the_same_mesh(libbfm):
         assert S.is_colouring(S.node_graph(sp.csr_matrix(K2), p.n_nodes), perm3, off3)
     finally:
         prob.close()
+
+
+@pytest.mark.parametrize("precision", [bfm_gb300.FP64, bfm_gb300.FP64_DF])
+def test_per_colour_kernels_match_the_persistent_kernel(libbfm, precision, monkeypatch):
+    """The per-colour launches (used where a graph cannot hold a cooperative
+    node) compute the same sweeps as the persistent kernel: same solution to
+    rounding, same iteration count to a couple of iterations (only the order
+    of the partial sums of (r, z) differs)."""
+    p = plate(seed=11)
+    prob = LN.DeviceProblem(p, precision=precision)
+    try:
+        s1 = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-10)
+        x1 = prob.solution()
+    finally:
+        prob.close()
+    monkeypatch.setenv("BFM_GPU_SSOR_PER_COLOUR", "1")
+    prob = LN.DeviceProblem(p, precision=precision)
+    try:
+        s2 = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-10)
+        persistent = C.c_int(-1)
+        t = C.c_double()
+        assert libbfm.bfm_gpu_problem_time_precond(prob.P, 2, C.byref(t), C.byref(persistent)) == 0
+        assert persistent.value == 0
+        x2 = prob.solution()
+    finally:
+        prob.close()
+    assert s1.status == 0 and s2.status == 0
+    assert abs(s1.iterations - s2.iterations) <= 2
+    assert rel(x2, x1) < 1e-9
