@@ -51,7 +51,9 @@ METHODS = {"fp64": ("FP64", "PC_JACOBI"), "fp64_df": ("FP64_DF", "PC_JACOBI"),
            "mixed_exact": ("MIXED_EXACT", "PC_JACOBI"), "mixed": ("MIXED", "PC_JACOBI"),
            "learned_fp64": ("FP64", "PC_LEARNED"), "learned_df": ("FP64_DF", "PC_LEARNED"),
            "learned_mixed": ("MIXED", "PC_LEARNED"), "ssor_fp64": ("FP64", "PC_SSOR"),
-           "ssor_df": ("FP64_DF", "PC_SSOR"), "learned_ssor_df": ("FP64_DF", "PC_LEARNED_SSOR")}
+           "ssor_df": ("FP64_DF", "PC_SSOR"), "learned_ssor_df": ("FP64_DF", "PC_LEARNED_SSOR"),
+           "ssor2_fp64": ("FP64", "PC_SSOR2"), "ssor2_df": ("FP64_DF", "PC_SSOR2"),
+           "learned_ssor2_df": ("FP64_DF", "PC_LEARNED_SSOR2")}
 # FP64 residual-replacement threshold per precision (the recurrence residual
 # must drop by this factor between replacements), from a sweep on the
 # 2048x512 perforated plate: FP64 is insensitive, the FP32-pipe paths converge
@@ -218,14 +220,17 @@ def run_gpu(args, rank: int, world: int):
     from bfm_gb300 import learned
     nets = {pc: learned.Network(path=w) for pc, w in ((bfm_gb300.PC_LEARNED, learned.WEIGHTS),
                                                     (bfm_gb300.PC_LEARNED_SSOR, learned.WEIGHTS_SSOR)) if w.exists()}
+    if bfm_gb300.PC_LEARNED_SSOR in nets:  # the relaxation blocks serve the two-level form too
+        nets[bfm_gb300.PC_LEARNED_SSOR2] = nets[bfm_gb300.PC_LEARNED_SSOR]
     if args.method == "best":
-        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed", "ssor_fp64", "ssor_df"] + \
+        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed", "ssor_fp64", "ssor_df", "ssor2_fp64", "ssor2_df"] + \
             (["learned_fp64", "learned_df", "learned_mixed"] if bfm_gb300.PC_LEARNED in nets else []) + \
-            (["learned_ssor_df"] if bfm_gb300.PC_LEARNED_SSOR in nets else [])
+            (["learned_ssor_df", "learned_ssor2_df"] if bfm_gb300.PC_LEARNED_SSOR in nets else [])
     else:
         chosen = args.method.split(",")
         for m in chosen:
-            if methods[m][1] in (bfm_gb300.PC_LEARNED, bfm_gb300.PC_LEARNED_SSOR) and methods[m][1] not in nets:
+            if methods[m][1] in (bfm_gb300.PC_LEARNED, bfm_gb300.PC_LEARNED_SSOR, bfm_gb300.PC_LEARNED_SSOR2) and \
+                    methods[m][1] not in nets:
                 raise SystemExit(f"the weights of {m} are missing: train them with python -m bfm_gb300.learned")
     results = {}
     P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
@@ -266,7 +271,7 @@ def run_gpu(args, rank: int, world: int):
         ncol = C.c_int(0)
         lib.bfm_gpu_problem_ordering(P, None, None, C.byref(ncol))
         t_pc, persist = C.c_double(0.0), C.c_int(0)
-        if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR):
+        if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR, bfm_gb300.PC_SSOR2, bfm_gb300.PC_LEARNED_SSOR2):
             assert lib.bfm_gpu_problem_time_precond(P, 20, C.byref(t_pc), C.byref(persist)) == 0, bfm_gb300.last_error()
         results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual, repl=s.replacements,
                           ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks, fallback=s.fallback,
@@ -301,7 +306,7 @@ def run_gpu(args, rank: int, world: int):
         (0 if p.elem_E is None else 8 * p.n_elems)
     d2h = p.n_dof * 8
     lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
-    for n_ in nets.values():
+    for n_ in {id(v): v for v in nets.values()}.values():
         n_.close()
     return p, results, best, dict(ms=e2e_ms, h2d=h2d, d2h=d2h)
 
@@ -360,10 +365,11 @@ def profile(args):
     ms_net = None
     ms_pc, ncol, persist = None, C.c_int(0), C.c_int(0)
     pc = getattr(bfm_gb300, METHODS.get(args.method, ("", "PC_JACOBI"))[1])
-    if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR):
-        # two iterations form the colour order and the sweep graph; then the
-        # sweeps alone, `reps` standalone applications
-        o = bfm_gb300.default_opts(precision=prec, precond=bfm_gb300.PC_SSOR, max_iters=2)
+    if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR, bfm_gb300.PC_SSOR2, bfm_gb300.PC_LEARNED_SSOR2):
+        # two iterations form the colour order (and the coarse operator) and
+        # the sweep graph; then the preconditioner alone, `reps` applications
+        two = pc in (bfm_gb300.PC_SSOR2, bfm_gb300.PC_LEARNED_SSOR2)
+        o = bfm_gb300.default_opts(precision=prec, precond=bfm_gb300.PC_SSOR2 if two else bfm_gb300.PC_SSOR, max_iters=2)
         assert lib.bfm_gpu_problem_solve(P, C.byref(o)) == 0, bfm_gb300.last_error()
         t = C.c_double()
         assert lib.bfm_gpu_problem_time_precond(P, args.reps, C.byref(t), C.byref(persist)) == 0, bfm_gb300.last_error()
@@ -463,7 +469,7 @@ def main():
     # solve init + 2 kernels per iteration + replacement kernels, finish;
     # the learned preconditioner adds its 12 inference kernels per solve
     per_iter = 3 if split else 2
-    ssor = r["pc"] in (3, 4)
+    ssor = r["pc"] in (3, 4, 5, 6)
     if ssor:
         # the SSOR sweeps after the init, every update and every replacement:
         # one cooperative launch, or 2 nc - 1 colour phases
@@ -471,7 +477,7 @@ def main():
     else:
         per_pc = 0
     launches_per_step = 24 + 1 + (per_iter + per_pc) * r["iters"] + (2 + per_pc) * r["repl"] + per_pc + 2 + \
-        (12 if r["pc"] in (2, 4) else 0)
+        (12 if r["pc"] in (2, 4, 6) else 0)
     spmv_roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                  "frac": round(achieved / hbm, 3), "traffic": traffic, "traffic_source": traffic_src,
                  "kernel": kernel, "spmv_shape": r["shape"], "algorithmic_bytes": bytes_spmv,
@@ -515,7 +521,7 @@ def main():
                         "spmv_shape": v["shape"],
                         **({"precond_ms": round(v["ms_precond"], 5), "colours": v["ncol"],
                             "sweeps": "persistent" if v["persistent"] else "per colour"}
-                           if v["pc"] in (3, 4) else {})}
+                           if v["pc"] in (3, 4, 5, 6) else {})}
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),

@@ -32,7 +32,7 @@ class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
 
 
 FP64, MIXED, MIXED_EXACT, FP64_DF = 0, 1, 2, 3
-PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_SSOR, PC_LEARNED_SSOR = 0, 1, 2, 3, 4
+PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_SSOR, PC_LEARNED_SSOR, PC_SSOR2, PC_LEARNED_SSOR2 = 0, 1, 2, 3, 4, 5, 6
 HOST, DEVICE = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error", 5: "stagnated"}
 

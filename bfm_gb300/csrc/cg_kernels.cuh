@@ -1361,7 +1361,12 @@ struct SsorArgs {
 	unsigned* bar;      // grid barrier: arrivals, generation
 	int ncol;
 	int off[65];        // colour c: rows [off[c], off[c + 1])
+	// two-level form: z += P yc, the coarse correction (yc == nullptr: none)
+	const int* agg;      // aggregate of each node
+	const float4* pnode; // per node: (dx / H, dy / H, u free, v free)
+	const float2* yc;    // A_c^-1 P^T r, double-float pair per coarse DOF
 };
+
 
 // a * b for a float and a double-float (TwoProduct of the high part)
 __device__ __forceinline__ dfl df_mul_f(float a, dfl b) {
@@ -1423,9 +1428,25 @@ __device__ __forceinline__ void ssor_ld_r(const void* r, int i, dfl& r0, dfl& r1
 	}
 }
 
+// the coarse correction of node i, (P yc)_i = [f0 (y0 - dy y2), f1 (y1 + dx y2)]
+__device__ __forceinline__ void coarse_term(const int* agg, const float4* pnode, const float2* yc, int i, dfl& c0, dfl& c1) {
+	int const I = agg[i];
+	float4 const q = pnode[i];
+	float2 const a = yc[3 * I], b = yc[3 * I + 1], c = yc[3 * I + 2];
+	dfl const y2 = {c.x, c.y};
+	c0 = q.z != 0.f ? df_add({a.x, a.y}, df_mul_f(-q.y, y2)) : dfl{0.f, 0.f};
+	c1 = q.w != 0.f ? df_add({b.x, b.y}, df_mul_f(q.x, y2)) : dfl{0.f, 0.f};
+}
+
 template <bool DF>
 __device__ __forceinline__ void ssor_st_z(const SsorArgs& a, int i, dfl z0, dfl z1, dfl r0, dfl r1, double q0, double q1,
                                           dfl& acc, double& acc64) {
+	if (a.yc) {
+		dfl c0, c1;
+		coarse_term(a.agg, a.pnode, a.yc, i, c0, c1);
+		z0 = df_add(z0, c0);
+		z1 = df_add(z1, c1);
+	}
 	if constexpr (DF) {
 		df_st((float*) a.z, i, z0, z1);
 		acc = df_add(acc, df_add(df_mul(r0, z0), df_mul(r1, z1)));
@@ -1518,12 +1539,12 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
 // the limit the kernel records the timeout, and the blocks stop sweeping.
 constexpr long SSOR_SPIN_LIMIT = 1l << 24;
 
-__device__ bool ssor_barrier(const SsorArgs& a) {
+__device__ bool grid_barrier(unsigned* bar, int* err) {
 	__shared__ int ok;
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		unsigned* count = a.bar;
-		unsigned* gen = a.bar + 1;
+		unsigned* count = bar;
+		unsigned* gen = bar + 1;
 		unsigned const g = atomicAdd(gen, 0u);
 		__threadfence();
 		int good = 1;
@@ -1539,8 +1560,8 @@ __device__ bool ssor_barrier(const SsorArgs& a) {
 				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gen) : "memory");
 				if (cur != g) break;
 				__nanosleep(20);
-				if (++spins > SSOR_SPIN_LIMIT || atomicAdd(&a.st->ssor_err, 0) != 0) {
-					atomicExch(&a.st->ssor_err, 1);
+				if (++spins > SSOR_SPIN_LIMIT || atomicAdd(err, 0) != 0) {
+					atomicExch(err, 1);
 					good = 0;
 					break;
 				}
@@ -1552,6 +1573,8 @@ __device__ bool ssor_barrier(const SsorArgs& a) {
 	__syncthreads();
 	return ok;
 }
+
+__device__ __forceinline__ bool ssor_barrier(const SsorArgs& a) { return grid_barrier(a.bar, &a.st->ssor_err); }
 
 template <bool DF>
 __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
@@ -1595,6 +1618,286 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 	double v[1] = {DF ? df_dbl(acc) : acc64};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
+}
+
+// ---------------------------------------------------------------- coarse space (two-level SSOR)
+// M^-1 = M_SSOR^-1 + P A_c^-1 P^T, A_c = P^T A P: one aggregate per cell of a
+// grid laid over the mesh's bounding box, three coarse DOFs per aggregate
+// (the two translations and the rotation about the cell centre, scaled by
+// the cell size H), rows of constrained DOFs zero.  The sweeps add P yc to z
+// when they store it, so the recursion itself stays M_SSOR^-1.
+
+struct CoarseArgs {
+	int na, nc;               // aggregates (cells), coarse DOFs (3 na)
+	int gx;                   // cells per grid row: cell I = cx + gx cy
+	const int* agg_ptr;       // nodes of aggregate I: agg_nodes[agg_ptr[I] .. agg_ptr[I + 1]), ascending
+	const int* agg_nodes;
+	const int* agg;
+	const float4* pnode;
+	double* ainv;             // A_c, then A_c^-1 in place (nc x nc, row-major)
+	double* diag0;            // Gauss-Jordan: A_c's diagonal before elimination (the drop test)
+	float2* yc;               // A_c^-1 P^T r (double-float pairs)
+	double* rc;               // P^T r
+	const void* r;
+	int df;                   // r in double-float (float4 per node) or FP64 (double2)
+	const int* row_ptr;
+	const int* cols;
+	const double* vals64;
+	int* err;
+	unsigned* bar;
+	int* gj_err;
+	// chunks of at most COARSE_CHUNK nodes of one aggregate: chunk q covers
+	// agg_nodes[chunk_start[q] .. chunk_start[q + 1]) of aggregate chunk_agg[q];
+	// the chunks of aggregate I are [agg_chunk[I], agg_chunk[I + 1])
+	int nchunk;
+	const int* chunk_start;
+	const int* chunk_agg;
+	const int* agg_chunk;
+	double* part;        // per chunk: 3 (restriction) or 81 (coarse matrix) partial sums
+	double* gjt;         // blocked Gauss-Jordan: pivot block inverse (GJB^2), row panel (GJB x nc), column panel (nc x GJB)
+};
+
+constexpr int GJB = 32;  // pivot block of the blocked Gauss-Jordan inversion
+
+constexpr int COARSE_CHUNK = 128;
+
+// rc = P^T r in two deterministic stages: one warp per chunk of an
+// aggregate (lanes in a fixed stride, double-float sums, a fixed shuffle
+// tree), then per aggregate the chunks' sums in chunk order
+__global__ void k_restrict(CoarseArgs a) {
+	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if (q >= a.nchunk) return;
+	dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+	for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
+		int const i = a.agg_nodes[k];
+		dfl r0, r1;
+		if (a.df) df_ld((const float*) a.r, i, r0, r1);
+		else {
+			double2 const t = ld2((const double*) a.r, i);
+			r0 = df_make(t.x);
+			r1 = df_make(t.y);
+		}
+		float4 const pq = a.pnode[i];
+		if (pq.z == 0.f) r0 = {0.f, 0.f};
+		if (pq.w == 0.f) r1 = {0.f, 0.f};
+		s0 = df_add(s0, r0);
+		s1 = df_add(s1, r1);
+		s2 = df_add(s2, df_add(df_mul_f(-pq.y, r0), df_mul_f(pq.x, r1)));
+	}
+#pragma unroll
+	for (int o = 16; o; o >>= 1) {
+		s0 = df_add(s0, {__shfl_xor_sync(0xffffffffu, s0.hi, o), __shfl_xor_sync(0xffffffffu, s0.lo, o)});
+		s1 = df_add(s1, {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)});
+		s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
+	}
+	if (lane == 0) {
+		a.part[3l * q] = df_dbl(s0);
+		a.part[3l * q + 1] = df_dbl(s1);
+		a.part[3l * q + 2] = df_dbl(s2);
+	}
+}
+
+__global__ void k_restrict_sum(CoarseArgs a) {
+	int const t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= a.nc) return;
+	int const I = t / 3, m = t % 3;
+	double s = 0.0;
+	for (int q = a.agg_chunk[I]; q < a.agg_chunk[I + 1]; q++) s += a.part[3l * q + m];
+	a.rc[t] = s;
+}
+
+// yc = A_c^-1 rc: one block per coarse row, fixed thread stride, warp
+// shuffle trees and the warps' sums in order (deterministic)
+__global__ void __launch_bounds__(TPB_K) k_coarse_mv(CoarseArgs a) {
+	__shared__ double ws[TPB_K / 32];
+	int const row = blockIdx.x;
+	if (row >= a.nc) return;
+	const double* m = a.ainv + (long) row * a.nc;
+	double s = 0.0;
+	for (int j = threadIdx.x; j < a.nc; j += blockDim.x) s += m[j] * a.rc[j];
+#pragma unroll
+	for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t = 0.0;
+		for (int w = 0; w < (int) (blockDim.x >> 5); w++) t += ws[w];
+		dfl const y = df_make(t);
+		a.yc[row] = make_float2(y.hi, y.lo);
+	}
+}
+
+// A_c = P^T A P in two deterministic stages.  One warp per chunk of
+// aggregate I: every lane keeps the 3x3 blocks of the 9 cells around I (slot
+// = cell offset), so the lanes' partial sums line up and are reduced in a
+// fixed order into the chunk's 81 values; then per aggregate and entry the
+// chunks in chunk order.  A neighbour outside those 9 cells sets *err (the
+// caller then drops the coarse correction).
+__global__ void k_coarse_ac(CoarseArgs a) {
+	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if (q >= a.nchunk) return;
+	int const I = a.chunk_agg[q];
+	int const cx = I % a.gx, cy = I / a.gx;
+	double acc[9][9];
+	for (int s = 0; s < 9; s++)
+		for (int t = 0; t < 9; t++) acc[s][t] = 0.0;
+	for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
+		int const i = a.agg_nodes[k];
+		float4 const pi = a.pnode[i];
+		double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
+		for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
+			int const j = a.cols[e];
+			int const J = a.agg[j];
+			int const ox = J % a.gx - cx, oy = J / a.gx - cy;
+			if (ox < -1 || ox > 1 || oy < -1 || oy > 1) {
+				atomicOr(a.err, 1);
+				continue;
+			}
+			int const slot = (oy + 1) * 3 + (ox + 1);
+			float4 const pj = a.pnode[j];
+			double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
+			const double* m = a.vals64 + 4l * e;
+			// A P_j (2x3), then P_i^T (3x2) times it
+			double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
+			                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};
+			double const pt[3][2] = {{fi0, 0.0}, {0.0, fi1}, {-fi0 * dyi, fi1 * dxi}};
+#pragma unroll
+			for (int u = 0; u < 3; u++)
+#pragma unroll
+				for (int v = 0; v < 3; v++) acc[slot][3 * u + v] += pt[u][0] * ap[0][v] + pt[u][1] * ap[1][v];
+		}
+	}
+	for (int s = 0; s < 9; s++)
+		for (int t = 0; t < 9; t++) {
+			double x = acc[s][t];
+#pragma unroll
+			for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+			if (lane == 0) a.part[81l * q + 9 * s + t] = x;
+		}
+}
+
+__global__ void k_coarse_ac_sum(CoarseArgs a) {
+	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (t >= 81l * a.na) return;
+	int const I = (int) (t / 81), e = (int) (t % 81), s = e / 9, u = (e % 9) / 3, v = e % 3;
+	int const jx = I % a.gx + s % 3 - 1, jy = I / a.gx + s / 3 - 1;
+	if (jx < 0 || jx >= a.gx || jy < 0 || jy * a.gx >= a.na) return;
+	double x = 0.0;
+	for (int q = a.agg_chunk[I]; q < a.agg_chunk[I + 1]; q++) x += a.part[81l * q + e];
+	int const J = jx + a.gx * jy;
+	a.ainv[(long) (3 * I + u) * a.nc + 3 * J + v] = x;
+}
+
+// symmetric average (i < j), and the diagonal saved for the pivot test
+// (coarse DOFs without any coupling -- empty cells, all-constrained or
+// degenerate modes -- have a zero diagonal and are dropped by it)
+__global__ void k_coarse_sym(CoarseArgs a) {
+	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (t >= (long) a.nc * a.nc) return;
+	int const i = (int) (t / a.nc), j = (int) (t % a.nc);
+	if (i < j) {
+		double const m = 0.5 * (a.ainv[(long) i * a.nc + j] + a.ainv[(long) j * a.nc + i]);
+		a.ainv[(long) i * a.nc + j] = m;
+		a.ainv[(long) j * a.nc + i] = m;
+	}
+	if (i == j) a.diag0[i] = a.ainv[(long) i * a.nc + i];
+}
+
+// Blocked Gauss-Jordan (pivot blocks of GJB): per step K = [k0, k0 + kb),
+//   A_KK <- A_KK^-1,  A_Kj <- A_KK^-1 A_Kj,  A_iK <- -A_iK A_KK^-1,
+//   A_ij <- A_ij - A_iK A_KK^-1 A_Kj   (i, j outside K),
+// which after the last block leaves A^-1 in place.  The pivot block is
+// inverted by block 0 in shared memory (unblocked; a pivot below 1e-12 of
+// its original diagonal -- a coarse mode that A barely sees: an empty cell,
+// the rotation of a single node -- drops that DOF, whose row and column of
+// the inverse are then zero); the rank-kb update runs over 32 x 32 tiles staged in
+// shared memory.  Three grid barriers per block step; every read of the
+// matrix and the panels goes past L1.
+__global__ void __launch_bounds__(256) k_coarse_gjb(CoarseArgs a) {
+	__shared__ double D[GJB][GJB + 1];
+	__shared__ double Cs[32][GJB + 1];
+	__shared__ double Rs[GJB][32 + 1];
+	int const n = a.nc;
+	double* T = a.gjt;                      // GJB x GJB
+	double* Rp = a.gjt + GJB * GJB;         // GJB x n
+	double* Cp = Rp + (long) GJB * n;       // n x GJB
+	long const tid = blockIdx.x * (long) blockDim.x + threadIdx.x, stride = (long) gridDim.x * blockDim.x;
+	for (int k0 = 0; k0 < n; k0 += GJB) {
+		int const kb = n - k0 < GJB ? n - k0 : GJB;
+		if (blockIdx.x == 0) {
+			for (int e = threadIdx.x; e < GJB * GJB; e += blockDim.x) {
+				int const r = e / GJB, c = e % GJB;
+				D[r][c] = r < kb && c < kb ? __ldcg(a.ainv + (long) (k0 + r) * n + k0 + c) : 0.0;
+			}
+			__syncthreads();
+			for (int k = 0; k < kb; k++) {
+				__shared__ double col[GJB];
+				double const p = D[k][k];
+				bool const drop = !(p > 1e-12 * a.diag0[k0 + k]);
+				double const ip = drop ? 0.0 : 1.0 / p;
+				if (threadIdx.x < GJB) col[threadIdx.x] = threadIdx.x == k || drop ? 0.0 : D[threadIdx.x][k];
+				__syncthreads();
+				if (threadIdx.x < GJB && threadIdx.x != k) D[k][threadIdx.x] = drop ? 0.0 : D[k][threadIdx.x] * ip;
+				__syncthreads();
+				if (threadIdx.x == 0) D[k][k] = ip;
+				__syncthreads();
+				for (int e = threadIdx.x; e < GJB * GJB; e += blockDim.x) {
+					int const i = e / GJB, j = e % GJB;
+					if (i == k || i >= kb || j >= kb) continue;
+					D[i][j] = j == k ? -col[i] * D[k][k] : D[i][j] - col[i] * D[k][j];
+				}
+				__syncthreads();
+			}
+			for (int e = threadIdx.x; e < GJB * GJB; e += blockDim.x) T[e] = D[e / GJB][e % GJB];
+		}
+		if (!grid_barrier(a.bar, a.gj_err)) return;
+		// panels: Rp = A_KK^-1 A_Kj (j outside K), Cp = A_iK (i outside K)
+		for (long e = tid; e < (long) kb * n; e += stride) {
+			int const r = (int) (e / n), j = (int) (e % n);
+			if (j >= k0 && j < k0 + kb) continue;
+			double x = 0.0;
+			for (int m = 0; m < kb; m++) x += __ldcg(T + r * GJB + m) * __ldcg(a.ainv + (long) (k0 + m) * n + j);
+			Rp[(long) r * n + j] = x;
+		}
+		for (long e = tid; e < (long) n * kb; e += stride) {
+			int const i = (int) (e / kb), m = (int) (e % kb);
+			Cp[(long) i * GJB + m] = (i >= k0 && i < k0 + kb) ? 0.0 : __ldcg(a.ainv + (long) i * n + k0 + m);
+		}
+		if (!grid_barrier(a.bar, a.gj_err)) return;
+		// the update, 32 x 32 tiles
+		int const nt = (n + 31) / 32;
+		for (long tile = blockIdx.x; tile < (long) nt * nt; tile += gridDim.x) {
+			int const i0 = (int) (tile / nt) * 32, j0 = (int) (tile % nt) * 32;
+			for (int e = threadIdx.x; e < 32 * GJB; e += blockDim.x) {
+				int const r = e / GJB, m = e % GJB;
+				Cs[r][m] = i0 + r < n && m < kb ? __ldcg(Cp + (long) (i0 + r) * GJB + m) : 0.0;
+				int const mm = e / 32, c = e % 32;
+				Rs[mm][c] = j0 + c < n && mm < kb ? __ldcg(Rp + (long) mm * n + j0 + c) : 0.0;
+			}
+			__syncthreads();
+			for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+				int const r = e / 32, c = e % 32, i = i0 + r, j = j0 + c;
+				if (i >= n || j >= n) continue;
+				bool const iK = i >= k0 && i < k0 + kb, jK = j >= k0 && j < k0 + kb;
+				long const at = (long) i * n + j;
+				if (iK && jK) a.ainv[at] = __ldcg(T + (i - k0) * GJB + (j - k0));
+				else if (iK) a.ainv[at] = __ldcg(Rp + (long) (i - k0) * n + j);
+				else if (jK) {
+					double x = 0.0;
+					for (int m = 0; m < kb; m++) x += Cs[r][m] * __ldcg(T + m * GJB + (j - k0));
+					a.ainv[at] = -x;
+				}
+				else {
+					double x = 0.0;
+#pragma unroll 8
+					for (int m = 0; m < GJB; m++) x += Cs[r][m] * Rs[m][c];
+					a.ainv[at] = __ldcg(a.ainv + at) - x;
+				}
+			}
+			__syncthreads();
+		}
+		if (!grid_barrier(a.bar, a.gj_err)) return;
+	}
 }
 
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner

@@ -261,6 +261,19 @@ __global__ void k_rows_fill(int N, int kind, const int* __restrict__ inc_ptr, co
 // and its higher-colour neighbours in that order, and a colour is a
 // contiguous range of rows.
 
+// two-level SSOR: per node its offset from its cell's centre (scaled by the
+// cell size H) and which of its DOFs are free (constrained ones get no
+// coarse correction)
+__global__ void k_pnode(int N, const double* __restrict__ coords, const int* __restrict__ agg, const int* __restrict__ last_ci,
+                        double x0, double y0, double cw, double ch, int gx, double H, float4* __restrict__ pnode) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	int const I = agg[i];
+	double const xc = x0 + (I % gx + 0.5) * cw, yc = y0 + (I / gx + 0.5) * ch;
+	pnode[i] = make_float4((float) ((coords[2l * i] - xc) / H), (float) ((coords[2l * i + 1] - yc) / H),
+	                       last_ci[2l * i] < 0 ? 1.f : 0.f, last_ci[2l * i + 1] < 0 ? 1.f : 0.f);
+}
+
 // dst[i] = src[map[i]] for `width` consecutive elements per node
 template <typename T>
 __global__ void k_gather_nodes(long N, int width, const T* __restrict__ src, const int* __restrict__ map, T* __restrict__ dst) {
@@ -1323,6 +1336,23 @@ struct bfm_gpu_problem {
 	float* ssor_y; // sweep vector (double-float, 4 floats per node)
 	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
 	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
+
+	// two-level SSOR: aggregates are the cells of a gx x gy grid over the
+	// bounding box (origin ax0, ay0, cell acw x ach, rotation scale aH)
+	bool agg_valid;      // the aggregation belongs to the current node order and coordinates
+	int coarse_ok;       // A_c^-1 is ready (else the solve runs plain SSOR)
+	int na, nc, nc_cap, agx;
+	double ax0, ay0, acw, ach, aH;
+	int *agg, *agg_ptr, *agg_nodes;
+	int nchunk, chunk_cap;
+	int *chunk_start, *chunk_agg, *agg_chunk;
+	double* cpart;  // per chunk partial sums (81 doubles)
+	float4* pnode;
+	double *ainv, *diag0, *rc, *gjt;
+	float2* yc;
+	unsigned* gj_bar;
+	int* gj_err;
+	int gj_grid;
 };
 
 enum : unsigned { ORD_COORDS = 1, ORD_ELEMS = 2, ORD_MASKS = 4, ORD_EDGES = 8, ORD_FIELDS = 16, ORD_LEDGES = 32, ORD_ALL = 63 };
@@ -1386,7 +1416,13 @@ int incidence(bfm_gpu_problem* P, const int* items, int n_items, int arity, int*
 	return 0;
 }
 
-bool ssor_pc(int pc) { return pc == BFM_GPU_PC_SSOR || pc == BFM_GPU_PC_LEARNED_SSOR; }
+bool ssor_pc(int pc) {
+	return pc == BFM_GPU_PC_SSOR || pc == BFM_GPU_PC_LEARNED_SSOR || pc == BFM_GPU_PC_SSOR2 || pc == BFM_GPU_PC_LEARNED_SSOR2;
+}
+bool coarse_pc(int pc) { return pc == BFM_GPU_PC_SSOR2 || pc == BFM_GPU_PC_LEARNED_SSOR2; }
+bool learned_pc(int pc) {
+	return pc == BFM_GPU_PC_LEARNED || pc == BFM_GPU_PC_LEARNED_SSOR || pc == BFM_GPU_PC_LEARNED_SSOR2;
+}
 
 // Node-block pattern of the current element array (steps 1-2 of the assembly).
 int build_pattern(bfm_gpu_problem* P) {
@@ -1509,6 +1545,7 @@ int color_nodes(bfm_gpu_problem* P) {
 	free(cols);
 	if (rc) return rc;
 	P->colored = true;
+	P->agg_valid = false;
 	P->graph_precision = -1;  // the solve graph's sweep phases follow the colour ranges
 	return 0;
 }
@@ -1586,6 +1623,214 @@ int prepare_order(bfm_gpu_problem* P) {
 		}
 	}
 	return reorder_inputs(P, true);
+}
+
+// ---- two-level SSOR: aggregation, coarse operator
+CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
+	CoarseArgs c;
+	memset(&c, 0, sizeof c);
+	c.na = P->na;
+	c.nc = P->nc;
+	c.gx = P->agx;
+	c.agg_ptr = P->agg_ptr;
+	c.agg_nodes = P->agg_nodes;
+	c.agg = P->agg;
+	c.pnode = P->pnode;
+	c.ainv = P->ainv;
+	c.diag0 = P->diag0;
+	c.yc = P->yc;
+	c.rc = P->rc;
+	c.r = r;
+	c.df = df;
+	c.row_ptr = P->row_ptr;
+	c.cols = P->cols;
+	c.vals64 = P->vals64;
+	c.err = P->gj_err;
+	c.bar = P->gj_bar;
+	c.gj_err = P->gj_err;
+	c.nchunk = P->nchunk;
+	c.chunk_start = P->chunk_start;
+	c.chunk_agg = P->chunk_agg;
+	c.agg_chunk = P->agg_chunk;
+	c.part = P->cpart;
+	c.gjt = P->gjt;
+	return c;
+}
+
+// Aggregates for the current (working-order) coordinates: cells of a grid
+// over the bounding box, about one per 2,500 nodes (at most 384), as square
+// as the box allows; node lists per cell in ascending node order (a host
+// counting sort: deterministic).  Redone when the colouring is.
+int build_aggregates(bfm_gpu_problem* P) {
+	cudaStream_t const st = P->stream;
+	long const N = P->N;
+	double* xy = (double*) malloc((2 * N + 2) * sizeof(double));
+	int* ag = (int*) malloc((N + 1) * sizeof(int));
+	int* nodes = (int*) malloc((N + 1) * sizeof(int));
+	int rc = 0;
+	if (!xy || !ag || !nodes) rc = fail("out of host memory");
+	if (!rc && (cudaMemcpyAsync(xy, P->coords, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+	            cudaStreamSynchronize(st) != cudaSuccess))
+		rc = fail("coordinate copy failed");
+	int gx = 1, gy = 1;
+	double x0 = 0, y0 = 0, cw = 1, ch = 1;
+	if (!rc) {
+		double x1 = 0, y1 = 0;
+		for (long i = 0; i < N; i++) {
+			double const x = xy[2 * i], y = xy[2 * i + 1];
+			if (i == 0 || x < x0) x0 = x;
+			if (i == 0 || x > x1) x1 = x;
+			if (i == 0 || y < y0) y0 = y;
+			if (i == 0 || y > y1) y1 = y;
+		}
+		double const w = x1 - x0, h = y1 - y0;
+		long target = N / 2500;
+		target = target < 1 ? 1 : target > 384 ? 384 : target;
+		if (w > 0 && h > 0) {
+			gx = (int) lround(sqrt((double) target * w / h));
+			gx = gx < 1 ? 1 : gx > target ? (int) target : gx;
+			gy = (int) lround((double) target / gx);
+			gy = gy < 1 ? 1 : gy;
+		}
+		else if (w > 0) gx = (int) target;
+		else if (h > 0) gy = (int) target;
+		// cells a hair wider than the box, so the far edge falls inside the last one
+		cw = w > 0 ? w * (1.0 + 1e-12) / gx : 1.0;
+		ch = h > 0 ? h * (1.0 + 1e-12) / gy : 1.0;
+		for (long i = 0; i < N; i++) {
+			int cx = (int) ((xy[2 * i] - x0) / cw), cy = (int) ((xy[2 * i + 1] - y0) / ch);
+			cx = cx < 0 ? 0 : cx >= gx ? gx - 1 : cx;
+			cy = cy < 0 ? 0 : cy >= gy ? gy - 1 : cy;
+			ag[i] = cx + gx * cy;
+		}
+	}
+	int const na = gx * gy, nc = 3 * na;
+	int* ptr = (int*) calloc(na + 1, sizeof(int));
+	if (!rc && !ptr) rc = fail("out of host memory");
+	if (!rc) {
+		for (long i = 0; i < N; i++) ptr[ag[i] + 1]++;
+		for (int I = 0; I < na; I++) ptr[I + 1] += ptr[I];
+		int* next = (int*) malloc((na + 1) * sizeof(int));
+		if (!next) rc = fail("out of host memory");
+		else {
+			memcpy(next, ptr, na * sizeof(int));
+			for (long i = 0; i < N; i++) nodes[next[ag[i]]++] = (int) i;
+			free(next);
+		}
+	}
+	// chunks of at most COARSE_CHUNK nodes per aggregate, for the parallel reductions
+	int nchunk = 0;
+	if (!rc)
+		for (int I = 0; I < na; I++) nchunk += (ptr[I + 1] - ptr[I] + COARSE_CHUNK - 1) / COARSE_CHUNK;
+	int* cst = (int*) malloc((nchunk + 1) * sizeof(int));
+	int* cag = (int*) malloc((nchunk + 1) * sizeof(int));
+	int* ach = (int*) malloc((na + 1) * sizeof(int));
+	if (!rc && (!cst || !cag || !ach)) rc = fail("out of host memory");
+	if (!rc) {
+		int q = 0;
+		for (int I = 0; I < na; I++) {
+			ach[I] = q;
+			for (int k = ptr[I]; k < ptr[I + 1]; k += COARSE_CHUNK) {
+				cst[q] = k;
+				cag[q] = I;
+				q++;
+			}
+		}
+		ach[na] = q;
+		cst[q] = ptr[na];
+	}
+	if (!rc && nchunk + 1 > P->chunk_cap) {
+		void* old[] = {P->chunk_start, P->chunk_agg, P->cpart};
+		for (void* o : old)
+			if (o) cudaFree(o);
+		P->chunk_start = P->chunk_agg = nullptr;
+		P->cpart = nullptr;
+		if (dalloc(&P->chunk_start, nchunk + 1) || dalloc(&P->chunk_agg, nchunk + 1) || dalloc(&P->cpart, 81l * (nchunk + 1)))
+			rc = -1;
+		else P->chunk_cap = nchunk + 1;
+	}
+	if (!rc && nc > P->nc_cap) {
+		// (re)allocate for the larger coarse space
+		void* old[] = {P->agg_ptr, P->agg_chunk, P->ainv, P->diag0, P->rc, P->yc, P->gjt};
+		for (void* q : old)
+			if (q) cudaFree(q);
+		P->agg_ptr = P->agg_chunk = nullptr;
+		P->ainv = P->diag0 = P->rc = P->gjt = nullptr;
+		P->yc = nullptr;
+		if (dalloc(&P->agg_ptr, na + 1) || dalloc(&P->agg_chunk, na + 1) || dalloc(&P->ainv, (long) nc * nc) ||
+		    dalloc(&P->diag0, nc) || dalloc(&P->rc, nc) || dalloc(&P->yc, nc) ||
+		    dalloc(&P->gjt, (long) GJB * GJB + 2l * GJB * nc))
+			rc = -1;
+		else P->nc_cap = nc;
+	}
+	if (!rc && !P->agg && (dalloc(&P->agg, N) || dalloc(&P->agg_nodes, N) || dalloc(&P->pnode, N) || dalloc(&P->gj_bar, 2) ||
+	                       dalloc(&P->gj_err, 1)))
+		rc = -1;
+	if (!rc && (cudaMemcpyAsync(P->agg, ag, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	            cudaMemcpyAsync(P->agg_nodes, nodes, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	            cudaMemcpyAsync(P->agg_ptr, ptr, (na + 1) * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	            cudaMemcpyAsync(P->chunk_start, cst, (nchunk + 1) * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	            cudaMemcpyAsync(P->chunk_agg, cag, (nchunk + 1) * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	            cudaMemcpyAsync(P->agg_chunk, ach, (na + 1) * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	            cudaStreamSynchronize(st) != cudaSuccess))
+		rc = fail("aggregate upload failed");
+	free(xy);
+	free(ag);
+	free(nodes);
+	free(ptr);
+	free(cst);
+	free(cag);
+	free(ach);
+	if (rc) return rc;
+	if (!P->gj_grid) {
+		// one block per SM: each step is a small rank-1 update, the two grid
+		// barriers per step cost less with fewer blocks
+		int nb = 0;
+		CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_coarse_gjb, 256, 0));
+		if (nb < 1) return fail("the coarse inversion kernel does not fit on an SM");
+		P->gj_grid = num_sms();
+	}
+	P->na = na;
+	P->nc = nc;
+	P->nchunk = nchunk;
+	P->agx = gx;
+	P->ax0 = x0;
+	P->ay0 = y0;
+	P->acw = cw;
+	P->ach = ch;
+	P->aH = cw > ch ? cw : ch;
+	P->agg_valid = true;
+	P->graph_precision = -1;  // the graph's coarse kernels take the new sizes
+	return 0;
+}
+
+// Per assembly: node offsets and free DOFs, A_c = P^T A P, A_c^-1.  Any
+// failure (a neighbour beyond the adjacent cells, a barrier timeout) leaves
+// the solve on plain SSOR (coarse_ok = 0).
+int coarse_setup(bfm_gpu_problem* P) {
+	cudaStream_t const st = P->stream;
+	P->coarse_ok = 0;
+	if (P->N == 0) return 0;
+	if (!P->agg_valid && build_aggregates(P)) return -1;
+	k_pnode<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->coords, P->agg, P->last_ci, P->ax0, P->ay0, P->acw, P->ach, P->agx,
+	                                          P->aH, P->pnode);
+	CK(cudaMemsetAsync(P->ainv, 0, (size_t) P->nc * P->nc * sizeof(double), st));
+	CK(cudaMemsetAsync(P->gj_err, 0, sizeof(int), st));
+	CK(cudaMemsetAsync(P->gj_bar, 0, 2 * sizeof(unsigned), st));
+	CoarseArgs ca = coarse_args(P, nullptr, true);
+	k_coarse_ac<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
+	k_coarse_ac_sum<<<blocks_for(81l * P->na), TPB, 0, st>>>(ca);
+	k_coarse_sym<<<blocks_for((long) P->nc * P->nc), TPB, 0, st>>>(ca);
+	int err = 0;
+	CK(cudaMemcpyAsync(&err, P->gj_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	if (err) return 0;
+	void* pa[1] = {&ca};
+	CK(cudaLaunchCooperativeKernel((const void*) k_coarse_gjb, dim3(P->gj_grid), dim3(256), pa, 0, st));
+	CK(cudaMemcpyAsync(&err, P->gj_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	P->coarse_ok = !err;
+	return 0;
 }
 
 template <typename V>
@@ -1702,6 +1947,20 @@ SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
 int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cudaGraphNode_t* dep, SsorArgs base, bool df,
              int mode) {
 	int const nc = P->ncol > 0 ? P->ncol : 1;
+	if (coarse_pc(P->precond) && P->coarse_ok) {
+		// two-level: yc = A_c^-1 P^T r first; the sweeps add P yc to z
+		CoarseArgs ca = coarse_args(P, base.r, df);
+		void* pc[1] = {&ca};
+		cudaGraphNode_t n1, n2, n3;
+		if (add_node(g, &n1, dep, (void*) k_restrict, blocks_for(32l * P->nchunk), pc)) return -1;
+		if (add_node(g, &n2, &n1, (void*) k_restrict_sum, blocks_for(P->nc), pc)) return -1;
+		if (add_node(g, &n3, &n2, (void*) k_coarse_mv, P->nc, pc)) return -1;
+		*last = n3;
+		dep = last;
+		base.agg = P->agg;
+		base.pnode = P->pnode;
+		base.yc = P->yc;
+	}
 	if (P->ssor_grid > 0) {
 		// one cooperative launch for every phase
 		SsorArgs a = base;
@@ -2013,7 +2272,19 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms) {
 	int const nc = P->ncol > 0 ? P->ncol : 1;
 	cudaEvent_t e[2];
 	for (auto& x : e) cudaEventCreate(&x);
+	CoarseArgs ca = coarse_args(P, P->vec[0], df);
+	bool const coarse = coarse_pc(P->precond) && P->coarse_ok;
+	if (coarse) {
+		base.agg = P->agg;
+		base.pnode = P->pnode;
+		base.yc = P->yc;
+	}
 	auto once = [&]() {
+		if (coarse) {
+			k_restrict<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
+			k_restrict_sum<<<blocks_for(P->nc), TPB, 0, st>>>(ca);
+			k_coarse_mv<<<P->nc, TPB, 0, st>>>(ca);
+		}
 		if (P->ssor_grid > 0) {
 			SsorArgs a = base;
 			a.ncol = nc;
@@ -2188,7 +2459,8 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	for (int i = 0; i < MAXF; i++)
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y,
-	              P->ssor_bar};
+	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->ainv, P->diag0, P->rc, P->yc,
+	              P->gj_bar, P->gj_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart, P->gjt};
 	for (void* q : lb)
 		if (q) cudaFree(q);
 	if (P->ext && P->ext_free) P->ext_free(P->ext);
@@ -2589,6 +2861,8 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		k_edge_loads<<<blocks_for(N), TPB, 0, st>>>(P->N, P->ledges, P->lloads, P->lptr, P->llist, P->coords, P->last_ci, P->b);
 	}
 	CK(cudaGetLastError());
+	// two-level SSOR: the coarse operator of this matrix
+	if (coarse_pc(P->precond) && coarse_setup(P)) return -1;
 	CK(cudaEventRecord(P->ev[1], st));
 	P->assembled = true;
 	P->solved = false;
@@ -2602,7 +2876,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	if (opts) o = *opts;
 	else bfm_gpu_default_opts(&o);
 	if (!(o.rtol >= 0.0) || o.max_iters < 0) return fail("invalid solver options");
-	if (o.precond < BFM_GPU_PC_JACOBI || o.precond > BFM_GPU_PC_LEARNED_SSOR) return fail("unknown preconditioner %d", o.precond);
+	if (o.precond < BFM_GPU_PC_JACOBI || o.precond > BFM_GPU_PC_LEARNED_SSOR2) return fail("unknown preconditioner %d", o.precond);
 	if (ssor_pc(o.precond) && P->precision != BFM_GPU_FP64 && P->precision != BFM_GPU_FP64_DF)
 		return fail("the SSOR preconditioners run on the FP64 and FP64_DF paths");
 	if (o.precond != P->precond) {
@@ -2626,7 +2900,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		P->graph_lpr = P->lpr;
 		P->graph_opts = o;
 	}
-	bool const learned = P->precond == BFM_GPU_PC_LEARNED || P->precond == BFM_GPU_PC_LEARNED_SSOR;
+	bool const learned = learned_pc(P->precond);
 	P->fallback = 0;
 	CK(cudaEventRecord(P->ev[2], P->stream));
 	// the learned blocks depend on the load vector: formed for every solve, inside the timed region

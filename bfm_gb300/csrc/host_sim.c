@@ -56,6 +56,8 @@ static bfm_gpu_opts_t current_opts(void) {
 		if (pc && (!strcmp(pc, "learned") || !strcmp(pc, "2"))) t_opts.precond = BFM_GPU_PC_LEARNED;
 		if (pc && (!strcmp(pc, "ssor") || !strcmp(pc, "3"))) t_opts.precond = BFM_GPU_PC_SSOR;
 		if (pc && (!strcmp(pc, "learned_ssor") || !strcmp(pc, "4"))) t_opts.precond = BFM_GPU_PC_LEARNED_SSOR;
+		if (pc && (!strcmp(pc, "ssor2") || !strcmp(pc, "5"))) t_opts.precond = BFM_GPU_PC_SSOR2;
+		if (pc && (!strcmp(pc, "learned_ssor2") || !strcmp(pc, "6"))) t_opts.precond = BFM_GPU_PC_LEARNED_SSOR2;
 		t_opts_set = 1;
 	}
 	return t_opts;
@@ -322,7 +324,9 @@ static int env_network(bfm_state_t* st) {
 static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	bfm_state_t* const st = sim->state;
 	bfm_gpu_opts_t const o = current_opts();
-	if ((o.precond == BFM_GPU_PC_LEARNED || o.precond == BFM_GPU_PC_LEARNED_SSOR) && env_network(st) < 0) return -1;
+	if ((o.precond == BFM_GPU_PC_LEARNED || o.precond == BFM_GPU_PC_LEARNED_SSOR || o.precond == BFM_GPU_PC_LEARNED_SSOR2) &&
+	    env_network(st) < 0)
+		return -1;
 	bfm_gpu_problem_t* P = upload_and_assemble(st, sim, inst, stress, o.precision, o.precond);
 	if (!P) return -1;
 	if (bfm_gpu_problem_solve(P, &o) < 0) return REPORT(st, "%s", bfm_gpu_last_error());

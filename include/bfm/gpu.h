@@ -59,6 +59,14 @@ enum {
 	/* The same sweeps with relaxation blocks from the message-passing
 	 * network (bfm_gpu_mpnn_use); block SSOR is its fallback. */
 	BFM_GPU_PC_LEARNED_SSOR = 4,
+	/* Two-level: the SSOR sweeps plus a coarse correction, additively,
+	 * M^-1 = M_SSOR^-1 + P A_c^-1 P^T, with P the rigid-body modes (two
+	 * translations and a rotation) of the cells of a grid over the mesh's
+	 * bounding box (about one cell per 2,500 nodes, at most 384) and
+	 * A_c = P^T A P inverted on the device at assembly.  FP64 and FP64_DF. */
+	BFM_GPU_PC_SSOR2 = 5,
+	/* The two-level form with the network's relaxation blocks. */
+	BFM_GPU_PC_LEARNED_SSOR2 = 6,
 };
 
 /* solver status codes (bfm_gpu_stats_t.status) */
