@@ -110,3 +110,70 @@ def pcg(A: sp.spmatrix, b: np.ndarray, apply, rtol: float = 1e-8, max_iters: int
         p = z + (g2 / g) * p
         g = g2
     return x, max_iters
+
+
+def cell_grid(coords: np.ndarray):
+    """The aggregation of the two-level preconditioner (bfm_gb300/csrc/
+    fem_gpu.cu, build_aggregates): a grid of cells over the bounding box, about
+    one cell per 2,500 nodes (at most 384), as square as the box allows.
+    Returns (cell of each node, gx, gy, x0, y0, cw, ch)."""
+    n = len(coords)
+    x0, y0 = coords.min(0)
+    x1, y1 = coords.max(0)
+    w, h = x1 - x0, y1 - y0
+    target = min(max(n // 2500, 1), 384)
+    gx = gy = 1
+    if w > 0 and h > 0:
+        gx = min(max(int(np.floor(np.sqrt(target * w / h) + 0.5)), 1), target)
+        gy = max(int(np.floor(target / gx + 0.5)), 1)
+    elif w > 0:
+        gx = target
+    elif h > 0:
+        gy = target
+    cw = w * (1 + 1e-12) / gx if w > 0 else 1.0
+    ch = h * (1 + 1e-12) / gy if h > 0 else 1.0
+    cx = np.clip(((coords[:, 0] - x0) / cw).astype(np.int64), 0, gx - 1)
+    cy = np.clip(((coords[:, 1] - y0) / ch).astype(np.int64), 0, gy - 1)
+    return cx + gx * cy, gx, gy, x0, y0, cw, ch
+
+
+class TwoLevel:
+    """z = M_SSOR^-1 r + P A_c^-1 P^T r (additive), P the rigid-body modes of
+    each cell -- per node [[1, 0, -dy], [0, 1, dx]] with (dx, dy) its offset
+    from the cell centre over H = max(cell width, height), rounded to FP32 as
+    the GPU stores them, rows of constrained DOFs zero -- and A_c = P^T A P on
+    the coarse DOFs that A sees (the others dropped, as the GPU's pivot test
+    does).  A and coords in the caller's order; `free` per DOF."""
+
+    def __init__(self, A: sp.spmatrix, coords: np.ndarray, free: np.ndarray, ssor: BlockSSOR):
+        A = sp.csr_matrix(A)
+        n = len(coords)
+        cell, gx, gy, x0, y0, cw, ch = cell_grid(coords)
+        H = max(cw, ch)
+        xc = x0 + (cell % gx + 0.5) * cw
+        yc = y0 + (cell // gx + 0.5) * ch
+        dx = ((coords[:, 0] - xc) / H).astype(np.float32).astype(np.float64)
+        dy = ((coords[:, 1] - yc) / H).astype(np.float32).astype(np.float64)
+        f0, f1 = free[0::2].astype(float), free[1::2].astype(float)
+        nc = 3 * gx * gy
+        rows = np.concatenate([2 * np.arange(n), 2 * np.arange(n), 2 * np.arange(n) + 1, 2 * np.arange(n) + 1])
+        cols = np.concatenate([3 * cell, 3 * cell + 2, 3 * cell + 1, 3 * cell + 2])
+        vals = np.concatenate([f0, -dy * f0, f1, dx * f1])
+        P = sp.csr_matrix((vals, (rows, cols)), shape=(2 * n, nc))
+        Ac = (P.T @ A @ P).toarray()
+        Ac = 0.5 * (Ac + Ac.T)
+        keep = np.diag(Ac) > 0
+        self.P = P[:, keep].tocsr()
+        self.Ainv = np.linalg.inv(Ac[np.ix_(keep, keep)])
+        self.ssor = ssor
+        self.n_cells = gx * gy
+
+    def apply(self, r: np.ndarray) -> np.ndarray:
+        return self.ssor.apply(r) + self.P @ (self.Ainv @ (self.P.T @ r))
+
+
+def free_dofs(A: sp.spmatrix) -> np.ndarray:
+    """DOFs whose row is not an eliminated Dirichlet row (a lone 1 on the diagonal)."""
+    A = sp.csr_matrix(A)
+    nnz = np.diff(A.indptr)
+    return ~((nnz == 1) & (A.diagonal() == 1.0))

@@ -241,3 +241,64 @@ def test_per_colour_kernels_match_the_persistent_kernel(libbfm, precision, monke
     assert s1.status == 0 and s2.status == 0
     assert abs(s1.iterations - s2.iterations) <= 2
     assert rel(x2, x1) < 1e-9
+
+
+@pytest.mark.parametrize("precision,tol", [(bfm_gb300.FP64, 1e-10), (bfm_gb300.FP64_DF, 1e-8)])
+def test_two_level_matches_direct_oracle_and_restatement(libbfm, precision, tol):
+    """Two-level SSOR (additive rigid-body coarse correction on a cell grid)
+    on a 256x64 plate (5 cells): the solution against the direct oracle, the
+    iteration count against the float64 restatement with the GPU's own
+    colouring, and fewer iterations than plain SSOR."""
+    p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
+    prob = LN.DeviceProblem(p, precision=precision)
+    try:
+        s1 = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-10)
+        s2 = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-10)
+        assert s2.status == 0 and s2.rel_residual <= 1e-10
+        x, _, _ = O.solve_direct(p)
+        assert rel(prob.solution(), x) < tol
+        # five cells only at this size; the 2048x512 plate's 390 cells cut 6,172 iterations to about 470
+        assert s2.iterations < 0.6 * s1.iterations, (s2.iterations, s1.iterations)
+        perm, off, _ = ordering(prob)
+        K, b = O.assemble_csr(p)
+        K = sp.csr_matrix(K)
+        tl = S.TwoLevel(K, p.coords, S.free_dofs(K), S.BlockSSOR(K, perm, off))
+        _, it = S.pcg(K, b, tl.apply, rtol=1e-10)
+        assert abs(s2.iterations - it) <= max(3, 0.1 * it), (s2.iterations, it)
+    finally:
+        prob.close()
+
+
+def test_untrained_learned_two_level_is_two_level(libbfm):
+    p = M.cfg_perforated(nx=128, ny=32, n_holes=40, seed=6)
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    net = LN.Network(seed=0)
+    try:
+        net.use()
+        s0 = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-8)
+        x0 = prob.solution()
+        s1 = prob.solve(precond=bfm_gb300.PC_LEARNED_SSOR2, rtol=1e-8)
+        assert s1.status == 0 and s1.fallback == 0 and s1.iterations == s0.iterations
+        np.testing.assert_array_equal(prob.solution(), x0)
+    finally:
+        net.close()
+        prob.close()
+
+
+@pytest.mark.parametrize("name", ["p1_16x8_nt", "q1_24x8_jitter", "axi_p1_12x8", "lepl8", "gear12"])
+def test_sim_run_with_two_level(libbfm, name, monkeypatch):
+    """bfm_sim_run with the two-level SSOR on every fixture (a single cell on
+    these small meshes: the coarse space is the three rigid-body modes of the
+    whole body), against the FP64 direct oracle."""
+    monkeypatch.setenv("BFM_GPU_AXISYM_REFERENCE", "0")
+    p, _ = load(name)
+    if p.stress == 3:
+        p.stress = 2
+    libbfm.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=1e-12, precond=bfm_gb300.PC_SSOR2)))
+    try:
+        h = api.SimHandle.from_problem(libbfm, p)
+        assert h.run() == 0, h.error()
+        x, _, _ = O.solve_direct(p)
+        assert rel(h.effects(), x) < 1e-9
+    finally:
+        libbfm.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
