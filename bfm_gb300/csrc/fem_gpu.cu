@@ -2259,7 +2259,7 @@ int time_iteration(bfm_gpu_problem* P, int lpr, int reps, double* ms_spmv, doubl
 
 // Mean duration (ms) of one SSOR application z = M^-1 r (every sweep phase),
 // launched standalone on a scratch solver state.  Overwrites the Krylov vectors.
-int time_ssor(bfm_gpu_problem* P, int reps, double* ms) {
+int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 	if (!ssor_pc(P->precond)) return fail("time the SSOR sweeps of a problem solved with an SSOR preconditioner");
 	CgState* scratch = nullptr;
 	if (dalloc(&scratch, 1)) return -1;
@@ -2279,8 +2279,8 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms) {
 		base.pnode = P->pnode;
 		base.yc = P->yc;
 	}
-	auto once = [&]() {
-		if (coarse) {
+	auto once = [&](bool with_coarse) {
+		if (coarse && with_coarse) {
 			k_restrict<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
 			k_restrict_sum<<<blocks_for(P->nc), TPB, 0, st>>>(ca);
 			k_coarse_mv<<<P->nc, TPB, 0, st>>>(ca);
@@ -2312,13 +2312,23 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms) {
 			                 dim3(P->grid), dim3(TPB), pa, 0, st);
 		}
 	};
-	once();
+	once(true);
 	cudaEventRecord(e[0], st);
-	for (int i = 0; i < reps; i++) once();
+	for (int i = 0; i < reps; i++) once(true);
 	cudaEventRecord(e[1], st);
-	cudaError_t const err = cudaStreamSynchronize(st);
+	cudaError_t err = cudaStreamSynchronize(st);
 	float t = 0;
 	cudaEventElapsedTime(&t, e[0], e[1]);
+	if (ms_sweeps && err == cudaSuccess) {
+		// the sweeps alone (the coarse correction's yc from the last application)
+		cudaEventRecord(e[0], st);
+		for (int i = 0; i < reps; i++) once(false);
+		cudaEventRecord(e[1], st);
+		err = cudaStreamSynchronize(st);
+		float t2 = 0;
+		cudaEventElapsedTime(&t2, e[0], e[1]);
+		*ms_sweeps = t2 / reps;
+	}
 	for (auto& x : e) cudaEventDestroy(x);
 	cudaFree(scratch);
 	CK(err);
@@ -3033,11 +3043,11 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 	return time_iteration(P, P->lpr, reps > 0 ? reps : 1, ms_spmv, ms_update);
 }
 
-int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* P, int reps, double* ms, int* persistent) {
+int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* P, int reps, double* ms, double* ms_sweeps, int* persistent) {
 	g_err[0] = 0;
 	if (!P->assembled) return fail("assemble first");
 	if (persistent) *persistent = P->ssor_grid > 0;
-	return time_ssor(P, reps > 0 ? reps : 1, ms);
+	return time_ssor(P, reps > 0 ? reps : 1, ms, ms_sweeps);
 }
 
 int bfm_gpu_problem_autotune(bfm_gpu_problem_t* P, int* lanes_per_row) {

@@ -252,12 +252,13 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t
 int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int* status, int* replacements,
                                double* rel_residual, int* rows_per_tile, int* lanes_per_row, double* ms_solve);
 
-/* Mean duration (ms) of one application of an SSOR preconditioner (every
- * sweep phase) over `reps` standalone launches on a scratch solver state;
- * *persistent = 1 when the phases run as one cooperative kernel.  Needs a
- * solve with BFM_GPU_PC_SSOR or BFM_GPU_PC_LEARNED_SSOR first (which forms
- * the colour order); overwrites the Krylov vectors. */
-int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* problem, int reps, double* ms, int* persistent);
+/* Mean duration (ms) of one application of an SSOR preconditioner (the
+ * coarse correction of the two-level form and every sweep phase) over `reps`
+ * standalone launches on a scratch solver state; *ms_sweeps (may be NULL)
+ * the sweeps alone; *persistent = 1 when the phases run as one cooperative
+ * kernel.  Needs a solve with one of the SSOR preconditioners first (which
+ * forms the colour order); overwrites the Krylov vectors. */
+int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* problem, int reps, double* ms, double* ms_sweeps, int* persistent);
 
 /* Working node order of the last assembly: perm[w] = the caller's index of
  * working node w (n_nodes ints, host memory; the identity unless an SSOR

@@ -233,7 +233,7 @@ def test_per_colour_kernels_match_the_persistent_kernel(libbfm, precision, monke
         s2 = prob.solve(precond=bfm_gb300.PC_SSOR, rtol=1e-10)
         persistent = C.c_int(-1)
         t = C.c_double()
-        assert libbfm.bfm_gpu_problem_time_precond(prob.P, 2, C.byref(t), C.byref(persistent)) == 0
+        assert libbfm.bfm_gpu_problem_time_precond(prob.P, 2, C.byref(t), None, C.byref(persistent)) == 0
         assert persistent.value == 0
         x2 = prob.solution()
     finally:
