@@ -1624,28 +1624,36 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 // M^-1 = M_SSOR^-1 + P A_c^-1 P^T, A_c = P^T A P: one aggregate per cell of a
 // grid laid over the mesh's bounding box, three coarse DOFs per aggregate
 // (the two translations and the rotation about the cell centre, scaled by
-// the cell size H), rows of constrained DOFs zero.  The sweeps add P yc to z
-// when they store it, so the recursion itself stays M_SSOR^-1.
+// the cell size H), rows of constrained DOFs zero.  The cells are numbered
+// along the grid's shorter side first, so A_c, which couples each cell with
+// the 8 around it, is a band matrix of half-width bw = 3 (short side + 1) + 2.
+// Its band Cholesky factor L gives X = L^-1 (a dense lower triangle, stored
+// in FP32), and the correction is applied as yc = X^T (X P^T r) with
+// double-float sums: symmetric positive (semi)definite by construction,
+// whatever the rounding of X.  The sweeps add P yc to z when they store it,
+// so the recursion itself stays M_SSOR^-1.
 
 struct CoarseArgs {
 	int na, nc;               // aggregates (cells), coarse DOFs (3 na)
-	int gx;                   // cells per grid row: cell I = cx + gx cy
+	int gx, gy, xfast;        // cell grid; cell (cx, cy) is cx + gx cy when xfast, else cy + gy cx
+	int bw;                   // half-bandwidth of A_c
 	const int* agg_ptr;       // nodes of aggregate I: agg_nodes[agg_ptr[I] .. agg_ptr[I + 1]), ascending
 	const int* agg_nodes;
 	const int* agg;
 	const float4* pnode;
-	double* ainv;             // A_c, then A_c^-1 in place (nc x nc, row-major)
-	double* diag0;            // Gauss-Jordan: A_c's diagonal before elimination (the drop test)
-	float2* yc;               // A_c^-1 P^T r (double-float pairs)
-	double* rc;               // P^T r
+	double* band;             // A_c, then L in place: entry (i, i - t) at band[i (bw + 1) + t], 1 / L_ii on the diagonal
+	double* diag0;            // A_c's diagonal (the pivot test)
+	float* xl;                // X = L^-1 by rows: row i (columns 0..i) at xrow(i), rows padded to 4 floats
+	float* xu;                // X^T by rows: row j (columns j..nc-1) at xrow(nc - 1 - j)
+	float2* rc;               // P^T r          (double-float pairs, 4 zero pads after the last)
+	float2* yt;               // X rc           (the same)
+	float2* yc;               // X^T X rc
 	const void* r;
 	int df;                   // r in double-float (float4 per node) or FP64 (double2)
 	const int* row_ptr;
 	const int* cols;
 	const double* vals64;
 	int* err;
-	unsigned* bar;
-	int* gj_err;
 	// chunks of at most COARSE_CHUNK nodes of one aggregate: chunk q covers
 	// agg_nodes[chunk_start[q] .. chunk_start[q + 1]) of aggregate chunk_agg[q];
 	// the chunks of aggregate I are [agg_chunk[I], agg_chunk[I + 1])
@@ -1654,12 +1662,69 @@ struct CoarseArgs {
 	const int* chunk_agg;
 	const int* agg_chunk;
 	double* part;        // per chunk: 3 (restriction) or 81 (coarse matrix) partial sums
-	double* gjt;         // blocked Gauss-Jordan: pivot block inverse (GJB^2), row panel (GJB x nc), column panel (nc x GJB)
 };
 
-constexpr int GJB = 32;  // pivot block of the blocked Gauss-Jordan inversion
-
 constexpr int COARSE_CHUNK = 128;
+constexpr int COARSE_MAX_BW = 101;  // widest band: the factorisation's shared window and the solve's registers
+constexpr int CHOL_T = 512;         // threads of the factorisation block
+constexpr int LINV_C = 8;           // columns per warp of the inversion (4 lanes each)
+constexpr int LINV_W = 4;           // warps per block of the inversion
+
+__host__ __device__ __forceinline__ void cell_xy(int I, int gx, int gy, int xfast, int& cx, int& cy) {
+	if (xfast) {
+		cx = I % gx;
+		cy = I / gx;
+	}
+	else {
+		cy = I % gy;
+		cx = I / gy;
+	}
+}
+__host__ __device__ __forceinline__ int cell_id(int cx, int cy, int gx, int gy, int xfast) {
+	return xfast ? cx + gx * cy : cy + gy * cx;
+}
+// start of row i of a triangle whose row i has i + 1 entries, each row padded
+// to a multiple of 4 floats (16-byte rows): rows 4q .. 4q + 3 take 4 (q + 1) each
+__host__ __device__ __forceinline__ long xrow(int i) {
+	long const q = i / 4, r = i % 4;
+	return 4 * (q + 1) * (2 * q + r);
+}
+
+// shared memory of the factorisation: the (bw + 2)^2 window, the scaled
+// column, the next pivot, the update's (row, column) pairs
+__host__ __device__ constexpr size_t chol_smem(int bw) {
+	return sizeof(double) * ((size_t) (bw + 2) * (bw + 2) + (bw + 2) + 2) + sizeof(short2) * ((size_t) bw * (bw + 1) / 2);
+}
+// shared memory of the inversion: per warp LINV_C column rings and two staged rows of L
+__host__ __device__ constexpr size_t linv_smem(int bw) {
+	return sizeof(double) * LINV_W * ((size_t) LINV_C * (bw + 2) + 2 * (bw + 1));
+}
+
+// 1 / sqrt(p) for the factorisation's pivots: the FP32 estimate rsqrtf
+// refined by two Newton-Raphson steps y <- y (3 - p y^2) / 2 in FP64
+// (quadratic convergence: about 23 -> 46 -> full precision); 1 / sqrt(p) for
+// p outside FP32's normal range
+__device__ __forceinline__ double rsqrt_nr(double p) {
+	if (!(p > 1e-30 && p < 1e30)) return 1.0 / sqrt(p);
+	double y = (double) rsqrtf((float) p);
+	y = y * (1.5 - 0.5 * p * y * y);
+	y = y * (1.5 - 0.5 * p * y * y);
+	return y;
+}
+
+// per node its offset from its cell's centre (scaled by the cell size H) and
+// which of its DOFs are free (constrained ones get no coarse correction)
+__global__ void k_pnode(int N, const double* __restrict__ coords, const int* __restrict__ agg, const int* __restrict__ last_ci,
+                        double x0, double y0, double cw, double ch, int gx, int gy, int xfast, double H,
+                        float4* __restrict__ pnode) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	int cx, cy;
+	cell_xy(agg[i], gx, gy, xfast, cx, cy);
+	double const xc = x0 + (cx + 0.5) * cw, yc = y0 + (cy + 0.5) * ch;
+	pnode[i] = make_float4((float) ((coords[2l * i] - xc) / H), (float) ((coords[2l * i + 1] - yc) / H),
+	                       last_ci[2l * i] < 0 ? 1.f : 0.f, last_ci[2l * i + 1] < 0 ? 1.f : 0.f);
+}
 
 // rc = P^T r in two deterministic stages: one warp per chunk of an
 // aggregate (lanes in a fixed stride, double-float sums, a fixed shuffle
@@ -1703,28 +1768,57 @@ __global__ void k_restrict_sum(CoarseArgs a) {
 	int const I = t / 3, m = t % 3;
 	double s = 0.0;
 	for (int q = a.agg_chunk[I]; q < a.agg_chunk[I + 1]; q++) s += a.part[3l * q + m];
-	a.rc[t] = s;
+	dfl const v = df_make(s);
+	a.rc[t] = make_float2(v.hi, v.lo);
 }
 
-// yc = A_c^-1 rc: one block per coarse row, fixed thread stride, warp
-// shuffle trees and the warps' sums in order (deterministic)
-__global__ void __launch_bounds__(TPB_K) k_coarse_mv(CoarseArgs a) {
-	__shared__ double ws[TPB_K / 32];
-	int const row = blockIdx.x;
-	if (row >= a.nc) return;
-	const double* m = a.ainv + (long) row * a.nc;
-	double s = 0.0;
-	for (int j = threadIdx.x; j < a.nc; j += blockDim.x) s += m[j] * a.rc[j];
+// one row of a padded FP32 triangle times a double-float vector: lane l takes
+// the 16-byte groups l, l + 32, .. (double-float products and sums), then a
+// fixed shuffle tree (deterministic; every lane gets the sum)
+__device__ __forceinline__ dfl coarse_row_dot(const float* __restrict__ row, int len, const float2* __restrict__ v, int lane) {
+	constexpr int U = 4;  // groups per lane in flight
+	dfl s = {0.f, 0.f};
+	int const ng = (len + 3) >> 2;
+	const float4* r4 = reinterpret_cast<const float4*>(row);
+	for (int g0 = lane; g0 < ng; g0 += 32 * U) {
+		float4 x[U];
 #pragma unroll
-	for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-	if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		double t = 0.0;
-		for (int w = 0; w < (int) (blockDim.x >> 5); w++) t += ws[w];
-		dfl const y = df_make(t);
-		a.yc[row] = make_float2(y.hi, y.lo);
+		for (int u = 0; u < U; u++) {
+			int const g = g0 + 32 * u;
+			x[u] = g < ng ? __ldg(r4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			int const g = g0 + 32 * u;
+			if (g < ng) {
+				float2 const v0 = v[4 * g], v1 = v[4 * g + 1], v2 = v[4 * g + 2], v3 = v[4 * g + 3];
+				s = df_add(s, df_mul_f(x[u].x, {v0.x, v0.y}));
+				s = df_add(s, df_mul_f(x[u].y, {v1.x, v1.y}));
+				s = df_add(s, df_mul_f(x[u].z, {v2.x, v2.y}));
+				s = df_add(s, df_mul_f(x[u].w, {v3.x, v3.y}));
+			}
+		}
 	}
+#pragma unroll
+	for (int o = 16; o; o >>= 1) s = df_add(s, {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+	return s;
+}
+
+// yt = X rc: one warp per row of X (the padding of a row is zero, and rc has
+// zero pads past its end)
+__global__ void k_coarse_x(CoarseArgs a) {
+	int const i = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (i >= a.nc) return;
+	dfl const s = coarse_row_dot(a.xl + xrow(i), i + 1, a.rc, lane);
+	if (lane == 0) a.yt[i] = make_float2(s.hi, s.lo);
+}
+
+// yc = X^T yt, the same way over the rows of X^T (row j starts at column j)
+__global__ void k_coarse_xt(CoarseArgs a) {
+	int const j = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (j >= a.nc) return;
+	dfl const s = coarse_row_dot(a.xu + xrow(a.nc - 1 - j), a.nc - j, a.yt + j, lane);
+	if (lane == 0) a.yc[j] = make_float2(s.hi, s.lo);
 }
 
 // A_c = P^T A P in two deterministic stages.  One warp per chunk of
@@ -1736,8 +1830,8 @@ __global__ void __launch_bounds__(TPB_K) k_coarse_mv(CoarseArgs a) {
 __global__ void k_coarse_ac(CoarseArgs a) {
 	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if (q >= a.nchunk) return;
-	int const I = a.chunk_agg[q];
-	int const cx = I % a.gx, cy = I / a.gx;
+	int cx, cy;
+	cell_xy(a.chunk_agg[q], a.gx, a.gy, a.xfast, cx, cy);
 	double acc[9][9];
 	for (int s = 0; s < 9; s++)
 		for (int t = 0; t < 9; t++) acc[s][t] = 0.0;
@@ -1747,8 +1841,9 @@ __global__ void k_coarse_ac(CoarseArgs a) {
 		double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
 		for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
 			int const j = a.cols[e];
-			int const J = a.agg[j];
-			int const ox = J % a.gx - cx, oy = J / a.gx - cy;
+			int jx, jy;
+			cell_xy(a.agg[j], a.gx, a.gy, a.xfast, jx, jy);
+			int const ox = jx - cx, oy = jy - cy;
 			if (ox < -1 || ox > 1 || oy < -1 || oy > 1) {
 				atomicOr(a.err, 1);
 				continue;
@@ -1776,127 +1871,173 @@ __global__ void k_coarse_ac(CoarseArgs a) {
 		}
 }
 
+// The chunks' sums per aggregate into the lower band of A_c, each entry the
+// mean of itself and its transpose (the same coupling seen from the other
+// cell: the mirrored slot, u and v swapped), and the diagonal saved for the
+// pivot test.  Coarse DOFs without any coupling -- empty cells, all-constrained
+// or degenerate modes -- get a zero diagonal, which the pivot test drops.
 __global__ void k_coarse_ac_sum(CoarseArgs a) {
 	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
 	if (t >= 81l * a.na) return;
 	int const I = (int) (t / 81), e = (int) (t % 81), s = e / 9, u = (e % 9) / 3, v = e % 3;
-	int const jx = I % a.gx + s % 3 - 1, jy = I / a.gx + s / 3 - 1;
-	if (jx < 0 || jx >= a.gx || jy < 0 || jy * a.gx >= a.na) return;
-	double x = 0.0;
-	for (int q = a.agg_chunk[I]; q < a.agg_chunk[I + 1]; q++) x += a.part[81l * q + e];
-	int const J = jx + a.gx * jy;
-	a.ainv[(long) (3 * I + u) * a.nc + 3 * J + v] = x;
-}
-
-// symmetric average (i < j), and the diagonal saved for the pivot test
-// (coarse DOFs without any coupling -- empty cells, all-constrained or
-// degenerate modes -- have a zero diagonal and are dropped by it)
-__global__ void k_coarse_sym(CoarseArgs a) {
-	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
-	if (t >= (long) a.nc * a.nc) return;
-	int const i = (int) (t / a.nc), j = (int) (t % a.nc);
-	if (i < j) {
-		double const m = 0.5 * (a.ainv[(long) i * a.nc + j] + a.ainv[(long) j * a.nc + i]);
-		a.ainv[(long) i * a.nc + j] = m;
-		a.ainv[(long) j * a.nc + i] = m;
+	int cx, cy;
+	cell_xy(I, a.gx, a.gy, a.xfast, cx, cy);
+	int const jx = cx + s % 3 - 1, jy = cy + s / 3 - 1;
+	if (jx < 0 || jx >= a.gx || jy < 0 || jy >= a.gy) return;
+	int const J = cell_id(jx, jy, a.gx, a.gy, a.xfast);
+	int const row = 3 * I + u, col = 3 * J + v;
+	if (row < col) return;
+	if (row - col > a.bw) {
+		atomicOr(a.err, 1);
+		return;
 	}
-	if (i == j) a.diag0[i] = a.ainv[(long) i * a.nc + i];
+	double x = 0.0, y = 0.0;
+	for (int q = a.agg_chunk[I]; q < a.agg_chunk[I + 1]; q++) x += a.part[81l * q + e];
+	int const et = 9 * (8 - s) + 3 * v + u;
+	for (int q = a.agg_chunk[J]; q < a.agg_chunk[J + 1]; q++) y += a.part[81l * q + et];
+	double const m = 0.5 * (x + y);
+	a.band[(long) row * (a.bw + 1) + (row - col)] = m;
+	if (row == col) a.diag0[row] = m;
 }
 
-// Blocked Gauss-Jordan (pivot blocks of GJB): per step K = [k0, k0 + kb),
-//   A_KK <- A_KK^-1,  A_Kj <- A_KK^-1 A_Kj,  A_iK <- -A_iK A_KK^-1,
-//   A_ij <- A_ij - A_iK A_KK^-1 A_Kj   (i, j outside K),
-// which after the last block leaves A^-1 in place.  The pivot block is
-// inverted by block 0 in shared memory (unblocked; a pivot below 1e-12 of
-// its original diagonal -- a coarse mode that A barely sees: an empty cell,
-// the rotation of a single node -- drops that DOF, whose row and column of
-// the inverse are then zero); the rank-kb update runs over 32 x 32 tiles staged in
-// shared memory.  Three grid barriers per block step; every read of the
-// matrix and the panels goes past L1.
-__global__ void __launch_bounds__(256) k_coarse_gjb(CoarseArgs a) {
-	__shared__ double D[GJB][GJB + 1];
-	__shared__ double Cs[32][GJB + 1];
-	__shared__ double Rs[GJB][32 + 1];
-	int const n = a.nc;
-	double* T = a.gjt;                      // GJB x GJB
-	double* Rp = a.gjt + GJB * GJB;         // GJB x n
-	double* Cp = Rp + (long) GJB * n;       // n x GJB
-	long const tid = blockIdx.x * (long) blockDim.x + threadIdx.x, stride = (long) gridDim.x * blockDim.x;
-	for (int k0 = 0; k0 < n; k0 += GJB) {
-		int const kb = n - k0 < GJB ? n - k0 : GJB;
-		if (blockIdx.x == 0) {
-			for (int e = threadIdx.x; e < GJB * GJB; e += blockDim.x) {
-				int const r = e / GJB, c = e % GJB;
-				D[r][c] = r < kb && c < kb ? __ldcg(a.ainv + (long) (k0 + r) * n + k0 + c) : 0.0;
-			}
-			__syncthreads();
-			for (int k = 0; k < kb; k++) {
-				__shared__ double col[GJB];
-				double const p = D[k][k];
-				bool const drop = !(p > 1e-12 * a.diag0[k0 + k]);
-				double const ip = drop ? 0.0 : 1.0 / p;
-				if (threadIdx.x < GJB) col[threadIdx.x] = threadIdx.x == k || drop ? 0.0 : D[threadIdx.x][k];
-				__syncthreads();
-				if (threadIdx.x < GJB && threadIdx.x != k) D[k][threadIdx.x] = drop ? 0.0 : D[k][threadIdx.x] * ip;
-				__syncthreads();
-				if (threadIdx.x == 0) D[k][k] = ip;
-				__syncthreads();
-				for (int e = threadIdx.x; e < GJB * GJB; e += blockDim.x) {
-					int const i = e / GJB, j = e % GJB;
-					if (i == k || i >= kb || j >= kb) continue;
-					D[i][j] = j == k ? -col[i] * D[k][k] : D[i][j] - col[i] * D[k][j];
-				}
-				__syncthreads();
-			}
-			for (int e = threadIdx.x; e < GJB * GJB; e += blockDim.x) T[e] = D[e / GJB][e % GJB];
+// Band Cholesky A_c = L L^T in place, one block.  The active part of the
+// trailing matrix (rows k .. k + bw, their band) lives in a (bw + 2)^2 window
+// in shared memory, rows in a ring.  Step k: the pivot p = S_kk; p at or below
+// 1e-12 of A_c's diagonal entry (a coarse mode that A barely sees: an empty
+// cell, the rotation of a single node) drops DOF k: its column of L is zero
+// and 1 / L_kk = 0 marks it, so the factorisation goes on as that of A_c
+// without that DOF.  Otherwise column k is scaled by 1/sqrt(p) and written
+// out (the diagonal holds 1/sqrt(p)), the next row of A_c (loaded while the
+// column is scaled) enters the ring slot of the finished row k - 1, and the
+// window takes the rank-1 update; the thread that updates S_{k+1,k+1} then
+// forms the next pivot's 1/sqrt.  Two barriers per step.
+__global__ void __launch_bounds__(CHOL_T) k_coarse_chol(CoarseArgs a) {
+	extern __shared__ double sm[];
+	int const n = a.nc, bw = a.bw, B = bw + 1, M = bw + 2;
+	double* W = sm;                     // entry (r, c) at W[(r % M) M + c % M]
+	double* col = W + M * M;            // scaled column k (rows k + 1 ..)
+	double* piv = col + M;              // 1/sqrt of the current pivot (0: dropped)
+	short2* pr = reinterpret_cast<short2*>(piv + 2);  // update pairs (ii, jj), jj <= ii < bw, by rows
+	for (int ii = threadIdx.x; ii < bw; ii += blockDim.x)
+		for (int jj = 0; jj <= ii; jj++) pr[ii * (ii + 1) / 2 + jj] = make_short2((short) ii, (short) jj);
+	for (int e = threadIdx.x; e < B * B; e += blockDim.x) {
+		int const r = e / B, t = e % B;
+		if (r < n && r - t >= 0) W[(r % M) * M + (r - t) % M] = a.band[(long) r * B + t];
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) piv[0] = W[0] > 1e-12 * a.diag0[0] ? rsqrt_nr(W[0]) : 0.0;
+	__syncthreads();
+	// ring slots advance with k: s1 = (k + 1) % M, sk = k % M; the row entering
+	// at step k (k + bw + 1) was loaded one step earlier
+	int const tx = threadIdx.x;
+	double nv = (bw + 1 < n && tx < B) ? a.band[(long) (bw + 1) * B + tx] : 0.0;
+	int sk = 0;
+	for (int k = 0; k < n; k++) {
+		double const isq = piv[0];
+		int const s1 = sk + 1 == M ? 0 : sk + 1;
+		int const m = min(bw, n - 1 - k);  // rows k + 1 .. k + m below the pivot
+		int const r = k + bw + 1;
+		bool const ld = r < n && tx < B;
+		double const nv2 = (r + 1 < n && tx < B) ? a.band[(long) (r + 1) * B + tx] : 0.0;
+		for (int ii = tx; ii < m; ii += blockDim.x) {
+			int si = s1 + ii;
+			si -= si >= M ? M : 0;
+			double const c = W[si * M + sk] * isq;
+			col[ii] = c;
+			a.band[(long) (k + 1 + ii) * B + ii + 1] = c;
 		}
-		if (!grid_barrier(a.bar, a.gj_err)) return;
-		// panels: Rp = A_KK^-1 A_Kj (j outside K), Cp = A_iK (i outside K)
-		for (long e = tid; e < (long) kb * n; e += stride) {
-			int const r = (int) (e / n), j = (int) (e % n);
-			if (j >= k0 && j < k0 + kb) continue;
-			double x = 0.0;
-			for (int m = 0; m < kb; m++) x += __ldcg(T + r * GJB + m) * __ldcg(a.ainv + (long) (k0 + m) * n + j);
-			Rp[(long) r * n + j] = x;
+		if (tx == 0) a.band[(long) k * B] = isq;
+		if (ld) {
+			// row r's slot is that of row k - 1, i.e. sk - 1; entry (r, r - tx) at column slot (r - tx) % M
+			int const sr = sk == 0 ? M - 1 : sk - 1;
+			int sc = sr - tx;
+			sc += sc < 0 ? M : 0;
+			W[sr * M + sc] = nv;
 		}
-		for (long e = tid; e < (long) n * kb; e += stride) {
-			int const i = (int) (e / kb), m = (int) (e % kb);
-			Cp[(long) i * GJB + m] = (i >= k0 && i < k0 + kb) ? 0.0 : __ldcg(a.ainv + (long) i * n + k0 + m);
+		nv = nv2;
+		__syncthreads();
+		int const nu = m * (m + 1) / 2;
+		for (int e = tx; e < nu; e += blockDim.x) {
+			short2 const q = pr[e];
+			int si = s1 + q.x, sj = s1 + q.y;
+			si -= si >= M ? M : 0;
+			sj -= sj >= M ? M : 0;
+			W[si * M + sj] -= col[q.x] * col[q.y];
 		}
-		if (!grid_barrier(a.bar, a.gj_err)) return;
-		// the update, 32 x 32 tiles
-		int const nt = (n + 31) / 32;
-		for (long tile = blockIdx.x; tile < (long) nt * nt; tile += gridDim.x) {
-			int const i0 = (int) (tile / nt) * 32, j0 = (int) (tile % nt) * 32;
-			for (int e = threadIdx.x; e < 32 * GJB; e += blockDim.x) {
-				int const r = e / GJB, m = e % GJB;
-				Cs[r][m] = i0 + r < n && m < kb ? __ldcg(Cp + (long) (i0 + r) * GJB + m) : 0.0;
-				int const mm = e / 32, c = e % 32;
-				Rs[mm][c] = j0 + c < n && mm < kb ? __ldcg(Rp + (long) mm * n + j0 + c) : 0.0;
+		if (tx == 0 && m > 0) {
+			// pair 0 is S_{k+1,k+1}, updated by this thread above
+			double const p = W[s1 * M + s1];
+			piv[0] = p > 1e-12 * a.diag0[k + 1] ? rsqrt_nr(p) : 0.0;
+		}
+		sk = s1;
+		__syncthreads();
+	}
+}
+
+// X = L^-1 by columns: each warp takes LINV_C consecutive columns j0 ..,
+// four lanes per column (lane h of a column takes the band entries t = 1 + h,
+// 5 + h, ..), a shuffle sum over the four, forward substitution down the
+// band from row j0 (rows above a column's own j come out zero).  The rows of
+// L are staged in shared memory (the next one loaded while this one is
+// used), each column's last bw values in a shared ring.  A dropped DOF
+// (1 / L_ii = 0) gets a zero row, and a zero column.  X is written, rounded
+// to FP32, by rows to xl and transposed to xu.
+__global__ void __launch_bounds__(32 * LINV_W) k_coarse_linv(CoarseArgs a) {
+	extern __shared__ double lsm[];
+	constexpr int NL = (COARSE_MAX_BW + 1 + 31) / 32;  // row entries per lane when staging
+	int const n = a.nc, bw = a.bw, B = bw + 1, M = bw + 2;
+	int const w = threadIdx.x >> 5, lane = threadIdx.x & 31, c = lane >> 2, h = lane & 3;
+	int const j0 = (blockIdx.x * LINV_W + w) * LINV_C;
+	if (j0 >= n) return;
+	double* ring = lsm + (size_t) w * (LINV_C * M + 2 * B);
+	double* Lr = ring + LINV_C * M;
+	int const j = j0 + c;
+	for (int t = lane; t < LINV_C * M; t += 32) ring[t] = 0.0;
+	for (int t = lane; t < B; t += 32) Lr[t] = a.band[(long) j0 * B + t];
+	__syncwarp();
+	double* R = ring + c * M;
+	int si = j0 % M;  // ring slot of row i
+	for (int i = j0; i < n; i++) {
+		const double* cur = Lr + ((i - j0) & 1) * B;
+		double* nxt = Lr + ((i - j0 + 1) & 1) * B;
+		double nv[NL];
+#pragma unroll
+		for (int u = 0; u < NL; u++) {
+			int const t = lane + 32 * u;
+			nv[u] = (i + 1 < n && t < B) ? a.band[(long) (i + 1) * B + t] : 0.0;
+		}
+		int const tmax = min(bw, i - j0);
+		double s0 = 0.0, s1 = 0.0;
+		// ring slot of row i - t, stepped down by 4 per term
+		int sl = si - 1 - h;
+		sl += sl < 0 ? M : 0;
+		for (int t = 1 + h; t <= tmax; t += 8) {
+			s0 += cur[t] * R[sl];
+			sl -= 4;
+			sl += sl < 0 ? M : 0;
+			if (t + 4 <= tmax) s1 += cur[t + 4] * R[sl];
+			sl -= 4;
+			sl += sl < 0 ? M : 0;
+		}
+		double s = s0 + s1;
+		s += __shfl_xor_sync(0xffffffffu, s, 1);
+		s += __shfl_xor_sync(0xffffffffu, s, 2);
+		double const x = ((i == j ? 1.0 : 0.0) - s) * cur[0];
+		__syncwarp();
+		if (h == 0 && j < n) {
+			R[si] = x;
+			if (i >= j) {
+				a.xl[xrow(i) + j] = (float) x;
+				a.xu[xrow(n - 1 - j) + (i - j)] = (float) x;
 			}
-			__syncthreads();
-			for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
-				int const r = e / 32, c = e % 32, i = i0 + r, j = j0 + c;
-				if (i >= n || j >= n) continue;
-				bool const iK = i >= k0 && i < k0 + kb, jK = j >= k0 && j < k0 + kb;
-				long const at = (long) i * n + j;
-				if (iK && jK) a.ainv[at] = __ldcg(T + (i - k0) * GJB + (j - k0));
-				else if (iK) a.ainv[at] = __ldcg(Rp + (long) (i - k0) * n + j);
-				else if (jK) {
-					double x = 0.0;
-					for (int m = 0; m < kb; m++) x += Cs[r][m] * __ldcg(T + m * GJB + (j - k0));
-					a.ainv[at] = -x;
-				}
-				else {
-					double x = 0.0;
-#pragma unroll 8
-					for (int m = 0; m < GJB; m++) x += Cs[r][m] * Rs[m][c];
-					a.ainv[at] = __ldcg(a.ainv + at) - x;
-				}
-			}
-			__syncthreads();
 		}
-		if (!grid_barrier(a.bar, a.gj_err)) return;
+#pragma unroll
+		for (int u = 0; u < NL; u++) {
+			int const t = lane + 32 * u;
+			if (t < B) nxt[t] = nv[u];
+		}
+		si = si + 1 == M ? 0 : si + 1;
+		__syncwarp();
 	}
 }
 

@@ -261,19 +261,6 @@ __global__ void k_rows_fill(int N, int kind, const int* __restrict__ inc_ptr, co
 // and its higher-colour neighbours in that order, and a colour is a
 // contiguous range of rows.
 
-// two-level SSOR: per node its offset from its cell's centre (scaled by the
-// cell size H) and which of its DOFs are free (constrained ones get no
-// coarse correction)
-__global__ void k_pnode(int N, const double* __restrict__ coords, const int* __restrict__ agg, const int* __restrict__ last_ci,
-                        double x0, double y0, double cw, double ch, int gx, double H, float4* __restrict__ pnode) {
-	int const i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= N) return;
-	int const I = agg[i];
-	double const xc = x0 + (I % gx + 0.5) * cw, yc = y0 + (I / gx + 0.5) * ch;
-	pnode[i] = make_float4((float) ((coords[2l * i] - xc) / H), (float) ((coords[2l * i + 1] - yc) / H),
-	                       last_ci[2l * i] < 0 ? 1.f : 0.f, last_ci[2l * i + 1] < 0 ? 1.f : 0.f);
-}
-
 // dst[i] = src[map[i]] for `width` consecutive elements per node
 template <typename T>
 __global__ void k_gather_nodes(long N, int width, const T* __restrict__ src, const int* __restrict__ map, T* __restrict__ dst) {
@@ -1337,22 +1324,22 @@ struct bfm_gpu_problem {
 	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
 	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
 
-	// two-level SSOR: aggregates are the cells of a gx x gy grid over the
-	// bounding box (origin ax0, ay0, cell acw x ach, rotation scale aH)
+	// two-level SSOR: aggregates are the cells of an agx x agy grid over the
+	// bounding box (origin ax0, ay0, cell acw x ach, rotation scale aH),
+	// numbered along the shorter side first (axfast: x is that side)
 	bool agg_valid;      // the aggregation belongs to the current node order and coordinates
-	int coarse_ok;       // A_c^-1 is ready (else the solve runs plain SSOR)
-	int na, nc, nc_cap, agx;
+	int coarse_ok;       // the coarse factor is ready (else the solve runs plain SSOR)
+	int na, nc, nc_cap, agx, agy, axfast, abw;
 	double ax0, ay0, acw, ach, aH;
 	int *agg, *agg_ptr, *agg_nodes;
 	int nchunk, chunk_cap;
 	int *chunk_start, *chunk_agg, *agg_chunk;
 	double* cpart;  // per chunk partial sums (81 doubles)
 	float4* pnode;
-	double *ainv, *diag0, *rc, *gjt;
-	float2* yc;
-	unsigned* gj_bar;
-	int* gj_err;
-	int gj_grid;
+	double *aband, *diag0;  // band A_c then L, the diagonal of A_c
+	float *xl, *xu;         // X = L^-1 and X^T by rows (FP32, padded rows)
+	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
+	int* coarse_err;
 };
 
 enum : unsigned { ORD_COORDS = 1, ORD_ELEMS = 2, ORD_MASKS = 4, ORD_EDGES = 8, ORD_FIELDS = 16, ORD_LEDGES = 32, ORD_ALL = 63 };
@@ -1632,35 +1619,73 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
 	c.na = P->na;
 	c.nc = P->nc;
 	c.gx = P->agx;
+	c.gy = P->agy;
+	c.xfast = P->axfast;
+	c.bw = P->abw;
 	c.agg_ptr = P->agg_ptr;
 	c.agg_nodes = P->agg_nodes;
 	c.agg = P->agg;
 	c.pnode = P->pnode;
-	c.ainv = P->ainv;
+	c.band = P->aband;
 	c.diag0 = P->diag0;
+	c.xl = P->xl;
+	c.xu = P->xu;
 	c.yc = P->yc;
 	c.rc = P->rc;
+	c.yt = P->ayt;
 	c.r = r;
 	c.df = df;
 	c.row_ptr = P->row_ptr;
 	c.cols = P->cols;
 	c.vals64 = P->vals64;
-	c.err = P->gj_err;
-	c.bar = P->gj_bar;
-	c.gj_err = P->gj_err;
+	c.err = P->coarse_err;
 	c.nchunk = P->nchunk;
 	c.chunk_start = P->chunk_start;
 	c.chunk_agg = P->chunk_agg;
 	c.agg_chunk = P->agg_chunk;
 	c.part = P->cpart;
-	c.gjt = P->gjt;
 	return c;
 }
 
+// Cells of the coarse grid for n nodes in a w x h box: about one per
+// `per_cell` nodes (BFM_GPU_COARSE_NODES, default 1250), at most 1024, as
+// square as the box allows, and fewer while the band factorisation (one
+// block, about 3 cells x bw^2 / 2 FP64 updates) would exceed 4e6 updates.
+// Returns the half-bandwidth of A_c for the short-side-first numbering.
+int coarse_grid(long n, double w, double h, int* gx_out, int* gy_out) {
+	long per_cell = 1250;
+	if (const char* e = getenv("BFM_GPU_COARSE_NODES")) {
+		long const v = atol(e);
+		if (v > 0) per_cell = v;
+	}
+	long target = n / per_cell;
+	target = target < 1 ? 1 : target > 1024 ? 1024 : target;
+	for (;;) {
+		int gx = 1, gy = 1;
+		if (w > 0 && h > 0) {
+			gx = (int) lround(sqrt((double) target * w / h));
+			gx = gx < 1 ? 1 : gx > target ? (int) target : gx;
+			gy = (int) lround((double) target / gx);
+			gy = gy < 1 ? 1 : gy;
+		}
+		else if (w > 0) gx = (int) target;
+		else if (h > 0) gy = (int) target;
+		int const gs = gx < gy ? gx : gy;
+		int const bw = 3 * (gs + 1) + 2;
+		double const cost = 1.5 * gx * gy * (double) bw * bw;
+		if ((bw <= COARSE_MAX_BW && cost <= 4e6) || target == 1) {
+			*gx_out = gx;
+			*gy_out = gy;
+			return bw;
+		}
+		target = target * 9 / 10;
+	}
+}
+
 // Aggregates for the current (working-order) coordinates: cells of a grid
-// over the bounding box, about one per 2,500 nodes (at most 384), as square
-// as the box allows; node lists per cell in ascending node order (a host
-// counting sort: deterministic).  Redone when the colouring is.
+// over the bounding box (coarse_grid), numbered along the shorter side
+// first; node lists per cell in ascending node order (a host counting sort:
+// deterministic).  Redone when the colouring is.
 int build_aggregates(bfm_gpu_problem* P) {
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
@@ -1672,7 +1697,7 @@ int build_aggregates(bfm_gpu_problem* P) {
 	if (!rc && (cudaMemcpyAsync(xy, P->coords, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
 	            cudaStreamSynchronize(st) != cudaSuccess))
 		rc = fail("coordinate copy failed");
-	int gx = 1, gy = 1;
+	int gx = 1, gy = 1, bw = 8;
 	double x0 = 0, y0 = 0, cw = 1, ch = 1;
 	if (!rc) {
 		double x1 = 0, y1 = 0;
@@ -1684,16 +1709,7 @@ int build_aggregates(bfm_gpu_problem* P) {
 			if (i == 0 || y > y1) y1 = y;
 		}
 		double const w = x1 - x0, h = y1 - y0;
-		long target = N / 2500;
-		target = target < 1 ? 1 : target > 384 ? 384 : target;
-		if (w > 0 && h > 0) {
-			gx = (int) lround(sqrt((double) target * w / h));
-			gx = gx < 1 ? 1 : gx > target ? (int) target : gx;
-			gy = (int) lround((double) target / gx);
-			gy = gy < 1 ? 1 : gy;
-		}
-		else if (w > 0) gx = (int) target;
-		else if (h > 0) gy = (int) target;
+		bw = coarse_grid(N, w, h, &gx, &gy);
 		// cells a hair wider than the box, so the far edge falls inside the last one
 		cw = w > 0 ? w * (1.0 + 1e-12) / gx : 1.0;
 		ch = h > 0 ? h * (1.0 + 1e-12) / gy : 1.0;
@@ -1701,7 +1717,7 @@ int build_aggregates(bfm_gpu_problem* P) {
 			int cx = (int) ((xy[2 * i] - x0) / cw), cy = (int) ((xy[2 * i + 1] - y0) / ch);
 			cx = cx < 0 ? 0 : cx >= gx ? gx - 1 : cx;
 			cy = cy < 0 ? 0 : cy >= gy ? gy - 1 : cy;
-			ag[i] = cx + gx * cy;
+			ag[i] = cell_id(cx, cy, gx, gy, gx <= gy);
 		}
 	}
 	int const na = gx * gy, nc = 3 * na;
@@ -1750,21 +1766,23 @@ int build_aggregates(bfm_gpu_problem* P) {
 		else P->chunk_cap = nchunk + 1;
 	}
 	if (!rc && nc > P->nc_cap) {
-		// (re)allocate for the larger coarse space
-		void* old[] = {P->agg_ptr, P->agg_chunk, P->ainv, P->diag0, P->rc, P->yc, P->gjt};
+		// (re)allocate for the larger coarse space (the band at the widest bandwidth)
+		void* old[] = {P->agg_ptr, P->agg_chunk, P->aband, P->diag0, P->rc, P->ayt, P->yc, P->xl, P->xu};
 		for (void* q : old)
 			if (q) cudaFree(q);
 		P->agg_ptr = P->agg_chunk = nullptr;
-		P->ainv = P->diag0 = P->rc = P->gjt = nullptr;
-		P->yc = nullptr;
-		if (dalloc(&P->agg_ptr, na + 1) || dalloc(&P->agg_chunk, na + 1) || dalloc(&P->ainv, (long) nc * nc) ||
-		    dalloc(&P->diag0, nc) || dalloc(&P->rc, nc) || dalloc(&P->yc, nc) ||
-		    dalloc(&P->gjt, (long) GJB * GJB + 2l * GJB * nc))
+		P->aband = P->diag0 = nullptr;
+		P->xl = P->xu = nullptr;
+		P->rc = P->ayt = P->yc = nullptr;
+		if (dalloc(&P->agg_ptr, na + 1) || dalloc(&P->agg_chunk, na + 1) ||
+		    dalloc(&P->aband, (long) nc * (COARSE_MAX_BW + 1)) || dalloc(&P->diag0, nc) || dalloc(&P->rc, nc + 4) ||
+		    dalloc(&P->ayt, nc + 4) || dalloc(&P->yc, nc) || dalloc(&P->xl, xrow(nc)) || dalloc(&P->xu, xrow(nc)) ||
+		    cudaMemsetAsync(P->rc, 0, (nc + 4) * sizeof(float2), st) != cudaSuccess ||
+		    cudaMemsetAsync(P->ayt, 0, (nc + 4) * sizeof(float2), st) != cudaSuccess)
 			rc = -1;
 		else P->nc_cap = nc;
 	}
-	if (!rc && !P->agg && (dalloc(&P->agg, N) || dalloc(&P->agg_nodes, N) || dalloc(&P->pnode, N) || dalloc(&P->gj_bar, 2) ||
-	                       dalloc(&P->gj_err, 1)))
+	if (!rc && !P->agg && (dalloc(&P->agg, N) || dalloc(&P->agg_nodes, N) || dalloc(&P->pnode, N) || dalloc(&P->coarse_err, 1)))
 		rc = -1;
 	if (!rc && (cudaMemcpyAsync(P->agg, ag, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
 	            cudaMemcpyAsync(P->agg_nodes, nodes, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
@@ -1782,18 +1800,13 @@ int build_aggregates(bfm_gpu_problem* P) {
 	free(cag);
 	free(ach);
 	if (rc) return rc;
-	if (!P->gj_grid) {
-		// one block per SM: each step is a small rank-1 update, the two grid
-		// barriers per step cost less with fewer blocks
-		int nb = 0;
-		CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_coarse_gjb, 256, 0));
-		if (nb < 1) return fail("the coarse inversion kernel does not fit on an SM");
-		P->gj_grid = num_sms();
-	}
 	P->na = na;
 	P->nc = nc;
 	P->nchunk = nchunk;
 	P->agx = gx;
+	P->agy = gy;
+	P->axfast = gx <= gy;
+	P->abw = bw;
 	P->ax0 = x0;
 	P->ay0 = y0;
 	P->acw = cw;
@@ -1804,8 +1817,8 @@ int build_aggregates(bfm_gpu_problem* P) {
 	return 0;
 }
 
-// Per assembly: node offsets and free DOFs, A_c = P^T A P, A_c^-1.  Any
-// failure (a neighbour beyond the adjacent cells, a barrier timeout) leaves
+// Per assembly: node offsets and free DOFs, A_c = P^T A P (band), its band
+// Cholesky factor and X = L^-1.  A neighbour beyond the adjacent cells leaves
 // the solve on plain SSOR (coarse_ok = 0).
 int coarse_setup(bfm_gpu_problem* P) {
 	cudaStream_t const st = P->stream;
@@ -1813,23 +1826,26 @@ int coarse_setup(bfm_gpu_problem* P) {
 	if (P->N == 0) return 0;
 	if (!P->agg_valid && build_aggregates(P)) return -1;
 	k_pnode<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->coords, P->agg, P->last_ci, P->ax0, P->ay0, P->acw, P->ach, P->agx,
-	                                          P->aH, P->pnode);
-	CK(cudaMemsetAsync(P->ainv, 0, (size_t) P->nc * P->nc * sizeof(double), st));
-	CK(cudaMemsetAsync(P->gj_err, 0, sizeof(int), st));
-	CK(cudaMemsetAsync(P->gj_bar, 0, 2 * sizeof(unsigned), st));
+	                                          P->agy, P->axfast, P->aH, P->pnode);
+	CK(cudaMemsetAsync(P->aband, 0, (size_t) P->nc * (P->abw + 1) * sizeof(double), st));
+	CK(cudaMemsetAsync(P->diag0, 0, (size_t) P->nc * sizeof(double), st));
+	CK(cudaMemsetAsync(P->coarse_err, 0, sizeof(int), st));
 	CoarseArgs ca = coarse_args(P, nullptr, true);
 	k_coarse_ac<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
 	k_coarse_ac_sum<<<blocks_for(81l * P->na), TPB, 0, st>>>(ca);
-	k_coarse_sym<<<blocks_for((long) P->nc * P->nc), TPB, 0, st>>>(ca);
 	int err = 0;
-	CK(cudaMemcpyAsync(&err, P->gj_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(&err, P->coarse_err, sizeof(int), cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 	if (err) return 0;
-	void* pa[1] = {&ca};
-	CK(cudaLaunchCooperativeKernel((const void*) k_coarse_gjb, dim3(P->gj_grid), dim3(256), pa, 0, st));
-	CK(cudaMemcpyAsync(&err, P->gj_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-	CK(cudaStreamSynchronize(st));
-	P->coarse_ok = !err;
+	CK(cudaFuncSetAttribute((const void*) k_coarse_chol, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                        (int) chol_smem(COARSE_MAX_BW)));
+	k_coarse_chol<<<1, CHOL_T, chol_smem(P->abw), st>>>(ca);
+	// the padding of X's rows stays zero (the products read whole 16-byte groups)
+	CK(cudaMemsetAsync(P->xl, 0, xrow(P->nc) * sizeof(float), st));
+	CK(cudaMemsetAsync(P->xu, 0, xrow(P->nc) * sizeof(float), st));
+	k_coarse_linv<<<(P->nc + LINV_C * LINV_W - 1) / (LINV_C * LINV_W), 32 * LINV_W, linv_smem(P->abw), st>>>(ca);
+	CK(cudaGetLastError());
+	P->coarse_ok = 1;
 	return 0;
 }
 
@@ -1951,11 +1967,12 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		// two-level: yc = A_c^-1 P^T r first; the sweeps add P yc to z
 		CoarseArgs ca = coarse_args(P, base.r, df);
 		void* pc[1] = {&ca};
-		cudaGraphNode_t n1, n2, n3;
+		cudaGraphNode_t n1, n2, n3, n4;
 		if (add_node(g, &n1, dep, (void*) k_restrict, blocks_for(32l * P->nchunk), pc)) return -1;
 		if (add_node(g, &n2, &n1, (void*) k_restrict_sum, blocks_for(P->nc), pc)) return -1;
-		if (add_node(g, &n3, &n2, (void*) k_coarse_mv, P->nc, pc)) return -1;
-		*last = n3;
+		if (add_node(g, &n3, &n2, (void*) k_coarse_x, blocks_for(32l * P->nc), pc)) return -1;
+		if (add_node(g, &n4, &n3, (void*) k_coarse_xt, blocks_for(32l * P->nc), pc)) return -1;
+		*last = n4;
 		dep = last;
 		base.agg = P->agg;
 		base.pnode = P->pnode;
@@ -2283,7 +2300,8 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 		if (coarse && with_coarse) {
 			k_restrict<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
 			k_restrict_sum<<<blocks_for(P->nc), TPB, 0, st>>>(ca);
-			k_coarse_mv<<<P->nc, TPB, 0, st>>>(ca);
+			k_coarse_x<<<blocks_for(32l * P->nc), TPB, 0, st>>>(ca);
+			k_coarse_xt<<<blocks_for(32l * P->nc), TPB, 0, st>>>(ca);
 		}
 		if (P->ssor_grid > 0) {
 			SsorArgs a = base;
@@ -2469,8 +2487,8 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	for (int i = 0; i < MAXF; i++)
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y,
-	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->ainv, P->diag0, P->rc, P->yc,
-	              P->gj_bar, P->gj_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart, P->gjt};
+	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
+	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart};
 	for (void* q : lb)
 		if (q) cudaFree(q);
 	if (P->ext && P->ext_free) P->ext_free(P->ext);

@@ -112,24 +112,40 @@ def pcg(A: sp.spmatrix, b: np.ndarray, apply, rtol: float = 1e-8, max_iters: int
     return x, max_iters
 
 
+def coarse_grid(n: int, w: float, h: float, per_cell: int = 1250):
+    """Cell counts (gx, gy) of the coarse grid for n nodes in a w x h box
+    (bfm_gb300/csrc/fem_gpu.cu, coarse_grid): about one cell per `per_cell`
+    nodes, at most 1024, as square as the box allows, and fewer while the band
+    factorisation's cost 1.5 cells bw^2 (bw = 3 (shorter side + 1) + 2, the
+    half-bandwidth of A_c for cells numbered along the shorter side first)
+    exceeds 4e6 or bw exceeds 101."""
+    target = min(max(n // per_cell, 1), 1024)
+    while True:
+        gx = gy = 1
+        if w > 0 and h > 0:
+            gx = min(max(int(np.floor(np.sqrt(target * w / h) + 0.5)), 1), target)
+            gy = max(int(np.floor(target / gx + 0.5)), 1)
+        elif w > 0:
+            gx = target
+        elif h > 0:
+            gy = target
+        bw = 3 * (min(gx, gy) + 1) + 2
+        if (bw <= 101 and 1.5 * gx * gy * bw * bw <= 4e6) or target == 1:
+            return gx, gy
+        target = target * 9 // 10
+
+
 def cell_grid(coords: np.ndarray):
     """The aggregation of the two-level preconditioner (bfm_gb300/csrc/
-    fem_gpu.cu, build_aggregates): a grid of cells over the bounding box, about
-    one cell per 2,500 nodes (at most 384), as square as the box allows.
-    Returns (cell of each node, gx, gy, x0, y0, cw, ch)."""
+    fem_gpu.cu, build_aggregates): the coarse_grid cells over the bounding box.
+    Returns (cell of each node, gx, gy, x0, y0, cw, ch); cells are numbered
+    cx + gx cy here (the GPU numbers them along the shorter side first, which
+    only reorders the coarse DOFs)."""
     n = len(coords)
     x0, y0 = coords.min(0)
     x1, y1 = coords.max(0)
     w, h = x1 - x0, y1 - y0
-    target = min(max(n // 2500, 1), 384)
-    gx = gy = 1
-    if w > 0 and h > 0:
-        gx = min(max(int(np.floor(np.sqrt(target * w / h) + 0.5)), 1), target)
-        gy = max(int(np.floor(target / gx + 0.5)), 1)
-    elif w > 0:
-        gx = target
-    elif h > 0:
-        gy = target
+    gx, gy = coarse_grid(n, w, h)
     cw = w * (1 + 1e-12) / gx if w > 0 else 1.0
     ch = h * (1 + 1e-12) / gy if h > 0 else 1.0
     cx = np.clip(((coords[:, 0] - x0) / cw).astype(np.int64), 0, gx - 1)

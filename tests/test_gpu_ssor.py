@@ -246,7 +246,7 @@ def test_per_colour_kernels_match_the_persistent_kernel(libbfm, precision, monke
 @pytest.mark.parametrize("precision,tol", [(bfm_gb300.FP64, 1e-10), (bfm_gb300.FP64_DF, 1e-8)])
 def test_two_level_matches_direct_oracle_and_restatement(libbfm, precision, tol):
     """Two-level SSOR (additive rigid-body coarse correction on a cell grid)
-    on a 256x64 plate (5 cells): the solution against the direct oracle, the
+    on a 256x64 plate (7 x 2 cells): the solution against the direct oracle, the
     iteration count against the float64 restatement with the GPU's own
     colouring, and fewer iterations than plain SSOR."""
     p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
@@ -257,7 +257,7 @@ def test_two_level_matches_direct_oracle_and_restatement(libbfm, precision, tol)
         assert s2.status == 0 and s2.rel_residual <= 1e-10
         x, _, _ = O.solve_direct(p)
         assert rel(prob.solution(), x) < tol
-        # five cells only at this size; the 2048x512 plate's 390 cells cut 6,172 iterations to about 470
+        # 14 cells only at this size; the 2048x512 plate's 812 cells cut 6,172 iterations to a few hundred
         assert s2.iterations < 0.6 * s1.iterations, (s2.iterations, s1.iterations)
         perm, off, _ = ordering(prob)
         K, b = O.assemble_csr(p)
@@ -288,8 +288,9 @@ def test_untrained_learned_two_level_is_two_level(libbfm):
 @pytest.mark.parametrize("name", ["p1_16x8_nt", "q1_24x8_jitter", "axi_p1_12x8", "lepl8", "gear12"])
 def test_sim_run_with_two_level(libbfm, name, monkeypatch):
     """bfm_sim_run with the two-level SSOR on every fixture (a single cell on
-    these small meshes: the coarse space is the three rigid-body modes of the
-    whole body), against the FP64 direct oracle."""
+    the small meshes: the coarse space is the three rigid-body modes of the
+    whole body; three on gear12, some of them nearly empty), against the FP64
+    direct oracle."""
     monkeypatch.setenv("BFM_GPU_AXISYM_REFERENCE", "0")
     p, _ = load(name)
     if p.stress == 3:
