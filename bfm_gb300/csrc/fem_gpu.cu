@@ -389,6 +389,8 @@ struct AsmArgs {
 	const float4* coords32;  // FP32 integration: per node (x hi, y hi, x lo, y lo)
 	int const_grad;          // FP32 integration: shape gradients equal at every Gauss point (P1)
 	const float4* mat32;     // FP32 integration: per-element (a, b, c) material constants, or nullptr
+	const double* egrad;     // exact P1 integration: per element dx[3], dy[3], det w, a, b, c (k_elem_grad), or nullptr
+	int NE;
 	double* dinv64;  // jacobi: 2 per node; block-jacobi: 4 per node
 	float* dinv32;
 	int precond;
@@ -434,6 +436,43 @@ __global__ void k_split_coords(int N, const double* __restrict__ coords, float4*
 	double2 const c = reinterpret_cast<const double2*>(coords)[i];
 	float const xh = (float) c.x, yh = (float) c.y;
 	out[i] = make_float4(xh, yh, (float) (c.x - (double) xh), (float) (c.y - (double) yh));
+}
+
+// Exact FP64 integration of P1 elements under a rule whose shape gradients
+// and weights are the same at every point: the Jacobian, the shape gradients
+// and det w then come out the same at every point (the same operations on
+// the same values), so they are formed once per element here -- in the
+// operation order of k_assemble<true> below, at point 0 -- instead of once per
+// owner row and point (three rows, three points).  Per element, 10 doubles:
+// dx[3], dy[3], det w, and the material constants a, b, c.
+__global__ void k_elem_grad(AsmArgs a, double* __restrict__ eg) {
+	int const e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= a.NE) return;
+	double x[3], y[3];
+	for (int j = 0; j < 3; j++) {
+		int const m = a.elems[3l * e + j];
+		x[j] = a.coords[2l * m];
+		y[j] = a.coords[2l * m + 1];
+	}
+	double dx_dxsi = 0, dx_deta = 0, dy_dxsi = 0, dy_deta = 0;
+	for (int j = 0; j < 3; j++) {
+		dx_dxsi = xa(dx_dxsi, xm(x[j], a.rule.dxi[0][j]));
+		dx_deta = xa(dx_deta, xm(x[j], a.rule.deta[0][j]));
+		dy_dxsi = xa(dy_dxsi, xm(y[j], a.rule.dxi[0][j]));
+		dy_deta = xa(dy_deta, xm(y[j], a.rule.deta[0][j]));
+	}
+	double const det = fabs(xs(xm(dx_dxsi, dy_deta), xm(dx_deta, dy_dxsi)));
+	double* o = eg + 10l * e;
+	for (int j = 0; j < 3; j++) {
+		o[j] = xd(xs(xm(a.rule.dxi[0][j], dy_deta), xm(a.rule.deta[0][j], dy_dxsi)), det);
+		o[3 + j] = xd(xs(xm(a.rule.deta[0][j], dx_dxsi), xm(a.rule.dxi[0][j], dx_deta)), det);
+	}
+	o[6] = xm(det, a.rule.w[0]);
+	double ea, eb, ec;
+	material_abc(a.elemE ? a.elemE[e] : a.E, a.elemNu ? a.elemNu[e] : a.nu, a.stress, ea, eb, ec);
+	o[7] = ea;
+	o[8] = eb;
+	o[9] = ec;
 }
 
 // One thread per node row (owner computes, no atomics): walk the node's
@@ -494,6 +533,46 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 			material_abc(E, nu, a.stress, ea, eb, ec);
 		}
 		if constexpr (EXACT) {
+			if (a.egrad) {
+				// P1 with point-independent gradients (k_elem_grad): this row's
+				// contributions formed once, then added once per point in the
+				// order of the loop below, so the sums are the same bit for bit
+				const double* g = a.egrad + 10l * e;
+				double const dw = g[6];
+				ea = g[7];
+				eb = g[8];
+				ec = g[9];
+				for (int q = 0; q < a.rule.nq; q++) {
+					double const ph = a.rule.phi[q][jr];
+					for (int f = 0; f < a.forces.nf; f++) {
+						double fx = a.forces.f[f][0], fy = a.forces.f[f][1];
+						if (a.forces.field[f]) {
+							fx = a.forces.field[f][2l * r];
+							fy = a.forces.field[f][2l * r + 1];
+						}
+						b0 = xa(b0, xm(xm(xm(dw, fx), a.rho), ph));
+						b1 = xa(b1, xm(xm(xm(dw, fy), a.rho), ph));
+					}
+				}
+				double const xj = g[jr], yj = g[3 + jr];
+				double c[3][4];
+				for (int k = 0; k < 3; k++) {
+					double const dk = g[k], ek = g[3 + k];
+					c[k][0] = xm(dw, xa(xm(xm(ea, xj), dk), xm(xm(ec, yj), ek)));
+					c[k][1] = xm(dw, xa(xm(xm(eb, xj), ek), xm(xm(ec, yj), dk)));
+					c[k][2] = xm(dw, xa(xm(xm(eb, yj), dk), xm(xm(ec, xj), ek)));
+					c[k][3] = xm(dw, xa(xm(xm(ea, yj), ek), xm(xm(ec, xj), dk)));
+				}
+				for (int q = 0; q < a.rule.nq; q++)
+					for (int k = 0; k < 3; k++) {
+						int const s = slot[k];
+						acc[s][0] = xa(acc[s][0], c[k][0]);
+						acc[s][1] = xa(acc[s][1], c[k][1]);
+						acc[s][2] = xa(acc[s][2], c[k][2]);
+						acc[s][3] = xa(acc[s][3], c[k][3]);
+					}
+				continue;
+			}
 			bool const axi = a.stress >= 2;
 			for (int q = 0; q < a.rule.nq; q++) {
 				double const w = a.rule.w[q];
@@ -1273,6 +1352,8 @@ struct bfm_gpu_problem {
 	float* srow_df;   // double-float path: block row sums (difference-form SpMV)
 	float4* coords32; // FP32 integration: hi/lo float split of the coordinates
 	float4* mat32;    // FP32 integration: per-element material constants
+	double* egrad;    // exact P1 integration: per-element gradients, det w and materials
+	int egrad_cap;
 	double* b;
 	int* last_ci;
 	double *first, *last;
@@ -2480,7 +2561,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->graph) cudaGraphExecDestroy(P->graph);
 	void* bufs[] = {P->coords, P->elems, P->elemE, P->elemNu, P->masks, P->edges, P->eboundary, P->cnt, P->inc_ptr, P->inc, P->cand,
 	                P->row_len, P->row_ptr, P->cols, P->ecnt, P->eptr, P->elist, P->scan_sums, P->scan_total, P->vals64,
-	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->mat32, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
+	                P->vals32, P->corr32, P->vals32lo, P->srow_df, P->coords32, P->mat32, P->egrad, P->b, P->last_ci, P->first, P->last, P->dinv64, P->dinv32, P->x, P->vec[0], P->vec[1], P->vec[2], P->vec[3], P->vec[4], P->vec[5],
 	                P->partials, P->ticket, P->st, P->err};
 	for (void* p : bufs)
 		if (p) cudaFree(p);
@@ -2834,6 +2915,24 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (precision != BFM_GPU_MIXED || P->stress >= 2) {
 		// (the FP32 element integration is planar only: axisymmetric
 		// mixed-precision solves round the exact FP64 values)
+		bool same_points = P->kind == 3 && P->stress < 2 && P->NE > 0;
+		for (int q = 1; q < P->rule.nq; q++) {
+			same_points &= P->rule.w[q] == P->rule.w[0];
+			for (int j = 0; j < P->kind; j++)
+				same_points &= P->rule.dxi[q][j] == P->rule.dxi[0][j] && P->rule.deta[q][j] == P->rule.deta[0][j];
+		}
+		if (same_points) {
+			if (P->NE > P->egrad_cap) {
+				if (P->egrad) cudaFree(P->egrad);
+				P->egrad = nullptr;
+				P->egrad_cap = 0;
+				if (dalloc(&P->egrad, 10l * P->NE)) return -1;
+				P->egrad_cap = P->NE;
+			}
+			a.NE = P->NE;
+			k_elem_grad<<<blocks_for(P->NE), TPB, 0, st>>>(a, P->egrad);
+			a.egrad = P->egrad;
+		}
 		k_assemble<true><<<blocks_for(N, 128), 128, 0, st>>>(a);
 		if (dfp || fp64_ssor) k_df_dinv<<<blocks_for(N), TPB, 0, st>>>(P->N, P->dinv64, P->dinv32, P->precond != BFM_GPU_PC_JACOBI);
 	}
