@@ -1654,6 +1654,8 @@ struct CoarseArgs {
 	const int* cols;
 	const double* vals64;
 	int* err;
+	unsigned* bar;       // grid barrier words of the one-launch form (k_coarse_apply)
+	int* berr;           // its timeout flag
 	// chunks of at most COARSE_CHUNK nodes of one aggregate: chunk q covers
 	// agg_nodes[chunk_start[q] .. chunk_start[q + 1]) of aggregate chunk_agg[q];
 	// the chunks of aggregate I are [agg_chunk[I], agg_chunk[I + 1])
@@ -1727,27 +1729,43 @@ __global__ void k_pnode(int N, const double* __restrict__ coords, const int* __r
 }
 
 // rc = P^T r in two deterministic stages: one warp per chunk of an
-// aggregate (lanes in a fixed stride, double-float sums, a fixed shuffle
-// tree), then per aggregate the chunks' sums in chunk order
-__global__ void k_restrict(CoarseArgs a) {
-	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-	if (q >= a.nchunk) return;
-	dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
-	for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
-		int const i = a.agg_nodes[k];
-		dfl r0, r1;
-		if (a.df) df_ld((const float*) a.r, i, r0, r1);
+// aggregate (lane l takes the chunk's nodes l, l + 32, ..: their indices
+// first, then their values, then double-float sums in that order and a fixed
+// shuffle tree), then per coarse DOF the chunks' sums in chunk order
+__device__ __forceinline__ void restrict_chunk(const CoarseArgs& a, int q, int lane) {
+	constexpr int PER = COARSE_CHUNK / 32;
+	int const k0 = a.chunk_start[q], k1 = a.chunk_start[q + 1];
+	int idx[PER];
+#pragma unroll
+	for (int u = 0; u < PER; u++) {
+		int const k = k0 + lane + 32 * u;
+		idx[u] = k < k1 ? a.agg_nodes[k] : -1;
+	}
+	dfl r0[PER], r1[PER];
+	float4 pq[PER];
+#pragma unroll
+	for (int u = 0; u < PER; u++) {
+		r0[u] = r1[u] = {0.f, 0.f};
+		pq[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+		int const i = idx[u];
+		if (i < 0) continue;
+		if (a.df) df_ld((const float*) a.r, i, r0[u], r1[u]);
 		else {
 			double2 const t = ld2((const double*) a.r, i);
-			r0 = df_make(t.x);
-			r1 = df_make(t.y);
+			r0[u] = df_make(t.x);
+			r1[u] = df_make(t.y);
 		}
-		float4 const pq = a.pnode[i];
-		if (pq.z == 0.f) r0 = {0.f, 0.f};
-		if (pq.w == 0.f) r1 = {0.f, 0.f};
-		s0 = df_add(s0, r0);
-		s1 = df_add(s1, r1);
-		s2 = df_add(s2, df_add(df_mul_f(-pq.y, r0), df_mul_f(pq.x, r1)));
+		pq[u] = a.pnode[i];
+	}
+	dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+#pragma unroll
+	for (int u = 0; u < PER; u++) {
+		if (idx[u] < 0) continue;
+		dfl const x0 = pq[u].z == 0.f ? dfl{0.f, 0.f} : r0[u];
+		dfl const x1 = pq[u].w == 0.f ? dfl{0.f, 0.f} : r1[u];
+		s0 = df_add(s0, x0);
+		s1 = df_add(s1, x1);
+		s2 = df_add(s2, df_add(df_mul_f(-pq[u].y, x0), df_mul_f(pq[u].x, x1)));
 	}
 #pragma unroll
 	for (int o = 16; o; o >>= 1) {
@@ -1762,63 +1780,104 @@ __global__ void k_restrict(CoarseArgs a) {
 	}
 }
 
-__global__ void k_restrict_sum(CoarseArgs a) {
-	int const t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= a.nc) return;
+__device__ __forceinline__ void restrict_sum_one(const CoarseArgs& a, int t) {
 	int const I = t / 3, m = t % 3;
-	double s = 0.0;
-	for (int q = a.agg_chunk[I]; q < a.agg_chunk[I + 1]; q++) s += a.part[3l * q + m];
-	dfl const v = df_make(s);
-	a.rc[t] = make_float2(v.hi, v.lo);
+	double v = 0.0;
+	for (int c = a.agg_chunk[I]; c < a.agg_chunk[I + 1]; c++) v += a.part[3l * c + m];
+	dfl const d = df_make(v);
+	a.rc[t] = make_float2(d.hi, d.lo);
 }
 
-// one row of a padded FP32 triangle times a double-float vector: lane l takes
-// the 16-byte groups l, l + 32, .. (double-float products and sums), then a
-// fixed shuffle tree (deterministic; every lane gets the sum)
-__device__ __forceinline__ dfl coarse_row_dot(const float* __restrict__ row, int len, const float2* __restrict__ v, int lane) {
-	constexpr int U = 4;  // groups per lane in flight
+__global__ void __launch_bounds__(256) k_restrict(CoarseArgs a) {
+	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if (q < a.nchunk) restrict_chunk(a, q, lane);
+}
+
+__global__ void k_restrict_sum(CoarseArgs a) {
+	int const t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t < a.nc) restrict_sum_one(a, t);
+}
+
+constexpr int CX_T = 256;  // threads per row of the coarse products
+
+// one row of a padded FP32 triangle times a double-float vector, one block:
+// thread t takes the 16-byte groups t, t + CX_T, .. (loads first, then
+// double-float products and sums), then a fixed shuffle tree per warp and
+// the warps' sums in order (deterministic); the result in thread 0
+__device__ __forceinline__ dfl coarse_row_dot(const float* __restrict__ row, int len, const float2* __restrict__ v) {
+	constexpr int U = 4;  // groups per thread in flight
+	__shared__ float2 ws[CX_T / 32];
+	int const tx = threadIdx.x, lane = tx & 31, w = tx >> 5;
 	dfl s = {0.f, 0.f};
 	int const ng = (len + 3) >> 2;
 	const float4* r4 = reinterpret_cast<const float4*>(row);
-	for (int g0 = lane; g0 < ng; g0 += 32 * U) {
+	for (int g0 = tx; g0 < ng; g0 += CX_T * U) {
 		float4 x[U];
+		float2 vv[U][4];
 #pragma unroll
 		for (int u = 0; u < U; u++) {
-			int const g = g0 + 32 * u;
+			int const g = g0 + CX_T * u;
 			x[u] = g < ng ? __ldg(r4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+			for (int c = 0; c < 4; c++) vv[u][c] = g < ng ? v[4 * g + c] : make_float2(0.f, 0.f);
 		}
 #pragma unroll
 		for (int u = 0; u < U; u++) {
-			int const g = g0 + 32 * u;
-			if (g < ng) {
-				float2 const v0 = v[4 * g], v1 = v[4 * g + 1], v2 = v[4 * g + 2], v3 = v[4 * g + 3];
-				s = df_add(s, df_mul_f(x[u].x, {v0.x, v0.y}));
-				s = df_add(s, df_mul_f(x[u].y, {v1.x, v1.y}));
-				s = df_add(s, df_mul_f(x[u].z, {v2.x, v2.y}));
-				s = df_add(s, df_mul_f(x[u].w, {v3.x, v3.y}));
-			}
+			if (g0 + CX_T * u >= ng) continue;
+			s = df_add(s, df_mul_f(x[u].x, {vv[u][0].x, vv[u][0].y}));
+			s = df_add(s, df_mul_f(x[u].y, {vv[u][1].x, vv[u][1].y}));
+			s = df_add(s, df_mul_f(x[u].z, {vv[u][2].x, vv[u][2].y}));
+			s = df_add(s, df_mul_f(x[u].w, {vv[u][3].x, vv[u][3].y}));
 		}
 	}
 #pragma unroll
 	for (int o = 16; o; o >>= 1) s = df_add(s, {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
-	return s;
+	if (lane == 0) ws[w] = make_float2(s.hi, s.lo);
+	__syncthreads();
+	dfl t = {0.f, 0.f};
+	if (tx == 0)
+		for (int k = 0; k < CX_T / 32; k++) t = df_add(t, {ws[k].x, ws[k].y});
+	return t;
 }
 
-// yt = X rc: one warp per row of X (the padding of a row is zero, and rc has
+// yt = X rc: one block per row of X (the padding of a row is zero, and rc has
 // zero pads past its end)
-__global__ void k_coarse_x(CoarseArgs a) {
-	int const i = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(CX_T) k_coarse_x(CoarseArgs a) {
+	int const i = blockIdx.x;
 	if (i >= a.nc) return;
-	dfl const s = coarse_row_dot(a.xl + xrow(i), i + 1, a.rc, lane);
-	if (lane == 0) a.yt[i] = make_float2(s.hi, s.lo);
+	dfl const s = coarse_row_dot(a.xl + xrow(i), i + 1, a.rc);
+	if (threadIdx.x == 0) a.yt[i] = make_float2(s.hi, s.lo);
 }
 
 // yc = X^T yt, the same way over the rows of X^T (row j starts at column j)
-__global__ void k_coarse_xt(CoarseArgs a) {
-	int const j = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(CX_T) k_coarse_xt(CoarseArgs a) {
+	int const j = blockIdx.x;
 	if (j >= a.nc) return;
-	dfl const s = coarse_row_dot(a.xu + xrow(a.nc - 1 - j), a.nc - j, a.yt + j, lane);
-	if (lane == 0) a.yc[j] = make_float2(s.hi, s.lo);
+	dfl const s = coarse_row_dot(a.xu + xrow(a.nc - 1 - j), a.nc - j, a.yt + j);
+	if (threadIdx.x == 0) a.yc[j] = make_float2(s.hi, s.lo);
+}
+
+// The four stages above in one cooperative launch, grid barriers between
+// them (bounded waits: a timeout sets *berr and every block returns), the
+// same arithmetic: restriction chunks by warps, chunk sums by threads, the
+// two triangular products by blocks (one row at a time)
+__global__ void __launch_bounds__(CX_T) k_coarse_apply(CoarseArgs a) {
+	int const nw = gridDim.x * (CX_T / 32), wid = blockIdx.x * (CX_T / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+	for (int q = wid; q < a.nchunk; q += nw) restrict_chunk(a, q, lane);
+	if (!grid_barrier(a.bar, a.berr)) return;
+	for (int t = blockIdx.x * CX_T + threadIdx.x; t < a.nc; t += gridDim.x * CX_T) restrict_sum_one(a, t);
+	if (!grid_barrier(a.bar, a.berr)) return;
+	for (int i = blockIdx.x; i < a.nc; i += gridDim.x) {
+		dfl const s = coarse_row_dot(a.xl + xrow(i), i + 1, a.rc);
+		if (threadIdx.x == 0) a.yt[i] = make_float2(s.hi, s.lo);
+		__syncthreads();
+	}
+	if (!grid_barrier(a.bar, a.berr)) return;
+	for (int j = blockIdx.x; j < a.nc; j += gridDim.x) {
+		dfl const s = coarse_row_dot(a.xu + xrow(a.nc - 1 - j), a.nc - j, a.yt + j);
+		if (threadIdx.x == 0) a.yc[j] = make_float2(s.hi, s.lo);
+		__syncthreads();
+	}
 }
 
 // A_c = P^T A P in two deterministic stages.  One warp per chunk of

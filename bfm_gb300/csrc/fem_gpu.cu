@@ -1421,6 +1421,7 @@ struct bfm_gpu_problem {
 	float *xl, *xu;         // X = L^-1 and X^T by rows (FP32, padded rows)
 	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
 	int* coarse_err;
+	int coarse_grid;        // cooperative grid of k_coarse_apply (0: not sized yet, -1: none)
 };
 
 enum : unsigned { ORD_COORDS = 1, ORD_ELEMS = 2, ORD_MASKS = 4, ORD_EDGES = 8, ORD_FIELDS = 16, ORD_LEDGES = 32, ORD_ALL = 63 };
@@ -1694,6 +1695,20 @@ int prepare_order(bfm_gpu_problem* P) {
 }
 
 // ---- two-level SSOR: aggregation, coarse operator
+// Cooperative grid of the one-launch coarse correction (every block resident:
+// its grid barriers wait for all of them); -1 where it does not fit
+int coarse_grid(bfm_gpu_problem* P) {
+	if (P->coarse_grid == 0) {
+		int nb = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_coarse_apply, CX_T, 0) != cudaSuccess || nb < 1) {
+			cudaGetLastError();
+			P->coarse_grid = -1;
+		}
+		else P->coarse_grid = nb * num_sms();
+	}
+	return P->coarse_grid;
+}
+
 CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
 	CoarseArgs c;
 	memset(&c, 0, sizeof c);
@@ -1720,6 +1735,8 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
 	c.cols = P->cols;
 	c.vals64 = P->vals64;
 	c.err = P->coarse_err;
+	c.bar = P->ssor_bar;
+	c.berr = P->st ? &P->st->ssor_err : P->coarse_err;
 	c.nchunk = P->nchunk;
 	c.chunk_start = P->chunk_start;
 	c.chunk_agg = P->chunk_agg;
@@ -1863,7 +1880,8 @@ int build_aggregates(bfm_gpu_problem* P) {
 			rc = -1;
 		else P->nc_cap = nc;
 	}
-	if (!rc && !P->agg && (dalloc(&P->agg, N) || dalloc(&P->agg_nodes, N) || dalloc(&P->pnode, N) || dalloc(&P->coarse_err, 1)))
+	if (!rc && !P->agg && (dalloc(&P->agg, N) || dalloc(&P->agg_nodes, N) || dalloc(&P->pnode, N) || dalloc(&P->coarse_err, 2) ||
+	                       cudaMemsetAsync(P->coarse_err, 0, 2 * sizeof(int), st) != cudaSuccess))
 		rc = -1;
 	if (!rc && (cudaMemcpyAsync(P->agg, ag, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
 	            cudaMemcpyAsync(P->agg_nodes, nodes, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
@@ -2048,12 +2066,33 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		// two-level: yc = A_c^-1 P^T r first; the sweeps add P yc to z
 		CoarseArgs ca = coarse_args(P, base.r, df);
 		void* pc[1] = {&ca};
-		cudaGraphNode_t n1, n2, n3, n4;
-		if (add_node(g, &n1, dep, (void*) k_restrict, blocks_for(32l * P->nchunk), pc)) return -1;
-		if (add_node(g, &n2, &n1, (void*) k_restrict_sum, blocks_for(P->nc), pc)) return -1;
-		if (add_node(g, &n3, &n2, (void*) k_coarse_x, blocks_for(32l * P->nc), pc)) return -1;
-		if (add_node(g, &n4, &n3, (void*) k_coarse_xt, blocks_for(32l * P->nc), pc)) return -1;
-		*last = n4;
+		static_assert(CX_T == TPB, "graph kernel nodes run TPB threads per block");
+		bool one = false;
+		if (P->ssor_grid > 0 && coarse_grid(P) > 0) {
+			// one cooperative launch for the whole correction
+			cudaGraphNode_t n;
+			if (add_node(g, &n, dep, (void*) k_coarse_apply, P->coarse_grid, pc)) return -1;
+			cudaLaunchAttributeValue v;
+			memset(&v, 0, sizeof v);
+			v.cooperative = 1;
+			if (cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v) == cudaSuccess) {
+				*last = n;
+				one = true;
+			}
+			else {
+				cudaGetLastError();
+				cudaGraphDestroyNode(n);
+				P->coarse_grid = -1;
+			}
+		}
+		if (!one) {
+			cudaGraphNode_t n1, n2, n3, n4;
+			if (add_node(g, &n1, dep, (void*) k_restrict, blocks_for(32l * P->nchunk), pc)) return -1;
+			if (add_node(g, &n2, &n1, (void*) k_restrict_sum, blocks_for(P->nc), pc)) return -1;
+			if (add_node(g, &n3, &n2, (void*) k_coarse_x, P->nc, pc)) return -1;
+			if (add_node(g, &n4, &n3, (void*) k_coarse_xt, P->nc, pc)) return -1;
+			*last = n4;
+		}
 		dep = last;
 		base.agg = P->agg;
 		base.pnode = P->pnode;
@@ -2371,6 +2410,7 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 	cudaEvent_t e[2];
 	for (auto& x : e) cudaEventCreate(&x);
 	CoarseArgs ca = coarse_args(P, P->vec[0], df);
+	ca.berr = &scratch->ssor_err;
 	bool const coarse = coarse_pc(P->precond) && P->coarse_ok;
 	if (coarse) {
 		base.agg = P->agg;
@@ -2379,10 +2419,17 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 	}
 	auto once = [&](bool with_coarse) {
 		if (coarse && with_coarse) {
-			k_restrict<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
-			k_restrict_sum<<<blocks_for(P->nc), TPB, 0, st>>>(ca);
-			k_coarse_x<<<blocks_for(32l * P->nc), TPB, 0, st>>>(ca);
-			k_coarse_xt<<<blocks_for(32l * P->nc), TPB, 0, st>>>(ca);
+			if (P->ssor_grid > 0 && coarse_grid(P) > 0) {
+				void* pa[1] = {&ca};
+				cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), st);
+				cudaLaunchCooperativeKernel((const void*) k_coarse_apply, dim3(P->coarse_grid), dim3(CX_T), pa, 0, st);
+			}
+			else {
+				k_restrict<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
+				k_restrict_sum<<<blocks_for(P->nc), TPB, 0, st>>>(ca);
+				k_coarse_x<<<P->nc, CX_T, 0, st>>>(ca);
+				k_coarse_xt<<<P->nc, CX_T, 0, st>>>(ca);
+			}
 		}
 		if (P->ssor_grid > 0) {
 			SsorArgs a = base;

@@ -269,6 +269,30 @@ def test_two_level_matches_direct_oracle_and_restatement(libbfm, precision, tol)
         prob.close()
 
 
+def test_two_level_one_launch_matches_separate_kernels(libbfm, monkeypatch):
+    """The coarse correction as one cooperative launch (with the persistent
+    sweeps) and as separate kernels (with the per-colour sweeps): the same
+    arithmetic, so the same iterations and solution up to the order of the
+    sweeps' dot products."""
+    p = M.cfg_perforated(nx=192, ny=48, n_holes=60, seed=8)
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    try:
+        s1 = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-10)
+        x1 = prob.solution()
+    finally:
+        prob.close()
+    monkeypatch.setenv("BFM_GPU_SSOR_PER_COLOUR", "1")
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    try:
+        s2 = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-10)
+        x2 = prob.solution()
+    finally:
+        prob.close()
+    assert s1.status == 0 and s2.status == 0
+    assert abs(s1.iterations - s2.iterations) <= 2, (s1.iterations, s2.iterations)
+    assert rel(x2, x1) < 1e-9
+
+
 def test_untrained_learned_two_level_is_two_level(libbfm):
     p = M.cfg_perforated(nx=128, ny=32, n_holes=40, seed=6)
     prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
