@@ -1539,35 +1539,63 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
 // the limit the kernel records the timeout, and the blocks stop sweeping.
 constexpr long SSOR_SPIN_LIMIT = 1l << 24;
 
+// Grid barrier words: the arrival count at word 0 and the generation at word
+// 32 (separate 128-byte lines, so the polling does not slow the arrivals)
+constexpr int BAR_WORDS = 64;
+
+// the generation this block waits past at its next grid barrier
+__device__ __forceinline__ unsigned& bar_expect() {
+	__shared__ unsigned g;
+	return g;
+}
+
+// at kernel start, before the first grid_barrier: no block can pass a
+// barrier before every block has arrived, so the generation read here is
+// the one before the first barrier
+__device__ __forceinline__ void grid_barrier_init(unsigned* bar) {
+	if (threadIdx.x == 0) {
+		unsigned v;
+		asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar + 32) : "memory");
+		bar_expect() = v;
+	}
+}
+
+// Grid-wide barrier of a cooperative launch: thread 0 of each block arrives
+// with one acquire-release atomic (the block's writes, ordered before it by
+// __syncthreads, are released with it); the last to arrive resets the count
+// and publishes the next generation with a release store; the others poll it
+// with acquire loads.  Bounded: after SSOR_SPIN_LIMIT polls, or when another
+// block has given up (*err, checked every 1024 polls), *err is set and false
+// returned.
 __device__ bool grid_barrier(unsigned* bar, int* err) {
 	__shared__ int ok;
 	__syncthreads();
 	if (threadIdx.x == 0) {
 		unsigned* count = bar;
-		unsigned* gen = bar + 1;
-		unsigned const g = atomicAdd(gen, 0u);
-		__threadfence();
+		unsigned* gen = bar + 32;
+		unsigned const target = bar_expect() + 1;
 		int good = 1;
-		if (atomicAdd(count, 1u) == gridDim.x - 1) {
-			atomicExch(count, 0u);
-			__threadfence();
-			atomicAdd(gen, 1u);
+		unsigned old;
+		asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
+		if (old == gridDim.x - 1) {
+			asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(count) : "memory");
+			asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(target) : "memory");
 		}
 		else {
 			long spins = 0;
 			unsigned cur;
 			while (true) {
 				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gen) : "memory");
-				if (cur != g) break;
-				__nanosleep(20);
-				if (++spins > SSOR_SPIN_LIMIT || atomicAdd(err, 0) != 0) {
+				if (cur == target) break;
+				++spins;
+				if (spins > SSOR_SPIN_LIMIT || ((spins & 1023) == 0 && *(volatile int*) err != 0)) {
 					atomicExch(err, 1);
 					good = 0;
 					break;
 				}
 			}
 		}
-		__threadfence();
+		bar_expect() = target;
 		ok = good;
 	}
 	__syncthreads();
@@ -1579,6 +1607,7 @@ __device__ __forceinline__ bool ssor_barrier(const SsorArgs& a) { return grid_ba
 template <bool DF>
 __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 	if (a.st->done && !a.timing) return;
+	grid_barrier_init(a.bar);
 	int const nc = a.ncol > 0 ? a.ncol : 1;
 	dfl acc = {0.f, 0.f};
 	double acc64 = 0.0;
@@ -1863,6 +1892,7 @@ __global__ void __launch_bounds__(CX_T) k_coarse_xt(CoarseArgs a) {
 // two triangular products by blocks (one row at a time)
 __global__ void __launch_bounds__(CX_T) k_coarse_apply(CoarseArgs a) {
 	int const nw = gridDim.x * (CX_T / 32), wid = blockIdx.x * (CX_T / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+	grid_barrier_init(a.bar);
 	for (int q = wid; q < a.nchunk; q += nw) restrict_chunk(a, q, lane);
 	if (!grid_barrier(a.bar, a.berr)) return;
 	for (int t = blockIdx.x * CX_T + threadIdx.x; t < a.nc; t += gridDim.x * CX_T) restrict_sum_one(a, t);

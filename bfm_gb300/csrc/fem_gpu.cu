@@ -1422,6 +1422,7 @@ struct bfm_gpu_problem {
 	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
 	int* coarse_err;
 	int coarse_grid;        // cooperative grid of k_coarse_apply (0: not sized yet, -1: none)
+
 };
 
 enum : unsigned { ORD_COORDS = 1, ORD_ELEMS = 2, ORD_MASKS = 4, ORD_EDGES = 8, ORD_FIELDS = 16, ORD_LEDGES = 32, ORD_ALL = 63 };
@@ -1567,6 +1568,78 @@ static int dsatur(long n, const int* rp, const int* cols, int* col) {
 	return 0;
 }
 
+// Cells of the coarse grid for n nodes in a w x h box: about one per
+// `per_cell` nodes (BFM_GPU_COARSE_NODES, default 1250), at most 1024, as
+// square as the box allows, and fewer while the band factorisation (one
+// block, about 3 cells x bw^2 / 2 FP64 updates) would exceed 4e6 updates.
+// Returns the half-bandwidth of A_c for the short-side-first numbering.
+int coarse_grid(long n, double w, double h, int* gx_out, int* gy_out) {
+	long per_cell = 1250;
+	if (const char* e = getenv("BFM_GPU_COARSE_NODES")) {
+		long const v = atol(e);
+		if (v > 0) per_cell = v;
+	}
+	long target = n / per_cell;
+	target = target < 1 ? 1 : target > 1024 ? 1024 : target;
+	for (;;) {
+		int gx = 1, gy = 1;
+		if (w > 0 && h > 0) {
+			gx = (int) lround(sqrt((double) target * w / h));
+			gx = gx < 1 ? 1 : gx > target ? (int) target : gx;
+			gy = (int) lround((double) target / gx);
+			gy = gy < 1 ? 1 : gy;
+		}
+		else if (w > 0) gx = (int) target;
+		else if (h > 0) gy = (int) target;
+		int const gs = gx < gy ? gx : gy;
+		int const bw = 3 * (gs + 1) + 2;
+		double const cost = 1.5 * gx * gy * (double) bw * bw;
+		if ((bw <= COARSE_MAX_BW && cost <= 4e6) || target == 1) {
+			*gx_out = gx;
+			*gy_out = gy;
+			return bw;
+		}
+		target = target * 9 / 10;
+	}
+}
+
+// The coarse cells of n nodes with coordinates xy (x, y per node): the
+// coarse_grid cells over the bounding box, numbered along the shorter side
+// first, cells a hair wider than the box so the far edge falls inside the
+// last one.  Depends only on the set of coordinates, not on the node order.
+struct CellGrid {
+	int gx = 1, gy = 1, bw = 8;
+	double x0 = 0, y0 = 0, cw = 1, ch = 1;
+};
+void node_cells(long N, const double* xy, int* ag, CellGrid* g) {
+	double x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+	for (long i = 0; i < N; i++) {
+		double const x = xy[2 * i], y = xy[2 * i + 1];
+		if (i == 0 || x < x0) x0 = x;
+		if (i == 0 || x > x1) x1 = x;
+		if (i == 0 || y < y0) y0 = y;
+		if (i == 0 || y > y1) y1 = y;
+	}
+	double const w = x1 - x0, h = y1 - y0;
+	int gx = 1, gy = 1;
+	int const bw = coarse_grid(N, w, h, &gx, &gy);
+	double const cw = w > 0 ? w * (1.0 + 1e-12) / gx : 1.0;
+	double const ch = h > 0 ? h * (1.0 + 1e-12) / gy : 1.0;
+	for (long i = 0; i < N; i++) {
+		int cx = (int) ((xy[2 * i] - x0) / cw), cy = (int) ((xy[2 * i + 1] - y0) / ch);
+		cx = cx < 0 ? 0 : cx >= gx ? gx - 1 : cx;
+		cy = cy < 0 ? 0 : cy >= gy ? gy - 1 : cy;
+		ag[i] = cell_id(cx, cy, gx, gy, gx <= gy);
+	}
+	g->gx = gx;
+	g->gy = gy;
+	g->bw = bw;
+	g->x0 = x0;
+	g->y0 = y0;
+	g->cw = cw;
+	g->ch = ch;
+}
+
 int color_nodes(bfm_gpu_problem* P) {
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
@@ -1595,13 +1668,36 @@ int color_nodes(bfm_gpu_problem* P) {
 			if (counts[c]) P->ncol = c + 1;
 			P->col_off[c + 1] = P->col_off[c] + counts[c];
 		}
-		int next[64];
-		for (int c = 0; c < 64; c++) next[c] = P->col_off[c];
-		for (long i = 0; i < N; i++) {
-			int const w = next[col[i]]++;
-			iperm[i] = w;
-			perm[w] = (int) i;
+		// within a colour (rows that share no element, so their order does not
+		// change the sweeps) the nodes go by coarse cell, then by index: a
+		// cell's nodes are then three or four contiguous runs, which the
+		// two-level form's restriction reads in whole sectors
+		double* xy = (double*) malloc((2 * N + 2) * sizeof(double));
+		int* cell = (int*) malloc((N + 1) * sizeof(int));
+		CellGrid g;
+		if (!xy || !cell) rc = fail("out of host memory");
+		else if (cudaMemcpyAsync(xy, P->coords, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+		         cudaStreamSynchronize(st) != cudaSuccess)
+			rc = fail("coordinate copy failed");
+		else node_cells(N, xy, cell, &g);
+		long const nb = 64l * g.gx * g.gy;
+		long* next = rc ? nullptr : (long*) calloc(nb + 1, sizeof(long));
+		if (!rc && !next) rc = fail("out of host memory");
+		if (!rc) {
+			// counting sort on (colour, cell), stable in the node index
+			for (long i = 0; i < N; i++) next[(long) col[i] * g.gx * g.gy + cell[i] + 1]++;
+			for (long k = 0; k < nb; k++) next[k + 1] += next[k];
+			for (long i = 0; i < N; i++) {
+				int const w = (int) next[(long) col[i] * g.gx * g.gy + cell[i]]++;
+				iperm[i] = w;
+				perm[w] = (int) i;
+			}
 		}
+		free(xy);
+		free(cell);
+		free(next);
+	}
+	if (!rc) {
 		if (cudaMemcpyAsync(P->perm, perm, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
 		    cudaMemcpyAsync(P->iperm, iperm, N * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
 		    cudaStreamSynchronize(st) != cudaSuccess)
@@ -1697,7 +1793,7 @@ int prepare_order(bfm_gpu_problem* P) {
 // ---- two-level SSOR: aggregation, coarse operator
 // Cooperative grid of the one-launch coarse correction (every block resident:
 // its grid barriers wait for all of them); -1 where it does not fit
-int coarse_grid(bfm_gpu_problem* P) {
+int coarse_apply_grid(bfm_gpu_problem* P) {
 	if (P->coarse_grid == 0) {
 		int nb = 0;
 		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_coarse_apply, CX_T, 0) != cudaSuccess || nb < 1) {
@@ -1745,40 +1841,6 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
 	return c;
 }
 
-// Cells of the coarse grid for n nodes in a w x h box: about one per
-// `per_cell` nodes (BFM_GPU_COARSE_NODES, default 1250), at most 1024, as
-// square as the box allows, and fewer while the band factorisation (one
-// block, about 3 cells x bw^2 / 2 FP64 updates) would exceed 4e6 updates.
-// Returns the half-bandwidth of A_c for the short-side-first numbering.
-int coarse_grid(long n, double w, double h, int* gx_out, int* gy_out) {
-	long per_cell = 1250;
-	if (const char* e = getenv("BFM_GPU_COARSE_NODES")) {
-		long const v = atol(e);
-		if (v > 0) per_cell = v;
-	}
-	long target = n / per_cell;
-	target = target < 1 ? 1 : target > 1024 ? 1024 : target;
-	for (;;) {
-		int gx = 1, gy = 1;
-		if (w > 0 && h > 0) {
-			gx = (int) lround(sqrt((double) target * w / h));
-			gx = gx < 1 ? 1 : gx > target ? (int) target : gx;
-			gy = (int) lround((double) target / gx);
-			gy = gy < 1 ? 1 : gy;
-		}
-		else if (w > 0) gx = (int) target;
-		else if (h > 0) gy = (int) target;
-		int const gs = gx < gy ? gx : gy;
-		int const bw = 3 * (gs + 1) + 2;
-		double const cost = 1.5 * gx * gy * (double) bw * bw;
-		if ((bw <= COARSE_MAX_BW && cost <= 4e6) || target == 1) {
-			*gx_out = gx;
-			*gy_out = gy;
-			return bw;
-		}
-		target = target * 9 / 10;
-	}
-}
 
 // Aggregates for the current (working-order) coordinates: cells of a grid
 // over the bounding box (coarse_grid), numbered along the shorter side
@@ -1795,29 +1857,10 @@ int build_aggregates(bfm_gpu_problem* P) {
 	if (!rc && (cudaMemcpyAsync(xy, P->coords, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
 	            cudaStreamSynchronize(st) != cudaSuccess))
 		rc = fail("coordinate copy failed");
-	int gx = 1, gy = 1, bw = 8;
-	double x0 = 0, y0 = 0, cw = 1, ch = 1;
-	if (!rc) {
-		double x1 = 0, y1 = 0;
-		for (long i = 0; i < N; i++) {
-			double const x = xy[2 * i], y = xy[2 * i + 1];
-			if (i == 0 || x < x0) x0 = x;
-			if (i == 0 || x > x1) x1 = x;
-			if (i == 0 || y < y0) y0 = y;
-			if (i == 0 || y > y1) y1 = y;
-		}
-		double const w = x1 - x0, h = y1 - y0;
-		bw = coarse_grid(N, w, h, &gx, &gy);
-		// cells a hair wider than the box, so the far edge falls inside the last one
-		cw = w > 0 ? w * (1.0 + 1e-12) / gx : 1.0;
-		ch = h > 0 ? h * (1.0 + 1e-12) / gy : 1.0;
-		for (long i = 0; i < N; i++) {
-			int cx = (int) ((xy[2 * i] - x0) / cw), cy = (int) ((xy[2 * i + 1] - y0) / ch);
-			cx = cx < 0 ? 0 : cx >= gx ? gx - 1 : cx;
-			cy = cy < 0 ? 0 : cy >= gy ? gy - 1 : cy;
-			ag[i] = cell_id(cx, cy, gx, gy, gx <= gy);
-		}
-	}
+	CellGrid cg;
+	if (!rc) node_cells(N, xy, ag, &cg);
+	int const gx = cg.gx, gy = cg.gy, bw = cg.bw;
+	double const x0 = cg.x0, y0 = cg.y0, cw = cg.cw, ch = cg.ch;
 	int const na = gx * gy, nc = 3 * na;
 	int* ptr = (int*) calloc(na + 1, sizeof(int));
 	if (!rc && !ptr) rc = fail("out of host memory");
@@ -2017,12 +2060,13 @@ DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	return a;
 }
 
-int add_node(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, void* fn, int grid, void** params) {
+int add_node(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, void* fn, int grid, void** params,
+             size_t smem = 0) {
 	cudaKernelNodeParams kp = {};
 	kp.func = fn;
 	kp.gridDim = dim3(grid);
 	kp.blockDim = dim3(TPB);
-	kp.sharedMemBytes = 0;
+	kp.sharedMemBytes = (unsigned) smem;
 	kp.kernelParams = params;
 	CK(cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp));
 	return 0;
@@ -2068,7 +2112,7 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		void* pc[1] = {&ca};
 		static_assert(CX_T == TPB, "graph kernel nodes run TPB threads per block");
 		bool one = false;
-		if (P->ssor_grid > 0 && coarse_grid(P) > 0) {
+		if (P->ssor_grid > 0 && coarse_apply_grid(P) > 0) {
 			// one cooperative launch for the whole correction
 			cudaGraphNode_t n;
 			if (add_node(g, &n, dep, (void*) k_coarse_apply, P->coarse_grid, pc)) return -1;
@@ -2419,9 +2463,9 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 	}
 	auto once = [&](bool with_coarse) {
 		if (coarse && with_coarse) {
-			if (P->ssor_grid > 0 && coarse_grid(P) > 0) {
+			if (P->ssor_grid > 0 && coarse_apply_grid(P) > 0) {
 				void* pa[1] = {&ca};
-				cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), st);
+				cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
 				cudaLaunchCooperativeKernel((const void*) k_coarse_apply, dim3(P->coarse_grid), dim3(CX_T), pa, 0, st);
 			}
 			else {
@@ -2438,7 +2482,7 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 			a.bar = P->ssor_bar;
 			a.first_acc = a.final_phase = 1;
 			void* pa[1] = {&a};
-			cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), st);
+			cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
 			cudaLaunchCooperativeKernel(df ? (void*) k_ssor_all<true> : (void*) k_ssor_all<false>, dim3(P->ssor_grid),
 			                            dim3(TPB), pa, 0, st);
 			return;
@@ -2888,8 +2932,8 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		k_diag_pos<<<blocks_for(N), TPB, 0, st>>>(P->N, P->row_ptr, P->cols, P->dpos);
 		if (!P->ssor_y && dalloc(&P->ssor_y, 4 * N)) return -1;
 		if (!P->ssor_bar) {
-			if (dalloc(&P->ssor_bar, 2)) return -1;
-			CK(cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), st));
+			if (dalloc(&P->ssor_bar, BAR_WORDS)) return -1;
+			CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st));
 			// every block of the persistent sweep kernel resident at once
 			int nb = 0, dev = 0, coop = 0;
 			CK(cudaGetDevice(&dev));
@@ -3079,7 +3123,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	CK(cudaEventRecord(P->ev[2], P->stream));
 	// the learned blocks depend on the load vector: formed for every solve, inside the timed region
 	if (learned && bfmi_learned_precond(P, 0)) return -1;
-	if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), P->stream));
+	if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
 	CK(cudaGraphLaunch(P->graph, P->stream));
 	if (learned) {
 		// Jacobi takes over when the learned preconditioner breaks down (a non-SPD
@@ -3091,7 +3135,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		if (h->status == BFM_GPU_BREAKDOWN || !(rel == rel) ||
 		    (h->status == BFM_GPU_STAGNATED && rel > LEARNED_FALLBACK_REL)) {
 			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
-			if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, 2 * sizeof(unsigned), P->stream));
+			if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
 			CK(cudaGraphLaunch(P->graph, P->stream));
 			P->fallback = 1;
 		}
