@@ -38,7 +38,7 @@ namespace {
 
 constexpr int BT = 256;          // threads per block
 constexpr int MAX_PARTS = 512;   // parts per batch (shared-memory replica)
-constexpr long SPIN_LIMIT = 1l << 25;  // ~2 s of __nanosleep(64) polls per barrier
+constexpr long SPIN_LIMIT = 1l << 25;  // polls per barrier (each an L2 round trip: seconds in all)
 
 enum : int { BERR_BARRIER_TIMEOUT = 1 };
 
@@ -84,33 +84,39 @@ struct Shared {
 };
 
 // grid-wide barrier with a bounded wait; returns false (and flags the
-// error word) if the other blocks did not arrive in time
+// error word) if the other blocks did not arrive in time.  Thread 0 arrives
+// with one acquire-release atomic (the block's writes, ordered before it by
+// __syncthreads, are released with it); the last to arrive resets the count
+// and publishes the next generation with a release store (count and
+// generation sit on separate 128-byte lines); the others poll it with
+// acquire loads, checking the error word every 1024 polls.
 __device__ bool grid_barrier(const BatchArgs& a, Shared& sh) {
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		unsigned const g = sh.gen;
+		unsigned const target = sh.gen + 1u;
 		int ok = 1;
-		__threadfence();
-		unsigned const arrived = atomicAdd(a.bar_count, 1u);
+		unsigned arrived;
+		asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(a.bar_count) : "memory");
 		if (arrived == gridDim.x - 1) {
-			atomicExch(a.bar_count, 0u);
-			__threadfence();
-			atomicExch(a.bar_gen, g + 1u);
+			asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(a.bar_count) : "memory");
+			asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.bar_gen), "r"(target) : "memory");
 		}
 		else {
 			long spins = 0;
-			while (atomicAdd(a.bar_gen, 0u) == g) {
-				__nanosleep(64);
-				if (++spins > SPIN_LIMIT || atomicAdd((unsigned*) a.err, 0u) != 0u) {
+			unsigned cur;
+			while (true) {
+				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(a.bar_gen) : "memory");
+				if (cur == target) break;
+				++spins;
+				if (spins > SPIN_LIMIT || ((spins & 1023) == 0 && *(volatile int*) a.err != 0)) {
 					atomicOr(a.err, BERR_BARRIER_TIMEOUT);
 					ok = 0;
 					break;
 				}
 			}
 		}
-		__threadfence();
-		sh.gen = g + 1u;
-		sh.bar_ok = ok && atomicAdd((unsigned*) a.err, 0u) == 0u;
+		sh.gen = target;
+		sh.bar_ok = ok && *(volatile int*) a.err == 0;
 	}
 	__syncthreads();
 	return sh.bar_ok;
@@ -152,7 +158,7 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 	Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
 	int const sub = threadIdx.x % LPR;
 	int const rows_per_pass = BT / LPR;
-	if (threadIdx.x == 0) sh.gen = atomicAdd(a.bar_gen, 0u);
+	if (threadIdx.x == 0) asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(sh.gen) : "l"(a.bar_gen) : "memory");
 	__syncthreads();
 
 	// ---- init: x = dx = p = 0, r = b; partials (b,b), (r, M r)
@@ -479,7 +485,7 @@ struct BatchState {
 	int *tile_part, *tile_begin, *tile_end, *part_tile;
 	double* partials;
 	PartState* ps;
-	unsigned* bar;         // count, gen
+	unsigned* bar;         // count (word 0), gen (word 32)
 	int* err;
 	cudaGraphExec_t graph;
 	double g_rtol, g_drop;
@@ -590,7 +596,7 @@ BatchArgs batch_args(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* 
 	a.partials = B->partials;
 	a.ps = B->ps;
 	a.bar_count = B->bar;
-	a.bar_gen = B->bar + 1;
+	a.bar_gen = B->bar + 32;
 	a.err = B->err;
 	if (o) {
 		a.rtol = o->rtol;
@@ -613,7 +619,7 @@ int coop_grid(int lpr, int* grid) {
 }
 
 int launch(BatchState* B, BatchArgs* a, int lpr, int grid, cudaStream_t st) {
-	BCK(cudaMemsetAsync(B->bar, 0, 2 * sizeof(unsigned), st));
+	BCK(cudaMemsetAsync(B->bar, 0, 64 * sizeof(unsigned), st));
 	BCK(cudaMemsetAsync(B->err, 0, sizeof(int), st));
 	void* params[1] = {a};
 	BCK(cudaLaunchCooperativeKernel(kernel_of(lpr), dim3(grid), dim3(BT), params, sizeof(Shared), st));
@@ -684,7 +690,7 @@ int bfm_gpu_problem_set_parts(bfm_gpu_problem_t* P, int n_parts, const int32_t* 
 	memcpy(B->node_off_h, node_offsets, sizeof(int) * (n_parts + 1));
 	BCK(cudaMalloc(&B->part_tile, sizeof(int) * (n_parts + 1)));
 	BCK(cudaMalloc(&B->ps, sizeof(PartState) * n_parts));
-	BCK(cudaMalloc(&B->bar, 2 * sizeof(unsigned)));
+	BCK(cudaMalloc(&B->bar, 64 * sizeof(unsigned)));
 	BCK(cudaMalloc(&B->err, sizeof(int)));
 	BCK(cudaEventCreate(&B->ev[0]));
 	BCK(cudaEventCreate(&B->ev[1]));
