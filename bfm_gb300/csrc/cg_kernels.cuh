@@ -795,6 +795,14 @@ __global__ void k_df_flush(DfArgs a) {
 }
 
 // FP64 preconditioner (Jacobi: 2 per node; block: 4 per node) in double-float layout
+// the FP32 halves of the double-float relaxation blocks packed 16 bytes per
+// node for the SSOR sweeps, which use no low halves (read in place they
+// would take every other 16 bytes of 32-byte sectors)
+__global__ void k_pack_hi(int N, const float4* __restrict__ dinv, float4* __restrict__ out) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < N) out[i] = dinv[2 * i];
+}
+
 __global__ void k_df_dinv(int N, const double* __restrict__ dinv64, float* __restrict__ dinv, int block) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
@@ -1342,7 +1350,7 @@ struct SsorArgs {
 	const int* cols;
 	const int* dpos;    // per row: first block at or after the diagonal
 	const float* hi;    // FP32 2x2 blocks
-	const float* dinv;  // relaxation block inverses, double-float layout: node i's FP32 block at [2 i]
+	const float* dinv;  // FP32 relaxation block inverses, 16 bytes per node (k_pack_hi)
 	const void* r;      // residual: double-float float4 (u_hi, v_hi, u_lo, v_lo) or FP64 double2 per node
 	void* z;            // z = M^-1 r, same layout
 	float* y;           // double-float float4 per node
@@ -1500,7 +1508,7 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_fwd(SsorArgs a) {
 		dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
 		ssor_row(a, a.row_ptr[i], a.dpos[i], 0, a.lo, t0, t1);
 		dfl y0, y1;
-		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[2 * i], df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), y0, y1);
+		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[i], df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), y0, y1);
 		df_st(a.y, i, y0, y1);
 		if (a.fwd_last) ssor_st_z<DF>(a, i, y0, y1, r0, r1, q0, q1, acc, acc64);
 	}
@@ -1519,7 +1527,7 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
 		dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
 		ssor_row(a, a.dpos[i] + 1, a.row_ptr[i + 1], a.hi_row, 0x7fffffff, t0, t1);
 		dfl w0, w1, y0, y1;
-		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[2 * i], t0, t1, w0, w1);
+		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[i], t0, t1, w0, w1);
 		df_ld(a.y, i, y0, y1);
 		dfl const z0 = df_add(y0, df_neg(w0)), z1 = df_add(y1, df_neg(w1));
 		df_st(a.y, i, z0, z1);
@@ -1622,7 +1630,7 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 			dfl r0, r1;
 			double q0 = 0.0, q1 = 0.0;
 			dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
-			float4 const d = reinterpret_cast<const float4*>(a.dinv)[2 * i];
+			float4 const d = reinterpret_cast<const float4*>(a.dinv)[i];
 			dfl z0, z1;
 			if (forward) {
 				ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);

@@ -1402,6 +1402,7 @@ struct bfm_gpu_problem {
 	int *perm, *iperm, *dpos;
 	void* otmp;    // scratch of the in-place permutations
 	float* ssor_y; // sweep vector (double-float, 4 floats per node)
+	float4* ssor_d;  // the relaxation blocks' FP32 halves, packed (k_pack_hi) before every solve
 	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
 	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
 
@@ -2091,7 +2092,7 @@ SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
 	a.cols = P->cols;
 	a.dpos = P->dpos;
 	a.hi = P->vals32;
-	a.dinv = P->dinv32;
+	a.dinv = reinterpret_cast<const float*>(P->ssor_d);
 	a.r = r;
 	a.z = z;
 	a.y = P->ssor_y;
@@ -2658,7 +2659,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 		if (p) cudaFree(p);
 	for (int i = 0; i < MAXF; i++)
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
-	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y,
+	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y, P->ssor_d,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
 	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart};
 	for (void* q : lb)
@@ -2931,6 +2932,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (ssor_pc(P->precond)) {
 		k_diag_pos<<<blocks_for(N), TPB, 0, st>>>(P->N, P->row_ptr, P->cols, P->dpos);
 		if (!P->ssor_y && dalloc(&P->ssor_y, 4 * N)) return -1;
+		if (!P->ssor_d && dalloc(&P->ssor_d, N)) return -1;
 		if (!P->ssor_bar) {
 			if (dalloc(&P->ssor_bar, BAR_WORDS)) return -1;
 			CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st));
@@ -3123,7 +3125,10 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	CK(cudaEventRecord(P->ev[2], P->stream));
 	// the learned blocks depend on the load vector: formed for every solve, inside the timed region
 	if (learned && bfmi_learned_precond(P, 0)) return -1;
-	if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
+	if (ssor_pc(P->precond) && P->ssor_bar) {
+		CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
+		k_pack_hi<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, reinterpret_cast<const float4*>(P->dinv32), P->ssor_d);
+	}
 	CK(cudaGraphLaunch(P->graph, P->stream));
 	if (learned) {
 		// Jacobi takes over when the learned preconditioner breaks down (a non-SPD
@@ -3135,7 +3140,10 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 		if (h->status == BFM_GPU_BREAKDOWN || !(rel == rel) ||
 		    (h->status == BFM_GPU_STAGNATED && rel > LEARNED_FALLBACK_REL)) {
 			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
-			if (ssor_pc(P->precond) && P->ssor_bar) CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
+			if (ssor_pc(P->precond) && P->ssor_bar) {
+				CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
+				k_pack_hi<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, reinterpret_cast<const float4*>(P->dinv32), P->ssor_d);
+			}
 			CK(cudaGraphLaunch(P->graph, P->stream));
 			P->fallback = 1;
 		}
