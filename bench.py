@@ -68,7 +68,7 @@ SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md")
                 1: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md"),
                 2: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md")}
 # the same for one launch of the SSOR sweep kernel (double-float vectors)
-SSOR_TRAFFIC = (359_802_368, "profiles/ssor_sweeps_perforated_2048x512.md")
+SSOR_TRAFFIC = (327_798_272, "profiles/ssor_sweeps_perforated_2048x512.md")
 
 
 def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int) -> int:
