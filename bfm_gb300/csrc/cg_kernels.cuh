@@ -1678,7 +1678,7 @@ struct CoarseArgs {
 	const int* agg_nodes;
 	const int* agg;
 	const float4* pnode;
-	double* band;             // A_c, then L in place: entry (i, i - t) at band[i (bw + 1) + t], 1 / L_ii on the diagonal
+	float2* band;             // A_c, then L in place (double-float pairs): entry (i, i - t) at band[i (bw + 1) + t], 1 / L_ii on the diagonal
 	double* diag0;            // A_c's diagonal (the pivot test)
 	float* xl;                // X = L^-1 by rows: row i (columns 0..i) at xrow(i), rows padded to 4 floats
 	float* xu;                // X^T by rows: row j (columns j..nc-1) at xrow(nc - 1 - j)
@@ -1706,7 +1706,8 @@ struct CoarseArgs {
 constexpr int COARSE_CHUNK = 128;
 constexpr int COARSE_MAX_BW = 101;  // widest band: the factorisation's shared window and the solve's registers
 constexpr int CHOL_T = 512;         // threads of the factorisation block
-constexpr int LINV_C = 8;           // columns per warp of the inversion (4 lanes each)
+constexpr int LINV_C = 2;           // columns per warp of the inversion
+constexpr int LINV_L = 32 / LINV_C;  // lanes per column
 constexpr int LINV_W = 4;           // warps per block of the inversion
 
 __host__ __device__ __forceinline__ void cell_xy(int I, int gx, int gy, int xfast, int& cx, int& cy) {
@@ -1729,26 +1730,29 @@ __host__ __device__ __forceinline__ long xrow(int i) {
 	return 4 * (q + 1) * (2 * q + r);
 }
 
-// shared memory of the factorisation: the (bw + 2)^2 window, the scaled
-// column, the next pivot, the update's (row, column) pairs
-__host__ __device__ constexpr size_t chol_smem(int bw) {
-	return sizeof(double) * ((size_t) (bw + 2) * (bw + 2) + (bw + 2) + 2) + sizeof(short2) * ((size_t) bw * (bw + 1) / 2);
+// shared memory of the factorisation (n coarse DOFs): the (bw + 2)^2
+// window, the scaled column, the pivot (double-float pairs), the pivots'
+// drop thresholds, the update's (row, column) pairs
+__host__ __device__ constexpr size_t chol_smem(int bw, int n) {
+	return sizeof(float2) * ((size_t) (bw + 2) * (bw + 2) + (bw + 2) + 2) + sizeof(float) * ((size_t) n + 1) +
+	       sizeof(short2) * ((size_t) bw * (bw + 1) / 2);
 }
 // shared memory of the inversion: per warp LINV_C column rings and two staged rows of L
 __host__ __device__ constexpr size_t linv_smem(int bw) {
-	return sizeof(double) * LINV_W * ((size_t) LINV_C * (bw + 2) + 2 * (bw + 1));
+	return sizeof(float2) * LINV_W * ((size_t) LINV_C * (bw + 2) + 2 * (bw + 1));
 }
 
-// 1 / sqrt(p) for the factorisation's pivots: the FP32 estimate rsqrtf
-// refined by two Newton-Raphson steps y <- y (3 - p y^2) / 2 in FP64
-// (quadratic convergence: about 23 -> 46 -> full precision); 1 / sqrt(p) for
-// p outside FP32's normal range
-__device__ __forceinline__ double rsqrt_nr(double p) {
-	if (!(p > 1e-30 && p < 1e30)) return 1.0 / sqrt(p);
-	double y = (double) rsqrtf((float) p);
-	y = y * (1.5 - 0.5 * p * y * y);
-	y = y * (1.5 - 0.5 * p * y * y);
-	return y;
+// 1 / sqrt(p) of a double-float pivot above the drop threshold (else 0: a
+// dropped DOF): the FP32 estimate y = rsqrtf(p) refined by one
+// Newton-Raphson step y + y (1 - p y^2) / 2 in double-float arithmetic
+// (quadratic convergence: about 23 -> 46 bits, the width of the pair)
+__device__ __forceinline__ dfl pivot_rsqrt(dfl p, float thr) {
+	if (!(p.hi > thr)) return {0.f, 0.f};
+	float const y = rsqrtf(p.hi);
+	float const yy = __fmul_rn(y, y);
+	dfl const y2 = {yy, __fmaf_rn(y, y, -yy)};
+	dfl const e = df_add({1.f, 0.f}, df_neg(df_mul(p, y2)));
+	return df_add({y, 0.f}, df_mul_f(0.5f * y, e));
 }
 
 // per node its offset from its cell's centre (scaled by the cell size H) and
@@ -1993,57 +1997,65 @@ __global__ void k_coarse_ac_sum(CoarseArgs a) {
 	int const et = 9 * (8 - s) + 3 * v + u;
 	for (int q = a.agg_chunk[J]; q < a.agg_chunk[J + 1]; q++) y += a.part[81l * q + et];
 	double const m = 0.5 * (x + y);
-	a.band[(long) row * (a.bw + 1) + (row - col)] = m;
+	dfl const d = df_make(m);
+	a.band[(long) row * (a.bw + 1) + (row - col)] = make_float2(d.hi, d.lo);
 	if (row == col) a.diag0[row] = m;
 }
 
-// Band Cholesky A_c = L L^T in place, one block.  The active part of the
-// trailing matrix (rows k .. k + bw, their band) lives in a (bw + 2)^2 window
-// in shared memory, rows in a ring.  Step k: the pivot p = S_kk; p at or below
-// 1e-12 of A_c's diagonal entry (a coarse mode that A barely sees: an empty
-// cell, the rotation of a single node) drops DOF k: its column of L is zero
-// and 1 / L_kk = 0 marks it, so the factorisation goes on as that of A_c
-// without that DOF.  Otherwise column k is scaled by 1/sqrt(p) and written
-// out (the diagonal holds 1/sqrt(p)), the next row of A_c (loaded while the
-// column is scaled) enters the ring slot of the finished row k - 1, and the
-// window takes the rank-1 update; the thread that updates S_{k+1,k+1} then
-// forms the next pivot's 1/sqrt.  Two barriers per step.
+// Band Cholesky A_c = L L^T in place, one block, in double-float arithmetic
+// on the FP32 pipe (FP64 issues at a small fraction of that rate on this
+// GPU).  The active part of the trailing matrix (rows k .. k + bw, their band)
+// lives in a (bw + 2)^2 window in shared memory, rows in a ring.  Step k: the
+// pivot p = S_kk; p at or below 1e-12 of A_c's diagonal entry (a coarse mode
+// that A barely sees: an empty cell, the rotation of a single node) drops DOF
+// k: its column of L is zero and 1 / L_kk = 0 marks it, so the factorisation
+// goes on as that of A_c without that DOF.  Otherwise column k is scaled by
+// 1/sqrt(p) and written out (the diagonal holds 1/sqrt(p)), the next row of
+// A_c (loaded one step ahead) enters the ring slot of the finished row
+// k - 1, and the window takes the rank-1 update; the thread that updates
+// S_{k+1,k+1} then forms the next pivot's 1/sqrt.  Two barriers per step.
 __global__ void __launch_bounds__(CHOL_T) k_coarse_chol(CoarseArgs a) {
-	extern __shared__ double sm[];
+	extern __shared__ float2 sm2[];
 	int const n = a.nc, bw = a.bw, B = bw + 1, M = bw + 2;
-	double* W = sm;                     // entry (r, c) at W[(r % M) M + c % M]
-	double* col = W + M * M;            // scaled column k (rows k + 1 ..)
-	double* piv = col + M;              // 1/sqrt of the current pivot (0: dropped)
-	short2* pr = reinterpret_cast<short2*>(piv + 2);  // update pairs (ii, jj), jj <= ii < bw, by rows
-	for (int ii = threadIdx.x; ii < bw; ii += blockDim.x)
+	float2* W = sm2;                    // entry (r, c) at W[(r % M) M + c % M]
+	float2* col = W + M * M;            // scaled column k (rows k + 1 ..)
+	float2* piv = col + M;              // 1/sqrt of the current pivot (0: dropped)
+	float* thr = reinterpret_cast<float*>(piv + 2);   // drop thresholds, 1e-12 A_c,kk
+	short2* pr = reinterpret_cast<short2*>(thr + n + 1);  // update pairs (ii, jj), jj <= ii < bw, by rows
+	int const tx = threadIdx.x;
+	for (int ii = tx; ii < bw; ii += blockDim.x)
 		for (int jj = 0; jj <= ii; jj++) pr[ii * (ii + 1) / 2 + jj] = make_short2((short) ii, (short) jj);
-	for (int e = threadIdx.x; e < B * B; e += blockDim.x) {
+	for (int k = tx; k < n; k += blockDim.x) thr[k] = (float) (1e-12 * a.diag0[k]);
+	for (int e = tx; e < B * B; e += blockDim.x) {
 		int const r = e / B, t = e % B;
 		if (r < n && r - t >= 0) W[(r % M) * M + (r - t) % M] = a.band[(long) r * B + t];
 	}
 	__syncthreads();
-	if (threadIdx.x == 0) piv[0] = W[0] > 1e-12 * a.diag0[0] ? rsqrt_nr(W[0]) : 0.0;
+	if (tx == 0) {
+		dfl const q = pivot_rsqrt({W[0].x, W[0].y}, thr[0]);
+		piv[0] = make_float2(q.hi, q.lo);
+	}
 	__syncthreads();
 	// ring slots advance with k: s1 = (k + 1) % M, sk = k % M; the row entering
 	// at step k (k + bw + 1) was loaded one step earlier
-	int const tx = threadIdx.x;
-	double nv = (bw + 1 < n && tx < B) ? a.band[(long) (bw + 1) * B + tx] : 0.0;
+	float2 nv = (bw + 1 < n && tx < B) ? a.band[(long) (bw + 1) * B + tx] : make_float2(0.f, 0.f);
 	int sk = 0;
 	for (int k = 0; k < n; k++) {
-		double const isq = piv[0];
+		dfl const isq = {piv[0].x, piv[0].y};
 		int const s1 = sk + 1 == M ? 0 : sk + 1;
 		int const m = min(bw, n - 1 - k);  // rows k + 1 .. k + m below the pivot
 		int const r = k + bw + 1;
 		bool const ld = r < n && tx < B;
-		double const nv2 = (r + 1 < n && tx < B) ? a.band[(long) (r + 1) * B + tx] : 0.0;
+		float2 const nv2 = (r + 1 < n && tx < B) ? a.band[(long) (r + 1) * B + tx] : make_float2(0.f, 0.f);
 		for (int ii = tx; ii < m; ii += blockDim.x) {
 			int si = s1 + ii;
 			si -= si >= M ? M : 0;
-			double const c = W[si * M + sk] * isq;
-			col[ii] = c;
-			a.band[(long) (k + 1 + ii) * B + ii + 1] = c;
+			float2 const w = W[si * M + sk];
+			dfl const c = df_mul({w.x, w.y}, isq);
+			col[ii] = make_float2(c.hi, c.lo);
+			a.band[(long) (k + 1 + ii) * B + ii + 1] = make_float2(c.hi, c.lo);
 		}
-		if (tx == 0) a.band[(long) k * B] = isq;
+		if (tx == 0) a.band[(long) k * B] = make_float2(isq.hi, isq.lo);
 		if (ld) {
 			// row r's slot is that of row k - 1, i.e. sk - 1; entry (r, r - tx) at column slot (r - tx) % M
 			int const sr = sk == 0 ? M - 1 : sk - 1;
@@ -2059,73 +2071,83 @@ __global__ void __launch_bounds__(CHOL_T) k_coarse_chol(CoarseArgs a) {
 			int si = s1 + q.x, sj = s1 + q.y;
 			si -= si >= M ? M : 0;
 			sj -= sj >= M ? M : 0;
-			W[si * M + sj] -= col[q.x] * col[q.y];
+			float2 const ci = col[q.x], cj = col[q.y], w = W[si * M + sj];
+			dfl const u = df_add({w.x, w.y}, df_neg(df_mul({ci.x, ci.y}, {cj.x, cj.y})));
+			W[si * M + sj] = make_float2(u.hi, u.lo);
 		}
 		if (tx == 0 && m > 0) {
 			// pair 0 is S_{k+1,k+1}, updated by this thread above
-			double const p = W[s1 * M + s1];
-			piv[0] = p > 1e-12 * a.diag0[k + 1] ? rsqrt_nr(p) : 0.0;
+			float2 const p = W[s1 * M + s1];
+			dfl const q = pivot_rsqrt({p.x, p.y}, thr[k + 1]);
+			piv[0] = make_float2(q.hi, q.lo);
 		}
 		sk = s1;
 		__syncthreads();
 	}
 }
 
-// X = L^-1 by columns: each warp takes LINV_C consecutive columns j0 ..,
-// four lanes per column (lane h of a column takes the band entries t = 1 + h,
-// 5 + h, ..), a shuffle sum over the four, forward substitution down the
-// band from row j0 (rows above a column's own j come out zero).  The rows of
-// L are staged in shared memory (the next one loaded while this one is
-// used), each column's last bw values in a shared ring.  A dropped DOF
-// (1 / L_ii = 0) gets a zero row, and a zero column.  X is written, rounded
-// to FP32, by rows to xl and transposed to xu.
+// X = L^-1 by columns, in double-float arithmetic: each warp takes LINV_C
+// consecutive columns j0 .., LINV_L lanes per column (lane h of a column takes
+// the band entries t = 1 + h, 1 + h + LINV_L, ..), a shuffle sum over them,
+// forward substitution down the band from row j0 (rows above a column's own
+// j come out zero).  The rows of L are staged in shared memory (the next one
+// loaded while this one is used), each column's last bw values in a shared
+// ring.  A dropped DOF (1 / L_ii = 0) gets a zero row, and a zero column.  X
+// is written, rounded to FP32, by rows to xl and transposed to xu.
 __global__ void __launch_bounds__(32 * LINV_W) k_coarse_linv(CoarseArgs a) {
-	extern __shared__ double lsm[];
+	extern __shared__ float2 lsm2[];
 	constexpr int NL = (COARSE_MAX_BW + 1 + 31) / 32;  // row entries per lane when staging
 	int const n = a.nc, bw = a.bw, B = bw + 1, M = bw + 2;
-	int const w = threadIdx.x >> 5, lane = threadIdx.x & 31, c = lane >> 2, h = lane & 3;
+	int const w = threadIdx.x >> 5, lane = threadIdx.x & 31, c = lane / LINV_L, h = lane % LINV_L;
 	int const j0 = (blockIdx.x * LINV_W + w) * LINV_C;
 	if (j0 >= n) return;
-	double* ring = lsm + (size_t) w * (LINV_C * M + 2 * B);
-	double* Lr = ring + LINV_C * M;
+	float2* ring = lsm2 + (size_t) w * (LINV_C * M + 2 * B);
+	float2* Lr = ring + LINV_C * M;
 	int const j = j0 + c;
-	for (int t = lane; t < LINV_C * M; t += 32) ring[t] = 0.0;
+	for (int t = lane; t < LINV_C * M; t += 32) ring[t] = make_float2(0.f, 0.f);
 	for (int t = lane; t < B; t += 32) Lr[t] = a.band[(long) j0 * B + t];
 	__syncwarp();
-	double* R = ring + c * M;
+	float2* R = ring + c * M;
 	int si = j0 % M;  // ring slot of row i
 	for (int i = j0; i < n; i++) {
-		const double* cur = Lr + ((i - j0) & 1) * B;
-		double* nxt = Lr + ((i - j0 + 1) & 1) * B;
-		double nv[NL];
+		const float2* cur = Lr + ((i - j0) & 1) * B;
+		float2* nxt = Lr + ((i - j0 + 1) & 1) * B;
+		float2 nv[NL];
 #pragma unroll
 		for (int u = 0; u < NL; u++) {
 			int const t = lane + 32 * u;
-			nv[u] = (i + 1 < n && t < B) ? a.band[(long) (i + 1) * B + t] : 0.0;
+			nv[u] = (i + 1 < n && t < B) ? a.band[(long) (i + 1) * B + t] : make_float2(0.f, 0.f);
 		}
 		int const tmax = min(bw, i - j0);
-		double s0 = 0.0, s1 = 0.0;
-		// ring slot of row i - t, stepped down by 4 per term
+		dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f};
+		// ring slot of row i - t, stepped down by LINV_L per term (M >= 10 and
+		// LINV_L <= 16: two wraps at most)
 		int sl = si - 1 - h;
-		sl += sl < 0 ? M : 0;
-		for (int t = 1 + h; t <= tmax; t += 8) {
-			s0 += cur[t] * R[sl];
-			sl -= 4;
-			sl += sl < 0 ? M : 0;
-			if (t + 4 <= tmax) s1 += cur[t + 4] * R[sl];
-			sl -= 4;
-			sl += sl < 0 ? M : 0;
+		while (sl < 0) sl += M;
+		for (int t = 1 + h; t <= tmax; t += 2 * LINV_L) {
+			float2 const l0 = cur[t], x0 = R[sl];
+			s0 = df_add(s0, df_mul({l0.x, l0.y}, {x0.x, x0.y}));
+			sl -= LINV_L;
+			while (sl < 0) sl += M;
+			if (t + LINV_L <= tmax) {
+				float2 const l1 = cur[t + LINV_L], x1 = R[sl];
+				s1 = df_add(s1, df_mul({l1.x, l1.y}, {x1.x, x1.y}));
+			}
+			sl -= LINV_L;
+			while (sl < 0) sl += M;
 		}
-		double s = s0 + s1;
-		s += __shfl_xor_sync(0xffffffffu, s, 1);
-		s += __shfl_xor_sync(0xffffffffu, s, 2);
-		double const x = ((i == j ? 1.0 : 0.0) - s) * cur[0];
+		dfl s = df_add(s0, s1);
+#pragma unroll
+		for (int o = 1; o < LINV_L; o <<= 1)
+			s = df_add(s, {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+		float2 const d = cur[0];
+		dfl const x = df_mul(df_add({i == j ? 1.f : 0.f, 0.f}, df_neg(s)), {d.x, d.y});
 		__syncwarp();
 		if (h == 0 && j < n) {
-			R[si] = x;
+			R[si] = make_float2(x.hi, x.lo);
 			if (i >= j) {
-				a.xl[xrow(i) + j] = (float) x;
-				a.xu[xrow(n - 1 - j) + (i - j)] = (float) x;
+				a.xl[xrow(i) + j] = x.hi;
+				a.xu[xrow(n - 1 - j) + (i - j)] = x.hi;
 			}
 		}
 #pragma unroll

@@ -1418,7 +1418,8 @@ struct bfm_gpu_problem {
 	int *chunk_start, *chunk_agg, *agg_chunk;
 	double* cpart;  // per chunk partial sums (81 doubles)
 	float4* pnode;
-	double *aband, *diag0;  // band A_c then L, the diagonal of A_c
+	float2* aband;          // band A_c then L (double-float pairs)
+	double* diag0;          // the diagonal of A_c
 	float *xl, *xu;         // X = L^-1 and X^T by rows (FP32, padded rows)
 	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
 	int* coarse_err;
@@ -1913,7 +1914,8 @@ int build_aggregates(bfm_gpu_problem* P) {
 		for (void* q : old)
 			if (q) cudaFree(q);
 		P->agg_ptr = P->agg_chunk = nullptr;
-		P->aband = P->diag0 = nullptr;
+		P->aband = nullptr;
+		P->diag0 = nullptr;
 		P->xl = P->xu = nullptr;
 		P->rc = P->ayt = P->yc = nullptr;
 		if (dalloc(&P->agg_ptr, na + 1) || dalloc(&P->agg_chunk, na + 1) ||
@@ -1970,7 +1972,7 @@ int coarse_setup(bfm_gpu_problem* P) {
 	if (!P->agg_valid && build_aggregates(P)) return -1;
 	k_pnode<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->coords, P->agg, P->last_ci, P->ax0, P->ay0, P->acw, P->ach, P->agx,
 	                                          P->agy, P->axfast, P->aH, P->pnode);
-	CK(cudaMemsetAsync(P->aband, 0, (size_t) P->nc * (P->abw + 1) * sizeof(double), st));
+	CK(cudaMemsetAsync(P->aband, 0, (size_t) P->nc * (P->abw + 1) * sizeof(float2), st));
 	CK(cudaMemsetAsync(P->diag0, 0, (size_t) P->nc * sizeof(double), st));
 	CK(cudaMemsetAsync(P->coarse_err, 0, sizeof(int), st));
 	CoarseArgs ca = coarse_args(P, nullptr, true);
@@ -1981,8 +1983,8 @@ int coarse_setup(bfm_gpu_problem* P) {
 	CK(cudaStreamSynchronize(st));
 	if (err) return 0;
 	CK(cudaFuncSetAttribute((const void*) k_coarse_chol, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                        (int) chol_smem(COARSE_MAX_BW)));
-	k_coarse_chol<<<1, CHOL_T, chol_smem(P->abw), st>>>(ca);
+	                        (int) chol_smem(COARSE_MAX_BW, 3 * 1024)));
+	k_coarse_chol<<<1, CHOL_T, chol_smem(P->abw, P->nc), st>>>(ca);
 	// the padding of X's rows stays zero (the products read whole 16-byte groups)
 	CK(cudaMemsetAsync(P->xl, 0, xrow(P->nc) * sizeof(float), st));
 	CK(cudaMemsetAsync(P->xu, 0, xrow(P->nc) * sizeof(float), st));
