@@ -1571,12 +1571,12 @@ static int dsatur(long n, const int* rp, const int* cols, int* col) {
 }
 
 // Cells of the coarse grid for n nodes in a w x h box: about one per
-// `per_cell` nodes (BFM_GPU_COARSE_NODES, default 1250), at most 1024, as
+// `per_cell` nodes (BFM_GPU_COARSE_NODES, default 1000), at most 1024, as
 // square as the box allows, and fewer while the band factorisation (one
-// block, about 3 cells x bw^2 / 2 FP64 updates) would exceed 4e6 updates.
+// block, about 3 cells x bw^2 / 2 double-float updates) would exceed 8e6.
 // Returns the half-bandwidth of A_c for the short-side-first numbering.
 int coarse_grid(long n, double w, double h, int* gx_out, int* gy_out) {
-	long per_cell = 1250;
+	long per_cell = 1000;
 	if (const char* e = getenv("BFM_GPU_COARSE_NODES")) {
 		long const v = atol(e);
 		if (v > 0) per_cell = v;
@@ -1596,7 +1596,7 @@ int coarse_grid(long n, double w, double h, int* gx_out, int* gy_out) {
 		int const gs = gx < gy ? gx : gy;
 		int const bw = 3 * (gs + 1) + 2;
 		double const cost = 1.5 * gx * gy * (double) bw * bw;
-		if ((bw <= COARSE_MAX_BW && cost <= 4e6) || target == 1) {
+		if ((bw <= COARSE_MAX_BW && cost <= 8e6) || target == 1) {
 			*gx_out = gx;
 			*gy_out = gy;
 			return bw;

@@ -112,13 +112,13 @@ def pcg(A: sp.spmatrix, b: np.ndarray, apply, rtol: float = 1e-8, max_iters: int
     return x, max_iters
 
 
-def coarse_grid(n: int, w: float, h: float, per_cell: int = 1250):
+def coarse_grid(n: int, w: float, h: float, per_cell: int = 1000):
     """Cell counts (gx, gy) of the coarse grid for n nodes in a w x h box
     (bfm_gb300/csrc/fem_gpu.cu, coarse_grid): about one cell per `per_cell`
     nodes, at most 1024, as square as the box allows, and fewer while the band
     factorisation's cost 1.5 cells bw^2 (bw = 3 (shorter side + 1) + 2, the
     half-bandwidth of A_c for cells numbered along the shorter side first)
-    exceeds 4e6 or bw exceeds 101."""
+    exceeds 8e6 or bw exceeds 101."""
     target = min(max(n // per_cell, 1), 1024)
     while True:
         gx = gy = 1
@@ -130,7 +130,7 @@ def coarse_grid(n: int, w: float, h: float, per_cell: int = 1250):
         elif h > 0:
             gy = target
         bw = 3 * (min(gx, gy) + 1) + 2
-        if (bw <= 101 and 1.5 * gx * gy * bw * bw <= 4e6) or target == 1:
+        if (bw <= 101 and 1.5 * gx * gy * bw * bw <= 8e6) or target == 1:
             return gx, gy
         target = target * 9 // 10
 

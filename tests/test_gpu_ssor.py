@@ -59,9 +59,17 @@ def test_colour_order_and_permuted_system(problem):
     assert np.array_equal(np.sort(perm), np.arange(p.n_nodes))
     K0 = scalar(rp0, c0, v0, p.n_nodes)
     assert S.is_colouring(S.node_graph(K0, p.n_nodes), perm, off)
-    # ascending caller index inside every colour
+    # inside every colour the nodes go by coarse cell (each cell one contiguous
+    # run), then by ascending caller index
+    cell = S.cell_grid(np.asarray(p.coords, dtype=np.float64))[0]
+    assert len(np.unique(cell)) >= 2
     for c in range(nc):
-        assert np.all(np.diff(perm[off[c]:off[c + 1]]) > 0)
+        seg = perm[off[c]:off[c + 1]]
+        cs = cell[seg]
+        starts = np.flatnonzero(np.r_[True, cs[1:] != cs[:-1]])
+        assert len(starts) == len(np.unique(cs))
+        for a, b in zip(starts, np.r_[starts[1:], len(seg)]):
+            assert np.all(np.diff(seg[a:b]) > 0)
     # the working system is P K P^T and P b, bit for bit
     rp, cols, vals, b = prob.download()
     dperm = np.stack([2 * perm, 2 * perm + 1], 1).ravel()
@@ -246,7 +254,7 @@ def test_per_colour_kernels_match_the_persistent_kernel(libbfm, precision, monke
 @pytest.mark.parametrize("precision,tol", [(bfm_gb300.FP64, 1e-10), (bfm_gb300.FP64_DF, 1e-8)])
 def test_two_level_matches_direct_oracle_and_restatement(libbfm, precision, tol):
     """Two-level SSOR (additive rigid-body coarse correction on a cell grid)
-    on a 256x64 plate (7 x 2 cells): the solution against the direct oracle, the
+    on a 256x64 plate (8 x 2 cells): the solution against the direct oracle, the
     iteration count against the float64 restatement with the GPU's own
     colouring, and fewer iterations than plain SSOR."""
     p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
@@ -257,7 +265,7 @@ def test_two_level_matches_direct_oracle_and_restatement(libbfm, precision, tol)
         assert s2.status == 0 and s2.rel_residual <= 1e-10
         x, _, _ = O.solve_direct(p)
         assert rel(prob.solution(), x) < tol
-        # 14 cells only at this size; the 2048x512 plate's 812 cells cut 6,172 iterations to a few hundred
+        # 16 cells only at this size; the 2048x512 plate's 1,024 cells cut 6,172 iterations to about 330
         assert s2.iterations < 0.6 * s1.iterations, (s2.iterations, s1.iterations)
         perm, off, _ = ordering(prob)
         K, b = O.assemble_csr(p)
