@@ -62,8 +62,9 @@ enum {
 	/* Two-level: the SSOR sweeps plus a coarse correction, additively,
 	 * M^-1 = M_SSOR^-1 + P A_c^-1 P^T, with P the rigid-body modes (two
 	 * translations and a rotation) of the cells of a grid over the mesh's
-	 * bounding box (about one cell per 2,500 nodes, at most 384) and
-	 * A_c = P^T A P inverted on the device at assembly.  FP64 and FP64_DF. */
+	 * bounding box (about one cell per 1,000 nodes, BFM_GPU_COARSE_NODES;
+	 * at most 1,024 cells) and A_c = P^T A P factored (band Cholesky, then
+	 * X = L^-1) on the device at assembly.  FP64 and FP64_DF. */
 	BFM_GPU_PC_SSOR2 = 5,
 	/* The two-level form with the network's relaxation blocks. */
 	BFM_GPU_PC_LEARNED_SSOR2 = 6,
