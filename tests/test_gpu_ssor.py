@@ -301,6 +301,28 @@ def test_two_level_one_launch_matches_separate_kernels(libbfm, monkeypatch):
     assert rel(x2, x1) < 1e-9
 
 
+def test_two_level_denser_grid(libbfm, monkeypatch):
+    """BFM_GPU_COARSE_NODES=300 on a 256x64 plate (15 x 4 cells instead of 8 x 2):
+    still the direct oracle's solution, and fewer iterations than the default
+    grid."""
+    p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    try:
+        s1 = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-10)
+    finally:
+        prob.close()
+    monkeypatch.setenv("BFM_GPU_COARSE_NODES", "300")
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+    try:
+        s2 = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-10)
+        assert s2.status == 0 and s2.rel_residual <= 1e-10
+        x, _, _ = O.solve_direct(p)
+        assert rel(prob.solution(), x) < 1e-8
+        assert s2.iterations < s1.iterations, (s2.iterations, s1.iterations)
+    finally:
+        prob.close()
+
+
 def test_untrained_learned_two_level_is_two_level(libbfm):
     p = M.cfg_perforated(nx=128, ny=32, n_holes=40, seed=6)
     prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
