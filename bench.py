@@ -476,9 +476,12 @@ def main():
     ssor = r["pc"] in (3, 4, 5, 6)
     if ssor:
         # the SSOR sweeps after the init, every update and every replacement:
-        # one cooperative launch, or 2 nc - 1 colour phases (the two-level
-        # form adds its restriction and the products by X and X^T)
-        per_pc = (1 if r["persistent"] else 2 * r["ncol"] - 1) + (3 if r["pc"] in (5, 6) else 0)
+        # one cooperative launch, or 2 nc - 1 colour phases; the two-level
+        # form adds its coarse correction, one cooperative launch beside the
+        # persistent sweeps, else four kernels (restriction, chunk sums, the
+        # products by X and X^T)
+        coarse = (1 if r["persistent"] else 4) if r["pc"] in (5, 6) else 0
+        per_pc = (1 if r["persistent"] else 2 * r["ncol"] - 1) + coarse
     else:
         per_pc = 0
     launches_per_step = 24 + 1 + (per_iter + per_pc) * r["iters"] + (2 + per_pc) * r["repl"] + per_pc + 2 + \
