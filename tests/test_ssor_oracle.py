@@ -49,6 +49,21 @@ def test_restatement():
     assert it_ssor < 0.5 * it_jac
 
 
+def test_coarse_grid_rule():
+    """The cell grid the GPU builds (fem_gpu.cu coarse_grid), restated: about
+    one cell per 1,000 nodes as square as the box allows, at most 1,024 cells,
+    fewer while the band factorisation's cost 1.5 cells bw^2 passes 8e6 (bw =
+    3 (shorter side + 1) + 2 <= 101)."""
+    assert S.coarse_grid(2049 * 513, 4.0, 1.0) == (64, 16)          # the 2.1M-DOF plate: 1,024 cells
+    assert S.coarse_grid(2049 * 513, 4.0, 1.0, per_cell=1250) == (58, 14)
+    assert S.coarse_grid(257 * 65, 4.0, 1.0) == (8, 2)
+    assert S.coarse_grid(500, 4.0, 1.0) == (1, 1)                   # fewer nodes than one cell
+    assert S.coarse_grid(10 ** 6, 0.0, 1.0) == (1, 1000)            # a line of nodes
+    gx, gy = S.coarse_grid(10 ** 6, 1.0, 1.0)                       # square box: the cost cap binds
+    bw = 3 * (min(gx, gy) + 1) + 2
+    assert gx * gy < 1000 and 1.5 * gx * gy * bw * bw <= 8e6 and bw <= 101
+
+
 def test_two_level_restatement():
     """The additive two-level preconditioner (rigid-body modes of a cell grid)
     on a 256x64 plate: 8 x 2 cells, and well under half of SSOR's iterations."""
