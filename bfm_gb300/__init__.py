@@ -22,7 +22,8 @@ _lib: C.CDLL | None = None
 
 class bfm_gpu_opts_t(C.Structure):  # include/bfm/gpu.h
     _fields_ = [("precision", C.c_int), ("precond", C.c_int), ("rtol", C.c_double), ("max_iters", C.c_int),
-                ("replace_drop", C.c_double), ("deterministic", C.c_int), ("autotune", C.c_int)]
+                ("replace_drop", C.c_double), ("deterministic", C.c_int), ("autotune", C.c_int),
+                ("barrier_polls", C.c_int64)]
 
 
 class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
@@ -34,7 +35,8 @@ class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
 FP64, MIXED, MIXED_EXACT, FP64_DF = 0, 1, 2, 3
 PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_SSOR, PC_LEARNED_SSOR, PC_SSOR2, PC_LEARNED_SSOR2 = 0, 1, 2, 3, 4, 5, 6
 HOST, DEVICE = 0, 1
-STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error", 5: "stagnated"}
+STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error", 5: "stagnated",
+          6: "barrier timeout"}
 
 _vp, _i, _d = C.c_void_p, C.c_int, C.c_double
 _P = C.POINTER

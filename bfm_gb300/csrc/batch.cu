@@ -38,7 +38,7 @@ namespace {
 
 constexpr int BT = 256;          // threads per block
 constexpr int MAX_PARTS = 512;   // parts per batch (shared-memory replica)
-constexpr long SPIN_LIMIT = 1l << 25;  // polls per barrier (each an L2 round trip: seconds in all)
+constexpr long SPIN_LIMIT = 1l << 25;  // default polls per barrier (each an L2 round trip: seconds in all)
 
 enum : int { BERR_BARRIER_TIMEOUT = 1 };
 
@@ -74,6 +74,7 @@ struct BatchArgs {
 	double rtol, drop2;
 	int max_iters;
 	int timing_iters;        // > 0: run exactly this many iterations (autotuner)
+	long polls;              // polls per grid barrier before it gives up
 };
 
 struct Shared {
@@ -108,7 +109,7 @@ __device__ bool grid_barrier(const BatchArgs& a, Shared& sh) {
 				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(a.bar_gen) : "memory");
 				if (cur == target) break;
 				++spins;
-				if (spins > SPIN_LIMIT || ((spins & 1023) == 0 && *(volatile int*) a.err != 0)) {
+				if (spins > a.polls || ((spins & 1023) == 0 && *(volatile int*) a.err != 0)) {
 					atomicOr(a.err, BERR_BARRIER_TIMEOUT);
 					ok = 0;
 					break;
@@ -490,6 +491,7 @@ struct BatchState {
 	cudaGraphExec_t graph;
 	double g_rtol, g_drop;
 	int g_iters, g_rpt, g_lpr;
+	int64_t g_polls;
 	float last_ms;
 	int direct;            // 1: launched without a graph (capture unsupported)
 	cudaEvent_t ev[2];
@@ -598,10 +600,12 @@ BatchArgs batch_args(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* 
 	a.bar_count = B->bar;
 	a.bar_gen = B->bar + 32;
 	a.err = B->err;
+	a.polls = SPIN_LIMIT;
 	if (o) {
 		a.rtol = o->rtol;
 		a.drop2 = o->replace_drop * o->replace_drop;
 		a.max_iters = o->max_iters;
+		if (o->barrier_polls > 0) a.polls = (long) o->barrier_polls;
 	}
 	return a;
 }
@@ -718,7 +722,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		B->graph = nullptr;
 	}
 	bool const same = (B->graph || B->direct) && B->g_rtol == o.rtol && B->g_drop == o.replace_drop && B->g_iters == o.max_iters &&
-	                  B->g_rpt == B->rows_per_tile && B->g_lpr == B->lpr;
+	                  B->g_rpt == B->rows_per_tile && B->g_lpr == B->lpr && B->g_polls == o.barrier_polls;
 	if (!same) {
 		// one graph: reset of the barrier words, the persistent cooperative
 		// kernel, the per-part FP64 residuals
@@ -755,6 +759,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		B->g_iters = o.max_iters;
 		B->g_rpt = B->rows_per_tile;
 		B->g_lpr = B->lpr;
+		B->g_polls = o.barrier_polls;
 	}
 	BCK(cudaEventRecord(B->ev[0], st));
 	if (B->graph) {

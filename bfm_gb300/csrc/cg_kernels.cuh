@@ -41,6 +41,7 @@ struct CgState {
 	int stall;          // replacements in a row without halving best_true2's norm
 	double ssor_acc;    // SSOR: (r, z) summed over the sweep phases
 	int ssor_err;       // SSOR: a grid barrier of the persistent sweep kernel timed out
+	int repl_req;       // outside a graph: the last K2 asked for a residual replacement
 };
 
 // After an FP64 true residual: converged, or stagnating at the roundoff floor
@@ -298,6 +299,7 @@ __global__ void __launch_bounds__(TPB_K) k_cg_init(CgArgs<V> a, int mixed) {
 		st->rho_ref = out[0];
 		st->true_res2 = out[0];
 		st->ssor_err = 0;
+		st->repl_req = 0;
 		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
 }
@@ -775,6 +777,7 @@ __global__ void __launch_bounds__(TPB_K) k_df_init(DfArgs a) {
 		st->rho_ref = out[0];
 		st->true_res2 = out[0];
 		st->ssor_err = 0;
+		st->repl_req = 0;
 		if (a.use_cond) cudaGraphSetConditional(a.cond, st->done ? 0u : 1u);
 	}
 }
@@ -874,6 +877,9 @@ __device__ __forceinline__ void hs_beta(CgState* st, double gamma, double rho, i
 	else if (repl && use_cond) {
 		cudaGraphSetConditional(cond_repl, 1u);
 	}
+	// launched from a host loop (no conditional nodes): the replacement
+	// kernel, launched after every K2, reads the request from the state
+	if (!use_cond) st->repl_req = repl && !stop;
 }
 
 // K2 finisher when the SSOR sweeps come next: the iteration count, the cap
@@ -958,6 +964,8 @@ template <int LPR>
 __global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
 	CgState* st = a.st;
 	if (st->done) return;
+	// outside a graph this kernel follows every K2 and works only on request
+	if (!a.use_cond && !st->repl_req) return;
 	double v[2] = {0.0, 0.0};
 	const double* __restrict__ x = a.x;
 	auto gx = [x](int c, double& g0, double& g1) {
@@ -983,6 +991,7 @@ __global__ void __launch_bounds__(TPB_K) k_hs64_replace(CgArgs<double> a) {
 	}
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		st->repl_req = 0;
 		if (!a.no_pc) st->gamma = out[1];
 		if (true_residual_verdict(st, out[0])) {
 			st->done = 1;
@@ -1367,6 +1376,7 @@ struct SsorArgs {
 	int timing;
 	// persistent form: every phase in one cooperative launch
 	unsigned* bar;      // grid barrier: arrivals, generation
+	long polls;         // polls per grid barrier before it gives up
 	int ncol;
 	int off[65];        // colour c: rows [off[c], off[c + 1])
 	// two-level form: z += P yc, the coarse correction (yc == nullptr: none)
@@ -1473,7 +1483,7 @@ __device__ __forceinline__ void ssor_finish(const SsorArgs& a, double part) {
 	double const g = st->ssor_acc;
 	if (st->ssor_err) {
 		st->done = 1;
-		st->status = BFM_GPU_BREAKDOWN;
+		st->status = BFM_GPU_TIMEOUT;
 		if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
 		return;
 	}
@@ -1544,8 +1554,10 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
 // Grid barrier of the persistent sweep kernel (cooperative launch: every
 // block is resident).  Arrivals count up; the last one resets the count and
 // advances the generation the others wait for.  The wait is bounded: past
-// the limit the kernel records the timeout, and the blocks stop sweeping.
-constexpr long SSOR_SPIN_LIMIT = 1l << 24;
+// the limit (polls per barrier, a kernel argument: bfm_gpu_opts_t's
+// barrier_polls, this default when 0) the kernel records the timeout, and
+// the blocks stop sweeping.
+constexpr long BARRIER_POLLS_DEFAULT = 1l << 24;
 
 // Grid barrier words: the arrival count at word 0 and the generation at word
 // 32 (separate 128-byte lines, so the polling does not slow the arrivals)
@@ -1572,10 +1584,10 @@ __device__ __forceinline__ void grid_barrier_init(unsigned* bar) {
 // with one acquire-release atomic (the block's writes, ordered before it by
 // __syncthreads, are released with it); the last to arrive resets the count
 // and publishes the next generation with a release store; the others poll it
-// with acquire loads.  Bounded: after SSOR_SPIN_LIMIT polls, or when another
-// block has given up (*err, checked every 1024 polls), *err is set and false
+// with acquire loads.  Bounded: after `polls` polls, or when another block
+// has given up (*err, checked every 1024 polls), *err is set and false
 // returned.
-__device__ bool grid_barrier(unsigned* bar, int* err) {
+__device__ bool grid_barrier(unsigned* bar, int* err, long polls) {
 	__shared__ int ok;
 	__syncthreads();
 	if (threadIdx.x == 0) {
@@ -1596,7 +1608,7 @@ __device__ bool grid_barrier(unsigned* bar, int* err) {
 				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gen) : "memory");
 				if (cur == target) break;
 				++spins;
-				if (spins > SSOR_SPIN_LIMIT || ((spins & 1023) == 0 && *(volatile int*) err != 0)) {
+				if (spins > polls || ((spins & 1023) == 0 && *(volatile int*) err != 0)) {
 					atomicExch(err, 1);
 					good = 0;
 					break;
@@ -1610,7 +1622,7 @@ __device__ bool grid_barrier(unsigned* bar, int* err) {
 	return ok;
 }
 
-__device__ __forceinline__ bool ssor_barrier(const SsorArgs& a) { return grid_barrier(a.bar, &a.st->ssor_err); }
+__device__ __forceinline__ bool ssor_barrier(const SsorArgs& a) { return grid_barrier(a.bar, &a.st->ssor_err, a.polls); }
 
 template <bool DF>
 __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
@@ -1693,6 +1705,7 @@ struct CoarseArgs {
 	int* err;
 	unsigned* bar;       // grid barrier words of the one-launch form (k_coarse_apply)
 	int* berr;           // its timeout flag
+	long polls;          // polls per grid barrier before it gives up
 	// chunks of at most COARSE_CHUNK nodes of one aggregate: chunk q covers
 	// agg_nodes[chunk_start[q] .. chunk_start[q + 1]) of aggregate chunk_agg[q];
 	// the chunks of aggregate I are [agg_chunk[I], agg_chunk[I + 1])
@@ -1904,17 +1917,18 @@ __global__ void __launch_bounds__(CX_T) k_coarse_xt(CoarseArgs a) {
 // two triangular products by blocks (one row at a time)
 __global__ void __launch_bounds__(CX_T) k_coarse_apply(CoarseArgs a) {
 	int const nw = gridDim.x * (CX_T / 32), wid = blockIdx.x * (CX_T / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+	if (*(volatile int*) a.berr) return;  // an earlier barrier of this solve timed out: the solve has stopped
 	grid_barrier_init(a.bar);
 	for (int q = wid; q < a.nchunk; q += nw) restrict_chunk(a, q, lane);
-	if (!grid_barrier(a.bar, a.berr)) return;
+	if (!grid_barrier(a.bar, a.berr, a.polls)) return;
 	for (int t = blockIdx.x * CX_T + threadIdx.x; t < a.nc; t += gridDim.x * CX_T) restrict_sum_one(a, t);
-	if (!grid_barrier(a.bar, a.berr)) return;
+	if (!grid_barrier(a.bar, a.berr, a.polls)) return;
 	for (int i = blockIdx.x; i < a.nc; i += gridDim.x) {
 		dfl const s = coarse_row_dot(a.xl + xrow(i), i + 1, a.rc);
 		if (threadIdx.x == 0) a.yt[i] = make_float2(s.hi, s.lo);
 		__syncthreads();
 	}
-	if (!grid_barrier(a.bar, a.berr)) return;
+	if (!grid_barrier(a.bar, a.berr, a.polls)) return;
 	for (int j = blockIdx.x; j < a.nc; j += gridDim.x) {
 		dfl const s = coarse_row_dot(a.xu + xrow(a.nc - 1 - j), a.nc - j, a.yt + j);
 		if (threadIdx.x == 0) a.yc[j] = make_float2(s.hi, s.lo);

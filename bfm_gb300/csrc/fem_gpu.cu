@@ -1405,6 +1405,7 @@ struct bfm_gpu_problem {
 	float4* ssor_d;  // the relaxation blocks' FP32 halves, packed (k_pack_hi) before every solve
 	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
 	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
+	long polls;          // polls per grid barrier before it gives up (the solve graph's)
 
 	// two-level SSOR: aggregates are the cells of an agx x agy grid over the
 	// bounding box (origin ax0, ay0, cell acw x ach, rotation scale aH),
@@ -1589,6 +1590,8 @@ int coarse_grid(long n, double w, double h, int* gx_out, int* gy_out) {
 			gx = (int) lround(sqrt((double) target * w / h));
 			gx = gx < 1 ? 1 : gx > target ? (int) target : gx;
 			gy = (int) lround((double) target / gx);
+			// rounding both counts may overshoot: at most `target` cells
+			gy = gy > target / gx ? (int) (target / gx) : gy;
 			gy = gy < 1 ? 1 : gy;
 		}
 		else if (w > 0) gx = (int) target;
@@ -1835,6 +1838,7 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
 	c.err = P->coarse_err;
 	c.bar = P->ssor_bar;
 	c.berr = P->st ? &P->st->ssor_err : P->coarse_err;
+	c.polls = P->polls;
 	c.nchunk = P->nchunk;
 	c.chunk_start = P->chunk_start;
 	c.chunk_agg = P->chunk_agg;
@@ -2101,6 +2105,7 @@ SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
 	a.partials = P->partials;
 	a.ticket = P->ticket;
 	a.st = P->st;
+	a.polls = P->polls;
 	return a;
 }
 
@@ -2574,6 +2579,7 @@ void bfm_gpu_default_opts(bfm_gpu_opts_t* o) {
 	o->replace_drop = 1e-1;
 	o->deterministic = 1;
 	o->autotune = 1;
+	o->barrier_polls = 0;
 }
 
 int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n_elems, int n_edges, int n_conds, void* stream) {
@@ -2593,6 +2599,7 @@ int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n
 	P->max_conds = n_conds;
 	P->precision = -1;
 	P->graph_precision = -1;
+	P->polls = BARRIER_POLLS_DEFAULT;
 	P->lpr = 8;
 	if (stream) {
 		P->stream = (cudaStream_t) stream;
@@ -3114,8 +3121,10 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	// options are baked into the graph's kernel parameters: rebuild only when they change
 	bool const same = P->graph && P->graph_precision == P->precision && P->graph_precond == P->precond &&
 	                  P->graph_lpr == P->lpr && P->graph_opts.rtol == o.rtol &&
-	                  P->graph_opts.max_iters == o.max_iters && P->graph_opts.replace_drop == o.replace_drop;
+	                  P->graph_opts.max_iters == o.max_iters && P->graph_opts.replace_drop == o.replace_drop &&
+	                  P->polls == (o.barrier_polls > 0 ? (long) o.barrier_polls : BARRIER_POLLS_DEFAULT);
 	if (!same) {
+		P->polls = o.barrier_polls > 0 ? (long) o.barrier_polls : BARRIER_POLLS_DEFAULT;
 		if (build_graph(P, &o)) return -1;
 		P->graph_precision = P->precision;
 		P->graph_precond = P->precond;

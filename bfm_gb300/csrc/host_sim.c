@@ -341,6 +341,9 @@ static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	if (s.status == BFM_GPU_BREAKDOWN)
 		return REPORT(st, "CG broke down after %d iterations: the system is not positive definite (missing constraints?)",
 		              s.iterations);
+	if (s.status == BFM_GPU_TIMEOUT)
+		return REPORT(st, "a grid barrier of the solver timed out after %d iterations (barrier_polls %lld)", s.iterations,
+		              (long long) o.barrier_polls);
 	return 0;
 }
 

@@ -79,6 +79,8 @@ enum {
 	BFM_GPU_CUDA_ERROR = 4,
 	BFM_GPU_STAGNATED = 5,     /* the FP64 true residual stopped decreasing above rtol: the
 	                              roundoff floor of this system; x is as accurate as it gets */
+	BFM_GPU_TIMEOUT = 6,       /* a grid barrier of a persistent kernel waited past
+	                              opts.barrier_polls; the solve stopped, the problem stays usable */
 };
 
 typedef struct {
@@ -92,6 +94,11 @@ typedef struct {
 	int deterministic; /* 1: fixed reduction order (always on; kept for ABI)    */
 	int autotune;      /* 1: pick the SpMV shape (lanes per block row) by timing
 	                      the candidates on the problem's own matrix, once    */
+	int64_t barrier_polls; /* grid barriers inside the persistent kernels (SSOR
+	                          sweeps, coarse correction, batched solver) give up
+	                          after this many polls and the solve ends with
+	                          BFM_GPU_TIMEOUT instead of waiting forever;
+	                          0: the default, 2^24 (seconds)                  */
 } bfm_gpu_opts_t;
 
 typedef struct {
@@ -106,7 +113,8 @@ typedef struct {
 	double ms_solve;      /* CG (device)                                   */
 } bfm_gpu_stats_t;
 
-/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 0.1, autotune on. */
+/* Defaults: FP64, Jacobi, rtol 1e-10, max_iters 200000, replace_drop 0.1, autotune on,
+ * barrier_polls 0 (2^24). */
 void bfm_gpu_default_opts(bfm_gpu_opts_t* opts);
 
 /* Options used by bfm_sim_run and the bfm_system_* creators of this thread. */
@@ -331,18 +339,24 @@ int bfm_gpu_mpnn_use(bfm_gpu_mpnn_t* net);
 /* No counterpart in the reference: an additive entry point for callers that
  * cannot allocate device memory (an application that owns every device byte
  * through its own pool, or code that must not call cudaMalloc).  Solves
- * A x = b by FP64 Jacobi-PCG, the method of bfm_gpu_problem_solve, with A a
- * 2x2-block CSR matrix already in device memory: row_ptr[n_nodes+1],
+ * A x = b by FP64 Jacobi-PCG with the kernels and stopping rule of
+ * bfm_gpu_problem_solve's FP64 path (Hestenes-Stiefel PCG with FP64 true
+ * residual replacements; converged when the true residual is at most rtol,
+ * or stagnated at the roundoff floor above it), launched from a host loop.
+ * A is a 2x2-block CSR matrix already in device memory: row_ptr[n_nodes+1],
  * cols[row_ptr[n_nodes]], vals[4*row_ptr[n_nodes]] (the layout
  * bfm_gpu_problem_download returns), b and x interleaved u,v, all device
  * pointers; x is written.  Nothing is allocated: the Krylov vectors and
  * solver state live in a fixed scratch array of about 6.4 MB that the library
  * keeps on every GPU that loads it, which limits n_nodes to 65,536
- * (131,072 DOF); larger sizes return -1 with a message.  The first call on a
- * device looks up that array's device address; make this first call before
- * any stream capture.  Calls share the array, so calls that overlap on the GPU
- * (two streams, two threads) race: serialize them.  Reports the iteration
- * count and the FP64 relative residual; returns -1 if CG does not converge. */
+ * (131,072 DOF); larger sizes return -1 with a message.  Every call looks up
+ * that array's address on the current device.  The call waits on `stream`
+ * and reads the solver state back, so it must not be made while that stream
+ * is being captured.  Calls share the array, so calls that overlap on the
+ * GPU (two streams, two threads) race: serialize them.  Reports the
+ * iteration count and the FP64 relative residual of x; returns 0 when
+ * converged or stagnated (as bfm_sim_run), -1 when CG does not converge or
+ * breaks down. */
 int bfm_gpu_pcg_solve_noalloc(int n_nodes, const int32_t* row_ptr, const int32_t* cols, const double* vals,
                               const double* b, double* x, double rtol, int max_iters, int* iterations,
                               double* rel_residual, void* stream);

@@ -115,7 +115,8 @@ def pcg(A: sp.spmatrix, b: np.ndarray, apply, rtol: float = 1e-8, max_iters: int
 def coarse_grid(n: int, w: float, h: float, per_cell: int = 1000):
     """Cell counts (gx, gy) of the coarse grid for n nodes in a w x h box
     (bfm_gb300/csrc/fem_gpu.cu, coarse_grid): about one cell per `per_cell`
-    nodes, at most 1024, as square as the box allows, and fewer while the band
+    nodes, at most 1024 (gy rounded, then capped so gx gy stays within the
+    target), as square as the box allows, and fewer while the band
     factorisation's cost 1.5 cells bw^2 (bw = 3 (shorter side + 1) + 2, the
     half-bandwidth of A_c for cells numbered along the shorter side first)
     exceeds 8e6 or bw exceeds 101."""
@@ -124,7 +125,7 @@ def coarse_grid(n: int, w: float, h: float, per_cell: int = 1000):
         gx = gy = 1
         if w > 0 and h > 0:
             gx = min(max(int(np.floor(np.sqrt(target * w / h) + 0.5)), 1), target)
-            gy = max(int(np.floor(target / gx + 0.5)), 1)
+            gy = max(min(int(np.floor(target / gx + 0.5)), target // gx), 1)
         elif w > 0:
             gx = target
         elif h > 0:

@@ -59,6 +59,11 @@ def test_coarse_grid_rule():
     assert S.coarse_grid(257 * 65, 4.0, 1.0) == (8, 2)
     assert S.coarse_grid(500, 4.0, 1.0) == (1, 1)                   # fewer nodes than one cell
     assert S.coarse_grid(10 ** 6, 0.0, 1.0) == (1, 1000)            # a line of nodes
+    # w/h = 2.16: 47 x 22 (1,034) after rounding both counts; capped to 47 x 21
+    assert S.coarse_grid(1024 * 1000, 2.16, 1.0) == (47, 21)
+    for n, w in ((1024 * 1000, 2.16), (1024 * 1000, 3.3), (700 * 1000, 1.7), (900 * 1000, 5.5)):
+        gx, gy = S.coarse_grid(n, w, 1.0)
+        assert gx * gy <= min(n // 1000, 1024)
     gx, gy = S.coarse_grid(10 ** 6, 1.0, 1.0)                       # square box: the cost cap binds
     bw = 3 * (min(gx, gy) + 1) + 2
     assert gx * gy < 1000 and 1.5 * gx * gy * bw * bw <= 8e6 and bw <= 101

@@ -5,7 +5,8 @@ and solver state live in a fixed array inside the library.  Here it gets a
 matrix assembled by the regular problem API, in device buffers the test owns,
 and must return the solution of the regular entry point (bfm_gpu_problem_solve,
 same FP64 Jacobi-PCG) within the tolerance of the parity tests, on two calls in
-a row (the second call finds the first call's leftovers in the array)."""
+a row (the second call finds the first call's leftovers in the array), and the
+FP64 direct solve of the oracle within the same tolerance."""
 import ctypes as C
 
 import numpy as np
@@ -64,8 +65,10 @@ def regular_solve(lib, p):
 
 def test_noalloc_matches_regular_solve_twice(libbfm):
     torch = pytest.importorskip("torch")
+    from oracle import oracle as O
     p = M.plate(96, 24, 3, traction=1e6)
     rp, cols, vals, b, x_ref = regular_solve(libbfm, p)
+    x_dir, _, _ = O.solve_direct(p)
     dev = torch.device("cuda", 0)
     d_rp = torch.from_numpy(rp).to(dev)
     d_cols = torch.from_numpy(cols).to(dev)
@@ -82,6 +85,8 @@ def test_noalloc_matches_regular_solve_twice(libbfm):
         x = d_x.cpu().numpy()
         err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
         assert err < MATCH, f"call {call}: relative difference {err:.3e}"
+        err_dir = np.linalg.norm(x - x_dir) / np.linalg.norm(x_dir)
+        assert err_dir < MATCH, f"call {call}: relative error {err_dir:.3e} vs the direct oracle"
         assert it.value > 0 and res.value < 1e-8
 
 
