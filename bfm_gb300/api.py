@@ -140,6 +140,103 @@ class SimHandle:
         return K, b, perm
 
 
+class DeviceProblem:
+    """A meshgen.Problem uploaded once through the device-resident problem API
+    (bfm_gpu_problem_*): assemble and solve repeatedly without re-uploading,
+    and read back the solution and the assembled system."""
+
+    def __init__(self, lib: C.CDLL, p, stream=None):
+        from . import meshgen as M
+        from . import last_error
+        self.lib, self.p = lib, p
+        self.keep: list = []
+        P = C.c_void_p()
+        n_edges = 0 if p.edges is None else len(p.edges)
+        rc = lib.bfm_gpu_problem_create(C.byref(P), p.kind, p.n_nodes, p.n_elems, n_edges, len(p.conds), stream)
+        assert rc == 0, last_error()
+        self.P = P
+        a = self._a
+        ok = lib.bfm_gpu_problem_set_geometry(P, a(p.coords, np.float64), a(p.elems, np.int32), 0) == 0
+        ok = ok and lib.bfm_gpu_problem_set_material(
+            P, p.E, p.nu, p.rho, int(p.stress), None if p.elem_E is None else a(p.elem_E, np.float64),
+            None if p.elem_nu is None else a(p.elem_nu, np.float64), 0) == 0
+        w, ph, dx, de = M.gauss_tables(p.kind)
+        ok = ok and lib.bfm_gpu_problem_set_rule(P, len(w), a(w, np.float64), a(ph, np.float64), a(dx, np.float64),
+                                                 a(de, np.float64)) == 0
+        f = np.array(p.forces, np.float64).reshape(-1)
+        ok = ok and lib.bfm_gpu_problem_set_forces(P, len(p.forces), a(f, np.float64) if len(f) else None, None, 0) == 0
+        if p.conds:
+            kinds = a([c[0] for c in p.conds], np.int32)
+            vals = a([c[1] for c in p.conds], np.float64)
+            masks = a(np.stack([c[2] for c in p.conds]).astype(np.uint8), np.uint8)
+            edges = a(p.edges, np.int32) if n_edges else None
+            ok = ok and lib.bfm_gpu_problem_set_conditions(P, len(p.conds), kinds, vals, masks, n_edges, edges, 0) == 0
+        assert ok, last_error()
+
+    def _a(self, x, dt):
+        x = np.ascontiguousarray(x, dtype=dt)
+        self.keep.append(x)
+        return x.ctypes.data
+
+    def assemble(self, precision: int) -> None:
+        from . import last_error
+        assert self.lib.bfm_gpu_problem_assemble(self.P, precision) == 0, last_error()
+
+    def solve(self, opts) -> None:
+        from . import last_error
+        assert self.lib.bfm_gpu_problem_solve(self.P, C.byref(opts)) == 0, last_error()
+
+    def stats(self):
+        from . import bfm_gpu_stats_t, last_error
+        s = bfm_gpu_stats_t()
+        assert self.lib.bfm_gpu_problem_stats(self.P, C.byref(s)) == 0, last_error()
+        return s
+
+    def solution(self) -> np.ndarray:
+        x = np.zeros(self.p.n_dof)
+        assert self.lib.bfm_gpu_problem_solution(self.P, x.ctypes.data, 0) == 0
+        return x
+
+    def system(self):
+        """The assembled system in the working node order: (row_ptr, cols,
+        vals (4 per block, FP64), b) and the order's perm (perm[w] = caller node)."""
+        nb = C.c_int64()
+        assert self.lib.bfm_gpu_problem_n_blocks(self.P, C.byref(nb)) == 0
+        n = self.p.n_nodes
+        rp = np.zeros(n + 1, np.int32)
+        cols = np.zeros(nb.value, np.int32)
+        vals = np.zeros(4 * nb.value)
+        b = np.zeros(2 * n)
+        assert self.lib.bfm_gpu_problem_download(self.P, rp.ctypes.data, cols.ctypes.data, vals.ctypes.data,
+                                                 b.ctypes.data) == 0
+        perm = np.zeros(n, np.int32)
+        assert self.lib.bfm_gpu_problem_ordering(self.P, perm.ctypes.data, None, None) == 0
+        return rp, cols, vals, b, perm
+
+    def close(self) -> None:
+        if self.P:
+            self.lib.bfm_gpu_problem_destroy(self.P)
+            self.P = None
+
+
+def scalar_csr(rp, cols, vals, n_nodes: int, perm=None):
+    """A 2x2-block CSR system as a scipy scalar CSR matrix (the caller's node
+    order when perm, perm[w] = caller node, is given)."""
+    import scipy.sparse as sp
+    nb = len(cols)
+    brow = np.repeat(np.arange(n_nodes), np.diff(rp))
+    if perm is not None:
+        brow = perm[brow]
+        bcol = perm[cols]
+    else:
+        bcol = cols
+    r = (2 * brow)[:, None] + np.array([0, 0, 1, 1])[None, :]
+    c = (2 * bcol)[:, None] + np.array([0, 1, 0, 1])[None, :]
+    K = sp.csr_matrix((vals.reshape(nb, 4).ravel(), (r.ravel(), c.ravel())), shape=(2 * n_nodes, 2 * n_nodes))
+    K.sort_indices()
+    return K
+
+
 # --------------------------------------------------------------------- pybfm-style classes
 
 class _State:

@@ -50,7 +50,8 @@ def sources() -> tuple[list[Path], list[Path]]:
 def build(force: bool = False, verbose: bool = False) -> Path:
     cu, c = sources()
     deps = cu + c + sorted(INCLUDE.rglob("*.h")) + sorted(CSRC.glob("*.h")) + [Path(__file__)]
-    if not force and LIB.exists() and LIB.stat().st_mtime > max(p.stat().st_mtime for p in deps):
+    if not force and LIB.exists() and (OUT_DIR / "libbfm.so.1").exists() and \
+            LIB.stat().st_mtime > max(p.stat().st_mtime for p in deps):
         return LIB
     BUILD_DIR.mkdir(exist_ok=True)
     OUT_DIR.mkdir(exist_ok=True)
@@ -73,6 +74,12 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs], "-Xlinker", "-Bsymbolic",
           "-Xlinker", "-soname=libbfm.so.1", "-lpthread", "-lm"])
     os.replace(tmp, LIB)
+    # the soname the link records (libbfm.so.1, as the reference's SOVERSION 1),
+    # for programs linked with -lbfm against this directory
+    so1 = OUT_DIR / "libbfm.so.1"
+    if so1.is_symlink() or so1.exists():
+        so1.unlink()
+    so1.symlink_to(LIB.name)
     return LIB
 
 

@@ -165,15 +165,22 @@ static int wavefront_edges(bfm_mesh_t* mesh) {
 		state->free(h);
 		return -1;
 	}
+	/* Walk the sorted list as the reference does: a half-edge and the next one
+	 * form an interior edge when they run in opposite directions; otherwise the
+	 * half-edge is a boundary edge.  The last half-edge is looked at only as
+	 * the second of a pair, so when it is unpaired it is left out (the
+	 * reference's edge list ends the same way; kept for parity, since the
+	 * edges feed the Neumann and normal/tangent conditions). */
 	size_t cur = 0;
-	for (size_t i = 0; i < total;) {
+	for (size_t i = 1; i < total;) {
 		bfm_edge_t* ed = &mesh->edges[cur++];
-		ed->nodes[0] = h[i].a;
-		ed->nodes[1] = h[i].b;
-		ed->elems[0] = (ssize_t) h[i].elem;
+		half_edge_t const* p = &h[i - 1];
+		ed->nodes[0] = p->a;
+		ed->nodes[1] = p->b;
+		ed->elems[0] = (ssize_t) p->elem;
 		ed->elems[1] = -1;
-		if (i + 1 < total && h[i + 1].lo == h[i].lo && h[i + 1].hi == h[i].hi) {
-			ed->elems[1] = (ssize_t) h[i + 1].elem;
+		if (p->a == h[i].b && p->b == h[i].a) {
+			ed->elems[1] = (ssize_t) h[i].elem;
 			i += 2;
 		}
 		else {

@@ -25,7 +25,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORC = HERE / "liborc.so"
 REF = HERE / "_ref" / "libbfm_ref.so"
-REF_TREE = Path(os.environ.get("BFM_REFERENCE", "/root/reference"))
+# the reference source tree: BFM_REFERENCE, else a "reference" folder beside the repository
+REF_TREE = Path(os.environ.get("BFM_REFERENCE", HERE.parent.parent / "reference"))
 
 _dp = C.POINTER(C.c_double)
 _lp = C.POINTER(C.c_int64)

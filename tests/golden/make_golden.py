@@ -9,7 +9,8 @@ Every fixture holds the problem's input arrays and what the reference library
 returned for it through its own public API (bfm_sim_run for displacements;
 bfm_system_create_planar_* + bfm_system_renumber for the assembled matrix, the
 right-hand side and the RCM permutation).  The 8.lepl1110 case also holds the
-values of the reference's shipped golden files data/U.txt and data/V.txt.
+values of the reference's shipped golden files data/U.txt and data/V.txt; the
+obj_*.npz files hold what its Wavefront reader made of two of its meshes.
 The GPU machine never needs the reference tree: tests read only these files.
 """
 from __future__ import annotations
@@ -95,12 +96,12 @@ def save(name: str, p, h, extra: dict | None = None, system: bool = True):
 
 
 def main():
+    from oracle import oracle as O
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("BFM_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("BFM_REFERENCE", str(O.REF_TREE)))
     ap.add_argument("--only", default=None, help="regenerate one fixture")
     args = ap.parse_args()
     os.environ["BFM_REFERENCE"] = args.reference
-    from oracle import oracle as O
     O.REF_TREE = Path(args.reference)
     from bfm_gb300 import api, meshgen as M
     R = O.ref_lib()
@@ -111,6 +112,8 @@ def main():
         normal_tangent_case(R, api, M)
     if args.only in (None, "axi"):
         axisymmetric_cases(R, api, M)
+    if args.only in (None, "obj"):
+        wavefront_cases(R, ref)
     if args.only is not None:
         return
 
@@ -231,6 +234,48 @@ def axisymmetric_cases(R, api, M):
         h = api.SimHandle.from_problem(R, p, elem_material=False)
         assert h.run() == 0
         save(name, p, h)
+
+
+def parse_obj(path: Path):
+    """Vertices (x, y) and triangles (0-based) of a Wavefront file."""
+    xy, tri = [], []
+    for line in path.read_text().splitlines():
+        t = line.split()
+        if t and t[0] == "v":
+            xy.append((float(t[1]), float(t[2])))
+        elif t and t[0] == "f":
+            tri.append(tuple(int(v.split("/")[0]) - 1 for v in t[1:4]))
+    return np.array(xy, np.float64), np.array(tri, np.int64)
+
+
+def wavefront_cases(R, ref: Path):
+    """The reference's Wavefront reader (mesh.c:203-279) with its edge
+    extraction (compute_edges, mesh.c:52-102) on two of its own meshes: the
+    vertices and faces it read, and its edge list in order -- end nodes in the
+    order kept, the two adjacent elements (-1: none).  The test writes the
+    vertices and faces back as a Wavefront file for the reader under test."""
+    import ctypes as C
+    import tempfile
+    from bfm_gb300 import abi
+    # a unit square of two triangles: its last sorted half-edge is unpaired
+    tmp = Path(tempfile.mkdtemp()) / "square.obj"
+    tmp.write_text("o sq\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3\nf 1 3 4\n")
+    for name, path in (("test", ref / "meshes" / "test.obj"), ("bridge", ref / "meshes" / "bridge.obj"),
+                       ("square", tmp)):
+        st = abi.bfm_state_t()
+        assert R.bfm_state_create(C.byref(st)) == 0
+        mesh = abi.bfm_mesh_t()
+        assert R.bfm_mesh_read_wavefront(C.byref(mesh), C.byref(st), str(path).encode(), False) == 0
+        n, m, ne = mesh.n_nodes, mesh.n_elems, mesh.n_edges
+        coords = np.ctypeslib.as_array(mesh.coords, shape=(n * 2,)).reshape(n, 2).copy()
+        elems = np.ctypeslib.as_array(mesh.elems, shape=(m * 3,)).reshape(m, 3).astype(np.int64)
+        ed = np.array([(mesh.edges[i].nodes[0], mesh.edges[i].nodes[1], mesh.edges[i].elems[0], mesh.edges[i].elems[1])
+                       for i in range(ne)], np.int64)
+        xy, tri = parse_obj(path)
+        assert np.array_equal(xy, coords) and np.array_equal(tri, elems)
+        np.savez_compressed(OUT / f"obj_{name}.npz", coords=coords, elems=elems, edge_nodes=ed[:, :2],
+                            edge_elems=ed[:, 2:])
+        print(f"obj_{name}: N={n} E={m} edges={ne}", file=sys.stderr)
 
 
 if __name__ == "__main__":

@@ -8,7 +8,7 @@ import pytest
 import scipy.sparse as sp
 
 from bfm_gb300 import abi
-from common import CASES, dense_K, gpu_available, load
+from common import CASES, GOLDEN, dense_K, gpu_available, load
 
 
 def rcm_lib(lib, K):
@@ -204,16 +204,35 @@ def test_lepl1110_reader_without_edge_section(libbfm, tmp_path):
     assert (mesh.n_nodes, mesh.n_elems, mesh.n_edges, mesh.kind) == (4418, 8186, 0, 3)
 
 
-def test_wavefront_reader_edges(libbfm, tmp_path):
-    (tmp_path / "t.obj").write_text("o sq\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3\nf 1/1 3/3 4/4\n")
+@pytest.mark.parametrize("name", ["test", "bridge", "square"])
+def test_wavefront_reader_matches_reference(libbfm, tmp_path, name):
+    """bfm_mesh_read_wavefront (mesh.c:203-279) and its edge list (compute_edges,
+    mesh.c:52-102) against the reference library's output on two of its own
+    meshes and a two-triangle square (tests/golden/obj_*.npz): vertices, faces,
+    and every edge in order -- end nodes, both adjacent elements -- bit for bit,
+    including the reference's dropping of an unpaired last half-edge."""
+    d = np.load(GOLDEN / f"obj_{name}.npz")
+    path = tmp_path / f"{name}.obj"
+    with open(path, "w") as f:
+        f.write("# vertices and faces as the reference read them\no shape\n")
+        for x, y in d["coords"]:
+            f.write(f"v {float(x)!r} {float(y)!r} 0.000000\n")
+        f.write("s 0\n")
+        for a, b, c in d["elems"] + 1:
+            f.write(f"f {a} {b} {c}\n")
     st = abi.bfm_state_t()
     libbfm.bfm_state_create(C.byref(st))
     mesh = abi.bfm_mesh_t()
-    assert libbfm.bfm_mesh_read_wavefront(C.byref(mesh), C.byref(st), str(tmp_path / "t.obj").encode(), False) == 0
-    assert (mesh.n_nodes, mesh.n_elems, mesh.n_edges) == (4, 2, 5)
-    edges = [(mesh.edges[i].nodes[0], mesh.edges[i].nodes[1], mesh.edges[i].elems[1]) for i in range(5)]
-    interior = [e for e in edges if e[2] != -1]
-    assert len(interior) == 1 and set(interior[0][:2]) == {0, 2}
+    assert libbfm.bfm_mesh_read_wavefront(C.byref(mesh), C.byref(st), str(path).encode(), False) == 0
+    n, m, ne = mesh.n_nodes, mesh.n_elems, mesh.n_edges
+    assert (n, m, ne) == (len(d["coords"]), len(d["elems"]), len(d["edge_nodes"]))
+    assert np.array_equal(np.ctypeslib.as_array(mesh.coords, shape=(2 * n,)).reshape(n, 2), d["coords"])
+    assert np.array_equal(np.ctypeslib.as_array(mesh.elems, shape=(3 * m,)).reshape(m, 3), d["elems"])
+    ed = np.array([(mesh.edges[i].nodes[0], mesh.edges[i].nodes[1], mesh.edges[i].elems[0], mesh.edges[i].elems[1])
+                   for i in range(ne)], np.int64)
+    assert np.array_equal(ed[:, :2], d["edge_nodes"])
+    assert np.array_equal(ed[:, 2:], d["edge_elems"])
+    libbfm.bfm_mesh_destroy(C.byref(mesh))
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU behaviour")
