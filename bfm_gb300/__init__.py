@@ -23,7 +23,7 @@ _lib: C.CDLL | None = None
 class bfm_gpu_opts_t(C.Structure):  # include/bfm/gpu.h
     _fields_ = [("precision", C.c_int), ("precond", C.c_int), ("rtol", C.c_double), ("max_iters", C.c_int),
                 ("replace_drop", C.c_double), ("deterministic", C.c_int), ("autotune", C.c_int),
-                ("barrier_polls", C.c_int64)]
+                ("barrier_polls", C.c_int64), ("refine_restart", C.c_int)]
 
 
 class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h

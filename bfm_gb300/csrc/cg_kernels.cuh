@@ -68,6 +68,7 @@ struct CgOpts {
 	double rtol;
 	double drop2;  // mixed: replace when (r,r) has dropped by this factor since the last replacement
 	int max_iters;
+	int restart;   // mixed: each FP64 refinement step restarts the inner PCG (beta = 0)
 };
 
 // Vectors are interleaved (u,v) per node and accessed as pairs.
@@ -89,6 +90,7 @@ struct CgArgs {
 	V* pn;  // mixed path: direction written this iteration (ping-pong with p)
 	V* s;   // FP64 path: s = A p by recurrence
 	V* w;   // FP64 path: w = A u; mixed path: q = A p
+	V* z;   // mixed path with SSOR sweeps: z = M r, formed by the sweeps (no_pc)
 	double* partials;
 	unsigned* ticket;
 	CgState* st;
@@ -418,6 +420,25 @@ __global__ void __launch_bounds__(TPB_K) k_cg64_update(CgArgs<double> a) {
 //   K2: dx += alpha p'; r -= alpha q; gamma' = (r, M r), rho = (r, r); beta
 //   on request (IF node): x += dx, dx = 0; r = b - A64 x in FP64; gamma = (r, M r)
 
+// K2 finisher when the SSOR sweeps come next: the iteration count, the cap
+// and the replacement request (from rho alone); beta and gamma follow from
+// the sweeps' (r, z)
+__device__ __forceinline__ void hs_rho(CgState* st, double rho, int timing, int use_cond, cudaGraphConditionalHandle cond,
+                                       cudaGraphConditionalHandle cond_repl) {
+	if (timing) return;
+	double const tol2 = st->rtol * st->rtol * st->bnorm2;
+	st->rho = rho;
+	st->iter += 1;
+	if (st->iter >= st->max_iters) {
+		st->status = BFM_GPU_NOT_CONVERGED;
+		st->done = 1;
+		if (use_cond) cudaGraphSetConditional(cond, 0u);
+	}
+	else if (use_cond && (rho <= st->drop2 * st->rho_ref || rho <= tol2)) {
+		cudaGraphSetConditional(cond_repl, 1u);
+	}
+}
+
 struct DF {
 	float hi, lo;
 };
@@ -448,11 +469,20 @@ __global__ void __launch_bounds__(TPB_K) k_mx_spmv(CgArgs<float> a) {
 	const float* __restrict__ r = a.r;
 	const float* __restrict__ p = a.p;
 	const float* __restrict__ dinv = a.dinv;
-	int const bpc = a.block_pc;
+	const float* __restrict__ zv = a.z;
+	int const bpc = a.block_pc, zpc = a.no_pc;
 	auto gather = [=](int c, float& g0, float& g1) {
-		float2 const rc = ld2(r, c), pc = ld2(p, c);
+		float2 const pc = ld2(p, c);
 		float z0, z1;
-		precond_apply(dinv, bpc, c, rc.x, rc.y, z0, z1);
+		if (zpc) {  // z = M r from the SSOR sweeps
+			float2 const zc = ld2(zv, c);
+			z0 = zc.x;
+			z1 = zc.y;
+		}
+		else {      // z = M r of the point or block Jacobi preconditioner, on the fly
+			float2 const rc = ld2(r, c);
+			precond_apply(dinv, bpc, c, rc.x, rc.y, z0, z1);
+		}
 		g0 = z0 + beta * pc.x;
 		g1 = z1 + beta * pc.y;
 	};
@@ -507,16 +537,22 @@ __global__ void __launch_bounds__(TPB_K) k_mx_update(CgArgs<float> a) {
 		st2(a.u, i, dx.x + alpha * pn.x, dx.y + alpha * pn.y);
 		float const r0 = r.x - alpha * q.x, r1 = r.y - alpha * q.y;
 		st2(a.r, i, r0, r1);
-		float z0, z1;
-		precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
-		df_add_prod(g, r0, z0);
-		df_add_prod(g, r1, z1);
+		if (!a.no_pc) {
+			float z0, z1;
+			precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
+			df_add_prod(g, r0, z0);
+			df_add_prod(g, r1, z1);
+		}
 		df_add_prod(rr, r0, r0);
 		df_add_prod(rr, r1, r1);
 	}
 	double v[2] = {df_value(g), df_value(rr)};
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+		if (a.no_pc) {  // the SSOR sweeps come next: gamma and beta follow from their (r, z)
+			hs_rho(st, out[1], a.timing, a.use_cond, a.cond, a.cond_repl);
+			return;
+		}
 		if (a.timing) return;
 		double const gamma = out[0], rho = out[1];
 		double const tol2 = st->rtol * st->rtol * st->bnorm2;
@@ -614,15 +650,19 @@ __global__ void __launch_bounds__(TPB_K) k_mx_replace(CgArgs<float> a) {
 		if (row_ < a.N && sub_ == 0) {
 			float const r0 = (float) e0, r1 = (float) e1;
 			st2(a.r, row_, r0, r1);
-			float z0, z1;
-			precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
 			v[0] += e0 * e0 + e1 * e1;
-			v[1] += (double) r0 * (double) z0 + (double) r1 * (double) z1;
+			if (!a.no_pc) {
+				float z0, z1;
+				precond_apply(a.dinv, a.block_pc, row_, r0, r1, z0, z1);
+				v[1] += (double) r0 * (double) z0 + (double) r1 * (double) z1;
+			}
 		}
 	}
 	double out[2];
 	if (grid_sum<2>(v, a.partials, a.ticket, out) && threadIdx.x == 0) {
-		st->gamma = out[1];
+		if (!a.no_pc) st->gamma = out[1];  // else the SSOR sweeps (mode 1) set it
+		// iterative refinement with restarts: the inner PCG starts afresh from this residual
+		if (a.opts.restart) st->beta = 0.0;
 		if (true_residual_verdict(st, out[0])) {
 			st->done = 1;
 			if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
@@ -880,25 +920,6 @@ __device__ __forceinline__ void hs_beta(CgState* st, double gamma, double rho, i
 	// launched from a host loop (no conditional nodes): the replacement
 	// kernel, launched after every K2, reads the request from the state
 	if (!use_cond) st->repl_req = repl && !stop;
-}
-
-// K2 finisher when the SSOR sweeps come next: the iteration count, the cap
-// and the replacement request (from rho alone); beta and gamma follow from
-// the sweeps' (r, z)
-__device__ __forceinline__ void hs_rho(CgState* st, double rho, int timing, int use_cond, cudaGraphConditionalHandle cond,
-                                       cudaGraphConditionalHandle cond_repl) {
-	if (timing) return;
-	double const tol2 = st->rtol * st->rtol * st->bnorm2;
-	st->rho = rho;
-	st->iter += 1;
-	if (st->iter >= st->max_iters) {
-		st->status = BFM_GPU_NOT_CONVERGED;
-		st->done = 1;
-		if (use_cond) cudaGraphSetConditional(cond, 0u);
-	}
-	else if (use_cond && (rho <= st->drop2 * st->rho_ref || rho <= tol2)) {
-		cudaGraphSetConditional(cond_repl, 1u);
-	}
 }
 
 template <int LPR, int NB = 1>
@@ -1383,6 +1404,20 @@ struct SsorArgs {
 	const int* agg;      // aggregate of each node
 	const float4* pnode; // per node: (dx / H, dy / H, u free, v free)
 	const float2* yc;    // A_c^-1 P^T r, double-float pair per coarse DOF
+	// the sweeps' blocks, apart from the CSR matrix: sliced ELL over slices
+	// of 32 consecutive rows of one colour, the slice's k-th block of row
+	// `lane` at [ptr[s] + 32 k + lane] (padding: column -1), so a warp reads
+	// 32 consecutive blocks per step.  Lower-colour blocks (forward sweep) and
+	// higher-colour blocks (backward) are kept apart: each phase streams only
+	// the blocks it uses, each once.
+	const float4* lv;
+	const int* lc;
+	const int* lp;
+	const float4* uv;
+	const int* uc;
+	const int* up;
+	int slice0;          // per-phase kernels: first slice of this phase's colour
+	int sbase[65];       // persistent kernel: first slice of colour c
 };
 
 
@@ -1401,28 +1436,30 @@ __device__ __forceinline__ void ssor_blk(float4 d, dfl s0, dfl s1, dfl& o0, dfl&
 	o1 = df_add(df_mul_f(d.z, s0), df_mul_f(d.w, s1));
 }
 
-// sum of A_ij v_j over blocks [k0, k1) of the row whose column lies in
-// [cmin, cmax), v double-float float4 per node (written by other blocks of
-// the persistent kernel: read past L1).  SSOR_CHUNK blocks at a time: their
-// column indices and values are loaded together, then their gathers.
+// sum of A_ij y_j over the sliced-ELL blocks of row `lane` of slice s, y
+// double-float float4 per node (written by other blocks of the persistent
+// kernel: read past L1).  SSOR_CHUNK blocks at a time: their column indices
+// and values are loaded together, then their gathers.  The slice's width is
+// the same for the whole warp.
 constexpr int SSOR_CHUNK = 2;  // with 8 resident blocks per SM (32 registers)
 
-__device__ __forceinline__ void ssor_row(const SsorArgs& a, int k0, int k1, int cmin, int cmax, dfl& t0, dfl& t1) {
-	for (int kb = k0; kb < k1; kb += SSOR_CHUNK) {
+__device__ __forceinline__ void sell_row(const float4* __restrict__ v, const int* __restrict__ cidx,
+                                         const int* __restrict__ ptr, int s, int lane, const float* y, dfl& t0, dfl& t1) {
+	int const k0 = ptr[s] + lane, w = (ptr[s + 1] - ptr[s]) >> 5;
+	for (int kb = 0; kb < w; kb += SSOR_CHUNK) {
 		int c[SSOR_CHUNK];
 		float4 m[SSOR_CHUNK];
 #pragma unroll
 		for (int j = 0; j < SSOR_CHUNK; j++) {
-			bool const in = kb + j < k1;
-			c[j] = in ? a.cols[kb + j] : -1;
-			m[j] = in ? reinterpret_cast<const float4*>(a.hi)[kb + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+			bool const in = kb + j < w;
+			int const e = k0 + 32 * (kb + j);
+			c[j] = in ? __ldcs(cidx + e) : -1;
+			m[j] = in ? __ldcs(v + e) : make_float4(0.f, 0.f, 0.f, 0.f);
 		}
 		float4 g[SSOR_CHUNK];
 #pragma unroll
-		for (int j = 0; j < SSOR_CHUNK; j++) {
-			bool const use = c[j] >= cmin && c[j] < cmax;
-			g[j] = use ? __ldcg(reinterpret_cast<const float4*>(a.y) + c[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
-		}
+		for (int j = 0; j < SSOR_CHUNK; j++)
+			g[j] = c[j] >= 0 ? __ldcg(reinterpret_cast<const float4*>(y) + c[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
 		for (int j = 0; j < SSOR_CHUNK; j++) {
 			dfl const g0 = {g[j].x, g[j].z}, g1 = {g[j].y, g[j].w};
@@ -1432,10 +1469,22 @@ __device__ __forceinline__ void ssor_row(const SsorArgs& a, int k0, int k1, int 
 	}
 }
 
-template <bool DF>
+// vector layouts of the residual r and z = M^-1 r the sweeps read and write
+enum : int {
+	VT_F64 = 0,  // double2 per node (FP64 path)
+	VT_DF = 1,   // double-float float4 per node (u_hi, v_hi, u_lo, v_lo)
+	VT_F32 = 2,  // float2 per node (mixed path); the sweeps still sum in double-float
+};
+
+template <int VT>
 __device__ __forceinline__ void ssor_ld_r(const void* r, int i, dfl& r0, dfl& r1, double& q0, double& q1) {
-	if constexpr (DF) {
+	if constexpr (VT == VT_DF) {
 		df_ld((const float*) r, i, r0, r1);
+	}
+	else if constexpr (VT == VT_F32) {
+		float2 const t = ld2((const float*) r, i);
+		r0 = {t.x, 0.f};
+		r1 = {t.y, 0.f};
 	}
 	else {
 		double2 const t = ld2((const double*) r, i);
@@ -1456,7 +1505,7 @@ __device__ __forceinline__ void coarse_term(const int* agg, const float4* pnode,
 	c1 = q.w != 0.f ? df_add({b.x, b.y}, df_mul_f(q.x, y2)) : dfl{0.f, 0.f};
 }
 
-template <bool DF>
+template <int VT>
 __device__ __forceinline__ void ssor_st_z(const SsorArgs& a, int i, dfl z0, dfl z1, dfl r0, dfl r1, double q0, double q1,
                                           dfl& acc, double& acc64) {
 	if (a.yc) {
@@ -1465,9 +1514,15 @@ __device__ __forceinline__ void ssor_st_z(const SsorArgs& a, int i, dfl z0, dfl 
 		z0 = df_add(z0, c0);
 		z1 = df_add(z1, c1);
 	}
-	if constexpr (DF) {
+	if constexpr (VT == VT_DF) {
 		df_st((float*) a.z, i, z0, z1);
 		acc = df_add(acc, df_add(df_mul(r0, z0), df_mul(r1, z1)));
+	}
+	else if constexpr (VT == VT_F32) {
+		// (r, z) of the rounded z the iteration will use
+		dfl const w0 = {__fadd_rn(z0.hi, z0.lo), 0.f}, w1 = {__fadd_rn(z1.hi, z1.lo), 0.f};
+		st2((float*) a.z, i, w0.hi, w1.hi);
+		acc = df_add(acc, df_add(df_mul(r0, w0), df_mul(r1, w1)));
 	}
 	else {
 		double const w0 = df_dbl(z0), w1 = df_dbl(z1);
@@ -1506,7 +1561,7 @@ __device__ __forceinline__ void ssor_finish(const SsorArgs& a, double part) {
 	}
 }
 
-template <bool DF>
+template <int VT>
 __global__ void __launch_bounds__(TPB_K) k_ssor_fwd(SsorArgs a) {
 	if (a.st->done && !a.timing) return;
 	dfl acc = {0.f, 0.f};
@@ -1514,28 +1569,28 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_fwd(SsorArgs a) {
 	for (int i = a.lo + blockIdx.x * blockDim.x + threadIdx.x; i < a.hi_row; i += gridDim.x * blockDim.x) {
 		dfl r0, r1;
 		double q0 = 0.0, q1 = 0.0;
-		ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
+		ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
 		dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
-		ssor_row(a, a.row_ptr[i], a.dpos[i], 0, a.lo, t0, t1);
+		sell_row(a.lv, a.lc, a.lp, a.slice0 + ((i - a.lo) >> 5), (i - a.lo) & 31, a.y, t0, t1);
 		dfl y0, y1;
 		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[i], df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), y0, y1);
 		df_st(a.y, i, y0, y1);
-		if (a.fwd_last) ssor_st_z<DF>(a, i, y0, y1, r0, r1, q0, q1, acc, acc64);
+		if (a.fwd_last) ssor_st_z<VT>(a, i, y0, y1, r0, r1, q0, q1, acc, acc64);
 	}
 	if (!a.fwd_last) return;
-	double v[1] = {DF ? df_dbl(acc) : acc64};
+	double v[1] = {VT == VT_F64 ? acc64 : df_dbl(acc)};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
 }
 
-template <bool DF>
+template <int VT>
 __global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
 	if (a.st->done && !a.timing) return;
 	dfl acc = {0.f, 0.f};
 	double acc64 = 0.0;
 	for (int i = a.lo + blockIdx.x * blockDim.x + threadIdx.x; i < a.hi_row; i += gridDim.x * blockDim.x) {
 		dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
-		ssor_row(a, a.dpos[i] + 1, a.row_ptr[i + 1], a.hi_row, 0x7fffffff, t0, t1);
+		sell_row(a.uv, a.uc, a.up, a.slice0 + ((i - a.lo) >> 5), (i - a.lo) & 31, a.y, t0, t1);
 		dfl w0, w1, y0, y1;
 		ssor_blk(reinterpret_cast<const float4*>(a.dinv)[i], t0, t1, w0, w1);
 		df_ld(a.y, i, y0, y1);
@@ -1543,10 +1598,10 @@ __global__ void __launch_bounds__(TPB_K) k_ssor_bwd(SsorArgs a) {
 		df_st(a.y, i, z0, z1);
 		dfl r0, r1;
 		double q0 = 0.0, q1 = 0.0;
-		ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
-		ssor_st_z<DF>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
+		ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+		ssor_st_z<VT>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
 	}
-	double v[1] = {DF ? df_dbl(acc) : acc64};
+	double v[1] = {VT == VT_F64 ? acc64 : df_dbl(acc)};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
 }
@@ -1624,7 +1679,7 @@ __device__ bool grid_barrier(unsigned* bar, int* err, long polls) {
 
 __device__ __forceinline__ bool ssor_barrier(const SsorArgs& a) { return grid_barrier(a.bar, &a.st->ssor_err, a.polls); }
 
-template <bool DF>
+template <int VT>
 __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 	if (a.st->done && !a.timing) return;
 	grid_barrier_init(a.bar);
@@ -1644,27 +1699,28 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 			dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
 			float4 const d = reinterpret_cast<const float4*>(a.dinv)[i];
 			dfl z0, z1;
+			int const sl = a.sbase[c] + ((i - lo) >> 5), lane = (i - lo) & 31;
 			if (forward) {
-				ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
-				ssor_row(a, a.row_ptr[i], a.dpos[i], 0, lo, t0, t1);
+				ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+				sell_row(a.lv, a.lc, a.lp, sl, lane, a.y, t0, t1);
 				ssor_blk(d, df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), z0, z1);
 			}
 			else {
-				ssor_row(a, a.dpos[i] + 1, a.row_ptr[i + 1], hi, 0x7fffffff, t0, t1);
+				sell_row(a.uv, a.uc, a.up, sl, lane, a.y, t0, t1);
 				dfl w0, w1;
 				ssor_blk(d, t0, t1, w0, w1);
 				float4 const yv = __ldcg(reinterpret_cast<const float4*>(a.y) + i);
 				z0 = df_add({yv.x, yv.z}, df_neg(w0));
 				z1 = df_add({yv.y, yv.w}, df_neg(w1));
-				ssor_ld_r<DF>(a.r, i, r0, r1, q0, q1);
+				ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
 			}
 			__stcg(reinterpret_cast<float4*>(a.y) + i, make_float4(z0.hi, z1.hi, z0.lo, z1.lo));
-			if (final_rows) ssor_st_z<DF>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
+			if (final_rows) ssor_st_z<VT>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
 		}
 		if (ph < 2 * nc - 2) alive = ssor_barrier(a);
 	}
 	// every block reaches the reduction, finished or not
-	double v[1] = {DF ? df_dbl(acc) : acc64};
+	double v[1] = {VT == VT_F64 ? acc64 : df_dbl(acc)};
 	double out[1];
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
 }
@@ -1698,10 +1754,12 @@ struct CoarseArgs {
 	float2* yt;               // X rc           (the same)
 	float2* yc;               // X^T X rc
 	const void* r;
-	int df;                   // r in double-float (float4 per node) or FP64 (double2)
+	int df;                   // layout of r: VT_F64 (double2 per node), VT_DF (float4) or VT_F32 (float2)
 	const int* row_ptr;
 	const int* cols;
-	const double* vals64;
+	const double* vals64;     // the operator A_c is formed from: FP64 blocks, or (nullptr)
+	const float* vals32;      // the FP32 blocks in difference form with the row-sum blocks
+	const float* corr32;      // corr32 (the MIXED precision)
 	int* err;
 	unsigned* bar;       // grid barrier words of the one-launch form (k_coarse_apply)
 	int* berr;           // its timeout flag
@@ -1803,7 +1861,12 @@ __device__ __forceinline__ void restrict_chunk(const CoarseArgs& a, int q, int l
 		pq[u] = make_float4(0.f, 0.f, 0.f, 0.f);
 		int const i = idx[u];
 		if (i < 0) continue;
-		if (a.df) df_ld((const float*) a.r, i, r0[u], r1[u]);
+		if (a.df == VT_DF) df_ld((const float*) a.r, i, r0[u], r1[u]);
+		else if (a.df == VT_F32) {
+			float2 const t = ld2((const float*) a.r, i);
+			r0[u] = {t.x, 0.f};
+			r1[u] = {t.y, 0.f};
+		}
 		else {
 			double2 const t = ld2((const double*) a.r, i);
 			r0[u] = df_make(t.x);
@@ -1954,6 +2017,18 @@ __global__ void k_coarse_ac(CoarseArgs a) {
 		int const i = a.agg_nodes[k];
 		float4 const pi = a.pnode[i];
 		double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
+		// the FP32 operator in difference form, (A g)_i = S_i g_i + sum_j A_ij (g_j - g_i):
+		// its diagonal block is S_i - sum_{j != i} A_ij
+		double deff[4] = {0.0, 0.0, 0.0, 0.0};
+		if (!a.vals64) {
+			float4 const sr = reinterpret_cast<const float4*>(a.corr32)[i];
+			deff[0] = sr.x; deff[1] = sr.y; deff[2] = sr.z; deff[3] = sr.w;
+			for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
+				if (a.cols[e] == i) continue;
+				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
+				deff[0] -= v.x; deff[1] -= v.y; deff[2] -= v.z; deff[3] -= v.w;
+			}
+		}
 		for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
 			int const j = a.cols[e];
 			int jx, jy;
@@ -1966,7 +2041,17 @@ __global__ void k_coarse_ac(CoarseArgs a) {
 			int const slot = (oy + 1) * 3 + (ox + 1);
 			float4 const pj = a.pnode[j];
 			double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
-			const double* m = a.vals64 + 4l * e;
+			double m[4];
+			if (a.vals64) {
+				for (int t = 0; t < 4; t++) m[t] = a.vals64[4l * e + t];
+			}
+			else if (j == i) {
+				for (int t = 0; t < 4; t++) m[t] = deff[t];
+			}
+			else {
+				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
+				m[0] = v.x; m[1] = v.y; m[2] = v.z; m[3] = v.w;
+			}
 			// A P_j (2x3), then P_i^T (3x2) times it
 			double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
 			                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};

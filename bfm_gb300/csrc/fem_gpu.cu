@@ -300,6 +300,83 @@ __global__ void k_map_ids(long n, int N, int* __restrict__ ids, const int* __res
 // first block of each row at or after the diagonal: the lower-colour
 // neighbours are [row_ptr[i], dpos[i]), the higher-colour ones follow the
 // diagonal block
+// ------------------------------------------------------------------ sliced ELL of the SSOR sweeps
+
+// slices of 32 consecutive rows of one colour: colour c's slices start at
+// sbase[c] (sbase[ncol] = all slices)
+struct SellMap {
+	int ncol;
+	int off[65];
+	int sbase[65];
+};
+
+// row of slice s and lane (or -1 past the colour's last row), its colour in c
+__device__ __forceinline__ int sell_row_of(const SellMap& m, int s, int lane, int& c) {
+	c = 0;
+	while (c + 1 < m.ncol && m.sbase[c + 1] <= s) c++;
+	int const row = m.off[c] + ((s - m.sbase[c]) << 5) + lane;
+	return row < m.off[c + 1] ? row : -1;
+}
+
+// per slice (one warp each): 32 x the most lower-colour and the most
+// higher-colour blocks any of its rows has
+__global__ void k_sell_width(int ns, SellMap m, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+                             int* __restrict__ lw, int* __restrict__ uw) {
+	int const s = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (s >= ns) return;  // whole warps
+	int c;
+	int const row = sell_row_of(m, s, lane, c);
+	int nl = 0, nu = 0;
+	if (row >= 0)
+		for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
+			int const j = cols[k];
+			nl += j < m.off[c];
+			nu += j >= m.off[c + 1];
+		}
+	nl = __reduce_max_sync(0xffffffffu, nl);
+	nu = __reduce_max_sync(0xffffffffu, nu);
+	if (lane == 0) {
+		lw[s] = 32 * nl;
+		uw[s] = 32 * nu;
+	}
+}
+
+// copy each row's lower- and higher-colour blocks (ascending columns, as in
+// the CSR rows) into its lane of the slice; pad with column -1
+__global__ void k_sell_fill(int ns, SellMap m, const int* __restrict__ row_ptr, const int* __restrict__ cols,
+                            const float4* __restrict__ vals, const int* __restrict__ lp, const int* __restrict__ up,
+                            float4* __restrict__ lv, int* __restrict__ lc, float4* __restrict__ uv, int* __restrict__ uc) {
+	int const s = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (s >= ns) return;
+	int c;
+	int const row = sell_row_of(m, s, lane, c);
+	int const el = lp[s] + lane, eu = up[s] + lane;
+	int const wl = (lp[s + 1] - lp[s]) >> 5, wu = (up[s + 1] - up[s]) >> 5;
+	int nl = 0, nu = 0;
+	if (row >= 0)
+		for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
+			int const j = cols[k];
+			if (j < m.off[c]) {
+				lc[el + 32 * nl] = j;
+				lv[el + 32 * nl] = vals[k];
+				nl++;
+			}
+			else if (j >= m.off[c + 1]) {
+				uc[eu + 32 * nu] = j;
+				uv[eu + 32 * nu] = vals[k];
+				nu++;
+			}
+		}
+	for (; nl < wl; nl++) {
+		lc[el + 32 * nl] = -1;
+		lv[el + 32 * nl] = make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+	for (; nu < wu; nu++) {
+		uc[eu + 32 * nu] = -1;
+		uv[eu + 32 * nu] = make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+}
+
 __global__ void k_diag_pos(int N, const int* __restrict__ row_ptr, const int* __restrict__ cols, int* __restrict__ dpos) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
@@ -1403,6 +1480,13 @@ struct bfm_gpu_problem {
 	void* otmp;    // scratch of the in-place permutations
 	float* ssor_y; // sweep vector (double-float, 4 floats per node)
 	float4* ssor_d;  // the relaxation blocks' FP32 halves, packed (k_pack_hi) before every solve
+	// the sweeps' blocks as sliced ELL (lower-colour and higher-colour parts)
+	int sl_n;            // slices
+	int sl_base[65];     // first slice of each colour
+	int *sl_lw, *sl_uw, *sl_lp, *sl_up;  // widths and slice offsets (n + 1 each)
+	long sl_lcap, sl_ucap;
+	float4 *sl_lv, *sl_uv;
+	int *sl_lc, *sl_uc;
 	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
 	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
 	long polls;          // polls per grid barrier before it gives up (the solve graph's)
@@ -1495,6 +1579,11 @@ bool ssor_pc(int pc) {
 bool coarse_pc(int pc) { return pc == BFM_GPU_PC_SSOR2 || pc == BFM_GPU_PC_LEARNED_SSOR2; }
 bool learned_pc(int pc) {
 	return pc == BFM_GPU_PC_LEARNED || pc == BFM_GPU_PC_LEARNED_SSOR || pc == BFM_GPU_PC_LEARNED_SSOR2;
+}
+bool mixed_prec(int precision) { return precision == BFM_GPU_MIXED || precision == BFM_GPU_MIXED_EXACT; }
+// the layout of the Krylov vectors the SSOR sweeps read and write
+int precision_vt(int precision) {
+	return precision == BFM_GPU_FP64_DF ? VT_DF : mixed_prec(precision) ? VT_F32 : VT_F64;
 }
 
 // Node-block pattern of the current element array (steps 1-2 of the assembly).
@@ -1810,7 +1899,7 @@ int coarse_apply_grid(bfm_gpu_problem* P) {
 	return P->coarse_grid;
 }
 
-CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
+CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, int vt) {
 	CoarseArgs c;
 	memset(&c, 0, sizeof c);
 	c.na = P->na;
@@ -1831,10 +1920,14 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, bool df) {
 	c.rc = P->rc;
 	c.yt = P->ayt;
 	c.r = r;
-	c.df = df;
+	c.df = vt;
 	c.row_ptr = P->row_ptr;
 	c.cols = P->cols;
-	c.vals64 = P->vals64;
+	// A_c from the FP64 operator where the precision assembles one, else from
+	// the FP32 operator (MIXED)
+	c.vals64 = P->precision != BFM_GPU_MIXED ? P->vals64 : nullptr;
+	c.vals32 = P->vals32;
+	c.corr32 = P->corr32;
 	c.err = P->coarse_err;
 	c.bar = P->ssor_bar;
 	c.berr = P->st ? &P->st->ssor_err : P->coarse_err;
@@ -1969,6 +2062,63 @@ int build_aggregates(bfm_gpu_problem* P) {
 // Per assembly: node offsets and free DOFs, A_c = P^T A P (band), its band
 // Cholesky factor and X = L^-1.  A neighbour beyond the adjacent cells leaves
 // the solve on plain SSOR (coarse_ok = 0).
+// The sweeps' sliced-ELL copy of the FP32 blocks of the current assembly
+// (after the values; the colour order must be the matrix's).  The slice
+// widths are read back to size the arrays: one host sync per assembly.
+int build_sell(bfm_gpu_problem* P) {
+	cudaStream_t const st = P->stream;
+	int const nc = P->ncol > 0 ? P->ncol : 1;
+	SellMap m;
+	memset(&m, 0, sizeof m);
+	m.ncol = nc;
+	int ns = 0;
+	for (int c = 0; c < nc; c++) {
+		m.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
+		m.sbase[c] = ns;
+		int const rows = (P->ncol > 0 ? P->col_off[c + 1] : P->N) - m.off[c];
+		ns += (rows + 31) / 32;
+	}
+	m.off[nc] = P->N;
+	m.sbase[nc] = ns;
+	P->sl_n = ns;
+	memcpy(P->sl_base, m.sbase, sizeof m.sbase);
+	long const cap_s = P->N / 32 + 66;
+	if (!P->sl_lw && (dalloc(&P->sl_lw, cap_s) || dalloc(&P->sl_uw, cap_s) || dalloc(&P->sl_lp, cap_s + 1) ||
+	                  dalloc(&P->sl_up, cap_s + 1)))
+		return -1;
+	if (ns == 0) return 0;
+	int const warps_tpb = TPB / 32;
+	k_sell_width<<<(ns + warps_tpb - 1) / warps_tpb, TPB, 0, st>>>(ns, m, P->row_ptr, P->cols, P->sl_lw, P->sl_uw);
+	if (scan(P, P->sl_lw, P->sl_lp, ns) || scan(P, P->sl_uw, P->sl_up, ns)) return -1;
+	int tot[2] = {0, 0};
+	CK(cudaMemcpyAsync(&tot[0], P->sl_lp + ns, sizeof(int), cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(&tot[1], P->sl_up + ns, sizeof(int), cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	if (tot[0] > P->sl_lcap) {
+		if (P->sl_lv) cudaFree(P->sl_lv);
+		if (P->sl_lc) cudaFree(P->sl_lc);
+		P->sl_lv = nullptr;
+		P->sl_lc = nullptr;
+		P->sl_lcap = 0;
+		if (dalloc(&P->sl_lv, tot[0]) || dalloc(&P->sl_lc, tot[0])) return -1;
+		P->sl_lcap = tot[0];
+	}
+	if (tot[1] > P->sl_ucap) {
+		if (P->sl_uv) cudaFree(P->sl_uv);
+		if (P->sl_uc) cudaFree(P->sl_uc);
+		P->sl_uv = nullptr;
+		P->sl_uc = nullptr;
+		P->sl_ucap = 0;
+		if (dalloc(&P->sl_uv, tot[1]) || dalloc(&P->sl_uc, tot[1])) return -1;
+		P->sl_ucap = tot[1];
+	}
+	k_sell_fill<<<(ns + warps_tpb - 1) / warps_tpb, TPB, 0, st>>>(ns, m, P->row_ptr, P->cols,
+	                                                            reinterpret_cast<const float4*>(P->vals32), P->sl_lp,
+	                                                            P->sl_up, P->sl_lv, P->sl_lc, P->sl_uv, P->sl_uc);
+	CK(cudaGetLastError());
+	return 0;
+}
+
 int coarse_setup(bfm_gpu_problem* P) {
 	cudaStream_t const st = P->stream;
 	P->coarse_ok = 0;
@@ -1979,7 +2129,7 @@ int coarse_setup(bfm_gpu_problem* P) {
 	CK(cudaMemsetAsync(P->aband, 0, (size_t) P->nc * (P->abw + 1) * sizeof(float2), st));
 	CK(cudaMemsetAsync(P->diag0, 0, (size_t) P->nc * sizeof(double), st));
 	CK(cudaMemsetAsync(P->coarse_err, 0, sizeof(int), st));
-	CoarseArgs ca = coarse_args(P, nullptr, true);
+	CoarseArgs ca = coarse_args(P, nullptr, VT_DF);
 	k_coarse_ac<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
 	k_coarse_ac_sum<<<blocks_for(81l * P->na), TPB, 0, st>>>(ca);
 	int err = 0;
@@ -2025,6 +2175,7 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 	a.s = (V*) P->vec[3];
 	a.pn = (V*) P->vec[3];
 	a.w = (V*) P->vec[4];
+	a.z = (V*) P->vec[5];
 	a.partials = P->partials;
 	a.ticket = P->ticket;
 	a.st = P->st;
@@ -2032,6 +2183,9 @@ CgArgs<V> cg_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		a.opts.rtol = o->rtol;
 		a.opts.drop2 = o->replace_drop * o->replace_drop;
 		a.opts.max_iters = o->max_iters;
+		// mixed precisions: restart the inner PCG at each FP64 refinement step,
+		// or keep its direction (the default: fewer iterations on the plates)
+		a.opts.restart = o->refine_restart == 1;
 	}
 	return a;
 }
@@ -2106,17 +2260,35 @@ SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
 	a.ticket = P->ticket;
 	a.st = P->st;
 	a.polls = P->polls;
+	a.lv = P->sl_lv;
+	a.lc = P->sl_lc;
+	a.lp = P->sl_lp;
+	a.uv = P->sl_uv;
+	a.uc = P->sl_uc;
+	a.up = P->sl_up;
+	memcpy(a.sbase, P->sl_base, sizeof a.sbase);
 	return a;
+}
+
+// the sweep kernels of a vector layout (VT_*)
+void* ssor_all_kernel(int vt) {
+	return vt == VT_DF ? (void*) k_ssor_all<VT_DF> : vt == VT_F32 ? (void*) k_ssor_all<VT_F32> : (void*) k_ssor_all<VT_F64>;
+}
+void* ssor_fwd_kernel(int vt) {
+	return vt == VT_DF ? (void*) k_ssor_fwd<VT_DF> : vt == VT_F32 ? (void*) k_ssor_fwd<VT_F32> : (void*) k_ssor_fwd<VT_F64>;
+}
+void* ssor_bwd_kernel(int vt) {
+	return vt == VT_DF ? (void*) k_ssor_bwd<VT_DF> : vt == VT_F32 ? (void*) k_ssor_bwd<VT_F32> : (void*) k_ssor_bwd<VT_F64>;
 }
 
 // The 2 nc - 1 sweep phases of one z = M^-1 r after node `dep` (nullptr: first
 // in the graph), in graph g; *last gets the final node.  mode as SsorArgs.
-int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cudaGraphNode_t* dep, SsorArgs base, bool df,
+int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cudaGraphNode_t* dep, SsorArgs base, int vt,
              int mode) {
 	int const nc = P->ncol > 0 ? P->ncol : 1;
 	if (coarse_pc(P->precond) && P->coarse_ok) {
 		// two-level: yc = A_c^-1 P^T r first; the sweeps add P yc to z
-		CoarseArgs ca = coarse_args(P, base.r, df);
+		CoarseArgs ca = coarse_args(P, base.r, vt);
 		void* pc[1] = {&ca};
 		static_assert(CX_T == TPB, "graph kernel nodes run TPB threads per block");
 		bool one = false;
@@ -2161,7 +2333,7 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		a.mode = mode;
 		void* pa[1] = {&a};
 		cudaGraphNode_t n;
-		if (add_node(g, &n, dep, df ? (void*) k_ssor_all<true> : (void*) k_ssor_all<false>, P->ssor_grid, pa)) return -1;
+		if (add_node(g, &n, dep, ssor_all_kernel(vt), P->ssor_grid, pa)) return -1;
 		cudaLaunchAttributeValue v;
 		memset(&v, 0, sizeof v);
 		v.cooperative = 1;
@@ -2174,8 +2346,8 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		cudaGraphDestroyNode(n);
 		P->ssor_grid = 0;
 	}
-	void* fwd = df ? (void*) k_ssor_fwd<true> : (void*) k_ssor_fwd<false>;
-	void* bwd = df ? (void*) k_ssor_bwd<true> : (void*) k_ssor_bwd<false>;
+	void* fwd = ssor_fwd_kernel(vt);
+	void* bwd = ssor_bwd_kernel(vt);
 	const cudaGraphNode_t* d = dep;
 	cudaGraphNode_t n;
 	for (int ph = 0; ph < 2 * nc - 1; ph++) {
@@ -2184,6 +2356,7 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		int const c = forward ? ph : 2 * nc - 2 - ph;
 		a.lo = P->col_off[c];
 		a.hi_row = P->col_off[c + 1];
+		a.slice0 = P->sl_base[c];
 		a.fwd_last = forward && c == nc - 1;
 		a.first_acc = a.fwd_last;
 		a.final_phase = ph == 2 * nc - 2;
@@ -2235,7 +2408,7 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		sa.cond = h;
 		void* pi[1] = {&a[0]};
 		if (add_node(g, &n_init, nullptr, (void*) k_df_init, P->grid, pi)) return -1;
-		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, true, 1)) return -1;
+		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, VT_DF, 1)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
 		for (int half = 0; half < 2; half++) {
 			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
@@ -2251,12 +2424,12 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			if (add_node(body, &n2, &n1, (void*) k_hsdf_update, P->grid, pa)) return -1;
 			SsorArgs sh = sa;
 			sh.cond_repl = a[half].cond_repl;
-			if (ssor && add_ssor(P, body, &n2, &n2, sh, true, 0)) return -1;
+			if (ssor && add_ssor(P, body, &n2, &n2, sh, VT_DF, 0)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			cudaGraphNode_t nf;
 			if (add_node(ifbody, &nf, nullptr, (void*) k_df_flush, P->grid, pa)) return -1;
 			if (add_node(ifbody, &nr, &nf, K.hsdfrepl, P->grid, pa)) return -1;
-			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, true, 1)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, VT_DF, 1)) return -1;
 			prev = nif;
 		}
 		cudaGraphNode_t n_fin, n_sw, n_loop2;
@@ -2270,7 +2443,7 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		SsorArgs sb = ssor_args(P, b[0].r, b[0].u);
 		sb.use_cond = 1;
 		sb.cond = b[0].cond;
-		if (ssor && add_ssor(P, g, &n_sw, &n_sw, sb, false, 1)) return -1;
+		if (ssor && add_ssor(P, g, &n_sw, &n_sw, sb, VT_F64, 1)) return -1;
 		cudaGraph_t body2;
 		if (add_conditional(g, &n_loop2, &n_sw, b[0].cond, cudaGraphCondTypeWhile, &body2)) return -1;
 		cudaGraphNode_t prev2 = nullptr;
@@ -2284,10 +2457,10 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			if (add_node(body2, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
 			SsorArgs sh = sb;
 			sh.cond_repl = b[half].cond_repl;
-			if (ssor && add_ssor(P, body2, &n2, &n2, sh, false, 0)) return -1;
+			if (ssor && add_ssor(P, body2, &n2, &n2, sh, VT_F64, 0)) return -1;
 			if (add_conditional(body2, &nif, &n2, b[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			if (add_node(ifbody, &nr, nullptr, K64.hs64repl, P->grid, pa)) return -1;
-			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, false, 1)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, VT_F64, 1)) return -1;
 			prev2 = nif;
 		}
 		void* pr[1] = {&b[0]};
@@ -2308,7 +2481,7 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 		sa.cond = h;
 		void* pi[2] = {&a[0], &imixed};
 		if (add_node(g, &n_init, nullptr, (void*) k_cg_init<double>, P->grid, pi)) return -1;
-		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, false, 1)) return -1;
+		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, VT_F64, 1)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
 		for (int half = 0; half < 2; half++) {
 			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
@@ -2324,25 +2497,33 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			if (add_node(body, &n2, &n1, (void*) k_hs64_update, P->grid, pa)) return -1;
 			SsorArgs sh = sa;
 			sh.cond_repl = a[half].cond_repl;
-			if (ssor && add_ssor(P, body, &n2, &n2, sh, false, 0)) return -1;
+			if (ssor && add_ssor(P, body, &n2, &n2, sh, VT_F64, 0)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			if (add_node(ifbody, &nr, nullptr, K.hs64repl, P->grid, pa)) return -1;
-			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, false, 1)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, VT_F64, 1)) return -1;
 			prev = nif;
 		}
 		void* pa[1] = {&a[0]};
 		if (add_node(g, &n_res, &n_loop, K.res64, P->grid, pa)) return -1;
 	}
 	else {
+		// mixed: FP32 operator and vectors, FP64 dots; each replacement is an
+		// FP64 iterative-refinement step (x += dx, r = b - A x in FP64)
+		bool const ssor = ssor_pc(P->precond);
 		CgArgs<float> a[2];
 		a[0] = cg_args<float>(P, o);
 		a[0].use_cond = 1;
 		a[0].cond = h;
+		a[0].no_pc = ssor;
 		a[1] = a[0];
 		a[1].p = a[0].pn;
 		a[1].pn = a[0].p;
+		SsorArgs sa = ssor_args(P, a[0].r, a[0].z);
+		sa.use_cond = 1;
+		sa.cond = h;
 		void* pi[2] = {&a[0], &imixed};
 		if (add_node(g, &n_init, nullptr, (void*) k_cg_init<float>, P->grid, pi)) return -1;
+		if (ssor && add_ssor(P, g, &n_init, &n_init, sa, VT_F32, 1)) return -1;
 		if (add_conditional(g, &n_loop, &n_init, h, cudaGraphCondTypeWhile, &body)) return -1;
 		for (int half = 0; half < 2; half++) {
 			CK(cudaGraphConditionalHandleCreate(&a[half].cond_repl, body, 0u, cudaGraphCondAssignDefault));
@@ -2351,10 +2532,14 @@ int build_graph(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 			cudaGraph_t ifbody;
 			if (add_node(body, &n1, prev ? &prev : nullptr, K.spmvmx, P->grid, pa)) return -1;
 			if (add_node(body, &n2, &n1, (void*) k_mx_update, P->grid, pa)) return -1;
+			SsorArgs sh = sa;
+			sh.cond_repl = a[half].cond_repl;
+			if (ssor && add_ssor(P, body, &n2, &n2, sh, VT_F32, 0)) return -1;
 			if (add_conditional(body, &nif, &n2, a[half].cond_repl, cudaGraphCondTypeIf, &ifbody)) return -1;
 			cudaGraphNode_t nf;
 			if (add_node(ifbody, &nf, nullptr, (void*) k_mx_flush, P->grid, pa)) return -1;
 			if (add_node(ifbody, &nr, &nf, K.replace, P->grid, pa)) return -1;
+			if (ssor && add_ssor(P, ifbody, &nr, &nr, sh, VT_F32, 1)) return -1;
 			prev = nif;
 		}
 		void* pa[1] = {&a[0]};
@@ -2454,14 +2639,14 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 	if (dalloc(&scratch, 1)) return -1;
 	cudaStream_t const st = P->stream;
 	CK(cudaMemsetAsync(scratch, 0, sizeof(CgState), st));
-	bool const df = P->precision == BFM_GPU_FP64_DF;
+	int const vt = precision_vt(P->precision);
 	SsorArgs base = ssor_args(P, P->vec[0], P->vec[1]);
 	base.st = scratch;
 	base.timing = 1;
 	int const nc = P->ncol > 0 ? P->ncol : 1;
 	cudaEvent_t e[2];
 	for (auto& x : e) cudaEventCreate(&x);
-	CoarseArgs ca = coarse_args(P, P->vec[0], df);
+	CoarseArgs ca = coarse_args(P, P->vec[0], vt);
 	ca.berr = &scratch->ssor_err;
 	bool const coarse = coarse_pc(P->precond) && P->coarse_ok;
 	if (coarse) {
@@ -2491,7 +2676,7 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 			a.first_acc = a.final_phase = 1;
 			void* pa[1] = {&a};
 			cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
-			cudaLaunchCooperativeKernel(df ? (void*) k_ssor_all<true> : (void*) k_ssor_all<false>, dim3(P->ssor_grid),
+			cudaLaunchCooperativeKernel(ssor_all_kernel(vt), dim3(P->ssor_grid),
 			                            dim3(TPB), pa, 0, st);
 			return;
 		}
@@ -2501,12 +2686,12 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 			int const c = forward ? ph : 2 * nc - 2 - ph;
 			a.lo = P->col_off[c];
 			a.hi_row = P->col_off[c + 1];
+			a.slice0 = P->sl_base[c];
 			a.fwd_last = forward && c == nc - 1;
 			a.first_acc = a.fwd_last;
 			a.final_phase = ph == 2 * nc - 2;
 			void* pa[1] = {&a};
-			cudaLaunchKernel(forward ? (df ? (void*) k_ssor_fwd<true> : (void*) k_ssor_fwd<false>)
-			                         : (df ? (void*) k_ssor_bwd<true> : (void*) k_ssor_bwd<false>),
+			cudaLaunchKernel(forward ? ssor_fwd_kernel(vt) : ssor_bwd_kernel(vt),
 			                 dim3(P->grid), dim3(TPB), pa, 0, st);
 		}
 	};
@@ -2580,6 +2765,7 @@ void bfm_gpu_default_opts(bfm_gpu_opts_t* o) {
 	o->deterministic = 1;
 	o->autotune = 1;
 	o->barrier_polls = 0;
+	o->refine_restart = 0;
 }
 
 int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n_elems, int n_edges, int n_conds, void* stream) {
@@ -2670,7 +2856,8 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y, P->ssor_d,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
-	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart};
+	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart,
+	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc};
 	for (void* q : lb)
 		if (q) cudaFree(q);
 	if (P->ext && P->ext_free) P->ext_free(P->ext);
@@ -2860,8 +3047,10 @@ int bfmi_mesh(bfm_gpu_problem_t* P, bfmi_mesh_t* o) {
 
 int bfmi_set_precond_blocks(bfm_gpu_problem_t* P, const double* blocks) {
 	if (!P->assembled) return fail("assemble before setting the preconditioner");
-	// FP64 SSOR sweeps read FP32 relaxation blocks: the double-float layout
-	int const layout = P->precision == BFM_GPU_FP64_DF || ssor_pc(P->precond) ? 2 : P->precision == BFM_GPU_FP64 ? 0 : 1;
+	// FP64 SSOR sweeps read FP32 relaxation blocks: the double-float layout;
+	// the mixed precisions keep FP32 blocks, 4 per node, for every preconditioner
+	int const layout = P->precision == BFM_GPU_FP64_DF || (ssor_pc(P->precond) && P->precision == BFM_GPU_FP64) ? 2
+	                   : P->precision == BFM_GPU_FP64 ? 0 : 1;
 	// without blocks: Jacobi, or block Jacobi as the SSOR relaxation blocks
 	k_store_blocks<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, blocks, P->row_ptr, P->cols,
 	                                                        P->precision != BFM_GPU_MIXED ? P->vals64 : nullptr, P->vals32,
@@ -2903,9 +3092,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	bool const dfp = precision == BFM_GPU_FP64_DF;
 	bool const want64 = precision != BFM_GPU_MIXED;  // FP64 values: the operator, or the residual operator
 	bool const want32 = precision != BFM_GPU_FP64;   // FP32 values: the mixed iteration operator / hi parts
-	// the preconditioner here is the last solve's: an SSOR one does not carry
-	// over to a precision without it (the next solve refuses SSOR there)
-	if (ssor_pc(P->precond) && precision != BFM_GPU_FP64 && !dfp) P->precond = BFM_GPU_PC_JACOBI;
+	// the preconditioner here is the last solve's (every precision has the SSOR ones)
 	bool const ssor = ssor_pc(P->precond);
 	bool const fp64_ssor = ssor && precision == BFM_GPU_FP64;  // FP32 blocks and relaxation blocks for the sweeps
 	cudaStream_t const st = P->stream;
@@ -2953,12 +3140,15 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 			// graph cannot hold a cooperative kernel node
 			char const* pcol = getenv("BFM_GPU_SSOR_PER_COLOUR");
 			if (pcol && pcol[0] == '1') coop = 0;
-			if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*) k_ssor_all<true>, TPB, 0) == cudaSuccess &&
+			if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ssor_all_kernel(VT_DF), TPB, 0) == cudaSuccess &&
 			    nb > 0) {
-				int nb64 = 0;
-				if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb64, (const void*) k_ssor_all<false>, TPB, 0) == cudaSuccess &&
-				    nb64 > 0 && nb64 < nb)
-					nb = nb64;
+				// one grid for every vector layout: the fewest resident blocks of the three
+				for (int vt : {VT_F64, VT_F32}) {
+					int nb2 = 0;
+					if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, ssor_all_kernel(vt), TPB, 0) == cudaSuccess &&
+					    nb2 > 0 && nb2 < nb)
+						nb = nb2;
+				}
 				P->ssor_grid = num_sms() * nb;
 			}
 			cudaGetLastError();
@@ -3090,11 +3280,25 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		k_edge_loads<<<blocks_for(N), TPB, 0, st>>>(P->N, P->ledges, P->lloads, P->lptr, P->llist, P->coords, P->last_ci, P->b);
 	}
 	CK(cudaGetLastError());
+	// SSOR: the sweeps' sliced-ELL blocks of this matrix
+	if (ssor && build_sell(P)) return -1;
 	// two-level SSOR: the coarse operator of this matrix
 	if (coarse_pc(P->precond) && coarse_setup(P)) return -1;
 	CK(cudaEventRecord(P->ev[1], st));
 	P->assembled = true;
 	P->solved = false;
+	return 0;
+}
+
+// The sweeps' FP32 relaxation blocks, 16 bytes per node: the high halves of
+// the double-float blocks (FP64 and FP64_DF), or the mixed precisions' FP32
+// blocks as they are
+static int pack_relaxation_blocks(bfm_gpu_problem_t* P) {
+	if (mixed_prec(P->precision))
+		CK(cudaMemcpyAsync(P->ssor_d, P->dinv32, 16l * P->N, cudaMemcpyDeviceToDevice, P->stream));
+	else
+		k_pack_hi<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, reinterpret_cast<const float4*>(P->dinv32), P->ssor_d);
+	CK(cudaGetLastError());
 	return 0;
 }
 
@@ -3106,8 +3310,6 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	else bfm_gpu_default_opts(&o);
 	if (!(o.rtol >= 0.0) || o.max_iters < 0) return fail("invalid solver options");
 	if (o.precond < BFM_GPU_PC_JACOBI || o.precond > BFM_GPU_PC_LEARNED_SSOR2) return fail("unknown preconditioner %d", o.precond);
-	if (ssor_pc(o.precond) && P->precision != BFM_GPU_FP64 && P->precision != BFM_GPU_FP64_DF)
-		return fail("the SSOR preconditioners run on the FP64 and FP64_DF paths");
 	if (o.precond != P->precond) {
 		// the preconditioner is formed by the assembly epilogue
 		P->precond = o.precond;
@@ -3122,6 +3324,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	bool const same = P->graph && P->graph_precision == P->precision && P->graph_precond == P->precond &&
 	                  P->graph_lpr == P->lpr && P->graph_opts.rtol == o.rtol &&
 	                  P->graph_opts.max_iters == o.max_iters && P->graph_opts.replace_drop == o.replace_drop &&
+	                  P->graph_opts.refine_restart == o.refine_restart &&
 	                  P->polls == (o.barrier_polls > 0 ? (long) o.barrier_polls : BARRIER_POLLS_DEFAULT);
 	if (!same) {
 		P->polls = o.barrier_polls > 0 ? (long) o.barrier_polls : BARRIER_POLLS_DEFAULT;
@@ -3138,7 +3341,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	if (learned && bfmi_learned_precond(P, 0)) return -1;
 	if (ssor_pc(P->precond) && P->ssor_bar) {
 		CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
-		k_pack_hi<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, reinterpret_cast<const float4*>(P->dinv32), P->ssor_d);
+		if (pack_relaxation_blocks(P)) return -1;
 	}
 	CK(cudaGraphLaunch(P->graph, P->stream));
 	if (learned) {
@@ -3153,7 +3356,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
 			if (ssor_pc(P->precond) && P->ssor_bar) {
 				CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
-				k_pack_hi<<<blocks_for(P->N), TPB, 0, P->stream>>>(P->N, reinterpret_cast<const float4*>(P->dinv32), P->ssor_d);
+				if (pack_relaxation_blocks(P)) return -1;
 			}
 			CK(cudaGraphLaunch(P->graph, P->stream));
 			P->fallback = 1;

@@ -99,6 +99,13 @@ typedef struct {
 	                          after this many polls and the solve ends with
 	                          BFM_GPU_TIMEOUT instead of waiting forever;
 	                          0: the default, 2^24 (seconds)                  */
+	int refine_restart;    /* MIXED and MIXED_EXACT: every FP64 residual
+	                          replacement is an iterative-refinement step
+	                          (x += dx in FP64, r = b - A x in compensated
+	                          FP64).  0 (default): the inner FP32 PCG keeps its
+	                          search direction across it (reliable updates);
+	                          1: it restarts from the new residual (beta = 0),
+	                          the classic refinement loop                      */
 } bfm_gpu_opts_t;
 
 typedef struct {

@@ -161,12 +161,44 @@ def test_switching_back_restores_the_caller_order(problem):
     np.testing.assert_array_equal(prob.solution(), x1)
 
 
-def test_mixed_precision_is_refused(libbfm):
-    prob = LN.DeviceProblem(plate(32, 8), precision=bfm_gb300.MIXED)
+@pytest.mark.parametrize("precision,tol", [(bfm_gb300.MIXED_EXACT, 1e-6), (bfm_gb300.MIXED, 1e-4)])
+@pytest.mark.parametrize("precond", [bfm_gb300.PC_SSOR, bfm_gb300.PC_SSOR2])
+def test_mixed_ssor_matches_direct_oracle(libbfm, precision, tol, precond):
+    """The mixed precisions with the SSOR preconditioners: FP32 operator,
+    vectors and sweeps' input and output, FP64 dots; every FP64 residual
+    replacement is an iterative-refinement step (the inner PCG keeps its
+    direction by default).  MIXED_EXACT solves the FP64 system (error bound of
+    the refinement), MIXED its FP32-integrated one (error bound of the FP32
+    element integration); the iteration count stays within 30% of the FP64
+    solve with the same preconditioner."""
+    p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
+    ref = LN.DeviceProblem(p, precision=bfm_gb300.FP64)
+    prob = LN.DeviceProblem(p, precision=precision)
     try:
-        o = bfm_gb300.default_opts(precond=bfm_gb300.PC_SSOR)
-        assert libbfm.bfm_gpu_problem_solve(prob.P, C.byref(o)) == -1
-        assert "SSOR" in bfm_gb300.last_error()
+        s64 = ref.solve(precond=precond, rtol=1e-8)
+        s = prob.solve(precond=precond, rtol=1e-8, replace_drop=0.01)
+        assert s.status == 0 and s.rel_residual <= 1e-8, (s.status, s.rel_residual)
+        assert s.replacements >= 2  # refinement steps
+        x, _, _ = O.solve_direct(p)
+        assert rel(prob.solution(), x) < tol
+        assert s.iterations <= 1.3 * s64.iterations, (s.iterations, s64.iterations)
+    finally:
+        prob.close()
+        ref.close()
+
+
+def test_mixed_refinement_keeps_or_restarts(libbfm):
+    """refine_restart: 0 keeps the inner PCG's direction across refinement
+    steps, 1 restarts it; both reach the solution of the FP64 system."""
+    p = M.cfg_perforated(nx=192, ny=48, n_holes=100, seed=6)
+    prob = LN.DeviceProblem(p, precision=bfm_gb300.MIXED_EXACT)
+    try:
+        x, _, _ = O.solve_direct(p)
+        for restart in (0, 1):
+            s = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-8, replace_drop=0.01, refine_restart=restart)
+            print(f"refine_restart {restart}: {s.iterations} iterations, {s.replacements} refinement steps")
+            assert s.status == 0 and s.replacements >= 2
+            assert rel(prob.solution(), x) < 1e-6
     finally:
         prob.close()
 
