@@ -1375,6 +1375,42 @@ __global__ void __launch_bounds__(TPB_K) k_df_switch(CgArgs<double> a, const flo
 // their (r, z) to the state; the last phase turns the sum into beta and
 // gamma (after an update) or gamma (after a replacement).
 
+struct CoarseArgs {
+	int na, nc;               // aggregates (cells), coarse DOFs (3 na)
+	int gx, gy, xfast;        // cell grid; cell (cx, cy) is cx + gx cy when xfast, else cy + gy cx
+	int bw;                   // half-bandwidth of A_c
+	const int* agg_ptr;       // nodes of aggregate I: agg_nodes[agg_ptr[I] .. agg_ptr[I + 1]), ascending
+	const int* agg_nodes;
+	const int* agg;
+	const float4* pnode;
+	float2* band;             // A_c, then L in place (double-float pairs): entry (i, i - t) at band[i (bw + 1) + t], 1 / L_ii on the diagonal
+	double* diag0;            // A_c's diagonal (the pivot test)
+	float* xl;                // X = L^-1 by rows: row i (columns 0..i) at xrow(i), rows padded to 4 floats
+	float* xu;                // X^T by rows: row j (columns j..nc-1) at xrow(nc - 1 - j)
+	float2* rc;               // P^T r          (double-float pairs, 4 zero pads after the last)
+	float2* yt;               // X rc           (the same)
+	float2* yc;               // X^T X rc
+	const void* r;
+	int df;                   // layout of r: VT_F64 (double2 per node), VT_DF (float4) or VT_F32 (float2)
+	const int* row_ptr;
+	const int* cols;
+	const double* vals64;     // the operator A_c is formed from: FP64 blocks, or (nullptr)
+	const float* vals32;      // the FP32 blocks in difference form with the row-sum blocks
+	const float* corr32;      // corr32 (the MIXED precision)
+	int* err;
+	unsigned* bar;       // grid barrier words of the one-launch form (k_coarse_apply)
+	int* berr;           // its timeout flag
+	long polls;          // polls per grid barrier before it gives up
+	// chunks of at most COARSE_CHUNK nodes of one aggregate: chunk q covers
+	// agg_nodes[chunk_start[q] .. chunk_start[q + 1]) of aggregate chunk_agg[q];
+	// the chunks of aggregate I are [agg_chunk[I], agg_chunk[I + 1])
+	int nchunk;
+	const int* chunk_start;
+	const int* chunk_agg;
+	const int* agg_chunk;
+	double* part;        // per chunk: 3 (restriction) or 81 (coarse matrix) partial sums
+};
+
 struct SsorArgs {
 	const int* row_ptr;
 	const int* cols;
@@ -1418,6 +1454,12 @@ struct SsorArgs {
 	const int* up;
 	int slice0;          // per-phase kernels: first slice of this phase's colour
 	int sbase[65];       // persistent kernel: first slice of colour c
+	// persistent kernel, at least 3 colours: the coarse correction's four
+	// stages run inside the sweep phases (restriction, chunk sums, X rc, X^T yt
+	// in phases 0-3, between the sweeps' own grid barriers); the rows
+	// finished before the last phase get their P yc term in the last one
+	int fuse;
+	CoarseArgs co;
 };
 
 
@@ -1529,6 +1571,40 @@ __device__ __forceinline__ void ssor_st_z(const SsorArgs& a, int i, dfl z0, dfl 
 		st2((double*) a.z, i, w0, w1);
 		acc64 += q0 * w0 + q1 * w1;
 	}
+}
+
+// store z without the coarse term (fused two-level form, before yc exists)
+template <int VT>
+__device__ __forceinline__ void ssor_st_plain(const SsorArgs& a, int i, dfl z0, dfl z1) {
+	if constexpr (VT == VT_DF) df_st((float*) a.z, i, z0, z1);
+	else if constexpr (VT == VT_F32) st2((float*) a.z, i, __fadd_rn(z0.hi, z0.lo), __fadd_rn(z1.hi, z1.lo));
+	else st2((double*) a.z, i, df_dbl(z0), df_dbl(z1));
+}
+
+// z_i += (P yc)_i for a row stored by ssor_st_plain, and its (r, z)
+template <int VT>
+__device__ __forceinline__ void ssor_add_coarse(const SsorArgs& a, int i, dfl& acc, double& acc64) {
+	// z was stored by other blocks in an earlier phase: read it from L2
+	dfl z0, z1;
+	if constexpr (VT == VT_DF) {
+		float4 const t = __ldcg(reinterpret_cast<const float4*>(a.z) + i);
+		z0 = {t.x, t.z};
+		z1 = {t.y, t.w};
+	}
+	else if constexpr (VT == VT_F32) {
+		float2 const t = __ldcg(reinterpret_cast<const float2*>(a.z) + i);
+		z0 = {t.x, 0.f};
+		z1 = {t.y, 0.f};
+	}
+	else {
+		double2 const t = __ldcg(reinterpret_cast<const double2*>(a.z) + i);
+		z0 = df_make(t.x);
+		z1 = df_make(t.y);
+	}
+	dfl r0, r1;
+	double q0 = 0.0, q1 = 0.0;
+	ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+	ssor_st_z<VT>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
 }
 
 __device__ __forceinline__ void ssor_finish(const SsorArgs& a, double part) {
@@ -1679,52 +1755,6 @@ __device__ bool grid_barrier(unsigned* bar, int* err, long polls) {
 
 __device__ __forceinline__ bool ssor_barrier(const SsorArgs& a) { return grid_barrier(a.bar, &a.st->ssor_err, a.polls); }
 
-template <int VT>
-__global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
-	if (a.st->done && !a.timing) return;
-	grid_barrier_init(a.bar);
-	int const nc = a.ncol > 0 ? a.ncol : 1;
-	dfl acc = {0.f, 0.f};
-	double acc64 = 0.0;
-	bool alive = true;
-	int const stride = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
-	for (int ph = 0; ph < 2 * nc - 1 && alive; ph++) {
-		bool const forward = ph < nc;
-		int const c = forward ? ph : 2 * nc - 2 - ph;
-		bool const final_rows = !forward || c == nc - 1;
-		int const lo = a.off[c], hi = a.off[c + 1];
-		for (int i = lo + tid; i < hi; i += stride) {
-			dfl r0, r1;
-			double q0 = 0.0, q1 = 0.0;
-			dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
-			float4 const d = reinterpret_cast<const float4*>(a.dinv)[i];
-			dfl z0, z1;
-			int const sl = a.sbase[c] + ((i - lo) >> 5), lane = (i - lo) & 31;
-			if (forward) {
-				ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
-				sell_row(a.lv, a.lc, a.lp, sl, lane, a.y, t0, t1);
-				ssor_blk(d, df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), z0, z1);
-			}
-			else {
-				sell_row(a.uv, a.uc, a.up, sl, lane, a.y, t0, t1);
-				dfl w0, w1;
-				ssor_blk(d, t0, t1, w0, w1);
-				float4 const yv = __ldcg(reinterpret_cast<const float4*>(a.y) + i);
-				z0 = df_add({yv.x, yv.z}, df_neg(w0));
-				z1 = df_add({yv.y, yv.w}, df_neg(w1));
-				ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
-			}
-			__stcg(reinterpret_cast<float4*>(a.y) + i, make_float4(z0.hi, z1.hi, z0.lo, z1.lo));
-			if (final_rows) ssor_st_z<VT>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
-		}
-		if (ph < 2 * nc - 2) alive = ssor_barrier(a);
-	}
-	// every block reaches the reduction, finished or not
-	double v[1] = {VT == VT_F64 ? acc64 : df_dbl(acc)};
-	double out[1];
-	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
-}
-
 // ---------------------------------------------------------------- coarse space (two-level SSOR)
 // M^-1 = M_SSOR^-1 + P A_c^-1 P^T, A_c = P^T A P: one aggregate per cell of a
 // grid laid over the mesh's bounding box, three coarse DOFs per aggregate
@@ -1738,41 +1768,6 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 // whatever the rounding of X.  The sweeps add P yc to z when they store it,
 // so the recursion itself stays M_SSOR^-1.
 
-struct CoarseArgs {
-	int na, nc;               // aggregates (cells), coarse DOFs (3 na)
-	int gx, gy, xfast;        // cell grid; cell (cx, cy) is cx + gx cy when xfast, else cy + gy cx
-	int bw;                   // half-bandwidth of A_c
-	const int* agg_ptr;       // nodes of aggregate I: agg_nodes[agg_ptr[I] .. agg_ptr[I + 1]), ascending
-	const int* agg_nodes;
-	const int* agg;
-	const float4* pnode;
-	float2* band;             // A_c, then L in place (double-float pairs): entry (i, i - t) at band[i (bw + 1) + t], 1 / L_ii on the diagonal
-	double* diag0;            // A_c's diagonal (the pivot test)
-	float* xl;                // X = L^-1 by rows: row i (columns 0..i) at xrow(i), rows padded to 4 floats
-	float* xu;                // X^T by rows: row j (columns j..nc-1) at xrow(nc - 1 - j)
-	float2* rc;               // P^T r          (double-float pairs, 4 zero pads after the last)
-	float2* yt;               // X rc           (the same)
-	float2* yc;               // X^T X rc
-	const void* r;
-	int df;                   // layout of r: VT_F64 (double2 per node), VT_DF (float4) or VT_F32 (float2)
-	const int* row_ptr;
-	const int* cols;
-	const double* vals64;     // the operator A_c is formed from: FP64 blocks, or (nullptr)
-	const float* vals32;      // the FP32 blocks in difference form with the row-sum blocks
-	const float* corr32;      // corr32 (the MIXED precision)
-	int* err;
-	unsigned* bar;       // grid barrier words of the one-launch form (k_coarse_apply)
-	int* berr;           // its timeout flag
-	long polls;          // polls per grid barrier before it gives up
-	// chunks of at most COARSE_CHUNK nodes of one aggregate: chunk q covers
-	// agg_nodes[chunk_start[q] .. chunk_start[q + 1]) of aggregate chunk_agg[q];
-	// the chunks of aggregate I are [agg_chunk[I], agg_chunk[I + 1])
-	int nchunk;
-	const int* chunk_start;
-	const int* chunk_agg;
-	const int* agg_chunk;
-	double* part;        // per chunk: 3 (restriction) or 81 (coarse matrix) partial sums
-};
 
 constexpr int COARSE_CHUNK = 128;
 constexpr int COARSE_MAX_BW = 101;  // widest band: the factorisation's shared window and the solve's registers
@@ -1897,6 +1892,45 @@ __device__ __forceinline__ void restrict_chunk(const CoarseArgs& a, int q, int l
 	}
 }
 
+// restrict_chunk with one node in flight per lane (for a kernel with few
+// registers): the same sums in the same order
+__device__ __forceinline__ void restrict_chunk_lean(const CoarseArgs& a, int q, int lane) {
+	int const k0 = a.chunk_start[q], k1 = a.chunk_start[q + 1];
+	dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+	for (int k = k0 + lane; k < k1; k += 32) {
+		int const i = a.agg_nodes[k];
+		dfl r0, r1;
+		if (a.df == VT_DF) df_ld((const float*) a.r, i, r0, r1);
+		else if (a.df == VT_F32) {
+			float2 const t = ld2((const float*) a.r, i);
+			r0 = {t.x, 0.f};
+			r1 = {t.y, 0.f};
+		}
+		else {
+			double2 const t = ld2((const double*) a.r, i);
+			r0 = df_make(t.x);
+			r1 = df_make(t.y);
+		}
+		float4 const pq = a.pnode[i];
+		dfl const x0 = pq.z == 0.f ? dfl{0.f, 0.f} : r0;
+		dfl const x1 = pq.w == 0.f ? dfl{0.f, 0.f} : r1;
+		s0 = df_add(s0, x0);
+		s1 = df_add(s1, x1);
+		s2 = df_add(s2, df_add(df_mul_f(-pq.y, x0), df_mul_f(pq.x, x1)));
+	}
+#pragma unroll
+	for (int o = 16; o; o >>= 1) {
+		s0 = df_add(s0, {__shfl_xor_sync(0xffffffffu, s0.hi, o), __shfl_xor_sync(0xffffffffu, s0.lo, o)});
+		s1 = df_add(s1, {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)});
+		s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
+	}
+	if (lane == 0) {
+		a.part[3l * q] = df_dbl(s0);
+		a.part[3l * q + 1] = df_dbl(s1);
+		a.part[3l * q + 2] = df_dbl(s2);
+	}
+}
+
 __device__ __forceinline__ void restrict_sum_one(const CoarseArgs& a, int t) {
 	int const I = t / 3, m = t % 3;
 	double v = 0.0;
@@ -1921,8 +1955,8 @@ constexpr int CX_T = 256;  // threads per row of the coarse products
 // thread t takes the 16-byte groups t, t + CX_T, .. (loads first, then
 // double-float products and sums), then a fixed shuffle tree per warp and
 // the warps' sums in order (deterministic); the result in thread 0
+template <int U = 4>  // groups per thread in flight
 __device__ __forceinline__ dfl coarse_row_dot(const float* __restrict__ row, int len, const float2* __restrict__ v) {
-	constexpr int U = 4;  // groups per thread in flight
 	__shared__ float2 ws[CX_T / 32];
 	int const tx = threadIdx.x, lane = tx & 31, w = tx >> 5;
 	dfl s = {0.f, 0.f};
@@ -1997,6 +2031,83 @@ __global__ void __launch_bounds__(CX_T) k_coarse_apply(CoarseArgs a) {
 		if (threadIdx.x == 0) a.yc[j] = make_float2(s.hi, s.lo);
 		__syncthreads();
 	}
+}
+
+template <int VT>
+__global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
+	if (a.st->done && !a.timing) return;
+	grid_barrier_init(a.bar);
+	int const nc = a.ncol > 0 ? a.ncol : 1;
+	dfl acc = {0.f, 0.f};
+	double acc64 = 0.0;
+	bool alive = true;
+	int const stride = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+	bool const fuse = a.fuse && nc >= 3;
+	for (int ph = 0; ph < 2 * nc - 1 && alive; ph++) {
+		bool const forward = ph < nc;
+		bool const last = ph == 2 * nc - 2;
+		int const c = forward ? ph : 2 * nc - 2 - ph;
+		bool const final_rows = !forward || c == nc - 1;
+		int const lo = a.off[c], hi = a.off[c + 1];
+		for (int i = lo + tid; i < hi; i += stride) {
+			dfl r0, r1;
+			double q0 = 0.0, q1 = 0.0;
+			dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
+			float4 const d = reinterpret_cast<const float4*>(a.dinv)[i];
+			dfl z0, z1;
+			int const sl = a.sbase[c] + ((i - lo) >> 5), lane = (i - lo) & 31;
+			if (forward) {
+				ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+				sell_row(a.lv, a.lc, a.lp, sl, lane, a.y, t0, t1);
+				ssor_blk(d, df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), z0, z1);
+			}
+			else {
+				sell_row(a.uv, a.uc, a.up, sl, lane, a.y, t0, t1);
+				dfl w0, w1;
+				ssor_blk(d, t0, t1, w0, w1);
+				float4 const yv = __ldcg(reinterpret_cast<const float4*>(a.y) + i);
+				z0 = df_add({yv.x, yv.z}, df_neg(w0));
+				z1 = df_add({yv.y, yv.w}, df_neg(w1));
+				ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+			}
+			__stcg(reinterpret_cast<float4*>(a.y) + i, make_float4(z0.hi, z1.hi, z0.lo, z1.lo));
+			if (final_rows) {
+				if (fuse && !last) ssor_st_plain<VT>(a, i, z0, z1);
+				else ssor_st_z<VT>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
+			}
+		}
+		if (fuse) {
+			CoarseArgs const& co = a.co;
+			if (ph == 0) {  // r_c = P^T r: chunk partial sums, a warp per chunk
+				int const nw = stride >> 5, wid = tid >> 5;
+				for (int q = wid; q < co.nchunk; q += nw) restrict_chunk_lean(co, q, threadIdx.x & 31);
+			}
+			else if (ph == 1) {  // the chunks of each coarse DOF, in order
+				for (int t = tid; t < co.nc; t += stride) restrict_sum_one(co, t);
+			}
+			else if (ph == 2) {  // y_t = X r_c, a block per row
+				for (int i = blockIdx.x; i < co.nc; i += gridDim.x) {
+					dfl const s = coarse_row_dot<1>(co.xl + xrow(i), i + 1, co.rc);
+					if (threadIdx.x == 0) co.yt[i] = make_float2(s.hi, s.lo);
+					__syncthreads();
+				}
+			}
+			else if (ph == 3) {  // y_c = X^T y_t
+				for (int j = blockIdx.x; j < co.nc; j += gridDim.x) {
+					dfl const s = coarse_row_dot<1>(co.xu + xrow(co.nc - 1 - j), co.nc - j, co.yt + j);
+					if (threadIdx.x == 0) co.yc[j] = make_float2(s.hi, s.lo);
+					__syncthreads();
+				}
+			}
+			if (last)  // the rows finished before y_c existed: every colour but colour 0
+				for (int i = a.off[1] + tid; i < a.off[nc]; i += stride) ssor_add_coarse<VT>(a, i, acc, acc64);
+		}
+		if (!last) alive = ssor_barrier(a);
+	}
+	// every block reaches the reduction, finished or not
+	double v[1] = {VT == VT_F64 ? acc64 : df_dbl(acc)};
+	double out[1];
+	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
 }
 
 // A_c = P^T A P in two deterministic stages.  One warp per chunk of

@@ -2270,6 +2270,14 @@ SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
 	return a;
 }
 
+// The two-level correction inside the persistent sweep kernel: at least three
+// colours (its four stages need the sweeps' first four grid barriers);
+// BFM_GPU_COARSE_SEPARATE=1 keeps it in a launch of its own
+bool fuse_coarse(bfm_gpu_problem* P) {
+	char const* e = getenv("BFM_GPU_COARSE_SEPARATE");
+	return P->ssor_grid > 0 && P->ncol >= 3 && !(e && e[0] == '1');
+}
+
 // the sweep kernels of a vector layout (VT_*)
 void* ssor_all_kernel(int vt) {
 	return vt == VT_DF ? (void*) k_ssor_all<VT_DF> : vt == VT_F32 ? (void*) k_ssor_all<VT_F32> : (void*) k_ssor_all<VT_F64>;
@@ -2286,7 +2294,15 @@ void* ssor_bwd_kernel(int vt) {
 int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cudaGraphNode_t* dep, SsorArgs base, int vt,
              int mode) {
 	int const nc = P->ncol > 0 ? P->ncol : 1;
-	if (coarse_pc(P->precond) && P->coarse_ok) {
+	if (coarse_pc(P->precond) && P->coarse_ok && fuse_coarse(P)) {
+		// two-level, fused: the persistent sweep kernel runs the coarse stages
+		base.fuse = 1;
+		base.co = coarse_args(P, base.r, vt);
+		base.agg = P->agg;
+		base.pnode = P->pnode;
+		base.yc = P->yc;
+	}
+	else if (coarse_pc(P->precond) && P->coarse_ok) {
 		// two-level: yc = A_c^-1 P^T r first; the sweeps add P yc to z
 		CoarseArgs ca = coarse_args(P, base.r, vt);
 		void* pc[1] = {&ca};
@@ -2342,9 +2358,15 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 			return 0;
 		}
 		// no cooperative kernel nodes here: the per-phase kernels instead
+		// (and the coarse correction in kernels of its own)
 		cudaGetLastError();
 		cudaGraphDestroyNode(n);
 		P->ssor_grid = 0;
+		if (base.fuse) {
+			base.fuse = 0;
+			base.yc = nullptr;
+			return add_ssor(P, g, last, dep, base, vt, mode);
+		}
 	}
 	void* fwd = ssor_fwd_kernel(vt);
 	void* bwd = ssor_bwd_kernel(vt);
@@ -2654,8 +2676,9 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 		base.pnode = P->pnode;
 		base.yc = P->yc;
 	}
+	bool const fused = coarse && fuse_coarse(P);
 	auto once = [&](bool with_coarse) {
-		if (coarse && with_coarse) {
+		if (coarse && with_coarse && !fused) {
 			if (P->ssor_grid > 0 && coarse_apply_grid(P) > 0) {
 				void* pa[1] = {&ca};
 				cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
@@ -2674,6 +2697,10 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 			for (int c = 0; c <= nc && c < 65; c++) a.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
 			a.bar = P->ssor_bar;
 			a.first_acc = a.final_phase = 1;
+			if (fused && with_coarse) {
+				a.fuse = 1;
+				a.co = ca;
+			}
 			void* pa[1] = {&a};
 			cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
 			cudaLaunchCooperativeKernel(ssor_all_kernel(vt), dim3(P->ssor_grid),
