@@ -12,9 +12,11 @@ clamped, gravity, 1e6 Pa traction on the right edge, plane stress.  One step
 host buffers: host->device upload of the mesh and conditions and
 device->host copy of the displacements are inside its timed region.
 
-Every method (precision x preconditioner, METHODS) is timed; the line reports
-the fastest one whose displacements agree with the FP64 solution to 1e-6, and
-`methods` lists them all.  `roofline` describes the dominant kernel of that
+Every default method (precision x preconditioner, bfm_gb300.methods) runs a
+short selection pass (3 warm-up + 3 timed steps); the fastest one whose
+displacements agree with a direct (SuperLU) solve of the FP64 system to 1e-6
+is then timed with the requested W + K steps and reported, and `methods`
+lists them all with their own step counts.  `roofline` describes the dominant kernel of that
 method's iteration (the SSOR sweep kernel for the SSOR methods, with the SpMV in
 `roofline_spmv`; the SpMV otherwise).
 
@@ -46,19 +48,14 @@ sys.path.insert(0, str(ROOT))
 METRIC = "solve ms to 1e-8 residual: learned+mixed PCG vs plain FP64 PCG; SpMV HBM GB/s"
 RTOL = 1e-8
 
-# solve methods: precision and preconditioner of bfm_gpu_problem_solve
-METHODS = {"fp64": ("FP64", "PC_JACOBI"), "fp64_df": ("FP64_DF", "PC_JACOBI"),
-           "mixed_exact": ("MIXED_EXACT", "PC_JACOBI"), "mixed": ("MIXED", "PC_JACOBI"),
-           "learned_fp64": ("FP64", "PC_LEARNED"), "learned_df": ("FP64_DF", "PC_LEARNED"),
-           "learned_mixed": ("MIXED", "PC_LEARNED"), "ssor_fp64": ("FP64", "PC_SSOR"),
-           "ssor_df": ("FP64_DF", "PC_SSOR"), "learned_ssor_df": ("FP64_DF", "PC_LEARNED_SSOR"),
-           "ssor2_fp64": ("FP64", "PC_SSOR2"), "ssor2_df": ("FP64_DF", "PC_SSOR2"),
-           "learned_ssor2_df": ("FP64_DF", "PC_LEARNED_SSOR2")}
-# FP64 residual-replacement threshold per precision (the recurrence residual
-# must drop by this factor between replacements), from a sweep on the
-# 2048x512 perforated plate: FP64 is insensitive, the FP32-pipe paths converge
-# in fewer iterations with rarer replacements
-REPLACE_DROP = {"FP64": 0.1, "FP64_DF": 0.01, "MIXED_EXACT": 0.001, "MIXED": 0.001}
+# methods timed by default (the bfm_gb300.methods table has them all): the
+# plain FP64 Jacobi-PCG baseline, the benchmark spec's mixed precision with the
+# learned preconditioner, and the fast preconditioners in every precision
+DEFAULT_METHODS = ("fp64", "fp64_df", "mixed", "learned_mixed", "learned_df", "ssor_df", "ssor2_fp64", "ssor2_df",
+                   "learned_ssor2_df", "ssor2_mixed", "learned_ssor2_mixed")
+SELECT_STEPS = 3  # timed steps per method in the selection pass (after 3 warm-up steps)
+SSOR_PCS = (3, 4, 5, 6)      # BFM_GPU_PC_SSOR, _LEARNED_SSOR, _SSOR2, _LEARNED_SSOR2
+LEARNED_PCS = (2, 4, 6)
 # fused SpMV kernel (K1) of each precision: the roofline kernel
 SPMV_KERNEL = {0: "k_hs64_spmv", 1: "k_mx_spmv", 2: "k_mx_spmv", 3: "k_hsdf_spmv"}
 # DRAM bytes (read + write) of one K1 launch on the 2048x512 perforated plate,
@@ -67,16 +64,19 @@ SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md")
                 3: (329_563_136, "profiles/spmv_df_hs_perforated_2048x512.md"),
                 1: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md"),
                 2: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md")}
-# the same for one launch of the SSOR sweep kernel (double-float vectors)
-SSOR_TRAFFIC = (327_798_272, "profiles/ssor_sweeps_perforated_2048x512.md")
+# the same for one launch of the SSOR sweep kernel, per precision (vector
+# layout), where a capture of the current kernel exists
+SSOR_TRAFFIC = {}
 
 
-def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int) -> int:
-    """One SSOR application: every off-diagonal block once (FP32 block + column
-    index, 20 B), and per node the row bounds and diagonal position (12 B), the
-    FP32 relaxation block (16 B), the residual in (16 B), z out (16 B) and the
-    sweep vector written once (12 B of its 16 B counted: 72 B in all)."""
-    return (n_blocks - n_nodes) * 20 + n_nodes * 72
+def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int, precision: int) -> int:
+    """One SSOR application: every off-diagonal block once (FP32 block +
+    column index, 20 B), and per node the FP32 relaxation block (16 B), the
+    residual read and z written (16 B each for FP64 and double-float, 8 B for
+    the mixed precisions' FP32 vectors) and the double-float sweep vector
+    written once (16 B)."""
+    vec = 8 if precision in (1, 2) else 16
+    return (n_blocks - n_nodes) * 20 + n_nodes * (16 + 2 * vec + 16)
 
 
 def max_over_ranks(x: float, world: int) -> float:
@@ -159,36 +159,6 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def device_problem(lib, p, stream):
-    """Upload a Problem once (outside the timed region)."""
-    from bfm_gb300 import meshgen as M
-    P = C.c_void_p()
-    n_edges = 0 if p.edges is None else len(p.edges)
-    rc = lib.bfm_gpu_problem_create(C.byref(P), p.kind, p.n_nodes, p.n_elems, n_edges, len(p.conds), stream)
-    assert rc == 0, lib.bfm_gpu_last_error()
-    keep = []
-
-    def a(x, dt):
-        x = np.ascontiguousarray(x, dtype=dt)
-        keep.append(x)
-        return x.ctypes.data
-
-    assert lib.bfm_gpu_problem_set_geometry(P, a(p.coords, np.float64), a(p.elems, np.int32), 0) == 0
-    assert lib.bfm_gpu_problem_set_material(P, p.E, p.nu, p.rho, int(p.stress),
-                                            None if p.elem_E is None else a(p.elem_E, np.float64), None, 0) == 0
-    w, ph, dx, de = M.gauss_tables(p.kind)
-    assert lib.bfm_gpu_problem_set_rule(P, len(w), a(w, np.float64), a(ph, np.float64), a(dx, np.float64),
-                                        a(de, np.float64)) == 0
-    f = np.array(p.forces, np.float64).reshape(-1)
-    assert lib.bfm_gpu_problem_set_forces(P, len(p.forces), a(f, np.float64) if len(f) else None, None, 0) == 0
-    kinds = a([c[0] for c in p.conds], np.int32)
-    vals = a([c[1] for c in p.conds], np.float64)
-    masks = a(np.stack([c[2] for c in p.conds]).astype(np.uint8), np.uint8)
-    edges = a(p.edges, np.int32) if p.edges is not None else None
-    assert lib.bfm_gpu_problem_set_conditions(P, len(p.conds), kinds, vals, masks, n_edges, edges, 0) == 0
-    return P, keep
-
-
 def algorithmic_bytes_spmv(n_blocks: int, n_nodes: int, precision: int, block_pc: bool = False) -> int:
     """Bytes one launch of the fused SpMV kernel (K1: direction update, A p,
     (p, A p)) must move at least: block values + column indices + row
@@ -201,10 +171,92 @@ def algorithmic_bytes_spmv(n_blocks: int, n_nodes: int, precision: int, block_pc
     return n_blocks * (16 + 4) + 4 * (n_nodes + 1) + n_nodes * (8 + 8 + (16 if block_pc else 8) + 16 + 8 + 8)
 
 
+def direct_solution(lib, D, p):
+    """Displacements of a direct (SuperLU) solve of the FP64 system the GPU
+    assembles, refined once with an extended-precision residual: the yardstick
+    of every method's displacement error.  The FP64 system is bit-identical
+    to the oracle's restatement of the reference assembly (the slow config
+    tests check that at this size)."""
+    import scipy.sparse.linalg as spla
+    import bfm_gb300
+    from bfm_gb300 import api
+    D.assemble(bfm_gb300.FP64)
+    rp, cols, vals, b = D.download()
+    perm = np.zeros(p.n_nodes, np.int32)
+    assert lib.bfm_gpu_problem_ordering(D.P, perm.ctypes.data, None, None) == 0
+    K = api.scalar_csr(rp, cols, vals.reshape(-1), p.n_nodes, perm)
+    bb = np.empty_like(b)
+    bb[np.stack([2 * perm, 2 * perm + 1], 1).ravel()] = b
+    t0 = time.perf_counter()
+    lu = spla.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A", options=dict(SymmetricMode=True))
+    x = lu.solve(bb)
+    KL = K.astype(np.longdouble)
+    r = bb.astype(np.longdouble) - KL @ x.astype(np.longdouble)
+    x = (x.astype(np.longdouble) + lu.solve(r.astype(np.float64))).astype(np.float64)
+    return x, time.perf_counter() - t0
+
+
+def time_method(lib, D, stream, m, nets, warmup, steps, clocks=False):
+    """W untimed + K timed steps of method m (assembly + solve, inputs in
+    HBM), CUDA events on the problem's stream; then its statistics, solution
+    and per-kernel durations."""
+    import torch
+    import bfm_gb300
+    from bfm_gb300.methods import METHODS, opts
+    prec, pc, _ = METHODS[m]
+    if pc in nets:
+        nets[pc].use()
+    o = opts(m, RTOL)
+
+    def step():
+        assert lib.bfm_gpu_problem_assemble(D.P, prec) == 0, bfm_gb300.last_error()
+        assert lib.bfm_gpu_problem_solve(D.P, C.byref(o)) == 0, bfm_gb300.last_error()
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clk = Clocks(int(os.environ.get("LOCAL_RANK", 0))) if clocks else None
+    if clk:
+        clk.__enter__()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if clk:
+        clk.__exit__()
+    ms = ev0.elapsed_time(ev1) / steps
+    s = bfm_gb300.bfm_gpu_stats_t()
+    assert lib.bfm_gpu_problem_stats(D.P, C.byref(s)) == 0
+    x = D.solution()
+    # per-kernel durations for the roofline (same stream, CUDA events)
+    t_spmv, t_upd = C.c_double(), C.c_double()
+    assert lib.bfm_gpu_problem_time_kernels(D.P, 50, C.byref(t_spmv), C.byref(t_upd)) == 0
+    shape = C.c_int()
+    lib.bfm_gpu_problem_shape(D.P, C.byref(shape))
+    ncol = C.c_int(0)
+    lib.bfm_gpu_problem_ordering(D.P, None, None, C.byref(ncol))
+    t_pc, t_sw, persist = C.c_double(0.0), C.c_double(0.0), C.c_int(0)
+    if pc in SSOR_PCS:
+        assert lib.bfm_gpu_problem_time_precond(D.P, 20, C.byref(t_pc), C.byref(t_sw), C.byref(persist)) == 0, \
+            bfm_gb300.last_error()
+    if pc in nets:
+        lib.bfm_gpu_mpnn_use(None)
+    return dict(ms=ms, steps=steps, warmup=warmup, iters=s.iterations, status=s.status, rel_res=s.rel_residual,
+                repl=s.replacements, ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks,
+                fallback=s.fallback, ms_spmv=t_spmv.value, ms_update=t_upd.value,
+                clocks=clk.summary() if clk else None, prec=prec, pc=pc, x=x, shape=shape.value, ncol=ncol.value,
+                ms_precond=t_pc.value, ms_sweeps=t_sw.value, persistent=persist.value)
+
+
 def run_gpu(args, rank: int, world: int):
     import torch
     import bfm_gb300
-    from bfm_gb300 import api
+    from bfm_gb300 import api, learned
+    from bfm_gb300.methods import METHODS, opts
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     lib = bfm_gb300.lib()
@@ -214,103 +266,67 @@ def run_gpu(args, rank: int, world: int):
     # would replace by a private one)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    methods = {k: (getattr(bfm_gb300, a), getattr(bfm_gb300, b)) for k, (a, b) in METHODS.items()}
     # the networks: block-Jacobi blocks, and SSOR relaxation blocks (each
     # trained in its own context)
-    from bfm_gb300 import learned
     nets = {pc: learned.Network(path=w) for pc, w in ((bfm_gb300.PC_LEARNED, learned.WEIGHTS),
                                                     (bfm_gb300.PC_LEARNED_SSOR, learned.WEIGHTS_SSOR)) if w.exists()}
     if bfm_gb300.PC_LEARNED_SSOR in nets:  # the relaxation blocks serve the two-level form too
         nets[bfm_gb300.PC_LEARNED_SSOR2] = nets[bfm_gb300.PC_LEARNED_SSOR]
-    if args.method == "best":
-        chosen = ["fp64", "fp64_df", "mixed_exact", "mixed", "ssor_fp64", "ssor_df", "ssor2_fp64", "ssor2_df"] + \
-            (["learned_fp64", "learned_df", "learned_mixed"] if bfm_gb300.PC_LEARNED in nets else []) + \
-            (["learned_ssor_df", "learned_ssor2_df"] if bfm_gb300.PC_LEARNED_SSOR in nets else [])
-    else:
-        chosen = args.method.split(",")
-        for m in chosen:
-            if methods[m][1] in (bfm_gb300.PC_LEARNED, bfm_gb300.PC_LEARNED_SSOR, bfm_gb300.PC_LEARNED_SSOR2) and \
-                    methods[m][1] not in nets:
-                raise SystemExit(f"the weights of {m} are missing: train them with python -m bfm_gb300.learned")
+    chosen = list(DEFAULT_METHODS) if args.method == "best" else args.method.split(",")
+    missing = [m for m in chosen if METHODS[m][1] in LEARNED_PCS and METHODS[m][1] not in nets]
+    if missing and args.method != "best":
+        raise SystemExit(f"the weights of {missing} are missing: train them with python -m bfm_gb300.learned")
+    chosen = [m for m in chosen if m not in missing]
+    D = learned.DeviceProblem(p, stream=stream.cuda_stream, precision=None)
+    x_direct, t_direct = (direct_solution(lib, D, p) if not args.no_direct else (None, 0.0))
+    # selection pass: a few steps of every method; then the fastest one whose
+    # displacements are within 1e-6 of the direct solve, W + K steps
     results = {}
-    P, keep = device_problem(lib, p, C.c_void_p(stream.cuda_stream))
+    single = len(chosen) == 1
     for m in chosen:
-        prec, pc = methods[m]
-        if pc in nets:
-            nets[pc].use()
-        o = bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc, replace_drop=REPLACE_DROP[METHODS[m][0]])
-
-        def step():
-            assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
-            assert lib.bfm_gpu_problem_solve(P, C.byref(o)) == 0, bfm_gb300.last_error()
-
-        for _ in range(args.warmup):
-            step()
-        torch.cuda.synchronize()
+        results[m] = time_method(lib, D, stream, m, nets, args.warmup if single else 3,
+                                 args.steps if single else min(args.steps, SELECT_STEPS), clocks=single)
+    for m, r in results.items():
+        r["err_vs_direct"] = None if x_direct is None else float(np.linalg.norm(r["x"] - x_direct) /
+                                                                   np.linalg.norm(x_direct))
+    ok = [m for m, r in results.items() if r["status"] == 0 and (r["err_vs_direct"] is None or r["err_vs_direct"] <= 1e-6)]
+    best = min(ok or results, key=lambda k: results[k]["ms"])
+    if not single:
         if world > 1:
             torch.distributed.barrier()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            for _ in range(args.steps):
-                step()
-            ev1.record(stream)
-            torch.cuda.synchronize()
-        ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world)
-        s = bfm_gb300.bfm_gpu_stats_t()
-        assert lib.bfm_gpu_problem_stats(P, C.byref(s)) == 0
-        x = np.zeros(p.n_dof)
-        lib.bfm_gpu_problem_solution(P, x.ctypes.data, 0)
-        # per-kernel durations for the roofline (same stream, CUDA events)
-        t_spmv, t_upd = C.c_double(), C.c_double()
-        assert lib.bfm_gpu_problem_time_kernels(P, 50, C.byref(t_spmv), C.byref(t_upd)) == 0
-        shape = C.c_int()
-        lib.bfm_gpu_problem_shape(P, C.byref(shape))
-        ncol = C.c_int(0)
-        lib.bfm_gpu_problem_ordering(P, None, None, C.byref(ncol))
-        t_pc, t_sw, persist = C.c_double(0.0), C.c_double(0.0), C.c_int(0)
-        if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR, bfm_gb300.PC_SSOR2, bfm_gb300.PC_LEARNED_SSOR2):
-            assert lib.bfm_gpu_problem_time_precond(P, 20, C.byref(t_pc), C.byref(t_sw), C.byref(persist)) == 0, \
-                bfm_gb300.last_error()
-        results[m] = dict(ms=ms, iters=s.iterations, status=s.status, rel_res=s.rel_residual, repl=s.replacements,
-                          ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks, fallback=s.fallback,
-                          ms_spmv=t_spmv.value, ms_update=t_upd.value, clocks=clk.summary(), prec=prec, pc=pc, x=x,
-                          shape=shape.value, ncol=ncol.value, ms_precond=t_pc.value, ms_sweeps=t_sw.value,
-                          persistent=persist.value)
-    lib.bfm_gpu_problem_destroy(P)
-    # displacement error of every method against the FP64 solution (the FP64
-    # direct oracle does not fit the host at this size; the FP64 PCG solution
-    # to 1e-8 stands in for it and is itself checked against the oracle in tests/)
-    ref = results.get("fp64", {}).get("x")
-    for m, r in results.items():
-        r["err_vs_fp64"] = None if ref is None else float(np.linalg.norm(r["x"] - ref) / np.linalg.norm(ref))
-    ok = [m for m, r in results.items() if r["status"] == 0 and (r["err_vs_fp64"] is None or r["err_vs_fp64"] <= 1e-6)]
-    best = min(ok or results, key=lambda k: results[k]["ms"])
+        err = results[best]["err_vs_direct"]
+        results[best] = time_method(lib, D, stream, best, nets, args.warmup, args.steps, clocks=True)
+        results[best]["err_vs_direct"] = err
+    D.close()
 
     # end-to-end through bfm_sim_run with host buffers (the learned methods use
-    # the network selected above through the same global options)
-    prec, pc = methods[best]
+    # the network selected above through the same global options); the first
+    # run on the mesh is cold: it colours it, forms the coarse grid and tunes
+    # the SpMV shape
+    prec, pc, _ = METHODS[best]
     if pc in nets:
         nets[pc].use()
-    lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts(rtol=RTOL, precision=prec, precond=pc,
-                                                        replace_drop=REPLACE_DROP[METHODS[best][0]])))
+    lib.bfm_gpu_set_opts(C.byref(opts(best, RTOL)))
     h = api.SimHandle.from_problem(lib, p)
-    assert h.run() == 0, h.error()  # warm: allocates the device problem once
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
+    assert h.run() == 0, h.error()
+    cold_ms = (time.perf_counter() - t0) * 1e3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n_e2e = max(1, args.steps // 2)
+    for _ in range(n_e2e):
         assert h.run() == 0, h.error()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / n_e2e
     n_masks = len(p.conds) * p.n_nodes
     h2d = p.n_nodes * 16 + p.n_elems * p.kind * 4 + n_masks + (0 if p.edges is None else 8 * len(p.edges)) + \
         (0 if p.elem_E is None else 8 * p.n_elems)
     d2h = p.n_dof * 8
     lib.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
+    lib.bfm_gpu_mpnn_use(None)
     for n_ in {id(v): v for v in nets.values()}.values():
         n_.close()
-    return p, results, best, dict(ms=e2e_ms, h2d=h2d, d2h=d2h)
+    return p, results, best, dict(ms=e2e_ms, cold_ms=cold_ms, h2d=h2d, d2h=d2h, steps=n_e2e), t_direct
 
 
 def run_batch(args, steps=3, warmup=1):
@@ -351,59 +367,60 @@ def run_batch(args, steps=3, warmup=1):
 
 def profile(args):
     """Assemble once, then the CG's SpMV+dots and update kernels as standalone
-    launches (the solve itself runs them inside a CUDA graph)."""
+    launches (the solve itself runs them inside a CUDA graph), the SSOR
+    preconditioner's applications and the network's inference where the
+    method has them."""
     import bfm_gb300
+    from bfm_gb300 import learned
+    from bfm_gb300.methods import METHODS
     lib = bfm_gb300.lib()
     p = workload(args.workload)
-    prec = getattr(bfm_gb300, METHODS.get(args.method, ("FP64", ""))[0])
-    P, keep = device_problem(lib, p, None)
-    assert lib.bfm_gpu_problem_assemble(P, prec) == 0, bfm_gb300.last_error()
+    prec, pc, drop = METHODS.get(args.method, METHODS["fp64"])
+    D = learned.DeviceProblem(p, precision=prec)
     s = bfm_gb300.bfm_gpu_stats_t()
-    assert lib.bfm_gpu_problem_stats(P, C.byref(s)) == 0
+    assert lib.bfm_gpu_problem_stats(D.P, C.byref(s)) == 0
     lpr = C.c_int(0)
-    assert lib.bfm_gpu_problem_autotune(P, C.byref(lpr)) == 0, bfm_gb300.last_error()
+    assert lib.bfm_gpu_problem_autotune(D.P, C.byref(lpr)) == 0, bfm_gb300.last_error()
     t_spmv, t_upd = C.c_double(), C.c_double()
-    assert lib.bfm_gpu_problem_time_kernels(P, args.reps, C.byref(t_spmv), C.byref(t_upd)) == 0
+    assert lib.bfm_gpu_problem_time_kernels(D.P, args.reps, C.byref(t_spmv), C.byref(t_upd)) == 0
     ms_net = None
     ms_pc, ms_sw, ncol, persist = None, None, C.c_int(0), C.c_int(0)
-    pc = getattr(bfm_gb300, METHODS.get(args.method, ("", "PC_JACOBI"))[1])
-    if pc in (bfm_gb300.PC_SSOR, bfm_gb300.PC_LEARNED_SSOR, bfm_gb300.PC_SSOR2, bfm_gb300.PC_LEARNED_SSOR2):
+    if pc in SSOR_PCS:
         # two iterations form the colour order (and the coarse operator) and
         # the sweep graph; then the preconditioner alone, `reps` applications
         two = pc in (bfm_gb300.PC_SSOR2, bfm_gb300.PC_LEARNED_SSOR2)
-        o = bfm_gb300.default_opts(precision=prec, precond=bfm_gb300.PC_SSOR2 if two else bfm_gb300.PC_SSOR, max_iters=2)
-        assert lib.bfm_gpu_problem_solve(P, C.byref(o)) == 0, bfm_gb300.last_error()
+        D.solve(precond=bfm_gb300.PC_SSOR2 if two else bfm_gb300.PC_SSOR, max_iters=2, replace_drop=drop)
         t, t_sw = C.c_double(), C.c_double()
-        assert lib.bfm_gpu_problem_time_precond(P, args.reps, C.byref(t), C.byref(t_sw), C.byref(persist)) == 0, \
+        assert lib.bfm_gpu_problem_time_precond(D.P, args.reps, C.byref(t), C.byref(t_sw), C.byref(persist)) == 0, \
             bfm_gb300.last_error()
         ms_sw = t_sw.value
-        lib.bfm_gpu_problem_ordering(P, None, None, C.byref(ncol))
+        lib.bfm_gpu_problem_ordering(D.P, None, None, C.byref(ncol))
         ms_pc = t.value
-    if METHODS.get(args.method, ("", ""))[1] == "PC_LEARNED":
+    if pc == bfm_gb300.PC_LEARNED:
         # the network's inference (features, 4 dense layers on the tensor cores, 3
         # aggregations, head), timed on the problem's stream with CUDA events
-        from bfm_gb300 import learned
-        net = learned.Network(path=learned.WEIGHTS)
-        stream = lib.bfm_gpu_problem_stream(P)
         import torch
+        net = learned.Network(path=learned.WEIGHTS)
+        stream = lib.bfm_gpu_problem_stream(D.P)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ext = torch.cuda.ExternalStream(stream)
         for _ in range(2):
-            assert lib.bfm_gpu_mpnn_forward(net.h, P, None, None, None) == 0, bfm_gb300.last_error()
+            assert lib.bfm_gpu_mpnn_forward(net.h, D.P, None, None, None) == 0, bfm_gb300.last_error()
         e0.record(ext)
         for _ in range(args.reps):
-            assert lib.bfm_gpu_mpnn_forward(net.h, P, None, None, None) == 0, bfm_gb300.last_error()
+            assert lib.bfm_gpu_mpnn_forward(net.h, D.P, None, None, None) == 0, bfm_gb300.last_error()
         e1.record(ext)
         torch.cuda.synchronize()
         ms_net = e0.elapsed_time(e1) / args.reps
         net.close()
-    lib.bfm_gpu_problem_destroy(P)
+    D.close()
     nbytes = algorithmic_bytes_spmv(s.n_blocks, p.n_nodes, prec)
     return {"workload": p.name, "method": args.method, "lanes_per_row": lpr.value, "n_blocks": s.n_blocks,
             "ms_assemble": s.ms_assemble,
             "spmv_ms": t_spmv.value, "update_ms": t_upd.value, "spmv_algorithmic_bytes": nbytes,
             "spmv_gbs": nbytes / (t_spmv.value * 1e-3) / 1e9, "network_forward_ms": ms_net,
-            "precond_ms": ms_pc, "sweeps_ms": ms_sw, "colours": ncol.value, "persistent_sweeps": persist.value}
+            "precond_ms": ms_pc, "sweeps_ms": ms_sw, "colours": ncol.value, "persistent_sweeps": persist.value,
+            "sweeps_algorithmic_bytes": algorithmic_bytes_ssor(s.n_blocks, p.n_nodes, prec) if ms_sw else None}
 
 
 def run_reference(args, rank: int, world: int):
@@ -421,8 +438,10 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="perforated")
     ap.add_argument("--method", default="best",
-                    help="best (all methods, fastest reported), or a comma-separated list of: " + ", ".join(METHODS))
+                    help="best (the default methods, fastest accurate one reported), or a comma-separated list of "
+                         "bfm_gb300.methods names")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-direct", action="store_true", help="skip the direct solve (no err_vs_direct)")
     ap.add_argument("--profile", action="store_true",
                     help="assemble once and launch the two CG kernels --reps times each, standalone "
                          "(for ncu: one JSON line with their CUDA-event durations)")
@@ -450,14 +469,15 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle.cpu_baseline import cpu_baseline
         full = 2 * 2049 * 513 if args.workload == "perforated" else 2 * 1025 * 257
-        cpu = cpu_baseline(args.workload, full, steps=1, warmup=0)["cpu_baseline"]
+        cpu = cpu_baseline(args.workload, full, steps=3, warmup=1)["cpu_baseline"]
 
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    p, results, best, e2e = run_gpu(args, rank, world)
+    p, results, best, e2e, t_direct = run_gpu(args, rank, world)
     if rank != 0:
         return
+    from bfm_gb300.methods import ARITHMETIC, DESCRIPTION
     hbm, peak_kind = peaks()
     r = results[best]
     nb = r["n_blocks"]
@@ -473,35 +493,36 @@ def main():
     # solve init + 2 kernels per iteration + replacement kernels, finish;
     # the learned preconditioner adds its 12 inference kernels per solve
     per_iter = 3 if split else 2
-    ssor = r["pc"] in (3, 4, 5, 6)
+    ssor = r["pc"] in SSOR_PCS
     if ssor:
         # the SSOR sweeps after the init, every update and every replacement:
-        # one cooperative launch, or 2 nc - 1 colour phases; the two-level
-        # form adds its coarse correction, one cooperative launch beside the
-        # persistent sweeps, else four kernels (restriction, chunk sums, the
-        # products by X and X^T)
-        coarse = (1 if r["persistent"] else 4) if r["pc"] in (5, 6) else 0
+        # one cooperative launch (the two-level form's coarse correction runs
+        # inside it), or 2 nc - 1 colour phases and four coarse kernels
+        # (restriction, chunk sums, the products by X and X^T)
+        coarse = (0 if r["persistent"] else 4) if r["pc"] in (5, 6) else 0
         per_pc = (1 if r["persistent"] else 2 * r["ncol"] - 1) + coarse
     else:
         per_pc = 0
     launches_per_step = 24 + 1 + (per_iter + per_pc) * r["iters"] + (2 + per_pc) * r["repl"] + per_pc + 2 + \
-        (12 if r["pc"] in (2, 4, 6) else 0)
+        (12 if r["pc"] in LEARNED_PCS else 0)
     spmv_roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                  "frac": round(achieved / hbm, 3), "traffic": traffic, "traffic_source": traffic_src,
                  "kernel": kernel, "spmv_shape": r["shape"], "algorithmic_bytes": bytes_spmv,
                  "kernel_ms": round(r["ms_spmv"], 5), "peak_source": peak_kind}
     if ssor:
-        # the dominant kernel of an SSOR iteration is the sweep kernel
-        b_pc = algorithmic_bytes_ssor(nb, p.n_nodes)
+        # the dominant kernel of an SSOR iteration is the sweep kernel (timed
+        # here without its fused coarse stages)
+        b_pc = algorithmic_bytes_ssor(nb, p.n_nodes, r["prec"])
         a_pc = b_pc / (r["ms_sweeps"] * 1e-3) / 1e9
-        ok_tr = args.workload == "perforated" and r["persistent"] and r["prec"] == 3
+        tr = SSOR_TRAFFIC.get(r["prec"]) if args.workload == "perforated" and r["persistent"] else None
         roof = {"bound": "hbm", "achieved": round(a_pc, 1), "peak": hbm, "unit": "GB/s", "frac": round(a_pc / hbm, 3),
-                "traffic": SSOR_TRAFFIC[0] if ok_tr else None, "traffic_source": SSOR_TRAFFIC[1] if ok_tr else None,
+                "traffic": tr[0] if tr else None, "traffic_source": tr[1] if tr else None,
                 "kernel": "k_ssor_all" if r["persistent"] else "k_ssor_fwd + k_ssor_bwd",
                 "algorithmic_bytes": b_pc, "kernel_ms": round(r["ms_sweeps"], 5), "peak_source": peak_kind}
     else:
         roof = spmv_roof
     value = r["ms"] / world
+    dtype = {0: "f64", 1: "f32", 2: "f32", 3: "f32x2 (double-float)"}[r["prec"]]
     line = {
         "metric": METRIC,
         "value": round(value, 3),
@@ -513,31 +534,36 @@ def main():
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if r["prec"] == 0 else "f32 (f64 dots/solution/residuals)",
+        "dtype": dtype,
+        "arithmetic": ARITHMETIC[r["prec"]],
         "data": "synthetic (seeded plate generator)",
         "config": {"workload": f"{p.name}: {p.n_dof} DOF, {p.n_elems} P{1 if p.kind == 3 else 2} elements",
-                   "method": best, "rtol": RTOL, "l2": "inputs larger than L2 (matrix %.0f MB)" %
-                   (nb * (4 * (8 if r['prec'] == 0 else 4) + 4) / 1e6), "parallelism": f"replicas{world}"},
+                   "method": best, "method_description": DESCRIPTION[best], "rtol": RTOL,
+                   "l2": "inputs larger than L2 (matrix %.0f MB)" % (nb * (4 * (8 if r['prec'] == 0 else 4) + 4) / 1e6),
+                   "parallelism": f"replicas{world}"},
         "iterations": r["iters"],
         "rel_residual": r["rel_res"],
+        "err_vs_direct": r.get("err_vs_direct"),
+        "direct_solve_s": round(t_direct, 1),
         "ms_assemble": round(r["ms_assemble"], 3),
         "ms_solve": round(r["ms_solve"], 3),
-        "methods": {k: {"ms": round(v["ms"], 3), "iterations": v["iters"], "status": v["status"],
-                        "rel_residual": v["rel_res"], "err_vs_fp64": v["err_vs_fp64"],
+        "methods": {k: {"ms": round(v["ms"], 3), "steps": v["steps"], "iterations": v["iters"], "status": v["status"],
+                        "rel_residual": v["rel_res"], "err_vs_direct": v.get("err_vs_direct"),
                         "replacements": v["repl"], "fallback": v["fallback"], "ms_assemble": round(v["ms_assemble"], 3),
                         "spmv_ms": round(v["ms_spmv"], 5), "update_ms": round(v["ms_update"], 5),
                         "spmv_shape": v["shape"],
                         **({"precond_ms": round(v["ms_precond"], 5), "sweeps_ms": round(v["ms_sweeps"], 5),
                             "colours": v["ncol"],
                             "sweeps": "persistent" if v["persistent"] else "per colour"}
-                           if v["pc"] in (3, 4, 5, 6) else {})}
+                           if v["pc"] in SSOR_PCS else {})}
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),
         "spmv_gbs": round(achieved, 1),
         "roofline": roof,
         **({"roofline_spmv": spmv_roof} if ssor else {}),
         "e2e": {"value": round(e2e["ms"], 3), "unit": "ms", "h2d_bytes_per_step": e2e["h2d"],
-                "d2h_bytes_per_step": e2e["d2h"]},
+                "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"]},
+        "e2e_cold_ms": round(e2e["cold_ms"], 3),
         "gpu_launches": launches_per_step * args.steps,
         "clocks": r["clocks"],
         "cpu_baseline": cpu,

@@ -22,6 +22,7 @@ import pytest
 
 import bfm_gb300
 from bfm_gb300 import api, batch as BA, meshgen as M
+from bfm_gb300.methods import METHODS as MT
 from oracle import oracle as O
 
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
@@ -94,9 +95,7 @@ def test_q1_large_fp64_jacobi_vs_direct(libbfm, q1_large):
         D.close()
 
 
-METHODS = [("ssor2_df", bfm_gb300.FP64_DF, bfm_gb300.PC_SSOR2),
-           ("ssor2_fp64", bfm_gb300.FP64, bfm_gb300.PC_SSOR2),
-           ("mixed_exact", bfm_gb300.MIXED_EXACT, bfm_gb300.PC_JACOBI)]
+METHODS = ["ssor2_df", "ssor2_fp64", "ssor2_mixed", "ssor2_mixed_exact", "mixed_exact"]
 
 
 def test_perforated_system_is_the_oracles(libbfm, perforated):
@@ -110,14 +109,17 @@ def test_perforated_system_is_the_oracles(libbfm, perforated):
         D.close()
 
 
-@pytest.mark.parametrize("name,precision,precond", METHODS, ids=[m[0] for m in METHODS])
-def test_perforated_methods_vs_direct(libbfm, perforated, name, precision, precond):
+@pytest.mark.parametrize("name", METHODS)
+def test_perforated_methods_vs_direct(libbfm, perforated, name):
+    """Every method to relative residual 1e-8 of its own operator, within 1e-6
+    of the direct solve.  The MIXED precision integrates in FP32, so its
+    operator differs from the FP64 one at the 1e-7 level and so does its
+    solution (measured 8e-8 on this plate)."""
     p, _, _, x, floor = perforated
+    precision, precond, drop = MT[name]
     D = api.DeviceProblem(libbfm, p)
     try:
-        o = bfm_gb300.default_opts(rtol=1e-8, precision=precision, precond=precond,
-                                   replace_drop=0.01 if precision == bfm_gb300.FP64_DF else
-                                   0.001 if precision in (bfm_gb300.MIXED, bfm_gb300.MIXED_EXACT) else 0.1)
+        o = bfm_gb300.default_opts(rtol=1e-8, precision=precision, precond=precond, replace_drop=drop)
         D.assemble(precision)
         D.solve(o)
         s = D.stats()
