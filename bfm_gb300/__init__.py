@@ -48,6 +48,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_last_stats": (_i, [_P(bfm_gpu_stats_t)]),
     "bfm_gpu_last_error": (C.c_char_p, []),
     "bfm_gpu_device_count": (_i, []),
+    "bfm_gpu_set_system_storage": (_i, [_i]),
     "bfm_gpu_instance_set_elem_material": (_i, [_P(abi.bfm_instance_t), _vp, _vp]),
     "bfm_gpu_problem_create": (_i, [_P(_vp), _i, _i, _i, _i, _i, _vp]),
     "bfm_gpu_problem_destroy": (_i, [_vp]),

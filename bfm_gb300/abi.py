@@ -116,8 +116,12 @@ class bfm_matrix_band_t(C.Structure):  # matrix.h:24-27
     _fields_ = [("k", c_size_t), ("data", c_double_p)]
 
 
+class bfm_matrix_sparse_t(C.Structure):  # matrix.h (additive kind)
+    _fields_ = [("handle", C.c_void_p), ("nnz", c_size_t)]
+
+
 class _matrix_u(C.Union):
-    _fields_ = [("full", bfm_matrix_full_t), ("band", bfm_matrix_band_t)]
+    _fields_ = [("full", bfm_matrix_full_t), ("band", bfm_matrix_band_t), ("sparse", bfm_matrix_sparse_t)]
 
 
 class bfm_matrix_t(C.Structure):  # matrix.h:29-43
@@ -223,7 +227,7 @@ SIM_NONE, SIM_PLANAR_STRAIN, SIM_PLANAR_STRESS, SIM_AXISYMMETRIC_STRAIN = 0, 1, 
 DIRICHLET_X, DIRICHLET_Y, NEUMANN_X, NEUMANN_Y = 0, 1, 2, 3
 NEUMANN_NORMAL, NEUMANN_TANGENT, DIRICHLET_NORMAL, DIRICHLET_TANGENT = 4, 5, 6, 7
 FORCE_NONE, FORCE_LINEAR, FORCE_FUNKY = 0, 1, 2
-MATRIX_FULL, MATRIX_BAND = 0, 1
+MATRIX_FULL, MATRIX_BAND, MATRIX_SPARSE = 0, 1, 2
 MAJOR_ROW, MAJOR_COLUMN = 0, 1
 
 

@@ -3072,6 +3072,37 @@ int bfmi_mesh(bfm_gpu_problem_t* P, bfmi_mesh_t* o) {
 	return 0;
 }
 
+int bfmi_solve_rhs(bfm_gpu_problem_t* P, const double* b, double* x, const bfm_gpu_opts_t* opts, int* status, int* iterations,
+                   double* rel_residual) {
+	g_err[0] = 0;
+	bfm_gpu_opts_t o = *opts;
+	o.precision = BFM_GPU_FP64;
+	// the right-hand side is replaced after the assembly, so the assembly
+	// (with this preconditioner, in FP64) comes first
+	if (!P->assembled || P->precision != BFM_GPU_FP64 || o.precond != P->precond) {
+		P->precond = o.precond;
+		if (bfm_gpu_problem_assemble(P, BFM_GPU_FP64)) return -1;
+	}
+	long const n = 2l * P->N;
+	if (P->ordered) {
+		// into the working (colour-major) order: b_w[w] = b[perm[w]]
+		if (ensure_otmp(P)) return -1;
+		CK(cudaMemcpyAsync(P->otmp, b, n * sizeof(double), cudaMemcpyHostToDevice, P->stream));
+		k_gather_nodes<double><<<blocks_for(n), TPB, 0, P->stream>>>(P->N, 2, (const double*) P->otmp, P->perm, P->b);
+		CK(cudaGetLastError());
+	}
+	else {
+		CK(cudaMemcpyAsync(P->b, b, n * sizeof(double), cudaMemcpyHostToDevice, P->stream));
+	}
+	if (bfm_gpu_problem_solve(P, &o)) return -1;
+	bfm_gpu_stats_t s;
+	if (bfm_gpu_problem_stats(P, &s)) return -1;
+	if (status) *status = s.status;
+	if (iterations) *iterations = s.iterations;
+	if (rel_residual) *rel_residual = s.rel_residual;
+	return bfm_gpu_problem_solution(P, x, BFM_GPU_HOST);
+}
+
 int bfmi_set_precond_blocks(bfm_gpu_problem_t* P, const double* blocks) {
 	if (!P->assembled) return fail("assemble before setting the preconditioner");
 	// FP64 SSOR sweeps read FP32 relaxation blocks: the double-float layout;

@@ -15,6 +15,8 @@
 #include <bfm/matrix.h>
 #include <bfm/perm.h>
 
+#include "internal.h"
+
 static double* zalloc_d(bfm_state_t* state, size_t n) {
 	double* p = state->alloc(n * sizeof *p);
 	if (p) memset(p, 0, n * sizeof *p);
@@ -55,6 +57,7 @@ int bfm_matrix_band_create(bfm_matrix_t* A, bfm_state_t* state, bfm_matrix_major
 }
 
 int bfm_matrix_destroy(bfm_matrix_t* A) {
+	if (A->kind == BFM_MATRIX_KIND_SPARSE) return bfmi_sparse_destroy(A);
 	if (A->kind == BFM_MATRIX_KIND_FULL) {
 		A->state->free(A->full.data);
 		A->full.data = NULL;
@@ -71,6 +74,7 @@ int bfm_matrix_destroy(bfm_matrix_t* A) {
 double bfm_matrix_get(bfm_matrix_t* A, size_t i, size_t j) {
 	if (i >= A->m || j >= A->m) return BFM_NAN;
 	if (A->kind == BFM_MATRIX_KIND_FULL) return A->full.data[full_index(A, i, j)];
+	if (A->kind == BFM_MATRIX_KIND_SPARSE) return bfmi_sparse_get(A, i, j);
 	if (A->kind == BFM_MATRIX_KIND_BAND) return in_band(A, i, j) ? A->band.data[band_index(A, i, j)] : 0.0;
 	return -1;
 }
@@ -105,6 +109,7 @@ int bfm_matrix_add(bfm_matrix_t* A, size_t i, size_t j, double v) {
 
 size_t bfm_matrix_bandwidth(bfm_matrix_t* A) {
 	if (A->kind == BFM_MATRIX_KIND_BAND) return A->band.k;
+	if (A->kind == BFM_MATRIX_KIND_SPARSE) return bfmi_sparse_bandwidth(A);
 	if (A->kind != BFM_MATRIX_KIND_FULL) return (size_t) -1;
 	size_t k = 0;
 	for (size_t i = 0; i < A->m; i++)
@@ -116,7 +121,7 @@ size_t bfm_matrix_bandwidth(bfm_matrix_t* A) {
 }
 
 int bfm_matrix_copy(bfm_matrix_t* A, bfm_matrix_t* src) {
-	if (A->m != src->m) return -1;
+	if (A->m != src->m || A->kind == BFM_MATRIX_KIND_SPARSE) return -1;  // sparse matrices are read-only
 	if (A->kind == BFM_MATRIX_KIND_FULL && src->kind == BFM_MATRIX_KIND_FULL) {
 		memcpy(A->full.data, src->full.data, src->m * src->m * sizeof(double));
 		return 0;
@@ -190,6 +195,7 @@ int bfm_matrix_lu_solve(bfm_matrix_t* A, bfm_vec_t* y) {
 }
 
 int bfm_matrix_solve(bfm_matrix_t* A, bfm_vec_t* y) {
+	if (A->kind == BFM_MATRIX_KIND_SPARSE) return bfmi_sparse_solve(A, y);  // the GPU PCG, not a factorization
 	if (bfm_matrix_lu(A) < 0) return -1;
 	return bfm_matrix_lu_solve(A, y);
 }
@@ -215,6 +221,7 @@ int bfm_perm_destroy(bfm_perm_t* perm) {
 
 /* new[p[i]][p[j]] = old[i][j] with p = perm (or inv_perm) */
 int bfm_perm_perm_matrix(bfm_perm_t* perm, bfm_matrix_t* A, bool inv) {
+	if (A->kind == BFM_MATRIX_KIND_SPARSE) return bfmi_sparse_permute(perm, A, inv);
 	if (!perm->has_perm || A->m != perm->m || A->kind != BFM_MATRIX_KIND_FULL) return -1;
 	size_t const m = A->m;
 	size_t const* p = inv ? perm->inv_perm : perm->perm;
@@ -243,6 +250,7 @@ int bfm_perm_perm_vec(bfm_perm_t* perm, bfm_vec_t* vec, bool inv) {
 /* RCM of a full or band matrix: its numeric nonzeros go to CSR (one O(m^2)
  * scan, unavoidable for dense input), then the sparse bit-exact RCM. */
 int bfm_perm_rcm(bfm_perm_t* perm, bfm_matrix_t* A) {
+	if (A->kind == BFM_MATRIX_KIND_SPARSE) return bfmi_sparse_rcm(perm, A);
 	size_t const m = A->m;
 	if (perm->m != m) return -1;
 	bfm_state_t* const state = perm->state;

@@ -18,12 +18,31 @@
 #include <bfm/sim.h>
 #include <bfm/system.h>
 
+#include "internal.h"
+
 /* ---------------------------------------------------------------- errors and options */
 
 static _Thread_local char t_msg[512];
 static _Thread_local bfm_gpu_opts_t t_opts;
 static _Thread_local int t_opts_set;
 static _Thread_local bfm_gpu_stats_t t_stats;
+static _Thread_local int t_storage = -1;  /* system matrix storage: -1 = not set (environment) */
+
+int bfm_gpu_set_system_storage(int kind) {
+	if (kind != BFM_MATRIX_KIND_FULL && kind != BFM_MATRIX_KIND_SPARSE) return -1;
+	t_storage = kind;
+	return 0;
+}
+
+/* sparse storage: asked for, or a dense n x n matrix above 16 GB */
+static int sparse_system(size_t n) {
+	int kind = t_storage;
+	if (kind < 0) {
+		char const* e = getenv("BFM_GPU_SYSTEM_STORAGE");
+		kind = e && !strcmp(e, "sparse") ? BFM_MATRIX_KIND_SPARSE : BFM_MATRIX_KIND_FULL;
+	}
+	return kind == BFM_MATRIX_KIND_SPARSE || (double) n * (double) n * sizeof(double) > 16e9;
+}
 
 static int report(bfm_state_t* state, char const* func, int line, char const* fmt, ...) {
 	va_list ap;
@@ -274,7 +293,7 @@ static int gather(bfm_state_t* st, bfm_sim_t* sim, bfm_instance_t* inst, gathere
 
 /* Upload one instance and assemble it in `precision`. */
 static bfm_gpu_problem_t* upload_and_assemble(bfm_state_t* st, bfm_sim_t* sim, bfm_instance_t* inst, int stress, int precision,
-                                              int precond) {
+                                              int precond, int dedicated) {
 	gathered_t g;
 	if (gather(st, sim, inst, &g) < 0) {
 		release(&g);
@@ -283,7 +302,15 @@ static bfm_gpu_problem_t* upload_and_assemble(bfm_state_t* st, bfm_sim_t* sim, b
 	bfm_mesh_t* const mesh = inst->obj->mesh;
 	bfm_material_t* const mat = inst->obj->material;
 	elem_mat_t const em = elem_mat_of(inst);
-	bfm_gpu_problem_t* P = problem_for(inst, (int) mesh->kind, (int) mesh->n_nodes, (int) mesh->n_elems, g.n_edges, g.nc);
+	/* a dedicated problem (owned by the caller, e.g. a sparse system matrix) or the instance's cached one */
+	bfm_gpu_problem_t* P = NULL;
+	if (dedicated) {
+		if (bfm_gpu_problem_create(&P, (int) mesh->kind, (int) mesh->n_nodes, (int) mesh->n_elems, g.n_edges, g.nc, NULL) < 0)
+			P = NULL;
+	}
+	else {
+		P = problem_for(inst, (int) mesh->kind, (int) mesh->n_nodes, (int) mesh->n_elems, g.n_edges, g.nc);
+	}
 	int ok = P != NULL;
 	const double* fields[8];
 	for (int f = 0; f < 8; f++) fields[f] = g.fields[f];
@@ -298,6 +325,7 @@ static bfm_gpu_problem_t* upload_and_assemble(bfm_state_t* st, bfm_sim_t* sim, b
 	release(&g);
 	if (!ok) {
 		REPORT(st, "%s", bfm_gpu_last_error());
+		if (dedicated && P) bfm_gpu_problem_destroy(P);
 		return NULL;
 	}
 	return P;
@@ -327,7 +355,7 @@ static int run_instance(bfm_sim_t* sim, bfm_instance_t* inst, int stress) {
 	if ((o.precond == BFM_GPU_PC_LEARNED || o.precond == BFM_GPU_PC_LEARNED_SSOR || o.precond == BFM_GPU_PC_LEARNED_SSOR2) &&
 	    env_network(st) < 0)
 		return -1;
-	bfm_gpu_problem_t* P = upload_and_assemble(st, sim, inst, stress, o.precision, o.precond);
+	bfm_gpu_problem_t* P = upload_and_assemble(st, sim, inst, stress, o.precision, o.precond, 0);
 	if (!P) return -1;
 	if (bfm_gpu_problem_solve(P, &o) < 0) return REPORT(st, "%s", bfm_gpu_last_error());
 	bfm_gpu_stats_t s;
@@ -391,6 +419,13 @@ int bfm_system_destroy(bfm_system_t* s) {
 
 /* RCM renumbering, then conversion to band storage (ref system.c:44-81). */
 int bfm_system_renumber(bfm_system_t* s) {
+	if (s->A.kind == BFM_MATRIX_KIND_SPARSE) {
+		/* the reference's permutation and permuted right-hand side; the sparse
+		 * matrix records the permutation and keeps its storage */
+		if (bfm_perm_rcm(&s->perm, &s->A) < 0) return -1;
+		if (bfm_perm_perm_vec(&s->perm, &s->b, false) < 0) return -1;
+		return bfm_perm_perm_matrix(&s->perm, &s->A, false);
+	}
 	if (bfm_perm_rcm(&s->perm, &s->A) < 0) return -1;
 	if (bfm_perm_perm_matrix(&s->perm, &s->A, false) < 0) return -1;
 	if (bfm_perm_perm_vec(&s->perm, &s->b, false) < 0) return -1;
@@ -413,13 +448,32 @@ static int create_planar(bfm_system_t* s, bfm_instance_t* inst, size_t n_forces,
 	bfm_mesh_t* const mesh = inst->obj->mesh;
 	if (mesh->dim != 2 || (mesh->kind != BFM_ELEM_KIND_SIMPLEX && mesh->kind != BFM_ELEM_KIND_QUAD)) return -1;
 	size_t const n = mesh->n_nodes * 2;
-	if (bfm_system_create(s, st, n) < 0) return -1;
 	bfm_sim_t tmp;
 	memset(&tmp, 0, sizeof tmp);
 	tmp.state = st;
 	tmp.n_forces = n_forces;
 	tmp.forces = forces;
-	bfm_gpu_problem_t* P = upload_and_assemble(st, &tmp, inst, stress, BFM_GPU_FP64, BFM_GPU_PC_JACOBI);
+	if (sparse_system(n)) {
+		/* O(nnz): the device problem stays (the matrix owns it), a host copy of
+		 * its 2x2-block CSR for reads; no n x n storage anywhere */
+		s->state = st;
+		s->n = n;
+		if (bfm_perm_create(&s->perm, st, n) < 0) return -1;
+		if (bfm_vec_create(&s->b, st, n) < 0) return -1;
+		bfm_gpu_problem_t* P = upload_and_assemble(st, &tmp, inst, stress, BFM_GPU_FP64, BFM_GPU_PC_JACOBI, 1);
+		if (!P) {
+			bfm_vec_destroy(&s->b);
+			return -1;
+		}
+		if (bfmi_sparse_wrap(&s->A, st, P, mesh->n_nodes, s->b.data) < 0) {
+			bfm_gpu_problem_destroy(P);
+			bfm_vec_destroy(&s->b);
+			return REPORT(st, "%s", bfm_gpu_last_error());
+		}
+		return 0;
+	}
+	if (bfm_system_create(s, st, n) < 0) return -1;
+	bfm_gpu_problem_t* P = upload_and_assemble(st, &tmp, inst, stress, BFM_GPU_FP64, BFM_GPU_PC_JACOBI, 0);
 	if (!P) return -1;
 	int64_t nb = 0;
 	if (bfm_gpu_problem_n_blocks(P, &nb) < 0) return REPORT(st, "%s", bfm_gpu_last_error());

@@ -1,6 +1,8 @@
 /* Library-internal helpers shared by the translation units (not exported). */
 #pragma once
 
+#include <bfm/gpu.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -58,6 +60,29 @@ __attribute__((visibility("hidden"))) int bfmi_set_precond_blocks(struct bfm_gpu
 __attribute__((visibility("hidden"))) int bfmi_learned_precond(struct bfm_gpu_problem* P, int jacobi);
 
 __attribute__((visibility("hidden"))) int bfmi_buffers(struct bfm_gpu_problem* P, bfmi_buffers_t* out);
+
+/* Solve the assembled FP64 system for the right-hand side b (2 n_nodes
+ * doubles, host, the caller's node order) with the options' rtol and
+ * preconditioner (re-assembling first when the preconditioner changes) and
+ * copy the solution to x (host, the caller's order); *status gets the
+ * solver's BFM_GPU_* status.  Used by the sparse system matrices. */
+__attribute__((visibility("hidden"))) int bfmi_solve_rhs(struct bfm_gpu_problem* P, const double* b, double* x,
+                                                         const bfm_gpu_opts_t* opts, int* status, int* iterations,
+                                                         double* rel_residual);
+
+/* Sparse system matrices (host_sparse.c): a matrix of kind
+ * BFM_MATRIX_KIND_SPARSE around an assembled FP64 problem it then owns
+ * (n_nodes nodes; its right-hand side copied to b); the kind's operations. */
+#include <bfm/matrix.h>
+#include <bfm/perm.h>
+__attribute__((visibility("hidden"))) int bfmi_sparse_wrap(bfm_matrix_t* A, bfm_state_t* state, bfm_gpu_problem_t* P,
+                                                           size_t n_nodes, double* b);
+__attribute__((visibility("hidden"))) int bfmi_sparse_destroy(bfm_matrix_t* A);
+__attribute__((visibility("hidden"))) double bfmi_sparse_get(bfm_matrix_t* A, size_t i, size_t j);
+__attribute__((visibility("hidden"))) size_t bfmi_sparse_bandwidth(bfm_matrix_t* A);
+__attribute__((visibility("hidden"))) int bfmi_sparse_rcm(bfm_perm_t* perm, bfm_matrix_t* A);
+__attribute__((visibility("hidden"))) int bfmi_sparse_permute(bfm_perm_t* perm, bfm_matrix_t* A, bool inv);
+__attribute__((visibility("hidden"))) int bfmi_sparse_solve(bfm_matrix_t* A, bfm_vec_t* y);
 
 /* Extension slot of a problem: freed by bfm_gpu_problem_destroy. */
 __attribute__((visibility("hidden"))) void** bfmi_ext_slot(struct bfm_gpu_problem* P, void (**free_fn)(void*));

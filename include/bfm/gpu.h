@@ -134,6 +134,16 @@ int bfm_gpu_last_stats(bfm_gpu_stats_t* stats);
 /* Message of the last failure on this thread ("" if none). */
 const char* bfm_gpu_last_error(void);
 
+/* Storage of the stiffness matrix the bfm_system_create_planar_* and
+ * bfm_system_create_axisymmetric_strain creators of this thread return (an
+ * extension: the reference stores it dense, n^2 doubles, system.c:13):
+ * BFM_MATRIX_KIND_FULL (the default) or BFM_MATRIX_KIND_SPARSE.  Without a
+ * call, BFM_GPU_SYSTEM_STORAGE=sparse in the environment selects SPARSE, and
+ * systems whose dense matrix would pass 16 GB are SPARSE anyway.  A SPARSE
+ * system renumbers with the reference's RCM (the same permutation) but keeps
+ * its storage; bfm_matrix_solve then solves it on the GPU. */
+int bfm_gpu_set_system_storage(int kind);
+
 /* Number of usable CUDA devices (0 without a GPU; never fails). */
 int bfm_gpu_device_count(void);
 

@@ -13,6 +13,12 @@
 typedef enum {
 	BFM_MATRIX_KIND_FULL,
 	BFM_MATRIX_KIND_BAND,
+	/* Additive (not in the reference): the stiffness matrix of a
+	 * bfm_system_create_planar_* system kept sparse -- 2x2-block CSR in GPU
+	 * memory with a host copy, O(nnz) storage where FULL needs n^2.  Read-only
+	 * (bfm_matrix_set/add return -1); bfm_matrix_solve solves it with the GPU
+	 * PCG (bfm_gpu_get_opts: rtol, preconditioner) instead of a band LU. */
+	BFM_MATRIX_KIND_SPARSE,
 } bfm_matrix_kind_t;
 
 typedef enum {
@@ -30,6 +36,11 @@ typedef struct {
 } bfm_matrix_band_t;
 
 typedef struct {
+	void* handle; /* the library's sparse matrix object           */
+	size_t nnz;   /* stored scalar entries (4 per 2x2 block)       */
+} bfm_matrix_sparse_t;
+
+typedef struct {
 	bfm_state_t* state;
 	bfm_matrix_kind_t kind;
 	bfm_matrix_major_t major;
@@ -37,6 +48,7 @@ typedef struct {
 	union {
 		bfm_matrix_full_t full;
 		bfm_matrix_band_t band;
+		bfm_matrix_sparse_t sparse; /* same size as band: the struct keeps its layout */
 	};
 } bfm_matrix_t;
 
