@@ -73,6 +73,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_set_edge_boundary": (_i, [_vp, _vp, _i]),
     "bfm_gpu_problem_set_parts": (_i, [_vp, _i, _vp]),
     "bfm_gpu_problem_solve_parts": (_i, [_vp, _P(bfm_gpu_opts_t)]),
+    "bfm_gpu_problem_step_parts": (_i, [_vp, _i, _P(bfm_gpu_opts_t)]),
     "bfm_gpu_problem_part_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _P(_i), _P(_i), _P(_d)]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
     "bfm_gpu_problem_apply": (_i, [_vp, _vp, _vp, _i]),

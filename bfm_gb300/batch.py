@@ -81,6 +81,11 @@ class Batch:
         o = opts or default_opts(rtol=1e-8)
         assert self.lib.bfm_gpu_problem_solve_parts(self.P, C.byref(o)) == 0, last_error()
 
+    def step(self, precision=MIXED_EXACT, opts: bfm_gpu_opts_t | None = None):
+        """Assembly + solve as one CUDA graph launch (bfm_gpu_problem_step_parts)."""
+        o = opts or default_opts(rtol=1e-8)
+        assert self.lib.bfm_gpu_problem_step_parts(self.P, precision, C.byref(o)) == 0, last_error()
+
     def stats(self):
         n = len(self.problems)
         it = np.zeros(n, np.int32)

@@ -495,6 +495,12 @@ struct BatchState {
 	float last_ms;
 	int direct;            // 1: launched without a graph (capture unsupported)
 	cudaEvent_t ev[2];
+	// bfm_gpu_problem_step_parts: assembly + solve captured as one graph
+	cudaGraphExec_t step_graph;
+	int step_direct;       // capture unsupported here: the same work launched directly
+	int s_precision, s_rpt, s_lpr;
+	unsigned s_gen;
+	bfm_gpu_opts_t s_opts;
 };
 
 void batch_free(void* p) {
@@ -504,6 +510,7 @@ void batch_free(void* p) {
 	for (void* q : d)
 		if (q) cudaFree(q);
 	if (B->graph) cudaGraphExecDestroy(B->graph);
+	if (B->step_graph) cudaGraphExecDestroy(B->step_graph);
 	for (auto& e : B->ev)
 		if (e) cudaEventDestroy(e);
 	free(B->node_off_h);
@@ -769,6 +776,75 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		BatchArgs a = batch_args(P, B, &o);
 		if (launch(B, &a, B->lpr, B->grid, st)) return -1;
 	}
+	BCK(cudaEventRecord(B->ev[1], st));
+	return 0;
+}
+
+int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gpu_opts_t* opts) {
+	g_berr[0] = 0;
+	BatchState* B = state_of(P);
+	if (!B) return bfail("set the parts first (bfm_gpu_problem_set_parts)");
+	if (precision != BFM_GPU_MIXED && precision != BFM_GPU_MIXED_EXACT)
+		return bfail("the batched solver runs the mixed-precision iteration: BFM_GPU_MIXED or BFM_GPU_MIXED_EXACT");
+	bfm_gpu_opts_t o;
+	if (opts) o = *opts;
+	else bfm_gpu_default_opts(&o);
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	cudaStream_t const st = (cudaStream_t) bf.stream;
+	bool const same = (B->step_graph || B->step_direct) && B->s_precision == precision && B->s_gen == bf.inputs_gen &&
+	                  B->s_rpt == B->rows_per_tile && B->s_lpr == B->lpr && B->s_opts.rtol == o.rtol &&
+	                  B->s_opts.max_iters == o.max_iters && B->s_opts.replace_drop == o.replace_drop &&
+	                  B->s_opts.barrier_polls == o.barrier_polls && B->s_opts.autotune == o.autotune;
+	if (!same) {
+		// one step launched directly first: it sizes every buffer, tunes the
+		// tile shape and leaves nothing for the capture to allocate
+		if (bfm_gpu_problem_assemble(P, precision)) return -1;
+		if (bfm_gpu_problem_solve_parts(P, &o)) return -1;
+		BCK(cudaStreamSynchronize(st));
+		if (B->step_graph) cudaGraphExecDestroy(B->step_graph);
+		B->step_graph = nullptr;
+		B->step_direct = 0;
+		int grid = 0;
+		if (coop_grid(B->lpr, &grid)) return -1;
+		B->grid = grid;
+		BatchArgs a = batch_args(P, B, &o);
+		cudaGraph_t g = nullptr;
+		int rc = 0;
+		if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = bfail("stream capture failed");
+		if (!rc) rc = bfm_gpu_problem_assemble(P, precision);
+		if (!rc) {
+			BatchArgs a2 = batch_args(P, B, &o);  // the assembly's buffers, unchanged
+			a = a2;
+			rc = launch(B, &a, B->lpr, grid, st);
+		}
+		cudaError_t const ec = cudaStreamEndCapture(st, &g);
+		if (!rc && ec != cudaSuccess) rc = bfail("stream capture failed: %s", cudaGetErrorString(ec));
+		if (!rc) {
+			cudaError_t const ei = cudaGraphInstantiate(&B->step_graph, g, 0);
+			if (ei != cudaSuccess) rc = bfail("graph instantiation failed: %s", cudaGetErrorString(ei));
+		}
+		if (g) cudaGraphDestroy(g);
+		cudaGetLastError();
+		if (rc) {
+			// no capture of this work here: the same two calls, launched directly
+			B->step_graph = nullptr;
+			B->step_direct = 1;
+			g_berr[0] = 0;
+			bfm_gpu_set_last_error("");
+		}
+		B->s_precision = precision;
+		B->s_gen = bf.inputs_gen;
+		B->s_rpt = B->rows_per_tile;
+		B->s_lpr = B->lpr;
+		B->s_opts = o;
+	}
+	if (B->step_direct) {
+		if (bfm_gpu_problem_assemble(P, precision)) return -1;
+		return bfm_gpu_problem_solve_parts(P, &o);
+	}
+	BCK(cudaEventRecord(B->ev[0], st));
+	BCK(cudaGraphLaunch(B->step_graph, st));
 	BCK(cudaEventRecord(B->ev[1], st));
 	return 0;
 }

@@ -1464,6 +1464,7 @@ struct bfm_gpu_problem {
 	double* lloads;
 	int *lcnt, *lptr, *llist;
 
+	unsigned inputs_gen;     // bumped by every bfm_gpu_problem_set_* (captured assemblies bake some inputs in)
 	void* ext;               // batch solver state (batch.cu)
 	void (*ext_free)(void*);
 
@@ -2902,6 +2903,7 @@ void* bfm_gpu_problem_stream(bfm_gpu_problem_t* P) { return (void*) P->stream; }
 static cudaMemcpyKind kind_of(int where) { return where == BFM_GPU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
 
 int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* P, const double* coords, const int32_t* elems, int where) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	CK(cudaMemcpyAsync(P->coords, coords, 2l * P->N * sizeof(double), kind_of(where), P->stream));
 	CK(cudaMemcpyAsync(P->elems, elems, (long) P->NE * P->kind * sizeof(int), kind_of(where), P->stream));
@@ -2913,6 +2915,7 @@ int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* P, const double* coords, con
 
 int bfm_gpu_problem_set_material(bfm_gpu_problem_t* P, double E, double nu, double rho, int stress, const double* elem_E,
                                  const double* elem_nu, int where) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	if (stress < 0 || stress > 3) return fail("element formulation %d is not one of 0..3", stress);
 	P->E = E;
@@ -2935,6 +2938,7 @@ int bfm_gpu_problem_set_material(bfm_gpu_problem_t* P, double E, double nu, doub
 
 int bfm_gpu_problem_set_rule(bfm_gpu_problem_t* P, int n_points, const double* weights, const double* phi, const double* dxi,
                              const double* deta) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	if (n_points < 0 || n_points > MAXQ) return fail("integration rules of at most 16 points are supported");
 	P->rule.nq = n_points;
@@ -2951,6 +2955,7 @@ int bfm_gpu_problem_set_rule(bfm_gpu_problem_t* P, int n_points, const double* w
 }
 
 int bfm_gpu_problem_set_forces(bfm_gpu_problem_t* P, int n_forces, const double* values, const double* const* node_values, int where) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	if (n_forces < 0 || n_forces > MAXF) return fail("at most 8 body forces are supported");
 	P->forces.nf = n_forces;
@@ -2972,6 +2977,7 @@ int bfm_gpu_problem_set_forces(bfm_gpu_problem_t* P, int n_forces, const double*
 
 int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int* kinds, const double* values, const uint8_t* masks,
                                    int n_edges, const int32_t* edges, int where) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	if (n_conds > P->max_conds || n_conds < 0) return fail("more conditions than the problem was created for");
 	if (n_edges > P->max_edges || n_edges < 0) return fail("more edges than the problem was created for");
@@ -2994,6 +3000,7 @@ int bfm_gpu_problem_set_conditions(bfm_gpu_problem_t* P, int n_conds, const int*
 }
 
 int bfm_gpu_problem_set_edge_boundary(bfm_gpu_problem_t* P, const uint8_t* boundary, int where) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	if (P->n_edges) CK(cudaMemcpyAsync(P->eboundary, boundary, P->n_edges, kind_of(where), P->stream));
 	P->assembled = false;
@@ -3001,6 +3008,7 @@ int bfm_gpu_problem_set_edge_boundary(bfm_gpu_problem_t* P, const uint8_t* bound
 }
 
 int bfm_gpu_problem_set_edge_loads(bfm_gpu_problem_t* P, int n_loads, const int32_t* edges, const double* loads, int where) {
+	P->inputs_gen++;
 	g_err[0] = 0;
 	if (n_loads < 0) return fail("negative load count");
 	if (n_loads > P->cap_loads) {
@@ -3046,6 +3054,7 @@ int bfmi_buffers(bfm_gpu_problem_t* P, bfmi_buffers_t* o) {
 	o->x = P->x;
 	for (int i = 0; i < 5; i++) o->vec[i] = P->vec[i];
 	o->stream = (void*) P->stream;
+	o->inputs_gen = P->inputs_gen;
 	if (P->ordered) {
 		o->ncol = P->ncol;
 		for (int c = 0; c <= P->ncol && c < 65; c++) o->col_off[c] = P->col_off[c];
@@ -3177,7 +3186,12 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	// the SpMV shape is tuned per precision (each has its own kernels)
 	if (P->precision != precision) P->tuned = 0;
 	P->precision = precision;
-	CK(cudaEventRecord(P->ev[0], st));
+	// timing events only outside a stream capture (a captured assembly is
+	// timed by whoever launches the graph)
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	CK(cudaStreamIsCapturing(st, &cap));
+	bool const capturing = cap != cudaStreamCaptureStatusNone;
+	if (!capturing) CK(cudaEventRecord(P->ev[0], st));
 	CK(cudaMemsetAsync(P->err, 0, sizeof(int), st));
 	// 0. node order (colour-major for the SSOR preconditioners)
 	if (prepare_order(P)) return -1;
@@ -3342,7 +3356,7 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 	if (ssor && build_sell(P)) return -1;
 	// two-level SSOR: the coarse operator of this matrix
 	if (coarse_pc(P->precond) && coarse_setup(P)) return -1;
-	CK(cudaEventRecord(P->ev[1], st));
+	if (!capturing) CK(cudaEventRecord(P->ev[1], st));
 	P->assembled = true;
 	P->solved = false;
 	return 0;

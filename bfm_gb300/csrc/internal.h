@@ -34,6 +34,7 @@ typedef struct {
 	int ncol;
 	int col_off[65];
 	const int* dpos;
+	unsigned inputs_gen;  /* changes with every bfm_gpu_problem_set_* call */
 } bfmi_buffers_t;
 
 /* Mesh-side device arrays of a problem (read only). */

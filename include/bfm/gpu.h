@@ -272,6 +272,16 @@ int bfm_gpu_problem_set_edge_boundary(bfm_gpu_problem_t* problem, const uint8_t*
  * Grid barriers inside the kernel wait a bounded time, then report an error. */
 int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t* opts);
 
+/* One step of the batch -- assembly in `precision` (MIXED or MIXED_EXACT)
+ * and the batched solve -- as ONE CUDA graph launch: the first call runs the
+ * step directly (sizing every buffer, tuning the tile shape), then captures
+ * the whole step (pattern, element loop, conditions, loads, the persistent
+ * solver kernel and the per-part residuals) into a graph that later calls
+ * replay.  A change of options, precision or any input set through
+ * bfm_gpu_problem_set_* captures again.  Asynchronous; statistics via
+ * bfm_gpu_problem_part_stats (ms_solve: the device time of the whole step). */
+int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* problem, int precision, const bfm_gpu_opts_t* opts);
+
 /* Wait, then per part (arrays of n_parts, any may be NULL): iterations,
  * status (BFM_GPU_*), FP64 residual replacements, FP64 relative residual;
  * and the tile shape used and the device time of the last solve. */

@@ -66,3 +66,31 @@ def test_batch_rerun_is_bit_identical(libbfm):
     finally:
         B.close()
     assert np.array_equal(x1, x2)
+
+
+def test_step_graph_matches_separate_calls(libbfm):
+    """bfm_gpu_problem_step_parts (assembly + batched solve captured as one
+    graph) gives the solutions of the separate assemble + solve calls, bit for
+    bit, on every replay, and captures again when an input changes."""
+    ps = small_batch(8, seed=5)
+    B = BA.Batch(libbfm, ps)
+    try:
+        o = bfm_gb300.default_opts(rtol=1e-8, autotune=0)
+        B.assemble(bfm_gb300.MIXED_EXACT)
+        B.solve(o)
+        x0 = np.concatenate(B.solutions())
+        for _ in range(3):
+            B.step(bfm_gb300.MIXED_EXACT, o)
+            st = B.stats()
+            assert np.all(st["status"] == 0)
+            assert np.array_equal(np.concatenate(B.solutions()), x0)
+        # twice the loads: twice the displacements (linear elasticity)
+        lo = B.keep[7] * 2.0
+        le = B.keep[6]
+        assert libbfm.bfm_gpu_problem_set_edge_loads(B.P, len(le), le.ctypes.data, lo.ctypes.data, 0) == 0
+        B.keep.append(lo)
+        B.step(bfm_gb300.MIXED_EXACT, o)
+        x2 = np.concatenate(B.solutions())
+        assert np.linalg.norm(x2 - 2 * x0) <= 1e-7 * np.linalg.norm(2 * x0)
+    finally:
+        B.close()
