@@ -2370,6 +2370,96 @@ __global__ void __launch_bounds__(32 * LINV_W) k_coarse_linv(CoarseArgs a) {
 	}
 }
 
+// X = L^-1 by block rows (block size b >= bw, so L is block bidiagonal:
+// block row k holds its diagonal block L_kk and the block L_k,k-1).  Row i of
+// X follows x_i = d_i (e_i - sum_{i' < i} L_ii' x_i') with d_i = 1 / L_ii (0
+// for a dropped DOF: a zero row and column, as the column-wise form).  Within
+// block row k that forward substitution is linear in what block row k-1
+// feeds it, so X_kk is the substitution of the unit vectors and, for every
+// column of an earlier block, X_kj = M_k X_k-1,j with M_k = -X_kk L_k,k-1.
+// k_linv_diag forms X_kk and M_k for every k at once (a block each); then
+// k_linv_step, one launch per block row, forms X_kj for all j < k from the
+// previous block row: the sequential chain is nc / b launches instead of nc
+// dependent steps per column.  Double-float throughout; X and X^T written
+// rounded to FP32 in the layout of k_coarse_linv.
+constexpr int LB_T = 256;  // threads of the blocked-inversion kernels
+
+__host__ __device__ constexpr size_t linv_diag_smem(int b) { return sizeof(float2) * 2 * (size_t) b * b; }
+
+__global__ void __launch_bounds__(LB_T) k_linv_diag(CoarseArgs a, int b, float2* __restrict__ M, float2* __restrict__ Xd) {
+	extern __shared__ float2 lbs[];
+	int const n = a.nc, bw = a.bw, B = bw + 1;
+	int const k = blockIdx.x, r0 = k * b, rows = min(b, n - r0);
+	float2* Lk = lbs;          // [b][b]: L(r0 + i, r0 + i') for i' < i, 1 / L_ii on the diagonal
+	float2* Xk = lbs + b * b;  // [b][b]: X(r0 + i, r0 + j)
+	for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+		int const i = e / b, ip = e % b;
+		float2 v = make_float2(0.f, 0.f);
+		if (i < rows && ip <= i && i - ip <= bw) v = a.band[(long) (r0 + i) * B + (i - ip)];
+		Lk[e] = v;
+		Xk[e] = make_float2(0.f, 0.f);
+	}
+	__syncthreads();
+	for (int j = threadIdx.x; j < rows; j += blockDim.x)
+		for (int i = j; i < rows; i++) {
+			dfl s = {i == j ? 1.f : 0.f, 0.f};
+			for (int ip = max(j, i - bw); ip < i; ip++) {
+				float2 const l = Lk[i * b + ip], x = Xk[ip * b + j];
+				s = df_add(s, df_neg(df_mul({l.x, l.y}, {x.x, x.y})));
+			}
+			float2 const d = Lk[i * b + i];
+			dfl const x = df_mul(s, {d.x, d.y});
+			Xk[i * b + j] = make_float2(x.hi, x.lo);
+		}
+	__syncthreads();
+	for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+		int const i = e / b, j = e % b;
+		float2 const x = Xk[e];
+		Xd[(long) k * b * b + e] = x;
+		if (i < rows && j <= i) {
+			a.xl[xrow(r0 + i) + r0 + j] = x.x;
+			a.xu[xrow(n - 1 - (r0 + j)) + (i - j)] = x.x;
+		}
+	}
+	if (k == 0) return;
+	// M_k = -X_kk L_k,k-1: L(r0 + m, r0 - b + c) is in the band when m + b - c <= bw
+	for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+		int const i = e / b, c = e % b;
+		dfl s = {0.f, 0.f};
+		if (i < rows)
+			for (int m = 0; m <= i; m++) {
+				int const t = m + b - c;
+				if (t > bw) continue;
+				float2 const x = Xk[i * b + m], l = a.band[(long) (r0 + m) * B + t];
+				s = df_add(s, df_mul({x.x, x.y}, {l.x, l.y}));
+			}
+		M[(long) k * b * b + e] = make_float2(-s.hi, -s.lo);
+	}
+}
+
+// block row k of X for the columns of the earlier blocks (0 .. r0 - 1):
+// X(r0 + i, col) = sum_c M_k(i, c) X(r0 - b + c, col), the previous block row
+// read from Xw_prev (its columns before r0 - b) and Xd (its diagonal block)
+__global__ void __launch_bounds__(LB_T) k_linv_step(CoarseArgs a, int b, int k, const float2* __restrict__ M,
+                                                     const float2* __restrict__ Xd, const float2* __restrict__ Xw_prev,
+                                                     float2* __restrict__ Xw_cur) {
+	int const n = a.nc, r0 = k * b, rows = min(b, n - r0);
+	long const t = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (t >= (long) rows * r0) return;
+	int const i = (int) (t / r0), col = (int) (t % r0);
+	int const pb = r0 - b;  // first column of the previous diagonal block
+	const float2* Mi = M + ((long) k * b + i) * b;
+	dfl s = {0.f, 0.f};
+	for (int c = 0; c < b; c++) {
+		float2 const m = Mi[c];
+		float2 const x = col < pb ? Xw_prev[(long) c * n + col] : Xd[((long) (k - 1) * b + c) * b + (col - pb)];
+		s = df_add(s, df_mul({m.x, m.y}, {x.x, x.y}));
+	}
+	Xw_cur[(long) i * n + col] = make_float2(s.hi, s.lo);
+	a.xl[xrow(r0 + i) + col] = s.hi;
+	a.xu[xrow(n - 1 - col) + (r0 + i - col)] = s.hi;
+}
+
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner
 struct CgKernels {
 	void* hs64s;   // split-form K1 (with k_hs64_dir before it)

@@ -1507,6 +1507,7 @@ struct bfm_gpu_problem {
 	float2* aband;          // band A_c then L (double-float pairs)
 	double* diag0;          // the diagonal of A_c
 	float *xl, *xu;         // X = L^-1 and X^T by rows (FP32, padded rows)
+	float2 *lbm, *lbd, *lbw;  // blocked inversion: M_k, X_kk (nc_cap + COARSE_MAX_BW rows of bw), two block rows of X
 	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
 	int* coarse_err;
 	int coarse_grid;        // cooperative grid of k_coarse_apply (0: not sized yet, -1: none)
@@ -2008,9 +2009,10 @@ int build_aggregates(bfm_gpu_problem* P) {
 	}
 	if (!rc && nc > P->nc_cap) {
 		// (re)allocate for the larger coarse space (the band at the widest bandwidth)
-		void* old[] = {P->agg_ptr, P->agg_chunk, P->aband, P->diag0, P->rc, P->ayt, P->yc, P->xl, P->xu};
+		void* old[] = {P->agg_ptr, P->agg_chunk, P->aband, P->diag0, P->rc, P->ayt, P->yc, P->xl, P->xu, P->lbm, P->lbd, P->lbw};
 		for (void* q : old)
 			if (q) cudaFree(q);
+		P->lbm = P->lbd = P->lbw = nullptr;
 		P->agg_ptr = P->agg_chunk = nullptr;
 		P->aband = nullptr;
 		P->diag0 = nullptr;
@@ -2019,6 +2021,8 @@ int build_aggregates(bfm_gpu_problem* P) {
 		if (dalloc(&P->agg_ptr, na + 1) || dalloc(&P->agg_chunk, na + 1) ||
 		    dalloc(&P->aband, (long) nc * (COARSE_MAX_BW + 1)) || dalloc(&P->diag0, nc) || dalloc(&P->rc, nc + 4) ||
 		    dalloc(&P->ayt, nc + 4) || dalloc(&P->yc, nc) || dalloc(&P->xl, xrow(nc)) || dalloc(&P->xu, xrow(nc)) ||
+		    dalloc(&P->lbm, (long) (nc + COARSE_MAX_BW) * COARSE_MAX_BW) ||
+		    dalloc(&P->lbd, (long) (nc + COARSE_MAX_BW) * COARSE_MAX_BW) || dalloc(&P->lbw, 2l * COARSE_MAX_BW * nc) ||
 		    cudaMemsetAsync(P->rc, 0, (nc + 4) * sizeof(float2), st) != cudaSuccess ||
 		    cudaMemsetAsync(P->ayt, 0, (nc + 4) * sizeof(float2), st) != cudaSuccess)
 			rc = -1;
@@ -2143,7 +2147,24 @@ int coarse_setup(bfm_gpu_problem* P) {
 	// the padding of X's rows stays zero (the products read whole 16-byte groups)
 	CK(cudaMemsetAsync(P->xl, 0, xrow(P->nc) * sizeof(float), st));
 	CK(cudaMemsetAsync(P->xu, 0, xrow(P->nc) * sizeof(float), st));
-	k_coarse_linv<<<(P->nc + LINV_C * LINV_W - 1) / (LINV_C * LINV_W), 32 * LINV_W, linv_smem(P->abw), st>>>(ca);
+	char const* lv = getenv("BFM_GPU_COARSE_LINV_COLUMNS");
+	if (lv && lv[0] == '1') {
+		// the column-wise inversion (one dependent chain of nc steps per column)
+		k_coarse_linv<<<(P->nc + LINV_C * LINV_W - 1) / (LINV_C * LINV_W), 32 * LINV_W, linv_smem(P->abw), st>>>(ca);
+	}
+	else {
+		// by block rows of b = bw: nc / b dependent launches
+		int const b = P->abw > 0 ? P->abw : 1, nb = (P->nc + b - 1) / b;
+		CK(cudaFuncSetAttribute((const void*) k_linv_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                        (int) linv_diag_smem(COARSE_MAX_BW)));
+		k_linv_diag<<<nb, LB_T, linv_diag_smem(b), st>>>(ca, b, P->lbm, P->lbd);
+		for (int k = 1; k < nb; k++) {
+			long const outs = (long) std::min(b, P->nc - k * b) * (k * b);
+			k_linv_step<<<(int) ((outs + LB_T - 1) / LB_T), LB_T, 0, st>>>(ca, b, k, P->lbm, P->lbd,
+			                                                               P->lbw + (long) ((k + 1) & 1) * b * P->nc,
+			                                                               P->lbw + (long) (k & 1) * b * P->nc);
+		}
+	}
 	CK(cudaGetLastError());
 	P->coarse_ok = 1;
 	return 0;
@@ -2885,7 +2906,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y, P->ssor_d,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
 	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart,
-	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc};
+	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->lbm, P->lbd, P->lbw};
 	for (void* q : lb)
 		if (q) cudaFree(q);
 	if (P->ext && P->ext_free) P->ext_free(P->ext);

@@ -389,3 +389,22 @@ def test_sim_run_with_two_level(libbfm, name, monkeypatch):
         assert rel(h.effects(), x) < 1e-9
     finally:
         libbfm.bfm_gpu_set_opts(C.byref(bfm_gb300.default_opts()))
+
+
+def test_blocked_coarse_inverse_matches_columnwise(libbfm, monkeypatch):
+    """X = L^-1 of the coarse factor by block rows (the default) and column by
+    column (BFM_GPU_COARSE_LINV_COLUMNS=1): the same matrix up to the
+    summation order, so the same iterations (within 2) and solution."""
+    p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
+    out = []
+    for cols in ("0", "1"):
+        monkeypatch.setenv("BFM_GPU_COARSE_LINV_COLUMNS", cols)
+        prob = LN.DeviceProblem(p, precision=bfm_gb300.FP64_DF)
+        try:
+            s = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=1e-10)
+            assert s.status == 0
+            out.append((s.iterations, prob.solution()))
+        finally:
+            prob.close()
+    assert abs(out[0][0] - out[1][0]) <= 2, (out[0][0], out[1][0])
+    assert rel(out[0][1], out[1][1]) < 1e-9
