@@ -64,9 +64,9 @@ SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md")
                 3: (329_563_136, "profiles/spmv_df_hs_perforated_2048x512.md"),
                 1: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md"),
                 2: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md")}
-# the same for one launch of the SSOR sweep kernel, per precision (vector
-# layout), where a capture of the current kernel exists
-SSOR_TRAFFIC = {}
+# the same for one launch of the SSOR sweep kernel, per (precision, two-level
+# correction fused), where a capture of the current kernel exists
+SSOR_TRAFFIC = {(1, True): (269_338_112, "profiles/ssor2_fused_mixed_perforated_2048x512.md")}
 
 
 def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int, precision: int) -> int:
@@ -77,6 +77,15 @@ def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int, precision: int) -> int:
     written once (16 B)."""
     vec = 8 if precision in (1, 2) else 16
     return (n_blocks - n_nodes) * 20 + n_nodes * (16 + 2 * vec + 16)
+
+
+def algorithmic_bytes_coarse(n_nodes: int, n_chunks: int, x_bytes: int) -> int:
+    """The two-level correction's own reads inside the sweep kernel, per
+    application (the residual and z are counted with the sweeps): per node its
+    aggregate list entry and aggregate (4 B each) and its offset and free flags
+    (16 B); per restriction chunk its start (4 B) and 3 partial sums (24 B);
+    the rows of X and X^T (FP32, padded to 16 B)."""
+    return n_nodes * (4 + 4 + 16) + n_chunks * (4 + 24) + x_bytes
 
 
 def max_over_ranks(x: float, world: int) -> float:
@@ -240,16 +249,20 @@ def time_method(lib, D, stream, m, nets, warmup, steps, clocks=False):
     ncol = C.c_int(0)
     lib.bfm_gpu_problem_ordering(D.P, None, None, C.byref(ncol))
     t_pc, t_sw, persist = C.c_double(0.0), C.c_double(0.0), C.c_int(0)
+    n_coarse, n_chunks, x_bytes, fused = C.c_int64(0), C.c_int64(0), C.c_int64(0), C.c_int(0)
     if pc in SSOR_PCS:
         assert lib.bfm_gpu_problem_time_precond(D.P, 20, C.byref(t_pc), C.byref(t_sw), C.byref(persist)) == 0, \
             bfm_gb300.last_error()
+        lib.bfm_gpu_problem_coarse_info(D.P, C.byref(n_coarse), C.byref(n_chunks), C.byref(x_bytes), C.byref(fused))
     if pc in nets:
         lib.bfm_gpu_mpnn_use(None)
     return dict(ms=ms, steps=steps, warmup=warmup, iters=s.iterations, status=s.status, rel_res=s.rel_residual,
                 repl=s.replacements, ms_assemble=s.ms_assemble, ms_solve=s.ms_solve, n_blocks=s.n_blocks,
                 fallback=s.fallback, ms_spmv=t_spmv.value, ms_update=t_upd.value,
                 clocks=clk.summary() if clk else None, prec=prec, pc=pc, x=x, shape=shape.value, ncol=ncol.value,
-                ms_precond=t_pc.value, ms_sweeps=t_sw.value, persistent=persist.value)
+                ms_precond=t_pc.value, ms_sweeps=t_sw.value, persistent=persist.value,
+                coarse=dict(n_coarse=n_coarse.value, n_chunks=n_chunks.value, x_bytes=x_bytes.value,
+                            fused=fused.value))
 
 
 def run_gpu(args, rank: int, world: int):
@@ -512,15 +525,24 @@ def main():
                  "kernel": kernel, "spmv_shape": r["shape"], "algorithmic_bytes": bytes_spmv,
                  "kernel_ms": round(r["ms_spmv"], 5), "peak_source": peak_kind}
     if ssor:
-        # the dominant kernel of an SSOR iteration is the sweep kernel (timed
-        # here without its fused coarse stages)
+        # the dominant kernel of an SSOR iteration is the sweep kernel, as the
+        # solve launches it: with the two-level correction's stages inside when
+        # they are fused (then its bytes count too), else the sweeps alone
+        co = r["coarse"]
+        fused = bool(co["fused"]) and r["persistent"]
         b_pc = algorithmic_bytes_ssor(nb, p.n_nodes, r["prec"])
-        a_pc = b_pc / (r["ms_sweeps"] * 1e-3) / 1e9
-        tr = SSOR_TRAFFIC.get(r["prec"]) if args.workload == "perforated" and r["persistent"] else None
+        t_pc = r["ms_sweeps"]
+        if fused:
+            b_pc += algorithmic_bytes_coarse(p.n_nodes, co["n_chunks"], co["x_bytes"])
+            t_pc = r["ms_precond"]
+        a_pc = b_pc / (t_pc * 1e-3) / 1e9
+        tr = SSOR_TRAFFIC.get((r["prec"], fused)) if args.workload == "perforated" and r["persistent"] else None
         roof = {"bound": "hbm", "achieved": round(a_pc, 1), "peak": hbm, "unit": "GB/s", "frac": round(a_pc / hbm, 3),
                 "traffic": tr[0] if tr else None, "traffic_source": tr[1] if tr else None,
-                "kernel": "k_ssor_all" if r["persistent"] else "k_ssor_fwd + k_ssor_bwd",
-                "algorithmic_bytes": b_pc, "kernel_ms": round(r["ms_sweeps"], 5), "peak_source": peak_kind}
+                "kernel": ("k_ssor_all" + (" (two-level correction fused)" if fused else "")) if r["persistent"]
+                else "k_ssor_fwd + k_ssor_bwd",
+                "algorithmic_bytes": b_pc, "kernel_ms": round(t_pc, 5), "peak_source": peak_kind,
+                "coarse_dofs": co["n_coarse"]}
     else:
         roof = spmv_roof
     value = r["ms"] / world

@@ -79,6 +79,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_apply": (_i, [_vp, _vp, _vp, _i]),
     "bfm_gpu_problem_ordering": (_i, [_vp, _vp, _vp, _vp]),
     "bfm_gpu_problem_time_precond": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "bfm_gpu_problem_coarse_info": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "bfm_gpu_mpnn_param_count": (_i, []),
     "bfm_gpu_mpnn_create": (_i, [_P(_vp), C.c_uint]),
     "bfm_gpu_mpnn_destroy": (_i, [_vp]),

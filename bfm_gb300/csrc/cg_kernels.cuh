@@ -1460,6 +1460,16 @@ struct SsorArgs {
 	// finished before the last phase get their P yc term in the last one
 	int fuse;
 	CoarseArgs co;
+	// persistent kernel: at the start of each phase, thread 0 of each block
+	// asks the TMA unit to prefetch into L2 what the block's rows read in
+	// the next phase and what no phase writes (sliced-ELL blocks and
+	// columns, relaxation blocks, the coarse stages' rows of X), so those
+	// reads hit L2 after the grid barrier
+	int pf;
+	// TMA-staged persistent kernel (k_ssor_tma): slices per tile of each
+	// phase and the bytes of one ring stage
+	int spt[127];
+	int stage_bytes;
 };
 
 
@@ -2033,6 +2043,39 @@ __global__ void __launch_bounds__(CX_T) k_coarse_apply(CoarseArgs a) {
 	}
 }
 
+// bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+	if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// the inputs of phase ph of k_ssor_all that this block reads and no phase
+// writes: the rows it takes (the same grid-stride split as the sweeps, whole
+// slices: a block's rows start 32-aligned within the colour), and for the
+// fused coarse stages the rows of X and X^T it takes
+__device__ void ssor_prefetch_phase(const SsorArgs& a, int ph, int nc, int stride) {
+	bool const forward = ph < nc;
+	int const c = forward ? ph : 2 * nc - 2 - ph;
+	int const lo = a.off[c], hi = a.off[c + 1];
+	const float4* v = forward ? a.lv : a.uv;
+	const int* ci = forward ? a.lc : a.uc;
+	const int* ptr = forward ? a.lp : a.up;
+	for (int s0 = lo + blockIdx.x * (int) blockDim.x; s0 < hi; s0 += stride) {
+		int const e0 = min(s0 + (int) blockDim.x, hi);
+		int const sa = a.sbase[c] + ((s0 - lo) >> 5), sb = a.sbase[c] + ((e0 - lo + 31) >> 5);
+		int const k0 = __ldg(ptr + sa), k1 = __ldg(ptr + sb);
+		l2_prefetch(v + k0, 16u * (unsigned) (k1 - k0));
+		l2_prefetch(ci + k0, 4u * (unsigned) (k1 - k0));
+		l2_prefetch(reinterpret_cast<const float4*>(a.dinv) + s0, 16u * (unsigned) (e0 - s0));
+	}
+	if (!a.fuse) return;
+	CoarseArgs const& co = a.co;
+	if (ph == 2)
+		for (int i = blockIdx.x; i < co.nc; i += gridDim.x) l2_prefetch(co.xl + xrow(i), 4u * (unsigned) ((i + 4) & ~3));
+	else if (ph == 3)
+		for (int j = blockIdx.x; j < co.nc; j += gridDim.x)
+			l2_prefetch(co.xu + xrow(co.nc - 1 - j), 4u * (unsigned) ((co.nc - j + 3) & ~3));
+}
+
 template <int VT>
 __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 	if (a.st->done && !a.timing) return;
@@ -2049,6 +2092,7 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 		int const c = forward ? ph : 2 * nc - 2 - ph;
 		bool const final_rows = !forward || c == nc - 1;
 		int const lo = a.off[c], hi = a.off[c + 1];
+		if (a.pf && threadIdx.x == 0 && ph + 1 < 2 * nc - 1) ssor_prefetch_phase(a, ph + 1, nc, stride);
 		for (int i = lo + tid; i < hi; i += stride) {
 			dfl r0, r1;
 			double q0 = 0.0, q1 = 0.0;
@@ -2111,75 +2155,75 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 }
 
 // A_c = P^T A P in two deterministic stages.  One warp per chunk of
-// aggregate I: every lane keeps the 3x3 blocks of the 9 cells around I (slot
-// = cell offset), so the lanes' partial sums line up and are reduced in a
-// fixed order into the chunk's 81 values; then per aggregate and entry the
-// chunks in chunk order.  A neighbour outside those 9 cells sets *err (the
+// aggregate I: for each of the 9 cells around I (slot = cell offset) every
+// lane sums its nodes' 3x3 blocks coupling to that cell, so the lanes'
+// partial sums line up and are reduced in a fixed order into the chunk's 81
+// values; then per aggregate and entry the chunks in chunk order.  A neighbour outside those 9 cells sets *err (the
 // caller then drops the coarse correction).
 __global__ void k_coarse_ac(CoarseArgs a) {
 	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if (q >= a.nchunk) return;
 	int cx, cy;
 	cell_xy(a.chunk_agg[q], a.gx, a.gy, a.xfast, cx, cy);
-	double acc[9][9];
-	for (int s = 0; s < 9; s++)
-		for (int t = 0; t < 9; t++) acc[s][t] = 0.0;
-	for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
-		int const i = a.agg_nodes[k];
-		float4 const pi = a.pnode[i];
-		double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
-		// the FP32 operator in difference form, (A g)_i = S_i g_i + sum_j A_ij (g_j - g_i):
-		// its diagonal block is S_i - sum_{j != i} A_ij
-		double deff[4] = {0.0, 0.0, 0.0, 0.0};
-		if (!a.vals64) {
-			float4 const sr = reinterpret_cast<const float4*>(a.corr32)[i];
-			deff[0] = sr.x; deff[1] = sr.y; deff[2] = sr.z; deff[3] = sr.w;
+	// one neighbour slot at a time (9 accumulators per lane instead of 81):
+	// each slot's sums take the same terms in the same order
+	for (int slot = 0; slot < 9; slot++) {
+		double acc[9];
+#pragma unroll
+		for (int t = 0; t < 9; t++) acc[t] = 0.0;
+		for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
+			int const i = a.agg_nodes[k];
+			float4 const pi = a.pnode[i];
+			double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
 			for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
-				if (a.cols[e] == i) continue;
-				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
-				deff[0] -= v.x; deff[1] -= v.y; deff[2] -= v.z; deff[3] -= v.w;
+				int const j = a.cols[e];
+				int jx, jy;
+				cell_xy(a.agg[j], a.gx, a.gy, a.xfast, jx, jy);
+				int const ox = jx - cx, oy = jy - cy;
+				if (ox < -1 || ox > 1 || oy < -1 || oy > 1) {
+					if (slot == 0) atomicOr(a.err, 1);
+					continue;
+				}
+				if ((oy + 1) * 3 + (ox + 1) != slot) continue;
+				float4 const pj = a.pnode[j];
+				double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
+				double m[4];
+				if (a.vals64) {
+					for (int t = 0; t < 4; t++) m[t] = a.vals64[4l * e + t];
+				}
+				else if (j == i) {
+					// the FP32 operator in difference form, (A g)_i = S_i g_i + sum_j A_ij (g_j - g_i):
+					// its diagonal block is S_i - sum_{j != i} A_ij
+					float4 const sr = reinterpret_cast<const float4*>(a.corr32)[i];
+					m[0] = sr.x; m[1] = sr.y; m[2] = sr.z; m[3] = sr.w;
+					for (int f = a.row_ptr[i]; f < a.row_ptr[i + 1]; f++) {
+						if (a.cols[f] == i) continue;
+						float4 const v = reinterpret_cast<const float4*>(a.vals32)[f];
+						m[0] -= v.x; m[1] -= v.y; m[2] -= v.z; m[3] -= v.w;
+					}
+				}
+				else {
+					float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
+					m[0] = v.x; m[1] = v.y; m[2] = v.z; m[3] = v.w;
+				}
+				// A P_j (2x3), then P_i^T (3x2) times it
+				double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
+				                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};
+				double const pt[3][2] = {{fi0, 0.0}, {0.0, fi1}, {-fi0 * dyi, fi1 * dxi}};
+#pragma unroll
+				for (int u = 0; u < 3; u++)
+#pragma unroll
+					for (int v = 0; v < 3; v++) acc[3 * u + v] += pt[u][0] * ap[0][v] + pt[u][1] * ap[1][v];
 			}
 		}
-		for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
-			int const j = a.cols[e];
-			int jx, jy;
-			cell_xy(a.agg[j], a.gx, a.gy, a.xfast, jx, jy);
-			int const ox = jx - cx, oy = jy - cy;
-			if (ox < -1 || ox > 1 || oy < -1 || oy > 1) {
-				atomicOr(a.err, 1);
-				continue;
-			}
-			int const slot = (oy + 1) * 3 + (ox + 1);
-			float4 const pj = a.pnode[j];
-			double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
-			double m[4];
-			if (a.vals64) {
-				for (int t = 0; t < 4; t++) m[t] = a.vals64[4l * e + t];
-			}
-			else if (j == i) {
-				for (int t = 0; t < 4; t++) m[t] = deff[t];
-			}
-			else {
-				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
-				m[0] = v.x; m[1] = v.y; m[2] = v.z; m[3] = v.w;
-			}
-			// A P_j (2x3), then P_i^T (3x2) times it
-			double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
-			                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};
-			double const pt[3][2] = {{fi0, 0.0}, {0.0, fi1}, {-fi0 * dyi, fi1 * dxi}};
 #pragma unroll
-			for (int u = 0; u < 3; u++)
-#pragma unroll
-				for (int v = 0; v < 3; v++) acc[slot][3 * u + v] += pt[u][0] * ap[0][v] + pt[u][1] * ap[1][v];
-		}
-	}
-	for (int s = 0; s < 9; s++)
 		for (int t = 0; t < 9; t++) {
-			double x = acc[s][t];
+			double x = acc[t];
 #pragma unroll
 			for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-			if (lane == 0) a.part[81l * q + 9 * s + t] = x;
+			if (lane == 0) a.part[81l * q + 9 * slot + t] = x;
 		}
+	}
 }
 
 // The chunks' sums per aggregate into the lower band of A_c, each entry the
@@ -2458,6 +2502,35 @@ __global__ void __launch_bounds__(LB_T) k_linv_step(CoarseArgs a, int b, int k, 
 	Xw_cur[(long) i * n + col] = make_float2(s.hi, s.lo);
 	a.xl[xrow(r0 + i) + col] = s.hi;
 	a.xu[xrow(n - 1 - col) + (r0 + i - col)] = s.hi;
+}
+
+// k_linv_step for every block row in one cooperative launch: a grid barrier
+// between block rows instead of a launch each (bounded waits: a timeout sets
+// *a.berr and the blocks stop)
+__global__ void __launch_bounds__(LB_T) k_linv_all(CoarseArgs a, int b, const float2* __restrict__ M,
+                                                    const float2* __restrict__ Xd, float2* __restrict__ Xw) {
+	grid_barrier_init(a.bar);
+	int const n = a.nc, nb = (n + b - 1) / b;
+	long const stride = (long) gridDim.x * blockDim.x;
+	for (int k = 1; k < nb; k++) {
+		int const r0 = k * b, rows = min(b, n - r0), pb = r0 - b;
+		const float2* prev = Xw + (long) ((k + 1) & 1) * b * n;
+		float2* cur = Xw + (long) (k & 1) * b * n;
+		for (long t = blockIdx.x * (long) blockDim.x + threadIdx.x; t < (long) rows * r0; t += stride) {
+			int const i = (int) (t / r0), col = (int) (t % r0);
+			const float2* Mi = M + ((long) k * b + i) * b;
+			dfl s = {0.f, 0.f};
+			for (int c = 0; c < b; c++) {
+				float2 const m = Mi[c];
+				float2 const x = col < pb ? __ldcg(prev + (long) c * n + col) : Xd[((long) (k - 1) * b + c) * b + (col - pb)];
+				s = df_add(s, df_mul({m.x, m.y}, {x.x, x.y}));
+			}
+			__stcg(cur + (long) i * n + col, make_float2(s.hi, s.lo));
+			a.xl[xrow(r0 + i) + col] = s.hi;
+			a.xu[xrow(n - 1 - col) + (r0 + i - col)] = s.hi;
+		}
+		if (k + 1 < nb && !grid_barrier(a.bar, a.berr, a.polls)) return;
+	}
 }
 
 // kernels of one SpMV shape (lanes per row), for the graph builder and the autotuner

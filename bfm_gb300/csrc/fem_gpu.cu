@@ -341,6 +341,32 @@ __global__ void k_sell_width(int ns, SellMap m, const int* __restrict__ row_ptr,
 	}
 }
 
+// the widest slice of colour blockIdx.x, lower- and higher-colour blocks (in blocks)
+__global__ void k_sell_wmax(SellMap m, const int* __restrict__ lw, const int* __restrict__ uw, int* __restrict__ wm) {
+	int const c = blockIdx.x;
+	int l = 0, u = 0;
+	for (int s = m.sbase[c] + threadIdx.x; s < m.sbase[c + 1]; s += blockDim.x) {
+		l = max(l, lw[s]);
+		u = max(u, uw[s]);
+	}
+	l = __reduce_max_sync(0xffffffffu, l);
+	u = __reduce_max_sync(0xffffffffu, u);
+	__shared__ int sl[32], su[32];
+	if ((threadIdx.x & 31) == 0) {
+		sl[threadIdx.x >> 5] = l;
+		su[threadIdx.x >> 5] = u;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int w = 1; w < (int) (blockDim.x >> 5); w++) {
+			l = max(l, sl[w]);
+			u = max(u, su[w]);
+		}
+		wm[2 * c] = l / 32;
+		wm[2 * c + 1] = u / 32;
+	}
+}
+
 // copy each row's lower- and higher-colour blocks (ascending columns, as in
 // the CSR rows) into its lane of the slice; pad with column -1
 __global__ void k_sell_fill(int ns, SellMap m, const int* __restrict__ row_ptr, const int* __restrict__ cols,
@@ -1364,6 +1390,7 @@ __global__ void k_apply64(int N, const int* __restrict__ row_ptr, const int* __r
 }  // namespace
 
 #include "cg_kernels.cuh"
+#include "ssor_tma.cuh"
 
 namespace {
 
@@ -1485,11 +1512,16 @@ struct bfm_gpu_problem {
 	int sl_n;            // slices
 	int sl_base[65];     // first slice of each colour
 	int *sl_lw, *sl_uw, *sl_lp, *sl_up;  // widths and slice offsets (n + 1 each)
+	int* sl_wm;          // device copy of sl_wmax
 	long sl_lcap, sl_ucap;
 	float4 *sl_lv, *sl_uv;
 	int *sl_lc, *sl_uc;
+	int sl_wmax[64][2];  // widest slice of each colour: lower-colour, higher-colour blocks
 	unsigned* ssor_bar;  // grid barrier words of the persistent sweep kernel
 	int ssor_grid;       // its cooperative grid (0: the per-phase kernels)
+	int tma_grid;        // the TMA-staged sweep kernel's grid (one block per SM; 0: not used)
+	int tma_smem_max;    // dynamic shared memory a block of it may have
+	int linv_grid;       // cooperative grid of k_linv_all (0: not sized yet, -1: per-row launches)
 	long polls;          // polls per grid barrier before it gives up (the solve graph's)
 
 	// two-level SSOR: aggregates are the cells of an agx x agy grid over the
@@ -1976,10 +2008,18 @@ int build_aggregates(bfm_gpu_problem* P) {
 			free(next);
 		}
 	}
-	// chunks of at most COARSE_CHUNK nodes per aggregate, for the parallel reductions
+	// chunks for the parallel reductions: runs of consecutive nodes of one
+	// aggregate, at most COARSE_CHUNK each (a chunk's nodes are the rows
+	// agg_nodes[chunk start] onwards)
+	auto new_chunk = [&](int I, int k) { return k == ptr[I] || nodes[k] != nodes[k - 1] + 1; };
 	int nchunk = 0;
 	if (!rc)
-		for (int I = 0; I < na; I++) nchunk += (ptr[I + 1] - ptr[I] + COARSE_CHUNK - 1) / COARSE_CHUNK;
+		for (int I = 0; I < na; I++)
+			for (int k = ptr[I], len = 0; k < ptr[I + 1]; k++, len++)
+				if (new_chunk(I, k) || len == COARSE_CHUNK) {
+					nchunk++;
+					len = 0;
+				}
 	int* cst = (int*) malloc((nchunk + 1) * sizeof(int));
 	int* cag = (int*) malloc((nchunk + 1) * sizeof(int));
 	int* ach = (int*) malloc((na + 1) * sizeof(int));
@@ -1988,11 +2028,13 @@ int build_aggregates(bfm_gpu_problem* P) {
 		int q = 0;
 		for (int I = 0; I < na; I++) {
 			ach[I] = q;
-			for (int k = ptr[I]; k < ptr[I + 1]; k += COARSE_CHUNK) {
-				cst[q] = k;
-				cag[q] = I;
-				q++;
-			}
+			for (int k = ptr[I], len = 0; k < ptr[I + 1]; k++, len++)
+				if (new_chunk(I, k) || len == COARSE_CHUNK) {
+					cst[q] = k;
+					cag[q] = I;
+					q++;
+					len = 0;
+				}
 		}
 		ach[na] = q;
 		cst[q] = ptr[na];
@@ -2095,9 +2137,12 @@ int build_sell(bfm_gpu_problem* P) {
 	int const warps_tpb = TPB / 32;
 	k_sell_width<<<(ns + warps_tpb - 1) / warps_tpb, TPB, 0, st>>>(ns, m, P->row_ptr, P->cols, P->sl_lw, P->sl_uw);
 	if (scan(P, P->sl_lw, P->sl_lp, ns) || scan(P, P->sl_uw, P->sl_up, ns)) return -1;
+	if (!P->sl_wm && dalloc(&P->sl_wm, 2 * 64)) return -1;
+	k_sell_wmax<<<nc, TPB, 0, st>>>(m, P->sl_lw, P->sl_uw, P->sl_wm);
 	int tot[2] = {0, 0};
 	CK(cudaMemcpyAsync(&tot[0], P->sl_lp + ns, sizeof(int), cudaMemcpyDeviceToHost, st));
 	CK(cudaMemcpyAsync(&tot[1], P->sl_up + ns, sizeof(int), cudaMemcpyDeviceToHost, st));
+	CK(cudaMemcpyAsync(P->sl_wmax, P->sl_wm, 2 * nc * sizeof(int), cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 	if (tot[0] > P->sl_lcap) {
 		if (P->sl_lv) cudaFree(P->sl_lv);
@@ -2158,12 +2203,37 @@ int coarse_setup(bfm_gpu_problem* P) {
 		CK(cudaFuncSetAttribute((const void*) k_linv_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                        (int) linv_diag_smem(COARSE_MAX_BW)));
 		k_linv_diag<<<nb, LB_T, linv_diag_smem(b), st>>>(ca, b, P->lbm, P->lbd);
-		for (int k = 1; k < nb; k++) {
-			long const outs = (long) std::min(b, P->nc - k * b) * (k * b);
-			k_linv_step<<<(int) ((outs + LB_T - 1) / LB_T), LB_T, 0, st>>>(ca, b, k, P->lbm, P->lbd,
-			                                                               P->lbw + (long) ((k + 1) & 1) * b * P->nc,
-			                                                               P->lbw + (long) (k & 1) * b * P->nc);
+		// the block rows in one cooperative launch (BFM_GPU_COARSE_LINV_LAUNCHES=1: a launch each)
+		char const* ll = getenv("BFM_GPU_COARSE_LINV_LAUNCHES");
+		bool one = false;
+		if (!(ll && ll[0] == '1') && P->ssor_bar && nb > 1) {
+			if (!P->linv_grid) {
+				int nbk = 0;
+				P->linv_grid = -1;
+				if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbk, (const void*) k_linv_all, LB_T, 0) == cudaSuccess &&
+				    nbk > 0)
+					P->linv_grid = num_sms() * nbk;
+				cudaGetLastError();
+			}
+			if (P->linv_grid > 0) {
+				CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st));
+				float2* lbw = P->lbw;
+				void* pa[] = {&ca, (void*) &b, (void*) &P->lbm, (void*) &P->lbd, (void*) &lbw};
+				one = cudaLaunchCooperativeKernel((const void*) k_linv_all, dim3(P->linv_grid), dim3(LB_T), pa, 0, st) ==
+				      cudaSuccess;
+				if (!one) {
+					cudaGetLastError();
+					P->linv_grid = -1;
+				}
+			}
 		}
+		if (!one)
+			for (int k = 1; k < nb; k++) {
+				long const outs = (long) std::min(b, P->nc - k * b) * (k * b);
+				k_linv_step<<<(int) ((outs + LB_T - 1) / LB_T), LB_T, 0, st>>>(ca, b, k, P->lbm, P->lbd,
+				                                                               P->lbw + (long) ((k + 1) & 1) * b * P->nc,
+				                                                               P->lbw + (long) (k & 1) * b * P->nc);
+			}
 	}
 	CK(cudaGetLastError());
 	P->coarse_ok = 1;
@@ -2244,11 +2314,11 @@ DfArgs df_args(bfm_gpu_problem* P, const bfm_gpu_opts_t* o) {
 }
 
 int add_node(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, void* fn, int grid, void** params,
-             size_t smem = 0) {
+             size_t smem = 0, int block = TPB) {
 	cudaKernelNodeParams kp = {};
 	kp.func = fn;
 	kp.gridDim = dim3(grid);
-	kp.blockDim = dim3(TPB);
+	kp.blockDim = dim3(block);
 	kp.sharedMemBytes = (unsigned) smem;
 	kp.kernelParams = params;
 	CK(cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp));
@@ -2298,6 +2368,34 @@ SsorArgs ssor_args(bfm_gpu_problem* P, const void* r, void* z) {
 bool fuse_coarse(bfm_gpu_problem* P) {
 	char const* e = getenv("BFM_GPU_COARSE_SEPARATE");
 	return P->ssor_grid > 0 && P->ncol >= 3 && !(e && e[0] == '1');
+}
+
+// Tiling of the TMA-staged sweep kernel for the current colouring: the ring
+// takes what the block's shared memory leaves after the coarse vector (fused
+// two-level form); each phase's tiles hold as many whole slices as a stage
+// fits at the colour's widest slice.  Returns the dynamic shared memory of a
+// block, 0 when the kernel cannot be used here.
+size_t tma_tiling(bfm_gpu_problem* P, SsorArgs& a, bool fused) {
+	if (P->tma_grid <= 0 || P->ncol <= 0 || P->ncol > 63) return 0;
+	size_t const vec = fused ? (((size_t) P->nc + 4) * sizeof(float2) + 127) / 128 * 128 : 0;
+	if ((size_t) P->tma_smem_max < vec + ST_NS * 4096) return 0;
+	int const stage = (int) ((((size_t) P->tma_smem_max - vec) / ST_NS) / 128 * 128);
+	int const nc = P->ncol;
+	for (int ph = 0; ph < 2 * nc - 1; ph++) {
+		bool const fwd = ph < nc;
+		int const c = fwd ? ph : 2 * nc - 2 - ph;
+		int const w = P->sl_wmax[c][fwd ? 0 : 1];
+		int spt = (stage - ST_HDR) / (32 * (20 * w + 16));
+		if (spt > ST_MAX_SPT) spt = ST_MAX_SPT;
+		if (spt < 1) return 0;
+		a.spt[ph] = spt;
+	}
+	a.stage_bytes = stage;
+	return (size_t) stage * ST_NS + vec;
+}
+
+void* ssor_tma_kernel(int vt) {
+	return vt == VT_DF ? (void*) k_ssor_tma<VT_DF> : vt == VT_F32 ? (void*) k_ssor_tma<VT_F32> : (void*) k_ssor_tma<VT_F64>;
 }
 
 // the sweep kernels of a vector layout (VT_*)
@@ -2360,11 +2458,39 @@ int add_ssor(bfm_gpu_problem* P, cudaGraph_t g, cudaGraphNode_t* last, const cud
 		base.pnode = P->pnode;
 		base.yc = P->yc;
 	}
+	if (P->tma_grid > 0) {
+		// one cooperative launch, operands staged by TMA
+		SsorArgs a = base;
+		a.ncol = nc;
+		for (int c = 0; c <= nc && c < 65; c++) a.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
+		a.bar = P->ssor_bar;
+		a.first_acc = 1;
+		a.final_phase = 1;
+		a.mode = mode;
+		size_t const smem = tma_tiling(P, a, a.fuse);
+		if (smem > 0) {
+			void* pa[1] = {&a};
+			cudaGraphNode_t n;
+			if (add_node(g, &n, dep, ssor_tma_kernel(vt), P->tma_grid, pa, smem, ST_THREADS)) return -1;
+			cudaLaunchAttributeValue v;
+			memset(&v, 0, sizeof v);
+			v.cooperative = 1;
+			if (cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v) == cudaSuccess) {
+				*last = n;
+				return 0;
+			}
+			cudaGetLastError();
+			cudaGraphDestroyNode(n);
+			P->tma_grid = 0;
+		}
+	}
 	if (P->ssor_grid > 0) {
 		// one cooperative launch for every phase
 		SsorArgs a = base;
 		a.ncol = nc;
 		for (int c = 0; c <= nc && c < 65; c++) a.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
+		char const* e = getenv("BFM_GPU_SSOR_PREFETCH");  // 0: no L2 prefetch of the next phase
+		a.pf = !(e && e[0] == '0');
 		a.bar = P->ssor_bar;
 		a.first_acc = 1;
 		a.final_phase = 1;
@@ -2713,6 +2839,24 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 				k_coarse_xt<<<P->nc, CX_T, 0, st>>>(ca);
 			}
 		}
+		if (P->tma_grid > 0) {
+			SsorArgs a = base;
+			a.ncol = nc;
+			for (int c = 0; c <= nc && c < 65; c++) a.off[c] = P->ncol > 0 ? P->col_off[c] : 0;
+			a.bar = P->ssor_bar;
+			a.first_acc = a.final_phase = 1;
+			if (fused && with_coarse) {
+				a.fuse = 1;
+				a.co = ca;
+			}
+			size_t const smem = tma_tiling(P, a, a.fuse);
+			if (smem > 0) {
+				void* pa[1] = {&a};
+				cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
+				cudaLaunchCooperativeKernel(ssor_tma_kernel(vt), dim3(P->tma_grid), dim3(ST_THREADS), pa, smem, st);
+				return;
+			}
+		}
 		if (P->ssor_grid > 0) {
 			SsorArgs a = base;
 			a.ncol = nc;
@@ -2906,7 +3050,8 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y, P->ssor_d,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
 	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart,
-	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->lbm, P->lbd, P->lbw};
+	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->sl_wm, P->lbm, P->lbd,
+	              P->lbw};
 	for (void* q : lb)
 		if (q) cudaFree(q);
 	if (P->ext && P->ext_free) P->ext_free(P->ext);
@@ -3245,6 +3390,26 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 				P->ssor_grid = num_sms() * nb;
 			}
 			cudaGetLastError();
+			// the TMA-staged sweep kernel: one block of ST_THREADS per SM with
+			// (nearly) all of the SM's shared memory (BFM_GPU_SSOR_TMA=0: not used)
+			char const* tma = getenv("BFM_GPU_SSOR_TMA");
+			int optin = 0;
+			P->tma_grid = 0;
+			if (coop && !(tma && tma[0] == '0') &&
+			    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess) {
+				int const smem = optin - 2048;  // the kernel's static shared memory and a margin
+				bool ok = smem > 64 * 1024;
+				for (void* f : {(void*) k_ssor_tma<VT_F64>, (void*) k_ssor_tma<VT_DF>, (void*) k_ssor_tma<VT_F32>}) {
+					int nb2 = 0;
+					ok = ok && cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess &&
+					     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, f, ST_THREADS, smem) == cudaSuccess && nb2 >= 1;
+				}
+				if (ok) {
+					P->tma_grid = num_sms();
+					P->tma_smem_max = smem;
+				}
+				cudaGetLastError();
+			}
 		}
 	}
 	// 3. Dirichlet bookkeeping, conditions in order (node -> edge incidence
@@ -3571,6 +3736,16 @@ int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* P, int reps, double* ms, dou
 	if (!P->assembled) return fail("assemble first");
 	if (persistent) *persistent = P->ssor_grid > 0;
 	return time_ssor(P, reps > 0 ? reps : 1, ms, ms_sweeps);
+}
+
+int bfm_gpu_problem_coarse_info(bfm_gpu_problem_t* P, int64_t* n_coarse, int64_t* n_chunks, int64_t* x_bytes, int* fused) {
+	g_err[0] = 0;
+	bool const on = coarse_pc(P->precond) && P->coarse_ok;
+	if (n_coarse) *n_coarse = on ? P->nc : 0;
+	if (n_chunks) *n_chunks = on ? P->nchunk : 0;
+	if (x_bytes) *x_bytes = on ? 2 * (int64_t) xrow(P->nc) * (int64_t) sizeof(float) : 0;
+	if (fused) *fused = on && fuse_coarse(P);
+	return 0;
 }
 
 int bfm_gpu_problem_autotune(bfm_gpu_problem_t* P, int* lanes_per_row) {

@@ -1,0 +1,477 @@
+// One application of the multicolour block SSOR preconditioner (and of the
+// two-level form's coarse correction) as ONE persistent kernel per SM whose
+// operands stream through shared memory by TMA bulk copies.
+//
+// The sweeps read, per phase (one colour, forward or backward), the phase's
+// sliced-ELL blocks and column indices and the rows' relaxation blocks:
+// nothing any phase writes.  So a producer warp per block streams them,
+// tile by tile, into a ring of shared-memory stages (cp.async.bulk, one
+// mbarrier per stage for "full" and one for "empty") as far ahead as the
+// ring allows -- across the grid barriers that separate the phases -- while
+// the block's consumer warps gather the neighbours' sweep values (the only
+// operands a phase depends on) from L2 and do the arithmetic.  A phase then
+// costs about its bytes at HBM bandwidth instead of a chain of dependent
+// loads per row.
+//
+// Layout of one stage (a tile: up to spt consecutive slices of 32 rows of
+// the block's share of the phase's colour):
+//   [0, 128)            entry offset of each slice relative to the tile
+//                       (spt + 1 ints; the last is the tile's entry count E)
+//   [128, 128 + 16 E)   the blocks (float4), column-major per slice
+//   [.., + 4 E)         their columns (int, -1 = padding)
+//   [.., + 16 rows)     the rows' FP32 relaxation block inverses
+//
+// Work split: block b takes slices [S b / G, S (b + 1) / G) of each colour
+// (S slices, G blocks); within a tile, slice j goes to consumer warp
+// (k + j) mod 31, k the number of slices the block has had before the tile,
+// so consecutive tiles fill all warps.  Lane = row within the slice.
+//
+// Two-level correction (at least 3 colours): its stages run between the
+// sweeps' own grid barriers -- restriction of the block's chunks at the end
+// of phase 0; at the start of phase 1 every block sums all chunk partials
+// into r_c in shared memory (the same sums in the same order in every block)
+// and forms its rows of y_t = X r_c; at the start of phase 2 it stages y_t
+// and forms its rows of y_c = X^T y_t.  The backward phases (from phase nc
+// on) add P y_c where they store z; the rows of colour nc - 1, stored in
+// phase nc - 1, get it at the start of phase nc when that is phase 3.
+//
+// Every wait is bounded: grid barriers by the polls argument (a timeout
+// sets the solve's error flag), the mbarrier waits by MBAR_POLLS.  A block
+// that gave up still drains the ring (waits for every copy it issued) so no
+// copy lands in the shared memory of an exited block.
+#pragma once
+
+#include "cg_kernels.cuh"
+
+namespace {
+
+constexpr int ST_THREADS = 1024;            // one block per SM
+constexpr int ST_CW = ST_THREADS / 32 - 1;  // consumer warps; warp ST_CW produces
+constexpr int ST_NS = 4;                    // ring stages
+constexpr int ST_HDR = 128;                 // header bytes of a stage
+constexpr int ST_MAX_SPT = 31;              // slices per tile (header: spt + 1 ints)
+constexpr long MBAR_POLLS = 1l << 26;       // tries per mbarrier wait before giving up
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned) __cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+	unsigned ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(bar), "r"(parity)
+	    : "memory");
+	return ok != 0;
+}
+// wait for the phase of the given parity to complete; false after MBAR_POLLS tries
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+	for (long k = 0; k < MBAR_POLLS; k++)
+		if (mbar_try(bar, parity)) return true;
+	return false;
+}
+// bulk copy global -> this block's shared memory, completing on mbarrier `bar`
+// (addresses 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+	             "l"(src), "r"(bytes), "r"(bar)
+	             : "memory");
+}
+// the consumer warps only (named barrier 1)
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(ST_CW * 32) : "memory"); }
+
+// Grid barrier of the consumer warps (the producer streams on): as
+// grid_barrier, with the block-level synchronisation on named barrier 1.
+// Every consumer thread calls it; a block that has given up (*dead: a wait
+// of one of its threads ran out) does not arrive and returns false, as do
+// all threads of a block whose wait here runs out -- so the result is the
+// same in every thread of the block
+__device__ bool st_grid_barrier(unsigned* bar, int* err, long polls, volatile int* dead) {
+	__shared__ int ok;
+	consumers_sync();
+	if (threadIdx.x == 0 && *dead) ok = 0;
+	else if (threadIdx.x == 0) {
+		unsigned* count = bar;
+		unsigned* gen = bar + 32;
+		unsigned const target = bar_expect() + 1;
+		int good = 1;
+		unsigned old;
+		asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
+		if (old == gridDim.x - 1) {
+			asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(count) : "memory");
+			asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(target) : "memory");
+		}
+		else {
+			long spins = 0;
+			unsigned cur;
+			while (true) {
+				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gen) : "memory");
+				if (cur == target) break;
+				++spins;
+				if (spins > polls || ((spins & 1023) == 0 && *(volatile int*) err != 0)) {
+					atomicExch(err, 1);
+					good = 0;
+					break;
+				}
+			}
+		}
+		bar_expect() = target;
+		ok = good;
+		if (!good) *dead = 1;
+	}
+	consumers_sync();
+	return ok;
+}
+
+// the block's share [lo, hi) of n items
+__device__ __forceinline__ void st_share(int n, int& lo, int& hi) {
+	lo = (int) ((long) n * blockIdx.x / gridDim.x);
+	hi = (int) ((long) n * (blockIdx.x + 1) / gridDim.x);
+}
+
+// the block's rows of a padded triangle (row i has i + 1 entries, xrow(i)
+// its start): equal shares of the stored floats
+__device__ __forceinline__ void st_tri_share(int n, int& lo, int& hi) {
+	long const tot = xrow(n);
+	auto first = [&](long target) {  // smallest i with xrow(i) >= target
+		int a = 0, b = n;
+		while (a < b) {
+			int const m = (a + b) >> 1;
+			if (xrow(m) < target) a = m + 1;
+			else b = m;
+		}
+		return a;
+	};
+	lo = first(tot * blockIdx.x / gridDim.x);
+	hi = first(tot * (blockIdx.x + 1) / gridDim.x);
+}
+
+// one warp: the dot product of a padded FP32 triangle row (len entries,
+// groups of 4) with a double-float vector in shared memory; lanes take
+// groups lane, lane + 32, .. (4 in flight), then a fixed shuffle tree
+__device__ __forceinline__ dfl st_row_dot(const float* __restrict__ row, int len, const float2* v, int lane) {
+	int const ng = (len + 3) >> 2;
+	const float4* r4 = reinterpret_cast<const float4*>(row);
+	dfl s = {0.f, 0.f};
+	for (int g0 = lane; g0 < ng; g0 += 128) {
+		float4 x[4];
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			int const g = g0 + 32 * u;
+			x[u] = g < ng ? __ldcs(r4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+#pragma unroll
+		for (int u = 0; u < 4; u++) {
+			int const g = g0 + 32 * u;
+			if (g >= ng) continue;
+			float2 const a = v[4 * g], b = v[4 * g + 1], c = v[4 * g + 2], d = v[4 * g + 3];
+			s = df_add(s, df_mul_f(x[u].x, {a.x, a.y}));
+			s = df_add(s, df_mul_f(x[u].y, {b.x, b.y}));
+			s = df_add(s, df_mul_f(x[u].z, {c.x, c.y}));
+			s = df_add(s, df_mul_f(x[u].w, {d.x, d.y}));
+		}
+	}
+#pragma unroll
+	for (int o = 16; o; o >>= 1) s = df_add(s, {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+	return s;
+}
+
+// restriction of one chunk (its nodes: the consecutive rows row0 ..
+// row0 + len - 1, len <= COARSE_CHUNK): lane l takes rows l, l + 32, ..
+// (all loads first), then double-float sums in that order and a fixed
+// shuffle tree; the chunk's 3 sums to part[3 q ..]
+template <int VT>
+__device__ __forceinline__ void st_restrict_chunk(const CoarseArgs& co, const void* r, int q, int lane) {
+	constexpr int PER = COARSE_CHUNK / 32;
+	int const k0 = co.chunk_start[q], len = co.chunk_start[q + 1] - k0;
+	int const row0 = co.agg_nodes[k0];
+	dfl r0[PER], r1[PER];
+	float4 pq[PER];
+#pragma unroll
+	for (int u = 0; u < PER; u++) {
+		int const k = lane + 32 * u;
+		double q0, q1;
+		r0[u] = r1[u] = {0.f, 0.f};
+		pq[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+		if (k < len) {
+			ssor_ld_r<VT>(r, row0 + k, r0[u], r1[u], q0, q1);
+			pq[u] = co.pnode[row0 + k];
+		}
+	}
+	dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+#pragma unroll
+	for (int u = 0; u < PER; u++) {
+		if (lane + 32 * u >= len) continue;
+		dfl const x0 = pq[u].z == 0.f ? dfl{0.f, 0.f} : r0[u];
+		dfl const x1 = pq[u].w == 0.f ? dfl{0.f, 0.f} : r1[u];
+		s0 = df_add(s0, x0);
+		s1 = df_add(s1, x1);
+		s2 = df_add(s2, df_add(df_mul_f(-pq[u].y, x0), df_mul_f(pq[u].x, x1)));
+	}
+#pragma unroll
+	for (int o = 16; o; o >>= 1) {
+		s0 = df_add(s0, {__shfl_xor_sync(0xffffffffu, s0.hi, o), __shfl_xor_sync(0xffffffffu, s0.lo, o)});
+		s1 = df_add(s1, {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)});
+		s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
+	}
+	if (lane == 0) {
+		co.part[3l * q] = df_dbl(s0);
+		co.part[3l * q + 1] = df_dbl(s1);
+		co.part[3l * q + 2] = df_dbl(s2);
+	}
+}
+
+// sum of A_ij y_j over the staged blocks of one row: w blocks at stride 32
+// in shared memory, 4 gathers of y (L2) in flight
+__device__ __forceinline__ void st_row_sum(const float4* sv, const int* sc, int w, const float* y, dfl& t0, dfl& t1) {
+	for (int kb = 0; kb < w; kb += 4) {
+		int c[4];
+#pragma unroll
+		for (int j = 0; j < 4; j++) c[j] = kb + j < w ? sc[32 * (kb + j)] : -1;
+		float4 g[4];
+#pragma unroll
+		for (int j = 0; j < 4; j++)
+			g[j] = c[j] >= 0 ? __ldcg(reinterpret_cast<const float4*>(y) + c[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+		for (int j = 0; j < 4; j++) {
+			if (c[j] < 0) continue;
+			float4 const m = sv[32 * (kb + j)];
+			dfl const g0 = {g[j].x, g[j].z}, g1 = {g[j].y, g[j].w};
+			t0 = df_add(t0, df_add(df_mul_f(m.x, g0), df_mul_f(m.y, g1)));
+			t1 = df_add(t1, df_add(df_mul_f(m.z, g0), df_mul_f(m.w, g1)));
+		}
+	}
+}
+
+template <int VT>
+__global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
+	if (a.st->done && !a.timing) return;
+	extern __shared__ __align__(128) unsigned char st_smem[];
+	__shared__ __align__(8) unsigned long long full[ST_NS], empty[ST_NS];
+	__shared__ volatile int s_abort, s_issued, s_dead;
+	__shared__ double s_red[ST_THREADS / 32];
+	__shared__ bool s_last;
+	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	int const nc = a.ncol > 0 ? a.ncol : 1, nph = 2 * nc - 1;
+	bool const fuse = a.fuse && nc >= 3;
+	float2* vec_s = reinterpret_cast<float2*>(st_smem + (size_t) ST_NS * a.stage_bytes);  // r_c, then y_t (fused)
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < ST_NS; s++) {
+			mbar_init(smem_u32(&full[s]), 1);
+			mbar_init(smem_u32(&empty[s]), ST_CW);
+		}
+		s_abort = 0;
+		s_issued = 0;
+		s_dead = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	grid_barrier_init(a.bar);
+	__syncthreads();
+	dfl acc = {0.f, 0.f};
+	double acc64 = 0.0;
+	if (warp == ST_CW) {
+		// ---------------------------------------------------------- producer
+		int t = 0;
+		bool ok = true;
+		for (int ph = 0; ph < nph && ok; ph++) {
+			bool const fwd = ph < nc;
+			int const c = fwd ? ph : 2 * nc - 2 - ph;
+			int const lo = a.off[c], hi = a.off[c + 1];
+			const int* ptr = fwd ? a.lp : a.up;
+			const float4* V = fwd ? a.lv : a.uv;
+			const int* CI = fwd ? a.lc : a.uc;
+			int sa, sb;
+			st_share(a.sbase[c + 1] - a.sbase[c], sa, sb);
+			sa += a.sbase[c];
+			sb += a.sbase[c];
+			int const spt = a.spt[ph];
+			for (int s0 = sa; s0 < sb; s0 += spt, t++) {
+				int const ns = min(spt, sb - s0), stg = t % ST_NS;
+				if (t >= ST_NS && !mbar_wait(smem_u32(&empty[stg]), ((t / ST_NS) - 1) & 1)) {
+					ok = false;
+					break;
+				}
+				unsigned char* base = st_smem + (size_t) stg * a.stage_bytes;
+				int const pk = lane <= ns ? __ldg(ptr + s0 + lane) : 0;
+				int const p0 = __shfl_sync(0xffffffffu, pk, 0), pe = __shfl_sync(0xffffffffu, pk, ns);
+				if (lane <= ns) reinterpret_cast<int*>(base)[lane] = pk - p0;
+				__syncwarp();
+				int const E = pe - p0;
+				int const r0 = lo + 32 * (s0 - a.sbase[c]);
+				int const rows = min(32 * ns, hi - r0);
+				if (ST_HDR + 20l * E + 16l * rows > a.stage_bytes) {  // tiling does not match the slices: stop
+					ok = false;
+					break;
+				}
+				if (lane == 0) {
+					unsigned const bar = smem_u32(&full[stg]);
+					mbar_expect_tx(bar, 20u * (unsigned) E + 16u * (unsigned) rows);
+					if (E > 0) {
+						bulk_g2s(smem_u32(base + ST_HDR), V + p0, 16u * (unsigned) E, bar);
+						bulk_g2s(smem_u32(base + ST_HDR + 16 * E), CI + p0, 4u * (unsigned) E, bar);
+					}
+					bulk_g2s(smem_u32(base + ST_HDR + 20 * E), reinterpret_cast<const float4*>(a.dinv) + r0, 16u * (unsigned) rows,
+					         bar);
+					s_issued = t + 1;
+				}
+				__syncwarp();
+			}
+		}
+		if (!ok && lane == 0) {
+			s_abort = 1;
+			atomicExch(&a.st->ssor_err, 1);
+		}
+	}
+	else {
+		// ---------------------------------------------------------- consumers
+		int t = 0, kg = 0;
+		bool alive = true;
+		CoarseArgs const& co = a.co;
+		for (int ph = 0; ph < nph; ph++) {
+			bool const fwd = ph < nc;
+			int const c = fwd ? ph : 2 * nc - 2 - ph;
+			int const lo = a.off[c], hi = a.off[c + 1];
+			if (ph > 0) alive = st_grid_barrier(a.bar, &a.st->ssor_err, a.polls, &s_dead);
+			if (fuse && alive && ph == 1) {
+				// r_c: every chunk partial, per coarse DOF in chunk order (as k_restrict_sum)
+				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32) {
+					float2 v = make_float2(0.f, 0.f);
+					if (u < co.nc) {
+						int const I = u / 3, m = u % 3;
+						double s = 0.0;
+						for (int q = co.agg_chunk[I]; q < co.agg_chunk[I + 1]; q++) s += __ldcg(co.part + 3l * q + m);
+						dfl const d = df_make(s);
+						v = make_float2(d.hi, d.lo);
+					}
+					vec_s[u] = v;
+				}
+				consumers_sync();
+				int i0, i1;
+				st_tri_share(co.nc, i0, i1);
+				for (int i = i0 + warp; i < i1; i += ST_CW) {
+					dfl const s = st_row_dot(co.xl + xrow(i), i + 1, vec_s, lane);
+					if (lane == 0) co.yt[i] = make_float2(s.hi, s.lo);
+				}
+			}
+			if (fuse && alive && ph == 2) {
+				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32)
+					vec_s[u] = u < co.nc ? __ldcg(co.yt + u) : make_float2(0.f, 0.f);
+				consumers_sync();
+				int r0, r1;
+				st_tri_share(co.nc, r0, r1);
+				for (int r = r0 + warp; r < r1; r += ST_CW) {  // row r of X^T: coarse DOF j = nc - 1 - r
+					int const j = co.nc - 1 - r;
+					dfl const s = st_row_dot(co.xu + xrow(r), r + 1, vec_s + j, lane);
+					if (lane == 0) co.yc[j] = make_float2(s.hi, s.lo);
+				}
+			}
+			if (fuse && alive && ph == 3 && nc == 3) {
+				// colour 2 was stored in phase 2, before y_c: its coarse term now
+				int ra, rb;
+				st_share(a.off[3] - a.off[2], ra, rb);
+				for (int i = a.off[2] + ra + threadIdx.x; i < a.off[2] + rb; i += ST_CW * 32) ssor_add_coarse<VT>(a, i, acc, acc64);
+			}
+			// the sweep tiles of this phase (also drained when the block gave up)
+			int sa, sb;
+			st_share(a.sbase[c + 1] - a.sbase[c], sa, sb);
+			sa += a.sbase[c];
+			sb += a.sbase[c];
+			int const spt = a.spt[ph];
+			bool const final_rows = !fwd || c == nc - 1;
+			bool const plain = fuse && fwd && nc == 3;  // final before y_c exists
+			for (int s0 = sa; s0 < sb; s0 += spt, t++) {
+				int const ns = min(spt, sb - s0), stg = t % ST_NS;
+				bool const have = !(s_abort && t >= s_issued);
+				bool const got = have && mbar_wait(smem_u32(&full[stg]), (t / ST_NS) & 1);
+				if (!got) {
+					if (alive && lane == 0) atomicExch(&a.st->ssor_err, 1);
+					alive = false;
+					s_dead = 1;
+				}
+				if (got && alive) {
+					const unsigned char* base = st_smem + (size_t) stg * a.stage_bytes;
+					const int* hdr = reinterpret_cast<const int*>(base);
+					int const E = hdr[ns];
+					int j = (warp - kg % ST_CW + ST_CW) % ST_CW;
+					for (; j < ns; j += ST_CW) {
+						int const e0 = hdr[j], w = (hdr[j + 1] - e0) >> 5;
+						int const i = lo + 32 * (s0 + j - a.sbase[c]) + lane;
+						if (i >= hi) continue;
+						const float4* sv = reinterpret_cast<const float4*>(base + ST_HDR) + e0 + lane;
+						const int* sc = reinterpret_cast<const int*>(base + ST_HDR + 16 * E) + e0 + lane;
+						float4 const d = reinterpret_cast<const float4*>(base + ST_HDR + 20 * E)[32 * j + lane];
+						dfl r0, r1, z0, z1;
+						double q0 = 0.0, q1 = 0.0;
+						dfl t0 = {0.f, 0.f}, t1 = {0.f, 0.f};
+						if (fwd) {
+							ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+							st_row_sum(sv, sc, w, a.y, t0, t1);
+							ssor_blk(d, df_add(r0, df_neg(t0)), df_add(r1, df_neg(t1)), z0, z1);
+						}
+						else {
+							float4 const yv = __ldcg(reinterpret_cast<const float4*>(a.y) + i);
+							ssor_ld_r<VT>(a.r, i, r0, r1, q0, q1);
+							st_row_sum(sv, sc, w, a.y, t0, t1);
+							dfl w0, w1;
+							ssor_blk(d, t0, t1, w0, w1);
+							z0 = df_add({yv.x, yv.z}, df_neg(w0));
+							z1 = df_add({yv.y, yv.w}, df_neg(w1));
+						}
+						__stcg(reinterpret_cast<float4*>(a.y) + i, make_float4(z0.hi, z1.hi, z0.lo, z1.lo));
+						if (final_rows) {
+							if (plain) ssor_st_plain<VT>(a, i, z0, z1);
+							else ssor_st_z<VT>(a, i, z0, z1, r0, r1, q0, q1, acc, acc64);
+						}
+					}
+				}
+				kg += ns;
+				__syncwarp();
+				if (got && lane == 0) mbar_arrive(smem_u32(&empty[stg]));
+			}
+			if (fuse && alive && ph == 0) {
+				int q0, q1;
+				st_share(co.nchunk, q0, q1);
+				for (int q = q0 + warp; q < q1; q += ST_CW) st_restrict_chunk<VT>(co, a.r, q, lane);
+			}
+		}
+	}
+	// every thread of every block reaches the reduction, finished or not:
+	// warps in order, then blocks in order (deterministic)
+	double v = VT == VT_F64 ? acc64 : df_dbl(acc);
+	for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+	if (lane == 0) s_red[warp] = v;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double s = 0.0;
+		for (int k = 0; k < ST_THREADS / 32; k++) s += s_red[k];
+		a.partials[blockIdx.x] = s;
+		__threadfence();
+		unsigned const tk = atomicAdd(a.ticket, 1u);
+		s_last = tk == gridDim.x - 1;
+	}
+	__syncthreads();
+	if (!s_last) return;
+	__threadfence();
+	double w = 0.0;
+	for (int blk = threadIdx.x; blk < gridDim.x; blk += blockDim.x) w += __ldcg(a.partials + blk);
+	for (int o = 16; o; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+	__syncthreads();
+	if (lane == 0) s_red[warp] = w;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double s = 0.0;
+		for (int k = 0; k < ST_THREADS / 32; k++) s += s_red[k];
+		*a.ticket = 0u;
+		ssor_finish(a, s);
+	}
+}
+
+}  // namespace

@@ -296,6 +296,14 @@ int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int*
  * forms the colour order); overwrites the Krylov vectors. */
 int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* problem, int reps, double* ms, double* ms_sweeps, int* persistent);
 
+/* The coarse space of the two-level SSOR preconditioner after a solve with
+ * it: *n_coarse coarse DOFs (0: none; the solve ran plain SSOR), *n_chunks
+ * restriction chunks, *x_bytes the bytes of X = L^-1 and X^T the correction
+ * reads per application, *fused = 1 when the correction runs inside the
+ * sweep kernel.  Any pointer may be NULL. */
+int bfm_gpu_problem_coarse_info(bfm_gpu_problem_t* problem, int64_t* n_coarse, int64_t* n_chunks, int64_t* x_bytes,
+                                int* fused);
+
 /* Working node order of the last assembly: perm[w] = the caller's index of
  * working node w (n_nodes ints, host memory; the identity unless an SSOR
  * preconditioner renumbered the nodes colour by colour), and the colour
