@@ -65,8 +65,9 @@ SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md")
                 1: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md"),
                 2: (205_397_248, "profiles/spmv_fp32_mixed_perforated_2048x512.md")}
 # the same for one launch of the SSOR sweep kernel, per (precision, two-level
-# correction fused), where a capture of the current kernel exists
-SSOR_TRAFFIC = {(1, True): (269_338_112, "profiles/ssor2_fused_mixed_perforated_2048x512.md")}
+# correction fused, kernel: 1 k_ssor_all, 2 k_ssor_tma), where a capture of the
+# current kernel exists
+SSOR_TRAFFIC = {(1, True, 1): (269_338_112, "profiles/ssor2_fused_mixed_perforated_2048x512.md")}
 
 
 def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int, precision: int) -> int:
@@ -536,10 +537,11 @@ def main():
             b_pc += algorithmic_bytes_coarse(p.n_nodes, co["n_chunks"], co["x_bytes"])
             t_pc = r["ms_precond"]
         a_pc = b_pc / (t_pc * 1e-3) / 1e9
-        tr = SSOR_TRAFFIC.get((r["prec"], fused)) if args.workload == "perforated" and r["persistent"] else None
+        tr = SSOR_TRAFFIC.get((r["prec"], fused, r["persistent"])) if args.workload == "perforated" else None
         roof = {"bound": "hbm", "achieved": round(a_pc, 1), "peak": hbm, "unit": "GB/s", "frac": round(a_pc / hbm, 3),
                 "traffic": tr[0] if tr else None, "traffic_source": tr[1] if tr else None,
-                "kernel": ("k_ssor_all" + (" (two-level correction fused)" if fused else "")) if r["persistent"]
+                "kernel": (("k_ssor_tma" if r["persistent"] == 2 else "k_ssor_all") +
+                           (" (two-level correction fused)" if fused else "")) if r["persistent"]
                 else "k_ssor_fwd + k_ssor_bwd",
                 "algorithmic_bytes": b_pc, "kernel_ms": round(t_pc, 5), "peak_source": peak_kind,
                 "coarse_dofs": co["n_coarse"]}
@@ -578,7 +580,7 @@ def main():
                         "spmv_shape": v["shape"],
                         **({"precond_ms": round(v["ms_precond"], 5), "sweeps_ms": round(v["ms_sweeps"], 5),
                             "colours": v["ncol"],
-                            "sweeps": "persistent" if v["persistent"] else "per colour"}
+                            "sweeps": {0: "per colour", 1: "persistent", 2: "persistent, TMA-staged"}[v["persistent"]]}
                            if v["pc"] in SSOR_PCS else {})}
                     for k, v in results.items()},
         "speedup_vs_fp64": (round(results["fp64"]["ms"] / r["ms"], 3) if "fp64" in results else None),

@@ -1409,6 +1409,7 @@ struct CoarseArgs {
 	const int* chunk_agg;
 	const int* agg_chunk;
 	double* part;        // per chunk: 3 (restriction) or 81 (coarse matrix) partial sums
+	unsigned* ccnt;      // per aggregate: restriction chunks done in this application (TMA sweep kernel; reset by its last chunk)
 };
 
 struct SsorArgs {
@@ -2155,75 +2156,75 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 }
 
 // A_c = P^T A P in two deterministic stages.  One warp per chunk of
-// aggregate I: for each of the 9 cells around I (slot = cell offset) every
-// lane sums its nodes' 3x3 blocks coupling to that cell, so the lanes'
-// partial sums line up and are reduced in a fixed order into the chunk's 81
-// values; then per aggregate and entry the chunks in chunk order.  A neighbour outside those 9 cells sets *err (the
+// aggregate I: every lane keeps the 3x3 blocks of the 9 cells around I (slot
+// = cell offset), so the lanes' partial sums line up and are reduced in a
+// fixed order into the chunk's 81 values; then per aggregate and entry the
+// chunks in chunk order.  A neighbour outside those 9 cells sets *err (the
 // caller then drops the coarse correction).
 __global__ void k_coarse_ac(CoarseArgs a) {
 	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if (q >= a.nchunk) return;
 	int cx, cy;
 	cell_xy(a.chunk_agg[q], a.gx, a.gy, a.xfast, cx, cy);
-	// one neighbour slot at a time (9 accumulators per lane instead of 81):
-	// each slot's sums take the same terms in the same order
-	for (int slot = 0; slot < 9; slot++) {
-		double acc[9];
-#pragma unroll
-		for (int t = 0; t < 9; t++) acc[t] = 0.0;
-		for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
-			int const i = a.agg_nodes[k];
-			float4 const pi = a.pnode[i];
-			double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
+	double acc[9][9];
+	for (int s = 0; s < 9; s++)
+		for (int t = 0; t < 9; t++) acc[s][t] = 0.0;
+	for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
+		int const i = a.agg_nodes[k];
+		float4 const pi = a.pnode[i];
+		double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
+		// the FP32 operator in difference form, (A g)_i = S_i g_i + sum_j A_ij (g_j - g_i):
+		// its diagonal block is S_i - sum_{j != i} A_ij
+		double deff[4] = {0.0, 0.0, 0.0, 0.0};
+		if (!a.vals64) {
+			float4 const sr = reinterpret_cast<const float4*>(a.corr32)[i];
+			deff[0] = sr.x; deff[1] = sr.y; deff[2] = sr.z; deff[3] = sr.w;
 			for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
-				int const j = a.cols[e];
-				int jx, jy;
-				cell_xy(a.agg[j], a.gx, a.gy, a.xfast, jx, jy);
-				int const ox = jx - cx, oy = jy - cy;
-				if (ox < -1 || ox > 1 || oy < -1 || oy > 1) {
-					if (slot == 0) atomicOr(a.err, 1);
-					continue;
-				}
-				if ((oy + 1) * 3 + (ox + 1) != slot) continue;
-				float4 const pj = a.pnode[j];
-				double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
-				double m[4];
-				if (a.vals64) {
-					for (int t = 0; t < 4; t++) m[t] = a.vals64[4l * e + t];
-				}
-				else if (j == i) {
-					// the FP32 operator in difference form, (A g)_i = S_i g_i + sum_j A_ij (g_j - g_i):
-					// its diagonal block is S_i - sum_{j != i} A_ij
-					float4 const sr = reinterpret_cast<const float4*>(a.corr32)[i];
-					m[0] = sr.x; m[1] = sr.y; m[2] = sr.z; m[3] = sr.w;
-					for (int f = a.row_ptr[i]; f < a.row_ptr[i + 1]; f++) {
-						if (a.cols[f] == i) continue;
-						float4 const v = reinterpret_cast<const float4*>(a.vals32)[f];
-						m[0] -= v.x; m[1] -= v.y; m[2] -= v.z; m[3] -= v.w;
-					}
-				}
-				else {
-					float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
-					m[0] = v.x; m[1] = v.y; m[2] = v.z; m[3] = v.w;
-				}
-				// A P_j (2x3), then P_i^T (3x2) times it
-				double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
-				                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};
-				double const pt[3][2] = {{fi0, 0.0}, {0.0, fi1}, {-fi0 * dyi, fi1 * dxi}};
-#pragma unroll
-				for (int u = 0; u < 3; u++)
-#pragma unroll
-					for (int v = 0; v < 3; v++) acc[3 * u + v] += pt[u][0] * ap[0][v] + pt[u][1] * ap[1][v];
+				if (a.cols[e] == i) continue;
+				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
+				deff[0] -= v.x; deff[1] -= v.y; deff[2] -= v.z; deff[3] -= v.w;
 			}
 		}
+		for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
+			int const j = a.cols[e];
+			int jx, jy;
+			cell_xy(a.agg[j], a.gx, a.gy, a.xfast, jx, jy);
+			int const ox = jx - cx, oy = jy - cy;
+			if (ox < -1 || ox > 1 || oy < -1 || oy > 1) {
+				atomicOr(a.err, 1);
+				continue;
+			}
+			int const slot = (oy + 1) * 3 + (ox + 1);
+			float4 const pj = a.pnode[j];
+			double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
+			double m[4];
+			if (a.vals64) {
+				for (int t = 0; t < 4; t++) m[t] = a.vals64[4l * e + t];
+			}
+			else if (j == i) {
+				for (int t = 0; t < 4; t++) m[t] = deff[t];
+			}
+			else {
+				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
+				m[0] = v.x; m[1] = v.y; m[2] = v.z; m[3] = v.w;
+			}
+			// A P_j (2x3), then P_i^T (3x2) times it
+			double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
+			                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};
+			double const pt[3][2] = {{fi0, 0.0}, {0.0, fi1}, {-fi0 * dyi, fi1 * dxi}};
 #pragma unroll
-		for (int t = 0; t < 9; t++) {
-			double x = acc[t];
+			for (int u = 0; u < 3; u++)
 #pragma unroll
-			for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-			if (lane == 0) a.part[81l * q + 9 * slot + t] = x;
+				for (int v = 0; v < 3; v++) acc[slot][3 * u + v] += pt[u][0] * ap[0][v] + pt[u][1] * ap[1][v];
 		}
 	}
+	for (int s = 0; s < 9; s++)
+		for (int t = 0; t < 9; t++) {
+			double x = acc[s][t];
+#pragma unroll
+			for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+			if (lane == 0) a.part[81l * q + 9 * s + t] = x;
+		}
 }
 
 // The chunks' sums per aggregate into the lower band of A_c, each entry the
@@ -2504,9 +2505,12 @@ __global__ void __launch_bounds__(LB_T) k_linv_step(CoarseArgs a, int b, int k, 
 	a.xu[xrow(n - 1 - col) + (r0 + i - col)] = s.hi;
 }
 
-// k_linv_step for every block row in one cooperative launch: a grid barrier
-// between block rows instead of a launch each (bounded waits: a timeout sets
-// *a.berr and the blocks stop)
+// The block rows of X in one cooperative launch: a grid barrier between block
+// rows instead of a launch each (bounded waits: a timeout sets *a.berr and the
+// blocks stop).  The recurrence X_kj = M_k X_k-1,j runs in FP32 on the
+// double-float M_k and diagonal blocks' leading parts: X is stored in FP32, and
+// its rounding already perturbs X^T X by about u_fp32 cond(A_c), the order of
+// what the FP32 recurrence adds (forward substitution is backward stable)
 __global__ void __launch_bounds__(LB_T) k_linv_all(CoarseArgs a, int b, const float2* __restrict__ M,
                                                     const float2* __restrict__ Xd, float2* __restrict__ Xw) {
 	grid_barrier_init(a.bar);
@@ -2519,15 +2523,15 @@ __global__ void __launch_bounds__(LB_T) k_linv_all(CoarseArgs a, int b, const fl
 		for (long t = blockIdx.x * (long) blockDim.x + threadIdx.x; t < (long) rows * r0; t += stride) {
 			int const i = (int) (t / r0), col = (int) (t % r0);
 			const float2* Mi = M + ((long) k * b + i) * b;
-			dfl s = {0.f, 0.f};
+			float s = 0.f;
 			for (int c = 0; c < b; c++) {
-				float2 const m = Mi[c];
-				float2 const x = col < pb ? __ldcg(prev + (long) c * n + col) : Xd[((long) (k - 1) * b + c) * b + (col - pb)];
-				s = df_add(s, df_mul({m.x, m.y}, {x.x, x.y}));
+				float const m = Mi[c].x;
+				float const x = col < pb ? __ldcg(prev + (long) c * n + col).x : Xd[((long) (k - 1) * b + c) * b + (col - pb)].x;
+				s = __fmaf_rn(m, x, s);
 			}
-			__stcg(cur + (long) i * n + col, make_float2(s.hi, s.lo));
-			a.xl[xrow(r0 + i) + col] = s.hi;
-			a.xu[xrow(n - 1 - col) + (r0 + i - col)] = s.hi;
+			__stcg(cur + (long) i * n + col, make_float2(s, 0.f));
+			a.xl[xrow(r0 + i) + col] = s;
+			a.xu[xrow(n - 1 - col) + (r0 + i - col)] = s;
 		}
 		if (k + 1 < nb && !grid_barrier(a.bar, a.berr, a.polls)) return;
 	}

@@ -1513,6 +1513,8 @@ struct bfm_gpu_problem {
 	int sl_base[65];     // first slice of each colour
 	int *sl_lw, *sl_uw, *sl_lp, *sl_up;  // widths and slice offsets (n + 1 each)
 	int* sl_wm;          // device copy of sl_wmax
+	unsigned* ccnt;      // per aggregate: restriction chunks done (CoarseArgs::ccnt), na_cap entries
+	int ccnt_cap;
 	long sl_lcap, sl_ucap;
 	float4 *sl_lv, *sl_uv;
 	int *sl_lc, *sl_uc;
@@ -1971,6 +1973,7 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, int vt) {
 	c.chunk_agg = P->chunk_agg;
 	c.agg_chunk = P->agg_chunk;
 	c.part = P->cpart;
+	c.ccnt = P->ccnt;
 	return c;
 }
 
@@ -2048,6 +2051,13 @@ int build_aggregates(bfm_gpu_problem* P) {
 		if (dalloc(&P->chunk_start, nchunk + 1) || dalloc(&P->chunk_agg, nchunk + 1) || dalloc(&P->cpart, 81l * (nchunk + 1)))
 			rc = -1;
 		else P->chunk_cap = nchunk + 1;
+	}
+	if (!rc && na > P->ccnt_cap) {
+		if (P->ccnt) cudaFree(P->ccnt);
+		P->ccnt = nullptr;
+		P->ccnt_cap = 0;
+		if (dalloc(&P->ccnt, na) || cudaMemsetAsync(P->ccnt, 0, na * sizeof(unsigned), st) != cudaSuccess) rc = -1;
+		else P->ccnt_cap = na;
 	}
 	if (!rc && nc > P->nc_cap) {
 		// (re)allocate for the larger coarse space (the band at the widest bandwidth)
@@ -2853,6 +2863,7 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 			if (smem > 0) {
 				void* pa[1] = {&a};
 				cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
+				if (P->ccnt) cudaMemsetAsync(P->ccnt, 0, P->ccnt_cap * sizeof(unsigned), st);
 				cudaLaunchCooperativeKernel(ssor_tma_kernel(vt), dim3(P->tma_grid), dim3(ST_THREADS), pa, smem, st);
 				return;
 			}
@@ -3050,7 +3061,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y, P->ssor_d,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
 	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart,
-	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->sl_wm, P->lbm, P->lbd,
+	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->sl_wm, P->ccnt, P->lbm, P->lbd,
 	              P->lbw};
 	for (void* q : lb)
 		if (q) cudaFree(q);
@@ -3599,6 +3610,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	if (learned && bfmi_learned_precond(P, 0)) return -1;
 	if (ssor_pc(P->precond) && P->ssor_bar) {
 		CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
+		if (P->ccnt) CK(cudaMemsetAsync(P->ccnt, 0, P->ccnt_cap * sizeof(unsigned), P->stream));
 		if (pack_relaxation_blocks(P)) return -1;
 	}
 	CK(cudaGraphLaunch(P->graph, P->stream));
@@ -3614,6 +3626,7 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
 			if (ssor_pc(P->precond) && P->ssor_bar) {
 				CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
+				if (P->ccnt) CK(cudaMemsetAsync(P->ccnt, 0, P->ccnt_cap * sizeof(unsigned), P->stream));
 				if (pack_relaxation_blocks(P)) return -1;
 			}
 			CK(cudaGraphLaunch(P->graph, P->stream));
@@ -3734,7 +3747,7 @@ int bfm_gpu_problem_time_kernels(bfm_gpu_problem_t* P, int reps, double* ms_spmv
 int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* P, int reps, double* ms, double* ms_sweeps, int* persistent) {
 	g_err[0] = 0;
 	if (!P->assembled) return fail("assemble first");
-	if (persistent) *persistent = P->ssor_grid > 0;
+	if (persistent) *persistent = P->tma_grid > 0 ? 2 : P->ssor_grid > 0 ? 1 : 0;
 	return time_ssor(P, reps > 0 ? reps : 1, ms, ms_sweeps);
 }
 

@@ -28,9 +28,9 @@
 //
 // Two-level correction (at least 3 colours): its stages run between the
 // sweeps' own grid barriers -- restriction of the block's chunks at the end
-// of phase 0; at the start of phase 1 every block sums all chunk partials
-// into r_c in shared memory (the same sums in the same order in every block)
-// and forms its rows of y_t = X r_c; at the start of phase 2 it stages y_t
+// of phase 0, where the last chunk of each aggregate to finish sums the
+// aggregate's chunk partials in chunk order into r_c; at the start of phase 1
+// every block stages r_c in shared memory and forms its rows of y_t = X r_c; at the start of phase 2 it stages y_t
 // and forms its rows of y_c = X^T y_t.  The backward phases (from phase nc
 // on) add P y_c where they store z; the rows of colour nc - 1, stored in
 // phase nc - 1, get it at the start of phase nc when that is phase 3.
@@ -222,11 +222,38 @@ __device__ __forceinline__ void st_restrict_chunk(const CoarseArgs& co, const vo
 		s1 = df_add(s1, {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)});
 		s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
 	}
+	// the last chunk of the aggregate to finish sums the aggregate's chunks in
+	// chunk order into r_c (the count is reset for the next application)
+	__shared__ int last[ST_THREADS / 32];
+	int const wl = threadIdx.x >> 5;
 	if (lane == 0) {
 		co.part[3l * q] = df_dbl(s0);
 		co.part[3l * q + 1] = df_dbl(s1);
 		co.part[3l * q + 2] = df_dbl(s2);
+		__threadfence();
+		int const I = co.chunk_agg[q];
+		unsigned const nq = (unsigned) (co.agg_chunk[I + 1] - co.agg_chunk[I]);
+		last[wl] = atomicAdd(co.ccnt + I, 1u) == nq - 1 ? I : -1;
 	}
+	__syncwarp();
+	int const I = last[wl];
+	if (I < 0) return;
+	__threadfence();
+	int const q0 = co.agg_chunk[I], q1 = co.agg_chunk[I + 1];
+	if (lane < 3) {
+		double s = 0.0;
+		for (int qb = q0; qb < q1; qb += 8) {  // 8 loads in flight, summed in chunk order
+			double pv[8];
+#pragma unroll
+			for (int k = 0; k < 8; k++) pv[k] = qb + k < q1 ? __ldcg(co.part + 3l * (qb + k) + lane) : 0.0;
+#pragma unroll
+			for (int k = 0; k < 8; k++)
+				if (qb + k < q1) s += pv[k];
+		}
+		dfl const d = df_make(s);
+		co.rc[3 * I + lane] = make_float2(d.hi, d.lo);
+	}
+	if (lane == 0) co.ccnt[I] = 0u;
 }
 
 // sum of A_ij y_j over the staged blocks of one row: w blocks at stride 32
@@ -341,18 +368,9 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 			int const lo = a.off[c], hi = a.off[c + 1];
 			if (ph > 0) alive = st_grid_barrier(a.bar, &a.st->ssor_err, a.polls, &s_dead);
 			if (fuse && alive && ph == 1) {
-				// r_c: every chunk partial, per coarse DOF in chunk order (as k_restrict_sum)
-				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32) {
-					float2 v = make_float2(0.f, 0.f);
-					if (u < co.nc) {
-						int const I = u / 3, m = u % 3;
-						double s = 0.0;
-						for (int q = co.agg_chunk[I]; q < co.agg_chunk[I + 1]; q++) s += __ldcg(co.part + 3l * q + m);
-						dfl const d = df_make(s);
-						v = make_float2(d.hi, d.lo);
-					}
-					vec_s[u] = v;
-				}
+				// r_c, summed by each aggregate's last restriction chunk in phase 0
+				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32)
+					vec_s[u] = u < co.nc ? __ldcg(co.rc + u) : make_float2(0.f, 0.f);
 				consumers_sync();
 				int i0, i1;
 				st_tri_share(co.nc, i0, i1);

@@ -292,7 +292,7 @@ int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int*
  * coarse correction of the two-level form and every sweep phase) over `reps`
  * standalone launches on a scratch solver state; *ms_sweeps (may be NULL)
  * the sweeps alone; *persistent = 1 when the phases run as one cooperative
- * kernel.  Needs a solve with one of the SSOR preconditioners first (which
+ * kernel, 2 when that kernel stages its operands by TMA (k_ssor_tma).  Needs a solve with one of the SSOR preconditioners first (which
  * forms the colour order); overwrites the Krylov vectors. */
 int bfm_gpu_problem_time_precond(bfm_gpu_problem_t* problem, int reps, double* ms, double* ms_sweeps, int* persistent);
 

@@ -395,9 +395,10 @@ def test_sim_run_with_two_level(libbfm, name, monkeypatch):
 
 
 def test_blocked_coarse_inverse_matches_columnwise(libbfm, monkeypatch):
-    """X = L^-1 of the coarse factor by block rows (the default) and column by
-    column (BFM_GPU_COARSE_LINV_COLUMNS=1): the same matrix up to the
-    summation order, so the same iterations (within 2) and solution."""
+    """X = L^-1 of the coarse factor by block rows (the default: the block-row
+    recurrence in FP32, X being stored in FP32) and column by column in
+    double-float (BFM_GPU_COARSE_LINV_COLUMNS=1): the same matrix to about
+    FP32 rounding, so the same iterations (within 2) and solution."""
     p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
     out = []
     for cols in ("0", "1"):
