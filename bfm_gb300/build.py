@@ -57,7 +57,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OUT_DIR.mkdir(exist_ok=True)
     nvcc = _nvcc()
     cc = os.environ.get("CC", "gcc")
-    inc = [f"-I{INCLUDE}", f"-I{CSRC}"]
+    # the CUDA toolkit's headers for the host C files too (NVTX ranges)
+    cuda_inc = Path(nvcc).resolve().parent.parent / "include"
+    inc = [f"-I{INCLUDE}", f"-I{CSRC}", f"-I{cuda_inc}"]
     jobs = []
     for src in cu:
         obj = BUILD_DIR / (src.stem + ".cu.o")
@@ -72,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         list(ex.map(lambda j: _run(j[0]), jobs))
     tmp = LIB.with_suffix(".so.tmp")
     _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs], "-Xlinker", "-Bsymbolic",
-          "-Xlinker", "-soname=libbfm.so.1", "-lpthread", "-lm"])
+          "-Xlinker", "-soname=libbfm.so.1", "-lpthread", "-lm", "-ldl"])
     os.replace(tmp, LIB)
     # the soname the link records (libbfm.so.1, as the reference's SOVERSION 1),
     # for programs linked with -lbfm against this directory

@@ -33,6 +33,7 @@
 
 #include "cg_kernels.cuh"
 #include "internal.h"
+#include "trace.h"
 
 namespace {
 
@@ -710,6 +711,7 @@ int bfm_gpu_problem_set_parts(bfm_gpu_problem_t* P, int n_parts, const int32_t* 
 }
 
 int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
+	BFM_RANGE("bfm_gpu_problem_solve_parts");
 	g_berr[0] = 0;
 	BatchState* B = state_of(P);
 	if (!B) return bfail("set the parts first (bfm_gpu_problem_set_parts)");
@@ -781,6 +783,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 }
 
 int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gpu_opts_t* opts) {
+	BFM_RANGE("bfm_gpu_problem_step_parts");
 	g_berr[0] = 0;
 	BatchState* B = state_of(P);
 	if (!B) return bfail("set the parts first (bfm_gpu_problem_set_parts)");

@@ -31,6 +31,7 @@
 #include <bfm/gpu.h>
 
 #include "internal.h"
+#include "trace.h"
 
 #include <pthread.h>
 #include <stdarg.h>
@@ -1771,6 +1772,7 @@ void node_cells(long N, const double* xy, int* ag, CellGrid* g) {
 }
 
 int color_nodes(bfm_gpu_problem* P) {
+	BFM_RANGE("color_nodes");
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
 	if (!P->perm && (dalloc(&P->perm, N) || dalloc(&P->iperm, N) || dalloc(&P->dpos, N))) return -1;
@@ -1983,6 +1985,7 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, int vt) {
 // first; node lists per cell in ascending node order (a host counting sort:
 // deterministic).  Redone when the colouring is.
 int build_aggregates(bfm_gpu_problem* P) {
+	BFM_RANGE("build_aggregates");
 	cudaStream_t const st = P->stream;
 	long const N = P->N;
 	double* xy = (double*) malloc((2 * N + 2) * sizeof(double));
@@ -2180,6 +2183,7 @@ int build_sell(bfm_gpu_problem* P) {
 }
 
 int coarse_setup(bfm_gpu_problem* P) {
+	BFM_RANGE("coarse_setup");
 	cudaStream_t const st = P->stream;
 	P->coarse_ok = 0;
 	if (P->N == 0) return 0;
@@ -2927,6 +2931,7 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 // flight per lane, split or fused direction) on this problem's matrix, 20
 // launches each, and keep the fastest.
 int autotune_lpr(bfm_gpu_problem* P) {
+	BFM_RANGE("autotune_lpr");
 	double best = 1e30;
 	int best_lpr = 8;
 	bool const mixed = P->precision == BFM_GPU_MIXED || P->precision == BFM_GPU_MIXED_EXACT;
@@ -3329,6 +3334,7 @@ int bfm_gpu_problem_apply(bfm_gpu_problem_t* P, const double* x, double* y, int 
 }
 
 int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
+	BFM_RANGE("bfm_gpu_problem_assemble");
 	g_err[0] = 0;
 	if (precision != BFM_GPU_FP64 && precision != BFM_GPU_MIXED && precision != BFM_GPU_MIXED_EXACT &&
 	    precision != BFM_GPU_FP64_DF)
@@ -3572,6 +3578,7 @@ static int pack_relaxation_blocks(bfm_gpu_problem_t* P) {
 }
 
 int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
+	BFM_RANGE("bfm_gpu_problem_solve");
 	g_err[0] = 0;
 	if (!P->assembled) return fail("assemble before solving");
 	bfm_gpu_opts_t o;

@@ -19,6 +19,7 @@
 #include <bfm/system.h>
 
 #include "internal.h"
+#include "trace.h"
 
 /* ---------------------------------------------------------------- errors and options */
 
@@ -391,9 +392,12 @@ int bfm_sim_run(bfm_sim_t* sim) {
 		return -1;
 	int const stress = sim->kind == BFM_SIM_KIND_AXISYMMETRIC_STRAIN ? axisym_mode()
 	                                                                 : sim->kind == BFM_SIM_KIND_PLANAR_STRESS;
-	for (size_t i = 0; i < sim->n_instances; i++)
-		if (run_instance(sim, sim->instances[i], stress) < 0) return -1;
-	return 0;
+	int rc = 0;
+	BFM_RANGE_PUSH("bfm_sim_run");
+	for (size_t i = 0; i < sim->n_instances && rc == 0; i++)
+		if (run_instance(sim, sim->instances[i], stress) < 0) rc = -1;
+	BFM_RANGE_POP();
+	return rc;
 }
 
 /* ---------------------------------------------------------------- dense systems (ref system.c) */

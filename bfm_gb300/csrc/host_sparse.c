@@ -21,6 +21,7 @@
 #include <bfm/perm.h>
 
 #include "internal.h"
+#include "trace.h"
 
 typedef struct {
 	bfm_state_t* state;

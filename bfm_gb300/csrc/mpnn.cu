@@ -32,6 +32,7 @@
 #include <bfm/gpu.h>
 
 #include "internal.h"
+#include "trace.h"
 #include "reduce.cuh"
 
 namespace {
@@ -1039,6 +1040,7 @@ int bfm_gpu_mpnn_load(bfm_gpu_mpnn_t* net, const char* path) {
 }
 
 int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, float* features, float* c_out, double* blocks) {
+	BFM_RANGE("bfm_gpu_mpnn_forward");
 	bfmi_buffers_t bf;
 	bfmi_buffers(P, &bf);
 	cudaStream_t const st = (cudaStream_t) bf.stream;
@@ -1076,6 +1078,7 @@ int bfm_gpu_mpnn_gradient(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const doubl
 
 int bfm_gpu_mpnn_train_step(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, const double* r, const double* e, double* v,
                             int power_iters, double lr, double* loss) {
+	BFM_RANGE("bfm_gpu_mpnn_train_step");
 	bfmi_buffers_t bf;
 	bfmi_buffers(P, &bf);
 	cudaStream_t const st = (cudaStream_t) bf.stream;

@@ -40,6 +40,18 @@ def test_library_exports_every_declared_symbol(libbfm_path):
     assert not missing, f"not exported: {sorted(missing)}"
 
 
+def test_entry_points_carry_nvtx_ranges(libbfm_path):
+    """The entry points and set-up phases push NVTX ranges named after them
+    (header-only NVTX: nothing of it is exported)."""
+    data = Path(libbfm_path).read_bytes()
+    for name in (b"bfm_sim_run", b"bfm_gpu_problem_assemble", b"bfm_gpu_problem_solve", b"bfm_gpu_problem_step_parts",
+                 b"bfm_gpu_mpnn_forward", b"color_nodes", b"coarse_setup", b"autotune_lpr"):
+        assert name + b"\0" in data, name
+    out = subprocess.run(["nm", "-D", "--defined-only", str(libbfm_path)], capture_output=True, text=True,
+                         check=True).stdout
+    assert "nvtx" not in out.lower()
+
+
 def test_library_loads_and_binds(libbfm):
     assert libbfm.bfm_gpu_device_count() >= 0
     s = __import__("bfm_gb300.abi", fromlist=["x"]).bfm_state_t()
