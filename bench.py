@@ -344,20 +344,28 @@ def run_gpu(args, rank: int, world: int):
     return p, results, best, dict(ms=e2e_ms, cold_ms=cold_ms, h2d=h2d, d2h=d2h, steps=n_e2e), t_direct
 
 
-def run_batch(steps=3, warmup=3):
+def run_batch(steps=3, warmup=3, precond=None):
     """256 independent plates (nx ~ U{32..256}, ny ~ U{8..64}, per-element E
     log-uniform in [1e9, 2e11], seed 4): every step is one CUDA graph launch
-    holding the assembly of the block-diagonal batch and the persistent
-    batched solve, every mesh to rtol 1e-8 (MIXED_EXACT: FP64 assembly, FP32
-    iteration, FP64 residuals)."""
+    holding the assembly of the block-diagonal batch, the preconditioner's
+    set-up and the persistent batched solve, every mesh to rtol 1e-8
+    (MIXED_EXACT: FP64 assembly, FP32 iteration, FP64 residuals).  The
+    reported preconditioner is the two-level block Jacobi (a rigid-body coarse
+    space per mesh); plain Jacobi is timed beside it (`jacobi`)."""
     import torch
     import bfm_gb300
     from bfm_gb300 import batch as BA, meshgen as M
+    if precond is None:
+        line = run_batch(steps, warmup, bfm_gb300.PC_TWO_LEVEL_JACOBI)
+        jac = run_batch(steps, warmup, bfm_gb300.PC_JACOBI)
+        line["jacobi"] = {k: jac[k] for k in ("ms_per_step", "dof_per_s", "all_converged", "iterations_min",
+                                              "iterations_median", "iterations_max")}
+        return line
     lib = bfm_gb300.lib()
     ps = M.batch_uneven(256, seed=4)
     stream = torch.cuda.Stream()
     B = BA.Batch(lib, ps, stream=C.c_void_p(stream.cuda_stream))
-    o = bfm_gb300.default_opts(rtol=RTOL)
+    o = bfm_gb300.default_opts(rtol=RTOL, precond=precond)
     for _ in range(warmup):
         B.step(bfm_gb300.MIXED_EXACT, o)
     torch.cuda.synchronize()
@@ -372,8 +380,9 @@ def run_batch(steps=3, warmup=3):
     B.close()
     dof = int(sum(p.n_dof for p in ps))
     it = st["iterations"]
+    name = "two-level block Jacobi" if precond == bfm_gb300.PC_TWO_LEVEL_JACOBI else "Jacobi"
     return {"workload": "256 uneven P1 plates (seed 4), one graph launch per step (assembly + batched solve)",
-            "dof": dof, "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3),
+            "preconditioner": name, "dof": dof, "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3),
             "dof_per_s": round(dof / (ms * 1e-3), 1), "all_converged": bool((st["status"] == 0).all()),
             "max_rel_residual": float(st["rel_residual"].max()), "iterations_min": int(it.min()),
             "iterations_median": int(np.median(it)), "iterations_max": int(it.max()),

@@ -34,6 +34,7 @@ class bfm_gpu_stats_t(C.Structure):  # include/bfm/gpu.h
 
 FP64, MIXED, MIXED_EXACT, FP64_DF = 0, 1, 2, 3
 PC_JACOBI, PC_BLOCK_JACOBI, PC_LEARNED, PC_SSOR, PC_LEARNED_SSOR, PC_SSOR2, PC_LEARNED_SSOR2 = 0, 1, 2, 3, 4, 5, 6
+PC_TWO_LEVEL_JACOBI = 7  # batched solver only: block Jacobi + per-part rigid-body coarse space
 HOST, DEVICE = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "breakdown", 3: "bad mesh", 4: "cuda error", 5: "stagnated",
           6: "barrier timeout"}
@@ -75,6 +76,7 @@ GPU_PROTOTYPES = {
     "bfm_gpu_problem_solve_parts": (_i, [_vp, _P(bfm_gpu_opts_t)]),
     "bfm_gpu_problem_step_parts": (_i, [_vp, _i, _P(bfm_gpu_opts_t)]),
     "bfm_gpu_problem_part_stats": (_i, [_vp, _vp, _vp, _vp, _vp, _P(_i), _P(_i), _P(_d)]),
+    "bfm_gpu_problem_parts_coarse": (_i, [_vp, _vp, _vp, _vp]),
     "bfm_gpu_rcm_csr": (_i, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
     "bfm_gpu_problem_apply": (_i, [_vp, _vp, _vp, _i]),
     "bfm_gpu_problem_ordering": (_i, [_vp, _vp, _vp, _vp]),

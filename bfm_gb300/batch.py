@@ -99,6 +99,17 @@ class Batch:
         return dict(iterations=it, status=st, replacements=rp, rel_residual=res, rows_per_tile=rpt.value,
                     lanes_per_row=lpr.value, ms_solve=ms.value)
 
+    def coarse(self):
+        """Per part, A_c^-1 of the two-level block Jacobi preconditioner (FP32)
+        after a solve with it."""
+        n = len(self.problems)
+        nc = np.zeros(n, np.int32)
+        off = np.zeros(n + 1, np.int64)
+        assert self.lib.bfm_gpu_problem_parts_coarse(self.P, nc.ctypes.data, off.ctypes.data, None) == 0, last_error()
+        a = np.zeros(max(int(off[-1]), 1), np.float32)
+        assert self.lib.bfm_gpu_problem_parts_coarse(self.P, None, None, a.ctypes.data) == 0, last_error()
+        return [a[off[k]:off[k] + nc[k] * nc[k]].reshape(nc[k], nc[k]) for k in range(n)]
+
     def assemble_stats(self):
         s = bfm_gpu_stats_t()
         assert self.lib.bfm_gpu_problem_stats(self.P, C.byref(s)) == 0

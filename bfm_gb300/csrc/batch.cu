@@ -20,6 +20,17 @@
 // block ever waits for another to publish them.  Grid barriers spin with an
 // iteration limit: on timeout the kernel records an error and every block
 // leaves the loop.
+//
+// Two-level block Jacobi (BFM_GPU_PC_TWO_LEVEL_JACOBI): M^-1 = D^-1 + P A_c^-1
+// P^T per part, D the 2x2 diagonal blocks, P the rigid-body modes of the
+// cells of a grid over the part's bounding box.  A_c = P^T A P (FP64 sums of
+// the FP32 operator in difference form) and A_c^-1 (FP32 Cholesky of the
+// diagonally scaled A_c, X = L^-1, X^T X) are formed per step by three
+// set-up kernels; per iteration, after phase 2 and after a replacement:
+//   stage R  one warp per cell: r_c = P^T r;                                barrier
+//   stage Y  one block per chunk of a part's cells: their rows of
+//            y_c = A_c^-1 r_c, P y_c at their nodes, a partial (r_c, y_c);   barrier
+// and z = D^-1 r + P y_c is formed where phase 1 gathers it.
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -40,6 +51,10 @@ namespace {
 constexpr int BT = 256;          // threads per block
 constexpr int MAX_PARTS = 512;   // parts per batch (shared-memory replica)
 constexpr long SPIN_LIMIT = 1l << 25;  // default polls per barrier (each an L2 round trip: seconds in all)
+constexpr int BC_MAX_CELLS = 64;       // two-level: coarse cells per part
+constexpr int BC_MAX_N = 3 * BC_MAX_CELLS;  // coarse DOFs per part
+constexpr int BC_INV_T = 1024;         // threads of the coarse inverse kernel
+constexpr int BC_CHUNK = 10;           // cells per work item of stage Y (30 rows of A_c^-1)
 
 enum : int { BERR_BARRIER_TIMEOUT = 1 };
 
@@ -76,11 +91,32 @@ struct BatchArgs {
 	int max_iters;
 	int timing_iters;        // > 0: run exactly this many iterations (autotuner)
 	long polls;              // polls per grid barrier before it gives up
+	int block_pc;            // dinv holds each node's inverse 2x2 diagonal block
+	// two-level correction (k_batch_pcg<LPR, true>)
+	int n_cells;
+	const int* part_cell;    // cells of part k: [part_cell[k], part_cell[k+1])
+	const int* cell_part;
+	const int* cell_ptr;     // nodes of cell c: cell_nodes[cell_ptr[c] .. cell_ptr[c+1])
+	const int* cell_nodes;
+	const int* node_cell;
+	const float4* pnode;     // per node: offset (dx, dy) from its cell's centre over H, free flags
+	const float* ainv;       // per part: A_c^-1, dense (3 cells)^2 FP32, from ainv_off[k]
+	const long long* ainv_off;
+	double* rc;              // r_c = P^T r, 3 per cell
+	float2* zc;              // P y_c per node (y_c = A_c^-1 r_c, rounded to FP32)
+	int n_chunks;            // stage Y's work items: BC_CHUNK consecutive cells of one part
+	const int* chunk_part;
+	const int* chunk_cell;   // first cell of the chunk
+	const int* part_chunk;   // chunks of part k: [part_chunk[k], part_chunk[k+1])
+	double* cdot;            // per chunk: its share of (r_c, y_c), the coarse part of (r, M r)
 };
 
 struct Shared {
 	double gamma[MAX_PARTS], alpha[MAX_PARTS], beta[MAX_PARTS], rho_ref[MAX_PARTS], bnorm2[MAX_PARTS];
 	int done[MAX_PARTS], repl[MAX_PARTS], iter[MAX_PARTS], status[MAX_PARTS], nrepl[MAX_PARTS];
+	double rcs[BC_MAX_N];                  // two-level: the part's r_c
+	double ydot[3 * BC_CHUNK];             //   terms of (r_c, y_c) of a chunk's rows
+	float ys[3 * BC_CHUNK];                //   the chunk's rows of y_c
 	int active, any_repl, bar_ok;
 	unsigned gen;
 };
@@ -124,10 +160,21 @@ __device__ bool grid_barrier(const BatchArgs& a, Shared& sh) {
 	return sh.bar_ok;
 }
 
-// sum of column `c` of the partials of part k's tiles, in tile order
+// sum of column `c` of the partials of part k's tiles, in tile order (loads
+// four at a time)
 __device__ __forceinline__ double part_sum(const BatchArgs& a, int k, int c) {
 	double s = 0.0;
-	for (int t = a.part_tile[k]; t < a.part_tile[k + 1]; t++) s += __ldcg(&a.partials[2 * t + c]);
+	int t = a.part_tile[k];
+	int const e = a.part_tile[k + 1];
+	for (; t + 4 <= e; t += 4) {
+		double const v0 = __ldcg(&a.partials[2 * t + c]), v1 = __ldcg(&a.partials[2 * t + 2 + c]);
+		double const v2 = __ldcg(&a.partials[2 * t + 4 + c]), v3 = __ldcg(&a.partials[2 * t + 6 + c]);
+		s += v0;
+		s += v1;
+		s += v2;
+		s += v3;
+	}
+	for (; t < e; t++) s += __ldcg(&a.partials[2 * t + c]);
 	return s;
 }
 
@@ -154,13 +201,120 @@ __device__ __forceinline__ void block_sum2(double& v0, double& v1) {
 	}
 }
 
-template <int LPR>
+// Stage R: r_c = P^T r for every cell of a part still iterating.  One warp
+// per cell, lanes over the cell's nodes, double sums in lane order and a
+// fixed shuffle tree (deterministic).  P_i = [[f0, 0, -f0 dy], [0, f1, f1 dx]].
+__device__ void coarse_restrict(const BatchArgs& a, const Shared& sh) {
+	int const lane = threadIdx.x & 31;
+	int const nw = gridDim.x * (BT / 32);
+	for (int c = blockIdx.x * (BT / 32) + (threadIdx.x >> 5); c < a.n_cells; c += nw) {
+		if (sh.done[a.cell_part[c]]) continue;
+		double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+		int const end = a.cell_ptr[c + 1];
+		for (int k0 = a.cell_ptr[c] + lane; k0 < end; k0 += 128) {
+			// four nodes per lane in flight, summed in node-list order
+			int id[4];
+			float2 rv[4];
+			float4 pq[4];
+#pragma unroll
+			for (int u = 0; u < 4; u++) id[u] = k0 + 32 * u < end ? a.cell_nodes[k0 + 32 * u] : -1;
+#pragma unroll
+			for (int u = 0; u < 4; u++) {
+				rv[u] = id[u] >= 0 ? __ldcg(reinterpret_cast<const float2*>(a.r) + id[u]) : make_float2(0.f, 0.f);
+				pq[u] = id[u] >= 0 ? a.pnode[id[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+			}
+#pragma unroll
+			for (int u = 0; u < 4; u++) {
+				if (id[u] < 0) continue;
+				double const x0 = pq[u].z != 0.f ? (double) rv[u].x : 0.0, x1 = pq[u].w != 0.f ? (double) rv[u].y : 0.0;
+				s0 += x0;
+				s1 += x1;
+				s2 += (double) pq[u].x * x1 - (double) pq[u].y * x0;
+			}
+		}
+		for (int o = 16; o; o >>= 1) {
+			s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+			s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+			s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+		}
+		if (lane == 0) {
+			a.rc[3l * c] = s0;
+			a.rc[3l * c + 1] = s1;
+			a.rc[3l * c + 2] = s2;
+		}
+	}
+}
+
+// Stage Y, one block per work item (BC_CHUNK consecutive cells of one part
+// still iterating): the part's r_c staged in shared memory; the chunk's rows
+// of y_c = A_c^-1 r_c, one warp per row (lanes over columns, four loads in
+// flight, fixed shuffle tree), rounded to FP32; P y_c written at the chunk's
+// nodes (their lists are contiguous: cells are listed in order); and the
+// chunk's share of (r_c, y_c) of the rounded values, in row order.
+__device__ void coarse_solve(const BatchArgs& a, Shared& sh) {
+	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for (int q = blockIdx.x; q < a.n_chunks; q += gridDim.x) {
+		int const k = a.chunk_part[q];
+		if (sh.done[k]) continue;  // the same in every thread of the block
+		int const c0 = a.part_cell[k], n = 3 * (a.part_cell[k + 1] - c0);
+		int const cq = a.chunk_cell[q], ce = min(cq + BC_CHUNK, a.part_cell[k + 1]);
+		int const row0 = 3 * (cq - c0), rows = 3 * (ce - cq);
+		__syncthreads();  // the previous item's shared arrays are read
+		for (int u = threadIdx.x; u < n; u += BT) sh.rcs[u] = __ldcg(a.rc + 3l * c0 + u);
+		__syncthreads();
+		const float* __restrict__ A = a.ainv + a.ainv_off[k];
+		for (int i = warp; i < rows; i += BT / 32) {
+			const float* __restrict__ Ar = A + (long) (row0 + i) * n;
+			double s = 0.0;
+			for (int j0 = lane; j0 < n; j0 += 128) {
+				float v[4];
+#pragma unroll
+				for (int u = 0; u < 4; u++) v[u] = j0 + 32 * u < n ? __ldg(Ar + j0 + 32 * u) : 0.f;
+#pragma unroll
+				for (int u = 0; u < 4; u++)
+					if (j0 + 32 * u < n) s += (double) v[u] * sh.rcs[j0 + 32 * u];
+			}
+			for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+			float const y = (float) s;
+			if (lane == 0) {
+				sh.ys[i] = y;
+				sh.ydot[i] = (double) y * sh.rcs[row0 + i];
+			}
+		}
+		__syncthreads();
+		for (int t = a.cell_ptr[cq] + threadIdx.x; t < a.cell_ptr[ce]; t += BT) {
+			int const i = a.cell_nodes[t];
+			int const l = 3 * (a.node_cell[i] - cq);
+			float4 const pq = a.pnode[i];
+			float const y0 = sh.ys[l], y1 = sh.ys[l + 1], y2 = sh.ys[l + 2];
+			a.zc[i] = make_float2(pq.z * (y0 - pq.y * y2), pq.w * (y1 + pq.x * y2));
+		}
+		if (warp == 0) {
+			double d = lane < rows ? sh.ydot[lane] : 0.0;
+			for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+			if (lane == 0) a.cdot[q] = d;
+		}
+	}
+}
+
+// the coarse share of (r, M r) of part k, its chunks in order (zero for
+// one-level Jacobi)
+template <bool TWO>
+__device__ __forceinline__ double coarse_gamma(const BatchArgs& a, int k) {
+	if (!TWO) return 0.0;
+	double s = 0.0;
+	for (int q = a.part_chunk[k]; q < a.part_chunk[k + 1]; q++) s += __ldcg(a.cdot + q);
+	return s;
+}
+
+template <int LPR, bool TWO>
 __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 	extern __shared__ unsigned char smem_raw[];
 	Shared& sh = *reinterpret_cast<Shared*>(smem_raw);
 	int const sub = threadIdx.x % LPR;
 	int const rows_per_pass = BT / LPR;
 	if (threadIdx.x == 0) asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(sh.gen) : "l"(a.bar_gen) : "memory");
+	for (int k = threadIdx.x; k < a.n_parts; k += BT) sh.done[k] = 0;  // the init's coarse stages run every part
 	__syncthreads();
 
 	// ---- init: x = dx = p = 0, r = b; partials (b,b), (r, M r)
@@ -170,7 +324,7 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 			double2 const bb = ld2(a.b, i);
 			float const r0 = (float) bb.x, r1 = (float) bb.y;
 			float z0, z1;
-			precond_apply(a.dinv, 0, i, r0, r1, z0, z1);
+			precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
 			st2(a.x, i, 0.0, 0.0);
 			st2(a.dx, i, 0.f, 0.f);
 			st2(a.r, i, r0, r1);
@@ -185,8 +339,14 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 		}
 	}
 	if (!grid_barrier(a, sh)) return;
+	if (TWO) {
+		coarse_restrict(a, sh);
+		if (!grid_barrier(a, sh)) return;
+		coarse_solve(a, sh);
+		if (!grid_barrier(a, sh)) return;
+	}
 	for (int k = threadIdx.x; k < a.n_parts; k += BT) {
-		double const bn = part_sum(a, k, 0), g = part_sum(a, k, 1);
+		double const bn = part_sum(a, k, 0), g = part_sum(a, k, 1) + coarse_gamma<TWO>(a, k);
 		sh.bnorm2[k] = bn;
 		sh.gamma[k] = g;
 		sh.beta[k] = 0.0;
@@ -219,10 +379,18 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 			const float* __restrict__ r = a.r;
 			const float* __restrict__ pp = pc;
 			const float* __restrict__ dinv = a.dinv;
+			int const bpc = a.block_pc;
+			const float2* zcv = a.zc;
+			// z = D^-1 r (+ P y_c, two-level), then p' = z + beta p
 			auto gather = [=](int c, float& g0, float& g1) {
 				float2 const rc = ld2(r, c), pv = ld2(pp, c);
 				float z0, z1;
-				precond_apply(dinv, 0, c, rc.x, rc.y, z0, z1);
+				precond_apply(dinv, bpc, c, rc.x, rc.y, z0, z1);
+				if (TWO) {
+					float2 const zv = __ldcg(zcv + c);
+					z0 += zv.x;
+					z1 += zv.y;
+				}
 				g0 = z0 + beta * pv.x;
 				g1 = z1 + beta * pv.y;
 			};
@@ -283,7 +451,7 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 				float const r0 = rv.x - alpha * qv.x, r1 = rv.y - alpha * qv.y;
 				st2(a.r, i, r0, r1);
 				float z0, z1;
-				precond_apply(a.dinv, 0, i, r0, r1, z0, z1);
+				precond_apply(a.dinv, a.block_pc, i, r0, r1, z0, z1);
 				df_add_prod(g, r0, z0);
 				df_add_prod(g, r1, z1);
 				df_add_prod(rr, r0, r0);
@@ -297,12 +465,18 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 			}
 		}
 		if (!grid_barrier(a, sh)) return;
+		if (TWO) {
+			coarse_restrict(a, sh);
+			if (!grid_barrier(a, sh)) return;
+			coarse_solve(a, sh);
+			if (!grid_barrier(a, sh)) return;
+		}
 		if (threadIdx.x == 0) sh.any_repl = 0;
 		__syncthreads();
 		for (int k = threadIdx.x; k < a.n_parts; k += BT) {
 			sh.repl[k] = 0;
 			if (sh.done[k]) continue;
-			double const gamma = part_sum(a, k, 0), rho = part_sum(a, k, 1);
+			double const gamma = part_sum(a, k, 0) + coarse_gamma<TWO>(a, k), rho = part_sum(a, k, 1);
 			double const tol2 = a.rtol * a.rtol * sh.bnorm2[k];
 			sh.iter[k] += 1;
 			sh.beta[k] = gamma / sh.gamma[k];
@@ -371,7 +545,7 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 					float const r0 = (float) e0, r1 = (float) e1;
 					st2(a.r, row, r0, r1);
 					float z0, z1;
-					precond_apply(a.dinv, 0, row, r0, r1, z0, z1);
+					precond_apply(a.dinv, a.block_pc, row, r0, r1, z0, z1);
 					v0 += e0 * e0 + e1 * e1;
 					v1 += (double) r0 * (double) z0 + (double) r1 * (double) z1;
 				}
@@ -383,12 +557,18 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 			}
 		}
 		if (!grid_barrier(a, sh)) return;
+		if (TWO) {
+			coarse_restrict(a, sh);
+			if (!grid_barrier(a, sh)) return;
+			coarse_solve(a, sh);
+			if (!grid_barrier(a, sh)) return;
+		}
 		for (int k = threadIdx.x; k < a.n_parts; k += BT) {
 			if (!sh.repl[k]) continue;
 			double const rr = part_sum(a, k, 0);
 			sh.nrepl[k] += 1;
 			sh.rho_ref[k] = rr;
-			sh.gamma[k] = part_sum(a, k, 1);
+			sh.gamma[k] = part_sum(a, k, 1) + coarse_gamma<TWO>(a, k);
 			if (rr <= a.rtol * a.rtol * sh.bnorm2[k]) sh.done[k] = 1;
 		}
 		__syncthreads();
@@ -456,6 +636,189 @@ __global__ void k_batch_part_residual(BatchArgs a) {
 	a.ps[k].true_res2 = part_sum(a, k, 0);
 }
 
+// ---- two-level set-up, per step (after the assembly, inside the step's graph)
+
+struct CoarseSetArgs {
+	int N, n_cells;
+	const int* part_cell;
+	const int* cell_ptr;
+	const int* cell_nodes;
+	const int* node_cell;
+	const int* cell_nbr;   // 9 per cell: the cell at grid offset (dx, dy) in slot 3 (dy + 1) + dx + 1, -1 outside
+	const int2* cell_xy;   // per cell: its position in its part's grid
+	const float2* dxdy;    // per node: offset from its cell's centre over H (FP32)
+	const int* last_ci;    // per DOF: >= 0 when a Dirichlet condition eliminates it
+	float4* pnode;
+	const int* row_ptr;
+	const int* cols;
+	const float* vals;     // the FP32 iteration operator, applied in difference form:
+	const float* corr;     //   (K g)_r = S_r g_r + sum_c K_rc (g_c - g_r)
+	double* ac;            // 81 per cell: the 3x3 blocks A_c(I, J) of its 9 slots
+	float* ainv;
+	const long long* ainv_off;
+};
+
+// per node: (dx, dy, f0, f1), f = 0 for an eliminated DOF (its row of P is zero)
+__global__ void k_bpnode(CoarseSetArgs a) {
+	int const i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= a.N) return;
+	float2 const d = a.dxdy[i];
+	a.pnode[i] = make_float4(d.x, d.y, a.last_ci[2 * i] < 0 ? 1.f : 0.f, a.last_ci[2 * i + 1] < 0 ? 1.f : 0.f);
+}
+
+// the 2x3 block P_i, or zero
+__device__ __forceinline__ void p_block(float4 q, bool on, double p[2][3]) {
+	double const f0 = on ? q.z : 0.f, f1 = on ? q.w : 0.f;
+	p[0][0] = f0;  p[0][1] = 0.0; p[0][2] = -f0 * (double) q.y;
+	p[1][0] = 0.0; p[1][1] = f1;  p[1][2] = f1 * (double) q.x;
+}
+
+// acc += P_r^T (M d), M a 2x2 block, d and P_r 2x3
+__device__ __forceinline__ void acc_ptmd(double acc[9], const double pr[2][3], double m0, double m1, double m2, double m3,
+                                         const double d[2][3]) {
+#pragma unroll
+	for (int b = 0; b < 3; b++) {
+		double const t0 = m0 * d[0][b] + m1 * d[1][b];
+		double const t1 = m2 * d[0][b] + m3 * d[1][b];
+#pragma unroll
+		for (int q = 0; q < 3; q++) acc[3 * q + b] += pr[0][q] * t0 + pr[1][q] * t1;
+	}
+}
+
+// A_c(I, J) = sum over the nodes r of cell I of P_r^T (K P^(J))_r, with the
+// operator in difference form: (K P^(J))_r = S_r P^(J)_r + sum_{c != r}
+// K_rc (P^(J)_c - P^(J)_r), P^(J)_c = P_c when c lies in cell J, else 0.
+// One thread per (cell, slot); the 9 threads of a cell walk the same rows in
+// the same order (FP64 sums, deterministic).  Translations of interior nodes
+// cancel exactly in the differences, so no large terms cancel in the sums.
+__global__ void k_bcoarse_ac(CoarseSetArgs a) {
+	long const t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= 9l * a.n_cells) return;
+	int const I = (int) (t / 9), slot = (int) (t % 9);
+	int const J = a.cell_nbr[9l * I + slot];
+	double acc[9];
+#pragma unroll
+	for (int e = 0; e < 9; e++) acc[e] = 0.0;
+	if (J >= 0) {
+		bool const same = J == I;
+		for (int k = a.cell_ptr[I]; k < a.cell_ptr[I + 1]; k++) {
+			int const r = a.cell_nodes[k];
+			double pr[2][3], prj[2][3];
+			p_block(a.pnode[r], true, pr);
+			p_block(a.pnode[r], same, prj);
+			if (same) {
+				float4 const S = reinterpret_cast<const float4*>(a.corr)[r];
+				acc_ptmd(acc, pr, S.x, S.y, S.z, S.w, prj);
+			}
+			for (int kb = a.row_ptr[r]; kb < a.row_ptr[r + 1]; kb++) {
+				int const c = a.cols[kb];
+				if (c == r) continue;
+				bool const inJ = a.node_cell[c] == J;
+				if (!inJ && !same) continue;  // P^(J) is zero at both ends
+				double pc[2][3], d[2][3];
+				p_block(a.pnode[c], inJ, pc);
+#pragma unroll
+				for (int u = 0; u < 2; u++)
+#pragma unroll
+					for (int b = 0; b < 3; b++) d[u][b] = pc[u][b] - prj[u][b];
+				float4 const K = reinterpret_cast<const float4*>(a.vals)[kb];
+				acc_ptmd(acc, pr, K.x, K.y, K.z, K.w, d);
+			}
+		}
+	}
+	double* o = a.ac + 81l * I + 9 * slot;
+#pragma unroll
+	for (int e = 0; e < 9; e++) o[e] = acc[e];
+}
+
+// entry (i, j) of a part's A_c (cells from c0), 0 where the cells are not neighbours
+__device__ __forceinline__ double ac_entry(const CoarseSetArgs& a, int c0, int i, int j) {
+	int const I = c0 + i / 3, J = c0 + j / 3;
+	int2 const pi = a.cell_xy[I], pj = a.cell_xy[J];
+	int const dx = pj.x - pi.x, dy = pj.y - pi.y;
+	if (dx < -1 || dx > 1 || dy < -1 || dy > 1) return 0.0;
+	return a.ac[81l * I + 9 * (3 * (dy + 1) + dx + 1) + 3 * (i % 3) + j % 3];
+}
+
+// A_c^-1 of one part per block, in FP32 in shared memory: symmetric
+// diagonal scaling s_i = A_ii^-1/2 (in FP64), Cholesky of the scaled matrix
+// (a pivot below 1e-5 drops its coarse DOF: a cell without free nodes, or a
+// mode the cell's nodes do not carry), X = L^-1 in place, then
+// A_c^-1 = S X^T X S written in full (both triangles, the same value):
+// symmetric positive semi-definite by construction, whatever the rounding.
+__global__ void __launch_bounds__(BC_INV_T) k_bcoarse_inv(CoarseSetArgs a) {
+	extern __shared__ float Sm[];  // n x n, row-major, lower triangle used
+	__shared__ double sc[BC_MAX_N];
+	__shared__ float tmp[BC_MAX_N];
+	__shared__ int keep[BC_MAX_N];
+	int const k = blockIdx.x;
+	int const c0 = a.part_cell[k], n = 3 * (a.part_cell[k + 1] - c0);
+	int const tid = threadIdx.x;
+	if (n == 0) return;
+	for (int i = tid; i < n; i += BC_INV_T) {
+		double const d = ac_entry(a, c0, i, i);
+		sc[i] = d > 0.0 ? 1.0 / sqrt(d) : 0.0;
+	}
+	__syncthreads();
+	for (int e = tid; e < n * n; e += BC_INV_T) {
+		int const i = e / n, j = e % n;
+		if (j > i) continue;
+		double const v = 0.5 * (ac_entry(a, c0, i, j) + ac_entry(a, c0, j, i));
+		Sm[e] = (float) (v * sc[i] * sc[j]);
+	}
+	__syncthreads();
+	// right-looking Cholesky, column by column
+	for (int kk = 0; kk < n; kk++) {
+		if (tid == 0) {
+			float const d = Sm[kk * n + kk];
+			keep[kk] = d > 1e-5f;
+			Sm[kk * n + kk] = keep[kk] ? sqrtf(d) : 0.f;
+		}
+		__syncthreads();
+		float const l = Sm[kk * n + kk];
+		for (int i = kk + 1 + tid; i < n; i += BC_INV_T) Sm[i * n + kk] = l > 0.f ? Sm[i * n + kk] / l : 0.f;
+		__syncthreads();
+		int const m = n - kk - 1;
+		for (int e = tid; e < m * m; e += BC_INV_T) {
+			int const ii = e / m, jj = e % m;
+			if (jj > ii) continue;
+			int const i = kk + 1 + ii, j = kk + 1 + jj;
+			Sm[i * n + j] -= Sm[i * n + kk] * Sm[j * n + kk];
+		}
+		__syncthreads();
+	}
+	// X = L^-1 in place, columns from the last: X_jj = 1 / L_jj and, below,
+	// X[i][j] = -X_jj sum_{m=j+1..i} X[i][m] L[m][j] (one warp per row);
+	// dropped DOFs get a zero row and column
+	int const lane = tid & 31, warp = tid >> 5;
+	for (int j = n - 1; j >= 0; j--) {
+		for (int i = j + 1 + tid; i < n; i += BC_INV_T) tmp[i] = Sm[i * n + j];
+		__syncthreads();
+		float const xjj = keep[j] && Sm[j * n + j] > 0.f ? 1.f / Sm[j * n + j] : 0.f;
+		for (int i = j + 1 + warp; i < n; i += BC_INV_T / 32) {
+			float s = 0.f;
+			if (keep[i])
+				for (int m = j + 1 + lane; m <= i; m += 32) s += Sm[i * n + m] * tmp[m];
+			for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+			if (lane == 0) Sm[i * n + j] = keep[i] ? -xjj * s : 0.f;
+		}
+		__syncthreads();
+		if (tid == 0) Sm[j * n + j] = xjj;
+		__syncthreads();
+	}
+	// A_c^-1 = S X^T X S: entry (i, j), i >= j, = s_i s_j sum_{m >= i} X[m][i] X[m][j]
+	float* out = a.ainv + a.ainv_off[k];
+	for (int e = tid; e < n * n; e += BC_INV_T) {
+		int const i = e / n, j = e % n;
+		if (j > i) continue;
+		float s = 0.f;
+		for (int m = i; m < n; m++) s += Sm[m * n + i] * Sm[m * n + j];
+		float const v = (float) (sc[i] * sc[j] * (double) s);
+		out[(long) i * n + j] = v;
+		out[(long) j * n + i] = v;
+	}
+}
+
 }  // namespace
 
 // ====================================================================== host side
@@ -502,12 +865,27 @@ struct BatchState {
 	int s_precision, s_rpt, s_lpr;
 	unsigned s_gen;
 	bfm_gpu_opts_t s_opts;
+	int two;               // the last solve's preconditioner is two-level
+	// two-level coarse space (host-built cell grids, device set-up per step)
+	int cb_built, n_cells, nmax, n_chunks;
+	unsigned cb_gen;       // inputs generation the cells were built for
+	int *part_cell, *cell_part, *cell_ptr, *cell_nodes, *node_cell, *cell_nbr;
+	int *chunk_part, *chunk_cell, *part_chunk;
+	int2* cell_xy;
+	float2 *dxdy, *zc;
+	float4* pnode;
+	double *ac, *rc, *cdot;
+	float* ainv;
+	long long* ainv_off;
 };
 
 void batch_free(void* p) {
 	BatchState* B = (BatchState*) p;
 	if (!B) return;
-	void* d[] = {B->tile_part, B->tile_begin, B->tile_end, B->part_tile, B->partials, B->ps, B->bar, B->err};
+	void* d[] = {B->tile_part, B->tile_begin, B->tile_end, B->part_tile, B->partials, B->ps, B->bar, B->err,
+	             B->part_cell, B->cell_part, B->cell_ptr, B->cell_nodes, B->node_cell, B->cell_nbr, B->cell_xy,
+	             B->dxdy, B->pnode, B->ac, B->rc, B->cdot, B->ainv, B->zc, B->ainv_off, B->chunk_part, B->chunk_cell,
+	             B->part_chunk};
 	for (void* q : d)
 		if (q) cudaFree(q);
 	if (B->graph) cudaGraphExecDestroy(B->graph);
@@ -570,12 +948,252 @@ int build_tiles(BatchState* B, int rpt) {
 	return rc;
 }
 
-void* kernel_of(int lpr) {
+void* kernel_of(int lpr, int two) {
 	switch (lpr) {
-	case 1: return (void*) k_batch_pcg<1>;
-	case 2: return (void*) k_batch_pcg<2>;
-	default: return (void*) k_batch_pcg<4>;
+	case 1: return two ? (void*) k_batch_pcg<1, true> : (void*) k_batch_pcg<1, false>;
+	case 2: return two ? (void*) k_batch_pcg<2, true> : (void*) k_batch_pcg<2, false>;
+	default: return two ? (void*) k_batch_pcg<4, true> : (void*) k_batch_pcg<4, false>;
 	}
+}
+
+// Cell grid of one part over its bounding box (w x h): about one cell per
+// `per_cell` nodes, at most BC_MAX_CELLS, as square as the box allows.
+void part_grid(int n, double w, double h, int per_cell, int* gx, int* gy) {
+	int target = n / per_cell;
+	target = target < 1 ? 1 : target > BC_MAX_CELLS ? BC_MAX_CELLS : target;
+	int x = 1, y = 1;
+	if (w > 0 && h > 0) {
+		x = (int) lround(sqrt((double) target * w / h));
+		x = x < 1 ? 1 : x > target ? target : x;
+		y = (int) lround((double) target / x);
+		y = y > target / x ? target / x : y;
+		y = y < 1 ? 1 : y;
+	}
+	else if (w > 0) x = target;
+	else if (h > 0) y = target;
+	*gx = x;
+	*gy = y;
+}
+
+int coarse_nodes_per_cell() {
+	char const* e = getenv("BFM_GPU_BATCH_COARSE_NODES");
+	int const v = e ? atoi(e) : 0;
+	return v >= 16 ? v : 64;
+}
+
+// The two-level coarse space of every part: its cell grid, the cell of each
+// node and its offset from the cell's centre over H = max(cell width,
+// height), the node lists per cell (a counting sort, ascending node index)
+// and the neighbour table.  Host work from the coordinates, redone when an
+// input changes; the device set-up (P's free flags, A_c, A_c^-1) runs per
+// step.
+int coarse_build(bfm_gpu_problem_t* P, BatchState* B, cudaStream_t st) {
+	bfmi_mesh_t m;
+	bfmi_mesh(P, &m);
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	int const N = bf.N, np = B->n_parts;
+	int const per_cell = coarse_nodes_per_cell();
+	double* xy = (double*) malloc(sizeof(double) * 2 * (N + 1));
+	int* pgx = (int*) malloc(sizeof(int) * np);
+	int* pgy = (int*) malloc(sizeof(int) * np);
+	int* part_cell = (int*) malloc(sizeof(int) * (np + 1));
+	long long* aoff = (long long*) malloc(sizeof(long long) * (np + 1));
+	if (!xy || !pgx || !pgy || !part_cell || !aoff) {
+		free(xy); free(pgx); free(pgy); free(part_cell); free(aoff);
+		return bfail("out of host memory");
+	}
+	int rc = 0;
+	if (cudaMemcpyAsync(xy, m.coords, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+	    cudaStreamSynchronize(st) != cudaSuccess)
+		rc = bfail("coordinate copy failed");
+	// per part: box and grid
+	double* box = (double*) malloc(sizeof(double) * 4 * np);
+	if (!rc && !box) rc = bfail("out of host memory");
+	int nc = 0, nmax = 0;
+	long long na = 0;
+	for (int k = 0; !rc && k < np; k++) {
+		int const i0 = B->node_off_h[k], i1 = B->node_off_h[k + 1];
+		double x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+		for (int i = i0; i < i1; i++) {
+			double const x = xy[2 * i], y = xy[2 * i + 1];
+			if (i == i0 || x < x0) x0 = x;
+			if (i == i0 || x > x1) x1 = x;
+			if (i == i0 || y < y0) y0 = y;
+			if (i == i0 || y > y1) y1 = y;
+		}
+		box[4 * k] = x0;
+		box[4 * k + 1] = y0;
+		box[4 * k + 2] = x1 - x0;
+		box[4 * k + 3] = y1 - y0;
+		if (i1 > i0) part_grid(i1 - i0, x1 - x0, y1 - y0, per_cell, &pgx[k], &pgy[k]);
+		else pgx[k] = pgy[k] = 0;
+		part_cell[k] = nc;
+		aoff[k] = na;
+		int const n = 3 * pgx[k] * pgy[k];
+		nc += pgx[k] * pgy[k];
+		na += (long long) n * n;
+		nmax = n > nmax ? n : nmax;
+	}
+	part_cell[np] = nc;
+	aoff[np] = na;
+	int* node_cell = (int*) malloc(sizeof(int) * (N + 1));
+	float* dxdy = (float*) malloc(sizeof(float) * 2 * (N + 1));
+	int* cell_ptr = (int*) calloc(nc + 1, sizeof(int));
+	int* cell_nodes = (int*) malloc(sizeof(int) * (N + 1));
+	int* cell_part = (int*) malloc(sizeof(int) * (nc + 1));
+	int* cell_nbr = (int*) malloc(sizeof(int) * 9 * (nc + 1));
+	int* cell_xy = (int*) malloc(sizeof(int) * 2 * (nc + 1));
+	if (!rc && (!node_cell || !dxdy || !cell_ptr || !cell_nodes || !cell_part || !cell_nbr || !cell_xy))
+		rc = bfail("out of host memory");
+	for (int k = 0; !rc && k < np; k++) {
+		int const gx = pgx[k], gy = pgy[k], c0 = part_cell[k];
+		double const x0 = box[4 * k], y0 = box[4 * k + 1], w = box[4 * k + 2], h = box[4 * k + 3];
+		double const cw = w > 0 ? w * (1.0 + 1e-12) / gx : 1.0, ch = h > 0 ? h * (1.0 + 1e-12) / gy : 1.0;
+		double const H = cw > ch ? cw : ch;
+		for (int i = B->node_off_h[k]; i < B->node_off_h[k + 1]; i++) {
+			int cx = (int) ((xy[2 * i] - x0) / cw), cy = (int) ((xy[2 * i + 1] - y0) / ch);
+			cx = cx < 0 ? 0 : cx >= gx ? gx - 1 : cx;
+			cy = cy < 0 ? 0 : cy >= gy ? gy - 1 : cy;
+			node_cell[i] = c0 + cx + gx * cy;
+			dxdy[2 * i] = (float) ((xy[2 * i] - (x0 + (cx + 0.5) * cw)) / H);
+			dxdy[2 * i + 1] = (float) ((xy[2 * i + 1] - (y0 + (cy + 0.5) * ch)) / H);
+			cell_ptr[node_cell[i] + 1]++;
+		}
+		for (int cy = 0; cy < gy; cy++)
+			for (int cx = 0; cx < gx; cx++) {
+				int const c = c0 + cx + gx * cy;
+				cell_part[c] = k;
+				cell_xy[2 * c] = cx;
+				cell_xy[2 * c + 1] = cy;
+				for (int dy = -1; dy <= 1; dy++)
+					for (int dx = -1; dx <= 1; dx++) {
+						int const ux = cx + dx, uy = cy + dy;
+						cell_nbr[9 * c + 3 * (dy + 1) + dx + 1] = ux >= 0 && ux < gx && uy >= 0 && uy < gy ? c0 + ux + gx * uy : -1;
+					}
+			}
+	}
+	// stage Y's work items: BC_CHUNK consecutive cells of one part
+	int nq = 0;
+	for (int k = 0; !rc && k < np; k++) nq += (part_cell[k + 1] - part_cell[k] + BC_CHUNK - 1) / BC_CHUNK;
+	int* chunk_part = (int*) malloc(sizeof(int) * (nq + 1));
+	int* chunk_cell = (int*) malloc(sizeof(int) * (nq + 1));
+	int* part_chunk = (int*) malloc(sizeof(int) * (np + 1));
+	if (!rc && (!chunk_part || !chunk_cell || !part_chunk)) rc = bfail("out of host memory");
+	if (!rc) {
+		int q = 0;
+		for (int k = 0; k < np; k++) {
+			part_chunk[k] = q;
+			for (int c = part_cell[k]; c < part_cell[k + 1]; c += BC_CHUNK) {
+				chunk_part[q] = k;
+				chunk_cell[q] = c;
+				q++;
+			}
+		}
+		part_chunk[np] = q;
+	}
+	if (!rc) {
+		for (int c = 0; c < nc; c++) cell_ptr[c + 1] += cell_ptr[c];
+		int* fill = (int*) malloc(sizeof(int) * (nc + 1));
+		if (!fill) rc = bfail("out of host memory");
+		else {
+			memcpy(fill, cell_ptr, sizeof(int) * (nc + 1));
+			for (int i = 0; i < N; i++) cell_nodes[fill[node_cell[i]]++] = i;
+			free(fill);
+		}
+	}
+	if (!rc) {
+		// device buffers, (re)sized for this batch
+		void* old[] = {B->part_cell, B->cell_part, B->cell_ptr, B->cell_nodes, B->node_cell, B->cell_nbr, B->cell_xy,
+		               B->dxdy, B->pnode, B->ac, B->rc, B->cdot, B->ainv, B->zc, B->ainv_off, B->chunk_part,
+		               B->chunk_cell, B->part_chunk};
+		for (void* q : old)
+			if (q) cudaFree(q);
+		B->part_cell = B->cell_part = B->cell_ptr = B->cell_nodes = B->node_cell = B->cell_nbr = nullptr;
+		B->chunk_part = B->chunk_cell = B->part_chunk = nullptr;
+		B->cell_xy = nullptr;
+		B->dxdy = B->zc = nullptr;
+		B->pnode = nullptr;
+		B->ac = B->rc = B->cdot = nullptr;
+		B->ainv = nullptr;
+		B->ainv_off = nullptr;
+		int const c1 = nc + 1;
+		if (cudaMalloc(&B->part_cell, sizeof(int) * (np + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->cell_part, sizeof(int) * c1) != cudaSuccess ||
+		    cudaMalloc(&B->cell_ptr, sizeof(int) * c1) != cudaSuccess ||
+		    cudaMalloc(&B->cell_nodes, sizeof(int) * (N + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->node_cell, sizeof(int) * (N + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->cell_nbr, sizeof(int) * 9 * c1) != cudaSuccess ||
+		    cudaMalloc(&B->cell_xy, sizeof(int2) * c1) != cudaSuccess ||
+		    cudaMalloc(&B->dxdy, sizeof(float2) * (N + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->pnode, sizeof(float4) * (N + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->ac, sizeof(double) * 81 * c1) != cudaSuccess ||
+		    cudaMalloc(&B->rc, sizeof(double) * 3 * c1) != cudaSuccess ||
+		    cudaMalloc(&B->cdot, sizeof(double) * (nq + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->ainv, sizeof(float) * (na + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->zc, sizeof(float2) * (N + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->ainv_off, sizeof(long long) * (np + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->chunk_part, sizeof(int) * (nq + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->chunk_cell, sizeof(int) * (nq + 1)) != cudaSuccess ||
+		    cudaMalloc(&B->part_chunk, sizeof(int) * (np + 1)) != cudaSuccess)
+			rc = bfail("cudaMalloc failed for the two-level coarse space");
+	}
+	if (!rc && (cudaMemcpy(B->part_cell, part_cell, sizeof(int) * (np + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->cell_part, cell_part, sizeof(int) * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->cell_ptr, cell_ptr, sizeof(int) * (nc + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->cell_nodes, cell_nodes, sizeof(int) * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->node_cell, node_cell, sizeof(int) * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->cell_nbr, cell_nbr, sizeof(int) * 9 * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->cell_xy, cell_xy, sizeof(int) * 2 * nc, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->dxdy, dxdy, sizeof(float) * 2 * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->ainv_off, aoff, sizeof(long long) * (np + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->chunk_part, chunk_part, sizeof(int) * nq, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->chunk_cell, chunk_cell, sizeof(int) * nq, cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemcpy(B->part_chunk, part_chunk, sizeof(int) * (np + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+	            cudaMemset(B->zc, 0, sizeof(float2) * (N + 1)) != cudaSuccess))
+		rc = bfail("cudaMemcpy failed for the two-level coarse space");
+	if (!rc && cudaFuncSetAttribute(k_bcoarse_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                (int) (nmax * nmax * sizeof(float))) != cudaSuccess)
+		rc = bfail("the coarse inverse kernel cannot have %d bytes of shared memory", (int) (nmax * nmax * sizeof(float)));
+	if (!rc) {
+		B->n_cells = nc;
+		B->n_chunks = nq;
+		B->nmax = nmax;
+		B->cb_built = 1;
+		B->cb_gen = bf.inputs_gen;
+	}
+	free(xy); free(pgx); free(pgy); free(part_cell); free(aoff); free(box);
+	free(node_cell); free(dxdy); free(cell_ptr); free(cell_nodes); free(cell_part); free(cell_nbr); free(cell_xy);
+	free(chunk_part); free(chunk_cell); free(part_chunk);
+	return rc;
+}
+
+CoarseSetArgs coarse_set_args(bfm_gpu_problem_t* P, BatchState* B) {
+	bfmi_mesh_t m;
+	bfmi_mesh(P, &m);
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	CoarseSetArgs c;
+	memset(&c, 0, sizeof c);
+	c.N = bf.N;
+	c.n_cells = B->n_cells;
+	c.part_cell = B->part_cell;
+	c.cell_ptr = B->cell_ptr;
+	c.cell_nodes = B->cell_nodes;
+	c.node_cell = B->node_cell;
+	c.cell_nbr = B->cell_nbr;
+	c.cell_xy = B->cell_xy;
+	c.dxdy = B->dxdy;
+	c.last_ci = m.last_ci;
+	c.pnode = B->pnode;
+	c.row_ptr = bf.row_ptr;
+	c.cols = bf.cols;
+	c.vals = bf.vals32;
+	c.corr = bf.corr32;
+	c.ac = B->ac;
+	c.ainv = B->ainv;
+	c.ainv_off = B->ainv_off;
+	return c;
 }
 
 BatchArgs batch_args(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* o) {
@@ -609,6 +1227,25 @@ BatchArgs batch_args(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* 
 	a.bar_gen = B->bar + 32;
 	a.err = B->err;
 	a.polls = SPIN_LIMIT;
+	a.block_pc = bf.precond != BFM_GPU_PC_JACOBI;
+	if (B->two) {
+		a.n_cells = B->n_cells;
+		a.part_cell = B->part_cell;
+		a.cell_part = B->cell_part;
+		a.cell_ptr = B->cell_ptr;
+		a.cell_nodes = B->cell_nodes;
+		a.node_cell = B->node_cell;
+		a.pnode = B->pnode;
+		a.ainv = B->ainv;
+		a.ainv_off = B->ainv_off;
+		a.rc = B->rc;
+		a.zc = B->zc;
+		a.cdot = B->cdot;
+		a.n_chunks = B->n_chunks;
+		a.chunk_part = B->chunk_part;
+		a.chunk_cell = B->chunk_cell;
+		a.part_chunk = B->part_chunk;
+	}
 	if (o) {
 		a.rtol = o->rtol;
 		a.drop2 = o->replace_drop * o->replace_drop;
@@ -619,22 +1256,34 @@ BatchArgs batch_args(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* 
 }
 
 // blocks of the persistent kernel that fit on the GPU at once (cooperative launch)
-int coop_grid(int lpr, int* grid) {
+int coop_grid(int lpr, int two, int* grid) {
 	int dev = 0, sms = 0, nb = 0;
 	BCK(cudaGetDevice(&dev));
 	BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-	BCK(cudaFuncSetAttribute(kernel_of(lpr), cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(Shared)));
-	BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel_of(lpr), BT, sizeof(Shared)));
+	BCK(cudaFuncSetAttribute(kernel_of(lpr, two), cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(Shared)));
+	BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel_of(lpr, two), BT, sizeof(Shared)));
 	if (nb < 1) return bfail("the batch kernel does not fit on an SM");
 	*grid = sms * nb;
 	return 0;
 }
 
-int launch(BatchState* B, BatchArgs* a, int lpr, int grid, cudaStream_t st) {
+int launch(bfm_gpu_problem_t* P, BatchState* B, BatchArgs* a, int lpr, int grid, cudaStream_t st) {
 	BCK(cudaMemsetAsync(B->bar, 0, 64 * sizeof(unsigned), st));
 	BCK(cudaMemsetAsync(B->err, 0, sizeof(int), st));
+	if (B->two) {
+		// the coarse space of this assembly: P's free flags, A_c, A_c^-1
+		// (k_bcoarse_inv's shared-memory size is set by coarse_build, outside any capture)
+		CoarseSetArgs c = coarse_set_args(P, B);
+		int const smem = B->nmax * B->nmax * (int) sizeof(float);
+		if (c.N > 0) k_bpnode<<<(c.N + 255) / 256, 256, 0, st>>>(c);
+		if (c.n_cells > 0) {
+			k_bcoarse_ac<<<(int) ((9l * c.n_cells + 127) / 128), 128, 0, st>>>(c);
+			k_bcoarse_inv<<<B->n_parts, BC_INV_T, smem, st>>>(c);
+		}
+		BCK(cudaGetLastError());
+	}
 	void* params[1] = {a};
-	BCK(cudaLaunchCooperativeKernel(kernel_of(lpr), dim3(grid), dim3(BT), params, sizeof(Shared), st));
+	BCK(cudaLaunchCooperativeKernel(kernel_of(lpr, B->two), dim3(grid), dim3(BT), params, sizeof(Shared), st));
 	k_batch_residual<<<grid, BT, 0, st>>>(*a);
 	k_batch_part_residual<<<(B->n_parts + 127) / 128, 128, 0, st>>>(*a);
 	BCK(cudaGetLastError());
@@ -653,11 +1302,11 @@ int autotune(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* o, cudaS
 		if (build_tiles(B, rpt)) return -1;
 		for (int lpr : lprs) {
 			int grid = 0;
-			if (coop_grid(lpr, &grid)) return -1;
+			if (coop_grid(lpr, B->two, &grid)) return -1;
 			BatchArgs a = batch_args(P, B, o);
 			a.timing_iters = 10;
 			BCK(cudaEventRecord(B->ev[0], st));
-			if (launch(B, &a, lpr, grid, st)) return -1;
+			if (launch(P, B, &a, lpr, grid, st)) return -1;
 			BCK(cudaEventRecord(B->ev[1], st));
 			BCK(cudaStreamSynchronize(st));
 			float ms = 0;
@@ -720,11 +1369,28 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 	if (!bf.assembled) return bfail("assemble before solving");
 	if (bf.precision != BFM_GPU_MIXED && bf.precision != BFM_GPU_MIXED_EXACT)
 		return bfail("the batched solver runs the mixed-precision iteration: assemble with BFM_GPU_MIXED or BFM_GPU_MIXED_EXACT");
-	if (bf.precond != BFM_GPU_PC_JACOBI) return bfail("the batched solver uses the Jacobi preconditioner");
 	bfm_gpu_opts_t o;
 	if (opts) o = *opts;
 	else bfm_gpu_default_opts(&o);
 	cudaStream_t const st = (cudaStream_t) bf.stream;
+	if (o.precond != BFM_GPU_PC_JACOBI && o.precond != BFM_GPU_PC_BLOCK_JACOBI && o.precond != BFM_GPU_PC_TWO_LEVEL_JACOBI)
+		return bfail("the batched solver takes the Jacobi, block Jacobi or two-level block Jacobi preconditioner, got %d",
+		             o.precond);
+	// the smoother's layout is formed by the assembly: assemble again if it differs
+	int const want_pc = o.precond == BFM_GPU_PC_JACOBI ? BFM_GPU_PC_JACOBI : BFM_GPU_PC_BLOCK_JACOBI;
+	if (bf.precond != want_pc) {
+		if (bfmi_set_precond(P, want_pc) || bfm_gpu_problem_assemble(P, bf.precision)) return -1;
+		bfmi_buffers(P, &bf);
+	}
+	int const two = o.precond == BFM_GPU_PC_TWO_LEVEL_JACOBI;
+	if (two && (!B->cb_built || B->cb_gen != bf.inputs_gen) && coarse_build(P, B, st)) return -1;
+	if (two != B->two) {
+		B->two = two;
+		B->tuned = 0;  // the tile shapes are tuned per kernel
+		if (B->graph) cudaGraphExecDestroy(B->graph);
+		B->graph = nullptr;
+		B->direct = 0;
+	}
 	if (o.autotune && !B->tuned) {
 		if (autotune(P, B, &o, st)) return -1;
 		if (B->graph) cudaGraphExecDestroy(B->graph);
@@ -736,7 +1402,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		// one graph: reset of the barrier words, the persistent cooperative
 		// kernel, the per-part FP64 residuals
 		int grid = 0;
-		if (coop_grid(B->lpr, &grid)) return -1;
+		if (coop_grid(B->lpr, B->two, &grid)) return -1;
 		B->grid = grid;
 		BatchArgs a = batch_args(P, B, &o);
 		cudaStream_t cs;
@@ -744,7 +1410,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		cudaGraph_t g = nullptr;
 		int rc = 0;
 		if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = bfail("stream capture failed");
-		if (!rc) rc = launch(B, &a, B->lpr, grid, cs);
+		if (!rc) rc = launch(P, B, &a, B->lpr, grid, cs);
 		cudaError_t const ec = cudaStreamEndCapture(cs, &g);
 		cudaStreamDestroy(cs);
 		if (!rc && ec != cudaSuccess) rc = bfail("stream capture failed: %s", cudaGetErrorString(ec));
@@ -776,7 +1442,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 	}
 	else {
 		BatchArgs a = batch_args(P, B, &o);
-		if (launch(B, &a, B->lpr, B->grid, st)) return -1;
+		if (launch(P, B, &a, B->lpr, B->grid, st)) return -1;
 	}
 	BCK(cudaEventRecord(B->ev[1], st));
 	return 0;
@@ -792,13 +1458,19 @@ int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gp
 	bfm_gpu_opts_t o;
 	if (opts) o = *opts;
 	else bfm_gpu_default_opts(&o);
+	if (o.precond != BFM_GPU_PC_JACOBI && o.precond != BFM_GPU_PC_BLOCK_JACOBI && o.precond != BFM_GPU_PC_TWO_LEVEL_JACOBI)
+		return bfail("the batched solver takes the Jacobi, block Jacobi or two-level block Jacobi preconditioner, got %d",
+		             o.precond);
+	// the smoother's layout of the assemblies below
+	if (bfmi_set_precond(P, o.precond == BFM_GPU_PC_JACOBI ? BFM_GPU_PC_JACOBI : BFM_GPU_PC_BLOCK_JACOBI)) return -1;
 	bfmi_buffers_t bf;
 	bfmi_buffers(P, &bf);
 	cudaStream_t const st = (cudaStream_t) bf.stream;
 	bool const same = (B->step_graph || B->step_direct) && B->s_precision == precision && B->s_gen == bf.inputs_gen &&
 	                  B->s_rpt == B->rows_per_tile && B->s_lpr == B->lpr && B->s_opts.rtol == o.rtol &&
 	                  B->s_opts.max_iters == o.max_iters && B->s_opts.replace_drop == o.replace_drop &&
-	                  B->s_opts.barrier_polls == o.barrier_polls && B->s_opts.autotune == o.autotune;
+	                  B->s_opts.barrier_polls == o.barrier_polls && B->s_opts.autotune == o.autotune &&
+	                  B->s_opts.precond == o.precond;
 	if (!same) {
 		// one step launched directly first: it sizes every buffer, tunes the
 		// tile shape and leaves nothing for the capture to allocate
@@ -809,7 +1481,7 @@ int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gp
 		B->step_graph = nullptr;
 		B->step_direct = 0;
 		int grid = 0;
-		if (coop_grid(B->lpr, &grid)) return -1;
+		if (coop_grid(B->lpr, B->two, &grid)) return -1;
 		B->grid = grid;
 		BatchArgs a = batch_args(P, B, &o);
 		cudaGraph_t g = nullptr;
@@ -819,7 +1491,7 @@ int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gp
 		if (!rc) {
 			BatchArgs a2 = batch_args(P, B, &o);  // the assembly's buffers, unchanged
 			a = a2;
-			rc = launch(B, &a, B->lpr, grid, st);
+			rc = launch(P, B, &a, B->lpr, grid, st);
 		}
 		cudaError_t const ec = cudaStreamEndCapture(st, &g);
 		if (!rc && ec != cudaSuccess) rc = bfail("stream capture failed: %s", cudaGetErrorString(ec));
@@ -850,6 +1522,41 @@ int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gp
 	BCK(cudaGraphLaunch(B->step_graph, st));
 	BCK(cudaEventRecord(B->ev[1], st));
 	return 0;
+}
+
+int bfm_gpu_problem_parts_coarse(bfm_gpu_problem_t* P, int* n_coarse, int64_t* ainv_offsets, float* ainv) {
+	g_berr[0] = 0;
+	BatchState* B = state_of(P);
+	if (!B) return bfail("no parts set");
+	if (!B->two || !B->cb_built) return bfail("no two-level solve of this batch yet");
+	bfmi_buffers_t bf;
+	bfmi_buffers(P, &bf);
+	BCK(cudaStreamSynchronize((cudaStream_t) bf.stream));
+	int const np = B->n_parts;
+	int* pc = (int*) malloc(sizeof(int) * (np + 1));
+	long long* off = (long long*) malloc(sizeof(long long) * (np + 1));
+	if (!pc || !off) {
+		free(pc);
+		free(off);
+		return bfail("out of host memory");
+	}
+	int rc = 0;
+	if (cudaMemcpy(pc, B->part_cell, sizeof(int) * (np + 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
+	    cudaMemcpy(off, B->ainv_off, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost) != cudaSuccess)
+		rc = bfail("cudaMemcpy failed");
+	if (!rc) {
+		for (int k = 0; k < np; k++) {
+			if (n_coarse) n_coarse[k] = 3 * (pc[k + 1] - pc[k]);
+			if (ainv_offsets) ainv_offsets[k] = off[k];
+		}
+		if (ainv_offsets) ainv_offsets[np] = off[np];
+		if (ainv && off[np] > 0 &&
+		    cudaMemcpy(ainv, B->ainv, sizeof(float) * (size_t) off[np], cudaMemcpyDeviceToHost) != cudaSuccess)
+			rc = bfail("cudaMemcpy failed");
+	}
+	free(pc);
+	free(off);
+	return rc;
 }
 
 int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* P, int* iterations, int* status, int* replacements, double* rel_residual,

@@ -3245,6 +3245,16 @@ int bfmi_buffers(bfm_gpu_problem_t* P, bfmi_buffers_t* o) {
 	return 0;
 }
 
+int bfmi_set_precond(bfm_gpu_problem_t* P, int precond) {
+	if (precond != BFM_GPU_PC_JACOBI && precond != BFM_GPU_PC_BLOCK_JACOBI)
+		return fail("bfmi_set_precond: Jacobi or block Jacobi only, got %d", precond);
+	if (P->precond != precond) {
+		P->precond = precond;
+		P->assembled = 0;  // the preconditioner is formed by the assembly epilogue
+	}
+	return 0;
+}
+
 void** bfmi_ext_slot(bfm_gpu_problem_t* P, void (**free_fn)(void*)) {
 	if (free_fn) P->ext_free = *free_fn;
 	return &P->ext;

@@ -88,6 +88,11 @@ __attribute__((visibility("hidden"))) int bfmi_sparse_solve(bfm_matrix_t* A, bfm
 /* Extension slot of a problem: freed by bfm_gpu_problem_destroy. */
 __attribute__((visibility("hidden"))) void** bfmi_ext_slot(struct bfm_gpu_problem* P, void (**free_fn)(void*));
 
+/* Preconditioner layout of the next assembly (BFM_GPU_PC_JACOBI: 2 values per
+ * node, BFM_GPU_PC_BLOCK_JACOBI: the inverse 2x2 diagonal block); a change
+ * marks the problem unassembled.  Used by the batched solver. */
+__attribute__((visibility("hidden"))) int bfmi_set_precond(struct bfm_gpu_problem* P, int precond);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,15 @@ enum {
 	BFM_GPU_PC_SSOR2 = 5,
 	/* The two-level form with the network's relaxation blocks. */
 	BFM_GPU_PC_LEARNED_SSOR2 = 6,
+	/* Batched solver only (bfm_gpu_problem_solve_parts / _step_parts): two-level
+	 * block Jacobi, M^-1 = D^-1 + P A_c^-1 P^T per part, with D the nodes' 2x2
+	 * diagonal blocks and P the rigid-body modes of the cells of a grid over
+	 * each part's bounding box (about one cell per 64 nodes,
+	 * BFM_GPU_BATCH_COARSE_NODES; at most 64 cells per part).  A_c = P^T A P
+	 * and its inverse are formed on the device at every step, inside the
+	 * step's graph.  The iteration count then depends little on a part's
+	 * size, so the persistent kernel no longer waits on its largest part. */
+	BFM_GPU_PC_TWO_LEVEL_JACOBI = 7,
 };
 
 /* solver status codes (bfm_gpu_stats_t.status) */
@@ -281,6 +290,12 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t
  * bfm_gpu_problem_set_* captures again.  Asynchronous; statistics via
  * bfm_gpu_problem_part_stats (ms_solve: the device time of the whole step). */
 int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* problem, int precision, const bfm_gpu_opts_t* opts);
+
+/* After a batched solve with BFM_GPU_PC_TWO_LEVEL_JACOBI: per part its number
+ * of coarse DOFs (3 per cell) and where its A_c^-1 starts in `ainv`
+ * (ainv_offsets has n_parts + 1 entries), and every part's A_c^-1 (FP32,
+ * dense, row-major; ainv_offsets[n_parts] floats).  Any pointer may be NULL. */
+int bfm_gpu_problem_parts_coarse(bfm_gpu_problem_t* problem, int* n_coarse, int64_t* ainv_offsets, float* ainv);
 
 /* Wait, then per part (arrays of n_parts, any may be NULL): iterations,
  * status (BFM_GPU_*), FP64 residual replacements, FP64 relative residual;

@@ -190,7 +190,89 @@ class TwoLevel:
 
 
 def free_dofs(A: sp.spmatrix) -> np.ndarray:
-    """DOFs whose row is not an eliminated Dirichlet row (a lone 1 on the diagonal)."""
-    A = sp.csr_matrix(A)
+    """DOFs whose row is not an eliminated Dirichlet row (a lone 1 on the
+    diagonal).  Explicitly stored zeros do not count: the oracle's assembly
+    keeps the structural pattern, zeros of eliminated rows included."""
+    A = sp.csr_matrix(A, copy=True)
+    A.eliminate_zeros()
     nnz = np.diff(A.indptr)
     return ~((nnz == 1) & (A.diagonal() == 1.0))
+
+
+# ---------------------------------------------------------------- batched two-level block Jacobi
+
+def part_grid(n: int, w: float, h: float, per_cell: int = 64, max_cells: int = 64):
+    """Cell counts (gx, gy) of one part's coarse grid in the batched solver's
+    two-level block Jacobi (bfm_gb300/csrc/batch.cu, part_grid): about one
+    cell per `per_cell` nodes, at most `max_cells`, as square as the part's
+    bounding box allows (gy rounded, then capped so gx gy stays within the
+    target)."""
+    target = min(max(n // per_cell, 1), max_cells)
+    gx = gy = 1
+    if w > 0 and h > 0:
+        gx = min(max(int(np.floor(np.sqrt(target * w / h) + 0.5)), 1), target)
+        gy = max(min(int(np.floor(target / gx + 0.5)), target // gx), 1)
+    elif w > 0:
+        gx = target
+    elif h > 0:
+        gy = target
+    return gx, gy
+
+
+class BlockJacobi:
+    """z = D^-1 r, D the nodes' 2x2 diagonal blocks of A (scalar CSR)."""
+
+    def __init__(self, A: sp.spmatrix):
+        A = sp.csr_matrix(A)
+        n = A.shape[0] // 2
+        D = np.zeros((n, 2, 2))
+        idx = np.arange(n)
+        for a in range(2):
+            for b in range(2):
+                D[:, a, b] = np.asarray(A[2 * idx + a, 2 * idx + b]).ravel()
+        self.Dinv = np.linalg.inv(D)
+
+    def apply(self, r: np.ndarray) -> np.ndarray:
+        return np.einsum("nij,nj->ni", self.Dinv, r.reshape(-1, 2)).ravel()
+
+
+class TwoLevelJacobi:
+    """One part of the batched solver's two-level block Jacobi: z = D^-1 r +
+    P A_c^-1 P^T r, with the part_grid cells over the part's bounding box, P
+    per node [[f0, 0, -f0 dy], [0, f1, f1 dx]] ((dx, dy) the offset from the
+    cell's centre over H = max(cell width, height), rounded to FP32 as the GPU
+    stores it; f = 0 on an eliminated DOF) and A_c = P^T A P on the coarse DOFs
+    A sees (the GPU drops a coarse DOF whose pivot in the Cholesky of the
+    diagonally scaled A_c falls below 1e-5; here the ones with a zero
+    diagonal).  A and coords of the part alone; `free` per DOF."""
+
+    def __init__(self, A: sp.spmatrix, coords: np.ndarray, free: np.ndarray, per_cell: int = 64, max_cells: int = 64):
+        A = sp.csr_matrix(A)
+        n = len(coords)
+        x0, y0 = coords.min(0)
+        w, h = coords.max(0) - coords.min(0)
+        gx, gy = part_grid(n, w, h, per_cell, max_cells)
+        cw = w * (1 + 1e-12) / gx if w > 0 else 1.0
+        ch = h * (1 + 1e-12) / gy if h > 0 else 1.0
+        H = max(cw, ch)
+        cx = np.clip(((coords[:, 0] - x0) / cw).astype(np.int64), 0, gx - 1)
+        cy = np.clip(((coords[:, 1] - y0) / ch).astype(np.int64), 0, gy - 1)
+        cell = cx + gx * cy
+        dx = ((coords[:, 0] - (x0 + (cx + 0.5) * cw)) / H).astype(np.float32).astype(np.float64)
+        dy = ((coords[:, 1] - (y0 + (cy + 0.5) * ch)) / H).astype(np.float32).astype(np.float64)
+        f0, f1 = free[0::2].astype(float), free[1::2].astype(float)
+        idx = np.arange(n)
+        rows = np.concatenate([2 * idx, 2 * idx, 2 * idx + 1, 2 * idx + 1])
+        cols = np.concatenate([3 * cell, 3 * cell + 2, 3 * cell + 1, 3 * cell + 2])
+        vals = np.concatenate([f0, -dy * f0, f1, dx * f1])
+        P = sp.csr_matrix((vals, (rows, cols)), shape=(2 * n, 3 * gx * gy))
+        Ac = (P.T @ A @ P).toarray()
+        Ac = 0.5 * (Ac + Ac.T)
+        keep = np.diag(Ac) > 0
+        self.P = P[:, keep].tocsr()
+        self.Ainv = np.linalg.inv(Ac[np.ix_(keep, keep)])
+        self.smoother = BlockJacobi(A)
+        self.n_cells = gx * gy
+
+    def apply(self, r: np.ndarray) -> np.ndarray:
+        return self.smoother.apply(r) + self.P @ (self.Ainv @ (self.P.T @ r))

@@ -132,12 +132,13 @@ def test_perforated_methods_vs_direct(libbfm, perforated, name):
         D.close()
 
 
-def test_batch_256_uneven_vs_direct(libbfm):
+@pytest.mark.parametrize("pc", [bfm_gb300.PC_JACOBI, bfm_gb300.PC_TWO_LEVEL_JACOBI])
+def test_batch_256_uneven_vs_direct(libbfm, pc):
     ps = M.batch_uneven(256, seed=4)
     B = BA.Batch(libbfm, ps)
     try:
         B.assemble(bfm_gb300.MIXED_EXACT)
-        B.solve(bfm_gb300.default_opts(rtol=1e-8))
+        B.solve(bfm_gb300.default_opts(rtol=1e-8, precond=pc))
         st = B.stats()
         xs = B.solutions()
     finally:
