@@ -109,6 +109,10 @@ struct BatchArgs {
 	const int* chunk_cell;   // first cell of the chunk
 	const int* part_chunk;   // chunks of part k: [part_chunk[k], part_chunk[k+1])
 	double* cdot;            // per chunk: its share of (r_c, y_c), the coarse part of (r, M r)
+	// block-per-part kernel (k_batch_block)
+	const int* node_off;     // nodes of part k: [node_off[k], node_off[k+1])
+	const int* block_part;   // the part of each block (largest parts first)
+	float* z;                // z = M r, materialized per node
 };
 
 struct Shared {
@@ -594,6 +598,271 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 		}
 }
 
+// ====================================================================== block per part
+//
+// k_batch_block: one thread block runs one part's whole PCG -- the same
+// mixed-precision iteration as k_batch_pcg (FP32 operator in difference form
+// and FP32 vectors, FP64 inner products from double-float partial sums, FP64
+// residual replacements, the same stopping rules) -- with block barriers only:
+// no grid barrier, no spin wait, no cooperative launch.  Blocks take the
+// parts largest first (block_part), so the longest solves start first.  With
+// TWO, z = D^-1 r + P A_c^-1 P^T r is formed in three block-local stages:
+// r_c = P^T r (a warp per cell, into shared memory), y_c = A_c^-1 r_c (a warp
+// per row of A_c^-1, into shared memory), z at every node.  All sums are in a
+// fixed order (lane strided, shuffle trees, warps in order): deterministic.
+
+constexpr int BB_MAX_T = 1024;
+constexpr int BB_MAX_NODES = 131072;  // larger parts go to the tiled persistent kernel
+
+// block-wide sum of per-thread doubles, warps in order (every thread calls;
+// every thread gets the result)
+__device__ __forceinline__ double bb_sum(double v) {
+	__shared__ double red[BB_MAX_T / 32];
+	__shared__ double total;
+	int const lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+	__syncthreads();  // red and total are free again
+	if (lane == 0) red[w] = v;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t = 0.0;
+		for (int k = 0; k < nw; k++) t += red[k];
+		total = t;
+	}
+	__syncthreads();
+	return total;
+}
+
+// z = M r over the part's nodes [n0, n1), returns (r, z) (block-wide)
+template <bool TWO>
+__device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* rcs, float* ys) {
+	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	int c0 = 0;
+	if (TWO) {
+		c0 = a.part_cell[k];
+		int const c1 = a.part_cell[k + 1], n = 3 * (c1 - c0);
+		// r_c = P^T r, a warp per cell (four nodes per lane in flight, summed in list order)
+		for (int c = c0 + warp; c < c1; c += nw) {
+			double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+			int const end = a.cell_ptr[c + 1];
+			for (int k0 = a.cell_ptr[c] + lane; k0 < end; k0 += 128) {
+				int id[4];
+				float2 rv[4];
+				float4 pq[4];
+#pragma unroll
+				for (int u = 0; u < 4; u++) id[u] = k0 + 32 * u < end ? a.cell_nodes[k0 + 32 * u] : -1;
+#pragma unroll
+				for (int u = 0; u < 4; u++) {
+					rv[u] = id[u] >= 0 ? __ldcg(reinterpret_cast<const float2*>(a.r) + id[u]) : make_float2(0.f, 0.f);
+					pq[u] = id[u] >= 0 ? a.pnode[id[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+				}
+#pragma unroll
+				for (int u = 0; u < 4; u++) {
+					if (id[u] < 0) continue;
+					double const x0 = pq[u].z != 0.f ? (double) rv[u].x : 0.0, x1 = pq[u].w != 0.f ? (double) rv[u].y : 0.0;
+					s0 += x0;
+					s1 += x1;
+					s2 += (double) pq[u].x * x1 - (double) pq[u].y * x0;
+				}
+			}
+			for (int o = 16; o; o >>= 1) {
+				s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+				s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+				s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+			}
+			if (lane == 0) {
+				rcs[3 * (c - c0)] = s0;
+				rcs[3 * (c - c0) + 1] = s1;
+				rcs[3 * (c - c0) + 2] = s2;
+			}
+		}
+		__syncthreads();
+		// y_c = A_c^-1 r_c, a warp per row, rounded to FP32
+		const float* __restrict__ A = a.ainv + a.ainv_off[k];
+		for (int i = warp; i < n; i += nw) {
+			const float* __restrict__ Ar = A + (long) i * n;
+			double s = 0.0;
+			for (int j0 = lane; j0 < n; j0 += 128) {
+				float v[4];
+#pragma unroll
+				for (int u = 0; u < 4; u++) v[u] = j0 + 32 * u < n ? __ldg(Ar + j0 + 32 * u) : 0.f;
+#pragma unroll
+				for (int u = 0; u < 4; u++)
+					if (j0 + 32 * u < n) s += (double) v[u] * rcs[j0 + 32 * u];
+			}
+			for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+			if (lane == 0) ys[i] = (float) s;
+		}
+		__syncthreads();
+	}
+	DF g = {0.f, 0.f};
+	for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
+		float2 const rv = __ldcg(reinterpret_cast<const float2*>(a.r) + i);
+		float z0, z1;
+		precond_apply(a.dinv, a.block_pc, i, rv.x, rv.y, z0, z1);
+		if (TWO) {
+			int const l = 3 * (a.node_cell[i] - c0);
+			float4 const pq = a.pnode[i];
+			z0 += pq.z * (ys[l] - pq.y * ys[l + 2]);
+			z1 += pq.w * (ys[l + 1] + pq.x * ys[l + 2]);
+		}
+		st2(a.z, i, z0, z1);
+		df_add_prod(g, rv.x, z0);
+		df_add_prod(g, rv.y, z1);
+	}
+	return bb_sum(df_value(g));
+}
+
+template <int LPR, bool TWO>
+__global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
+	__shared__ double rcs[BC_MAX_N];
+	__shared__ float ys[BC_MAX_N];
+	int const k = a.block_part[blockIdx.x];
+	int const n0 = a.node_off[k], n1 = a.node_off[k + 1];
+	int const sub = threadIdx.x % LPR;
+	int const rows_per_pass = blockDim.x / LPR;
+	// ---- init: x = dx = p = 0, r = b, z = M r
+	double bb = 0.0;
+	for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
+		double2 const bv = ld2(a.b, i);
+		st2(a.x, i, 0.0, 0.0);
+		st2(a.dx, i, 0.f, 0.f);
+		st2(a.r, i, (float) bv.x, (float) bv.y);
+		st2(a.p0, i, 0.f, 0.f);
+		bb += bv.x * bv.x + bv.y * bv.y;
+	}
+	double const bnorm2 = bb_sum(bb);  // its barriers also order the stores above
+	double gamma = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys);
+	double beta = 0.0, rho_ref = bnorm2;
+	double const tol2 = a.rtol * a.rtol * bnorm2;
+	int iter = 0, status = BFM_GPU_OK, nrepl = 0;
+	bool done = a.timing_iters > 0 ? false : bnorm2 == 0.0;
+	float* const p = a.p0;
+	while (!done) {
+		if (a.timing_iters > 0 && iter >= a.timing_iters) break;
+		// p = z + beta p
+		float const fb = (float) beta;
+		for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
+			float2 const zv = ld2(a.z, i), pv = ld2(p, i);
+			st2(p, i, zv.x + fb * pv.x, zv.y + fb * pv.y);
+		}
+		__syncthreads();
+		// q = A32 p in difference form, (p, q)
+		DF pq = {0.f, 0.f};
+		for (int base = n0; base < n1; base += rows_per_pass) {
+			int const row = base + (int) threadIdx.x / LPR;
+			bool const ok = row < n1;
+			int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+			float2 const pr = ok ? __ldcg(reinterpret_cast<const float2*>(p) + row) : make_float2(0.f, 0.f);
+			auto dg = [=](int c, float& d0, float& d1) {
+				float2 const pc = __ldcg(reinterpret_cast<const float2*>(p) + c);
+				d0 = pc.x - pr.x;
+				d1 = pc.y - pr.y;
+			};
+			float y0, y1;
+			row_product_pf<LPR, 4, float>(a.cols, a.vals, ks, ke, sub, dg, y0, y1);
+			if (ok && sub == 0) {
+				float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
+				y0 += cc.x * pr.x + cc.y * pr.y;
+				y1 += cc.z * pr.x + cc.w * pr.y;
+				st2(a.q, row, y0, y1);
+				df_add_prod(pq, pr.x, y0);
+				df_add_prod(pq, pr.y, y1);
+			}
+		}
+		double const d = bb_sum(df_value(pq));
+		if (!(d > 0.0) && a.timing_iters == 0) {
+			status = BFM_GPU_BREAKDOWN;
+			break;
+		}
+		float const alpha = d > 0.0 ? (float) (gamma / d) : 0.f;
+		// dx += alpha p, r -= alpha q, (r, r)
+		DF rr = {0.f, 0.f};
+		for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
+			float2 const pv = ld2(p, i), qv = ld2(a.q, i), rv = ld2(a.r, i), dv = ld2(a.dx, i);
+			st2(a.dx, i, dv.x + alpha * pv.x, dv.y + alpha * pv.y);
+			float const r0 = rv.x - alpha * qv.x, r1 = rv.y - alpha * qv.y;
+			st2(a.r, i, r0, r1);
+			df_add_prod(rr, r0, r0);
+			df_add_prod(rr, r1, r1);
+		}
+		double const rho = bb_sum(df_value(rr));
+		iter++;
+		double const gnew = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys);
+		beta = gamma != 0.0 ? gnew / gamma : 0.0;
+		gamma = gnew;
+		if (a.timing_iters > 0) continue;
+		if (iter >= a.max_iters) {
+			status = BFM_GPU_NOT_CONVERGED;
+			break;
+		}
+		if (!(gnew > 0.0) && gnew != 0.0) {
+			status = BFM_GPU_BREAKDOWN;
+			break;
+		}
+		if (gnew == 0.0 || rho <= a.drop2 * rho_ref || rho <= tol2) {
+			// FP64 residual replacement: x += dx, r = b - A x in FP64
+			for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
+				float2 const dv = ld2(a.dx, i);
+				double2 const xv = ld2(a.x, i);
+				st2(a.x, i, xv.x + (double) dv.x, xv.y + (double) dv.y);
+				st2(a.dx, i, 0.f, 0.f);
+			}
+			__syncthreads();
+			double e2 = 0.0;
+			const double* __restrict__ xx = a.x;
+			for (int base = n0; base < n1; base += rows_per_pass) {
+				int const row = base + (int) threadIdx.x / LPR;
+				bool const ok = row < n1;
+				int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
+				double2 const xi = ok ? __ldcg(reinterpret_cast<const double2*>(xx) + row) : make_double2(0.0, 0.0);
+				double2 const x0 = a.vals64 ? make_double2(0.0, 0.0) : xi;
+				auto gx = [xx, x0](int c, double& g0, double& g1) {
+					double2 const v = __ldcg(reinterpret_cast<const double2*>(xx) + c);
+					g0 = v.x - x0.x;
+					g1 = v.y - x0.y;
+				};
+				double y0, y1;
+				if (a.vals64) row_product<LPR, double>(a.cols, a.vals64, ks, ke, sub, gx, y0, y1);
+				else row_product<LPR, double>(a.cols, a.vals, ks, ke, sub, gx, y0, y1);
+				if (ok && sub == 0) {
+					if (!a.vals64) {
+						float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
+						y0 += (double) cc.x * xi.x + (double) cc.y * xi.y;
+						y1 += (double) cc.z * xi.x + (double) cc.w * xi.y;
+					}
+					double2 const bv = ld2(a.b, row);
+					double const e0 = bv.x - y0, e1 = bv.y - y1;
+					st2(a.r, row, (float) e0, (float) e1);
+					e2 += e0 * e0 + e1 * e1;
+				}
+			}
+			double const r2 = bb_sum(e2);
+			nrepl++;
+			rho_ref = r2;
+			gamma = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys);
+			if (r2 <= tol2) break;
+		}
+	}
+	// flush the grouped update; statistics
+	__syncthreads();
+	for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
+		float2 const dv = ld2(a.dx, i);
+		double2 const xv = ld2(a.x, i);
+		st2(a.x, i, xv.x + (double) dv.x, xv.y + (double) dv.y);
+		st2(a.dx, i, 0.f, 0.f);
+	}
+	if (threadIdx.x == 0) {
+		PartState& s = a.ps[k];
+		s.bnorm2 = bnorm2;
+		s.gamma = gamma;
+		s.iter = iter;
+		s.status = status;
+		s.replacements = nrepl;
+		s.done = 1;
+	}
+}
+
 // ||b - A x||^2 per part (FP64 operator), after the persistent solve
 __global__ void __launch_bounds__(BT) k_batch_residual(BatchArgs a) {
 	for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
@@ -847,6 +1116,11 @@ struct BatchState {
 	int* node_off_h;       // host copy of the part offsets
 	int rows_per_tile, lpr, tuned;
 	int n_tiles, grid;
+	// block-per-part kernel: used when every part has at most BB_MAX_NODES nodes
+	int use_block, bnt;    // bnt: threads per block (autotuned with lpr)
+	int* node_off_d;
+	int* block_part;       // parts by decreasing node count
+	int g_bnt, s_bnt;
 	int *tile_part, *tile_begin, *tile_end, *part_tile;
 	double* partials;
 	PartState* ps;
@@ -885,7 +1159,7 @@ void batch_free(void* p) {
 	void* d[] = {B->tile_part, B->tile_begin, B->tile_end, B->part_tile, B->partials, B->ps, B->bar, B->err,
 	             B->part_cell, B->cell_part, B->cell_ptr, B->cell_nodes, B->node_cell, B->cell_nbr, B->cell_xy,
 	             B->dxdy, B->pnode, B->ac, B->rc, B->cdot, B->ainv, B->zc, B->ainv_off, B->chunk_part, B->chunk_cell,
-	             B->part_chunk};
+	             B->part_chunk, B->node_off_d, B->block_part};
 	for (void* q : d)
 		if (q) cudaFree(q);
 	if (B->graph) cudaGraphExecDestroy(B->graph);
@@ -946,6 +1220,14 @@ int build_tiles(BatchState* B, int rpt) {
 	}
 	free(tp); free(tb); free(te); free(pt);
 	return rc;
+}
+
+void* kernel_of_block(int lpr, int two) {
+	switch (lpr) {
+	case 1: return two ? (void*) k_batch_block<1, true> : (void*) k_batch_block<1, false>;
+	case 2: return two ? (void*) k_batch_block<2, true> : (void*) k_batch_block<2, false>;
+	default: return two ? (void*) k_batch_block<4, true> : (void*) k_batch_block<4, false>;
+	}
 }
 
 void* kernel_of(int lpr, int two) {
@@ -1228,6 +1510,9 @@ BatchArgs batch_args(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* 
 	a.err = B->err;
 	a.polls = SPIN_LIMIT;
 	a.block_pc = bf.precond != BFM_GPU_PC_JACOBI;
+	a.node_off = B->node_off_d;
+	a.block_part = B->block_part;
+	a.z = (float*) bf.vec[3];
 	if (B->two) {
 		a.n_cells = B->n_cells;
 		a.part_cell = B->part_cell;
@@ -1282,8 +1567,15 @@ int launch(bfm_gpu_problem_t* P, BatchState* B, BatchArgs* a, int lpr, int grid,
 		}
 		BCK(cudaGetLastError());
 	}
-	void* params[1] = {a};
-	BCK(cudaLaunchCooperativeKernel(kernel_of(lpr, B->two), dim3(grid), dim3(BT), params, sizeof(Shared), st));
+	if (B->use_block) {
+		// one block per part, largest parts first; block barriers only
+		void* params[1] = {a};
+		BCK(cudaLaunchKernel(kernel_of_block(lpr, B->two), dim3(B->n_parts), dim3(B->bnt), params, 0, st));
+	}
+	else {
+		void* params[1] = {a};
+		BCK(cudaLaunchCooperativeKernel(kernel_of(lpr, B->two), dim3(grid), dim3(BT), params, sizeof(Shared), st));
+	}
 	k_batch_residual<<<grid, BT, 0, st>>>(*a);
 	k_batch_part_residual<<<(B->n_parts + 127) / 128, 128, 0, st>>>(*a);
 	BCK(cudaGetLastError());
@@ -1293,7 +1585,46 @@ int launch(bfm_gpu_problem_t* P, BatchState* B, BatchArgs* a, int lpr, int grid,
 // Project autotuner for the batch: rows per tile x lanes per row, each
 // candidate timed over 10 iterations of the persistent kernel on the
 // assembled batch (timing mode: no stopping test), fastest kept.
+// one timed launch of 10 iterations of the current shape (timing mode: no stopping test)
+int time_shape(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* o, cudaStream_t st, int lpr, int grid, float* ms) {
+	BatchArgs a = batch_args(P, B, o);
+	a.timing_iters = 10;
+	BCK(cudaEventRecord(B->ev[0], st));
+	if (launch(P, B, &a, lpr, grid, st)) return -1;
+	BCK(cudaEventRecord(B->ev[1], st));
+	BCK(cudaStreamSynchronize(st));
+	BCK(cudaEventElapsedTime(ms, B->ev[0], B->ev[1]));
+	int err = 0;
+	BCK(cudaMemcpy(&err, B->err, sizeof err, cudaMemcpyDeviceToHost));
+	if (err) return bfail("batch kernel barrier timed out during autotuning");
+	return 0;
+}
+
 int autotune(bfm_gpu_problem_t* P, BatchState* B, const bfm_gpu_opts_t* o, cudaStream_t st) {
+	if (B->use_block) {
+		// threads per block x lanes per row of the block-per-part kernel
+		int const nts[] = {256, 512, 1024};
+		int const lprs[] = {1, 2, 4};
+		int grid = 0;
+		if (coop_grid(2, B->two, &grid)) return -1;
+		float best = 1e30f;
+		int best_nt = 512, best_lpr = 2;
+		for (int nt : nts)
+			for (int lpr : lprs) {
+				B->bnt = nt;
+				float ms = 0;
+				if (time_shape(P, B, o, st, lpr, grid, &ms)) return -1;
+				if (ms < best) {
+					best = ms;
+					best_nt = nt;
+					best_lpr = lpr;
+				}
+			}
+		B->bnt = best_nt;
+		B->lpr = best_lpr;
+		B->tuned = 1;
+		return 0;
+	}
 	int const rpts[] = {128, 256, 512, 1024};
 	int const lprs[] = {1, 2, 4};
 	float best = 1e30f;
@@ -1356,6 +1687,33 @@ int bfm_gpu_problem_set_parts(bfm_gpu_problem_t* P, int n_parts, const int32_t* 
 	BCK(cudaEventCreate(&B->ev[0]));
 	BCK(cudaEventCreate(&B->ev[1]));
 	B->lpr = 2;
+	// the block-per-part kernel unless a part is too large for one block
+	// (BFM_GPU_BATCH_KERNEL=tiled asks for the tiled persistent kernel)
+	int maxn = 0;
+	for (int k = 0; k < n_parts; k++)
+		maxn = node_offsets[k + 1] - node_offsets[k] > maxn ? node_offsets[k + 1] - node_offsets[k] : maxn;
+	char const* kern = getenv("BFM_GPU_BATCH_KERNEL");
+	B->use_block = maxn <= BB_MAX_NODES && !(kern && strcmp(kern, "tiled") == 0);
+	B->bnt = 512;
+	int* order = (int*) malloc(sizeof(int) * n_parts);
+	if (!order) return bfail("out of host memory");
+	for (int k = 0; k < n_parts; k++) order[k] = k;
+	// largest first, ties in part order (insertion sort: n_parts <= 512)
+	for (int k = 1; k < n_parts; k++) {
+		int const v = order[k], nv = node_offsets[v + 1] - node_offsets[v];
+		int j = k - 1;
+		while (j >= 0 && node_offsets[order[j] + 1] - node_offsets[order[j]] < nv) {
+			order[j + 1] = order[j];
+			j--;
+		}
+		order[j + 1] = v;
+	}
+	cudaError_t e = cudaMalloc(&B->block_part, sizeof(int) * n_parts);
+	if (e == cudaSuccess) e = cudaMalloc(&B->node_off_d, sizeof(int) * (n_parts + 1));
+	if (e == cudaSuccess) e = cudaMemcpy(B->block_part, order, sizeof(int) * n_parts, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(B->node_off_d, node_offsets, sizeof(int) * (n_parts + 1), cudaMemcpyHostToDevice);
+	free(order);
+	if (e != cudaSuccess) return bfail("CUDA error %s", cudaGetErrorString(e));
 	return build_tiles(B, 256);
 }
 
@@ -1397,7 +1755,8 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		B->graph = nullptr;
 	}
 	bool const same = (B->graph || B->direct) && B->g_rtol == o.rtol && B->g_drop == o.replace_drop && B->g_iters == o.max_iters &&
-	                  B->g_rpt == B->rows_per_tile && B->g_lpr == B->lpr && B->g_polls == o.barrier_polls;
+	                  B->g_rpt == B->rows_per_tile && B->g_lpr == B->lpr && B->g_polls == o.barrier_polls &&
+	                  B->g_bnt == B->bnt;
 	if (!same) {
 		// one graph: reset of the barrier words, the persistent cooperative
 		// kernel, the per-part FP64 residuals
@@ -1435,6 +1794,7 @@ int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts
 		B->g_rpt = B->rows_per_tile;
 		B->g_lpr = B->lpr;
 		B->g_polls = o.barrier_polls;
+		B->g_bnt = B->bnt;
 	}
 	BCK(cudaEventRecord(B->ev[0], st));
 	if (B->graph) {
@@ -1467,7 +1827,7 @@ int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gp
 	bfmi_buffers(P, &bf);
 	cudaStream_t const st = (cudaStream_t) bf.stream;
 	bool const same = (B->step_graph || B->step_direct) && B->s_precision == precision && B->s_gen == bf.inputs_gen &&
-	                  B->s_rpt == B->rows_per_tile && B->s_lpr == B->lpr && B->s_opts.rtol == o.rtol &&
+	                  B->s_rpt == B->rows_per_tile && B->s_lpr == B->lpr && B->s_bnt == B->bnt && B->s_opts.rtol == o.rtol &&
 	                  B->s_opts.max_iters == o.max_iters && B->s_opts.replace_drop == o.replace_drop &&
 	                  B->s_opts.barrier_polls == o.barrier_polls && B->s_opts.autotune == o.autotune &&
 	                  B->s_opts.precond == o.precond;
@@ -1512,6 +1872,7 @@ int bfm_gpu_problem_step_parts(bfm_gpu_problem_t* P, int precision, const bfm_gp
 		B->s_gen = bf.inputs_gen;
 		B->s_rpt = B->rows_per_tile;
 		B->s_lpr = B->lpr;
+		B->s_bnt = B->bnt;
 		B->s_opts = o;
 	}
 	if (B->step_direct) {
@@ -1584,7 +1945,7 @@ int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* P, int* iterations, int* statu
 		if (rel_residual) rel_residual[k] = h[k].bnorm2 > 0 ? sqrt(h[k].true_res2 / h[k].bnorm2) : 0.0;
 	}
 	free(h);
-	if (rows_per_tile) *rows_per_tile = B->rows_per_tile;
+	if (rows_per_tile) *rows_per_tile = B->use_block ? B->bnt : B->rows_per_tile;
 	if (lanes_per_row) *lanes_per_row = B->lpr;
 	if (ms_solve) {
 		float ms = 0;

@@ -272,13 +272,19 @@ int bfm_gpu_problem_set_parts(bfm_gpu_problem_t* problem, int n_parts, const int
  * without this call every edge counts as one. */
 int bfm_gpu_problem_set_edge_boundary(bfm_gpu_problem_t* problem, const uint8_t* boundary, int where);
 
-/* Enqueue the batched solve: one persistent cooperative kernel in which each
- * part runs mixed-precision Jacobi-PCG (FP32 operator and vectors, FP64
- * inner products and residual replacement) with its own scalars and stopping
- * test, captured in a CUDA graph.  Needs an assembly in BFM_GPU_MIXED or
- * BFM_GPU_MIXED_EXACT.  With opts->autotune the first call times the tile
- * shapes (rows per tile x lanes per row) on this batch and keeps the fastest.
- * Grid barriers inside the kernel wait a bounded time, then report an error. */
+/* Enqueue the batched solve: one kernel launch in which each part runs
+ * mixed-precision PCG (FP32 operator and vectors, FP64 inner products and
+ * residual replacement) with its own scalars and stopping test, captured in a
+ * CUDA graph.  Preconditioner (opts->precond): BFM_GPU_PC_JACOBI,
+ * BFM_GPU_PC_BLOCK_JACOBI or BFM_GPU_PC_TWO_LEVEL_JACOBI.  When every part
+ * has at most 131,072 nodes, one thread block runs each part (block barriers
+ * only, largest parts launched first); otherwise, or with
+ * BFM_GPU_BATCH_KERNEL=tiled when the parts are set, one persistent
+ * cooperative kernel cuts the parts into row tiles, with grid barriers that
+ * wait a bounded time and then report an error.  Needs an assembly in
+ * BFM_GPU_MIXED or BFM_GPU_MIXED_EXACT.  With opts->autotune the first call
+ * times the shapes (threads per block, or rows per tile, x lanes per row) on
+ * this batch and keeps the fastest. */
 int bfm_gpu_problem_solve_parts(bfm_gpu_problem_t* problem, const bfm_gpu_opts_t* opts);
 
 /* One step of the batch -- assembly in `precision` (MIXED or MIXED_EXACT)
@@ -299,7 +305,9 @@ int bfm_gpu_problem_parts_coarse(bfm_gpu_problem_t* problem, int* n_coarse, int6
 
 /* Wait, then per part (arrays of n_parts, any may be NULL): iterations,
  * status (BFM_GPU_*), FP64 residual replacements, FP64 relative residual;
- * and the tile shape used and the device time of the last solve. */
+ * and the shape used (rows_per_tile: the threads per block of the
+ * block-per-part kernel, or the rows per tile of the tiled one; lanes per
+ * row) and the device time of the last solve. */
 int bfm_gpu_problem_part_stats(bfm_gpu_problem_t* problem, int* iterations, int* status, int* replacements,
                                double* rel_residual, int* rows_per_tile, int* lanes_per_row, double* ms_solve);
 

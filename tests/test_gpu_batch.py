@@ -3,6 +3,8 @@ mesh by mesh against the FP64 direct oracle (displacement error <= 1e-6,
 the mixed-precision bound), with the Jacobi and the two-level block Jacobi
 preconditioners; the two-level form's iteration counts against its float64
 restatement (oracle/ssor_ref.py, TwoLevelJacobi)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -14,6 +16,20 @@ from oracle import ssor_ref as S
 pytestmark = pytest.mark.gpu
 
 PCS = [bfm_gb300.PC_JACOBI, bfm_gb300.PC_TWO_LEVEL_JACOBI]
+KERNELS = ["block", "tiled"]  # one block per part (default) / the tiled persistent kernel
+
+
+def make_batch(lib, ps, kernel="block"):
+    """A Batch on the given kernel (chosen when the parts are set)."""
+    old = os.environ.get("BFM_GPU_BATCH_KERNEL")
+    os.environ["BFM_GPU_BATCH_KERNEL"] = kernel
+    try:
+        return BA.Batch(lib, ps)
+    finally:
+        if old is None:
+            del os.environ["BFM_GPU_BATCH_KERNEL"]
+        else:
+            os.environ["BFM_GPU_BATCH_KERNEL"] = old
 
 
 def small_batch(n=12, seed=9):
@@ -38,10 +54,11 @@ def small_batch(n=12, seed=9):
     return out
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("pc", PCS)
-def test_batch_matches_direct_oracle(libbfm, pc):
+def test_batch_matches_direct_oracle(libbfm, pc, kernel):
     ps = small_batch()
-    B = BA.Batch(libbfm, ps)
+    B = make_batch(libbfm, ps, kernel)
     try:
         B.assemble(bfm_gb300.MIXED_EXACT)
         B.solve(bfm_gb300.default_opts(rtol=1e-10, precond=pc))
@@ -104,13 +121,14 @@ def test_step_graph_matches_separate_calls(libbfm, pc):
         B.close()
 
 
-def test_two_level_operator_matches_restatement(libbfm):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_two_level_operator_matches_restatement(libbfm, kernel):
     """The two-level block Jacobi operator itself: after exactly one iteration
     each mesh's solution is alpha M b, so its direction must be that of the
     float64 restatement's M b (oracle/ssor_ref.py, TwoLevelJacobi).  The GPU
     forms A_c from the FP32 operator and A_c^-1 in FP32: agreement to 2e-3."""
     ps = small_batch(10, seed=11)
-    B = BA.Batch(libbfm, ps)
+    B = make_batch(libbfm, ps, kernel)
     try:
         B.assemble(bfm_gb300.MIXED_EXACT)
         B.solve(bfm_gb300.default_opts(rtol=1e-8, max_iters=1, precond=bfm_gb300.PC_TWO_LEVEL_JACOBI))
@@ -168,3 +186,24 @@ def test_two_level_cuts_the_tail(libbfm):
     print(f"jacobi {int(np.median(jac))}/{int(jac.max())}, two-level {int(np.median(two))}/{int(two.max())} (median/max)")
     assert two.max() * 3 <= jac.max()
     assert two.max() <= 2 * np.median(two)
+
+
+@pytest.mark.parametrize("pc", PCS)
+def test_block_and_tiled_kernels_agree(libbfm, pc):
+    """The block-per-part kernel and the tiled persistent kernel run the same
+    iteration: every mesh converges in both, with solutions within the
+    mixed-precision bound of each other and about the same iteration counts."""
+    ps = small_batch(12, seed=21)
+    out = {}
+    for kernel in KERNELS:
+        B = make_batch(libbfm, ps, kernel)
+        try:
+            B.assemble(bfm_gb300.MIXED_EXACT)
+            B.solve(bfm_gb300.default_opts(rtol=1e-8, precond=pc))
+            out[kernel] = (B.stats(), np.concatenate(B.solutions()))
+        finally:
+            B.close()
+    (sb, xb), (st, xt) = out["block"], out["tiled"]
+    assert np.all(sb["status"] == 0) and np.all(st["status"] == 0)
+    assert np.linalg.norm(xb - xt) <= 1e-6 * np.linalg.norm(xt)
+    assert np.all(np.abs(sb["iterations"] - st["iterations"]) <= 0.1 * st["iterations"] + 5)
