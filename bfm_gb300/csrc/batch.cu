@@ -935,33 +935,15 @@ __global__ void k_bpnode(CoarseSetArgs a) {
 	a.pnode[i] = make_float4(d.x, d.y, a.last_ci[2 * i] < 0 ? 1.f : 0.f, a.last_ci[2 * i + 1] < 0 ? 1.f : 0.f);
 }
 
-// the 2x3 block P_i, or zero
-__device__ __forceinline__ void p_block(float4 q, bool on, double p[2][3]) {
-	double const f0 = on ? q.z : 0.f, f1 = on ? q.w : 0.f;
-	p[0][0] = f0;  p[0][1] = 0.0; p[0][2] = -f0 * (double) q.y;
-	p[1][0] = 0.0; p[1][1] = f1;  p[1][2] = f1 * (double) q.x;
-}
-
-// acc += P_r^T (M d), M a 2x2 block, d and P_r 2x3
-__device__ __forceinline__ void acc_ptmd(double acc[9], const double pr[2][3], double m0, double m1, double m2, double m3,
-                                         const double d[2][3]) {
-#pragma unroll
-	for (int b = 0; b < 3; b++) {
-		double const t0 = m0 * d[0][b] + m1 * d[1][b];
-		double const t1 = m2 * d[0][b] + m3 * d[1][b];
-#pragma unroll
-		for (int q = 0; q < 3; q++) acc[3 * q + b] += pr[0][q] * t0 + pr[1][q] * t1;
-	}
-}
-
 // A_c(I, J) = sum over the nodes r of cell I of P_r^T (K P^(J))_r, with the
 // operator in difference form: (K P^(J))_r = S_r P^(J)_r + sum_{c != r}
 // K_rc (P^(J)_c - P^(J)_r), P^(J)_c = P_c when c lies in cell J, else 0.
-// One thread per (cell, slot); the 9 threads of a cell walk the same rows in
-// the same order (FP64 sums, deterministic).  Translations of interior nodes
+// One warp per (cell, slot), lanes over the cell's nodes, FP64 sums per lane
+// then a fixed shuffle tree (deterministic).  Translations of interior nodes
 // cancel exactly in the differences, so no large terms cancel in the sums.
 __global__ void k_bcoarse_ac(CoarseSetArgs a) {
-	long const t = (long) blockIdx.x * blockDim.x + threadIdx.x;
+	long const t = ((long) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	int const lane = threadIdx.x & 31;
 	if (t >= 9l * a.n_cells) return;
 	int const I = (int) (t / 9), slot = (int) (t % 9);
 	int const J = a.cell_nbr[9l * I + slot];
@@ -970,7 +952,7 @@ __global__ void k_bcoarse_ac(CoarseSetArgs a) {
 	for (int e = 0; e < 9; e++) acc[e] = 0.0;
 	if (J >= 0) {
 		bool const same = J == I;
-		for (int k = a.cell_ptr[I]; k < a.cell_ptr[I + 1]; k++) {
+		for (int k = a.cell_ptr[I] + lane; k < a.cell_ptr[I + 1]; k += 32) {
 			int const r = a.cell_nodes[k];
 			double pr[2][3], prj[2][3];
 			p_block(a.pnode[r], true, pr);
@@ -995,9 +977,14 @@ __global__ void k_bcoarse_ac(CoarseSetArgs a) {
 			}
 		}
 	}
-	double* o = a.ac + 81l * I + 9 * slot;
 #pragma unroll
-	for (int e = 0; e < 9; e++) o[e] = acc[e];
+	for (int e = 0; e < 9; e++)
+		for (int o = 16; o; o >>= 1) acc[e] += __shfl_xor_sync(0xffffffffu, acc[e], o);
+	if (lane == 0) {
+		double* o = a.ac + 81l * I + 9 * slot;
+#pragma unroll
+		for (int e = 0; e < 9; e++) o[e] = acc[e];
+	}
 }
 
 // entry (i, j) of a part's A_c (cells from c0), 0 where the cells are not neighbours
@@ -1260,7 +1247,7 @@ void part_grid(int n, double w, double h, int per_cell, int* gx, int* gy) {
 int coarse_nodes_per_cell() {
 	char const* e = getenv("BFM_GPU_BATCH_COARSE_NODES");
 	int const v = e ? atoi(e) : 0;
-	return v >= 16 ? v : 64;
+	return v >= 16 ? v : 48;
 }
 
 // The two-level coarse space of every part: its cell grid, the cell of each
@@ -1562,7 +1549,7 @@ int launch(bfm_gpu_problem_t* P, BatchState* B, BatchArgs* a, int lpr, int grid,
 		int const smem = B->nmax * B->nmax * (int) sizeof(float);
 		if (c.N > 0) k_bpnode<<<(c.N + 255) / 256, 256, 0, st>>>(c);
 		if (c.n_cells > 0) {
-			k_bcoarse_ac<<<(int) ((9l * c.n_cells + 127) / 128), 128, 0, st>>>(c);
+			k_bcoarse_ac<<<(int) ((9l * 32 * c.n_cells + 127) / 128), 128, 0, st>>>(c);
 			k_bcoarse_inv<<<B->n_parts, BC_INV_T, smem, st>>>(c);
 		}
 		BCK(cudaGetLastError());

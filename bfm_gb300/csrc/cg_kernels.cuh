@@ -2155,6 +2155,26 @@ __global__ void __launch_bounds__(TPB_K, 8) k_ssor_all(SsorArgs a) {
 	if (grid_sum<1>(v, a.partials, a.ticket, out) && threadIdx.x == 0) ssor_finish(a, out[0]);
 }
 
+// the 2x3 block P_i = [[f0, 0, -f0 dy], [0, f1, f1 dx]] of a node with
+// q = (dx, dy, f0, f1), or zero
+__device__ __forceinline__ void p_block(float4 q, bool on, double p[2][3]) {
+	double const f0 = on ? q.z : 0.f, f1 = on ? q.w : 0.f;
+	p[0][0] = f0;  p[0][1] = 0.0; p[0][2] = -f0 * (double) q.y;
+	p[1][0] = 0.0; p[1][1] = f1;  p[1][2] = f1 * (double) q.x;
+}
+
+// acc += P_r^T (M d), M a 2x2 block, d and P_r 2x3
+__device__ __forceinline__ void acc_ptmd(double acc[9], const double pr[2][3], double m0, double m1, double m2, double m3,
+                                         const double d[2][3]) {
+#pragma unroll
+	for (int b = 0; b < 3; b++) {
+		double const t0 = m0 * d[0][b] + m1 * d[1][b];
+		double const t1 = m2 * d[0][b] + m3 * d[1][b];
+#pragma unroll
+		for (int q = 0; q < 3; q++) acc[3 * q + b] += pr[0][q] * t0 + pr[1][q] * t1;
+	}
+}
+
 // A_c = P^T A P in two deterministic stages.  One warp per chunk of
 // aggregate I: every lane keeps the 3x3 blocks of the 9 cells around I (slot
 // = cell offset), so the lanes' partial sums line up and are reduced in a

@@ -71,7 +71,7 @@ enum {
 	/* Batched solver only (bfm_gpu_problem_solve_parts / _step_parts): two-level
 	 * block Jacobi, M^-1 = D^-1 + P A_c^-1 P^T per part, with D the nodes' 2x2
 	 * diagonal blocks and P the rigid-body modes of the cells of a grid over
-	 * each part's bounding box (about one cell per 64 nodes,
+	 * each part's bounding box (about one cell per 48 nodes,
 	 * BFM_GPU_BATCH_COARSE_NODES; at most 64 cells per part).  A_c = P^T A P
 	 * and its inverse are formed on the device at every step, inside the
 	 * step's graph.  The iteration count then depends little on a part's

@@ -201,7 +201,7 @@ def free_dofs(A: sp.spmatrix) -> np.ndarray:
 
 # ---------------------------------------------------------------- batched two-level block Jacobi
 
-def part_grid(n: int, w: float, h: float, per_cell: int = 64, max_cells: int = 64):
+def part_grid(n: int, w: float, h: float, per_cell: int = 48, max_cells: int = 64):
     """Cell counts (gx, gy) of one part's coarse grid in the batched solver's
     two-level block Jacobi (bfm_gb300/csrc/batch.cu, part_grid): about one
     cell per `per_cell` nodes, at most `max_cells`, as square as the part's
@@ -246,7 +246,7 @@ class TwoLevelJacobi:
     diagonally scaled A_c falls below 1e-5; here the ones with a zero
     diagonal).  A and coords of the part alone; `free` per DOF."""
 
-    def __init__(self, A: sp.spmatrix, coords: np.ndarray, free: np.ndarray, per_cell: int = 64, max_cells: int = 64):
+    def __init__(self, A: sp.spmatrix, coords: np.ndarray, free: np.ndarray, per_cell: int = 48, max_cells: int = 64):
         A = sp.csr_matrix(A)
         n = len(coords)
         x0, y0 = coords.min(0)
