@@ -540,7 +540,7 @@ def main():
         # solve launches it: with the two-level correction's stages inside when
         # they are fused (then its bytes count too), else the sweeps alone
         co = r["coarse"]
-        fused = bool(co["fused"]) and r["persistent"]
+        fused = bool(co["fused"]) and bool(r["persistent"])
         b_pc = algorithmic_bytes_ssor(nb, p.n_nodes, r["prec"])
         t_pc = r["ms_sweeps"]
         if fused:

@@ -696,6 +696,7 @@ __device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* 
 		__syncthreads();
 	}
 	DF g = {0.f, 0.f};
+	#pragma unroll 4
 	for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
 		float2 const rv = __ldcg(reinterpret_cast<const float2*>(a.r) + i);
 		float z0, z1;
@@ -742,32 +743,48 @@ __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
 		if (a.timing_iters > 0 && iter >= a.timing_iters) break;
 		// p = z + beta p
 		float const fb = (float) beta;
+		#pragma unroll 4
 		for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
 			float2 const zv = ld2(a.z, i), pv = ld2(p, i);
 			st2(p, i, zv.x + fb * pv.x, zv.y + fb * pv.y);
 		}
 		__syncthreads();
-		// q = A32 p in difference form, (p, q)
+		// q = A32 p in difference form, (p, q); two rows per thread per pass
+		// (independent gathers in flight), summed into (p, q) in row order
 		DF pq = {0.f, 0.f};
-		for (int base = n0; base < n1; base += rows_per_pass) {
-			int const row = base + (int) threadIdx.x / LPR;
-			bool const ok = row < n1;
-			int const ks = ok ? a.row_ptr[row] : 0, ke = ok ? a.row_ptr[row + 1] : 0;
-			float2 const pr = ok ? __ldcg(reinterpret_cast<const float2*>(p) + row) : make_float2(0.f, 0.f);
-			auto dg = [=](int c, float& d0, float& d1) {
-				float2 const pc = __ldcg(reinterpret_cast<const float2*>(p) + c);
-				d0 = pc.x - pr.x;
-				d1 = pc.y - pr.y;
-			};
-			float y0, y1;
-			row_product_pf<LPR, 4, float>(a.cols, a.vals, ks, ke, sub, dg, y0, y1);
-			if (ok && sub == 0) {
-				float4 const cc = reinterpret_cast<const float4*>(a.corr)[row];
-				y0 += cc.x * pr.x + cc.y * pr.y;
-				y1 += cc.z * pr.x + cc.w * pr.y;
-				st2(a.q, row, y0, y1);
-				df_add_prod(pq, pr.x, y0);
-				df_add_prod(pq, pr.y, y1);
+		for (int base = n0; base < n1; base += 2 * rows_per_pass) {
+			int rw[2], ks[2], ke[2];
+			bool ok[2];
+			float2 pr[2];
+#pragma unroll
+			for (int h = 0; h < 2; h++) {
+				rw[h] = base + h * rows_per_pass + (int) threadIdx.x / LPR;
+				ok[h] = rw[h] < n1;
+				ks[h] = ok[h] ? a.row_ptr[rw[h]] : 0;
+				ke[h] = ok[h] ? a.row_ptr[rw[h] + 1] : 0;
+				pr[h] = ok[h] ? __ldcg(reinterpret_cast<const float2*>(p) + rw[h]) : make_float2(0.f, 0.f);
+			}
+			float y0[2], y1[2];
+#pragma unroll
+			for (int h = 0; h < 2; h++) {
+				float2 const prh = pr[h];
+				auto dg = [=](int c, float& d0, float& d1) {
+					float2 const pc = __ldcg(reinterpret_cast<const float2*>(p) + c);
+					d0 = pc.x - prh.x;
+					d1 = pc.y - prh.y;
+				};
+				row_product_pf<LPR, 4, float>(a.cols, a.vals, ks[h], ke[h], sub, dg, y0[h], y1[h]);
+			}
+#pragma unroll
+			for (int h = 0; h < 2; h++) {
+				if (ok[h] && sub == 0) {
+					float4 const cc = reinterpret_cast<const float4*>(a.corr)[rw[h]];
+					float const q0 = y0[h] + cc.x * pr[h].x + cc.y * pr[h].y;
+					float const q1 = y1[h] + cc.z * pr[h].x + cc.w * pr[h].y;
+					st2(a.q, rw[h], q0, q1);
+					df_add_prod(pq, pr[h].x, q0);
+					df_add_prod(pq, pr[h].y, q1);
+				}
 			}
 		}
 		double const d = bb_sum(df_value(pq));
@@ -778,6 +795,7 @@ __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
 		float const alpha = d > 0.0 ? (float) (gamma / d) : 0.f;
 		// dx += alpha p, r -= alpha q, (r, r)
 		DF rr = {0.f, 0.f};
+		#pragma unroll 4
 		for (int i = n0 + threadIdx.x; i < n1; i += blockDim.x) {
 			float2 const pv = ld2(p, i), qv = ld2(a.q, i), rv = ld2(a.r, i), dv = ld2(a.dx, i);
 			st2(a.dx, i, dv.x + alpha * pv.x, dv.y + alpha * pv.y);

@@ -9,6 +9,7 @@ and its first poll for all of them): the solve must end with the timeout
 status and an error, without hanging, and the same problem must solve
 normally right after with the default limit."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -49,8 +50,19 @@ def test_barrier_timeout_reports_and_recovers(libbfm, precision):
 
 
 def test_batch_barrier_timeout_reports_and_recovers(libbfm):
+    """The tiled persistent batch kernel (the one with grid barriers; the
+    block-per-part kernel has none) gives up a barrier after one poll, the
+    statistics call reports it, and the next solve of the same batch runs."""
     ps = M.batch_uneven(4, seed=11)
-    B = BA.Batch(libbfm, ps)
+    old = os.environ.get("BFM_GPU_BATCH_KERNEL")
+    os.environ["BFM_GPU_BATCH_KERNEL"] = "tiled"
+    try:
+        B = BA.Batch(libbfm, ps)
+    finally:
+        if old is None:
+            del os.environ["BFM_GPU_BATCH_KERNEL"]
+        else:
+            os.environ["BFM_GPU_BATCH_KERNEL"] = old
     try:
         B.assemble(bfm_gb300.MIXED_EXACT)
         o = bfm_gb300.default_opts(rtol=1e-8, autotune=0, barrier_polls=1)
