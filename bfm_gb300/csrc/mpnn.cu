@@ -700,6 +700,180 @@ __global__ void k_to_bf16(int n, const float* theta, bf16* wb) {
 	if (k < n) wb[k] = __float2bfloat16(theta[k]);
 }
 
+
+// ---------------------------------------------------------------- tcgen05 forward layer
+//
+// y = relu(x W^T + bias) for a 128-node tile per MMA, on the fifth-generation
+// tensor cores: the x tile (128 x K BF16) and W (64 x K BF16) are staged in
+// shared memory in the canonical K-major layout without swizzle (core
+// matrices of 8 rows x 16 bytes: element (m, k) of a 16-wide K-slice s at
+// s * slice_bytes + (m / 8) * 256 + ((k % 16) / 8) * 128 + (m % 8) * 16 +
+// (k % 8) * 2, so core matrices adjacent along K are 128 bytes apart and along
+// M (or N) 256 bytes); one elected thread issues K / 16 tcgen05.mma
+// (kind::f16, M = 128, N = 64, BF16 in, FP32 accumulator in 64 TMEM columns)
+// and commits them to an mbarrier; after a bounded wait each warp reads its 32
+// TMEM lanes (rows) with tcgen05.ld and applies bias and ReLU.  A wait that
+// runs out sets *err and the block stops issuing MMAs; TMEM is freed on every
+// path.
+constexpr int TC_M = 128;               // nodes per tile (the MMA's M)
+constexpr int TC_T = 128;               // threads: warp w reads TMEM lanes 32w .. 32w + 31
+constexpr long TC_POLLS = 1l << 24;     // mbarrier polls before a wait gives up
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t) __cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading-dimension byte
+// offset (between core matrices along K), stride byte offset (along M or N),
+// all in 16-byte units; descriptor version 1 (bits 46-47); no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+	return (uint64_t) ((addr >> 4) & 0x3FFFu) | ((uint64_t) ((lbo >> 4) & 0x3FFFu) << 16) |
+	       ((uint64_t) ((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), A and
+// B BF16 (bits 7-9 and 10-12 = 1), both K-major, N / 8 at bit 17, M / 16 at bit 24
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t) (N >> 3) << 17) | ((uint32_t) (M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool tc_mbar_try(uint32_t bar, uint32_t parity) {
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	             : "=r"(ok)
+	             : "r"(bar), "r"(parity)
+	             : "memory");
+	return ok != 0;
+}
+
+// 16 consecutive accumulator columns of this warp's 32 lanes
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+	asm volatile(
+	    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+	    "[%16];"
+	    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+	      "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+	    : "r"(taddr)
+	    : "memory");
+}
+
+constexpr size_t tc_smem_bytes(int K) { return (size_t) (TC_M + HID) * K * sizeof(bf16); }
+
+template <int K>
+__global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __restrict__ x0, const bf16* __restrict__ x1,
+                                                       const bf16* __restrict__ w, const float* __restrict__ bias,
+                                                       bf16* __restrict__ y, int* err) {
+	extern __shared__ __align__(1024) unsigned char tc_sm[];
+	constexpr int NS = K / 16;   // MMA K-slices
+	constexpr int CH = K / 8;    // 16-byte chunks per row
+	unsigned char* const xs = tc_sm;                        // x tile, slice s at s * TC_M * 32 bytes
+	unsigned char* const ws = tc_sm + (size_t) TC_M * K * 2;  // W, slice s at s * HID * 32 bytes
+	__shared__ __align__(8) unsigned long long mbar;
+	__shared__ uint32_t tmem_slot;
+	__shared__ int s_ok;
+	__shared__ float bs[HID];
+	int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	for (int e = tid; e < HID * CH; e += TC_T) {
+		int const n = e / CH, q = e % CH;
+		uint4 const v = reinterpret_cast<const uint4*>(w)[e];  // row n of W, features 8q .. 8q + 7
+		*reinterpret_cast<uint4*>(ws + (q >> 1) * (HID * 32) + (n >> 3) * 256 + (q & 1) * 128 + (n & 7) * 16) = v;
+	}
+	if (tid < HID) bs[tid] = bias[tid];
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_slot)), "r"(HID)
+		             : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	if (tid == 0) {
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mbar)) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		s_ok = 1;
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	uint32_t const tmem = tmem_slot;
+	uint32_t const bar = tc_smem(&mbar);
+	uint32_t phase = 0;
+	int const tiles = (N + TC_M - 1) / TC_M;
+	for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+		int const node0 = tile * TC_M;
+		for (int e = tid; e < TC_M * CH; e += TC_T) {
+			int const m = e / CH, q = e % CH, node = node0 + m;
+			uint4 v = make_uint4(0u, 0u, 0u, 0u);
+			if (node < N) {
+				if (K == FIN) v = reinterpret_cast<const uint4*>(x0 + (long) node * FIN)[q];
+				else v = q < HID / 8 ? reinterpret_cast<const uint4*>(x0 + (long) node * HID)[q]
+				                     : reinterpret_cast<const uint4*>(x1 + (long) node * HID)[q - HID / 8];
+			}
+			*reinterpret_cast<uint4*>(xs + (q >> 1) * (TC_M * 32) + (m >> 3) * 256 + (q & 1) * 128 + (m & 7) * 16) = v;
+		}
+		// the generic-proxy stores above, then the tensor cores' (async-proxy) reads
+		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+		asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+		__syncthreads();
+		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+		bool const live = s_ok != 0;
+		if (!live) break;  // the same in every thread: a wait ran out
+		if (tid == 0) {
+#pragma unroll
+			for (int sl = 0; sl < NS; sl++) {
+				uint64_t const ad = tc_desc(tc_smem(xs) + sl * TC_M * 32, 128, 256);
+				uint64_t const bd = tc_desc(tc_smem(ws) + sl * HID * 32, 128, 256);
+				asm volatile(
+				    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+				    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+				    "l"(ad), "l"(bd), "r"(tc_idesc(TC_M, HID)), "r"(sl > 0 ? 1 : 0)
+				    : "memory");
+			}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+			             : "memory");
+		}
+		bool got = false;
+		for (long it = 0; it < TC_POLLS; it++)
+			if (tc_mbar_try(bar, phase)) {
+				got = true;
+				break;
+			}
+		if (got) phase ^= 1u;  // else the drain below waits for this completion
+		else {
+			atomicExch(err, 1);
+			s_ok = 0;
+		}
+		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+		int const node = node0 + warp * 32 + lane;
+		uint32_t const taddr = tmem + ((uint32_t) (warp * 32) << 16);
+#pragma unroll
+		for (int c0 = 0; c0 < HID; c0 += 16) {
+			uint32_t r[16];
+			tc_ld16(taddr + c0, r);
+			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+			if (got && node < N) {
+				uint32_t pk[8];
+#pragma unroll
+				for (int j = 0; j < 8; j++) {
+					float const v0 = fmaxf(__uint_as_float(r[2 * j]) + bs[c0 + 2 * j], 0.f);
+					float const v1 = fmaxf(__uint_as_float(r[2 * j + 1]) + bs[c0 + 2 * j + 1], 0.f);
+					pk[j] = pack2(__float2bfloat16(v0), __float2bfloat16(v1));
+				}
+				uint4* dst = reinterpret_cast<uint4*>(y + (long) node * HID + c0);
+				dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+				dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+			}
+		}
+		asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+		__syncthreads();  // TMEM read and smem free before the next tile's MMAs
+		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	}
+	// a wait that ran out: one more bounded wait for the MMAs in flight, then free TMEM
+	if (!s_ok) {
+		for (long it = 0; it < TC_POLLS; it++)
+			if (tc_mbar_try(bar, phase)) break;
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(HID) : "memory");
+}
+
 inline int nb(long n, int t = 256) { return (int) ((n + t - 1) / t) > 0 ? (int) ((n + t - 1) / t) : 1; }
 
 }  // namespace
@@ -715,6 +889,7 @@ struct bfm_gpu_mpnn {
 	float *o, *d_o, *dh, *dx;
 	double *blocks, *lfac, *z, *az, *sc, *partials, *rms, *scratch;
 	unsigned* ticket;
+	int* tc_err;   // set by a tcgen05 layer whose completion wait ran out
 };
 
 namespace {
@@ -727,6 +902,28 @@ int persistent_grid() {
 		cudaGetDevice(&dev);
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 		g = 6 * (sms > 0 ? sms : 1);
+	}
+	return g;
+}
+
+// the forward dense layers run on tcgen05 unless BFM_GPU_MPNN_GEMM=mma asks
+// for the warp-level mma.sync kernels (read at each forward)
+bool tc_layers() {
+	char const* e = getenv("BFM_GPU_MPNN_GEMM");
+	return !(e && strcmp(e, "mma") == 0);
+}
+
+// blocks of the tcgen05 layers: four per SM (48 KB of shared memory and 64
+// TMEM columns each); the shared-memory attribute is set once
+int tc_grid() {
+	static int g = 0;
+	if (!g) {
+		int dev = 0, sms = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		cudaFuncSetAttribute(k_dense_fwd_tc<FIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tc_smem_bytes(FIN));
+		cudaFuncSetAttribute(k_dense_fwd_tc<HK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tc_smem_bytes(HK));
+		g = 4 * (sms > 0 ? sms : 1);
 	}
 	return g;
 }
@@ -809,13 +1006,27 @@ int forward(bfm_gpu_mpnn* net, bfm_gpu_problem_t* P, cudaStream_t st) {
 	fa.f = net->f;
 	k_feat1<<<FEAT_GRID, TPB_K, 0, st>>>(fa);
 	k_feat2<<<nb(N), 256, 0, st>>>(fa);
-	int const tiles = (N + TILE - 1) / TILE > 0 ? (N + TILE - 1) / TILE : 1;
-	int const pgrid = tiles < persistent_grid() ? tiles : persistent_grid();
-	k_dense_fwd<FIN><<<pgrid, MT, 0, st>>>(N, net->f, nullptr, net->d.wb + O_W0, net->d.theta + O_B0, net->h[0]);
-	for (int l = 1; l <= 3; l++) {
-		k_agg<<<nb((long) N * (HID / 8)), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->h[l - 1], net->m[l - 1]);
-		k_dense_fwd<HK><<<pgrid, MT, 0, st>>>(N, net->h[l - 1], net->m[l - 1], net->d.wb + o_w(l), net->d.theta + o_b(l),
-		                                      net->h[l]);
+	if (tc_layers()) {
+		// the dense layers on the tcgen05 tensor cores (128-node tiles)
+		int const tiles = (N + TC_M - 1) / TC_M > 0 ? (N + TC_M - 1) / TC_M : 1;
+		int const g = tiles < tc_grid() ? tiles : tc_grid();
+		k_dense_fwd_tc<FIN><<<g, TC_T, tc_smem_bytes(FIN), st>>>(N, net->f, nullptr, net->d.wb + O_W0,
+		                                                           net->d.theta + O_B0, net->h[0], net->tc_err);
+		for (int l = 1; l <= 3; l++) {
+			k_agg<<<nb((long) N * (HID / 8)), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->h[l - 1], net->m[l - 1]);
+			k_dense_fwd_tc<HK><<<g, TC_T, tc_smem_bytes(HK), st>>>(N, net->h[l - 1], net->m[l - 1], net->d.wb + o_w(l),
+			                                                          net->d.theta + o_b(l), net->h[l], net->tc_err);
+		}
+	}
+	else {
+		int const tiles = (N + TILE - 1) / TILE > 0 ? (N + TILE - 1) / TILE : 1;
+		int const pgrid = tiles < persistent_grid() ? tiles : persistent_grid();
+		k_dense_fwd<FIN><<<pgrid, MT, 0, st>>>(N, net->f, nullptr, net->d.wb + O_W0, net->d.theta + O_B0, net->h[0]);
+		for (int l = 1; l <= 3; l++) {
+			k_agg<<<nb((long) N * (HID / 8)), 256, 0, st>>>(N, bf.row_ptr, bf.cols, net->h[l - 1], net->m[l - 1]);
+			k_dense_fwd<HK><<<pgrid, MT, 0, st>>>(N, net->h[l - 1], net->m[l - 1], net->d.wb + o_w(l),
+			                                      net->d.theta + o_b(l), net->h[l]);
+		}
 	}
 	k_head<<<nb(N), 256, 0, st>>>(N, net->h[3], net->d.theta, net->o, bf.row_ptr, bf.cols, bf.vals64_any, bf.vals32,
 	                               net->blocks, net->lfac);
@@ -941,7 +1152,7 @@ int bfm_gpu_mpnn_create(bfm_gpu_mpnn_t** out, unsigned seed) {
 	if (!net) return mfail("out of host memory");
 	if (alloc(&net->d.theta, NPARAM) || alloc(&net->d.grad, NPARAM) || alloc(&net->d.adam_m, NPARAM) ||
 	    alloc(&net->d.adam_v, NPARAM) || alloc(&net->d.wb, NPARAM) || alloc(&net->sc, 6) ||
-	    alloc(&net->partials, 4 * FEAT_GRID) || alloc(&net->rms, 1) || alloc(&net->ticket, 1)) {
+	    alloc(&net->partials, 4 * FEAT_GRID) || alloc(&net->rms, 1) || alloc(&net->ticket, 1) || alloc(&net->tc_err, 1)) {
 		bfm_gpu_mpnn_destroy(net);
 		return -1;
 	}
@@ -954,6 +1165,7 @@ int bfm_gpu_mpnn_create(bfm_gpu_mpnn_t** out, unsigned seed) {
 	cudaError_t e = cudaMemcpy(net->d.theta, th, NPARAM * sizeof(float), cudaMemcpyHostToDevice);
 	free(th);
 	if (e == cudaSuccess) e = cudaMemset(net->ticket, 0, sizeof(unsigned));
+	if (e == cudaSuccess) e = cudaMemset(net->tc_err, 0, sizeof(int));
 	if (e == cudaSuccess) e = cudaMemset(net->d.adam_m, 0, NPARAM * sizeof(float));
 	if (e == cudaSuccess) e = cudaMemset(net->d.adam_v, 0, NPARAM * sizeof(float));
 	if (e == cudaSuccess) {
@@ -974,7 +1186,7 @@ int bfm_gpu_mpnn_destroy(bfm_gpu_mpnn_t* net) {
 	cudaDeviceSynchronize();
 	free_acts(net);
 	void* p[] = {net->d.theta, net->d.grad, net->d.adam_m, net->d.adam_v, net->d.wb, net->d.gpart, net->sc, net->partials,
-	             net->rms, net->ticket};
+	             net->rms, net->ticket, net->tc_err};
 	for (void* q : p)
 		if (q) cudaFree(q);
 	free(net);
@@ -1046,6 +1258,9 @@ int bfm_gpu_mpnn_forward(bfm_gpu_mpnn_t* net, bfm_gpu_problem_t* P, float* featu
 	cudaStream_t const st = (cudaStream_t) bf.stream;
 	if (forward(net, P, st)) return -1;
 	MCK(cudaStreamSynchronize(st));
+	int tc_err = 0;
+	MCK(cudaMemcpy(&tc_err, net->tc_err, sizeof tc_err, cudaMemcpyDeviceToHost));
+	if (tc_err) return mfail("a tcgen05 layer's completion wait ran out");
 	long const N = bf.N;
 	if (features) {
 		bf16* tmp = (bf16*) malloc(N * FIN * sizeof(bf16) + 1);

@@ -103,6 +103,35 @@ def test_forward_matches_oracle(setup):
         net.set_weights(init)
 
 
+def test_tcgen05_and_mma_layers_agree(setup):
+    """The forward dense layers on the tcgen05 tensor cores (the default) and
+    on the warp-level mma.sync path (BFM_GPU_MPNN_GEMM=mma) give the same
+    network output up to FP32 accumulation order (1e-3 of the output scale,
+    as against the oracle), on a mesh whose node count is not a multiple of
+    the 128-node tile."""
+    import os
+    p, prob, net, _ = setup
+    assert p.n_nodes % 128 != 0
+    th = random_theta(net, 2)
+    init = net.weights()
+    net.set_weights(th)
+    old = os.environ.get("BFM_GPU_MPNN_GEMM")
+    try:
+        os.environ.pop("BFM_GPU_MPNN_GEMM", None)
+        _, c_tc, B_tc = net.forward(prob)
+        os.environ["BFM_GPU_MPNN_GEMM"] = "mma"
+        _, c_mma, B_mma = net.forward(prob)
+    finally:
+        if old is None:
+            os.environ.pop("BFM_GPU_MPNN_GEMM", None)
+        else:
+            os.environ["BFM_GPU_MPNN_GEMM"] = old
+        net.set_weights(init)
+    assert np.abs(c_mma).max() > 0.05
+    assert np.abs(c_tc - c_mma).max() <= 1e-3 * R.C_SCALE
+    assert np.linalg.norm(B_tc - B_mma) <= 5e-3 * np.linalg.norm(B_mma)
+
+
 @pytest.fixture(scope="module")
 def pair(setup):
     """(r, e, v): a solver pair and a power vector of B K (60 steps, untrained network)."""
