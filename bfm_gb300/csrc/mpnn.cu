@@ -755,7 +755,25 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 	    : "memory");
 }
 
-constexpr size_t tc_smem_bytes(int K) { return (size_t) (TC_M + HID) * K * sizeof(bf16); }
+constexpr size_t tc_smem_bytes(int K) { return (size_t) (2 * TC_M + HID) * K * sizeof(bf16); }
+
+// one 16-byte piece of a node's input row into the tile's layout by cp.async
+// (zero-filled past the last node), chunk q of row m
+template <int K>
+__device__ __forceinline__ void tc_fetch(unsigned char* xs, int N, int node0, const bf16* x0, const bf16* x1, int e) {
+	constexpr int CH = K / 8;
+	int const m = e / CH, q = e % CH, node = node0 + m;
+	const void* src = x0;
+	int bytes = 0;
+	if (node < N) {
+		bytes = 16;
+		if (K == FIN) src = reinterpret_cast<const uint4*>(x0 + (long) node * FIN) + q;
+		else src = q < HID / 8 ? reinterpret_cast<const uint4*>(x0 + (long) node * HID) + q
+		                       : reinterpret_cast<const uint4*>(x1 + (long) node * HID) + (q - HID / 8);
+	}
+	uint32_t const dst = tc_smem(xs + (q >> 1) * (TC_M * 32) + (m >> 3) * 256 + (q & 1) * 128 + (m & 7) * 16);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
 
 template <int K>
 __global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __restrict__ x0, const bf16* __restrict__ x1,
@@ -764,13 +782,18 @@ __global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __rest
 	extern __shared__ __align__(1024) unsigned char tc_sm[];
 	constexpr int NS = K / 16;   // MMA K-slices
 	constexpr int CH = K / 8;    // 16-byte chunks per row
-	unsigned char* const xs = tc_sm;                        // x tile, slice s at s * TC_M * 32 bytes
-	unsigned char* const ws = tc_sm + (size_t) TC_M * K * 2;  // W, slice s at s * HID * 32 bytes
+	constexpr int XB = TC_M * K * 2;  // bytes of one x tile
+	unsigned char* const ws = tc_sm + 2 * XB;  // W, slice s at s * HID * 32 bytes; two x tiles before it
 	__shared__ __align__(8) unsigned long long mbar;
 	__shared__ uint32_t tmem_slot;
 	__shared__ int s_ok;
 	__shared__ float bs[HID];
 	int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	int const tiles = (N + TC_M - 1) / TC_M;
+	// the first tile in flight while W is staged
+	if ((int) blockIdx.x < tiles)
+		for (int e = tid; e < TC_M * CH; e += TC_T) tc_fetch<K>(tc_sm, N, blockIdx.x * TC_M, x0, x1, e);
+	asm volatile("cp.async.commit_group;" ::: "memory");
 	for (int e = tid; e < HID * CH; e += TC_T) {
 		int const n = e / CH, q = e % CH;
 		uint4 const v = reinterpret_cast<const uint4*>(w)[e];  // row n of W, features 8q .. 8q + 7
@@ -787,32 +810,21 @@ __global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __rest
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		s_ok = 1;
 	}
-	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-	__syncthreads();
-	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-	uint32_t const tmem = tmem_slot;
-	uint32_t const bar = tc_smem(&mbar);
 	uint32_t phase = 0;
-	int const tiles = (N + TC_M - 1) / TC_M;
-	for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+	int buf = 0;
+	uint32_t const bar = tc_smem(&mbar);
+	for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, buf ^= 1) {
 		int const node0 = tile * TC_M;
-		for (int e = tid; e < TC_M * CH; e += TC_T) {
-			int const m = e / CH, q = e % CH, node = node0 + m;
-			uint4 v = make_uint4(0u, 0u, 0u, 0u);
-			if (node < N) {
-				if (K == FIN) v = reinterpret_cast<const uint4*>(x0 + (long) node * FIN)[q];
-				else v = q < HID / 8 ? reinterpret_cast<const uint4*>(x0 + (long) node * HID)[q]
-				                     : reinterpret_cast<const uint4*>(x1 + (long) node * HID)[q - HID / 8];
-			}
-			*reinterpret_cast<uint4*>(xs + (q >> 1) * (TC_M * 32) + (m >> 3) * 256 + (q & 1) * 128 + (m & 7) * 16) = v;
-		}
-		// the generic-proxy stores above, then the tensor cores' (async-proxy) reads
+		unsigned char* const xs = tc_sm + buf * XB;
+		// this tile's copies landed; the generic-proxy writes (W, the copies)
+		// before the tensor cores' (async-proxy) reads
+		asm volatile("cp.async.wait_all;" ::: "memory");
 		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 		asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 		__syncthreads();
 		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-		bool const live = s_ok != 0;
-		if (!live) break;  // the same in every thread: a wait ran out
+		uint32_t const tmem = tmem_slot;
+		if (s_ok == 0) break;  // the same in every thread: a wait ran out
 		if (tid == 0) {
 #pragma unroll
 			for (int sl = 0; sl < NS; sl++) {
@@ -827,6 +839,12 @@ __global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __rest
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
 			             : "memory");
 		}
+		// the next tile's copies into the other buffer (its last reader, the
+		// previous tile's MMAs, has completed), in flight during this epilogue
+		int const next = tile + gridDim.x;
+		if (next < tiles)
+			for (int e = tid; e < TC_M * CH; e += TC_T) tc_fetch<K>(tc_sm + (buf ^ 1) * XB, N, next * TC_M, x0, x1, e);
+		asm volatile("cp.async.commit_group;" ::: "memory");
 		bool got = false;
 		for (long it = 0; it < TC_POLLS; it++)
 			if (tc_mbar_try(bar, phase)) {
@@ -860,10 +878,10 @@ __global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __rest
 			}
 		}
 		asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-		__syncthreads();  // TMEM read and smem free before the next tile's MMAs
-		asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 	}
-	// a wait that ran out: one more bounded wait for the MMAs in flight, then free TMEM
+	// copies still in flight land before the block exits; a wait that ran out
+	// gets one more bounded wait for the MMAs in flight; then TMEM is freed
+	asm volatile("cp.async.wait_all;" ::: "memory");
 	if (!s_ok) {
 		for (long it = 0; it < TC_POLLS; it++)
 			if (tc_mbar_try(bar, phase)) break;
@@ -871,7 +889,7 @@ __global__ void __launch_bounds__(TC_T) k_dense_fwd_tc(int N, const bf16* __rest
 	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 	__syncthreads();
 	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(HID) : "memory");
+	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot), "r"(HID) : "memory");
 }
 
 inline int nb(long n, int t = 256) { return (int) ((n + t - 1) / t) > 0 ? (int) ((n + t - 1) / t) : 1; }
@@ -913,8 +931,8 @@ bool tc_layers() {
 	return !(e && strcmp(e, "mma") == 0);
 }
 
-// blocks of the tcgen05 layers: four per SM (48 KB of shared memory and 64
-// TMEM columns each); the shared-memory attribute is set once
+// blocks of the tcgen05 layers: two per SM (80 KB of shared memory and 64
+// TMEM columns each at K = 128); the shared-memory attribute is set once
 int tc_grid() {
 	static int g = 0;
 	if (!g) {
@@ -923,7 +941,7 @@ int tc_grid() {
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 		cudaFuncSetAttribute(k_dense_fwd_tc<FIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tc_smem_bytes(FIN));
 		cudaFuncSetAttribute(k_dense_fwd_tc<HK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tc_smem_bytes(HK));
-		g = 4 * (sms > 0 ? sms : 1);
+		g = 2 * (sms > 0 ? sms : 1);
 	}
 	return g;
 }
