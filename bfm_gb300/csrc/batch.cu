@@ -614,28 +614,29 @@ __global__ void __launch_bounds__(BT) k_batch_pcg(BatchArgs a) {
 constexpr int BB_MAX_T = 1024;
 constexpr int BB_MAX_NODES = 131072;  // larger parts go to the tiled persistent kernel
 
-// block-wide sum of per-thread doubles, warps in order (every thread calls;
-// every thread gets the result)
-__device__ __forceinline__ double bb_sum(double v) {
-	__shared__ double red[BB_MAX_T / 32];
-	__shared__ double total;
+// block-wide sum of per-thread doubles (every thread calls, every thread gets
+// the result), one barrier: each warp's shuffle sum goes to a slot of a
+// double-buffered array (`ph` alternates with every call, the same in every
+// thread), then every warp reduces the slots in the same fixed shuffle tree
+// (deterministic).  A buffer is rewritten two calls later, after the next
+// call's barrier, when every thread has read it.
+__device__ __forceinline__ double bb_sum(double v, int& ph) {
+	__shared__ double red[2][BB_MAX_T / 32];
 	int const lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-	__syncthreads();  // red and total are free again
-	if (lane == 0) red[w] = v;
+	for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	if (lane == 0) red[ph][w] = v;
 	__syncthreads();
-	if (threadIdx.x == 0) {
-		double t = 0.0;
-		for (int k = 0; k < nw; k++) t += red[k];
-		total = t;
-	}
-	__syncthreads();
-	return total;
+	double t = lane < nw ? red[ph][lane] : 0.0;
+	for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+	ph ^= 1;
+	return t;
 }
 
-// z = M r over the part's nodes [n0, n1), returns (r, z) (block-wide)
+// z = M r over the part's nodes [n0, n1), returns (r, z) (block-wide).  The
+// coarse stages sum in double-float on the FP32 pipe (GB300 issues FP64 at a
+// small fraction of that rate): r_c = P^T r per cell, y_c = A_c^-1 r_c.
 template <bool TWO>
-__device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* rcs, float* ys) {
+__device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, float2* rcs, float* ys, int& ph) {
 	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	int c0 = 0;
 	if (TWO) {
@@ -643,7 +644,7 @@ __device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* 
 		int const c1 = a.part_cell[k + 1], n = 3 * (c1 - c0);
 		// r_c = P^T r, a warp per cell (four nodes per lane in flight, summed in list order)
 		for (int c = c0 + warp; c < c1; c += nw) {
-			double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+			dfl s0 = {0.f, 0.f}, s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
 			int const end = a.cell_ptr[c + 1];
 			for (int k0 = a.cell_ptr[c] + lane; k0 < end; k0 += 128) {
 				int id[4];
@@ -659,21 +660,21 @@ __device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* 
 #pragma unroll
 				for (int u = 0; u < 4; u++) {
 					if (id[u] < 0) continue;
-					double const x0 = pq[u].z != 0.f ? (double) rv[u].x : 0.0, x1 = pq[u].w != 0.f ? (double) rv[u].y : 0.0;
-					s0 += x0;
-					s1 += x1;
-					s2 += (double) pq[u].x * x1 - (double) pq[u].y * x0;
+					float const x0 = pq[u].z != 0.f ? rv[u].x : 0.f, x1 = pq[u].w != 0.f ? rv[u].y : 0.f;
+					s0 = df_add(s0, {x0, 0.f});
+					s1 = df_add(s1, {x1, 0.f});
+					s2 = df_add(s2, df_add(df_mul_f(pq[u].x, {x1, 0.f}), df_neg(df_mul_f(pq[u].y, {x0, 0.f}))));
 				}
 			}
 			for (int o = 16; o; o >>= 1) {
-				s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-				s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-				s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+				s0 = df_add(s0, {__shfl_xor_sync(0xffffffffu, s0.hi, o), __shfl_xor_sync(0xffffffffu, s0.lo, o)});
+				s1 = df_add(s1, {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)});
+				s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
 			}
 			if (lane == 0) {
-				rcs[3 * (c - c0)] = s0;
-				rcs[3 * (c - c0) + 1] = s1;
-				rcs[3 * (c - c0) + 2] = s2;
+				rcs[3 * (c - c0)] = make_float2(s0.hi, s0.lo);
+				rcs[3 * (c - c0) + 1] = make_float2(s1.hi, s1.lo);
+				rcs[3 * (c - c0) + 2] = make_float2(s2.hi, s2.lo);
 			}
 		}
 		__syncthreads();
@@ -681,17 +682,20 @@ __device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* 
 		const float* __restrict__ A = a.ainv + a.ainv_off[k];
 		for (int i = warp; i < n; i += nw) {
 			const float* __restrict__ Ar = A + (long) i * n;
-			double s = 0.0;
+			dfl s = {0.f, 0.f};
 			for (int j0 = lane; j0 < n; j0 += 128) {
 				float v[4];
 #pragma unroll
 				for (int u = 0; u < 4; u++) v[u] = j0 + 32 * u < n ? __ldg(Ar + j0 + 32 * u) : 0.f;
 #pragma unroll
 				for (int u = 0; u < 4; u++)
-					if (j0 + 32 * u < n) s += (double) v[u] * rcs[j0 + 32 * u];
+					if (j0 + 32 * u < n) {
+						float2 const rj = rcs[j0 + 32 * u];
+						s = df_add(s, df_mul_f(v[u], {rj.x, rj.y}));
+					}
 			}
-			for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-			if (lane == 0) ys[i] = (float) s;
+			for (int o = 16; o; o >>= 1) s = df_add(s, {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+			if (lane == 0) ys[i] = s.hi + s.lo;
 		}
 		__syncthreads();
 	}
@@ -711,12 +715,12 @@ __device__ double bb_apply_m(const BatchArgs& a, int k, int n0, int n1, double* 
 		df_add_prod(g, rv.x, z0);
 		df_add_prod(g, rv.y, z1);
 	}
-	return bb_sum(df_value(g));
+	return bb_sum(df_value(g), ph);
 }
 
 template <int LPR, bool TWO>
 __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
-	__shared__ double rcs[BC_MAX_N];
+	__shared__ float2 rcs[BC_MAX_N];  // r_c as double-float pairs
 	__shared__ float ys[BC_MAX_N];
 	int const k = a.block_part[blockIdx.x];
 	int const n0 = a.node_off[k], n1 = a.node_off[k + 1];
@@ -732,8 +736,9 @@ __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
 		st2(a.p0, i, 0.f, 0.f);
 		bb += bv.x * bv.x + bv.y * bv.y;
 	}
-	double const bnorm2 = bb_sum(bb);  // its barriers also order the stores above
-	double gamma = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys);
+	int ph = 0;  // bb_sum's buffer, the same in every thread
+	double const bnorm2 = bb_sum(bb, ph);  // its barrier also orders the stores above
+	double gamma = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys, ph);
 	double beta = 0.0, rho_ref = bnorm2;
 	double const tol2 = a.rtol * a.rtol * bnorm2;
 	int iter = 0, status = BFM_GPU_OK, nrepl = 0;
@@ -787,7 +792,7 @@ __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
 				}
 			}
 		}
-		double const d = bb_sum(df_value(pq));
+		double const d = bb_sum(df_value(pq), ph);
 		if (!(d > 0.0) && a.timing_iters == 0) {
 			status = BFM_GPU_BREAKDOWN;
 			break;
@@ -804,9 +809,9 @@ __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
 			df_add_prod(rr, r0, r0);
 			df_add_prod(rr, r1, r1);
 		}
-		double const rho = bb_sum(df_value(rr));
+		double const rho = bb_sum(df_value(rr), ph);
 		iter++;
-		double const gnew = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys);
+		double const gnew = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys, ph);
 		beta = gamma != 0.0 ? gnew / gamma : 0.0;
 		gamma = gnew;
 		if (a.timing_iters > 0) continue;
@@ -855,10 +860,10 @@ __global__ void __launch_bounds__(BB_MAX_T) k_batch_block(BatchArgs a) {
 					e2 += e0 * e0 + e1 * e1;
 				}
 			}
-			double const r2 = bb_sum(e2);
+			double const r2 = bb_sum(e2, ph);
 			nrepl++;
 			rho_ref = r2;
-			gamma = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys);
+			gamma = bb_apply_m<TWO>(a, k, n0, n1, rcs, ys, ph);
 			if (r2 <= tol2) break;
 		}
 	}
