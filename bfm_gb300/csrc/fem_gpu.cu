@@ -282,6 +282,20 @@ __host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long 
 	x ^= x >> 33;
 	return x;
 }
+// 64-bit node ids of the reference's element array (size_t) to the int32 ids
+// the kernels use; an id at or beyond N records the lowest such position
+__global__ void k_elems_from_u64(long n, int N, const unsigned long long* __restrict__ in, int* __restrict__ out,
+                                 unsigned long long* __restrict__ bad) {
+	long const i = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	unsigned long long const v = in[i];
+	if (v >= (unsigned long long) N) {
+		atomicMin(bad, (unsigned long long) i);
+		out[i] = 0;
+	}
+	else out[i] = (int) v;
+}
+
 __global__ void k_elems_hash(long n, const int* __restrict__ elems, unsigned long long* __restrict__ out) {
 	unsigned long long h = 0;
 	for (long t = blockIdx.x * (long) blockDim.x + threadIdx.x; t < n; t += (long) gridDim.x * blockDim.x)
@@ -1531,6 +1545,8 @@ struct bfm_gpu_problem {
 	// bounding box (origin ax0, ay0, cell acw x ach, rotation scale aH),
 	// numbered along the shorter side first (axfast: x is that side)
 	bool agg_valid;      // the aggregation belongs to the current node order and coordinates
+	unsigned long long* e64;  // staging of 64-bit element ids (bfmi_set_geometry_u64), and its error word
+	unsigned long long* e64_bad;
 	int coarse_ok;       // the coarse factor is ready (else the solve runs plain SSOR)
 	int na, nc, nc_cap, agx, agy, axfast, abw;
 	double ax0, ay0, acw, ach, aH;
@@ -3064,6 +3080,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	for (int i = 0; i < MAXF; i++)
 		if (P->force_fields[i]) cudaFree(P->force_fields[i]);
 	void* lb[] = {P->ledges, P->lloads, P->lcnt, P->lptr, P->llist, P->perm, P->iperm, P->dpos, P->otmp, P->ssor_y, P->ssor_d,
+	              P->e64, P->e64_bad,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
 	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart,
 	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->sl_wm, P->ccnt, P->lbm, P->lbd,
@@ -3083,6 +3100,29 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 void* bfm_gpu_problem_stream(bfm_gpu_problem_t* P) { return (void*) P->stream; }
 
 static cudaMemcpyKind kind_of(int where) { return where == BFM_GPU_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
+
+int bfmi_set_geometry_u64(bfm_gpu_problem_t* P, const double* coords, const uint64_t* elems, long* bad_index) {
+	P->inputs_gen++;
+	g_err[0] = 0;
+	*bad_index = -1;
+	long const n = (long) P->NE * P->kind;
+	cudaStream_t const st = P->stream;
+	if (!P->e64 && dalloc(&P->e64, n > 0 ? n : 1)) return -1;
+	if (!P->e64_bad && dalloc(&P->e64_bad, 1)) return -1;
+	CK(cudaMemcpyAsync(P->coords, coords, 2l * P->N * sizeof(double), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(P->e64, elems, n * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(P->e64_bad, 0xff, sizeof(unsigned long long), st));
+	if (n > 0) k_elems_from_u64<<<blocks_for(n), TPB, 0, st>>>(n, P->N, P->e64, P->elems, P->e64_bad);
+	CK(cudaGetLastError());
+	unsigned long long bad = 0;
+	CK(cudaMemcpyAsync(&bad, P->e64_bad, sizeof bad, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	if (bad != ~0ull) *bad_index = (long) bad;
+	P->ordered &= ~(ORD_COORDS | ORD_ELEMS);
+	P->colored = false;
+	P->assembled = false;
+	return 0;
+}
 
 int bfm_gpu_problem_set_geometry(bfm_gpu_problem_t* P, const double* coords, const int32_t* elems, int where) {
 	P->inputs_gen++;

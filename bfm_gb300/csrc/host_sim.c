@@ -208,12 +208,15 @@ static int gather(bfm_state_t* st, bfm_sim_t* sim, bfm_instance_t* inst, gathere
 	if (kind != BFM_ELEM_KIND_SIMPLEX && kind != BFM_ELEM_KIND_QUAD)
 		return REPORT(st, "only linear triangles and bilinear quads are supported (kind = %zu)", kind);
 	if (N > INT_MAX / 2 || E * kind > INT_MAX) return REPORT(st, "mesh too large for 32-bit indices");
-	/* connectivity */
-	g->elems = malloc(E * kind * sizeof *g->elems + 1);
-	if (!g->elems) return REPORT(st, "out of host memory");
-	for (size_t i = 0; i < E * kind; i++) {
-		if (mesh->elems[i] >= N) return REPORT(st, "element %zu refers to node %zu of %zu", i / kind, mesh->elems[i], N);
-		g->elems[i] = (int32_t) mesh->elems[i];
+	/* connectivity: 64-bit ids go to the device as they are (narrowed and
+	 * checked there); other widths are converted here */
+	if (sizeof(size_t) != sizeof(uint64_t)) {
+		g->elems = malloc(E * kind * sizeof *g->elems + 1);
+		if (!g->elems) return REPORT(st, "out of host memory");
+		for (size_t i = 0; i < E * kind; i++) {
+			if (mesh->elems[i] >= N) return REPORT(st, "element %zu refers to node %zu of %zu", i / kind, mesh->elems[i], N);
+			g->elems[i] = (int32_t) mesh->elems[i];
+		}
 	}
 	/* shape functions sampled at the integration points through the rule's own pointers */
 	if (rule->n_points > 16) return REPORT(st, "integration rules of at most 16 points are supported");
@@ -271,7 +274,9 @@ static int gather(bfm_state_t* st, bfm_sim_t* sim, bfm_instance_t* inst, gathere
 		need_edges |= k != BFM_CONDITION_KIND_DIRICHLET_X && k != BFM_CONDITION_KIND_DIRICHLET_Y;
 		g->kinds[c] = k;
 		g->values[c] = C->value;
-		for (size_t i = 0; i < N; i++) g->masks[(size_t) c * N + i] = C->nodes[i] ? 1 : 0;
+		/* a C bool is one byte holding 0 or 1: the mask's own layout */
+		_Static_assert(sizeof(bool) == 1, "one-byte bool");
+		memcpy(g->masks + (size_t) c * N, C->nodes, N);
 	}
 	if (need_edges && mesh->n_edges) {
 		if (mesh->n_edges > INT_MAX / 2) return REPORT(st, "too many edges");
@@ -315,7 +320,18 @@ static bfm_gpu_problem_t* upload_and_assemble(bfm_state_t* st, bfm_sim_t* sim, b
 	int ok = P != NULL;
 	const double* fields[8];
 	for (int f = 0; f < 8; f++) fields[f] = g.fields[f];
-	ok = ok && bfm_gpu_problem_set_geometry(P, mesh->coords, g.elems, BFM_GPU_HOST) == 0;
+	if (ok && g.elems) ok = bfm_gpu_problem_set_geometry(P, mesh->coords, g.elems, BFM_GPU_HOST) == 0;
+	else if (ok) {
+		long bad = -1;
+		ok = bfmi_set_geometry_u64(P, mesh->coords, (const uint64_t*) mesh->elems, &bad) == 0;
+		if (ok && bad >= 0) {
+			REPORT(st, "element %zu refers to node %zu of %zu", (size_t) bad / (size_t) mesh->kind, mesh->elems[bad],
+			       mesh->n_nodes);
+			if (dedicated) bfm_gpu_problem_destroy(P);
+			release(&g);
+			return NULL;
+		}
+	}
 	ok = ok && bfm_gpu_problem_set_material(P, mat->E, mat->nu, mat->rho, stress, em.E, em.nu, BFM_GPU_HOST) == 0;
 	ok = ok && bfm_gpu_problem_set_rule(P, g.nq, g.weights, g.phi, g.dxi, g.deta) == 0;
 	ok = ok && bfm_gpu_problem_set_forces(P, g.nf, g.fval, fields, BFM_GPU_HOST) == 0;

@@ -93,6 +93,14 @@ __attribute__((visibility("hidden"))) void** bfmi_ext_slot(struct bfm_gpu_proble
  * marks the problem unassembled.  Used by the batched solver. */
 __attribute__((visibility("hidden"))) int bfmi_set_precond(struct bfm_gpu_problem* P, int precond);
 
+/* bfm_gpu_problem_set_geometry from host arrays with 64-bit node ids (the
+ * reference's size_t element array), narrowed to int32 on the device: no host
+ * pass over the elements.  *bad_index = the lowest position holding an id at
+ * or beyond n_nodes (the elements are then not usable), else -1.  Waits for
+ * the copies. */
+__attribute__((visibility("hidden"))) int bfmi_set_geometry_u64(struct bfm_gpu_problem* P, const double* coords,
+                                                                const uint64_t* elems, long* bad_index);
+
 #ifdef __cplusplus
 }
 #endif

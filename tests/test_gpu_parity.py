@@ -190,6 +190,24 @@ def test_valence_cap_reports_error_and_recovers(libbfm):
     assert rel(h2.effects(), d["effects"]) < PARITY_RTOL
 
 
+def test_bad_element_index_reports_error_and_recovers(libbfm):
+    """An element referring to a node beyond the mesh is reported (the 64-bit
+    ids are narrowed and checked on the device), and the same handle runs
+    again once the element array is repaired."""
+    p = M.plate(8, 4, 3)
+    h = api.SimHandle.from_problem(libbfm, p)
+    assert h.run() == 0
+    good = h.effects().copy()
+    elems = h.keep[1]  # the mesh's size_t element array (uint64, flat)
+    old = int(elems[7])
+    elems[7] = p.n_nodes + 5
+    assert h.run() == -1
+    assert "refers to node" in h.error() and f"element {7 // 3}" in h.error()
+    elems[7] = old
+    assert h.run() == 0
+    assert np.array_equal(h.effects(), good)
+
+
 def test_no_constraints_is_reported(libbfm):
     p = M.plate(8, 4, 3)
     p.conds = []
