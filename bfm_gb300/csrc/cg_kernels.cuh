@@ -2181,28 +2181,33 @@ __device__ __forceinline__ void acc_ptmd(double acc[9], const double pr[2][3], d
 // fixed order into the chunk's 81 values; then per aggregate and entry the
 // chunks in chunk order.  A neighbour outside those 9 cells sets *err (the
 // caller then drops the coarse correction).
+// The sums run in double-float on the FP32 pipe (GB300 issues FP64 at a small
+// fraction of that rate): the FP32 operator's products are exact (TwoProduct
+// by FMA), FP64 operator values enter as pairs.
 __global__ void k_coarse_ac(CoarseArgs a) {
 	int const q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if (q >= a.nchunk) return;
 	int cx, cy;
 	cell_xy(a.chunk_agg[q], a.gx, a.gy, a.xfast, cx, cy);
-	double acc[9][9];
+	dfl acc[9][9];
 	for (int s = 0; s < 9; s++)
-		for (int t = 0; t < 9; t++) acc[s][t] = 0.0;
+		for (int t = 0; t < 9; t++) acc[s][t] = {0.f, 0.f};
 	for (int k = a.chunk_start[q] + lane; k < a.chunk_start[q + 1]; k += 32) {
 		int const i = a.agg_nodes[k];
 		float4 const pi = a.pnode[i];
-		double const fi0 = pi.z, fi1 = pi.w, dxi = pi.x, dyi = pi.y;
+		float const fi0 = pi.z, fi1 = pi.w;
+		float const p20 = -fi0 * pi.y, p21 = fi1 * pi.x;  // the rotation row of P_i^T (exact: f is 0 or 1)
 		// the FP32 operator in difference form, (A g)_i = S_i g_i + sum_j A_ij (g_j - g_i):
 		// its diagonal block is S_i - sum_{j != i} A_ij
-		double deff[4] = {0.0, 0.0, 0.0, 0.0};
+		dfl deff[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 		if (!a.vals64) {
 			float4 const sr = reinterpret_cast<const float4*>(a.corr32)[i];
-			deff[0] = sr.x; deff[1] = sr.y; deff[2] = sr.z; deff[3] = sr.w;
+			deff[0] = {sr.x, 0.f}; deff[1] = {sr.y, 0.f}; deff[2] = {sr.z, 0.f}; deff[3] = {sr.w, 0.f};
 			for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
 				if (a.cols[e] == i) continue;
 				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
-				deff[0] -= v.x; deff[1] -= v.y; deff[2] -= v.z; deff[3] -= v.w;
+				deff[0] = df_add(deff[0], {-v.x, 0.f}); deff[1] = df_add(deff[1], {-v.y, 0.f});
+				deff[2] = df_add(deff[2], {-v.z, 0.f}); deff[3] = df_add(deff[3], {-v.w, 0.f});
 			}
 		}
 		for (int e = a.row_ptr[i]; e < a.row_ptr[i + 1]; e++) {
@@ -2216,34 +2221,35 @@ __global__ void k_coarse_ac(CoarseArgs a) {
 			}
 			int const slot = (oy + 1) * 3 + (ox + 1);
 			float4 const pj = a.pnode[j];
-			double const gj0 = pj.z, gj1 = pj.w, dxj = pj.x, dyj = pj.y;
-			double m[4];
+			float const gj0 = pj.z, gj1 = pj.w, r0 = -gj0 * pj.y, r1 = gj1 * pj.x;  // exact: g is 0 or 1
+			dfl m[4];
 			if (a.vals64) {
-				for (int t = 0; t < 4; t++) m[t] = a.vals64[4l * e + t];
+				for (int t = 0; t < 4; t++) m[t] = df_make(a.vals64[4l * e + t]);
 			}
 			else if (j == i) {
 				for (int t = 0; t < 4; t++) m[t] = deff[t];
 			}
 			else {
 				float4 const v = reinterpret_cast<const float4*>(a.vals32)[e];
-				m[0] = v.x; m[1] = v.y; m[2] = v.z; m[3] = v.w;
+				m[0] = {v.x, 0.f}; m[1] = {v.y, 0.f}; m[2] = {v.z, 0.f}; m[3] = {v.w, 0.f};
 			}
 			// A P_j (2x3), then P_i^T (3x2) times it
-			double const ap[2][3] = {{m[0] * gj0, m[1] * gj1, -m[0] * gj0 * dyj + m[1] * gj1 * dxj},
-			                         {m[2] * gj0, m[3] * gj1, -m[2] * gj0 * dyj + m[3] * gj1 * dxj}};
-			double const pt[3][2] = {{fi0, 0.0}, {0.0, fi1}, {-fi0 * dyi, fi1 * dxi}};
+			dfl const ap[2][3] = {{df_mul_f(gj0, m[0]), df_mul_f(gj1, m[1]), df_add(df_mul_f(r0, m[0]), df_mul_f(r1, m[1]))},
+			                      {df_mul_f(gj0, m[2]), df_mul_f(gj1, m[3]), df_add(df_mul_f(r0, m[2]), df_mul_f(r1, m[3]))}};
 #pragma unroll
-			for (int u = 0; u < 3; u++)
-#pragma unroll
-				for (int v = 0; v < 3; v++) acc[slot][3 * u + v] += pt[u][0] * ap[0][v] + pt[u][1] * ap[1][v];
+			for (int v = 0; v < 3; v++) {
+				acc[slot][v] = df_add(acc[slot][v], df_mul_f(fi0, ap[0][v]));
+				acc[slot][3 + v] = df_add(acc[slot][3 + v], df_mul_f(fi1, ap[1][v]));
+				acc[slot][6 + v] = df_add(acc[slot][6 + v], df_add(df_mul_f(p20, ap[0][v]), df_mul_f(p21, ap[1][v])));
+			}
 		}
 	}
 	for (int s = 0; s < 9; s++)
 		for (int t = 0; t < 9; t++) {
-			double x = acc[s][t];
+			dfl x = acc[s][t];
 #pragma unroll
-			for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-			if (lane == 0) a.part[81l * q + 9 * s + t] = x;
+			for (int o = 16; o; o >>= 1) x = df_add(x, {__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)});
+			if (lane == 0) a.part[81l * q + 9 * s + t] = df_dbl(x);
 		}
 }
 
