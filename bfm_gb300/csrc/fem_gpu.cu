@@ -919,12 +919,40 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a) {
 // once per element rather than once per owner row (three or four times):
 // computed in FP64 and rounded once, so they are the FP64 constants to FP32
 // precision
+// 1/x in FP64 from an FP32 estimate and two Newton steps (FMA form), for x
+// in FP32 range: a few FP64 operations where a correctly rounded division
+// takes many more on this GPU's FP64 pipe; within an ulp or two of 1/x
+__device__ __forceinline__ double recip_nr(double x) {
+	double r = (double) __frcp_rn((float) x);
+	r = __fma_rn(r, __fma_rn(-x, r, 1.0), r);
+	return __fma_rn(r, __fma_rn(-x, r, 1.0), r);
+}
+
+// material_abc's formulas with reciprocals in place of its correctly rounded
+// divisions: the FP64 result is within a few ulps, so its rounding to FP32
+// is the same but for values within a few FP64 ulps of an FP32 tie
+__device__ __forceinline__ void material_abc_fast(double E, double nu, int stress, double& a, double& b, double& c) {
+	double const r1 = recip_nr(1.0 + nu);
+	if (stress != 1) {
+		double const den = 1.0 - 2.0 * nu;
+		double const ef = E * (1.0 - nu) * r1;
+		a = stress == 3 ? ef * den : ef * recip_nr(den);
+		b = E * nu * r1 * recip_nr(den);
+	}
+	else {
+		double const rd = recip_nr(1.0 - nu * nu);
+		a = E * rd;
+		b = E * nu * rd;
+	}
+	c = E * 0.5 * r1;
+}
+
 __global__ void k_elem_mat32(int NE, const double* __restrict__ elemE, const double* __restrict__ elemNu, double E,
                              double nu, int stress, float4* __restrict__ mat) {
 	int const e = blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= NE) return;
 	double da, db, dc;
-	material_abc(elemE ? elemE[e] : E, elemNu ? elemNu[e] : nu, stress, da, db, dc);
+	material_abc_fast(elemE ? elemE[e] : E, elemNu ? elemNu[e] : nu, stress, da, db, dc);
 	mat[e] = make_float4((float) da, (float) db, (float) dc, 0.f);
 }
 
@@ -2208,8 +2236,13 @@ int coarse_setup(bfm_gpu_problem* P) {
 	                                          P->agy, P->axfast, P->aH, P->pnode);
 	CK(cudaMemsetAsync(P->aband, 0, (size_t) P->nc * (P->abw + 1) * sizeof(float2), st));
 	CK(cudaMemsetAsync(P->diag0, 0, (size_t) P->nc * sizeof(double), st));
-	CK(cudaMemsetAsync(P->coarse_err, 0, sizeof(int), st));
+	CK(cudaMemsetAsync(P->coarse_err, 0, 2 * sizeof(int), st));
 	CoarseArgs ca = coarse_args(P, nullptr, VT_DF);
+	// The set-up's grid barriers wait with the default limit (the solver
+	// options' limit belongs to the solves) and report a timeout in
+	// coarse_err[1], which no solve resets
+	ca.polls = BARRIER_POLLS_DEFAULT;
+	ca.berr = P->coarse_err + 1;
 	k_coarse_ac<<<blocks_for(32l * P->nchunk), TPB, 0, st>>>(ca);
 	k_coarse_ac_sum<<<blocks_for(81l * P->na), TPB, 0, st>>>(ca);
 	int err = 0;
@@ -2266,6 +2299,11 @@ int coarse_setup(bfm_gpu_problem* P) {
 			}
 	}
 	CK(cudaGetLastError());
+	if (P->linv_grid > 0) {
+		CK(cudaMemcpyAsync(&err, P->coarse_err + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+		CK(cudaStreamSynchronize(st));
+		if (err) return fail("a grid barrier of the coarse inverse timed out");
+	}
 	P->coarse_ok = 1;
 	return 0;
 }
