@@ -1409,8 +1409,20 @@ struct CoarseArgs {
 	const int* chunk_agg;
 	const int* agg_chunk;
 	double* part;        // per chunk: 3 (restriction) or 81 (coarse matrix) partial sums
-	unsigned* ccnt;      // per aggregate: restriction chunks done in this application (TMA sweep kernel; reset by its last chunk)
+	// the triangular products' work list of the TMA sweep kernel (built for
+	// a grid of tri_g blocks; tri_g 0: none): block b's segments
+	// tri_seg[tri_sp[b] .. tri_sp[b + 1]) as (row, first entry, entries,
+	// slot), its rows tri_row[tri_rp[b] .. tri_rp[b + 1]) as (row, first
+	// slot, slots, 0)
+	int tri_g;
+	const int* tri_sp;
+	const int* tri_rp;
+	const int4* tri_seg;
+	const int4* tri_row;
 };
+
+constexpr int TRI_SEG = 512;    // entries of a triangle row per segment (4 groups per lane)
+constexpr int TRI_SLOTS = 128;  // segment sums a block holds in shared memory
 
 struct SsorArgs {
 	const int* row_ptr;

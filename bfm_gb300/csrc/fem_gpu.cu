@@ -35,7 +35,9 @@
 
 #include <pthread.h>
 #include <stdarg.h>
+#include <algorithm>
 #include <type_traits>
+#include <vector>
 
 namespace {
 
@@ -1556,8 +1558,6 @@ struct bfm_gpu_problem {
 	int sl_base[65];     // first slice of each colour
 	int *sl_lw, *sl_uw, *sl_lp, *sl_up;  // widths and slice offsets (n + 1 each)
 	int* sl_wm;          // device copy of sl_wmax
-	unsigned* ccnt;      // per aggregate: restriction chunks done (CoarseArgs::ccnt), na_cap entries
-	int ccnt_cap;
 	long sl_lcap, sl_ucap;
 	float4 *sl_lv, *sl_uv;
 	int *sl_lc, *sl_uc;
@@ -1590,6 +1590,12 @@ struct bfm_gpu_problem {
 	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
 	int* coarse_err;
 	int coarse_grid;        // cooperative grid of k_coarse_apply (0: not sized yet, -1: none)
+	// the TMA sweep kernel's work list for the triangular products
+	// (CoarseArgs::tri_*), packed: built for tri_n coarse DOFs and tri_g blocks
+	int* tri;
+	long tri_cap;
+	int tri_g, tri_n;
+	long tri_seg_off, tri_row_off;
 
 };
 
@@ -2019,8 +2025,71 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, int vt) {
 	c.chunk_agg = P->chunk_agg;
 	c.agg_chunk = P->agg_chunk;
 	c.part = P->cpart;
-	c.ccnt = P->ccnt;
+	c.tri_g = P->tri_g;
+	if (P->tri_g > 0) {
+		c.tri_sp = P->tri;
+		c.tri_rp = P->tri + P->tri_g + 1;
+		c.tri_seg = reinterpret_cast<const int4*>(P->tri + P->tri_seg_off);
+		c.tri_row = reinterpret_cast<const int4*>(P->tri + P->tri_row_off);
+	}
 	return c;
+}
+
+// Work list of the TMA sweep kernel's triangular products (y_t = X r_c, y_c =
+// X^T y_t) for a grid of G blocks.  Rows go to blocks in zig-zag order (block
+// b: rows 2 G m + b and 2 G m + 2 G - 1 - b, m = 0, 1, .., so every block's
+// rows add up to about the same length), each row cut into segments of at
+// most TRI_SEG entries, a block's segments sorted longest first (the kernel
+// deals them to its warps in turn).  Packed into one device buffer; left
+// unbuilt (tri_g = 0: the kernel's per-warp rows instead) when a block would
+// need more than TRI_SLOTS segment sums.
+int build_tri_lists(bfm_gpu_problem* P, int G) {
+	int const n = P->nc;
+	if (G <= 0 || (P->tri_g == G && P->tri_n == n)) return 0;
+	P->tri_g = 0;
+	std::vector<int> sp(G + 1), rp(G + 1);
+	std::vector<int4> segs, rows;
+	for (int b = 0; b < G; b++) {
+		sp[b] = (int) segs.size();
+		rp[b] = (int) rows.size();
+		size_t const first = segs.size();
+		int slot = 0;
+		for (long m = 0;; m++) {
+			long const pair[2] = {2l * G * m + b, 2l * G * m + 2l * G - 1 - b};
+			if (pair[0] >= n) break;
+			for (long i : pair) {
+				if (i >= n) continue;
+				int const len = (int) i + 1, cnt = (len + TRI_SEG - 1) / TRI_SEG;
+				rows.push_back(make_int4((int) i, slot, cnt, 0));
+				for (int q = 0; q < cnt; q++)
+					segs.push_back(make_int4((int) i, q * TRI_SEG, std::min(TRI_SEG, len - q * TRI_SEG), slot++));
+			}
+		}
+		if (slot > TRI_SLOTS) return 0;
+		std::stable_sort(segs.begin() + first, segs.end(), [](const int4& x, const int4& y) { return x.z > y.z; });
+	}
+	sp[G] = (int) segs.size();
+	rp[G] = (int) rows.size();
+	long const hdr = (2l * G + 2 + 3) / 4 * 4;
+	long const total = hdr + 4l * (long) (segs.size() + rows.size());
+	if (total > P->tri_cap) {
+		if (P->tri) cudaFree(P->tri);
+		P->tri = nullptr;
+		P->tri_cap = 0;
+		if (dalloc(&P->tri, total)) return -1;
+		P->tri_cap = total;
+	}
+	std::vector<int> h((size_t) total, 0);
+	std::copy(sp.begin(), sp.end(), h.begin());
+	std::copy(rp.begin(), rp.end(), h.begin() + G + 1);
+	memcpy(h.data() + hdr, segs.data(), segs.size() * sizeof(int4));
+	memcpy(h.data() + hdr + 4 * segs.size(), rows.data(), rows.size() * sizeof(int4));
+	CK(cudaMemcpy(P->tri, h.data(), (size_t) total * sizeof(int), cudaMemcpyHostToDevice));
+	P->tri_seg_off = hdr;
+	P->tri_row_off = hdr + 4l * (long) segs.size();
+	P->tri_g = G;
+	P->tri_n = n;
+	return 0;
 }
 
 
@@ -2098,13 +2167,6 @@ int build_aggregates(bfm_gpu_problem* P) {
 		if (dalloc(&P->chunk_start, nchunk + 1) || dalloc(&P->chunk_agg, nchunk + 1) || dalloc(&P->cpart, 81l * (nchunk + 1)))
 			rc = -1;
 		else P->chunk_cap = nchunk + 1;
-	}
-	if (!rc && na > P->ccnt_cap) {
-		if (P->ccnt) cudaFree(P->ccnt);
-		P->ccnt = nullptr;
-		P->ccnt_cap = 0;
-		if (dalloc(&P->ccnt, na) || cudaMemsetAsync(P->ccnt, 0, na * sizeof(unsigned), st) != cudaSuccess) rc = -1;
-		else P->ccnt_cap = na;
 	}
 	if (!rc && nc > P->nc_cap) {
 		// (re)allocate for the larger coarse space (the band at the widest bandwidth)
@@ -2299,6 +2361,7 @@ int coarse_setup(bfm_gpu_problem* P) {
 			}
 	}
 	CK(cudaGetLastError());
+	if (P->tma_grid > 0 && build_tri_lists(P, P->tma_grid)) return -1;
 	if (P->linv_grid > 0) {
 		CK(cudaMemcpyAsync(&err, P->coarse_err + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
 		CK(cudaStreamSynchronize(st));
@@ -2445,7 +2508,8 @@ bool fuse_coarse(bfm_gpu_problem* P) {
 // block, 0 when the kernel cannot be used here.
 size_t tma_tiling(bfm_gpu_problem* P, SsorArgs& a, bool fused) {
 	if (P->tma_grid <= 0 || P->ncol <= 0 || P->ncol > 63) return 0;
-	size_t const vec = fused ? (((size_t) P->nc + 4) * sizeof(float2) + 127) / 128 * 128 : 0;
+	// the staged coarse vector: nc + 4 entries, in 4 planes of (nc + 7) / 4
+	size_t const vec = fused ? (((size_t) P->nc + 8) * sizeof(float2) + 127) / 128 * 128 : 0;
 	if ((size_t) P->tma_smem_max < vec + ST_NS * 4096) return 0;
 	int const stage = (int) ((((size_t) P->tma_smem_max - vec) / ST_NS) / 128 * 128);
 	int const nc = P->ncol;
@@ -2921,7 +2985,6 @@ int time_ssor(bfm_gpu_problem* P, int reps, double* ms, double* ms_sweeps) {
 			if (smem > 0) {
 				void* pa[1] = {&a};
 				cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), st);
-				if (P->ccnt) cudaMemsetAsync(P->ccnt, 0, P->ccnt_cap * sizeof(unsigned), st);
 				cudaLaunchCooperativeKernel(ssor_tma_kernel(vt), dim3(P->tma_grid), dim3(ST_THREADS), pa, smem, st);
 				return;
 			}
@@ -3121,7 +3184,7 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	              P->e64, P->e64_bad,
 	              P->ssor_bar, P->agg, P->agg_ptr, P->agg_nodes, P->pnode, P->aband, P->diag0, P->rc, P->yc,
 	              P->ayt, P->xl, P->xu, P->coarse_err, P->chunk_start, P->chunk_agg, P->agg_chunk, P->cpart,
-	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->sl_wm, P->ccnt, P->lbm, P->lbd,
+	              P->sl_lw, P->sl_uw, P->sl_lp, P->sl_up, P->sl_lv, P->sl_uv, P->sl_lc, P->sl_uc, P->sl_wm, P->tri, P->lbm, P->lbd,
 	              P->lbw};
 	for (void* q : lb)
 		if (q) cudaFree(q);
@@ -3705,7 +3768,6 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 	if (learned && bfmi_learned_precond(P, 0)) return -1;
 	if (ssor_pc(P->precond) && P->ssor_bar) {
 		CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
-		if (P->ccnt) CK(cudaMemsetAsync(P->ccnt, 0, P->ccnt_cap * sizeof(unsigned), P->stream));
 		if (pack_relaxation_blocks(P)) return -1;
 	}
 	CK(cudaGraphLaunch(P->graph, P->stream));
@@ -3721,7 +3783,6 @@ int bfm_gpu_problem_solve(bfm_gpu_problem_t* P, const bfm_gpu_opts_t* opts) {
 			if (bfmi_set_precond_blocks(P, nullptr)) return -1;
 			if (ssor_pc(P->precond) && P->ssor_bar) {
 				CK(cudaMemsetAsync(P->ssor_bar, 0, BAR_WORDS * sizeof(unsigned), P->stream));
-				if (P->ccnt) CK(cudaMemsetAsync(P->ccnt, 0, P->ccnt_cap * sizeof(unsigned), P->stream));
 				if (pack_relaxation_blocks(P)) return -1;
 			}
 			CK(cudaGraphLaunch(P->graph, P->stream));

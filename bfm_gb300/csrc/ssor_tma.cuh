@@ -27,13 +27,19 @@
 // so consecutive tiles fill all warps.  Lane = row within the slice.
 //
 // Two-level correction (at least 3 colours): its stages run between the
-// sweeps' own grid barriers -- restriction of the block's chunks at the end
-// of phase 0, where the last chunk of each aggregate to finish sums the
-// aggregate's chunk partials in chunk order into r_c; at the start of phase 1
-// every block stages r_c in shared memory and forms its rows of y_t = X r_c; at the start of phase 2 it stages y_t
-// and forms its rows of y_c = X^T y_t.  The backward phases (from phase nc
-// on) add P y_c where they store z; the rows of colour nc - 1, stored in
-// phase nc - 1, get it at the start of phase nc when that is phase 3.
+// sweeps' own grid barriers -- at the start of phase 0, while the producer
+// fills the ring, each block restricts whole aggregates (its share of them:
+// the chunks' partial sums, then each aggregate's sum in chunk order into
+// r_c); at the start of phase 1 every block stages r_c in shared memory and
+// forms its rows of y_t = X r_c; at the start of phase 2 it stages y_t and
+// forms its rows of y_c = X^T y_t.  The triangular products follow a work
+// list built on the host for the grid (st_tri_list: whole rows per block in
+// zig-zag order, cut into segments dealt to the warps): they are bound by
+// instruction issue, so every warp gets about the same number of entries and
+// no index arithmetic beyond a table lookup.  The backward phases (from
+// phase nc on) add P y_c where they store z; the rows of colour nc - 1,
+// stored in phase nc - 1, get it at the start of phase nc when that is
+// phase 3.
 //
 // Every wait is bounded: grid barriers by the polls argument (a timeout
 // sets the solve's error flag), the mbarrier waits by MBAR_POLLS.  A block
@@ -132,9 +138,18 @@ __device__ bool st_grid_barrier(unsigned* bar, int* err, long polls, volatile in
 }
 
 // the block's share [lo, hi) of n items
+// (32-bit division when n G fits: a few instructions instead of a 64-bit
+// division routine in every consumer warp)
 __device__ __forceinline__ void st_share(int n, int& lo, int& hi) {
-	lo = (int) ((long) n * blockIdx.x / gridDim.x);
-	hi = (int) ((long) n * (blockIdx.x + 1) / gridDim.x);
+	unsigned const G = gridDim.x, b = blockIdx.x;
+	if ((unsigned long long) n * G < (1ull << 32)) {
+		lo = (int) ((unsigned) n * b / G);
+		hi = (int) ((unsigned) n * (b + 1) / G);
+	}
+	else {
+		lo = (int) ((long) n * b / G);
+		hi = (int) ((long) n * (b + 1) / G);
+	}
 }
 
 // the block's rows of a padded triangle (row i has i + 1 entries, xrow(i)
@@ -222,38 +237,110 @@ __device__ __forceinline__ void st_restrict_chunk(const CoarseArgs& co, const vo
 		s1 = df_add(s1, {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)});
 		s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
 	}
-	// the last chunk of the aggregate to finish sums the aggregate's chunks in
-	// chunk order into r_c (the count is reset for the next application)
-	__shared__ int last[ST_THREADS / 32];
-	int const wl = threadIdx.x >> 5;
 	if (lane == 0) {
 		co.part[3l * q] = df_dbl(s0);
 		co.part[3l * q + 1] = df_dbl(s1);
 		co.part[3l * q + 2] = df_dbl(s2);
-		__threadfence();
-		int const I = co.chunk_agg[q];
-		unsigned const nq = (unsigned) (co.agg_chunk[I + 1] - co.agg_chunk[I]);
-		last[wl] = atomicAdd(co.ccnt + I, 1u) == nq - 1 ? I : -1;
 	}
-	__syncwarp();
-	int const I = last[wl];
-	if (I < 0) return;
-	__threadfence();
+}
+
+// r_c of aggregate I: the partial sums of its chunks in chunk order, lanes
+// 0-2 one component each, 8 loads in flight
+__device__ __forceinline__ void st_restrict_sum(const CoarseArgs& co, int I, int lane) {
+	if (lane >= 3) return;
 	int const q0 = co.agg_chunk[I], q1 = co.agg_chunk[I + 1];
-	if (lane < 3) {
-		double s = 0.0;
-		for (int qb = q0; qb < q1; qb += 8) {  // 8 loads in flight, summed in chunk order
-			double pv[8];
+	double s = 0.0;
+	for (int qb = q0; qb < q1; qb += 8) {
+		double pv[8];
 #pragma unroll
-			for (int k = 0; k < 8; k++) pv[k] = qb + k < q1 ? __ldcg(co.part + 3l * (qb + k) + lane) : 0.0;
+		for (int k = 0; k < 8; k++) pv[k] = qb + k < q1 ? __ldcg(co.part + 3l * (qb + k) + lane) : 0.0;
 #pragma unroll
-			for (int k = 0; k < 8; k++)
-				if (qb + k < q1) s += pv[k];
-		}
-		dfl const d = df_make(s);
-		co.rc[3 * I + lane] = make_float2(d.hi, d.lo);
+		for (int k = 0; k < 8; k++)
+			if (qb + k < q1) s += pv[k];
 	}
-	if (lane == 0) co.ccnt[I] = 0u;
+	dfl const d = df_make(s);
+	co.rc[3 * I + lane] = make_float2(d.hi, d.lo);
+}
+
+// one warp: the dot product of a segment of a padded FP32 triangle row
+// (len <= TRI_SEG entries, groups of 4; lane takes groups lane, lane + 32,
+// lane + 64, lane + 96, all loads first) with the entries c, c + 1, .. of a
+// double-float vector staged in shared memory in 4 planes of S (entry e at
+// vs[(e & 3) S + (e >> 2)]), so that the lanes of a warp read consecutive
+// words of one plane: no bank conflicts, whatever c.  Each lane sums in the manner of Ogita, Rump and Oishi's
+// Dot2: the products x v_hi split exactly by an FMA, the running sum by
+// TwoSum, the rounding errors and x v_lo gathered in a second float -- 11
+// FP32 operations per entry where a double-float multiply-add takes 17,
+// the same accuracy class (as if summed in twice the working precision);
+// then the lanes' double-float sums in a fixed shuffle tree
+__device__ __forceinline__ dfl st_seg_dot(const float* __restrict__ row, int len, const float2* vs, int S, int c,
+                                          int lane) {
+	int const ng = (len + 3) >> 2;
+	const float2* v0 = vs + (c & 3) * S + (c >> 2);
+	const float2* v1 = vs + ((c + 1) & 3) * S + ((c + 1) >> 2);
+	const float2* v2 = vs + ((c + 2) & 3) * S + ((c + 2) >> 2);
+	const float2* v3 = vs + ((c + 3) & 3) * S + ((c + 3) >> 2);
+	const float4* r4 = reinterpret_cast<const float4*>(row);
+	float4 x[4];
+#pragma unroll
+	for (int u = 0; u < 4; u++) {
+		int const g = lane + 32 * u;
+		x[u] = g < ng ? __ldcs(r4 + g) : make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+	float p = 0.f, er = 0.f;
+	auto acc = [&](float xv, float2 vv) {
+		float const h = __fmul_rn(xv, vv.x);
+		float r = __fmaf_rn(xv, vv.x, -h);
+		r = __fmaf_rn(xv, vv.y, r);
+		float const s = __fadd_rn(p, h);
+		float const bb = __fsub_rn(s, p);
+		float const q = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(h, bb));
+		p = s;
+		er = __fadd_rn(er, __fadd_rn(q, r));
+	};
+#pragma unroll
+	for (int u = 0; u < 4; u++) {
+		int const g = lane + 32 * u;
+		if (g >= ng) continue;
+		acc(x[u].x, v0[g]);
+		acc(x[u].y, v1[g]);
+		acc(x[u].z, v2[g]);
+		acc(x[u].w, v3[g]);
+	}
+	float const h = __fadd_rn(p, er);
+	dfl s = {h, __fsub_rn(er, __fsub_rn(h, p))};
+#pragma unroll
+	for (int o = 16; o; o >>= 1) s = df_add(s, {__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)});
+	return s;
+}
+
+// y_t = X r_c (tr false: row i of X gives y_t[i]) or y_c = X^T y_t (tr true:
+// row r of X^T gives y_c[n - 1 - r]) over the block's work list (built on the
+// host for this grid: whole rows per block in a zig-zag order, each cut into
+// segments of at most TRI_SEG entries, longest first), vec_s the staged
+// vector in 4 planes of S (st_seg_dot).  Consumer warp w takes the block's segments w, w + ST_CW, ..; their
+// double-float sums go to s_seg, and after the consumers' barrier one thread
+// per row adds the row's segments in order.  Deterministic; every warp gets
+// about the same number of entries whatever the rows' lengths
+__device__ void st_tri_list(const CoarseArgs& co, bool tr, const float2* vec_s, int S, float2* s_seg, int warp,
+                            int lane) {
+	int const b = blockIdx.x, n = co.nc;
+	const float* T = tr ? co.xu : co.xl;
+	int const sa = co.tri_sp[b], sb = co.tri_sp[b + 1];
+	for (int q = sa + warp; q < sb; q += ST_CW) {
+		int4 const w = co.tri_seg[q];  // row, first entry, entries, slot
+		int const j = tr ? n - 1 - w.x : 0;
+		dfl const d = st_seg_dot(T + xrow(w.x) + w.y, w.z, vec_s, S, j + w.y, lane);
+		if (lane == 0) s_seg[w.w] = make_float2(d.hi, d.lo);
+	}
+	consumers_sync();
+	int const ra = co.tri_rp[b], rb = co.tri_rp[b + 1];
+	for (int k = ra + (int) threadIdx.x; k < rb; k += ST_CW * 32) {
+		int4 const w = co.tri_row[k];  // row, first slot, slots
+		dfl acc = {0.f, 0.f};
+		for (int q = 0; q < w.z; q++) acc = df_add(acc, {s_seg[w.y + q].x, s_seg[w.y + q].y});
+		(tr ? co.yc : co.yt)[tr ? n - 1 - w.x : w.x] = make_float2(acc.hi, acc.lo);
+	}
 }
 
 // sum of A_ij y_j over the staged blocks of one row: w blocks at stride 32
@@ -286,6 +373,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 	__shared__ volatile int s_abort, s_issued, s_dead;
 	__shared__ double s_red[ST_THREADS / 32];
 	__shared__ bool s_last;
+	__shared__ float2 s_seg[TRI_SLOTS];  // segment sums of the triangular products
 	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int const nc = a.ncol > 0 ? a.ncol : 1, nph = 2 * nc - 1;
 	bool const fuse = a.fuse && nc >= 3;
@@ -367,28 +455,40 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 			int const c = fwd ? ph : 2 * nc - 2 - ph;
 			int const lo = a.off[c], hi = a.off[c + 1];
 			if (ph > 0) alive = st_grid_barrier(a.bar, &a.st->ssor_err, a.polls, &s_dead);
-			if (fuse && alive && ph == 1) {
-				// r_c, summed by each aggregate's last restriction chunk in phase 0
-				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32)
-					vec_s[u] = u < co.nc ? __ldcg(co.rc + u) : make_float2(0.f, 0.f);
+			if (fuse && ph == 0) {
+				// restriction by whole aggregates per block, while the producer
+				// fills the ring: the chunks' partial sums, then (after the
+				// consumers' barrier, which orders the block's global writes)
+				// each aggregate's sum in chunk order into r_c.  No other block
+				// touches these aggregates; the grid barrier before phase 1
+				// publishes r_c
+				int A0, A1;
+				st_share(co.na, A0, A1);
+				int const qa = co.agg_chunk[A0], qb = co.agg_chunk[A1];
+				for (int q = qa + warp; q < qb; q += ST_CW) st_restrict_chunk<VT>(co, a.r, q, lane);
 				consumers_sync();
-				int i0, i1;
-				st_tri_share(co.nc, i0, i1);
-				for (int i = i0 + warp; i < i1; i += ST_CW) {
-					dfl const s = st_row_dot(co.xl + xrow(i), i + 1, vec_s, lane);
-					if (lane == 0) co.yt[i] = make_float2(s.hi, s.lo);
-				}
+				for (int I = A0 + warp; I < A1; I += ST_CW) st_restrict_sum(co, I, lane);
 			}
-			if (fuse && alive && ph == 2) {
+			if (fuse && alive && (ph == 1 || ph == 2)) {
+				// y_t = X r_c (phase 1) or y_c = X^T y_t (phase 2), the vector
+				// (from the other blocks, published by the grid barrier) staged
+				// in shared memory
+				bool const tr = ph == 2;
+				bool const lst = co.tri_g == (int) gridDim.x;  // the work list (planar vector), else rows per warp
+				int const S = (co.nc + 7) >> 2;
 				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32)
-					vec_s[u] = u < co.nc ? __ldcg(co.yt + u) : make_float2(0.f, 0.f);
+					vec_s[lst ? (u & 3) * S + (u >> 2) : u] = u < co.nc ? __ldcg((tr ? co.yt : co.rc) + u) : make_float2(0.f, 0.f);
 				consumers_sync();
-				int r0, r1;
-				st_tri_share(co.nc, r0, r1);
-				for (int r = r0 + warp; r < r1; r += ST_CW) {  // row r of X^T: coarse DOF j = nc - 1 - r
-					int const j = co.nc - 1 - r;
-					dfl const s = st_row_dot(co.xu + xrow(r), r + 1, vec_s + j, lane);
-					if (lane == 0) co.yc[j] = make_float2(s.hi, s.lo);
+				if (lst) st_tri_list(co, tr, vec_s, S, s_seg, warp, lane);
+				else {
+					// one warp per row of the block's contiguous share
+					int i0, i1;
+					st_tri_share(co.nc, i0, i1);
+					for (int i = i0 + warp; i < i1; i += ST_CW) {
+						int const j = tr ? co.nc - 1 - i : i;
+						dfl const d = st_row_dot((tr ? co.xu : co.xl) + xrow(i), i + 1, tr ? vec_s + j : vec_s, lane);
+						if (lane == 0) (tr ? co.yc : co.yt)[j] = make_float2(d.hi, d.lo);
+					}
 				}
 			}
 			if (fuse && alive && ph == 3 && nc == 3) {
@@ -453,11 +553,6 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 				kg += ns;
 				__syncwarp();
 				if (got && lane == 0) mbar_arrive(smem_u32(&empty[stg]));
-			}
-			if (fuse && alive && ph == 0) {
-				int q0, q1;
-				st_share(co.nchunk, q0, q1);
-				for (int q = q0 + warp; q < q1; q += ST_CW) st_restrict_chunk<VT>(co, a.r, q, lane);
 			}
 		}
 	}
