@@ -1715,7 +1715,7 @@ constexpr long BARRIER_POLLS_DEFAULT = 1l << 24;
 
 // Grid barrier words: the arrival count at word 0 and the generation at word
 // 32 (separate 128-byte lines, so the polling does not slow the arrivals)
-constexpr int BAR_WORDS = 64;
+constexpr int BAR_WORDS = 96;  // count (word 0), generation (32), the TMA sweep kernel's arrival counter (64)
 
 // the generation this block waits past at its next grid barrier
 __device__ __forceinline__ unsigned& bar_expect() {

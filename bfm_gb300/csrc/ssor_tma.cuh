@@ -94,42 +94,57 @@ __device__ __forceinline__ void bulk_g2s(unsigned dst, const void* src, unsigned
 // the consumer warps only (named barrier 1)
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(ST_CW * 32) : "memory"); }
 
-// Grid barrier of the consumer warps (the producer streams on): as
-// grid_barrier, with the block-level synchronisation on named barrier 1.
-// Every consumer thread calls it; a block that has given up (*dead: a wait
-// of one of its threads ran out) does not arrive and returns false, as do
-// all threads of a block whose wait here runs out -- so the result is the
-// same in every thread of the block
+// Grid barrier of the consumer warps (the producer streams on), on a
+// monotone arrival counter of its own cache line (word 64 of the barrier
+// words): thread 0 of each block adds 1 with a release reduction (no reply
+// to wait for) and polls with acquire loads until the counter reaches the
+// next multiple of the grid size -- one trip to L2 after the last arrival,
+// where a counter that is reset needs the last arriver's atomic reply and
+// then its store of a new generation.  Every launch that uses the word has
+// the same grid and passes all its barriers, and the word is zeroed before
+// each solve, so the counter is a multiple of the grid size at each launch
+// start (st_grid_barrier_init).  Block-level synchronisation on named
+// barrier 1.  Every consumer thread calls it; a block that has given up
+// (*dead: a wait of one of its threads ran out) does not arrive and returns
+// false, as do all threads of a block whose wait here runs out -- so the
+// result is the same in every thread of the block
+constexpr int BAR_CUM = 64;
+__device__ __forceinline__ unsigned& st_bar_target() {
+	__shared__ unsigned g;
+	return g;
+}
+// at kernel start, before any block can pass the first barrier: the count
+// read here lies between the launch's base (a multiple of the grid size)
+// and base + gridDim.x - 1
+__device__ __forceinline__ void st_grid_barrier_init(unsigned* bar) {
+	if (threadIdx.x == 0) {
+		unsigned v;
+		asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar + BAR_CUM) : "memory");
+		st_bar_target() = v - v % gridDim.x;
+	}
+}
 __device__ bool st_grid_barrier(unsigned* bar, int* err, long polls, volatile int* dead) {
 	__shared__ int ok;
 	consumers_sync();
 	if (threadIdx.x == 0 && *dead) ok = 0;
 	else if (threadIdx.x == 0) {
-		unsigned* count = bar;
-		unsigned* gen = bar + 32;
-		unsigned const target = bar_expect() + 1;
+		unsigned* count = bar + BAR_CUM;
+		unsigned const target = st_bar_target() + gridDim.x;
 		int good = 1;
-		unsigned old;
-		asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
-		if (old == gridDim.x - 1) {
-			asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(count) : "memory");
-			asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(gen), "r"(target) : "memory");
-		}
-		else {
-			long spins = 0;
-			unsigned cur;
-			while (true) {
-				asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gen) : "memory");
-				if (cur == target) break;
-				++spins;
-				if (spins > polls || ((spins & 1023) == 0 && *(volatile int*) err != 0)) {
-					atomicExch(err, 1);
-					good = 0;
-					break;
-				}
+		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+		long spins = 0;
+		unsigned cur;
+		while (true) {
+			asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
+			if ((int) (cur - target) >= 0) break;
+			++spins;
+			if (spins > polls || ((spins & 1023) == 0 && *(volatile int*) err != 0)) {
+				atomicExch(err, 1);
+				good = 0;
+				break;
 			}
 		}
-		bar_expect() = target;
+		st_bar_target() = target;
 		ok = good;
 		if (!good) *dead = 1;
 	}
@@ -388,7 +403,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 		s_dead = 0;
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
-	grid_barrier_init(a.bar);
+	st_grid_barrier_init(a.bar);
 	__syncthreads();
 	dfl acc = {0.f, 0.f};
 	double acc64 = 0.0;
