@@ -2508,8 +2508,8 @@ bool fuse_coarse(bfm_gpu_problem* P) {
 // block, 0 when the kernel cannot be used here.
 size_t tma_tiling(bfm_gpu_problem* P, SsorArgs& a, bool fused) {
 	if (P->tma_grid <= 0 || P->ncol <= 0 || P->ncol > 63) return 0;
-	// the staged coarse vector: nc + 4 entries, in 4 planes of (nc + 7) / 4
-	size_t const vec = fused ? (((size_t) P->nc + 8) * sizeof(float2) + 127) / 128 * 128 : 0;
+	// the staged coarse vector and the triangular products' work list
+	size_t const vec = fused ? st_vec_bytes(P->nc) + ST_LIST_BYTES : 0;
 	if ((size_t) P->tma_smem_max < vec + ST_NS * 4096) return 0;
 	int const stage = (int) ((((size_t) P->tma_smem_max - vec) / ST_NS) / 128 * 128);
 	int const nc = P->ncol;

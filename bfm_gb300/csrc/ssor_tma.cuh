@@ -94,6 +94,11 @@ __device__ __forceinline__ void bulk_g2s(unsigned dst, const void* src, unsigned
 // the consumer warps only (named barrier 1)
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"r"(ST_CW * 32) : "memory"); }
 
+// bytes of the staged coarse vector (nc + 4 entries in 4 planes of
+// (nc + 7) / 4), then the work list's TRI_SLOTS segments and TRI_SLOTS rows
+__host__ __device__ __forceinline__ size_t st_vec_bytes(int nc) { return (((size_t) nc + 8) * sizeof(float2) + 127) / 128 * 128; }
+constexpr size_t ST_LIST_BYTES = 2 * TRI_SLOTS * sizeof(int4);
+
 // Grid barrier of the consumer warps (the producer streams on), on a
 // monotone arrival counter of its own cache line (word 64 of the barrier
 // words): thread 0 of each block adds 1 with a release reduction (no reply
@@ -329,29 +334,41 @@ __device__ __forceinline__ dfl st_seg_dot(const float* __restrict__ row, int len
 	return s;
 }
 
+// the segments of the block's work list that consumer warp `warp` will take,
+// of triangle T, prefetched into L2 by the TMA unit (lane 0; addresses and
+// sizes are whole groups of 4 floats: 16-byte multiples), so the stage's
+// loads hit L2 instead of waiting on DRAM
+__device__ __forceinline__ void st_tri_prefetch(const int4* seg_s, int nseg, const float* T, int warp, int lane) {
+	if (lane != 0) return;
+	for (int q = warp; q < nseg; q += ST_CW) {
+		int4 const w = seg_s[q];
+		unsigned const bytes = 16u * (unsigned) ((w.z + 3) >> 2);
+		asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(T + xrow(w.x) + w.y), "r"(bytes) : "memory");
+	}
+}
+
 // y_t = X r_c (tr false: row i of X gives y_t[i]) or y_c = X^T y_t (tr true:
 // row r of X^T gives y_c[n - 1 - r]) over the block's work list (built on the
 // host for this grid: whole rows per block in a zig-zag order, each cut into
-// segments of at most TRI_SEG entries, longest first), vec_s the staged
-// vector in 4 planes of S (st_seg_dot).  Consumer warp w takes the block's segments w, w + ST_CW, ..; their
+// segments of at most TRI_SEG entries, longest first; copied to shared
+// memory at kernel start), vec_s the staged vector in 4 planes of S
+// (st_seg_dot).  Consumer warp w takes the block's segments w, w + ST_CW, ..; their
 // double-float sums go to s_seg, and after the consumers' barrier one thread
 // per row adds the row's segments in order.  Deterministic; every warp gets
 // about the same number of entries whatever the rows' lengths
-__device__ void st_tri_list(const CoarseArgs& co, bool tr, const float2* vec_s, int S, float2* s_seg, int warp,
-                            int lane) {
-	int const b = blockIdx.x, n = co.nc;
+__device__ void st_tri_list(const CoarseArgs& co, bool tr, const float2* vec_s, int S, float2* s_seg,
+                            const int4* seg_s, int nseg, const int4* row_s, int nrow, int warp, int lane) {
+	int const n = co.nc;
 	const float* T = tr ? co.xu : co.xl;
-	int const sa = co.tri_sp[b], sb = co.tri_sp[b + 1];
-	for (int q = sa + warp; q < sb; q += ST_CW) {
-		int4 const w = co.tri_seg[q];  // row, first entry, entries, slot
+	for (int q = warp; q < nseg; q += ST_CW) {
+		int4 const w = seg_s[q];  // row, first entry, entries, slot
 		int const j = tr ? n - 1 - w.x : 0;
 		dfl const d = st_seg_dot(T + xrow(w.x) + w.y, w.z, vec_s, S, j + w.y, lane);
 		if (lane == 0) s_seg[w.w] = make_float2(d.hi, d.lo);
 	}
 	consumers_sync();
-	int const ra = co.tri_rp[b], rb = co.tri_rp[b + 1];
-	for (int k = ra + (int) threadIdx.x; k < rb; k += ST_CW * 32) {
-		int4 const w = co.tri_row[k];  // row, first slot, slots
+	for (int k = threadIdx.x; k < nrow; k += ST_CW * 32) {
+		int4 const w = row_s[k];  // row, first slot, slots
 		dfl acc = {0.f, 0.f};
 		for (int q = 0; q < w.z; q++) acc = df_add(acc, {s_seg[w.y + q].x, s_seg[w.y + q].y});
 		(tr ? co.yc : co.yt)[tr ? n - 1 - w.x : w.x] = make_float2(acc.hi, acc.lo);
@@ -389,10 +406,14 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 	__shared__ double s_red[ST_THREADS / 32];
 	__shared__ bool s_last;
 	__shared__ float2 s_seg[TRI_SLOTS];  // segment sums of the triangular products
+	__shared__ int s_nseg, s_nrow;       // the block's work list: segments, rows
 	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int const nc = a.ncol > 0 ? a.ncol : 1, nph = 2 * nc - 1;
 	bool const fuse = a.fuse && nc >= 3;
 	float2* vec_s = reinterpret_cast<float2*>(st_smem + (size_t) ST_NS * a.stage_bytes);  // r_c, then y_t (fused)
+	// the block's work list of the triangular products (fused), after the vector
+	int4* seg_s = reinterpret_cast<int4*>(st_smem + (size_t) ST_NS * a.stage_bytes + st_vec_bytes(a.co.nc));
+	int4* row_s = seg_s + TRI_SLOTS;
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < ST_NS; s++) {
 			mbar_init(smem_u32(&full[s]), 1);
@@ -465,6 +486,19 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 		int t = 0, kg = 0;
 		bool alive = true;
 		CoarseArgs const& co = a.co;
+		bool const lst = fuse && co.tri_g == (int) gridDim.x;  // the work list (planar vector), else rows per warp
+		if (lst) {
+			// the block's work list to shared memory (read first in phase 0,
+			// after the restriction's consumer barrier)
+			int const sa = co.tri_sp[blockIdx.x], sb = co.tri_sp[blockIdx.x + 1];
+			int const ra = co.tri_rp[blockIdx.x], rb = co.tri_rp[blockIdx.x + 1];
+			if (threadIdx.x == 0) {
+				s_nseg = sb - sa;
+				s_nrow = rb - ra;
+			}
+			for (int u = threadIdx.x; u < sb - sa; u += ST_CW * 32) seg_s[u] = co.tri_seg[sa + u];
+			for (int u = threadIdx.x; u < rb - ra; u += ST_CW * 32) row_s[u] = co.tri_row[ra + u];
+		}
 		for (int ph = 0; ph < nph; ph++) {
 			bool const fwd = ph < nc;
 			int const c = fwd ? ph : 2 * nc - 2 - ph;
@@ -483,18 +517,21 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 				for (int q = qa + warp; q < qb; q += ST_CW) st_restrict_chunk<VT>(co, a.r, q, lane);
 				consumers_sync();
 				for (int I = A0 + warp; I < A1; I += ST_CW) st_restrict_sum(co, I, lane);
+				if (lst) st_tri_prefetch(seg_s, s_nseg, co.xl, warp, lane);  // X, for phase 1
 			}
 			if (fuse && alive && (ph == 1 || ph == 2)) {
 				// y_t = X r_c (phase 1) or y_c = X^T y_t (phase 2), the vector
 				// (from the other blocks, published by the grid barrier) staged
 				// in shared memory
 				bool const tr = ph == 2;
-				bool const lst = co.tri_g == (int) gridDim.x;  // the work list (planar vector), else rows per warp
 				int const S = (co.nc + 7) >> 2;
 				for (int u = threadIdx.x; u < co.nc + 4; u += ST_CW * 32)
 					vec_s[lst ? (u & 3) * S + (u >> 2) : u] = u < co.nc ? __ldcg((tr ? co.yt : co.rc) + u) : make_float2(0.f, 0.f);
 				consumers_sync();
-				if (lst) st_tri_list(co, tr, vec_s, S, s_seg, warp, lane);
+				if (lst) {
+					st_tri_list(co, tr, vec_s, S, s_seg, seg_s, s_nseg, row_s, s_nrow, warp, lane);
+					if (!tr) st_tri_prefetch(seg_s, s_nseg, co.xu, warp, lane);  // X^T, for phase 2
+				}
 				else {
 					// one warp per row of the block's contiguous share
 					int i0, i1;
