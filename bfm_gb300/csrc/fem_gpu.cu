@@ -2509,7 +2509,7 @@ bool fuse_coarse(bfm_gpu_problem* P) {
 size_t tma_tiling(bfm_gpu_problem* P, SsorArgs& a, bool fused) {
 	if (P->tma_grid <= 0 || P->ncol <= 0 || P->ncol > 63) return 0;
 	// the staged coarse vector and the triangular products' work list
-	size_t const vec = fused ? st_vec_bytes(P->nc) + ST_LIST_BYTES : 0;
+	size_t const vec = fused ? st_vec_bytes(P->nc) + ST_LIST_BYTES + (ST_RST_BYTES + 127) / 128 * 128 : 0;
 	if ((size_t) P->tma_smem_max < vec + ST_NS * 4096) return 0;
 	int const stage = (int) ((((size_t) P->tma_smem_max - vec) / ST_NS) / 128 * 128);
 	int const nc = P->ncol;

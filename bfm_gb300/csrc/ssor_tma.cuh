@@ -98,6 +98,11 @@ __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;
 // (nc + 7) / 4), then the work list's TRI_SLOTS segments and TRI_SLOTS rows
 __host__ __device__ __forceinline__ size_t st_vec_bytes(int nc) { return (((size_t) nc + 8) * sizeof(float2) + 127) / 128 * 128; }
 constexpr size_t ST_LIST_BYTES = 2 * TRI_SLOTS * sizeof(int4);
+// the restriction's table of the block's chunks (first row, rows), their
+// partial sums and the aggregates' first chunks, after the work list
+constexpr int RST_CHUNKS = 192;
+constexpr int RST_AGGS = 64;
+constexpr size_t ST_RST_BYTES = RST_CHUNKS * (sizeof(int2) + 3 * sizeof(double)) + (RST_AGGS + 1) * sizeof(int);
 
 // Grid barrier of the consumer warps (the producer streams on), on a
 // monotone arrival counter of its own cache line (word 64 of the barrier
@@ -224,10 +229,9 @@ __device__ __forceinline__ dfl st_row_dot(const float* __restrict__ row, int len
 // (all loads first), then double-float sums in that order and a fixed
 // shuffle tree; the chunk's 3 sums to part[3 q ..]
 template <int VT>
-__device__ __forceinline__ void st_restrict_chunk(const CoarseArgs& co, const void* r, int q, int lane) {
+__device__ __forceinline__ void st_restrict_chunk(const CoarseArgs& co, const void* r, int row0, int len, double* out,
+                                                  int lane) {
 	constexpr int PER = COARSE_CHUNK / 32;
-	int const k0 = co.chunk_start[q], len = co.chunk_start[q + 1] - k0;
-	int const row0 = co.agg_nodes[k0];
 	dfl r0[PER], r1[PER];
 	float4 pq[PER];
 #pragma unroll
@@ -258,26 +262,18 @@ __device__ __forceinline__ void st_restrict_chunk(const CoarseArgs& co, const vo
 		s2 = df_add(s2, {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)});
 	}
 	if (lane == 0) {
-		co.part[3l * q] = df_dbl(s0);
-		co.part[3l * q + 1] = df_dbl(s1);
-		co.part[3l * q + 2] = df_dbl(s2);
+		out[0] = df_dbl(s0);
+		out[1] = df_dbl(s1);
+		out[2] = df_dbl(s2);
 	}
 }
 
-// r_c of aggregate I: the partial sums of its chunks in chunk order, lanes
-// 0-2 one component each, 8 loads in flight
-__device__ __forceinline__ void st_restrict_sum(const CoarseArgs& co, int I, int lane) {
+// r_c of aggregate I: the partial sums of its chunks (part[3 c ..], c in
+// [c0, c1)) in chunk order, lanes 0-2 one component each
+__device__ __forceinline__ void st_restrict_sum(const CoarseArgs& co, const double* part, int c0, int c1, int I, int lane) {
 	if (lane >= 3) return;
-	int const q0 = co.agg_chunk[I], q1 = co.agg_chunk[I + 1];
 	double s = 0.0;
-	for (int qb = q0; qb < q1; qb += 8) {
-		double pv[8];
-#pragma unroll
-		for (int k = 0; k < 8; k++) pv[k] = qb + k < q1 ? __ldcg(co.part + 3l * (qb + k) + lane) : 0.0;
-#pragma unroll
-		for (int k = 0; k < 8; k++)
-			if (qb + k < q1) s += pv[k];
-	}
+	for (int c = c0; c < c1; c++) s += part[3 * c + lane];
 	dfl const d = df_make(s);
 	co.rc[3 * I + lane] = make_float2(d.hi, d.lo);
 }
@@ -414,6 +410,9 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 	// the block's work list of the triangular products (fused), after the vector
 	int4* seg_s = reinterpret_cast<int4*>(st_smem + (size_t) ST_NS * a.stage_bytes + st_vec_bytes(a.co.nc));
 	int4* row_s = seg_s + TRI_SLOTS;
+	double* rpart_s = reinterpret_cast<double*>(row_s + TRI_SLOTS);  // 3 per chunk
+	int2* rchk_s = reinterpret_cast<int2*>(rpart_s + 3 * RST_CHUNKS);  // first row, rows
+	int* ragg_s = reinterpret_cast<int*>(rchk_s + RST_CHUNKS);         // first chunk of each aggregate (local)
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < ST_NS; s++) {
 			mbar_init(smem_u32(&full[s]), 1);
@@ -499,6 +498,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 			for (int u = threadIdx.x; u < sb - sa; u += ST_CW * 32) seg_s[u] = co.tri_seg[sa + u];
 			for (int u = threadIdx.x; u < rb - ra; u += ST_CW * 32) row_s[u] = co.tri_row[ra + u];
 		}
+
 		for (int ph = 0; ph < nph; ph++) {
 			bool const fwd = ph < nc;
 			int const c = fwd ? ph : 2 * nc - 2 - ph;
@@ -506,17 +506,39 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 			if (ph > 0) alive = st_grid_barrier(a.bar, &a.st->ssor_err, a.polls, &s_dead);
 			if (fuse && ph == 0) {
 				// restriction by whole aggregates per block, while the producer
-				// fills the ring: the chunks' partial sums, then (after the
-				// consumers' barrier, which orders the block's global writes)
-				// each aggregate's sum in chunk order into r_c.  No other block
-				// touches these aggregates; the grid barrier before phase 1
-				// publishes r_c
+				// fills the ring: the chunks' partial sums, then (after a
+				// consumers' barrier) each aggregate's sum in chunk order into
+				// r_c.  No other block touches these aggregates; the grid
+				// barrier before phase 1 publishes r_c.  The block's chunks and
+				// partial sums sit in a shared-memory table when it fits (one
+				// round of lookups instead of a chain per chunk), else in the
+				// global arrays
 				int A0, A1;
 				st_share(co.na, A0, A1);
 				int const qa = co.agg_chunk[A0], qb = co.agg_chunk[A1];
-				for (int q = qa + warp; q < qb; q += ST_CW) st_restrict_chunk<VT>(co, a.r, q, lane);
-				consumers_sync();
-				for (int I = A0 + warp; I < A1; I += ST_CW) st_restrict_sum(co, I, lane);
+				bool const rtab = qb - qa <= RST_CHUNKS && A1 - A0 <= RST_AGGS;
+				if (rtab) {
+					for (int u = threadIdx.x; u < qb - qa; u += ST_CW * 32) {
+						int const k0 = co.chunk_start[qa + u], k1 = co.chunk_start[qa + u + 1];
+						rchk_s[u] = make_int2(co.agg_nodes[k0], k1 - k0);
+					}
+					for (int u = threadIdx.x; u <= A1 - A0; u += ST_CW * 32) ragg_s[u] = co.agg_chunk[A0 + u] - qa;
+					consumers_sync();  // the table
+					for (int q = warp; q < qb - qa; q += ST_CW)
+						st_restrict_chunk<VT>(co, a.r, rchk_s[q].x, rchk_s[q].y, rpart_s + 3 * q, lane);
+					consumers_sync();
+					for (int I = A0 + warp; I < A1; I += ST_CW)
+						st_restrict_sum(co, rpart_s, ragg_s[I - A0], ragg_s[I - A0 + 1], I, lane);
+				}
+				else {
+					for (int q = qa + warp; q < qb; q += ST_CW) {
+						int const k0 = co.chunk_start[q];
+						st_restrict_chunk<VT>(co, a.r, co.agg_nodes[k0], co.chunk_start[q + 1] - k0, co.part + 3l * q, lane);
+					}
+					consumers_sync();  // orders the block's global writes of the partial sums
+					for (int I = A0 + warp; I < A1; I += ST_CW)
+						st_restrict_sum(co, co.part, co.agg_chunk[I], co.agg_chunk[I + 1], I, lane);
+				}
 				if (lst) st_tri_prefetch(seg_s, s_nseg, co.xl, warp, lane);  // X, for phase 1
 			}
 			if (fuse && alive && (ph == 1 || ph == 2)) {
