@@ -68,7 +68,7 @@ SPMV_TRAFFIC = {0: (343_951_104, "profiles/spmv_fp64_hs_perforated_2048x512.md")
 # correction fused, kernel: 1 k_ssor_all, 2 k_ssor_tma), where a capture of the
 # current kernel exists
 SSOR_TRAFFIC = {(1, True, 1): (269_338_112, "profiles/ssor2_fused_mixed_perforated_2048x512.md"),
-                (1, True, 2): (266_733_824, "profiles/ssor2_tma_mixed_perforated_2048x512.md")}
+                (1, True, 2): (266_680_576, "profiles/ssor2_tma_mixed_perforated_2048x512.md")}
 
 
 def algorithmic_bytes_ssor(n_blocks: int, n_nodes: int, precision: int) -> int:
