@@ -1846,15 +1846,18 @@ __device__ __forceinline__ dfl pivot_rsqrt(dfl p, float thr) {
 
 // per node its offset from its cell's centre (scaled by the cell size H) and
 // which of its DOFs are free (constrained ones get no coarse correction)
+// (the offsets times 1 / H, which the host forms once: two FP64 divisions
+// per node cost more than the rest of the kernel on this GPU's FP64 pipe,
+// and the offsets are rounded to FP32 anyway)
 __global__ void k_pnode(int N, const double* __restrict__ coords, const int* __restrict__ agg, const int* __restrict__ last_ci,
-                        double x0, double y0, double cw, double ch, int gx, int gy, int xfast, double H,
+                        double x0, double y0, double cw, double ch, int gx, int gy, int xfast, double invH,
                         float4* __restrict__ pnode) {
 	int const i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
 	int cx, cy;
 	cell_xy(agg[i], gx, gy, xfast, cx, cy);
 	double const xc = x0 + (cx + 0.5) * cw, yc = y0 + (cy + 0.5) * ch;
-	pnode[i] = make_float4((float) ((coords[2l * i] - xc) / H), (float) ((coords[2l * i + 1] - yc) / H),
+	pnode[i] = make_float4((float) ((coords[2l * i] - xc) * invH), (float) ((coords[2l * i + 1] - yc) * invH),
 	                       last_ci[2l * i] < 0 ? 1.f : 0.f, last_ci[2l * i + 1] < 0 ? 1.f : 0.f);
 }
 
@@ -2359,7 +2362,7 @@ __global__ void __launch_bounds__(CHOL_T) k_coarse_chol(CoarseArgs a) {
 		nv = nv2;
 		__syncthreads();
 		int const nu = m * (m + 1) / 2;
-		for (int e = tx; e < nu; e += blockDim.x) {
+		auto upd = [&](int e) {
 			short2 const q = pr[e];
 			int si = s1 + q.x, sj = s1 + q.y;
 			si -= si >= M ? M : 0;
@@ -2367,13 +2370,18 @@ __global__ void __launch_bounds__(CHOL_T) k_coarse_chol(CoarseArgs a) {
 			float2 const ci = col[q.x], cj = col[q.y], w = W[si * M + sj];
 			dfl const u = df_add({w.x, w.y}, df_neg(df_mul({ci.x, ci.y}, {cj.x, cj.y})));
 			W[si * M + sj] = make_float2(u.hi, u.lo);
-		}
-		if (tx == 0 && m > 0) {
-			// pair 0 is S_{k+1,k+1}, updated by this thread above
+		};
+		// pair 0 is S_{k+1,k+1}: the block's last thread updates it first and
+		// forms the next pivot at once, and the other pairs go round-robin
+		// from thread 0, so the pivot's dependent chain runs in a warp with
+		// one pair fewer than the busiest ones instead of after thread 0's
+		if (tx == blockDim.x - 1 && m > 0) {
+			upd(0);
 			float2 const p = W[s1 * M + s1];
 			dfl const q = pivot_rsqrt({p.x, p.y}, thr[k + 1]);
 			piv[0] = make_float2(q.hi, q.lo);
 		}
+		for (int e = 1 + tx; e < nu; e += blockDim.x) upd(e);
 		sk = s1;
 		__syncthreads();
 	}

@@ -2295,7 +2295,7 @@ int coarse_setup(bfm_gpu_problem* P) {
 	if (P->N == 0) return 0;
 	if (!P->agg_valid && build_aggregates(P)) return -1;
 	k_pnode<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->coords, P->agg, P->last_ci, P->ax0, P->ay0, P->acw, P->ach, P->agx,
-	                                          P->agy, P->axfast, P->aH, P->pnode);
+	                                          P->agy, P->axfast, 1.0 / P->aH, P->pnode);
 	CK(cudaMemsetAsync(P->aband, 0, (size_t) P->nc * (P->abw + 1) * sizeof(float2), st));
 	CK(cudaMemsetAsync(P->diag0, 0, (size_t) P->nc * sizeof(double), st));
 	CK(cudaMemsetAsync(P->coarse_err, 0, 2 * sizeof(int), st));
