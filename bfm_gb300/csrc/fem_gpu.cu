@@ -1590,6 +1590,12 @@ struct bfm_gpu_problem {
 	float2 *rc, *ayt, *yc;  // coarse vectors (double-float pairs, zero pads)
 	int* coarse_err;
 	int coarse_grid;        // cooperative grid of k_coarse_apply (0: not sized yet, -1: none)
+	// the coarse factorisation and inverse run on a side stream while the
+	// main stream builds the sweeps' sliced-ELL copies (coarse_setup forks,
+	// coarse_finish joins): the factorisation holds one SM for milliseconds
+	cudaStream_t side;
+	cudaEvent_t fork_ev, join_ev;
+	int coarse_pending;
 	// the TMA sweep kernel's work list for the triangular products
 	// (CoarseArgs::tri_*), packed: built for tri_n coarse DOFs and tri_g blocks
 	int* tri;
@@ -2288,10 +2294,15 @@ int build_sell(bfm_gpu_problem* P) {
 	return 0;
 }
 
-int coarse_setup(bfm_gpu_problem* P) {
+int coarse_finish(bfm_gpu_problem* P);
+
+// fork: the factorisation and inverse go to the side stream (coarse_finish
+// joins it); else everything runs on the problem's stream
+int coarse_setup(bfm_gpu_problem* P, bool fork) {
 	BFM_RANGE("coarse_setup");
-	cudaStream_t const st = P->stream;
+	cudaStream_t st = P->stream;
 	P->coarse_ok = 0;
+	P->coarse_pending = 0;
 	if (P->N == 0) return 0;
 	if (!P->agg_valid && build_aggregates(P)) return -1;
 	k_pnode<<<blocks_for(P->N), TPB, 0, st>>>(P->N, P->coords, P->agg, P->last_ci, P->ax0, P->ay0, P->acw, P->ach, P->agx,
@@ -2311,6 +2322,11 @@ int coarse_setup(bfm_gpu_problem* P) {
 	CK(cudaMemcpyAsync(&err, P->coarse_err, sizeof(int), cudaMemcpyDeviceToHost, st));
 	CK(cudaStreamSynchronize(st));
 	if (err) return 0;
+	if (fork && P->side) {
+		CK(cudaEventRecord(P->fork_ev, st));
+		CK(cudaStreamWaitEvent(P->side, P->fork_ev, 0));
+		st = P->side;
+	}
 	CK(cudaFuncSetAttribute((const void*) k_coarse_chol, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                        (int) chol_smem(COARSE_MAX_BW, 3 * 1024)));
 	k_coarse_chol<<<1, CHOL_T, chol_smem(P->abw, P->nc), st>>>(ca);
@@ -2361,8 +2377,21 @@ int coarse_setup(bfm_gpu_problem* P) {
 			}
 	}
 	CK(cudaGetLastError());
+	if (st != P->stream) CK(cudaEventRecord(P->join_ev, st));
+	P->coarse_pending = 1;
+	return st == P->stream ? coarse_finish(P) : 0;
+}
+
+// the end of the coarse set-up: the problem's stream waits for the side
+// stream, then the work list and the inverse's timeout flag
+int coarse_finish(bfm_gpu_problem* P) {
+	if (!P->coarse_pending) return 0;
+	P->coarse_pending = 0;
+	cudaStream_t const st = P->stream;
+	CK(cudaStreamWaitEvent(st, P->join_ev, 0));
 	if (P->tma_grid > 0 && build_tri_lists(P, P->tma_grid)) return -1;
 	if (P->linv_grid > 0) {
+		int err = 0;
 		CK(cudaMemcpyAsync(&err, P->coarse_err + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
 		CK(cudaStreamSynchronize(st));
 		if (err) return fail("a grid barrier of the coarse inverse timed out");
@@ -3161,6 +3190,13 @@ int bfm_gpu_problem_create(bfm_gpu_problem_t** out, int kind, int n_nodes, int n
 		return fail("cudaMallocHost failed");
 	}
 	for (int i = 0; i < 4; i++) cudaEventCreate(&P->ev[i]);
+	if (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&P->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&P->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+		cudaGetLastError();
+		if (P->side) cudaStreamDestroy(P->side);
+		P->side = nullptr;  // the coarse set-up then runs on the problem's stream
+	}
 	cudaMemsetAsync(P->ticket, 0, sizeof(unsigned), P->stream);
 	cudaMemsetAsync(P->err, 0, sizeof(int), P->stream);
 	cudaMemsetAsync(P->st, 0, sizeof(CgState), P->stream);
@@ -3193,6 +3229,9 @@ int bfm_gpu_problem_destroy(bfm_gpu_problem_t* P) {
 	if (P->err_host) cudaFreeHost(P->err_host);
 	for (int i = 0; i < 4; i++)
 		if (P->ev[i]) cudaEventDestroy(P->ev[i]);
+	if (P->fork_ev) cudaEventDestroy(P->fork_ev);
+	if (P->join_ev) cudaEventDestroy(P->join_ev);
+	if (P->side) cudaStreamDestroy(P->side);
 	if (P->own_stream && P->stream) cudaStreamDestroy(P->stream);
 	free(P);
 	return 0;
@@ -3706,10 +3745,12 @@ int bfm_gpu_problem_assemble(bfm_gpu_problem_t* P, int precision) {
 		k_edge_loads<<<blocks_for(N), TPB, 0, st>>>(P->N, P->ledges, P->lloads, P->lptr, P->llist, P->coords, P->last_ci, P->b);
 	}
 	CK(cudaGetLastError());
-	// SSOR: the sweeps' sliced-ELL blocks of this matrix
+	// two-level SSOR: the coarse operator of this matrix (its factorisation
+	// and inverse on the side stream), while the main stream builds the
+	// sweeps' sliced-ELL blocks of this matrix
+	if (coarse_pc(P->precond) && coarse_setup(P, ssor)) return -1;
 	if (ssor && build_sell(P)) return -1;
-	// two-level SSOR: the coarse operator of this matrix
-	if (coarse_pc(P->precond) && coarse_setup(P)) return -1;
+	if (coarse_pc(P->precond) && coarse_finish(P)) return -1;
 	if (!capturing) CK(cudaEventRecord(P->ev[1], st));
 	P->assembled = true;
 	P->solved = false;
