@@ -1415,6 +1415,7 @@ struct CoarseArgs {
 	// slot), its rows tri_row[tri_rp[b] .. tri_rp[b + 1]) as (row, first
 	// slot, slots, 0)
 	int tri_g;
+	int tables;          // 0: the TMA sweep kernel's fallbacks (per-warp rows of X, global restriction arrays)
 	const int* tri_sp;
 	const int* tri_rp;
 	const int4* tri_seg;

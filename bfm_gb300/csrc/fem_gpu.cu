@@ -2031,8 +2031,12 @@ CoarseArgs coarse_args(bfm_gpu_problem* P, const void* r, int vt) {
 	c.chunk_agg = P->chunk_agg;
 	c.agg_chunk = P->agg_chunk;
 	c.part = P->cpart;
-	c.tri_g = P->tri_g;
-	if (P->tri_g > 0) {
+	// BFM_GPU_SSOR_STAGE_TABLES=0: the sweep kernel's coarse stages take
+	// their fallback paths (tested against the tables on the same problem)
+	char const* tb = getenv("BFM_GPU_SSOR_STAGE_TABLES");
+	c.tables = !(tb && tb[0] == '0');
+	c.tri_g = c.tables ? P->tri_g : 0;
+	if (c.tri_g > 0) {
 		c.tri_sp = P->tri;
 		c.tri_rp = P->tri + P->tri_g + 1;
 		c.tri_seg = reinterpret_cast<const int4*>(P->tri + P->tri_seg_off);

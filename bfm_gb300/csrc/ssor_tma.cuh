@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_ssor_tma(SsorArgs a) {
 				int A0, A1;
 				st_share(co.na, A0, A1);
 				int const qa = co.agg_chunk[A0], qb = co.agg_chunk[A1];
-				bool const rtab = qb - qa <= RST_CHUNKS && A1 - A0 <= RST_AGGS;
+				bool const rtab = co.tables && qb - qa <= RST_CHUNKS && A1 - A0 <= RST_AGGS;
 				if (rtab) {
 					for (int u = threadIdx.x; u < qb - qa; u += ST_CW * 32) {
 						int const k0 = co.chunk_start[qa + u], k1 = co.chunk_start[qa + u + 1];

@@ -412,3 +412,26 @@ def test_blocked_coarse_inverse_matches_columnwise(libbfm, monkeypatch):
             prob.close()
     assert abs(out[0][0] - out[1][0]) <= 2, (out[0][0], out[1][0])
     assert rel(out[0][1], out[1][1]) < 1e-9
+
+
+@pytest.mark.parametrize("precision,rtol,tol", [(bfm_gb300.FP64_DF, 1e-10, 1e-9), (bfm_gb300.MIXED, 1e-8, 1e-7)])
+def test_sweep_kernel_stage_tables_match_fallbacks(libbfm, monkeypatch, precision, rtol, tol):
+    """The TMA sweep kernel's coarse stages with their shared-memory tables
+    (the host-built work list of the triangular products, the restriction's
+    chunk table: the default) and with the fallbacks a grid or coarse space
+    too large for the tables takes (one warp per row of X, the restriction's
+    global arrays; BFM_GPU_SSOR_STAGE_TABLES=0): the same operators summed
+    in other orders, so the same iterations (within 2) and solution."""
+    p = M.cfg_perforated(nx=256, ny=64, n_holes=200, seed=3)
+    out = []
+    for tables in ("1", "0"):
+        monkeypatch.setenv("BFM_GPU_SSOR_STAGE_TABLES", tables)
+        prob = LN.DeviceProblem(p, precision=precision)
+        try:
+            s = prob.solve(precond=bfm_gb300.PC_SSOR2, rtol=rtol, replace_drop=0.1)
+            assert s.status == 0 and s.rel_residual <= rtol, (s.status, s.rel_residual)
+            out.append((s.iterations, prob.solution()))
+        finally:
+            prob.close()
+    assert abs(out[0][0] - out[1][0]) <= 2, (out[0][0], out[1][0])
+    assert rel(out[0][1], out[1][1]) < tol
