@@ -41,6 +41,12 @@
 // stored in phase nc - 1, get it at the start of phase nc when that is
 // phase 3.
 //
+// Dynamic shared memory: the ring (ST_NS stages), then (fused form) the
+// staged coarse vector in 4 planes, the block's work list of the
+// triangular products (copied at kernel start) and the restriction's table
+// of the block's chunks and their partial sums.  The grid barriers between
+// the phases count arrivals on a monotone counter (st_grid_barrier).
+//
 // Every wait is bounded: grid barriers by the polls argument (a timeout
 // sets the solve's error flag), the mbarrier waits by MBAR_POLLS.  A block
 // that gave up still drains the ring (waits for every copy it issued) so no
